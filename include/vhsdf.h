@@ -1,0 +1,229 @@
+/*
+ * vhsdf.h - C ABI of the GB300 voxel-hashing TSDF engine.
+ *
+ * One handle owns one TSDF volume on one GPU: a lock-free open-addressed
+ * spatial hash of 8^3 voxel blocks, the block pool behind it, the per-frame
+ * block list, image staging buffers and the triangle buffer of the last
+ * marching-cubes extraction.  All entry points return a vh_status; nothing
+ * throws across the ABI and nothing exits the process.
+ *
+ * Each entry point names the reference interface it replaces
+ * (E-BAO/Voxel-Hashing-SDF, paths relative to that project).
+ *
+ * Threading: calls on one handle must be serialised by the caller; different
+ * handles are independent.  Work is enqueued on the handle's CUDA stream.
+ * With VH_FLAG_SYNC set (the default) every call that enqueues work waits
+ * for it and reports device-side errors before returning, like the
+ * reference's processFrame, which ends in blocking copies.
+ */
+#ifndef VHSDF_H
+#define VHSDF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VHSDF_ABI_VERSION 1
+
+typedef enum vh_status {
+  VH_OK = 0,
+  VH_ERR_INVALID_ARG = 1,     /* bad pointer, size or parameter            */
+  VH_ERR_CUDA = 2,            /* a CUDA runtime call failed                */
+  VH_ERR_TABLE_FULL = 3,      /* a hash probe sequence hit max_probe        */
+  VH_ERR_POOL_FULL = 4,       /* the voxel-block pool is exhausted          */
+  VH_ERR_RETRY_EXHAUSTED = 5, /* a bounded device wait gave up              */
+  VH_ERR_NOT_FINITE = 6,      /* non-finite pose or intrinsics              */
+  VH_ERR_UNSUPPORTED = 7,     /* feature not available (e.g. GL render)     */
+  VH_ERR_OUT_OF_RANGE = 8,    /* block coordinate outside the key range     */
+  VH_ERR_CAPACITY = 9,        /* an output buffer is too small              */
+  VH_ERR_IO = 10,             /* file could not be read or written          */
+  VH_ERR_NO_DEVICE = 11       /* no CUDA device                             */
+} vh_status;
+
+typedef enum vh_depth_fmt {
+  VH_DEPTH_U16_MM = 0, /* uint16, scaled by depth_scale (0.001 = millimetres) */
+  VH_DEPTH_F32_M = 1   /* float32 metres, the processFrame format             */
+} vh_depth_fmt;
+
+typedef enum vh_mem {
+  VH_MEM_HOST = 0,  /* pointer is host memory (pinned or pageable)            */
+  VH_MEM_DEVICE = 1 /* pointer is device memory of the handle's GPU           */
+} vh_mem;
+
+typedef enum vh_scope {
+  VH_SCOPE_FRAME = 0, /* blocks touched by the last integrated frame          */
+  VH_SCOPE_ALL = 1    /* every allocated block (full-volume extraction)       */
+} vh_scope;
+
+/* vh_params.flags */
+#define VH_FLAG_SYNC 0x1u      /* wait for device work inside every call     */
+#define VH_FLAG_NO_GRAPH 0x2u  /* launch kernels directly, no CUDA graphs    */
+#define VH_FLAG_PROFILE 0x4u   /* record per-stage CUDA events               */
+
+/*
+ * Volume and camera parameters.  Replaces the arguments of
+ * ark::GpuTsdfGenerator::GpuTsdfGenerator (include/tsdf.cuh:606-607,
+ * src/tsdf.cu:1248-1372) and the fields of ark::MarchingCubeParam
+ * (include/tsdf.cuh:220-233), plus the hash sizes that the reference
+ * hard-codes in processFrame (src/tsdf.cu:1488,1492).
+ */
+typedef struct vh_params {
+  int32_t width, height;     /* image size in pixels                        */
+  float fx, fy, cx, cy;      /* pinhole intrinsics, pixel centres at ints   */
+  float min_depth;           /* near end of a truncation band (m)           */
+  float max_depth;           /* depth beyond this is ignored (m)            */
+  float depth_scale;         /* metres per VH_DEPTH_U16_MM unit             */
+  float voxel_size;          /* voxel edge (m)                              */
+  float trunc;               /* truncation margin T (m)                     */
+  float mc_min_weight;       /* MC skips cubes with a corner weight below   */
+  int32_t table_log2;        /* hash slots = 2^table_log2                   */
+  int32_t max_probe;         /* bound on one linear-probe sequence          */
+  int64_t pool_blocks;       /* capacity of the voxel-block pool            */
+  int64_t max_frame_blocks;  /* capacity of the per-frame block list        */
+  int64_t max_triangles;     /* initial capacity of the triangle buffer     */
+  uint32_t flags;            /* VH_FLAG_*                                   */
+  int32_t device;            /* CUDA device ordinal                         */
+} vh_params;
+
+/* Block-edge length in voxels of every volume (fixed for this ABI). */
+#define VH_BLOCK_EDGE 8
+#define VH_BLOCK_VOXELS 512
+
+typedef struct vh_stats {
+  int64_t frames;            /* frames integrated since create/reset        */
+  int64_t blocks_allocated;  /* live blocks in the pool                     */
+  int64_t frame_blocks;      /* blocks in the last frame's block list       */
+  int64_t new_blocks;        /* blocks inserted by the last frame           */
+  int64_t voxels_updated;    /* voxel updates of the last frame             */
+  int64_t triangles;         /* triangles of the last extraction            */
+  int64_t pool_capacity;
+  int64_t table_slots;
+  int64_t tombstones;        /* erased hash slots not yet reclaimed         */
+  uint32_t device_error;     /* sticky device error bits (0 = none)         */
+  uint32_t reserved;
+  /* per-stage device time of the last frame in ms (VH_FLAG_PROFILE only)   */
+  float ms_allocate, ms_integrate, ms_extract, ms_frame;
+} vh_stats;
+
+/* A device-resident triangle soup: triangle t has vertices 3t..3t+2, each a
+ * float4 {x, y, z, rgb} in global voxel units (multiply by voxel_size for
+ * metres, as the reference's tsdf2mesh does, src/tsdf.cu:1815-1817); the
+ * fourth float holds the colour bytes r | g<<8 | b<<16.  Valid until the
+ * next call on the handle. */
+typedef struct vh_mesh_view {
+  const float *vertices;     /* device pointer, 12 floats per triangle      */
+  int64_t num_triangles;
+  float voxel_size;
+} vh_mesh_view;
+
+typedef struct vh_handle vh_handle;
+
+/* ---- parameters --------------------------------------------------------- */
+
+/* Defaults of the reference's scene YAML where it has one
+ * (scene0220_02/scene0220_02.yaml:12-15,21-22,37-62; min_depth 0.1 from
+ * src/tsdf.cu:1318), 8^3 blocks, 2^20 hash slots. Host only. */
+vh_status vh_params_default(vh_params *p);
+/* Checks a parameter set without touching the GPU. Host only. */
+vh_status vh_params_validate(const vh_params *p);
+const char *vh_status_string(vh_status s);
+
+/* ---- life cycle (ark::GpuTsdfGenerator) ---------------------------------- */
+
+/* Replaces GpuTsdfGenerator::GpuTsdfGenerator (src/tsdf.cu:1248-1372) and
+ * vhashing::HashTable::HashTable (include/vhashing.h:643-684). */
+vh_status vh_create(const vh_params *p, vh_handle **out);
+/* Replaces GpuTsdfGenerator::Shutdown (src/tsdf.cu:1620-1638). */
+vh_status vh_destroy(vh_handle *h);
+/* Clears the volume (all blocks, the hash and counters). */
+vh_status vh_reset(vh_handle *h);
+/* Uses cudaStream_t `stream` (NULL = the handle's own stream). */
+vh_status vh_set_stream(vh_handle *h, void *stream);
+/* Waits for the handle's stream and reports sticky device errors. */
+vh_status vh_sync(vh_handle *h);
+const char *vh_last_error(const vh_handle *h);
+
+/* ---- per-frame path (GpuTsdfGenerator::processFrame) ---------------------- */
+
+/* Allocation + integration of one frame: replaces the HashAssign and
+ * IntegrateHashKernel steps of GpuTsdfGenerator::processFrame
+ * (src/tsdf.cu:1484-1533, kernels src/tsdf.cu:2088-2238 and 599-751).
+ * depth: H*W row-major in `depth_fmt`; rgb: H*W*3 interleaved RGB bytes;
+ * c2w: 16 floats, row-major camera-to-world, host memory
+ * (PointCloudGenerator.cpp:118-127 builds it this way). */
+vh_status vh_integrate(vh_handle *h, const void *depth, int32_t depth_fmt,
+                       const uint8_t *rgb, const float *c2w, int32_t mem);
+/* Marching cubes over `scope`: replaces marchingCubeHashKernel
+ * (src/tsdf.cu:884-1110) for VH_SCOPE_FRAME and the volume walk of
+ * tsdf2mesh (src/tsdf.cu:1760-1832) for VH_SCOPE_ALL. `out` may be NULL. */
+vh_status vh_extract(vh_handle *h, int32_t scope, vh_mesh_view *out);
+/* vh_integrate followed by vh_extract(VH_SCOPE_FRAME): the whole of
+ * GpuTsdfGenerator::processFrame (src/tsdf.cu:1484-1598). */
+vh_status vh_process_frame(vh_handle *h, const void *depth, int32_t depth_fmt,
+                           const uint8_t *rgb, const float *c2w, int32_t mem,
+                           vh_mesh_view *out);
+/* Copies the last extraction to host: xyz (9 floats per triangle, voxel
+ * units) and rgb (9 bytes per triangle); either may be NULL. */
+vh_status vh_copy_mesh(vh_handle *h, float *xyz, uint8_t *rgb,
+                       int64_t capacity, int64_t *num_triangles);
+/* Full-volume extraction written as PLY with vertices merged by exact
+ * position, as GpuTsdfGenerator::SavePLY / tsdf2mesh
+ * (src/tsdf.cu:1696-1708,1760-1888). binary = 0 writes the reference's
+ * ASCII layout. */
+vh_status vh_save_ply(vh_handle *h, const char *path, int32_t binary);
+/* GpuTsdfGenerator::render (src/tsdf.cu:1710-1758) draws with OpenGL; there
+ * is no graphics stack here, so this returns VH_ERR_UNSUPPORTED. */
+vh_status vh_render(vh_handle *h);
+
+/* ---- hash surface (vhashing::HashTable) ---------------------------------- */
+
+/* Inserts n block keys (int32 x,y,z triples): replaces
+ * HashTable::AllocKeys (include/vhashing.h:530-603). Existing keys are kept.
+ * Every key is also added to the current block list. */
+vh_status vh_alloc_keys(vh_handle *h, const int32_t *xyz, int64_t n,
+                        int32_t mem);
+/* out_block[i] = pool index of key i or -1: replaces HashTable::find
+ * (include/vhashing.h:128-131). */
+vh_status vh_find_keys(vh_handle *h, const int32_t *xyz, int64_t n,
+                       int32_t *out_block, int32_t mem);
+/* Erases n keys and recycles their blocks (zeroed): replaces
+ * HashTable::erase (include/vhashing.h:244-256). */
+vh_status vh_erase_keys(vh_handle *h, const int32_t *xyz, int64_t n,
+                        int64_t *num_erased, int32_t mem);
+/* Empties the block list: replaces HashTable::clearheap
+ * (include/vhashing.h:80-91). */
+vh_status vh_clear_block_list(vh_handle *h);
+/* Copies the block list (the reference's key_heap / heap_counter,
+ * include/vhashing.h:43,55,417-425) to host int32 triples. */
+vh_status vh_block_list(vh_handle *h, int32_t *xyz, int64_t capacity,
+                        int64_t *n);
+/* The reference's BlockHasher (include/tsdf.cuh:144-156) value of a key. */
+uint64_t vh_block_hash_ref(int32_t x, int32_t y, int32_t z);
+
+/* ---- volume I/O ------------------------------------------------------------ */
+
+/* Copies every live block to host (any output may be NULL): keys as int32
+ * triples, then per block 512 voxels in x-fastest order (index x + 8y + 64z)
+ * of sdf, weight and rgb (3 bytes). Replaces the stream-out copy of
+ * getMapValueKernel / streamOutGPU2CPU (src/tsdf.cu:459-596). */
+vh_status vh_export_blocks(vh_handle *h, int32_t *xyz, float *sdf,
+                           float *weight, uint8_t *rgb, int64_t capacity,
+                           int64_t *n);
+/* Inserts the given blocks and overwrites their voxels. Replaces the
+ * stream-in copy of streamInCPU2GPU (src/tsdf.cu:277-457). */
+vh_status vh_import_blocks(vh_handle *h, const int32_t *xyz, const float *sdf,
+                           const float *weight, const uint8_t *rgb, int64_t n);
+/* Binary snapshot of the volume (header, keys, voxel payload). */
+vh_status vh_save(vh_handle *h, const char *path);
+vh_status vh_load(vh_handle *h, const char *path);
+
+vh_status vh_get_stats(vh_handle *h, vh_stats *out);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* VHSDF_H */

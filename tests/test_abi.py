@@ -1,0 +1,77 @@
+"""The C ABI library loads, exports every declared entry point and validates
+parameters on the host (no GPU needed)."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from conftest import REPO, cuda_available
+
+
+def declared_functions():
+    text = open(os.path.join(REPO, "include", "vhsdf.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(vh_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_every_declared_symbol_is_exported():
+    from vhsdf import _native as N
+    L = C.CDLL(N.ENGINE_PATH)
+    names = declared_functions()
+    assert len(names) >= 25
+    for n in names:
+        assert hasattr(L, n), n
+    assert set(names) == set(N.SIGNATURES), "ctypes binding out of sync with the header"
+
+
+def test_params_default_and_validate():
+    from vhsdf import _native as N
+    L = N.lib()
+    p = N.VhParams()
+    assert L.vh_params_default(C.byref(p)) == N.VH_OK
+    assert (p.width, p.height, p.fx, p.cx) == (640, 480, 577.0, 320.0)
+    assert abs(p.voxel_size - 0.036) < 1e-7 and abs(p.trunc - 0.18) < 1e-7
+    assert L.vh_params_validate(C.byref(p)) == N.VH_OK
+    bad = [("width", 0), ("fx", -1.0), ("voxel_size", 0.0), ("table_log2", 40),
+           ("max_probe", 0), ("pool_blocks", 0), ("flags", 0x80)]
+    for field, val in bad:
+        q = N.VhParams()
+        L.vh_params_default(C.byref(q))
+        setattr(q, field, val)
+        assert L.vh_params_validate(C.byref(q)) != N.VH_OK, field
+    q = N.VhParams()
+    L.vh_params_default(C.byref(q))
+    q.trunc = float("nan")
+    assert L.vh_params_validate(C.byref(q)) == N.VH_ERR_NOT_FINITE
+    assert L.vh_params_validate(None) == N.VH_ERR_INVALID_ARG
+
+
+def test_status_strings_and_null_handles():
+    from vhsdf import _native as N
+    L = N.lib()
+    for s in range(12):
+        assert L.vh_status_string(s)
+    assert L.vh_destroy(None) == N.VH_ERR_INVALID_ARG
+    assert L.vh_sync(None) == N.VH_ERR_INVALID_ARG
+    assert L.vh_render(None) == N.VH_ERR_UNSUPPORTED
+    assert L.vh_last_error(None) == b"null handle"
+
+
+@pytest.mark.skipif(cuda_available(), reason="checks the no-device path")
+def test_create_without_device_reports_no_device():
+    from vhsdf import _native as N
+    L = N.lib()
+    p = N.VhParams()
+    L.vh_params_default(C.byref(p))
+    h = C.c_void_p()
+    assert L.vh_create(C.byref(p), C.byref(h)) == N.VH_ERR_NO_DEVICE
+    assert not h.value
+
+
+def test_missing_library_fails_loudly(monkeypatch):
+    from vhsdf import _native as N
+    monkeypatch.setattr(N, "_lib", None)
+    monkeypatch.setattr(N, "ENGINE_PATH", "/nonexistent/libvhsdf.so")
+    with pytest.raises(ImportError):
+        N.lib()

@@ -1,0 +1,123 @@
+"""Known-answer tests of the CPU oracle (no GPU)."""
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+
+W, H = 64, 48
+FX = FY = 50.0
+CX, CY = 31.5, 23.5
+V, T = 0.01, 0.04
+
+
+def plane_frame(d):
+    depth = np.full((H, W), d, np.float32)
+    rgb = np.zeros((H, W, 3), np.uint8)
+    rgb[..., 0] = 200
+    rgb[..., 1] = np.arange(W, dtype=np.uint8)[None, :]
+    rgb[..., 2] = 7
+    return depth, rgb, np.eye(4, dtype=np.float32)
+
+
+def grid_of(z):
+    return np.floor(((np.float32(z) / np.float32(V)) + np.float32(0.5)) * np.float32(0.125))
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_fronto_parallel_plane_sdf(precision):
+    d = 1.2345
+    o = Oracle(W, H, FX, FY, CX, CY, min_depth=0.1, max_depth=4.0, voxel_size=V, trunc=T,
+               precision=precision)
+    depth, rgb, pose = plane_frame(d)
+    o.integrate(depth, rgb, pose)
+    e = o.export()
+    assert len(e["xyz"]) > 0
+    # every allocated block lies in the band's z-range of blocks
+    bz = set(e["xyz"][:, 2].tolist())
+    lo, hi = grid_of(np.float32(d) - np.float32(T)), grid_of(np.float32(d) + np.float32(T))
+    assert bz == set(range(int(lo), int(hi) + 1))
+    li = np.arange(512)
+    xs, ys, zs = li & 7, (li >> 3) & 7, li >> 6
+    iz = e["xyz"][:, 2:3] * 8 + zs[None, :]
+    ix = e["xyz"][:, 0:1] * 8 + xs[None, :]
+    iy = e["xyz"][:, 1:2] * 8 + ys[None, :]
+    z = iz.astype(np.float64) * V
+    u = FX * (ix * V) / z + CX
+    v = FY * (iy * V) / z + CY
+    inside = (u > 0.6) & (u < W - 1.6) & (v > 0.6) & (v < H - 1.6)
+    diff = np.float64(np.float32(d)) - z
+    upd = inside & (diff > -T + 1e-4)
+    skip = inside & (diff <= -T - 1e-4)
+    assert upd.sum() > 1000
+    expect = np.minimum(1.0, diff / T)
+    assert np.all(e["weight"][upd] == 1.0)
+    assert np.all(e["weight"][skip] == 0.0)
+    # z carries fp32 rounding of the camera transform (~1e-7 m at 1.2 m);
+    # dividing by T = 0.04 m scales that to a few 1e-6 in sdf units.
+    assert np.max(np.abs(e["sdf"][upd] - expect[upd])) < 5e-6
+    # colour of the single observation is the pixel's colour
+    assert np.all(e["rgb"][upd][:, 0] == 200) and np.all(e["rgb"][upd][:, 2] == 7)
+
+
+def test_running_average_repeats():
+    o = Oracle(W, H, FX, FY, CX, CY, max_depth=4.0, voxel_size=V, trunc=T, precision=64)
+    depth, rgb, pose = plane_frame(0.9)
+    o.integrate(depth, rgb, pose)
+    first = o.export()
+    for _ in range(2):
+        o.integrate(depth, rgb, pose)
+    e = o.export()
+    m = first["weight"] > 0
+    assert np.all(e["weight"][m] == 3.0)
+    assert np.max(np.abs(e["sdf"][m] - first["sdf"][m])) < 1e-6
+    assert np.array_equal(e["rgb"], first["rgb"])
+
+
+def test_weighted_average_two_depths():
+    o = Oracle(W, H, FX, FY, CX, CY, max_depth=4.0, voxel_size=V, trunc=T, precision=64)
+    d1, rgb, pose = plane_frame(1.0)
+    d2 = np.full_like(d1, 1.02)
+    o.integrate(d1, rgb, pose)
+    o.integrate(d2, rgb, pose)
+    e = o.export(fp64=True)
+    li = np.arange(512)
+    z = (e["xyz"][:, 2:3] * 8 + (li >> 6)[None, :]) * V
+    both = e["weight64"] == 2
+    s1 = np.minimum(1, (np.float32(1.0) - z) / T)
+    s2 = np.minimum(1, (np.float32(1.02) - z) / T)
+    ok = both & (z < 0.98 + T - 1e-3)
+    assert ok.sum() > 100
+    assert np.max(np.abs(e["sdf64"][ok] - 0.5 * (s1 + s2)[ok])) < 1e-5
+
+
+def test_empty_depth_allocates_nothing():
+    o = Oracle(W, H, FX, FY, CX, CY, max_depth=4.0, voxel_size=V, trunc=T)
+    depth = np.zeros((H, W), np.float32)
+    rgb = np.zeros((H, W, 3), np.uint8)
+    assert o.integrate(depth, rgb, np.eye(4, dtype=np.float32)) == 0
+    assert o.num_blocks() == 0
+    assert len(o.marching_cubes()["xyz"]) == 0
+
+
+def test_mc_vertices_stay_in_their_cube_and_fp64_agrees():
+    from vhsdf import synth
+    s = synth.Scene(kind=1, seed=0, num_frames=20, width=160, height=120)
+    o32 = Oracle(160, 120, s.fx, s.fy, s.cx, s.cy, max_depth=4.5, voxel_size=0.02, trunc=0.08,
+                 precision=32)
+    o64 = Oracle(160, 120, s.fx, s.fy, s.cx, s.cy, max_depth=4.5, voxel_size=0.02, trunc=0.08,
+                 precision=64)
+    for f in range(3):
+        d, c, p = s.render(f)
+        o32.integrate(d, c, p)
+        o64.integrate(d, c, p)
+    a, b = o32.export(), o64.export(fp64=True)
+    assert np.array_equal(a["xyz"], b["xyz"])
+    assert np.array_equal(a["weight"], b["weight"])
+    assert np.max(np.abs(a["sdf"].astype(np.float64) - b["sdf64"])) < 1e-5
+    assert np.max(np.abs(a["rgb"].astype(int) - b["rgb"].astype(int))) <= 1
+    m = o64.marching_cubes("all")
+    n = len(m["xyz"])
+    assert n > 1000
+    lo = m["cube"][:, None, :3].astype(np.float32)
+    assert np.all(m["xyz"] >= lo - 1e-4) and np.all(m["xyz"] <= lo + 1 + 1e-4)
+    assert np.max(np.abs(m["xyz"] - m["xyz64"])) < 1e-3

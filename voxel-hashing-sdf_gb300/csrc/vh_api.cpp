@@ -1,0 +1,799 @@
+// vh_api.cpp - host orchestration behind the C ABI (include/vhsdf.h).
+//
+// The reference's processFrame (src/tsdf.cu:1484-1598) rebuilds two hash
+// tables, streams host chunks in, runs three kernels with blocking copies in
+// between and streams everything back out every frame.  Here the volume stays
+// resident in HBM; a frame is three host->device copies into fixed staging
+// buffers followed by one CUDA graph:
+//     frame_begin -> allocate -> epoch_end -> integrate [-> mc_begin -> mc]
+// All counts stay on the device; the host reads the state block only when a
+// call has to report something (VH_FLAG_SYNC, stats, mesh copies).
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/vhsdf.h"
+#include "vh_common.cuh"
+#include "vh_mesh.h"
+
+using namespace vh;
+
+namespace {
+constexpr int kPoseRing = 64;
+constexpr int kNumEvents = 5;
+}  // namespace
+
+struct vh_handle {
+  vh_params p{};
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  VolumeView V{};
+  CamParams C{};
+  void *d_depth = nullptr;
+  uint8_t *d_rgb = nullptr;
+  float *d_pose = nullptr;
+  uint2 *d_pix = nullptr;
+  float4 *d_tris = nullptr;
+  int64_t tri_cap = 0;
+  float *h_pose_ring = nullptr;
+  cudaEvent_t ring_ev[kPoseRing] = {};
+  int ring_pos = 0;
+  DevState *h_state = nullptr;
+  cudaGraphExec_t graphs[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  cudaEvent_t ev[kNumEvents] = {};
+  bool ev_pending = false;
+  bool ev_has_mc = false;
+  int64_t frames = 0;
+  std::string last_error;
+  vh_stats stage{};
+};
+
+namespace {
+
+vh_status fail(vh_handle *h, vh_status s, const std::string &msg) {
+  if (h) h->last_error = msg;
+  return s;
+}
+
+vh_status cuda_fail(vh_handle *h, cudaError_t e, const char *what) {
+  return fail(h, VH_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define VH_CUDA(h, expr)                                   \
+  do {                                                     \
+    cudaError_t e__ = (expr);                              \
+    if (e__ != cudaSuccess) return cuda_fail(h, e__, #expr); \
+  } while (0)
+
+bool finite_pose(const float *c2w) {
+  for (int i = 0; i < 16; ++i)
+    if (!std::isfinite(c2w[i])) return false;
+  return true;
+}
+
+// Maps sticky device error bits to a status (most severe first).
+vh_status status_of_bits(uint32_t bits, std::string &msg) {
+  if (bits & kErrTableFull) {
+    msg = "hash table full: a probe sequence reached max_probe";
+    return VH_ERR_TABLE_FULL;
+  }
+  if (bits & kErrPoolFull) {
+    msg = "voxel-block pool exhausted (raise pool_blocks)";
+    return VH_ERR_POOL_FULL;
+  }
+  if (bits & kErrRange) {
+    msg = "a block coordinate left the key range [-2^20, 2^20)";
+    return VH_ERR_OUT_OF_RANGE;
+  }
+  if (bits & kErrFrameCap) {
+    msg = "frame block list overflowed max_frame_blocks";
+    return VH_ERR_CAPACITY;
+  }
+  if (bits & kErrTriCap) {
+    msg = "triangle buffer overflowed max_triangles";
+    return VH_ERR_CAPACITY;
+  }
+  if (bits & kErrRetry) {
+    msg = "a bounded device wait gave up";
+    return VH_ERR_RETRY_EXHAUSTED;
+  }
+  return VH_OK;
+}
+
+// Copies the device state into h->h_state and waits for the stream.
+vh_status pull_state(vh_handle *h) {
+  VH_CUDA(h, cudaMemcpyAsync(h->h_state, h->V.st, sizeof(DevState), cudaMemcpyDeviceToHost,
+                             h->stream));
+  VH_CUDA(h, cudaStreamSynchronize(h->stream));
+  VH_CUDA(h, cudaGetLastError());
+  return VH_OK;
+}
+
+// Synchronises, then reports (and clears) sticky device errors.
+vh_status sync_and_check(vh_handle *h) {
+  vh_status s = pull_state(h);
+  if (s != VH_OK) return s;
+  if (h->ev_pending && (h->p.flags & VH_FLAG_PROFILE)) {
+    float a = 0, b = 0, c = 0;
+    cudaEventElapsedTime(&a, h->ev[0], h->ev[1]);
+    cudaEventElapsedTime(&b, h->ev[1], h->ev[2]);
+    h->stage.ms_allocate = a;
+    h->stage.ms_integrate = b;
+    if (h->ev_has_mc) {
+      cudaEventElapsedTime(&c, h->ev[2], h->ev[3]);
+      h->stage.ms_extract = c;
+      cudaEventElapsedTime(&a, h->ev[0], h->ev[3]);
+    } else {
+      h->stage.ms_extract = 0;
+      cudaEventElapsedTime(&a, h->ev[0], h->ev[2]);
+    }
+    h->stage.ms_frame = a;
+    h->ev_pending = false;
+  }
+  const uint32_t bits = h->h_state->error;
+  if (!bits) return VH_OK;
+  std::string msg;
+  vh_status st = status_of_bits(bits, msg);
+  VH_CUDA(h, cudaMemsetAsync(&h->V.st->error, 0, sizeof(uint32_t), h->stream));
+  VH_CUDA(h, cudaStreamSynchronize(h->stream));
+  return fail(h, st, msg);
+}
+
+int integrate_grid(const vh_handle *h) { return h->sm_count * 8; }
+int mc_grid(const vh_handle *h) { return h->sm_count * 6; }
+
+// Enqueues one frame's kernels (optionally with per-stage events).
+void enqueue_frame(vh_handle *h, int fmt, bool with_mc, bool events) {
+  cudaStream_t s = h->stream;
+  if (events) cudaEventRecord(h->ev[0], s);
+  launch_frame_begin(h->V, s);
+  launch_allocate(h->V, h->C, h->d_depth, fmt, h->d_rgb, h->d_pose, h->d_pix, s);
+  launch_epoch_end(h->V, s);
+  if (events) cudaEventRecord(h->ev[1], s);
+  launch_integrate(h->V, h->C, h->d_pix, h->d_pose, integrate_grid(h), s);
+  if (events) cudaEventRecord(h->ev[2], s);
+  if (with_mc) {
+    launch_mc_begin(h->V, s);
+    launch_mc(h->V, 0, h->C.mc_min_weight, h->d_tris, (uint32_t)h->tri_cap, mc_grid(h), s);
+    if (events) cudaEventRecord(h->ev[3], s);
+  }
+}
+
+void drop_graphs(vh_handle *h) {
+  for (auto &row : h->graphs)
+    for (auto &g : row)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+}
+
+// Runs the frame chain as a CUDA graph (captured on first use) or directly.
+vh_status run_frame(vh_handle *h, int fmt, bool with_mc) {
+  const bool events = (h->p.flags & VH_FLAG_PROFILE) != 0;
+  const bool graphs_ok = !(h->p.flags & VH_FLAG_NO_GRAPH) && h->stream != nullptr;
+  if (graphs_ok) {
+    cudaGraphExec_t &g = h->graphs[fmt][with_mc ? 1 : 0];
+    if (!g) {
+      cudaGraph_t graph = nullptr;
+      VH_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+      enqueue_frame(h, fmt, with_mc, events);
+      cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+      if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
+      e = cudaGraphInstantiate(&g, graph, 0);
+      cudaGraphDestroy(graph);
+      if (e != cudaSuccess) {
+        g = nullptr;
+        return cuda_fail(h, e, "cudaGraphInstantiate");
+      }
+    }
+    VH_CUDA(h, cudaGraphLaunch(g, h->stream));
+  } else {
+    enqueue_frame(h, fmt, with_mc, events);
+    VH_CUDA(h, cudaGetLastError());
+  }
+  h->ev_pending = events;
+  h->ev_has_mc = with_mc;
+  return VH_OK;
+}
+
+// Stages depth, colour and pose of one frame into the fixed device buffers.
+vh_status stage_inputs(vh_handle *h, const void *depth, int32_t fmt, const uint8_t *rgb,
+                       const float *c2w, int32_t mem) {
+  if (!depth || !rgb || !c2w) return fail(h, VH_ERR_INVALID_ARG, "null input pointer");
+  if (fmt != VH_DEPTH_U16_MM && fmt != VH_DEPTH_F32_M)
+    return fail(h, VH_ERR_INVALID_ARG, "unknown depth format");
+  if (mem != VH_MEM_HOST && mem != VH_MEM_DEVICE)
+    return fail(h, VH_ERR_INVALID_ARG, "unknown memory kind");
+  if (!finite_pose(c2w)) return fail(h, VH_ERR_NOT_FINITE, "camera pose has a non-finite entry");
+  const size_t npx = (size_t)h->p.width * h->p.height;
+  // pose: host ring of pinned slots, each reused only after its copy ran
+  float *slot = h->h_pose_ring + 16 * h->ring_pos;
+  VH_CUDA(h, cudaEventSynchronize(h->ring_ev[h->ring_pos]));
+  std::memcpy(slot, c2w, 16 * sizeof(float));
+  VH_CUDA(h, cudaMemcpyAsync(h->d_pose, slot, 16 * sizeof(float), cudaMemcpyHostToDevice,
+                             h->stream));
+  VH_CUDA(h, cudaEventRecord(h->ring_ev[h->ring_pos], h->stream));
+  h->ring_pos = (h->ring_pos + 1) % kPoseRing;
+  const cudaMemcpyKind kind = mem == VH_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  const size_t dbytes = npx * (fmt == VH_DEPTH_U16_MM ? 2 : 4);
+  VH_CUDA(h, cudaMemcpyAsync(h->d_depth, depth, dbytes, kind, h->stream));
+  VH_CUDA(h, cudaMemcpyAsync(h->d_rgb, rgb, 3 * npx, kind, h->stream));
+  return VH_OK;
+}
+
+void free_all(vh_handle *h) {
+  drop_graphs(h);
+  cudaFree(h->V.slots);
+  cudaFree(h->V.pool);
+  cudaFree(h->V.block_keys);
+  cudaFree(h->V.free_list);
+  cudaFree(h->V.frame_list);
+  cudaFree(h->V.st);
+  cudaFree(h->d_depth);
+  cudaFree(h->d_rgb);
+  cudaFree(h->d_pose);
+  cudaFree(h->d_pix);
+  cudaFree(h->d_tris);
+  if (h->h_pose_ring) cudaFreeHost(h->h_pose_ring);
+  if (h->h_state) cudaFreeHost(h->h_state);
+  for (auto &e : h->ring_ev)
+    if (e) cudaEventDestroy(e);
+  for (auto &e : h->ev)
+    if (e) cudaEventDestroy(e);
+  if (h->own_stream) cudaStreamDestroy(h->own_stream);
+}
+
+// Clears table, pool blocks in use, key list and counters.
+vh_status clear_volume(vh_handle *h, bool zero_pool_prefix) {
+  cudaStream_t s = h->stream;
+  uint32_t used = (uint32_t)h->p.pool_blocks;
+  if (zero_pool_prefix) {
+    vh_status st = pull_state(h);
+    if (st != VH_OK) return st;
+    used = h->h_state->pool_top;
+  }
+  VH_CUDA(h, cudaMemsetAsync(h->V.slots, 0xFF, sizeof(Slot) * ((size_t)h->V.slot_mask + 1), s));
+  VH_CUDA(h, cudaMemsetAsync(h->V.block_keys, 0xFF, sizeof(unsigned long long) * h->p.pool_blocks, s));
+  if (used)
+    VH_CUDA(h, cudaMemsetAsync(h->V.pool, 0, sizeof(float) * kBlockWords * (size_t)used, s));
+  VH_CUDA(h, cudaMemsetAsync(h->V.st, 0, sizeof(DevState), s));
+  VH_CUDA(h, cudaStreamSynchronize(s));
+  h->frames = 0;
+  return VH_OK;
+}
+
+template <typename T>
+struct DevBuf {
+  T *ptr = nullptr;
+  ~DevBuf() {
+    if (ptr) cudaFree(ptr);
+  }
+};
+
+// Makes `n` elements available on the device: returns `src` itself for
+// device memory, else a temporary copy.
+template <typename T>
+vh_status device_view(vh_handle *h, const T *src, size_t n, int32_t mem, DevBuf<T> &tmp,
+                      const T **out) {
+  if (mem == VH_MEM_DEVICE) {
+    *out = src;
+    return VH_OK;
+  }
+  if (mem != VH_MEM_HOST) return fail(h, VH_ERR_INVALID_ARG, "unknown memory kind");
+  VH_CUDA(h, cudaMalloc(&tmp.ptr, sizeof(T) * (n ? n : 1)));
+  VH_CUDA(h, cudaMemcpyAsync(tmp.ptr, src, sizeof(T) * n, cudaMemcpyHostToDevice, h->stream));
+  *out = tmp.ptr;
+  return VH_OK;
+}
+
+vh_status grow_tris(vh_handle *h, int64_t need) {
+  int64_t cap = need + need / 4 + 1024;
+  if (cap > 0x7FFFFFFF / 3) cap = 0x7FFFFFFF / 3;
+  if (cap <= h->tri_cap) return VH_OK;
+  VH_CUDA(h, cudaStreamSynchronize(h->stream));
+  cudaFree(h->d_tris);
+  h->d_tris = nullptr;
+  h->tri_cap = 0;
+  drop_graphs(h);  // captured graphs hold the old pointer
+  VH_CUDA(h, cudaMalloc(&h->d_tris, sizeof(float4) * 3 * (size_t)cap));
+  h->tri_cap = cap;
+  return VH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *vh_status_string(vh_status s) {
+  switch (s) {
+    case VH_OK: return "ok";
+    case VH_ERR_INVALID_ARG: return "invalid argument";
+    case VH_ERR_CUDA: return "CUDA error";
+    case VH_ERR_TABLE_FULL: return "hash table full";
+    case VH_ERR_POOL_FULL: return "block pool full";
+    case VH_ERR_RETRY_EXHAUSTED: return "retry limit reached";
+    case VH_ERR_NOT_FINITE: return "non-finite input";
+    case VH_ERR_UNSUPPORTED: return "unsupported";
+    case VH_ERR_OUT_OF_RANGE: return "coordinate out of range";
+    case VH_ERR_CAPACITY: return "capacity exceeded";
+    case VH_ERR_IO: return "I/O error";
+    case VH_ERR_NO_DEVICE: return "no CUDA device";
+  }
+  return "unknown status";
+}
+
+vh_status vh_params_default(vh_params *p) {
+  if (!p) return VH_ERR_INVALID_ARG;
+  std::memset(p, 0, sizeof(*p));
+  p->width = 640;
+  p->height = 480;
+  p->fx = 577.0f;
+  p->fy = 577.0f;
+  p->cx = 320.0f;
+  p->cy = 240.0f;
+  p->min_depth = 0.1f;
+  p->max_depth = 10.0f;
+  p->depth_scale = 0.001f;
+  p->voxel_size = 0.036f;
+  p->trunc = 0.18f;
+  p->mc_min_weight = 1.0f;
+  p->table_log2 = 20;
+  p->max_probe = 256;
+  p->pool_blocks = 1 << 18;
+  p->max_frame_blocks = 1 << 18;
+  p->max_triangles = 1 << 22;
+  p->flags = VH_FLAG_SYNC;
+  p->device = 0;
+  return VH_OK;
+}
+
+vh_status vh_params_validate(const vh_params *p) {
+  if (!p) return VH_ERR_INVALID_ARG;
+  if (p->width < 1 || p->height < 1 || p->width > 16384 || p->height > 16384)
+    return VH_ERR_INVALID_ARG;
+  const float fs[] = {p->fx, p->fy, p->cx, p->cy, p->min_depth, p->max_depth,
+                      p->depth_scale, p->voxel_size, p->trunc, p->mc_min_weight};
+  for (float f : fs)
+    if (!std::isfinite(f)) return VH_ERR_NOT_FINITE;
+  if (!(p->fx > 0) || !(p->fy > 0)) return VH_ERR_INVALID_ARG;
+  if (!(p->min_depth >= 0) || !(p->max_depth > p->min_depth)) return VH_ERR_INVALID_ARG;
+  if (!(p->depth_scale > 0) || !(p->voxel_size > 0) || !(p->trunc > 0)) return VH_ERR_INVALID_ARG;
+  if (p->table_log2 < 8 || p->table_log2 > 31) return VH_ERR_INVALID_ARG;
+  if (p->max_probe < 1 || (int64_t)p->max_probe > (1ll << p->table_log2)) return VH_ERR_INVALID_ARG;
+  if (p->pool_blocks < 1 || p->pool_blocks > 0x7FFFFFFF) return VH_ERR_INVALID_ARG;
+  if (p->max_frame_blocks < 1 || p->max_frame_blocks > 0x7FFFFFFF) return VH_ERR_INVALID_ARG;
+  if (p->max_triangles < 0 || p->max_triangles > 0x7FFFFFFF / 3) return VH_ERR_INVALID_ARG;
+  if (p->device < 0) return VH_ERR_INVALID_ARG;
+  if (p->flags & ~(uint32_t)(VH_FLAG_SYNC | VH_FLAG_NO_GRAPH | VH_FLAG_PROFILE))
+    return VH_ERR_INVALID_ARG;
+  return VH_OK;
+}
+
+vh_status vh_create(const vh_params *p, vh_handle **out) {
+  if (!out) return VH_ERR_INVALID_ARG;
+  *out = nullptr;
+  vh_status vs = vh_params_validate(p);
+  if (vs != VH_OK) return vs;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return VH_ERR_NO_DEVICE;
+  }
+  if (p->device >= ndev) return VH_ERR_INVALID_ARG;
+  vh_handle *h = new vh_handle();
+  h->p = *p;
+  auto bail = [&](vh_status s) {
+    free_all(h);
+    delete h;
+    return s;
+  };
+  if (cudaSetDevice(p->device) != cudaSuccess) return bail(VH_ERR_CUDA);
+  if (cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess)
+    return bail(VH_ERR_CUDA);
+  if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(VH_ERR_CUDA);
+  h->stream = h->own_stream;
+  const size_t slots = (size_t)1 << p->table_log2;
+  const size_t npx = (size_t)p->width * p->height;
+  h->tri_cap = p->max_triangles;
+  bool ok = cudaMalloc(&h->V.slots, sizeof(Slot) * slots) == cudaSuccess &&
+            cudaMalloc(&h->V.pool, sizeof(float) * kBlockWords * (size_t)p->pool_blocks) == cudaSuccess &&
+            cudaMalloc(&h->V.block_keys, sizeof(unsigned long long) * p->pool_blocks) == cudaSuccess &&
+            cudaMalloc(&h->V.free_list, sizeof(uint32_t) * p->pool_blocks) == cudaSuccess &&
+            cudaMalloc(&h->V.frame_list, sizeof(uint32_t) * p->max_frame_blocks) == cudaSuccess &&
+            cudaMalloc(&h->V.st, sizeof(DevState)) == cudaSuccess &&
+            cudaMalloc(&h->d_depth, 4 * npx) == cudaSuccess &&
+            cudaMalloc(&h->d_rgb, 3 * npx) == cudaSuccess &&
+            cudaMalloc(&h->d_pose, 16 * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&h->d_pix, sizeof(uint2) * npx) == cudaSuccess &&
+            cudaMalloc(&h->d_tris, sizeof(float4) * 3 * (size_t)(h->tri_cap ? h->tri_cap : 1)) == cudaSuccess &&
+            cudaMallocHost(&h->h_pose_ring, sizeof(float) * 16 * kPoseRing) == cudaSuccess &&
+            cudaMallocHost(&h->h_state, sizeof(DevState)) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    h->last_error = "device allocation failed";
+    return bail(VH_ERR_CUDA);
+  }
+  for (auto &e : h->ring_ev)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return bail(VH_ERR_CUDA);
+  for (auto &e : h->ev)
+    if (cudaEventCreate(&e) != cudaSuccess) return bail(VH_ERR_CUDA);
+  for (int i = 0; i < kPoseRing; ++i) cudaEventRecord(h->ring_ev[i], h->stream);
+  h->V.slot_mask = (uint32_t)(slots - 1);
+  h->V.max_probe = p->max_probe;
+  h->V.frame_cap = (uint32_t)p->max_frame_blocks;
+  h->V.pool_cap = (uint32_t)p->pool_blocks;
+  h->C.width = p->width;
+  h->C.height = p->height;
+  h->C.wf = (float)p->width;
+  h->C.hf = (float)p->height;
+  h->C.fx = p->fx;
+  h->C.fy = p->fy;
+  h->C.cx = p->cx;
+  h->C.cy = p->cy;
+  h->C.min_depth = p->min_depth;
+  h->C.max_depth = p->max_depth;
+  h->C.depth_scale = p->depth_scale;
+  h->C.voxel = p->voxel_size;
+  h->C.trunc = p->trunc;
+  h->C.mc_min_weight = p->mc_min_weight;
+  vs = clear_volume(h, false);
+  if (vs != VH_OK) return bail(vs);
+  *out = h;
+  return VH_OK;
+}
+
+vh_status vh_destroy(vh_handle *h) {
+  if (!h) return VH_ERR_INVALID_ARG;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  free_all(h);
+  delete h;
+  return VH_OK;
+}
+
+vh_status vh_reset(vh_handle *h) {
+  if (!h) return VH_ERR_INVALID_ARG;
+  return clear_volume(h, true);
+}
+
+vh_status vh_set_stream(vh_handle *h, void *stream) {
+  if (!h) return VH_ERR_INVALID_ARG;
+  VH_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+  return VH_OK;
+}
+
+vh_status vh_sync(vh_handle *h) {
+  if (!h) return VH_ERR_INVALID_ARG;
+  return sync_and_check(h);
+}
+
+const char *vh_last_error(const vh_handle *h) { return h ? h->last_error.c_str() : "null handle"; }
+
+vh_status vh_integrate(vh_handle *h, const void *depth, int32_t depth_fmt, const uint8_t *rgb,
+                       const float *c2w, int32_t mem) {
+  if (!h) return VH_ERR_INVALID_ARG;
+  vh_status s = stage_inputs(h, depth, depth_fmt, rgb, c2w, mem);
+  if (s != VH_OK) return s;
+  s = run_frame(h, depth_fmt, false);
+  if (s != VH_OK) return s;
+  h->frames++;
+  return (h->p.flags & VH_FLAG_SYNC) ? sync_and_check(h) : VH_OK;
+}
+
+vh_status vh_extract(vh_handle *h, int32_t scope, vh_mesh_view *out) {
+  if (!h) return VH_ERR_INVALID_ARG;
+  if (scope != VH_SCOPE_FRAME && scope != VH_SCOPE_ALL)
+    return fail(h, VH_ERR_INVALID_ARG, "unknown extraction scope");
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    launch_mc_begin(h->V, h->stream);
+    launch_mc(h->V, scope == VH_SCOPE_ALL, h->C.mc_min_weight, h->d_tris, (uint32_t)h->tri_cap,
+              mc_grid(h), h->stream);
+    VH_CUDA(h, cudaGetLastError());
+    h->ev_pending = false;
+    if (scope == VH_SCOPE_FRAME && !out && !(h->p.flags & VH_FLAG_SYNC)) return VH_OK;
+    vh_status s = pull_state(h);
+    if (s != VH_OK) return s;
+    const int64_t need = h->h_state->tri_count;
+    if (need > h->tri_cap && attempt == 0) {
+      // too many triangles: clear the overflow bit, grow and extract again
+      VH_CUDA(h, cudaMemsetAsync(&h->V.st->error, 0, sizeof(uint32_t), h->stream));
+      s = grow_tris(h, need);
+      if (s != VH_OK) return s;
+      continue;
+    }
+    break;
+  }
+  vh_status s = sync_and_check(h);
+  if (out) {
+    out->vertices = (const float *)h->d_tris;
+    out->num_triangles = std::min<int64_t>(h->h_state->tri_count, h->tri_cap);
+    out->voxel_size = h->p.voxel_size;
+  }
+  return s;
+}
+
+vh_status vh_process_frame(vh_handle *h, const void *depth, int32_t depth_fmt, const uint8_t *rgb,
+                           const float *c2w, int32_t mem, vh_mesh_view *out) {
+  if (!h) return VH_ERR_INVALID_ARG;
+  vh_status s = stage_inputs(h, depth, depth_fmt, rgb, c2w, mem);
+  if (s != VH_OK) return s;
+  s = run_frame(h, depth_fmt, true);
+  if (s != VH_OK) return s;
+  h->frames++;
+  if (!(h->p.flags & VH_FLAG_SYNC) && !out) return VH_OK;
+  s = sync_and_check(h);
+  if (out) {
+    out->vertices = (const float *)h->d_tris;
+    out->num_triangles = std::min<int64_t>(h->h_state->tri_count, h->tri_cap);
+    out->voxel_size = h->p.voxel_size;
+  }
+  return s;
+}
+
+vh_status vh_copy_mesh(vh_handle *h, float *xyz, uint8_t *rgb, int64_t capacity,
+                       int64_t *num_triangles) {
+  if (!h || capacity < 0) return VH_ERR_INVALID_ARG;
+  vh_status s = pull_state(h);
+  if (s != VH_OK) return s;
+  const int64_t n = std::min<int64_t>(h->h_state->tri_count, h->tri_cap);
+  if (num_triangles) *num_triangles = n;
+  const int64_t m = std::min(n, capacity);
+  if (m > 0 && (xyz || rgb)) {
+    std::vector<float> buf((size_t)m * 12);
+    VH_CUDA(h, cudaMemcpy(buf.data(), h->d_tris, sizeof(float) * 12 * (size_t)m, cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < 3 * m; ++i) {
+      const float *v = &buf[4 * (size_t)i];
+      if (xyz) {
+        xyz[3 * i] = v[0];
+        xyz[3 * i + 1] = v[1];
+        xyz[3 * i + 2] = v[2];
+      }
+      if (rgb) {
+        uint32_t c;
+        std::memcpy(&c, &v[3], 4);
+        rgb[3 * i] = (uint8_t)(c & 0xFF);
+        rgb[3 * i + 1] = (uint8_t)((c >> 8) & 0xFF);
+        rgb[3 * i + 2] = (uint8_t)((c >> 16) & 0xFF);
+      }
+    }
+  }
+  return m < n ? fail(h, VH_ERR_CAPACITY, "mesh larger than the output capacity") : VH_OK;
+}
+
+vh_status vh_save_ply(vh_handle *h, const char *path, int32_t binary) {
+  if (!h || !path) return VH_ERR_INVALID_ARG;
+  vh_status s = vh_extract(h, VH_SCOPE_ALL, nullptr);
+  if (s != VH_OK) return s;
+  const int64_t n = std::min<int64_t>(h->h_state->tri_count, h->tri_cap);
+  std::vector<float> buf((size_t)n * 12);
+  if (n) VH_CUDA(h, cudaMemcpy(buf.data(), h->d_tris, sizeof(float) * 12 * (size_t)n, cudaMemcpyDeviceToHost));
+  if (!write_ply(path, buf.data(), n, h->p.voxel_size, binary != 0))
+    return fail(h, VH_ERR_IO, std::string("cannot write ") + path);
+  return VH_OK;
+}
+
+vh_status vh_render(vh_handle *h) {
+  return fail(h, VH_ERR_UNSUPPORTED, "render() needs OpenGL, which is not available");
+}
+
+vh_status vh_alloc_keys(vh_handle *h, const int32_t *xyz, int64_t n, int32_t mem) {
+  if (!h || n < 0 || (n && !xyz) || n > 0x7FFFFFFF / 3) return VH_ERR_INVALID_ARG;
+  if (!n) return VH_OK;
+  DevBuf<int32_t> tmp;
+  const int32_t *d = nullptr;
+  vh_status s = device_view(h, xyz, 3 * (size_t)n, mem, tmp, &d);
+  if (s != VH_OK) return s;
+  launch_epoch_end(h->V, h->stream);
+  launch_alloc_keys(h->V, d, (uint32_t)n, h->stream);
+  launch_epoch_end(h->V, h->stream);
+  VH_CUDA(h, cudaGetLastError());
+  return sync_and_check(h);
+}
+
+vh_status vh_find_keys(vh_handle *h, const int32_t *xyz, int64_t n, int32_t *out_block,
+                       int32_t mem) {
+  if (!h || n < 0 || (n && (!xyz || !out_block)) || n > 0x7FFFFFFF / 3) return VH_ERR_INVALID_ARG;
+  if (!n) return VH_OK;
+  DevBuf<int32_t> tmp, res;
+  const int32_t *d = nullptr;
+  vh_status s = device_view(h, xyz, 3 * (size_t)n, mem, tmp, &d);
+  if (s != VH_OK) return s;
+  int32_t *dout = out_block;
+  if (mem == VH_MEM_HOST) {
+    VH_CUDA(h, cudaMalloc(&res.ptr, sizeof(int32_t) * n));
+    dout = res.ptr;
+  }
+  launch_find_keys(h->V, d, (uint32_t)n, dout, h->stream);
+  VH_CUDA(h, cudaGetLastError());
+  if (mem == VH_MEM_HOST)
+    VH_CUDA(h, cudaMemcpyAsync(out_block, dout, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, h->stream));
+  return sync_and_check(h);
+}
+
+vh_status vh_erase_keys(vh_handle *h, const int32_t *xyz, int64_t n, int64_t *num_erased,
+                        int32_t mem) {
+  if (!h || n < 0 || (n && !xyz) || n > 0x7FFFFFFF / 3) return VH_ERR_INVALID_ARG;
+  if (num_erased) *num_erased = 0;
+  if (!n) return VH_OK;
+  DevBuf<int32_t> tmp;
+  const int32_t *d = nullptr;
+  vh_status s = device_view(h, xyz, 3 * (size_t)n, mem, tmp, &d);
+  if (s != VH_OK) return s;
+  launch_epoch_end(h->V, h->stream);
+  VH_CUDA(h, cudaMemsetAsync(&h->V.st->erased, 0, sizeof(uint32_t), h->stream));
+  launch_erase_keys(h->V, d, (uint32_t)n, h->stream);
+  VH_CUDA(h, cudaGetLastError());
+  s = sync_and_check(h);
+  if (num_erased) *num_erased = h->h_state->erased;
+  return s;
+}
+
+vh_status vh_clear_block_list(vh_handle *h) {
+  if (!h) return VH_ERR_INVALID_ARG;
+  launch_clear_list(h->V, h->stream);
+  VH_CUDA(h, cudaGetLastError());
+  return (h->p.flags & VH_FLAG_SYNC) ? sync_and_check(h) : VH_OK;
+}
+
+vh_status vh_block_list(vh_handle *h, int32_t *xyz, int64_t capacity, int64_t *n) {
+  if (!h || capacity < 0) return VH_ERR_INVALID_ARG;
+  vh_status s = pull_state(h);
+  if (s != VH_OK) return s;
+  const int64_t cnt = std::min<int64_t>(h->h_state->frame_count, h->p.max_frame_blocks);
+  if (n) *n = cnt;
+  const int64_t m = std::min(cnt, capacity);
+  if (m > 0 && xyz) {
+    DevBuf<int32_t> tmp;
+    VH_CUDA(h, cudaMalloc(&tmp.ptr, sizeof(int32_t) * 3 * m));
+    launch_list_keys(h->V, tmp.ptr, (uint32_t)m, h->stream);
+    VH_CUDA(h, cudaGetLastError());
+    VH_CUDA(h, cudaMemcpyAsync(xyz, tmp.ptr, sizeof(int32_t) * 3 * m, cudaMemcpyDeviceToHost, h->stream));
+    VH_CUDA(h, cudaStreamSynchronize(h->stream));
+  }
+  return m < cnt ? fail(h, VH_ERR_CAPACITY, "block list larger than the output capacity") : VH_OK;
+}
+
+uint64_t vh_block_hash_ref(int32_t x, int32_t y, int32_t z) { return ref_block_hash(x, y, z); }
+
+vh_status vh_export_blocks(vh_handle *h, int32_t *xyz, float *sdf, float *weight, uint8_t *rgb,
+                           int64_t capacity, int64_t *n) {
+  if (!h || capacity < 0) return VH_ERR_INVALID_ARG;
+  launch_epoch_end(h->V, h->stream);
+  vh_status s = pull_state(h);
+  if (s != VH_OK) return s;
+  const uint32_t top = h->h_state->pool_top;
+  std::vector<unsigned long long> keys(top);
+  if (top)
+    VH_CUDA(h, cudaMemcpy(keys.data(), h->V.block_keys, sizeof(unsigned long long) * top,
+                          cudaMemcpyDeviceToHost));
+  int64_t live = 0;
+  for (uint32_t b = 0; b < top; ++b) live += keys[b] < kTombKey;
+  if (n) *n = live;
+  const bool want_data = sdf || weight || rgb;
+  const uint32_t chunk = 8192;
+  std::vector<float> buf;
+  int64_t o = 0;
+  for (uint32_t b0 = 0; b0 < top && o < capacity; b0 += chunk) {
+    const uint32_t cnt = std::min(chunk, top - b0);
+    if (want_data) {
+      buf.resize((size_t)cnt * kBlockWords);
+      VH_CUDA(h, cudaMemcpy(buf.data(), h->V.pool + (size_t)b0 * kBlockWords,
+                            sizeof(float) * kBlockWords * cnt, cudaMemcpyDeviceToHost));
+    }
+    for (uint32_t j = 0; j < cnt && o < capacity; ++j) {
+      const unsigned long long k = keys[b0 + j];
+      if (k >= kTombKey) continue;
+      int x, y, z;
+      unpack_key(k, x, y, z);
+      if (xyz) {
+        xyz[3 * o] = x;
+        xyz[3 * o + 1] = y;
+        xyz[3 * o + 2] = z;
+      }
+      const float *blk = want_data ? &buf[(size_t)j * kBlockWords] : nullptr;
+      if (sdf) std::memcpy(sdf + (size_t)o * kB3, blk, sizeof(float) * kB3);
+      if (weight) std::memcpy(weight + (size_t)o * kB3, blk + kB3, sizeof(float) * kB3);
+      if (rgb) {
+        const uint32_t *c = reinterpret_cast<const uint32_t *>(blk + 2 * kB3);
+        uint8_t *dst = rgb + (size_t)o * kB3 * 3;
+        for (int v = 0; v < kB3; ++v) {
+          dst[3 * v] = (uint8_t)(c[v] & 0xFF);
+          dst[3 * v + 1] = (uint8_t)((c[v] >> 8) & 0xFF);
+          dst[3 * v + 2] = (uint8_t)((c[v] >> 16) & 0xFF);
+        }
+      }
+      ++o;
+    }
+  }
+  return o < live ? fail(h, VH_ERR_CAPACITY, "volume larger than the output capacity") : VH_OK;
+}
+
+vh_status vh_import_blocks(vh_handle *h, const int32_t *xyz, const float *sdf, const float *weight,
+                           const uint8_t *rgb, int64_t n) {
+  if (!h || n < 0 || (n && (!xyz || !sdf || !weight || !rgb)) || n > (1ll << 24))
+    return VH_ERR_INVALID_ARG;
+  if (!n) return VH_OK;
+  DevBuf<int32_t> dk;
+  DevBuf<float> ds, dw;
+  DevBuf<uint8_t> dc;
+  const int32_t *k = nullptr;
+  const float *s_ = nullptr, *w_ = nullptr;
+  const uint8_t *c_ = nullptr;
+  vh_status s;
+  if ((s = device_view(h, xyz, 3 * (size_t)n, VH_MEM_HOST, dk, &k)) != VH_OK) return s;
+  if ((s = device_view(h, sdf, (size_t)n * kB3, VH_MEM_HOST, ds, &s_)) != VH_OK) return s;
+  if ((s = device_view(h, weight, (size_t)n * kB3, VH_MEM_HOST, dw, &w_)) != VH_OK) return s;
+  if ((s = device_view(h, rgb, (size_t)n * kB3 * 3, VH_MEM_HOST, dc, &c_)) != VH_OK) return s;
+  launch_epoch_end(h->V, h->stream);
+  launch_alloc_keys(h->V, k, (uint32_t)n, h->stream);
+  launch_epoch_end(h->V, h->stream);
+  launch_scatter_blocks(h->V, k, s_, w_, c_, (uint32_t)n, h->stream);
+  VH_CUDA(h, cudaGetLastError());
+  return sync_and_check(h);
+}
+
+vh_status vh_save(vh_handle *h, const char *path) {
+  if (!h || !path) return VH_ERR_INVALID_ARG;
+  int64_t n = 0;
+  vh_status s = vh_export_blocks(h, nullptr, nullptr, nullptr, nullptr, 0, &n);
+  if (s != VH_OK && s != VH_ERR_CAPACITY) return s;
+  std::vector<int32_t> xyz(3 * (size_t)n);
+  std::vector<float> sdf((size_t)n * kB3), w((size_t)n * kB3);
+  std::vector<uint8_t> rgb((size_t)n * kB3 * 3);
+  s = vh_export_blocks(h, xyz.data(), sdf.data(), w.data(), rgb.data(), n, &n);
+  if (s != VH_OK) return s;
+  if (!write_snapshot(path, h->p.voxel_size, h->p.trunc, xyz.data(), sdf.data(), w.data(),
+                      rgb.data(), n))
+    return fail(h, VH_ERR_IO, std::string("cannot write ") + path);
+  return VH_OK;
+}
+
+vh_status vh_load(vh_handle *h, const char *path) {
+  if (!h || !path) return VH_ERR_INVALID_ARG;
+  std::vector<int32_t> xyz;
+  std::vector<float> sdf, w;
+  std::vector<uint8_t> rgb;
+  float voxel = 0, trunc = 0;
+  if (!read_snapshot(path, &voxel, &trunc, xyz, sdf, w, rgb))
+    return fail(h, VH_ERR_IO, std::string("cannot read snapshot ") + path);
+  if (voxel != h->p.voxel_size)
+    return fail(h, VH_ERR_INVALID_ARG, "snapshot voxel size differs from the handle's");
+  vh_status s = clear_volume(h, true);
+  if (s != VH_OK) return s;
+  const int64_t n = (int64_t)xyz.size() / 3;
+  s = vh_import_blocks(h, xyz.data(), sdf.data(), w.data(), rgb.data(), n);
+  if (s != VH_OK) return s;
+  return vh_clear_block_list(h);
+}
+
+vh_status vh_get_stats(vh_handle *h, vh_stats *out) {
+  if (!h || !out) return VH_ERR_INVALID_ARG;
+  launch_epoch_end(h->V, h->stream);
+  vh_status s = sync_and_check(h);
+  const DevState &d = *h->h_state;
+  std::memset(out, 0, sizeof(*out));
+  out->frames = h->frames;
+  out->blocks_allocated = (int64_t)d.pool_top - (int64_t)d.free_count;
+  out->frame_blocks = std::min<int64_t>(d.frame_count, h->p.max_frame_blocks);
+  out->new_blocks = d.new_blocks;
+  out->voxels_updated = (int64_t)d.voxels_updated;
+  out->triangles = d.tri_count;
+  out->pool_capacity = h->p.pool_blocks;
+  out->table_slots = (int64_t)h->V.slot_mask + 1;
+  out->tombstones = d.tombstones;
+  out->device_error = d.error;
+  out->ms_allocate = h->stage.ms_allocate;
+  out->ms_integrate = h->stage.ms_integrate;
+  out->ms_extract = h->stage.ms_extract;
+  out->ms_frame = h->stage.ms_frame;
+  return s;
+}
+
+}  // extern "C"

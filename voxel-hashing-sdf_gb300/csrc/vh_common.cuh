@@ -1,0 +1,140 @@
+// vh_common.cuh - data layout and device helpers shared by the kernels and
+// the host orchestration.
+//
+// HBM layout of one volume:
+//   slots       2^k x 16 B  open-addressed hash: {u64 key, u32 block, u32 stamp}
+//   pool        N x 6 KiB   voxel blocks; block b is sdf[512] | weight[512] |
+//                           rgba8[512] (x-fastest voxel order x + 8y + 64z)
+//   block_keys  N x 8 B     packed key of every pool block (EMPTY if free)
+//   free_list   N x 4 B     recycled (already zeroed) block ids
+//   frame_list  M x 4 B     slot ids touched by the current frame
+//   state       one DevState of counters and sticky error bits
+//
+// The reference keeps a bucketed, lock-protected table with overflow chains
+// (include/vhashing.h:149-239,394-484) and rebuilds it every frame
+// (src/tsdf.cu:1488,1492).  Here the table is resident and lock-free: a key
+// is claimed with one 64-bit atomicCAS and probes are linear and bounded.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace vh {
+
+constexpr int kB = 8;          // voxels per block edge
+constexpr int kB3 = 512;       // voxels per block
+constexpr int kBlockWords = 3 * kB3;  // sdf, weight, rgba
+constexpr int kKeyBias = 1 << 20;     // block coords in [-2^20, 2^20)
+constexpr unsigned long long kEmptyKey = 0xFFFFFFFFFFFFFFFFull;
+constexpr unsigned long long kTombKey = 0xFFFFFFFFFFFFFFFEull;
+constexpr uint32_t kNoBlock = 0xFFFFFFFFu;
+// |continuous block coordinate| bound that keeps every walked key in range
+constexpr float kGridLimit = 1048000.0f;
+
+// Device error bits (sticky until reported).
+enum : uint32_t {
+  kErrTableFull = 1u,
+  kErrPoolFull = 2u,
+  kErrRange = 4u,
+  kErrFrameCap = 8u,
+  kErrTriCap = 16u,
+  kErrRetry = 32u,
+};
+
+struct __align__(16) Slot {
+  unsigned long long key;
+  uint32_t block;
+  uint32_t stamp;
+};
+
+struct DevState {
+  uint32_t frame;        // stamp of the current block list (never 0 after begin)
+  uint32_t frame_count;  // entries appended to frame_list (may exceed capacity)
+  uint32_t pool_top;     // ids [0, pool_top) have been handed out at least once
+  uint32_t free_count;   // recycled ids in free_list[0, free_count)
+  uint32_t ticket;       // ids taken in the open allocation epoch
+  uint32_t new_blocks;   // blocks created by the last allocation epoch(s)
+  uint32_t tri_count;    // triangles produced by the last extraction
+  uint32_t error;        // sticky kErr* bits
+  unsigned long long voxels_updated;  // by the last integration
+  uint32_t tombstones;   // erased slots
+  uint32_t erased;       // keys erased by the last erase call
+  uint32_t pad[4];
+};
+
+// Everything a kernel needs to reach the volume; passed by value.
+struct VolumeView {
+  Slot *slots;
+  uint32_t slot_mask;
+  int32_t max_probe;
+  float *pool;
+  unsigned long long *block_keys;
+  uint32_t *free_list;
+  uint32_t *frame_list;
+  uint32_t frame_cap;
+  uint32_t pool_cap;
+  DevState *st;
+};
+
+// Camera and integration constants of a handle.
+struct CamParams {
+  int32_t width, height;
+  float wf, hf;  // width, height as floats
+  float fx, fy, cx, cy;
+  float min_depth, max_depth, depth_scale;
+  float voxel, trunc, mc_min_weight;
+};
+
+__host__ __device__ inline bool key_in_range(int x, int y, int z) {
+  return (uint32_t)(x + kKeyBias) < (1u << 21) && (uint32_t)(y + kKeyBias) < (1u << 21) &&
+         (uint32_t)(z + kKeyBias) < (1u << 21);
+}
+
+__host__ __device__ inline unsigned long long pack_key(int x, int y, int z) {
+  return (unsigned long long)(uint32_t)(x + kKeyBias) |
+         ((unsigned long long)(uint32_t)(y + kKeyBias) << 21) |
+         ((unsigned long long)(uint32_t)(z + kKeyBias) << 42);
+}
+
+__host__ __device__ inline void unpack_key(unsigned long long k, int &x, int &y, int &z) {
+  x = (int)(k & 0x1FFFFFull) - kKeyBias;
+  y = (int)((k >> 21) & 0x1FFFFFull) - kKeyBias;
+  z = (int)((k >> 42) & 0x1FFFFFull) - kKeyBias;
+}
+
+// 64-bit finaliser (splitmix64 / Stafford mix 13) for the slot index.
+__host__ __device__ inline unsigned long long mix64(unsigned long long z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// The reference's BlockHasher (include/tsdf.cuh:144-156): each int component
+// is converted to size_t (sign-extended), multiplied and XORed.
+__host__ __device__ inline unsigned long long ref_block_hash(int x, int y, int z) {
+  return ((unsigned long long)(long long)x * 73856093ull) ^
+         ((unsigned long long)(long long)y * 19349669ull) ^
+         ((unsigned long long)(long long)z * 83492791ull);
+}
+
+// ---- host-side launchers (vh_kernels.cu) ----------------------------------
+void launch_frame_begin(const VolumeView &V, cudaStream_t s);
+void launch_epoch_end(const VolumeView &V, cudaStream_t s);
+void launch_clear_list(const VolumeView &V, cudaStream_t s);
+void launch_mc_begin(const VolumeView &V, cudaStream_t s);
+// fmt: 0 = uint16 scaled by depth_scale, 1 = float metres
+void launch_allocate(const VolumeView &V, const CamParams &C, const void *depth, int fmt,
+                     const uint8_t *rgb, const float *pose, uint2 *pix, cudaStream_t s);
+void launch_integrate(const VolumeView &V, const CamParams &C, const uint2 *pix,
+                      const float *pose, int grid, cudaStream_t s);
+void launch_mc(const VolumeView &V, int scope_all, float min_weight, float4 *tris,
+               uint32_t tri_cap, int grid, cudaStream_t s);
+void launch_alloc_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, cudaStream_t s);
+void launch_find_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, int32_t *out,
+                      cudaStream_t s);
+void launch_erase_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, cudaStream_t s);
+void launch_list_keys(const VolumeView &V, int32_t *xyz, uint32_t n, cudaStream_t s);
+void launch_scatter_blocks(const VolumeView &V, const int32_t *xyz, const float *sdf,
+                           const float *w, const uint8_t *rgb, uint32_t n, cudaStream_t s);
+
+}  // namespace vh

@@ -1,0 +1,838 @@
+// vh_kernels.cu - the per-frame hot path on sm_103a.
+//
+//   k_allocate   one thread per pixel: walks the blocks of the pixel's
+//                truncation band, de-duplicates keys across the warp with
+//                __match_any_sync, claims new keys with one atomicCAS, hands
+//                out pool blocks with one warp-aggregated atomic, stamps each
+//                touched slot once per frame and appends it to the frame list
+//                (replaces HashAssignKernel, src/tsdf.cu:2088-2238, and the
+//                locked insert of include/vhashing.h:205-239,394-484).
+//   k_integrate  persistent CTAs of 128 threads, one voxel block per CTA
+//                iteration, four voxels per thread with 16-byte loads and
+//                stores of sdf, weight and colour (replaces
+//                IntegrateHashKernel, src/tsdf.cu:599-751).
+//   k_mc         persistent CTAs: one block plus its +x/+y/+z halo staged in
+//                shared memory (7 hash probes per block instead of up to 16
+//                per voxel), cube cases counted, a CTA-wide scan compacts the
+//                triangles into one output range (replaces
+//                marchingCubeHashKernel, src/tsdf.cu:884-1110).
+//
+// This file is compiled with -fmad=false: every fp32 operation that decides a
+// pixel, a block, a cube case or a stored value is a single IEEE rounding in
+// the reference's operation order, so the CPU oracle (built with
+// -ffp-contract=off) reproduces it bit for bit.
+//
+// Every loop is bounded (probe length <= max_probe, band walk <= the key
+// distance between its end blocks); no kernel waits on another thread.
+
+#include "vh_common.cuh"
+#include "vh_mc_tables.h"
+
+namespace vh {
+
+namespace {
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
+// Smallest float >= 1e-5: `fabs(v) < 0.00001` in the reference compares a
+// float against a double literal (src/tsdf.cu:1645-1650); for a float v that
+// is exactly `fabsf(v) < kSnap`.
+constexpr float kSnap = 0x1.4f8b5ap-17f;
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+__device__ __forceinline__ unsigned long long ld_volatile(const unsigned long long *p) {
+  return *(volatile const unsigned long long *)p;
+}
+__device__ __forceinline__ uint32_t ld_volatile(const uint32_t *p) {
+  return *(volatile const uint32_t *)p;
+}
+
+// Claims or finds `key`. Returns the slot index or kNoBlock (table full).
+__device__ uint32_t slot_insert(const VolumeView &V, unsigned long long key, bool *created) {
+  const uint32_t h = (uint32_t)mix64(key) & V.slot_mask;
+  for (int i = 0; i < V.max_probe; ++i) {
+    const uint32_t s = (h + (uint32_t)i) & V.slot_mask;
+    unsigned long long k = ld_volatile(&V.slots[s].key);
+    if (k == key) {
+      *created = false;
+      return s;
+    }
+    if (k == kEmptyKey) {
+      unsigned long long old = atomicCAS(&V.slots[s].key, kEmptyKey, key);
+      if (old == kEmptyKey) {
+        *created = true;
+        return s;
+      }
+      if (old == key) {
+        *created = false;
+        return s;
+      }
+    }
+  }
+  atomicOr(&V.st->error, kErrTableFull);
+  *created = false;
+  return kNoBlock;
+}
+
+// Slot of `key` or kNoBlock.  Only valid between kernels that insert.
+__device__ __forceinline__ uint32_t slot_find(const VolumeView &V, unsigned long long key) {
+  const uint32_t h = (uint32_t)mix64(key) & V.slot_mask;
+  for (int i = 0; i < V.max_probe; ++i) {
+    const uint32_t s = (h + (uint32_t)i) & V.slot_mask;
+    const unsigned long long k = __ldg(&V.slots[s].key);
+    if (k == key) return s;
+    if (k == kEmptyKey) return kNoBlock;
+  }
+  return kNoBlock;
+}
+
+__device__ __forceinline__ uint32_t block_of(const VolumeView &V, unsigned long long key) {
+  const uint32_t s = slot_find(V, key);
+  return s == kNoBlock ? kNoBlock : __ldg(&V.slots[s].block);
+}
+
+// Block id for allocation ticket t of the open epoch (free list first).
+__device__ __forceinline__ uint32_t take_block(const VolumeView &V, uint32_t t, uint32_t free0,
+                                               uint32_t top0) {
+  if (t < free0) return V.free_list[free0 - 1u - t];
+  const unsigned long long id = (unsigned long long)top0 + (t - free0);
+  if (id >= V.pool_cap) {
+    atomicOr(&V.st->error, kErrPoolFull);
+    return kNoBlock;
+  }
+  return (uint32_t)id;
+}
+
+// Called by every lane of a warp: lanes with `created` get pool blocks for
+// their freshly claimed slots (one atomic per warp).
+__device__ __forceinline__ void assign_blocks(const VolumeView &V, bool created, uint32_t slot,
+                                              unsigned long long key, uint32_t free0,
+                                              uint32_t top0) {
+  const unsigned cm = __ballot_sync(kFull, created);
+  if (!cm) return;
+  const int lane = threadIdx.x & 31;
+  const int first = __ffs(cm) - 1;
+  uint32_t base = 0;
+  if (lane == first) base = atomicAdd(&V.st->ticket, (uint32_t)__popc(cm));
+  base = __shfl_sync(kFull, base, first);
+  if (created) {
+    const uint32_t b = take_block(V, base + (uint32_t)__popc(cm & lanemask_lt()), free0, top0);
+    V.slots[slot].block = b;
+    if (b != kNoBlock) V.block_keys[b] = key;
+  }
+}
+
+// Called by every lane: stamps `slot` for this frame and appends it to the
+// frame list if this lane is the first to touch it (one atomic per warp).
+__device__ __forceinline__ void stamp_and_append(const VolumeView &V, bool leader, uint32_t slot,
+                                                 uint32_t frame) {
+  bool app = false;
+  if (leader && slot != kNoBlock) {
+    if (ld_volatile(&V.slots[slot].stamp) != frame)
+      app = atomicExch(&V.slots[slot].stamp, frame) != frame;
+  }
+  const unsigned am = __ballot_sync(kFull, app);
+  if (!am) return;
+  const int lane = threadIdx.x & 31;
+  const int first = __ffs(am) - 1;
+  uint32_t base = 0;
+  if (lane == first) base = atomicAdd(&V.st->frame_count, (uint32_t)__popc(am));
+  base = __shfl_sync(kFull, base, first);
+  if (app) {
+    const uint32_t i = base + (uint32_t)__popc(am & lanemask_lt());
+    if (i < V.frame_cap)
+      V.frame_list[i] = slot;
+    else
+      atomicOr(&V.st->error, kErrFrameCap);
+  }
+}
+
+// ---- band walk ---------------------------------------------------------------
+// 6-connected walk over the block cells between two continuous block
+// coordinates: exactly |dx|+|dy|+|dz| steps, each along the axis (with cells
+// left to cross) whose next boundary comes first; ties go x, y, z.
+struct BandWalk {
+  int cx, cy, cz;
+  int sx, sy, sz;
+  int rx, ry, rz;
+  float tx, ty, tz;
+  float dx, dy, dz;
+};
+
+__device__ __forceinline__ void walk_axis(float ga, float gb, int &c, int &st, int &rem, float &tm,
+                                          float &td) {
+  c = (int)floorf(ga);
+  const int e = (int)floorf(gb);
+  const float dir = gb - ga;
+  if (e > c) {
+    st = 1;
+    rem = e - c;
+    td = 1.0f / dir;
+    tm = ((float)(c + 1) - ga) / dir;
+  } else if (e < c) {
+    st = -1;
+    rem = c - e;
+    const float nd = -dir;
+    td = 1.0f / nd;
+    tm = (ga - (float)c) / nd;
+  } else {
+    st = 0;
+    rem = 0;
+    td = 0.0f;
+    tm = 0.0f;
+  }
+}
+
+__device__ __forceinline__ bool walk_next(BandWalk &w) {
+  int best = -1;
+  float bt = 0.0f;
+  if (w.rx) {
+    best = 0;
+    bt = w.tx;
+  }
+  if (w.ry && (best < 0 || w.ty < bt)) {
+    best = 1;
+    bt = w.ty;
+  }
+  if (w.rz && (best < 0 || w.tz < bt)) best = 2;
+  if (best == 0) {
+    w.cx += w.sx;
+    w.rx -= 1;
+    w.tx = w.tx + w.dx;
+  } else if (best == 1) {
+    w.cy += w.sy;
+    w.ry -= 1;
+    w.ty = w.ty + w.dy;
+  } else if (best == 2) {
+    w.cz += w.sz;
+    w.rz -= 1;
+    w.tz = w.tz + w.dz;
+  } else {
+    return false;
+  }
+  return true;
+}
+
+// frame2cam (src/tsdf.cu:67-74) then cam2base (src/tsdf.cu:95-106), then the
+// continuous block coordinate ((p / V) + 0.5) / 8.
+__device__ __forceinline__ void pixel_to_grid(int u, int v, float z, const CamParams &C,
+                                              const float P[12], float g[3]) {
+  const float c0 = (((float)u - C.cx) * z) / C.fx;
+  const float c1 = (((float)v - C.cy) * z) / C.fy;
+  const float c2 = z;
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    float a = c0 * P[r * 4 + 0];
+    a = a + c1 * P[r * 4 + 1];
+    a = a + c2 * P[r * 4 + 2];
+    a = a + P[r * 4 + 3];
+    float q = a / C.voxel;
+    q = q + 0.5f;
+    g[r] = q * 0.125f;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ float load_depth(const T *d, int i, float scale);
+template <>
+__device__ __forceinline__ float load_depth<uint16_t>(const uint16_t *d, int i, float scale) {
+  return (float)__ldg(d + i) * scale;
+}
+template <>
+__device__ __forceinline__ float load_depth<float>(const float *d, int i, float) {
+  return __ldg(d + i);
+}
+
+// ---- allocation ----------------------------------------------------------------
+template <typename DepthT>
+__global__ void __launch_bounds__(256) k_allocate(VolumeView V, CamParams C,
+                                                  const DepthT *__restrict__ depth,
+                                                  const uint8_t *__restrict__ rgb,
+                                                  const float *__restrict__ pose,
+                                                  uint2 *__restrict__ pix) {
+  const int npx = C.width * C.height;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  float P[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) P[k] = __ldg(pose + k);
+  const uint32_t frame = V.st->frame;
+  const uint32_t free0 = V.st->free_count;
+  const uint32_t top0 = V.st->pool_top;
+
+  bool active = false;
+  BandWalk w;
+  if (idx < npx) {
+    const float d = load_depth<DepthT>(depth, idx, C.depth_scale);
+    const uint32_t c = (uint32_t)__ldg(rgb + 3 * idx) | ((uint32_t)__ldg(rgb + 3 * idx + 1) << 8) |
+                       ((uint32_t)__ldg(rgb + 3 * idx + 2) << 16);
+    pix[idx] = make_uint2(__float_as_uint(d), c);
+    if (d > 0.0f && d <= C.max_depth) {
+      float z0 = d - C.trunc;
+      if (z0 < C.min_depth) z0 = C.min_depth;
+      const float z1 = d + C.trunc;
+      if (z1 > z0) {
+        const int u = idx % C.width, v = idx / C.width;
+        float ga[3], gb[3];
+        pixel_to_grid(u, v, z0, C, P, ga);
+        pixel_to_grid(u, v, z1, C, P, gb);
+        bool ok = true;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+          ok = ok && fabsf(ga[a]) < kGridLimit && fabsf(gb[a]) < kGridLimit;
+        if (ok) {
+          walk_axis(ga[0], gb[0], w.cx, w.sx, w.rx, w.tx, w.dx);
+          walk_axis(ga[1], gb[1], w.cy, w.sy, w.ry, w.ty, w.dy);
+          walk_axis(ga[2], gb[2], w.cz, w.sz, w.rz, w.tz, w.dz);
+          active = true;
+        } else {
+          atomicOr(&V.st->error, kErrRange);
+        }
+      }
+    }
+  }
+  while (__any_sync(kFull, active)) {
+    const unsigned long long key = active ? pack_key(w.cx, w.cy, w.cz) : kEmptyKey;
+    const unsigned peers = __match_any_sync(kFull, key);
+    const bool leader = active && (__ffs(peers) - 1) == lane;
+    bool created = false;
+    uint32_t slot = kNoBlock;
+    if (leader) slot = slot_insert(V, key, &created);
+    assign_blocks(V, created, slot, key, free0, top0);
+    stamp_and_append(V, leader, slot, frame);
+    if (active) active = walk_next(w);
+  }
+}
+
+// ---- integration ---------------------------------------------------------------
+// One voxel of IntegrateHashKernel (src/tsdf.cu:690-745), sdf averaged with
+// the old weight.
+__device__ __forceinline__ bool update_voxel(const CamParams &C, const float P[12],
+                                             const uint2 *__restrict__ pix, float wx, float wy,
+                                             float wz, float &sdf, float &wt, uint32_t &rgb) {
+  // base2cam (src/tsdf.cu:81-93)
+  const float t0 = wx - P[3], t1 = wy - P[7], t2 = wz - P[11];
+  float x = P[0] * t0;
+  x = x + P[4] * t1;
+  x = x + P[8] * t2;
+  float y = P[1] * t0;
+  y = y + P[5] * t1;
+  y = y + P[9] * t2;
+  float z = P[2] * t0;
+  z = z + P[6] * t1;
+  z = z + P[10] * t2;
+  if (!(z > 0.0f)) return false;
+  // cam2frame (src/tsdf.cu:75-79)
+  const float uf = roundf(C.fx * (x / z) + C.cx);
+  const float vf = roundf(C.fy * (y / z) + C.cy);
+  if (!(uf >= 0.0f && uf < C.wf && vf >= 0.0f && vf < C.hf)) return false;
+  const uint2 px = __ldg(pix + (int)vf * C.width + (int)uf);
+  const float d = __uint_as_float(px.x);
+  if (!(d > 0.0f && d <= C.max_depth)) return false;
+  const float diff = d - z;
+  if (diff <= -C.trunc) return false;
+  const float dist = fminf(1.0f, diff / C.trunc);
+  const float w_old = wt;
+  const float w_new = w_old + 1.0f;
+  sdf = (sdf * w_old + dist) / w_new;
+  uint32_t out = 0;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float old_c = (float)((rgb >> (8 * c)) & 0xFFu);
+    const float new_c = (float)((px.y >> (8 * c)) & 0xFFu);
+    const float v = (old_c * w_old + new_c) / w_new;
+    out |= (__float2uint_rz(v) & 0xFFu) << (8 * c);
+  }
+  rgb = out;
+  wt = w_new;
+  return true;
+}
+
+__global__ void __launch_bounds__(128) k_integrate(VolumeView V, CamParams C,
+                                                   const uint2 *__restrict__ pix,
+                                                   const float *__restrict__ pose) {
+  const uint32_t n = min(V.st->frame_count, V.frame_cap);
+  float P[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) P[k] = __ldg(pose + k);
+  const int t = threadIdx.x;
+  const int x0 = (t & 1) * 4, y = (t >> 1) & 7, z = t >> 4;
+  uint32_t updated = 0;
+  for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+    const uint32_t s = __ldg(V.frame_list + i);
+    const ulonglong2 sl = __ldg(reinterpret_cast<const ulonglong2 *>(V.slots) + s);
+    const unsigned long long key = sl.x;
+    const uint32_t b = (uint32_t)sl.y;
+    if (key >= kTombKey || b == kNoBlock) continue;
+    int bx, by, bz;
+    unpack_key(key, bx, by, bz);
+    float *base = V.pool + (size_t)b * kBlockWords;
+    float4 sd = reinterpret_cast<const float4 *>(base)[t];
+    float4 wt = reinterpret_cast<const float4 *>(base + kB3)[t];
+    uint4 cl = reinterpret_cast<const uint4 *>(base + 2 * kB3)[t];
+    const float wy = (float)(by * kB + y) * C.voxel;
+    const float wz = (float)(bz * kB + z) * C.voxel;
+    const int ix = bx * kB + x0;
+    bool a0 = update_voxel(C, P, pix, (float)(ix + 0) * C.voxel, wy, wz, sd.x, wt.x, cl.x);
+    bool a1 = update_voxel(C, P, pix, (float)(ix + 1) * C.voxel, wy, wz, sd.y, wt.y, cl.y);
+    bool a2 = update_voxel(C, P, pix, (float)(ix + 2) * C.voxel, wy, wz, sd.z, wt.z, cl.z);
+    bool a3 = update_voxel(C, P, pix, (float)(ix + 3) * C.voxel, wy, wz, sd.w, wt.w, cl.w);
+    const uint32_t nu = (uint32_t)a0 + a1 + a2 + a3;
+    if (nu) {
+      reinterpret_cast<float4 *>(base)[t] = sd;
+      reinterpret_cast<float4 *>(base + kB3)[t] = wt;
+      reinterpret_cast<uint4 *>(base + 2 * kB3)[t] = cl;
+    }
+    updated += nu;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) updated += __shfl_xor_sync(kFull, updated, o);
+  if ((t & 31) == 0 && updated) atomicAdd(&V.st->voxels_updated, (unsigned long long)updated);
+}
+
+// ---- marching cubes --------------------------------------------------------------
+constexpr int kH = 9;            // staged edge: 8 voxels + 1 halo
+constexpr int kH3 = kH * kH * kH;  // 729
+constexpr int kHalo = kH3 - kB3;   // 217
+
+struct McShared {
+  float sdf[kH3];      // NaN = corner unusable (absent block or low weight)
+  uint32_t rgb[kH3];
+  int8_t tri[256][16];
+  uint16_t edge[256];
+  uint32_t nb[8];
+  int key[3];
+  uint32_t warp_sum[4];
+  uint32_t base;
+};
+
+__device__ __forceinline__ int hidx(int x, int y, int z) { return x + kH * (y + kH * z); }
+
+__device__ __forceinline__ int corner_dx(int k) { return (kMcCornerBitsX >> k) & 1; }
+__device__ __forceinline__ int corner_dy(int k) { return (kMcCornerBitsY >> k) & 1; }
+__device__ __forceinline__ int corner_dz(int k) { return (kMcCornerBitsZ >> k) & 1; }
+
+// Edge vertex e of the cube whose corner 0 is staged at (x, y, z), global
+// voxel (gx, gy, gz): VertexInterp(p[a], p[b], val[a], val[b])
+// (src/tsdf.cu:1640-1660) in global voxel units; the colour truncates like
+// the reference's float-to-uchar store.
+__device__ __forceinline__ void edge_vertex(const McShared &S, int e, int x, int y, int z,
+                                            int gx, int gy, int gz, float &ox, float &oy,
+                                            float &oz, uint32_t &oc) {
+  const uint32_t code =
+      (uint32_t)((e < 8 ? kMcEdgeCodeLo >> (8 * e) : kMcEdgeCodeHi >> (8 * (e - 8))) & 0x3Fu);
+  const int a = (int)(code & 7u), b = (int)(code >> 3);
+  const int ax = corner_dx(a), ay = corner_dy(a), az = corner_dz(a);
+  const int bx = corner_dx(b), by = corner_dy(b), bz = corner_dz(b);
+  const int ia = hidx(x + ax, y + ay, z + az), ib = hidx(x + bx, y + by, z + bz);
+  const float v1 = S.sdf[ia], v2 = S.sdf[ib];
+  const uint32_t c1 = S.rgb[ia], c2 = S.rgb[ib];
+  const float p1x = (float)(gx + ax), p1y = (float)(gy + ay), p1z = (float)(gz + az);
+  const float p2x = (float)(gx + bx), p2y = (float)(gy + by), p2z = (float)(gz + bz);
+  if (fabsf(0.0f - v1) < kSnap) {
+    ox = p1x, oy = p1y, oz = p1z, oc = c1;
+    return;
+  }
+  if (fabsf(0.0f - v2) < kSnap) {
+    ox = p2x, oy = p2y, oz = p2z, oc = c2;
+    return;
+  }
+  if (fabsf(v1 - v2) < kSnap) {
+    ox = p1x, oy = p1y, oz = p1z, oc = c1;
+    return;
+  }
+  const float mu = (0.0f - v1) / (v2 - v1);
+  ox = p1x + mu * (p2x - p1x);
+  oy = p1y + mu * (p2y - p1y);
+  oz = p1z + mu * (p2z - p1z);
+  uint32_t out = 0;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const int q1 = (int)((c1 >> (8 * c)) & 0xFFu), q2 = (int)((c2 >> (8 * c)) & 0xFFu);
+    const float v = (float)q1 + mu * (float)(q2 - q1);
+    out |= (__float2uint_rz(v) & 0xFFu) << (8 * c);
+  }
+  oc = out;
+}
+
+// Cube case of the cube with staged corner 0 at (x, y, z); -1 if a corner is
+// unusable (src/tsdf.cu:930-986).
+__device__ __forceinline__ int cube_case(const McShared &S, int x, int y, int z) {
+  int ci = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const float v = S.sdf[hidx(x + corner_dx(k), y + corner_dy(k), z + corner_dz(k))];
+    if (v != v) return -1;
+    if (v < 0.0f) ci |= 1 << k;
+  }
+  return ci;
+}
+
+// Valid-triangle mask of a cube: the reference drops a triangle when
+// p0 == p1 || p1 == p2 (src/tsdf.cu:1055-1057).
+__device__ __forceinline__ uint32_t cube_mask(const McShared &S, int ci, int x, int y, int z,
+                                              int gx, int gy, int gz) {
+  uint32_t mask = 0;
+  for (int t = 0; t < 5; ++t) {
+    const int e0 = S.tri[ci][3 * t];
+    if (e0 < 0) break;
+    const int e1 = S.tri[ci][3 * t + 1], e2 = S.tri[ci][3 * t + 2];
+    float ax, ay, az, bx, by, bz, cx, cy, cz;
+    uint32_t cc;
+    edge_vertex(S, e0, x, y, z, gx, gy, gz, ax, ay, az, cc);
+    edge_vertex(S, e1, x, y, z, gx, gy, gz, bx, by, bz, cc);
+    edge_vertex(S, e2, x, y, z, gx, gy, gz, cx, cy, cz, cc);
+    const bool d01 = ax == bx && ay == by && az == bz;
+    const bool d12 = bx == cx && by == cy && bz == cz;
+    if (!(d01 || d12)) mask |= 1u << t;
+  }
+  return mask;
+}
+
+__global__ void __launch_bounds__(128) k_mc(VolumeView V, int scope_all, float min_weight,
+                                            float4 *__restrict__ tris, uint32_t tri_cap) {
+  __shared__ McShared S;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  for (int i = t; i < 256 * 16; i += 128) (&S.tri[0][0])[i] = kMcTri[i >> 4][i & 15];
+  for (int i = t; i < 256; i += 128) S.edge[i] = kMcEdgeMask[i];
+  const uint32_t n = scope_all ? V.st->pool_top : min(V.st->frame_count, V.frame_cap);
+  const float nanv = __int_as_float(0x7FC00000);
+  for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+    __syncthreads();  // previous iteration done with S
+    if (t == 0) {
+      unsigned long long key;
+      uint32_t b;
+      if (scope_all) {
+        key = V.block_keys[i];
+        b = key < kTombKey ? i : kNoBlock;
+      } else {
+        const Slot sl = V.slots[V.frame_list[i]];
+        key = sl.key;
+        b = key < kTombKey ? sl.block : kNoBlock;
+      }
+      int x = 0, y = 0, z = 0;
+      if (b != kNoBlock) unpack_key(key, x, y, z);
+      S.key[0] = x;
+      S.key[1] = y;
+      S.key[2] = z;
+      S.nb[0] = b;
+    }
+    __syncthreads();
+    if (S.nb[0] == kNoBlock) continue;
+    const int bx = S.key[0], by = S.key[1], bz = S.key[2];
+    if (t >= 1 && t < 8) {
+      const int nx = bx + (t & 1), ny = by + ((t >> 1) & 1), nz = bz + (t >> 2);
+      S.nb[t] = key_in_range(nx, ny, nz) ? block_of(V, pack_key(nx, ny, nz)) : kNoBlock;
+    }
+    // own block: 4 voxels per thread, 16-byte loads
+    {
+      const float *base = V.pool + (size_t)S.nb[0] * kBlockWords;
+      const float4 sd = reinterpret_cast<const float4 *>(base)[t];
+      const float4 wt = reinterpret_cast<const float4 *>(base + kB3)[t];
+      const uint4 cl = reinterpret_cast<const uint4 *>(base + 2 * kB3)[t];
+      const int li = 4 * t, x = li & 7, y = (li >> 3) & 7, z = li >> 6;
+      const int h = hidx(x, y, z);
+      S.sdf[h + 0] = wt.x >= min_weight ? sd.x : nanv;
+      S.sdf[h + 1] = wt.y >= min_weight ? sd.y : nanv;
+      S.sdf[h + 2] = wt.z >= min_weight ? sd.z : nanv;
+      S.sdf[h + 3] = wt.w >= min_weight ? sd.w : nanv;
+      S.rgb[h + 0] = cl.x;
+      S.rgb[h + 1] = cl.y;
+      S.rgb[h + 2] = cl.z;
+      S.rgb[h + 3] = cl.w;
+    }
+    __syncthreads();  // S.nb complete
+    // halo: x == 8 (81), then y == 8 with x < 8 (72), then z == 8 with x, y < 8 (64)
+    for (int hh = t; hh < kHalo; hh += 128) {
+      int x, y, z;
+      if (hh < 81) {
+        x = 8;
+        y = hh % 9;
+        z = hh / 9;
+      } else if (hh < 153) {
+        const int q = hh - 81;
+        x = q & 7;
+        y = 8;
+        z = q >> 3;
+      } else {
+        const int q = hh - 153;
+        x = q & 7;
+        y = q >> 3;
+        z = 8;
+      }
+      const int nbi = (x >> 3) | ((y >> 3) << 1) | ((z >> 3) << 2);
+      const uint32_t blk = S.nb[nbi];
+      float v = nanv;
+      uint32_t c = 0;
+      if (blk != kNoBlock) {
+        const float *base = V.pool + (size_t)blk * kBlockWords;
+        const int li = (x & 7) + 8 * (y & 7) + 64 * (z & 7);
+        const float wv = __ldg(base + kB3 + li);
+        v = wv >= min_weight ? __ldg(base + li) : nanv;
+        c = __ldg(reinterpret_cast<const uint32_t *>(base + 2 * kB3) + li);
+      }
+      S.sdf[hidx(x, y, z)] = v;
+      S.rgb[hidx(x, y, z)] = c;
+    }
+    __syncthreads();
+    // pass 1: cases and valid-triangle masks of this thread's 4 cubes
+    const int gx0 = bx * kB, gy0 = by * kB, gz0 = bz * kB;
+    uint32_t packed[4];
+    uint32_t count = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int c = t + 128 * j;
+      const int x = c & 7, y = (c >> 3) & 7, z = c >> 6;
+      packed[j] = 0;
+      const int ci = cube_case(S, x, y, z);
+      if (ci > 0 && S.edge[ci] != 0) {
+        const uint32_t m = cube_mask(S, ci, x, y, z, gx0 + x, gy0 + y, gz0 + z);
+        packed[j] = (uint32_t)ci | (m << 8);
+        count += __popc(m);
+      }
+    }
+    // CTA exclusive scan of the counts, one global atomic per block
+    uint32_t incl = count;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t v = __shfl_up_sync(kFull, incl, o);
+      if (lane >= o) incl += v;
+    }
+    if (lane == 31) S.warp_sum[warp] = incl;
+    __syncthreads();
+    if (t == 0) {
+      const uint32_t tot = S.warp_sum[0] + S.warp_sum[1] + S.warp_sum[2] + S.warp_sum[3];
+      S.base = tot ? atomicAdd(&V.st->tri_count, tot) : 0u;
+    }
+    __syncthreads();
+    uint32_t out = S.base + incl - count;
+    for (int q = 0; q < warp; ++q) out += S.warp_sum[q];
+    // pass 2: write the valid triangles
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint32_t pk = packed[j];
+      const uint32_t m = pk >> 8;
+      if (!m) continue;
+      const int ci = (int)(pk & 0xFFu);
+      const int c = t + 128 * j;
+      const int x = c & 7, y = (c >> 3) & 7, z = c >> 6;
+      for (int tt = 0; tt < 5; ++tt) {
+        if (!(m & (1u << tt))) continue;
+        if (out < tri_cap) {
+          float4 *dst = tris + 3 * (size_t)out;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            float vx, vy, vz;
+            uint32_t vc;
+            edge_vertex(S, S.tri[ci][3 * tt + k], x, y, z, gx0 + x, gy0 + y, gz0 + z, vx, vy, vz,
+                        vc);
+            dst[k] = make_float4(vx, vy, vz, __uint_as_float(vc));
+          }
+        } else {
+          atomicOr(&V.st->error, kErrTriCap);
+        }
+        ++out;
+      }
+    }
+  }
+}
+
+// ---- small state kernels --------------------------------------------------------
+__device__ void reconcile(const VolumeView &V) {
+  DevState *st = V.st;
+  const uint32_t t = st->ticket;
+  if (!t) return;
+  const uint32_t from_free = min(t, st->free_count);
+  st->free_count -= from_free;
+  const unsigned long long top = (unsigned long long)st->pool_top + (t - from_free);
+  const uint32_t new_top = (uint32_t)min(top, (unsigned long long)V.pool_cap);
+  st->new_blocks += from_free + (new_top - st->pool_top);
+  st->pool_top = new_top;
+  st->ticket = 0;
+}
+
+__global__ void k_frame_begin(VolumeView V) {
+  if (threadIdx.x != 0) return;
+  reconcile(V);
+  DevState *st = V.st;
+  uint32_t f = st->frame + 1u;
+  if (f == 0u || f == 0xFFFFFFFFu) f = 1u;  // 0xFFFFFFFF marks never-stamped slots
+  st->frame = f;
+  st->frame_count = 0;
+  st->new_blocks = 0;
+  st->voxels_updated = 0;
+}
+
+__global__ void k_epoch_end(VolumeView V) {
+  if (threadIdx.x == 0) reconcile(V);
+}
+
+__global__ void k_clear_list(VolumeView V) {
+  if (threadIdx.x != 0) return;
+  reconcile(V);
+  uint32_t f = V.st->frame + 1u;
+  if (f == 0u || f == 0xFFFFFFFFu) f = 1u;
+  V.st->frame = f;
+  V.st->frame_count = 0;
+}
+
+__global__ void k_mc_begin(VolumeView V) {
+  if (threadIdx.x == 0) {
+    reconcile(V);
+    V.st->tri_count = 0;
+  }
+}
+
+// ---- hash surface -----------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_alloc_keys(VolumeView V, const int32_t *__restrict__ xyz,
+                                                    uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t frame = V.st->frame;
+  const uint32_t free0 = V.st->free_count, top0 = V.st->pool_top;
+  bool active = false;
+  unsigned long long key = kEmptyKey;
+  if (i < n) {
+    const int x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+    if (key_in_range(x, y, z)) {
+      key = pack_key(x, y, z);
+      active = true;
+    } else {
+      atomicOr(&V.st->error, kErrRange);
+    }
+  }
+  const unsigned peers = __match_any_sync(kFull, key);
+  const bool leader = active && (__ffs(peers) - 1) == (int)(threadIdx.x & 31);
+  bool created = false;
+  uint32_t slot = kNoBlock;
+  if (leader) slot = slot_insert(V, key, &created);
+  assign_blocks(V, created, slot, key, free0, top0);
+  stamp_and_append(V, leader, slot, frame);
+}
+
+__global__ void __launch_bounds__(256) k_find_keys(VolumeView V, const int32_t *__restrict__ xyz,
+                                                   uint32_t n, int32_t *__restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+  uint32_t b = kNoBlock;
+  if (key_in_range(x, y, z)) b = block_of(V, pack_key(x, y, z));
+  out[i] = b == kNoBlock ? -1 : (int32_t)b;
+}
+
+// Erases keys: the slot becomes a tombstone, the block is zeroed and pushed
+// onto the free list (no allocation runs concurrently with this kernel).
+__global__ void __launch_bounds__(256) k_erase_keys(VolumeView V, const int32_t *__restrict__ xyz,
+                                                    uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+  if (!key_in_range(x, y, z)) return;
+  const unsigned long long key = pack_key(x, y, z);
+  const uint32_t h = (uint32_t)mix64(key) & V.slot_mask;
+  for (int p = 0; p < V.max_probe; ++p) {
+    const uint32_t s = (h + (uint32_t)p) & V.slot_mask;
+    const unsigned long long k = ld_volatile(&V.slots[s].key);
+    if (k == kEmptyKey) return;
+    if (k != key) continue;
+    if (atomicCAS(&V.slots[s].key, key, kTombKey) != key) return;  // erased by a duplicate
+    const uint32_t b = V.slots[s].block;
+    V.slots[s].block = kNoBlock;
+    atomicAdd(&V.st->tombstones, 1u);
+    atomicAdd(&V.st->erased, 1u);
+    if (b != kNoBlock) {
+      float4 *blk = reinterpret_cast<float4 *>(V.pool + (size_t)b * kBlockWords);
+      for (int q = 0; q < kBlockWords / 4; ++q) blk[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+      V.block_keys[b] = kEmptyKey;
+      __threadfence();
+      const uint32_t f = atomicAdd(&V.st->free_count, 1u);
+      V.free_list[f] = b;
+    }
+    return;
+  }
+}
+
+__global__ void k_list_keys(VolumeView V, int32_t *__restrict__ xyz, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const unsigned long long key = V.slots[V.frame_list[i]].key;
+  int x = 0, y = 0, z = 0;
+  if (key < kTombKey) unpack_key(key, x, y, z);
+  xyz[3 * i] = x;
+  xyz[3 * i + 1] = y;
+  xyz[3 * i + 2] = z;
+}
+
+// Overwrites the voxels of already inserted blocks; one CTA per block.
+__global__ void __launch_bounds__(128) k_scatter_blocks(VolumeView V, const int32_t *__restrict__ xyz,
+                                                        const float *__restrict__ sdf,
+                                                        const float *__restrict__ w,
+                                                        const uint8_t *__restrict__ rgb,
+                                                        uint32_t n) {
+  const uint32_t i = blockIdx.x;
+  if (i >= n) return;
+  const int x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+  if (!key_in_range(x, y, z)) return;
+  const uint32_t b = block_of(V, pack_key(x, y, z));
+  if (b == kNoBlock) return;
+  float *base = V.pool + (size_t)b * kBlockWords;
+  for (int v = threadIdx.x; v < kB3; v += blockDim.x) {
+    const size_t src = (size_t)i * kB3 + v;
+    base[v] = sdf[src];
+    base[kB3 + v] = w[src];
+    const uint32_t c = (uint32_t)rgb[3 * src] | ((uint32_t)rgb[3 * src + 1] << 8) |
+                       ((uint32_t)rgb[3 * src + 2] << 16);
+    reinterpret_cast<uint32_t *>(base + 2 * kB3)[v] = c;
+  }
+}
+
+inline unsigned grid_for(uint32_t n, unsigned threads) { return (n + threads - 1) / threads; }
+
+}  // namespace
+
+void launch_frame_begin(const VolumeView &V, cudaStream_t s) { k_frame_begin<<<1, 32, 0, s>>>(V); }
+void launch_epoch_end(const VolumeView &V, cudaStream_t s) { k_epoch_end<<<1, 32, 0, s>>>(V); }
+void launch_clear_list(const VolumeView &V, cudaStream_t s) { k_clear_list<<<1, 32, 0, s>>>(V); }
+void launch_mc_begin(const VolumeView &V, cudaStream_t s) { k_mc_begin<<<1, 32, 0, s>>>(V); }
+
+void launch_allocate(const VolumeView &V, const CamParams &C, const void *depth, int fmt,
+                     const uint8_t *rgb, const float *pose, uint2 *pix, cudaStream_t s) {
+  const unsigned grid = grid_for((uint32_t)C.width * (uint32_t)C.height, 256);
+  if (fmt == 0)
+    k_allocate<uint16_t><<<grid, 256, 0, s>>>(V, C, (const uint16_t *)depth, rgb, pose, pix);
+  else
+    k_allocate<float><<<grid, 256, 0, s>>>(V, C, (const float *)depth, rgb, pose, pix);
+}
+
+void launch_integrate(const VolumeView &V, const CamParams &C, const uint2 *pix, const float *pose,
+                      int grid, cudaStream_t s) {
+  k_integrate<<<grid, 128, 0, s>>>(V, C, pix, pose);
+}
+
+void launch_mc(const VolumeView &V, int scope_all, float min_weight, float4 *tris,
+               uint32_t tri_cap, int grid, cudaStream_t s) {
+  k_mc<<<grid, 128, 0, s>>>(V, scope_all, min_weight, tris, tri_cap);
+}
+
+void launch_alloc_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, cudaStream_t s) {
+  if (n) k_alloc_keys<<<grid_for(n, 256), 256, 0, s>>>(V, xyz, n);
+}
+void launch_find_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, int32_t *out,
+                      cudaStream_t s) {
+  if (n) k_find_keys<<<grid_for(n, 256), 256, 0, s>>>(V, xyz, n, out);
+}
+void launch_erase_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, cudaStream_t s) {
+  if (n) k_erase_keys<<<grid_for(n, 256), 256, 0, s>>>(V, xyz, n);
+}
+void launch_list_keys(const VolumeView &V, int32_t *xyz, uint32_t n, cudaStream_t s) {
+  if (n) k_list_keys<<<grid_for(n, 256), 256, 0, s>>>(V, xyz, n);
+}
+void launch_scatter_blocks(const VolumeView &V, const int32_t *xyz, const float *sdf,
+                           const float *w, const uint8_t *rgb, uint32_t n, cudaStream_t s) {
+  if (n) k_scatter_blocks<<<n, 128, 0, s>>>(V, xyz, sdf, w, rgb, n);
+}
+
+}  // namespace vh

@@ -1,0 +1,209 @@
+"""Pythonic handle over the C ABI: one TSDF volume on one GPU.
+
+Arrays may be numpy (host memory) or CUDA torch tensors (device memory of the
+volume's GPU); the call passes raw pointers and the memory kind to the
+library.  Nothing here computes anything itself.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+
+
+def _is_cuda_tensor(a):
+    return type(a).__module__.startswith("torch") and getattr(a, "is_cuda", False)
+
+
+class _Arg:
+    """Pointer + memory kind of an input array, keeping host copies alive."""
+
+    def __init__(self, a, dtype=None):
+        if _is_cuda_tensor(a):
+            if not a.is_contiguous():
+                raise ValueError("device tensors must be contiguous")
+            self.keep = a
+            self.ptr = a.data_ptr()
+            self.mem = N.VH_MEM_DEVICE
+            self.dtype = str(a.dtype).replace("torch.", "")
+        else:
+            arr = np.ascontiguousarray(a if dtype is None else np.asarray(a, dtype=dtype))
+            self.keep = arr
+            self.ptr = arr.ctypes.data
+            self.mem = N.VH_MEM_HOST
+            self.dtype = str(arr.dtype)
+
+
+def _depth_fmt(dtype, override=None):
+    """uint16 -> scaled integer depth, float32 -> metres.  `override` ("u16" or
+    "f32") reinterprets the bytes, e.g. an int16 device tensor holding uint16."""
+    if override == "u16" or (override is None and dtype == "uint16"):
+        return N.VH_DEPTH_U16_MM
+    if override == "f32" or (override is None and dtype == "float32"):
+        return N.VH_DEPTH_F32_M
+    raise TypeError(f"depth must be uint16 (scaled) or float32 metres, got {dtype}")
+
+
+class Volume:
+    """A voxel-hashed TSDF volume (8^3 blocks) resident on one GPU."""
+
+    def __init__(self, **params):
+        self._L = N.lib()
+        p = N.VhParams()
+        self._L.vh_params_default(C.byref(p))
+        for k, v in params.items():
+            if not hasattr(p, k):
+                raise TypeError(f"unknown parameter {k}")
+            setattr(p, k, v)
+        self.params = p
+        h = C.c_void_p()
+        N.check(self._L.vh_create(C.byref(p), C.byref(h)))
+        self._h = h
+
+    # ---- life cycle ----
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.vh_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, status):
+        N.check(status, self._h)
+
+    def reset(self):
+        self._check(self._L.vh_reset(self._h))
+
+    def sync(self):
+        self._check(self._L.vh_sync(self._h))
+
+    def set_stream(self, stream_ptr):
+        self._check(self._L.vh_set_stream(self._h, C.c_void_p(stream_ptr)))
+
+    # ---- per-frame path ----
+    def _frame_args(self, depth, rgb, c2w):
+        d = _Arg(depth)
+        c = _Arg(rgb, np.uint8)
+        if d.mem != c.mem:
+            raise ValueError("depth and rgb must both be host or both be device arrays")
+        pose = np.ascontiguousarray(np.asarray(c2w, dtype=np.float32).reshape(16))
+        return d, c, pose
+
+    def integrate(self, depth, rgb, c2w, depth_format=None):
+        d, c, pose = self._frame_args(depth, rgb, c2w)
+        self._check(self._L.vh_integrate(self._h, d.ptr, _depth_fmt(d.dtype, depth_format), c.ptr,
+                                         pose.ctypes.data, d.mem))
+
+    def process_frame(self, depth, rgb, c2w, depth_format=None):
+        d, c, pose = self._frame_args(depth, rgb, c2w)
+        self._check(self._L.vh_process_frame(self._h, d.ptr, _depth_fmt(d.dtype, depth_format),
+                                             c.ptr, pose.ctypes.data, d.mem, None))
+
+    def extract(self, scope="frame"):
+        """Runs marching cubes; returns (device pointer, triangle count)."""
+        view = N.VhMeshView()
+        sc = N.VH_SCOPE_ALL if scope == "all" else N.VH_SCOPE_FRAME
+        self._check(self._L.vh_extract(self._h, sc, C.byref(view)))
+        return view.vertices, view.num_triangles
+
+    def mesh(self):
+        """Last extraction as (xyz float32 [n,3,3] voxel units, rgb uint8 [n,3,3])."""
+        n = C.c_int64()
+        self._check(self._L.vh_copy_mesh(self._h, None, None, 0, C.byref(n)))
+        xyz = np.empty((n.value, 3, 3), np.float32)
+        rgb = np.empty((n.value, 3, 3), np.uint8)
+        self._check(self._L.vh_copy_mesh(self._h, xyz.ctypes.data, rgb.ctypes.data, n.value,
+                                         C.byref(n)))
+        return xyz, rgb
+
+    def save_ply(self, path, binary=False):
+        self._check(self._L.vh_save_ply(self._h, str(path).encode(), int(binary)))
+
+    def render(self):
+        self._check(self._L.vh_render(self._h))
+
+    # ---- hash surface ----
+    @staticmethod
+    def _keys(keys):
+        if _is_cuda_tensor(keys):
+            return _Arg(keys), keys.numel() // 3
+        k = np.ascontiguousarray(np.asarray(keys, dtype=np.int32).reshape(-1, 3))
+        return _Arg(k), k.shape[0]
+
+    def alloc_keys(self, keys):
+        a, n = self._keys(keys)
+        self._check(self._L.vh_alloc_keys(self._h, a.ptr, n, a.mem))
+
+    def find_keys(self, keys):
+        a, n = self._keys(keys)
+        if a.mem == N.VH_MEM_DEVICE:
+            import torch
+            out = torch.empty(n, dtype=torch.int32, device=keys.device)
+            self._check(self._L.vh_find_keys(self._h, a.ptr, n, out.data_ptr(), a.mem))
+            return out
+        out = np.empty(n, np.int32)
+        self._check(self._L.vh_find_keys(self._h, a.ptr, n, out.ctypes.data, a.mem))
+        return out
+
+    def erase_keys(self, keys):
+        a, n = self._keys(keys)
+        cnt = C.c_int64()
+        self._check(self._L.vh_erase_keys(self._h, a.ptr, n, C.byref(cnt), a.mem))
+        return cnt.value
+
+    def clear_block_list(self):
+        self._check(self._L.vh_clear_block_list(self._h))
+
+    def block_list(self):
+        n = C.c_int64()
+        self._check(self._L.vh_block_list(self._h, None, 0, C.byref(n)))
+        out = np.empty((n.value, 3), np.int32)
+        self._check(self._L.vh_block_list(self._h, out.ctypes.data, n.value, C.byref(n)))
+        return out
+
+    # ---- volume I/O ----
+    def export_blocks(self):
+        n = C.c_int64()
+        self._check(self._L.vh_export_blocks(self._h, None, None, None, None, 0, C.byref(n)))
+        m = n.value
+        xyz = np.empty((m, 3), np.int32)
+        sdf = np.empty((m, N.BLOCK_VOXELS), np.float32)
+        w = np.empty((m, N.BLOCK_VOXELS), np.float32)
+        rgb = np.empty((m, N.BLOCK_VOXELS, 3), np.uint8)
+        self._check(self._L.vh_export_blocks(self._h, xyz.ctypes.data, sdf.ctypes.data,
+                                             w.ctypes.data, rgb.ctypes.data, m, C.byref(n)))
+        return {"xyz": xyz, "sdf": sdf, "weight": w, "rgb": rgb}
+
+    def import_blocks(self, xyz, sdf, weight, rgb):
+        xyz = np.ascontiguousarray(xyz, np.int32)
+        sdf = np.ascontiguousarray(sdf, np.float32)
+        weight = np.ascontiguousarray(weight, np.float32)
+        rgb = np.ascontiguousarray(rgb, np.uint8)
+        self._check(self._L.vh_import_blocks(self._h, xyz.ctypes.data, sdf.ctypes.data,
+                                             weight.ctypes.data, rgb.ctypes.data, xyz.shape[0]))
+
+    def save(self, path):
+        self._check(self._L.vh_save(self._h, str(path).encode()))
+
+    def load(self, path):
+        self._check(self._L.vh_load(self._h, str(path).encode()))
+
+    def stats(self):
+        s = N.VhStats()
+        self._check(self._L.vh_get_stats(self._h, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in N.VhStats._fields_ if f != "reserved"}
+
+
+def block_hash_ref(x, y, z):
+    """The reference's BlockHasher value (include/tsdf.cuh:144-156)."""
+    return int(N.lib().vh_block_hash_ref(int(x), int(y), int(z)))
