@@ -166,7 +166,11 @@ vh_status vh_process_frame(vh_handle *h, const void *depth, int32_t depth_fmt,
                            const uint8_t *rgb, const float *c2w, int32_t mem,
                            vh_mesh_view *out);
 /* Copies the last extraction to host: xyz (9 floats per triangle, voxel
- * units) and rgb (9 bytes per triangle); either may be NULL. */
+ * units) and rgb (9 bytes per triangle).  Output copies and size queries
+ * (all outputs NULL) follow one rule for every copy-out call here: the full
+ * count is returned in the count argument, at most `capacity` items are
+ * written, and VH_ERR_CAPACITY is returned only when outputs were given and
+ * the capacity was too small. */
 vh_status vh_copy_mesh(vh_handle *h, float *xyz, uint8_t *rgb,
                        int64_t capacity, int64_t *num_triangles);
 /* Full-volume extraction written as PLY with vertices merged by exact

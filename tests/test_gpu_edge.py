@@ -1,0 +1,116 @@
+"""Edge cases of the per-frame path: empty input, bad poses, capacity limits."""
+import numpy as np
+import pytest
+
+from helpers import oracle_for, small_scene, sort_rows, tri_rows, volume_for
+from vhsdf import VhError, _native as N
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def scene(gpu):
+    return small_scene()
+
+
+def test_empty_depth_changes_nothing(scene):
+    vol = volume_for(scene)
+    for f in range(3):
+        vol.integrate(*scene.render(f))
+    before = vol.export_blocks()
+    d, c, p = scene.render(5)
+    vol.process_frame(np.zeros_like(d), c, p)
+    st = vol.stats()
+    assert st["frame_blocks"] == 0 and st["voxels_updated"] == 0 and st["triangles"] == 0
+    after = vol.export_blocks()
+    for k in before:
+        assert np.array_equal(before[k], after[k])
+
+
+def test_non_finite_pose_is_rejected(scene):
+    vol = volume_for(scene)
+    d, c, p = scene.render(0)
+    bad = p.copy()
+    bad[0, 3] = np.nan
+    with pytest.raises(VhError) as e:
+        vol.integrate(d, c, bad)
+    assert e.value.status == N.VH_ERR_NOT_FINITE
+    vol.integrate(d, c, p)  # still usable
+    assert vol.stats()["frames"] == 1
+
+
+def test_far_away_pose_reports_out_of_range(scene):
+    vol = volume_for(scene)
+    d, c, p = scene.render(0)
+    far = p.copy()
+    far[0, 3] = 1.0e6  # 1000 km: beyond the 2^20-block key range at 2 cm voxels
+    with pytest.raises(VhError) as e:
+        vol.integrate(d, c, far)
+    assert e.value.status == N.VH_ERR_OUT_OF_RANGE
+    assert vol.stats()["frame_blocks"] == 0
+
+
+def test_frame_list_capacity(scene):
+    vol = volume_for(scene, max_frame_blocks=16)
+    with pytest.raises(VhError) as e:
+        vol.integrate(*scene.render(0))
+    assert e.value.status == N.VH_ERR_CAPACITY
+
+
+def test_triangle_capacity_per_frame_and_growth(scene):
+    vol = volume_for(scene, max_triangles=10)
+    orc = oracle_for(vol)
+    d, c, p = scene.render(0)
+    orc.integrate(d, c, p)
+    with pytest.raises(VhError) as e:
+        vol.process_frame(d, c, p)
+    assert e.value.status == N.VH_ERR_CAPACITY
+    # full-volume extraction grows the buffer and matches the oracle
+    vol.extract("all")
+    gx, gc = vol.mesh()
+    m = orc.marching_cubes("all")
+    assert len(gx) == len(m["xyz"]) > 10
+    assert np.array_equal(sort_rows(tri_rows(gx, gc)), sort_rows(tri_rows(m["xyz"], m["rgb"])))
+    # and per-frame extraction now fits too
+    vol.process_frame(d, c, p)
+
+
+def test_bad_arguments(scene):
+    vol = volume_for(scene)
+    d, c, p = scene.render(0)
+    with pytest.raises(TypeError):
+        vol.integrate(d.astype(np.int32), c, p)
+    L = N.lib()
+    assert L.vh_integrate(vol._h, None, 0, None, None, 0) == N.VH_ERR_INVALID_ARG
+    assert L.vh_extract(vol._h, 7, None) == N.VH_ERR_INVALID_ARG
+    with pytest.raises(VhError) as e:
+        vol.render()
+    assert e.value.status == N.VH_ERR_UNSUPPORTED
+
+
+def test_reset_clears_volume(scene):
+    vol = volume_for(scene)
+    vol.integrate(*scene.render(0))
+    assert vol.stats()["blocks_allocated"] > 0
+    vol.reset()
+    st = vol.stats()
+    assert st["blocks_allocated"] == 0 and st["frames"] == 0
+    assert len(vol.export_blocks()["xyz"]) == 0
+    vol.integrate(*scene.render(0))
+    orc = oracle_for(vol)
+    orc.integrate(*scene.render(0))
+    assert vol.stats()["blocks_allocated"] == orc.num_blocks()
+
+
+def test_external_stream(scene):
+    import torch
+    vol = volume_for(scene, flags=0)  # asynchronous
+    s = torch.cuda.Stream()
+    vol.set_stream(s.cuda_stream)
+    for f in range(4):
+        vol.process_frame(*scene.render(f))
+    vol.sync()
+    orc = oracle_for(vol)
+    for f in range(4):
+        orc.integrate(*scene.render(f))
+    assert vol.stats()["blocks_allocated"] == orc.num_blocks()

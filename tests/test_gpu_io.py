@@ -1,0 +1,104 @@
+"""Volume snapshots, PLY export and the reference-named front ends."""
+import numpy as np
+import pytest
+
+from helpers import assert_same_blocks, oracle_for, small_scene, volume_for
+from vhsdf import GpuTsdfGenerator, HashTable, VhError
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def scene(gpu):
+    return small_scene()
+
+
+def test_snapshot_round_trip(scene, tmp_path):
+    vol = volume_for(scene)
+    for f in range(4):
+        vol.integrate(*scene.render(f))
+    path = tmp_path / "vol.vhs"
+    vol.save(path)
+    other = volume_for(scene)
+    other.load(path)
+    assert_same_blocks(other.export_blocks(), vol.export_blocks())
+    # integration continues identically after a reload
+    vol.integrate(*scene.render(4))
+    other.integrate(*scene.render(4))
+    assert_same_blocks(other.export_blocks(), vol.export_blocks())
+
+
+def read_ply(path):
+    with open(path, "rb") as f:
+        header = []
+        while True:
+            line = f.readline().decode().strip()
+            header.append(line)
+            if line == "end_header":
+                break
+        nv = int([h for h in header if h.startswith("element vertex")][0].split()[-1])
+        nf = int([h for h in header if h.startswith("element face")][0].split()[-1])
+        binary = any("binary_little_endian" in h for h in header)
+        if binary:
+            vdt = np.dtype([("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("r", "u1"), ("g", "u1"),
+                            ("b", "u1")])
+            v = np.frombuffer(f.read(nv * vdt.itemsize), vdt)
+            fdt = np.dtype([("n", "u1"), ("i", "<i4", 3)])
+            fc = np.frombuffer(f.read(nf * fdt.itemsize), fdt)
+            return np.stack([v["x"], v["y"], v["z"]], -1), fc["i"], fc["n"]
+        rows = [f.readline().split() for _ in range(nv)]
+        v = np.array([[float(r[0]), float(r[1]), float(r[2])] for r in rows])
+        fr = [f.readline().split() for _ in range(nf)]
+        return v, np.array([[int(r[1]), int(r[2]), int(r[3])] for r in fr]), \
+            np.array([int(r[0]) for r in fr])
+
+
+@pytest.mark.parametrize("binary", [False, True])
+def test_ply_export(scene, tmp_path, binary):
+    vol = volume_for(scene)
+    for f in range(3):
+        vol.integrate(*scene.render(f))
+    path = tmp_path / "mesh.ply"
+    vol.save_ply(path, binary=binary)
+    v, faces, nper = read_ply(path)
+    vol.extract("all")
+    xyz, _ = vol.mesh()
+    assert len(faces) == len(xyz) and np.all(nper == 3)
+    uniq = np.unique(xyz.reshape(-1, 3), axis=0)
+    assert len(v) == len(uniq)
+    assert faces.min() >= 0 and faces.max() < len(v)
+    vs = vol.params.voxel_size
+    got = np.sort(v[faces].reshape(-1, 3), axis=0)
+    want = np.sort((xyz * np.float32(vs)).reshape(-1, 3).astype(np.float64), axis=0)
+    assert np.allclose(got, want, atol=1e-5 if not binary else 0)
+
+
+def test_gpu_tsdf_generator_front_end(scene, tmp_path):
+    """ark::GpuTsdfGenerator surface: float metre depth, RGB, row-major c2w."""
+    gen = GpuTsdfGenerator(scene.width, scene.height, scene.fx, scene.fy, scene.cx, scene.cy,
+                           4.5, vox_size=0.02, trunc_m=0.08, table_log2=18,
+                           pool_blocks=1 << 16, max_frame_blocks=1 << 16)
+    orc = oracle_for(gen.volume, 32)
+    for f in range(3):
+        d, c, p = scene.render(f)
+        dm = d.astype(np.float32) * np.float32(0.001)
+        gen.processFrame(dm, c, p.reshape(-1))
+        orc.integrate(dm, c, p)
+    assert_same_blocks(gen.volume.export_blocks(), orc.export())
+    gen.SavePLY(str(tmp_path / "g.ply"))
+    verts, cols = gen.getVertices()
+    faces = gen.getFaces()
+    assert verts.shape[1] == 3 and cols.shape == verts.shape and faces.max() < len(verts)
+    mc = gen.getMarchingCubeParam()
+    assert abs(mc["block_size"] - 0.16) < 1e-7
+    with pytest.raises(VhError):
+        gen.render()
+    table = gen.getHashMap()
+    assert isinstance(table, HashTable)
+    keys = gen.volume.export_blocks()["xyz"][:5]
+    assert np.all(table.find(keys) >= 0)
+    table.clearheap()
+    assert table.heap_counter == 0
+    table.AllocKeys(np.array([[500, 500, 500]], np.int32))
+    assert table.heap_counter == 1 and table.erase(np.array([[500, 500, 500]], np.int32)) == 1
+    gen.Shutdown()

@@ -147,20 +147,29 @@ vh_status sync_and_check(vh_handle *h) {
 int integrate_grid(const vh_handle *h) { return h->sm_count * 8; }
 int mc_grid(const vh_handle *h) { return h->sm_count * 6; }
 
+// Records a stage event; inside a stream capture it must become a real
+// event-record node of the graph (cudaEventRecordExternal).
+void stage_event(cudaEvent_t ev, cudaStream_t s, bool capturing) {
+  if (capturing)
+    cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal);
+  else
+    cudaEventRecord(ev, s);
+}
+
 // Enqueues one frame's kernels (optionally with per-stage events).
-void enqueue_frame(vh_handle *h, int fmt, bool with_mc, bool events) {
+void enqueue_frame(vh_handle *h, int fmt, bool with_mc, bool events, bool capturing) {
   cudaStream_t s = h->stream;
-  if (events) cudaEventRecord(h->ev[0], s);
+  if (events) stage_event(h->ev[0], s, capturing);
   launch_frame_begin(h->V, s);
   launch_allocate(h->V, h->C, h->d_depth, fmt, h->d_rgb, h->d_pose, h->d_pix, s);
   launch_epoch_end(h->V, s);
-  if (events) cudaEventRecord(h->ev[1], s);
+  if (events) stage_event(h->ev[1], s, capturing);
   launch_integrate(h->V, h->C, h->d_pix, h->d_pose, integrate_grid(h), s);
-  if (events) cudaEventRecord(h->ev[2], s);
+  if (events) stage_event(h->ev[2], s, capturing);
   if (with_mc) {
     launch_mc_begin(h->V, s);
     launch_mc(h->V, 0, h->C.mc_min_weight, h->d_tris, (uint32_t)h->tri_cap, mc_grid(h), s);
-    if (events) cudaEventRecord(h->ev[3], s);
+    if (events) stage_event(h->ev[3], s, capturing);
   }
 }
 
@@ -182,7 +191,7 @@ vh_status run_frame(vh_handle *h, int fmt, bool with_mc) {
     if (!g) {
       cudaGraph_t graph = nullptr;
       VH_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-      enqueue_frame(h, fmt, with_mc, events);
+      enqueue_frame(h, fmt, with_mc, events, true);
       cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
       if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
       e = cudaGraphInstantiate(&g, graph, 0);
@@ -194,7 +203,7 @@ vh_status run_frame(vh_handle *h, int fmt, bool with_mc) {
     }
     VH_CUDA(h, cudaGraphLaunch(g, h->stream));
   } else {
-    enqueue_frame(h, fmt, with_mc, events);
+    enqueue_frame(h, fmt, with_mc, events, false);
     VH_CUDA(h, cudaGetLastError());
   }
   h->ev_pending = events;
@@ -564,7 +573,8 @@ vh_status vh_copy_mesh(vh_handle *h, float *xyz, uint8_t *rgb, int64_t capacity,
       }
     }
   }
-  return m < n ? fail(h, VH_ERR_CAPACITY, "mesh larger than the output capacity") : VH_OK;
+  if (m < n && (xyz || rgb)) return fail(h, VH_ERR_CAPACITY, "mesh larger than the output capacity");
+  return VH_OK;
 }
 
 vh_status vh_save_ply(vh_handle *h, const char *path, int32_t binary) {
@@ -657,7 +667,8 @@ vh_status vh_block_list(vh_handle *h, int32_t *xyz, int64_t capacity, int64_t *n
     VH_CUDA(h, cudaMemcpyAsync(xyz, tmp.ptr, sizeof(int32_t) * 3 * m, cudaMemcpyDeviceToHost, h->stream));
     VH_CUDA(h, cudaStreamSynchronize(h->stream));
   }
-  return m < cnt ? fail(h, VH_ERR_CAPACITY, "block list larger than the output capacity") : VH_OK;
+  if (m < cnt && xyz) return fail(h, VH_ERR_CAPACITY, "block list larger than the output capacity");
+  return VH_OK;
 }
 
 uint64_t vh_block_hash_ref(int32_t x, int32_t y, int32_t z) { return ref_block_hash(x, y, z); }
@@ -712,7 +723,9 @@ vh_status vh_export_blocks(vh_handle *h, int32_t *xyz, float *sdf, float *weight
       ++o;
     }
   }
-  return o < live ? fail(h, VH_ERR_CAPACITY, "volume larger than the output capacity") : VH_OK;
+  if (o < live && (xyz || want_data))
+    return fail(h, VH_ERR_CAPACITY, "volume larger than the output capacity");
+  return VH_OK;
 }
 
 vh_status vh_import_blocks(vh_handle *h, const int32_t *xyz, const float *sdf, const float *weight,
