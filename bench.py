@@ -194,6 +194,8 @@ def run_engine(args):
     scene, frames = make_frames(nframes, seed)
     params = dict(ENGINE_PARAMS, fx=scene.fx, fy=scene.fy, cx=scene.cx, cy=scene.cy,
                   flags=N.VH_FLAG_PROFILE, device=local)
+    if args.pool_blocks:
+        params["pool_blocks"] = args.pool_blocks
 
     stream = torch.cuda.Stream()
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.int32, device="cuda")
@@ -318,6 +320,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--pool-blocks", type=int, default=0,
+                    help="smaller block pool (for short profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
     if args.impl == "reference":

@@ -177,3 +177,32 @@ def test_invalid_depth_values_are_skipped_like_the_oracle(scene):
     vol.integrate(df, c, p)
     orc.integrate(df, c, p)
     assert_same_blocks(vol.export_blocks(), orc.export())
+
+
+def test_frame_scope_mc_after_list_change_without_integration(scene):
+    """Import / alloc_keys change the block list without integrating; the
+    per-frame extraction must then rebuild its neighbour table."""
+    vol = volume_for(scene)
+    orc = oracle_for(vol, 32)
+    for f in range(4):
+        orc.integrate(*scene.render(f))
+    o = orc.export()
+    vol.import_blocks(o["xyz"], o["sdf"], o["weight"], o["rgb"])  # list = imported keys
+    lst = vol.block_list()
+    orc.set_frame(lst)
+    vol.extract("frame")
+    gx, gc = vol.mesh()
+    m = orc.marching_cubes("frame")
+    assert len(gx) == len(m["xyz"]) > 100
+    assert np.array_equal(sort_rows(tri_rows(gx, gc)), sort_rows(tri_rows(m["xyz"], m["rgb"])))
+    # erase half the listed blocks: their cubes and neighbours disappear
+    vol.erase_keys(lst[::2])
+    keep = lst[1::2]
+    orc2 = oracle_for(vol, 32)
+    e = vol.export_blocks()
+    orc2.import_blocks(e["xyz"], e["sdf"], e["weight"], e["rgb"])
+    orc2.set_frame(keep)
+    vol.extract("frame")
+    gx, gc = vol.mesh()
+    m = orc2.marching_cubes("frame")
+    assert np.array_equal(sort_rows(tri_rows(gx, gc)), sort_rows(tri_rows(m["xyz"], m["rgb"])))

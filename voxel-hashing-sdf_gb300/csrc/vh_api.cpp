@@ -30,6 +30,8 @@ constexpr int kNumEvents = 5;
 struct vh_handle {
   vh_params p{};
   int sm_count = 0;
+  int integrate_per_sm = 1;
+  int mc_per_sm = 1;
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
   VolumeView V{};
@@ -49,6 +51,7 @@ struct vh_handle {
   bool ev_pending = false;
   bool ev_has_mc = false;
   int64_t frames = 0;
+  bool nb_valid = false;  // frame_nb matches the current block list
   std::string last_error;
   vh_stats stage{};
 };
@@ -144,8 +147,9 @@ vh_status sync_and_check(vh_handle *h) {
   return fail(h, st, msg);
 }
 
-int integrate_grid(const vh_handle *h) { return h->sm_count * 8; }
-int mc_grid(const vh_handle *h) { return h->sm_count * 6; }
+// Persistent grids: exactly the CTAs that are resident at once (no tail wave).
+int integrate_grid(const vh_handle *h) { return h->sm_count * h->integrate_per_sm; }
+int mc_grid(const vh_handle *h) { return h->sm_count * h->mc_per_sm; }
 
 // Records a stage event; inside a stream capture it must become a real
 // event-record node of the graph (cudaEventRecordExternal).
@@ -243,6 +247,7 @@ void free_all(vh_handle *h) {
   cudaFree(h->V.block_keys);
   cudaFree(h->V.free_list);
   cudaFree(h->V.frame_list);
+  cudaFree(h->V.frame_nb);
   cudaFree(h->V.st);
   cudaFree(h->d_depth);
   cudaFree(h->d_rgb);
@@ -274,6 +279,7 @@ vh_status clear_volume(vh_handle *h, bool zero_pool_prefix) {
   VH_CUDA(h, cudaMemsetAsync(h->V.st, 0, sizeof(DevState), s));
   VH_CUDA(h, cudaStreamSynchronize(s));
   h->frames = 0;
+  h->nb_valid = false;
   return VH_OK;
 }
 
@@ -408,6 +414,8 @@ vh_status vh_create(const vh_params *p, vh_handle **out) {
   if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess)
     return bail(VH_ERR_CUDA);
   h->stream = h->own_stream;
+  h->integrate_per_sm = integrate_ctas_per_sm();
+  h->mc_per_sm = mc_ctas_per_sm();
   const size_t slots = (size_t)1 << p->table_log2;
   const size_t npx = (size_t)p->width * p->height;
   h->tri_cap = p->max_triangles;
@@ -416,6 +424,7 @@ vh_status vh_create(const vh_params *p, vh_handle **out) {
             cudaMalloc(&h->V.block_keys, sizeof(unsigned long long) * p->pool_blocks) == cudaSuccess &&
             cudaMalloc(&h->V.free_list, sizeof(uint32_t) * p->pool_blocks) == cudaSuccess &&
             cudaMalloc(&h->V.frame_list, sizeof(uint32_t) * p->max_frame_blocks) == cudaSuccess &&
+            cudaMalloc(&h->V.frame_nb, 8 * sizeof(uint32_t) * p->max_frame_blocks) == cudaSuccess &&
             cudaMalloc(&h->V.st, sizeof(DevState)) == cudaSuccess &&
             cudaMalloc(&h->d_depth, 4 * npx) == cudaSuccess &&
             cudaMalloc(&h->d_rgb, 3 * npx) == cudaSuccess &&
@@ -493,6 +502,7 @@ vh_status vh_integrate(vh_handle *h, const void *depth, int32_t depth_fmt, const
   s = run_frame(h, depth_fmt, false);
   if (s != VH_OK) return s;
   h->frames++;
+  h->nb_valid = true;
   return (h->p.flags & VH_FLAG_SYNC) ? sync_and_check(h) : VH_OK;
 }
 
@@ -500,6 +510,10 @@ vh_status vh_extract(vh_handle *h, int32_t scope, vh_mesh_view *out) {
   if (!h) return VH_ERR_INVALID_ARG;
   if (scope != VH_SCOPE_FRAME && scope != VH_SCOPE_ALL)
     return fail(h, VH_ERR_INVALID_ARG, "unknown extraction scope");
+  if (scope == VH_SCOPE_FRAME && !h->nb_valid) {
+    launch_frame_nb(h->V, h->stream);
+    h->nb_valid = true;
+  }
   for (int attempt = 0; attempt < 2; ++attempt) {
     launch_mc_begin(h->V, h->stream);
     launch_mc(h->V, scope == VH_SCOPE_ALL, h->C.mc_min_weight, h->d_tris, (uint32_t)h->tri_cap,
@@ -536,6 +550,7 @@ vh_status vh_process_frame(vh_handle *h, const void *depth, int32_t depth_fmt, c
   s = run_frame(h, depth_fmt, true);
   if (s != VH_OK) return s;
   h->frames++;
+  h->nb_valid = true;
   if (!(h->p.flags & VH_FLAG_SYNC) && !out) return VH_OK;
   s = sync_and_check(h);
   if (out) {
@@ -594,6 +609,7 @@ vh_status vh_render(vh_handle *h) {
 }
 
 vh_status vh_alloc_keys(vh_handle *h, const int32_t *xyz, int64_t n, int32_t mem) {
+  if (h) h->nb_valid = false;
   if (!h || n < 0 || (n && !xyz) || n > 0x7FFFFFFF / 3) return VH_ERR_INVALID_ARG;
   if (!n) return VH_OK;
   DevBuf<int32_t> tmp;
@@ -629,6 +645,7 @@ vh_status vh_find_keys(vh_handle *h, const int32_t *xyz, int64_t n, int32_t *out
 
 vh_status vh_erase_keys(vh_handle *h, const int32_t *xyz, int64_t n, int64_t *num_erased,
                         int32_t mem) {
+  if (h) h->nb_valid = false;
   if (!h || n < 0 || (n && !xyz) || n > 0x7FFFFFFF / 3) return VH_ERR_INVALID_ARG;
   if (num_erased) *num_erased = 0;
   if (!n) return VH_OK;
@@ -646,6 +663,7 @@ vh_status vh_erase_keys(vh_handle *h, const int32_t *xyz, int64_t n, int64_t *nu
 }
 
 vh_status vh_clear_block_list(vh_handle *h) {
+  if (h) h->nb_valid = false;
   if (!h) return VH_ERR_INVALID_ARG;
   launch_clear_list(h->V, h->stream);
   VH_CUDA(h, cudaGetLastError());
@@ -730,6 +748,7 @@ vh_status vh_export_blocks(vh_handle *h, int32_t *xyz, float *sdf, float *weight
 
 vh_status vh_import_blocks(vh_handle *h, const int32_t *xyz, const float *sdf, const float *weight,
                            const uint8_t *rgb, int64_t n) {
+  if (h) h->nb_valid = false;
   if (!h || n < 0 || (n && (!xyz || !sdf || !weight || !rgb)) || n > (1ll << 24))
     return VH_ERR_INVALID_ARG;
   if (!n) return VH_OK;

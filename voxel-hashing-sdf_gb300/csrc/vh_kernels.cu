@@ -352,6 +352,28 @@ __device__ __forceinline__ bool update_voxel(const CamParams &C, const float P[1
   return true;
 }
 
+// Loads the slot of frame-list entry i and the block's voxel quad of thread t.
+struct BlockQuad {
+  unsigned long long key;
+  uint32_t block;
+  float4 sdf, wt;
+  uint4 rgb;
+};
+
+__device__ __forceinline__ void load_quad(const VolumeView &V, uint32_t i, int t, BlockQuad &q) {
+  const uint32_t s = __ldg(V.frame_list + i);
+  const ulonglong2 sl = __ldg(reinterpret_cast<const ulonglong2 *>(V.slots) + s);
+  q.key = sl.x;
+  q.block = (uint32_t)sl.y;
+  if (q.key >= kTombKey || q.block == kNoBlock) return;
+  const float *base = V.pool + (size_t)q.block * kBlockWords;
+  q.sdf = __ldcs(reinterpret_cast<const float4 *>(base) + t);
+  q.wt = __ldcs(reinterpret_cast<const float4 *>(base + kB3) + t);
+  q.rgb = __ldcs(reinterpret_cast<const uint4 *>(base + 2 * kB3) + t);
+}
+
+// Persistent CTAs, one block per iteration, the next block's loads issued
+// before the current block is computed (two blocks in flight per thread).
 __global__ void __launch_bounds__(128) k_integrate(VolumeView V, CamParams C,
                                                    const uint2 *__restrict__ pix,
                                                    const float *__restrict__ pose) {
@@ -362,32 +384,47 @@ __global__ void __launch_bounds__(128) k_integrate(VolumeView V, CamParams C,
   const int t = threadIdx.x;
   const int x0 = (t & 1) * 4, y = (t >> 1) & 7, z = t >> 4;
   uint32_t updated = 0;
-  for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
-    const uint32_t s = __ldg(V.frame_list + i);
-    const ulonglong2 sl = __ldg(reinterpret_cast<const ulonglong2 *>(V.slots) + s);
-    const unsigned long long key = sl.x;
-    const uint32_t b = (uint32_t)sl.y;
-    if (key >= kTombKey || b == kNoBlock) continue;
-    int bx, by, bz;
-    unpack_key(key, bx, by, bz);
-    float *base = V.pool + (size_t)b * kBlockWords;
-    float4 sd = reinterpret_cast<const float4 *>(base)[t];
-    float4 wt = reinterpret_cast<const float4 *>(base + kB3)[t];
-    uint4 cl = reinterpret_cast<const uint4 *>(base + 2 * kB3)[t];
-    const float wy = (float)(by * kB + y) * C.voxel;
-    const float wz = (float)(bz * kB + z) * C.voxel;
-    const int ix = bx * kB + x0;
-    bool a0 = update_voxel(C, P, pix, (float)(ix + 0) * C.voxel, wy, wz, sd.x, wt.x, cl.x);
-    bool a1 = update_voxel(C, P, pix, (float)(ix + 1) * C.voxel, wy, wz, sd.y, wt.y, cl.y);
-    bool a2 = update_voxel(C, P, pix, (float)(ix + 2) * C.voxel, wy, wz, sd.z, wt.z, cl.z);
-    bool a3 = update_voxel(C, P, pix, (float)(ix + 3) * C.voxel, wy, wz, sd.w, wt.w, cl.w);
-    const uint32_t nu = (uint32_t)a0 + a1 + a2 + a3;
-    if (nu) {
-      reinterpret_cast<float4 *>(base)[t] = sd;
-      reinterpret_cast<float4 *>(base + kB3)[t] = wt;
-      reinterpret_cast<uint4 *>(base + 2 * kB3)[t] = cl;
+  uint32_t i = blockIdx.x;
+  BlockQuad cur;
+  if (i < n) load_quad(V, i, t, cur);
+  for (; i < n; i += gridDim.x) {
+    BlockQuad nxt;
+    const uint32_t j = i + gridDim.x;
+    if (j < n) load_quad(V, j, t, nxt);
+    const bool live = cur.key < kTombKey && cur.block != kNoBlock;
+    if (t < 8) {
+      // neighbour ids for marching cubes: lane 0 the block itself, lane k the
+      // block at +(k & 1, k >> 1 & 1, k >> 2)
+      uint32_t nbid = kNoBlock;
+      if (live) {
+        int bx, by, bz;
+        unpack_key(cur.key, bx, by, bz);
+        const int nx = bx + (t & 1), ny = by + ((t >> 1) & 1), nz = bz + (t >> 2);
+        nbid = t == 0 ? cur.block
+                      : (key_in_range(nx, ny, nz) ? block_of(V, pack_key(nx, ny, nz)) : kNoBlock);
+      }
+      V.frame_nb[8 * (size_t)i + t] = nbid;
     }
-    updated += nu;
+    if (live) {
+      int bx, by, bz;
+      unpack_key(cur.key, bx, by, bz);
+      const float wy = (float)(by * kB + y) * C.voxel;
+      const float wz = (float)(bz * kB + z) * C.voxel;
+      const int ix = bx * kB + x0;
+      const bool a0 = update_voxel(C, P, pix, (float)(ix + 0) * C.voxel, wy, wz, cur.sdf.x, cur.wt.x, cur.rgb.x);
+      const bool a1 = update_voxel(C, P, pix, (float)(ix + 1) * C.voxel, wy, wz, cur.sdf.y, cur.wt.y, cur.rgb.y);
+      const bool a2 = update_voxel(C, P, pix, (float)(ix + 2) * C.voxel, wy, wz, cur.sdf.z, cur.wt.z, cur.rgb.z);
+      const bool a3 = update_voxel(C, P, pix, (float)(ix + 3) * C.voxel, wy, wz, cur.sdf.w, cur.wt.w, cur.rgb.w);
+      const uint32_t nu = (uint32_t)a0 + a1 + a2 + a3;
+      if (nu) {
+        float *base = V.pool + (size_t)cur.block * kBlockWords;
+        reinterpret_cast<float4 *>(base)[t] = cur.sdf;
+        reinterpret_cast<float4 *>(base + kB3)[t] = cur.wt;
+        reinterpret_cast<uint4 *>(base + 2 * kB3)[t] = cur.rgb;
+      }
+      updated += nu;
+    }
+    cur = nxt;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) updated += __shfl_xor_sync(kFull, updated, o);
@@ -395,23 +432,27 @@ __global__ void __launch_bounds__(128) k_integrate(VolumeView V, CamParams C,
 }
 
 // ---- marching cubes --------------------------------------------------------------
-constexpr int kH = 9;            // staged edge: 8 voxels + 1 halo
+constexpr int kH = 9;              // staged edge: 8 voxels + 1 halo
 constexpr int kH3 = kH * kH * kH;  // 729
 constexpr int kHalo = kH3 - kB3;   // 217
+constexpr int kMcThreads = 128;
 
 struct McShared {
-  float sdf[kH3];      // NaN = corner unusable (absent block or low weight)
+  float sdf[kH3];  // NaN = corner unusable (absent block or low weight)
   uint32_t rgb[kH3];
+  uint32_t act[kB3];  // active cubes: cube index | case << 16
   int8_t tri[256][16];
   uint16_t edge[256];
+  uint32_t prefix[kMcThreads + 1];  // exclusive scan of valid-triangle counts
+  uint32_t tmask[kMcThreads];       // valid-triangle mask | case << 8 | cube << 16
   uint32_t nb[8];
+  uint32_t warp_sum[kMcThreads / 32];
   int key[3];
-  uint32_t warp_sum[4];
+  uint32_t n_active;
   uint32_t base;
 };
 
 __device__ __forceinline__ int hidx(int x, int y, int z) { return x + kH * (y + kH * z); }
-
 __device__ __forceinline__ int corner_dx(int k) { return (kMcCornerBitsX >> k) & 1; }
 __device__ __forceinline__ int corner_dy(int k) { return (kMcCornerBitsY >> k) & 1; }
 __device__ __forceinline__ int corner_dz(int k) { return (kMcCornerBitsZ >> k) & 1; }
@@ -419,10 +460,9 @@ __device__ __forceinline__ int corner_dz(int k) { return (kMcCornerBitsZ >> k) &
 // Edge vertex e of the cube whose corner 0 is staged at (x, y, z), global
 // voxel (gx, gy, gz): VertexInterp(p[a], p[b], val[a], val[b])
 // (src/tsdf.cu:1640-1660) in global voxel units; the colour truncates like
-// the reference's float-to-uchar store.
-__device__ __forceinline__ void edge_vertex(const McShared &S, int e, int x, int y, int z,
-                                            int gx, int gy, int gz, float &ox, float &oy,
-                                            float &oz, uint32_t &oc) {
+// the reference's float-to-uchar store.  Returns {x, y, z, rgb bits}.
+__device__ __forceinline__ float4 edge_vertex(const McShared &S, int e, int x, int y, int z,
+                                              int gx, int gy, int gz) {
   const uint32_t code =
       (uint32_t)((e < 8 ? kMcEdgeCodeLo >> (8 * e) : kMcEdgeCodeHi >> (8 * (e - 8))) & 0x3Fu);
   const int a = (int)(code & 7u), b = (int)(code >> 3);
@@ -433,22 +473,10 @@ __device__ __forceinline__ void edge_vertex(const McShared &S, int e, int x, int
   const uint32_t c1 = S.rgb[ia], c2 = S.rgb[ib];
   const float p1x = (float)(gx + ax), p1y = (float)(gy + ay), p1z = (float)(gz + az);
   const float p2x = (float)(gx + bx), p2y = (float)(gy + by), p2z = (float)(gz + bz);
-  if (fabsf(0.0f - v1) < kSnap) {
-    ox = p1x, oy = p1y, oz = p1z, oc = c1;
-    return;
-  }
-  if (fabsf(0.0f - v2) < kSnap) {
-    ox = p2x, oy = p2y, oz = p2z, oc = c2;
-    return;
-  }
-  if (fabsf(v1 - v2) < kSnap) {
-    ox = p1x, oy = p1y, oz = p1z, oc = c1;
-    return;
-  }
+  if (fabsf(0.0f - v1) < kSnap) return make_float4(p1x, p1y, p1z, __uint_as_float(c1));
+  if (fabsf(0.0f - v2) < kSnap) return make_float4(p2x, p2y, p2z, __uint_as_float(c2));
+  if (fabsf(v1 - v2) < kSnap) return make_float4(p1x, p1y, p1z, __uint_as_float(c1));
   const float mu = (0.0f - v1) / (v2 - v1);
-  ox = p1x + mu * (p2x - p1x);
-  oy = p1y + mu * (p2y - p1y);
-  oz = p1z + mu * (p2z - p1z);
   uint32_t out = 0;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
@@ -456,7 +484,8 @@ __device__ __forceinline__ void edge_vertex(const McShared &S, int e, int x, int
     const float v = (float)q1 + mu * (float)(q2 - q1);
     out |= (__float2uint_rz(v) & 0xFFu) << (8 * c);
   }
-  oc = out;
+  return make_float4(p1x + mu * (p2x - p1x), p1y + mu * (p2y - p1y), p1z + mu * (p2z - p1z),
+                     __uint_as_float(out));
 }
 
 // Cube case of the cube with staged corner 0 at (x, y, z); -1 if a corner is
@@ -472,33 +501,39 @@ __device__ __forceinline__ int cube_case(const McShared &S, int x, int y, int z)
   return ci;
 }
 
-// Valid-triangle mask of a cube: the reference drops a triangle when
-// p0 == p1 || p1 == p2 (src/tsdf.cu:1055-1057).
-__device__ __forceinline__ uint32_t cube_mask(const McShared &S, int ci, int x, int y, int z,
-                                              int gx, int gy, int gz) {
-  uint32_t mask = 0;
-  for (int t = 0; t < 5; ++t) {
-    const int e0 = S.tri[ci][3 * t];
-    if (e0 < 0) break;
-    const int e1 = S.tri[ci][3 * t + 1], e2 = S.tri[ci][3 * t + 2];
-    float ax, ay, az, bx, by, bz, cx, cy, cz;
-    uint32_t cc;
-    edge_vertex(S, e0, x, y, z, gx, gy, gz, ax, ay, az, cc);
-    edge_vertex(S, e1, x, y, z, gx, gy, gz, bx, by, bz, cc);
-    edge_vertex(S, e2, x, y, z, gx, gy, gz, cx, cy, cz, cc);
-    const bool d01 = ax == bx && ay == by && az == bz;
-    const bool d12 = bx == cx && by == cy && bz == cz;
-    if (!(d01 || d12)) mask |= 1u << t;
-  }
-  return mask;
+__device__ __forceinline__ bool same_pos(const float4 &a, const float4 &b) {
+  return a.x == b.x && a.y == b.y && a.z == b.z;
 }
 
-__global__ void __launch_bounds__(128) k_mc(VolumeView V, int scope_all, float min_weight,
-                                            float4 *__restrict__ tris, uint32_t tri_cap) {
-  __shared__ McShared S;
+// Exclusive CTA-wide scan of `v` (kMcThreads threads); returns the prefix and
+// leaves the total in *total.  Contains __syncthreads.
+__device__ __forceinline__ uint32_t cta_scan(McShared &S, uint32_t v, uint32_t *total) {
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  for (int i = t; i < 256 * 16; i += 128) (&S.tri[0][0])[i] = kMcTri[i >> 4][i & 15];
-  for (int i = t; i < 256; i += 128) S.edge[i] = kMcEdgeMask[i];
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t u = __shfl_up_sync(kFull, incl, o);
+    if (lane >= o) incl += u;
+  }
+  if (lane == 31) S.warp_sum[warp] = incl;
+  __syncthreads();
+  uint32_t before = 0, tot = 0;
+#pragma unroll
+  for (int q = 0; q < kMcThreads / 32; ++q) {
+    const uint32_t ws = S.warp_sum[q];
+    before += q < warp ? ws : 0u;
+    tot += ws;
+  }
+  *total = tot;
+  return before + incl - v;
+}
+
+__global__ void __launch_bounds__(kMcThreads, 8) k_mc(VolumeView V, int scope_all, float min_weight,
+                                                   float4 *__restrict__ tris, uint32_t tri_cap) {
+  __shared__ McShared S;
+  const int t = threadIdx.x;
+  for (int i = t; i < 256 * 16; i += kMcThreads) (&S.tri[0][0])[i] = kMcTri[i >> 4][i & 15];
+  for (int i = t; i < 256; i += kMcThreads) S.edge[i] = kMcEdgeMask[i];
   const uint32_t n = scope_all ? V.st->pool_top : min(V.st->frame_count, V.frame_cap);
   const float nanv = __int_as_float(0x7FC00000);
   for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
@@ -519,17 +554,17 @@ __global__ void __launch_bounds__(128) k_mc(VolumeView V, int scope_all, float m
       S.key[0] = x;
       S.key[1] = y;
       S.key[2] = z;
-      S.nb[0] = b;
+      if (scope_all) S.nb[0] = b;
     }
+    if (!scope_all && t >= 32 && t < 40) S.nb[t - 32] = __ldg(V.frame_nb + 8 * (size_t)i + (t - 32));
     __syncthreads();
     if (S.nb[0] == kNoBlock) continue;
     const int bx = S.key[0], by = S.key[1], bz = S.key[2];
-    if (t >= 1 && t < 8) {
+    if (scope_all && t >= 1 && t < 8) {
       const int nx = bx + (t & 1), ny = by + ((t >> 1) & 1), nz = bz + (t >> 2);
       S.nb[t] = key_in_range(nx, ny, nz) ? block_of(V, pack_key(nx, ny, nz)) : kNoBlock;
     }
-    // own block: 4 voxels per thread, 16-byte loads
-    {
+    {  // own block: 4 voxels per thread, 16-byte loads
       const float *base = V.pool + (size_t)S.nb[0] * kBlockWords;
       const float4 sd = reinterpret_cast<const float4 *>(base)[t];
       const float4 wt = reinterpret_cast<const float4 *>(base + kB3)[t];
@@ -547,7 +582,7 @@ __global__ void __launch_bounds__(128) k_mc(VolumeView V, int scope_all, float m
     }
     __syncthreads();  // S.nb complete
     // halo: x == 8 (81), then y == 8 with x < 8 (72), then z == 8 with x, y < 8 (64)
-    for (int hh = t; hh < kHalo; hh += 128) {
+    for (int hh = t; hh < kHalo; hh += kMcThreads) {
       int x, y, z;
       if (hh < 81) {
         x = 8;
@@ -564,78 +599,88 @@ __global__ void __launch_bounds__(128) k_mc(VolumeView V, int scope_all, float m
         y = q >> 3;
         z = 8;
       }
-      const int nbi = (x >> 3) | ((y >> 3) << 1) | ((z >> 3) << 2);
-      const uint32_t blk = S.nb[nbi];
+      const uint32_t blk = S.nb[(x >> 3) | ((y >> 3) << 1) | ((z >> 3) << 2)];
       float v = nanv;
       uint32_t c = 0;
       if (blk != kNoBlock) {
         const float *base = V.pool + (size_t)blk * kBlockWords;
         const int li = (x & 7) + 8 * (y & 7) + 64 * (z & 7);
-        const float wv = __ldg(base + kB3 + li);
-        v = wv >= min_weight ? __ldg(base + li) : nanv;
+        v = __ldg(base + kB3 + li) >= min_weight ? __ldg(base + li) : nanv;
         c = __ldg(reinterpret_cast<const uint32_t *>(base + 2 * kB3) + li);
       }
       S.sdf[hidx(x, y, z)] = v;
       S.rgb[hidx(x, y, z)] = c;
     }
     __syncthreads();
-    // pass 1: cases and valid-triangle masks of this thread's 4 cubes
+    // classify this thread's 4 cubes and compact the active ones
+    uint32_t mine[4];
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int c = t + kMcThreads * j;
+      const int ci = cube_case(S, c & 7, (c >> 3) & 7, c >> 6);
+      mine[j] = 0xFFFFFFFFu;
+      if (ci > 0 && S.edge[ci] != 0) mine[cnt++] = (uint32_t)c | ((uint32_t)ci << 16);
+    }
+    uint32_t n_active;
+    const uint32_t off = cta_scan(S, cnt, &n_active);
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if ((uint32_t)j < cnt) S.act[off + j] = mine[j];
     const int gx0 = bx * kB, gy0 = by * kB, gz0 = bz * kB;
-    uint32_t packed[4];
-    uint32_t count = 0;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int c = t + 128 * j;
-      const int x = c & 7, y = (c >> 3) & 7, z = c >> 6;
-      packed[j] = 0;
-      const int ci = cube_case(S, x, y, z);
-      if (ci > 0 && S.edge[ci] != 0) {
-        const uint32_t m = cube_mask(S, ci, x, y, z, gx0 + x, gy0 + y, gz0 + z);
-        packed[j] = (uint32_t)ci | (m << 8);
-        count += __popc(m);
-      }
-    }
-    // CTA exclusive scan of the counts, one global atomic per block
-    uint32_t incl = count;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t v = __shfl_up_sync(kFull, incl, o);
-      if (lane >= o) incl += v;
-    }
-    if (lane == 31) S.warp_sum[warp] = incl;
-    __syncthreads();
-    if (t == 0) {
-      const uint32_t tot = S.warp_sum[0] + S.warp_sum[1] + S.warp_sum[2] + S.warp_sum[3];
-      S.base = tot ? atomicAdd(&V.st->tri_count, tot) : 0u;
-    }
-    __syncthreads();
-    uint32_t out = S.base + incl - count;
-    for (int q = 0; q < warp; ++q) out += S.warp_sum[q];
-    // pass 2: write the valid triangles
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const uint32_t pk = packed[j];
-      const uint32_t m = pk >> 8;
-      if (!m) continue;
-      const int ci = (int)(pk & 0xFFu);
-      const int c = t + 128 * j;
-      const int x = c & 7, y = (c >> 3) & 7, z = c >> 6;
-      for (int tt = 0; tt < 5; ++tt) {
-        if (!(m & (1u << tt))) continue;
-        if (out < tri_cap) {
-          float4 *dst = tris + 3 * (size_t)out;
-#pragma unroll
-          for (int k = 0; k < 3; ++k) {
-            float vx, vy, vz;
-            uint32_t vc;
-            edge_vertex(S, S.tri[ci][3 * tt + k], x, y, z, gx0 + x, gy0 + y, gz0 + z, vx, vy, vz,
-                        vc);
-            dst[k] = make_float4(vx, vy, vz, __uint_as_float(vc));
-          }
-        } else {
-          atomicOr(&V.st->error, kErrTriCap);
+    for (uint32_t r = 0; r < n_active; r += kMcThreads) {
+      __syncthreads();  // act[] written / previous round's prefix consumed
+      // one active cube per thread: valid-triangle mask
+      uint32_t tm = 0, tcount = 0;
+      if (r + t < n_active) {
+        const uint32_t a = S.act[r + t];
+        const int c = (int)(a & 0xFFFFu), ci = (int)(a >> 16);
+        const int x = c & 7, y = (c >> 3) & 7, z = c >> 6;
+        uint32_t m = 0;
+        for (int tt = 0; tt < 5; ++tt) {
+          const int e0 = S.tri[ci][3 * tt];
+          if (e0 < 0) break;
+          const int e1 = S.tri[ci][3 * tt + 1], e2 = S.tri[ci][3 * tt + 2];
+          const float4 p0 = edge_vertex(S, e0, x, y, z, gx0 + x, gy0 + y, gz0 + z);
+          const float4 p1 = edge_vertex(S, e1, x, y, z, gx0 + x, gy0 + y, gz0 + z);
+          const float4 p2 = edge_vertex(S, e2, x, y, z, gx0 + x, gy0 + y, gz0 + z);
+          // the reference drops p0 == p1 || p1 == p2 (src/tsdf.cu:1055-1057)
+          if (!(same_pos(p0, p1) || same_pos(p1, p2))) m |= 1u << tt;
         }
-        ++out;
+        tm = m | ((uint32_t)ci << 8) | ((uint32_t)c << 16);
+        tcount = __popc(m);
+      }
+      uint32_t total;
+      const uint32_t pre = cta_scan(S, tcount, &total);
+      S.prefix[t] = pre;
+      S.tmask[t] = tm;
+      if (t == 0) {
+        S.prefix[kMcThreads] = total;
+        S.base = total ? atomicAdd(&V.st->tri_count, total) : 0u;
+      }
+      __syncthreads();
+      // cooperative, contiguous write of this round's triangles (float4 units);
+      // each output vertex is recomputed from the staged corners
+      const uint32_t base = S.base;
+      for (uint32_t q = t; q < 3u * total; q += kMcThreads) {
+        const uint32_t k = q / 3u, j = q - 3u * k;
+        int lo = 0, hi = kMcThreads;  // owner: last thread with prefix <= k
+        while (hi - lo > 1) {
+          const int mid = (lo + hi) >> 1;
+          if (S.prefix[mid] <= k) lo = mid; else hi = mid;
+        }
+        const uint32_t tmk = S.tmask[lo];
+        uint32_t m = tmk & 0x1Fu;
+        for (uint32_t skip = k - S.prefix[lo]; skip; --skip) m &= m - 1u;
+        const int tt = __ffs(m) - 1;
+        const int ci = (int)((tmk >> 8) & 0xFFu), c = (int)(tmk >> 16);
+        const int x = c & 7, y = (c >> 3) & 7, z = c >> 6;
+        const uint32_t out = base + k;
+        if (out < tri_cap)
+          tris[3 * (size_t)out + j] =
+              edge_vertex(S, S.tri[ci][3 * tt + (int)j], x, y, z, gx0 + x, gy0 + y, gz0 + z);
+        else if (j == 0)
+          atomicOr(&V.st->error, kErrTriCap);
       }
     }
   }
@@ -755,6 +800,25 @@ __global__ void __launch_bounds__(256) k_erase_keys(VolumeView V, const int32_t 
   }
 }
 
+// Rebuilds frame_nb for the current block list (needed when the list changed
+// without an integration, e.g. after alloc_keys or erase).  8 threads per entry.
+__global__ void __launch_bounds__(256) k_frame_nb(VolumeView V) {
+  const uint32_t n = min(V.st->frame_count, V.frame_cap);
+  const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = idx >> 3, k = idx & 7u;
+  if (i >= n) return;
+  const Slot sl = V.slots[V.frame_list[i]];
+  uint32_t nbid = kNoBlock;
+  if (sl.key < kTombKey && sl.block != kNoBlock) {
+    int bx, by, bz;
+    unpack_key(sl.key, bx, by, bz);
+    const int nx = bx + (int)(k & 1u), ny = by + (int)((k >> 1) & 1u), nz = bz + (int)(k >> 2);
+    nbid = k == 0 ? sl.block
+                  : (key_in_range(nx, ny, nz) ? block_of(V, pack_key(nx, ny, nz)) : kNoBlock);
+  }
+  V.frame_nb[8 * (size_t)i + k] = nbid;
+}
+
 __global__ void k_list_keys(VolumeView V, int32_t *__restrict__ xyz, uint32_t n) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -807,6 +871,18 @@ void launch_allocate(const VolumeView &V, const CamParams &C, const void *depth,
     k_allocate<float><<<grid, 256, 0, s>>>(V, C, (const float *)depth, rgb, pose, pix);
 }
 
+int integrate_ctas_per_sm() {
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_integrate, 128, 0);
+  return n > 0 ? n : 1;
+}
+
+int mc_ctas_per_sm() {
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mc, kMcThreads, 0);
+  return n > 0 ? n : 1;
+}
+
 void launch_integrate(const VolumeView &V, const CamParams &C, const uint2 *pix, const float *pose,
                       int grid, cudaStream_t s) {
   k_integrate<<<grid, 128, 0, s>>>(V, C, pix, pose);
@@ -814,7 +890,7 @@ void launch_integrate(const VolumeView &V, const CamParams &C, const uint2 *pix,
 
 void launch_mc(const VolumeView &V, int scope_all, float min_weight, float4 *tris,
                uint32_t tri_cap, int grid, cudaStream_t s) {
-  k_mc<<<grid, 128, 0, s>>>(V, scope_all, min_weight, tris, tri_cap);
+  k_mc<<<grid, kMcThreads, 0, s>>>(V, scope_all, min_weight, tris, tri_cap);
 }
 
 void launch_alloc_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, cudaStream_t s) {
@@ -826,6 +902,9 @@ void launch_find_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, int32
 }
 void launch_erase_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, cudaStream_t s) {
   if (n) k_erase_keys<<<grid_for(n, 256), 256, 0, s>>>(V, xyz, n);
+}
+void launch_frame_nb(const VolumeView &V, cudaStream_t s) {
+  k_frame_nb<<<grid_for(V.frame_cap * 8u, 256), 256, 0, s>>>(V);
 }
 void launch_list_keys(const VolumeView &V, int32_t *xyz, uint32_t n, cudaStream_t s) {
   if (n) k_list_keys<<<grid_for(n, 256), 256, 0, s>>>(V, xyz, n);
