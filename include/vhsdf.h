@@ -119,6 +119,16 @@ typedef struct vh_mesh_view {
   float voxel_size;
 } vh_mesh_view;
 
+/* Launch configuration of the per-frame kernels.  Every configuration
+ * computes identical results; only the speed differs. */
+typedef struct vh_tuning {
+  int32_t integrate_variant;     /* 0: one block in flight per CTA,          */
+                                 /* 1: next block's voxels prefetched        */
+  int32_t integrate_ctas_per_sm; /* resident CTAs per SM (0 = occupancy max) */
+  int32_t mc_ctas_per_sm;        /* resident CTAs per SM (0 = occupancy max) */
+  int32_t reserved;
+} vh_tuning;
+
 typedef struct vh_handle vh_handle;
 
 /* ---- parameters --------------------------------------------------------- */
@@ -225,6 +235,19 @@ vh_status vh_save(vh_handle *h, const char *path);
 vh_status vh_load(vh_handle *h, const char *path);
 
 vh_status vh_get_stats(vh_handle *h, vh_stats *out);
+
+/* ---- launch tuning (no reference counterpart: the reference launches fixed
+ * shapes, src/tsdf.cu:1526-1545,2262-2264) ------------------------------- */
+
+vh_status vh_get_tuning(vh_handle *h, vh_tuning *out);
+vh_status vh_set_tuning(vh_handle *h, const vh_tuning *t);
+/* Times every candidate configuration on one frame in a scratch volume with
+ * the handle's parameters (the handle's volume is not touched), applies the
+ * fastest and returns it in `chosen` (may be NULL).  Results are cached per
+ * process and, when the environment variable VHSDF_TUNING_CACHE names a
+ * file, in that file, keyed by GPU, image size and volume parameters. */
+vh_status vh_autotune(vh_handle *h, const void *depth, int32_t depth_fmt, const uint8_t *rgb,
+                      const float *c2w, int32_t mem, vh_tuning *chosen);
 
 #ifdef __cplusplus
 } /* extern "C" */

@@ -206,3 +206,41 @@ def test_frame_scope_mc_after_list_change_without_integration(scene):
     gx, gc = vol.mesh()
     m = orc2.marching_cubes("frame")
     assert np.array_equal(sort_rows(tri_rows(gx, gc)), sort_rows(tri_rows(m["xyz"], m["rgb"])))
+
+
+def test_every_launch_configuration_is_bit_exact(scene):
+    """The tuner only changes speed: each configuration reproduces the oracle."""
+    orc = None
+    results = []
+    configs = [(0, 0, 0), (1, 0, 0), (0, 2, 3), (1, 1, 1)]
+    for cfg in configs:
+        vol = volume_for(scene)
+        vol.set_tuning(*cfg)
+        if orc is None:
+            orc = oracle_for(vol, 32)
+            for f in range(4):
+                orc.integrate(*scene.render(f))
+        for f in range(4):
+            vol.process_frame(*scene.render(f))
+        assert_same_blocks(vol.export_blocks(), orc.export())
+        vol.extract("all")
+        results.append(sort_rows(tri_rows(*vol.mesh())))
+        vol.close()
+    m = orc.marching_cubes("all")
+    want = sort_rows(tri_rows(m["xyz"], m["rgb"]))
+    for r in results:
+        assert np.array_equal(r, want)
+
+
+def test_autotune_picks_a_valid_configuration(scene, tmp_path, monkeypatch):
+    monkeypatch.setenv("VHSDF_TUNING_CACHE", str(tmp_path / "tune.txt"))
+    vol = volume_for(scene)
+    d, c, p = scene.render(0)
+    t = vol.autotune(d, c, p)
+    assert t["integrate_variant"] in (0, 1)
+    assert t["integrate_ctas_per_sm"] >= 1 and t["mc_ctas_per_sm"] >= 1
+    assert vol.stats()["blocks_allocated"] == 0  # the handle's volume is untouched
+    assert vol.tuning() == t
+    assert (tmp_path / "tune.txt").read_text().strip()
+    vol2 = volume_for(scene)
+    assert vol2.autotune(d, c, p) == t  # served from the cache

@@ -12,7 +12,12 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <fstream>
+#include <map>
+#include <mutex>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -30,8 +35,9 @@ constexpr int kNumEvents = 5;
 struct vh_handle {
   vh_params p{};
   int sm_count = 0;
-  int integrate_per_sm = 1;
+  int integrate_per_sm = 1;  // resident CTAs per SM in use
   int mc_per_sm = 1;
+  vh_tuning tuning{};        // requested configuration (0 = occupancy max)
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
   VolumeView V{};
@@ -168,7 +174,8 @@ void enqueue_frame(vh_handle *h, int fmt, bool with_mc, bool events, bool captur
   launch_allocate(h->V, h->C, h->d_depth, fmt, h->d_rgb, h->d_pose, h->d_pix, s);
   launch_epoch_end(h->V, s);
   if (events) stage_event(h->ev[1], s, capturing);
-  launch_integrate(h->V, h->C, h->d_pix, h->d_pose, integrate_grid(h), s);
+  launch_integrate(h->V, h->C, h->d_pix, h->d_pose, integrate_grid(h),
+                   h->tuning.integrate_variant, s);
   if (events) stage_event(h->ev[2], s, capturing);
   if (with_mc) {
     launch_mc_begin(h->V, s);
@@ -184,6 +191,20 @@ void drop_graphs(vh_handle *h) {
         cudaGraphExecDestroy(g);
         g = nullptr;
       }
+}
+
+// Resolves a requested configuration against the occupancy limits.
+void apply_tuning(vh_handle *h, const vh_tuning &t) {
+  h->tuning = t;
+  h->tuning.integrate_variant = t.integrate_variant == 1 ? 1 : 0;
+  const int imax = integrate_ctas_per_sm(h->tuning.integrate_variant);
+  const int mmax = mc_ctas_per_sm();
+  h->integrate_per_sm =
+      t.integrate_ctas_per_sm > 0 && t.integrate_ctas_per_sm < imax ? t.integrate_ctas_per_sm : imax;
+  h->mc_per_sm = t.mc_ctas_per_sm > 0 && t.mc_ctas_per_sm < mmax ? t.mc_ctas_per_sm : mmax;
+  h->tuning.integrate_ctas_per_sm = h->integrate_per_sm;
+  h->tuning.mc_ctas_per_sm = h->mc_per_sm;
+  drop_graphs(h);  // graphs hold the grid sizes
 }
 
 // Runs the frame chain as a CUDA graph (captured on first use) or directly.
@@ -414,8 +435,7 @@ vh_status vh_create(const vh_params *p, vh_handle **out) {
   if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess)
     return bail(VH_ERR_CUDA);
   h->stream = h->own_stream;
-  h->integrate_per_sm = integrate_ctas_per_sm();
-  h->mc_per_sm = mc_ctas_per_sm();
+  apply_tuning(h, vh_tuning{});
   const size_t slots = (size_t)1 << p->table_log2;
   const size_t npx = (size_t)p->width * p->height;
   h->tri_cap = p->max_triangles;
@@ -828,4 +848,146 @@ vh_status vh_get_stats(vh_handle *h, vh_stats *out) {
   return s;
 }
 
+vh_status vh_get_tuning(vh_handle *h, vh_tuning *out) {
+  if (!h || !out) return VH_ERR_INVALID_ARG;
+  *out = h->tuning;
+  return VH_OK;
+}
+
+vh_status vh_set_tuning(vh_handle *h, const vh_tuning *t) {
+  if (!h || !t || t->integrate_variant < 0 || t->integrate_variant > 1 ||
+      t->integrate_ctas_per_sm < 0 || t->mc_ctas_per_sm < 0)
+    return VH_ERR_INVALID_ARG;
+  VH_CUDA(h, cudaStreamSynchronize(h->stream));
+  apply_tuning(h, *t);
+  return VH_OK;
+}
+
 }  // extern "C"
+
+namespace {
+
+std::mutex g_tune_mu;
+std::map<std::string, vh_tuning> g_tune_cache;
+
+std::string tune_key(const vh_handle *h) {
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, h->p.device) != cudaSuccess) std::strcpy(prop.name, "?");
+  std::ostringstream k;
+  k << prop.name << "|sm" << h->sm_count << "|" << h->p.width << "x" << h->p.height << "|v"
+    << h->p.voxel_size << "|t" << h->p.trunc << "|d" << h->p.min_depth << "-" << h->p.max_depth
+    << "|f" << h->p.fx << "|w" << h->p.mc_min_weight;
+  std::string s = k.str();
+  for (char &c : s)
+    if (c == ' ' || c == '\t' || c == '\n') c = '_';
+  return s;
+}
+
+bool cache_lookup(const std::string &key, vh_tuning *t) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  auto it = g_tune_cache.find(key);
+  if (it != g_tune_cache.end()) {
+    *t = it->second;
+    return true;
+  }
+  const char *path = std::getenv("VHSDF_TUNING_CACHE");
+  if (!path) return false;
+  std::ifstream f(path);
+  std::string k;
+  vh_tuning v{};
+  while (f >> k >> v.integrate_variant >> v.integrate_ctas_per_sm >> v.mc_ctas_per_sm) {
+    if (k == key) {
+      g_tune_cache[key] = v;
+      *t = v;
+      return true;
+    }
+  }
+  return false;
+}
+
+void cache_store(const std::string &key, const vh_tuning &t) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune_cache[key] = t;
+  const char *path = std::getenv("VHSDF_TUNING_CACHE");
+  if (!path) return;
+  std::ofstream f(path, std::ios::app);
+  f << key << " " << t.integrate_variant << " " << t.integrate_ctas_per_sm << " "
+    << t.mc_ctas_per_sm << "\n";
+}
+
+float median(std::vector<float> v) {
+  std::sort(v.begin(), v.end());
+  return v.empty() ? 0.0f : v[v.size() / 2];
+}
+
+}  // namespace
+
+extern "C" vh_status vh_autotune(vh_handle *h, const void *depth, int32_t depth_fmt,
+                                 const uint8_t *rgb, const float *c2w, int32_t mem,
+                                 vh_tuning *chosen) {
+  if (!h) return VH_ERR_INVALID_ARG;
+  const std::string key = tune_key(h);
+  vh_tuning best{};
+  if (cache_lookup(key, &best)) {
+    vh_status s = vh_set_tuning(h, &best);
+    if (chosen) *chosen = h->tuning;
+    return s;
+  }
+  vh_params sp = h->p;
+  sp.flags = VH_FLAG_SYNC | VH_FLAG_PROFILE | VH_FLAG_NO_GRAPH;
+  sp.pool_blocks = std::min<int64_t>(h->p.pool_blocks, h->p.max_frame_blocks + 4096);
+  vh_handle *sc = nullptr;
+  vh_status s = vh_create(&sp, &sc);
+  if (s != VH_OK) return fail(h, s, "autotune: cannot create the scratch volume");
+  const int reps = 5;
+  auto run = [&](const vh_tuning &t, float *ms_int, float *ms_mc) -> vh_status {
+    apply_tuning(sc, t);
+    std::vector<float> a, b;
+    for (int r = 0; r < reps; ++r) {
+      vh_status st = vh_process_frame(sc, depth, depth_fmt, rgb, c2w, mem, nullptr);
+      if (st != VH_OK) return st;
+      a.push_back(sc->stage.ms_integrate);
+      b.push_back(sc->stage.ms_extract);
+    }
+    *ms_int = median(a);
+    *ms_mc = median(b);
+    return VH_OK;
+  };
+  float mi = 0, mm = 0;
+  s = run(vh_tuning{}, &mi, &mm);  // also allocates the frame's blocks
+  float best_int = 1e30f, best_mc = 1e30f;
+  for (int variant = 0; variant < 2 && s == VH_OK; ++variant) {
+    const int occ = integrate_ctas_per_sm(variant);
+    const int opts[3] = {occ, std::max(1, occ * 3 / 4), std::max(1, occ / 2)};
+    for (int o = 0; o < 3 && s == VH_OK; ++o) {
+      if (o > 0 && opts[o] == opts[o - 1]) continue;
+      vh_tuning t{};
+      t.integrate_variant = variant;
+      t.integrate_ctas_per_sm = opts[o];
+      s = run(t, &mi, &mm);
+      if (s == VH_OK && mi < best_int) {
+        best_int = mi;
+        best.integrate_variant = variant;
+        best.integrate_ctas_per_sm = opts[o];
+      }
+    }
+  }
+  const int mocc = mc_ctas_per_sm();
+  const int mopts[3] = {mocc, std::max(1, mocc * 2 / 3), std::max(1, mocc / 2)};
+  for (int o = 0; o < 3 && s == VH_OK; ++o) {
+    if (o > 0 && mopts[o] == mopts[o - 1]) continue;
+    vh_tuning t = best;
+    t.mc_ctas_per_sm = mopts[o];
+    s = run(t, &mi, &mm);
+    if (s == VH_OK && mm < best_mc) {
+      best_mc = mm;
+      best.mc_ctas_per_sm = mopts[o];
+    }
+  }
+  vh_destroy(sc);
+  if (s != VH_OK) return fail(h, s, "autotune: a trial frame failed");
+  cache_store(key, best);
+  s = vh_set_tuning(h, &best);
+  if (chosen) *chosen = h->tuning;
+  return s;
+}

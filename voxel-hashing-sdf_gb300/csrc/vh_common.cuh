@@ -128,12 +128,13 @@ void launch_mc_begin(const VolumeView &V, cudaStream_t s);
 // fmt: 0 = uint16 scaled by depth_scale, 1 = float metres
 void launch_allocate(const VolumeView &V, const CamParams &C, const void *depth, int fmt,
                      const uint8_t *rgb, const float *pose, uint2 *pix, cudaStream_t s);
+// variant 0: one block in flight per CTA; 1: next block prefetched
 void launch_integrate(const VolumeView &V, const CamParams &C, const uint2 *pix,
-                      const float *pose, int grid, cudaStream_t s);
+                      const float *pose, int grid, int variant, cudaStream_t s);
 void launch_mc(const VolumeView &V, int scope_all, float min_weight, float4 *tris,
                uint32_t tri_cap, int grid, cudaStream_t s);
 // Resident CTAs per SM of the persistent kernels (for grid sizing).
-int integrate_ctas_per_sm();
+int integrate_ctas_per_sm(int variant);
 int mc_ctas_per_sm();
 void launch_alloc_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, cudaStream_t s);
 void launch_find_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, int32_t *out,

@@ -367,13 +367,17 @@ __device__ __forceinline__ void load_quad(const VolumeView &V, uint32_t i, int t
   q.block = (uint32_t)sl.y;
   if (q.key >= kTombKey || q.block == kNoBlock) return;
   const float *base = V.pool + (size_t)q.block * kBlockWords;
-  q.sdf = __ldcs(reinterpret_cast<const float4 *>(base) + t);
-  q.wt = __ldcs(reinterpret_cast<const float4 *>(base + kB3) + t);
-  q.rgb = __ldcs(reinterpret_cast<const uint4 *>(base + 2 * kB3) + t);
+  q.sdf = reinterpret_cast<const float4 *>(base)[t];
+  q.wt = reinterpret_cast<const float4 *>(base + kB3)[t];
+  q.rgb = reinterpret_cast<const uint4 *>(base + 2 * kB3)[t];
 }
 
-// Persistent CTAs, one block per iteration, the next block's loads issued
-// before the current block is computed (two blocks in flight per thread).
+// Persistent CTAs of 128 threads, one voxel block per iteration, 4 voxels
+// per thread.  kPrefetch: the next block's loads are issued before the
+// current block is computed (two blocks in flight per thread, more
+// registers); otherwise one block in flight and higher occupancy.
+// Threads 0..7 also record the block's +x/+y/+z neighbour ids for MC.
+template <bool kPrefetch>
 __global__ void __launch_bounds__(128) k_integrate(VolumeView V, CamParams C,
                                                    const uint2 *__restrict__ pix,
                                                    const float *__restrict__ pose) {
@@ -386,15 +390,18 @@ __global__ void __launch_bounds__(128) k_integrate(VolumeView V, CamParams C,
   uint32_t updated = 0;
   uint32_t i = blockIdx.x;
   BlockQuad cur;
-  if (i < n) load_quad(V, i, t, cur);
+  if (kPrefetch && i < n) load_quad(V, i, t, cur);
   for (; i < n; i += gridDim.x) {
     BlockQuad nxt;
-    const uint32_t j = i + gridDim.x;
-    if (j < n) load_quad(V, j, t, nxt);
+    if (kPrefetch) {
+      const uint32_t j = i + gridDim.x;
+      if (j < n) load_quad(V, j, t, nxt);
+    } else {
+      load_quad(V, i, t, cur);
+    }
     const bool live = cur.key < kTombKey && cur.block != kNoBlock;
     if (t < 8) {
-      // neighbour ids for marching cubes: lane 0 the block itself, lane k the
-      // block at +(k & 1, k >> 1 & 1, k >> 2)
+      // lane 0: the block itself; lane k: the block at +(k & 1, k >> 1 & 1, k >> 2)
       uint32_t nbid = kNoBlock;
       if (live) {
         int bx, by, bz;
@@ -424,7 +431,7 @@ __global__ void __launch_bounds__(128) k_integrate(VolumeView V, CamParams C,
       }
       updated += nu;
     }
-    cur = nxt;
+    if (kPrefetch) cur = nxt;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) updated += __shfl_xor_sync(kFull, updated, o);
@@ -436,19 +443,20 @@ constexpr int kH = 9;              // staged edge: 8 voxels + 1 halo
 constexpr int kH3 = kH * kH * kH;  // 729
 constexpr int kHalo = kH3 - kB3;   // 217
 constexpr int kMcThreads = 128;
+constexpr int kMaxCand = kB3 * 5;  // at most 5 triangles per cube
 
 struct McShared {
   float sdf[kH3];  // NaN = corner unusable (absent block or low weight)
   uint32_t rgb[kH3];
-  uint32_t act[kB3];  // active cubes: cube index | case << 16
   int8_t tri[256][16];
   uint16_t edge[256];
-  uint32_t prefix[kMcThreads + 1];  // exclusive scan of valid-triangle counts
-  uint32_t tmask[kMcThreads];       // valid-triangle mask | case << 8 | cube << 16
+  uint8_t ntri[256];
+  uint8_t cases[kB3];        // cube case, 0 when the cube emits nothing
+  uint16_t cand[kMaxCand];   // candidate triangles: cube | triangle << 9
+  uint16_t valid[kMaxCand];  // candidates that survive the degenerate test
   uint32_t nb[8];
   uint32_t warp_sum[kMcThreads / 32];
   int key[3];
-  uint32_t n_active;
   uint32_t base;
 };
 
@@ -457,35 +465,88 @@ __device__ __forceinline__ int corner_dx(int k) { return (kMcCornerBitsX >> k) &
 __device__ __forceinline__ int corner_dy(int k) { return (kMcCornerBitsY >> k) & 1; }
 __device__ __forceinline__ int corner_dz(int k) { return (kMcCornerBitsZ >> k) & 1; }
 
-// Edge vertex e of the cube whose corner 0 is staged at (x, y, z), global
-// voxel (gx, gy, gz): VertexInterp(p[a], p[b], val[a], val[b])
-// (src/tsdf.cu:1640-1660) in global voxel units; the colour truncates like
-// the reference's float-to-uchar store.  Returns {x, y, z, rgb bits}.
-__device__ __forceinline__ float4 edge_vertex(const McShared &S, int e, int x, int y, int z,
-                                              int gx, int gy, int gz) {
+// Corners a -> b of edge e of the cube with staged corner 0 at (x, y, z).
+struct EdgeEnds {
+  int ia, ib;     // staged indices
+  int ax, ay, az; // offset of corner a
+  int axis;       // axis along which b differs from a
+  int dir;        // +1 or -1
+};
+
+__device__ __forceinline__ EdgeEnds edge_ends(int e, int x, int y, int z) {
   const uint32_t code =
       (uint32_t)((e < 8 ? kMcEdgeCodeLo >> (8 * e) : kMcEdgeCodeHi >> (8 * (e - 8))) & 0x3Fu);
   const int a = (int)(code & 7u), b = (int)(code >> 3);
-  const int ax = corner_dx(a), ay = corner_dy(a), az = corner_dz(a);
+  EdgeEnds r;
+  r.ax = corner_dx(a);
+  r.ay = corner_dy(a);
+  r.az = corner_dz(a);
   const int bx = corner_dx(b), by = corner_dy(b), bz = corner_dz(b);
-  const int ia = hidx(x + ax, y + ay, z + az), ib = hidx(x + bx, y + by, z + bz);
-  const float v1 = S.sdf[ia], v2 = S.sdf[ib];
-  const uint32_t c1 = S.rgb[ia], c2 = S.rgb[ib];
-  const float p1x = (float)(gx + ax), p1y = (float)(gy + ay), p1z = (float)(gz + az);
-  const float p2x = (float)(gx + bx), p2y = (float)(gy + by), p2z = (float)(gz + bz);
-  if (fabsf(0.0f - v1) < kSnap) return make_float4(p1x, p1y, p1z, __uint_as_float(c1));
-  if (fabsf(0.0f - v2) < kSnap) return make_float4(p2x, p2y, p2z, __uint_as_float(c2));
-  if (fabsf(v1 - v2) < kSnap) return make_float4(p1x, p1y, p1z, __uint_as_float(c1));
-  const float mu = (0.0f - v1) / (v2 - v1);
-  uint32_t out = 0;
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    const int q1 = (int)((c1 >> (8 * c)) & 0xFFu), q2 = (int)((c2 >> (8 * c)) & 0xFFu);
-    const float v = (float)q1 + mu * (float)(q2 - q1);
-    out |= (__float2uint_rz(v) & 0xFFu) << (8 * c);
+  r.ia = hidx(x + r.ax, y + r.ay, z + r.az);
+  r.ib = hidx(x + bx, y + by, z + bz);
+  r.axis = bx != r.ax ? 0 : (by != r.ay ? 1 : 2);
+  const int d = (bx - r.ax) + (by - r.ay) + (bz - r.az);
+  r.dir = d;
+  return r;
+}
+
+// Vertex of edge e: VertexInterp(p[a], p[b], val[a], val[b])
+// (src/tsdf.cu:1640-1660) in global voxel units; (gx, gy, gz) is the global
+// voxel of staged corner 0.  Corners are one voxel apart along one axis, so
+// p1 + mu * (p2 - p1) changes only that coordinate: the others are
+// p1 + mu * 0 = p1 exactly (mu is finite and >= 0 on a cut edge).
+// With `colour`, the colour is interpolated and truncated like the
+// reference's float-to-uchar store.
+template <bool colour>
+__device__ __forceinline__ float4 mc_vertex(const McShared &S, int e, int x, int y, int z,
+                                           int gx, int gy, int gz) {
+  const EdgeEnds E = edge_ends(e, x, y, z);
+  const float v1 = S.sdf[E.ia], v2 = S.sdf[E.ib];
+  float px = (float)(gx + E.ax), py = (float)(gy + E.ay), pz = (float)(gz + E.az);
+  uint32_t c1 = 0, c2 = 0;
+  if (colour) {
+    c1 = S.rgb[E.ia];
+    c2 = S.rgb[E.ib];
   }
-  return make_float4(p1x + mu * (p2x - p1x), p1y + mu * (p2y - p1y), p1z + mu * (p2z - p1z),
-                     __uint_as_float(out));
+  float mu;
+  bool interp = false;
+  if (fabsf(0.0f - v1) < kSnap) {
+    mu = 0.0f;  // p1
+  } else if (fabsf(0.0f - v2) < kSnap) {
+    mu = 1.0f;  // p2
+  } else if (fabsf(v1 - v2) < kSnap) {
+    mu = 0.0f;  // p1
+  } else {
+    mu = (0.0f - v1) / (v2 - v1);
+    interp = true;
+  }
+  // snapped: move to the chosen corner exactly (integer coordinates)
+  const float step = (float)E.dir;  // p2 - p1 along the axis
+  float moved;
+  if (E.axis == 0) moved = px;
+  else if (E.axis == 1) moved = py;
+  else moved = pz;
+  if (interp)
+    moved = moved + mu * step;
+  else if (mu == 1.0f)
+    moved = moved + step;
+  if (E.axis == 0) px = moved;
+  else if (E.axis == 1) py = moved;
+  else pz = moved;
+  uint32_t out = 0;
+  if (colour) {
+    if (!interp) {
+      out = mu == 1.0f ? c2 : c1;
+    } else {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int q1 = (int)((c1 >> (8 * c)) & 0xFFu), q2 = (int)((c2 >> (8 * c)) & 0xFFu);
+        const float v = (float)q1 + mu * (float)(q2 - q1);
+        out |= (__float2uint_rz(v) & 0xFFu) << (8 * c);
+      }
+    }
+  }
+  return make_float4(px, py, pz, __uint_as_float(out));
 }
 
 // Cube case of the cube with staged corner 0 at (x, y, z); -1 if a corner is
@@ -505,8 +566,8 @@ __device__ __forceinline__ bool same_pos(const float4 &a, const float4 &b) {
   return a.x == b.x && a.y == b.y && a.z == b.z;
 }
 
-// Exclusive CTA-wide scan of `v` (kMcThreads threads); returns the prefix and
-// leaves the total in *total.  Contains __syncthreads.
+// Exclusive CTA-wide scan of `v`; returns the prefix, total in *total.
+// Contains one __syncthreads; the caller separates consecutive scans.
 __device__ __forceinline__ uint32_t cta_scan(McShared &S, uint32_t v, uint32_t *total) {
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   uint32_t incl = v;
@@ -528,12 +589,22 @@ __device__ __forceinline__ uint32_t cta_scan(McShared &S, uint32_t v, uint32_t *
   return before + incl - v;
 }
 
+// Persistent CTAs, one block (plus its +x/+y/+z halo) per iteration:
+//   stage 9^3 corners -> classify 512 cubes -> expand into candidate
+//   triangles (scan) -> one thread per candidate tests the reference's
+//   degenerate-triangle rule -> compact (scan) -> one atomic per block ->
+//   one thread per output float4, contiguous stores.
 __global__ void __launch_bounds__(kMcThreads, 8) k_mc(VolumeView V, int scope_all, float min_weight,
-                                                   float4 *__restrict__ tris, uint32_t tri_cap) {
+                                                      float4 *__restrict__ tris, uint32_t tri_cap) {
   __shared__ McShared S;
   const int t = threadIdx.x;
   for (int i = t; i < 256 * 16; i += kMcThreads) (&S.tri[0][0])[i] = kMcTri[i >> 4][i & 15];
-  for (int i = t; i < 256; i += kMcThreads) S.edge[i] = kMcEdgeMask[i];
+  for (int i = t; i < 256; i += kMcThreads) {
+    S.edge[i] = kMcEdgeMask[i];
+    int n = 0;
+    while (n < 5 && kMcTri[i][3 * n] >= 0) ++n;
+    S.ntri[i] = (uint8_t)n;
+  }
   const uint32_t n = scope_all ? V.st->pool_top : min(V.st->frame_count, V.frame_cap);
   const float nanv = __int_as_float(0x7FC00000);
   for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
@@ -612,76 +683,69 @@ __global__ void __launch_bounds__(kMcThreads, 8) k_mc(VolumeView V, int scope_al
       S.rgb[hidx(x, y, z)] = c;
     }
     __syncthreads();
-    // classify this thread's 4 cubes and compact the active ones
-    uint32_t mine[4];
-    uint32_t cnt = 0;
+    // 1. classify this thread's 4 cubes; count their candidate triangles
+    uint32_t ncand_mine = 0;
+    int cs[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int c = t + kMcThreads * j;
-      const int ci = cube_case(S, c & 7, (c >> 3) & 7, c >> 6);
-      mine[j] = 0xFFFFFFFFu;
-      if (ci > 0 && S.edge[ci] != 0) mine[cnt++] = (uint32_t)c | ((uint32_t)ci << 16);
+      int ci = cube_case(S, c & 7, (c >> 3) & 7, c >> 6);
+      if (ci < 0 || S.edge[ci] == 0) ci = 0;
+      cs[j] = ci;
+      S.cases[c] = (uint8_t)ci;
+      ncand_mine += S.ntri[ci];
     }
-    uint32_t n_active;
-    const uint32_t off = cta_scan(S, cnt, &n_active);
+    uint32_t ncand;
+    uint32_t off = cta_scan(S, ncand_mine, &ncand);
+    if (ncand == 0) continue;  // uniform: nothing to emit in this block
 #pragma unroll
-    for (int j = 0; j < 4; ++j)
-      if ((uint32_t)j < cnt) S.act[off + j] = mine[j];
+    for (int j = 0; j < 4; ++j) {
+      const int c = t + kMcThreads * j;
+      const int nt = S.ntri[cs[j]];
+      for (int tt = 0; tt < nt; ++tt) S.cand[off++] = (uint16_t)(c | (tt << 9));
+    }
+    __syncthreads();
+    // 2. one thread per candidate: the reference drops p0 == p1 || p1 == p2
+    //    (src/tsdf.cu:1055-1057)
     const int gx0 = bx * kB, gy0 = by * kB, gz0 = bz * kB;
-    for (uint32_t r = 0; r < n_active; r += kMcThreads) {
-      __syncthreads();  // act[] written / previous round's prefix consumed
-      // one active cube per thread: valid-triangle mask
-      uint32_t tm = 0, tcount = 0;
-      if (r + t < n_active) {
-        const uint32_t a = S.act[r + t];
-        const int c = (int)(a & 0xFFFFu), ci = (int)(a >> 16);
-        const int x = c & 7, y = (c >> 3) & 7, z = c >> 6;
-        uint32_t m = 0;
-        for (int tt = 0; tt < 5; ++tt) {
-          const int e0 = S.tri[ci][3 * tt];
-          if (e0 < 0) break;
-          const int e1 = S.tri[ci][3 * tt + 1], e2 = S.tri[ci][3 * tt + 2];
-          const float4 p0 = edge_vertex(S, e0, x, y, z, gx0 + x, gy0 + y, gz0 + z);
-          const float4 p1 = edge_vertex(S, e1, x, y, z, gx0 + x, gy0 + y, gz0 + z);
-          const float4 p2 = edge_vertex(S, e2, x, y, z, gx0 + x, gy0 + y, gz0 + z);
-          // the reference drops p0 == p1 || p1 == p2 (src/tsdf.cu:1055-1057)
-          if (!(same_pos(p0, p1) || same_pos(p1, p2))) m |= 1u << tt;
-        }
-        tm = m | ((uint32_t)ci << 8) | ((uint32_t)c << 16);
-        tcount = __popc(m);
+    uint32_t vmask = 0, nvalid_mine = 0;
+    for (uint32_t k = t, m = 0; k < ncand; k += kMcThreads, ++m) {
+      const uint32_t ent = S.cand[k];
+      const int c = (int)(ent & 511u), tt = (int)(ent >> 9);
+      const int x = c & 7, y = (c >> 3) & 7, z = c >> 6;
+      const int ci = S.cases[c];
+      const float4 p0 = mc_vertex<false>(S, S.tri[ci][3 * tt], x, y, z, gx0 + x, gy0 + y, gz0 + z);
+      const float4 p1 =
+          mc_vertex<false>(S, S.tri[ci][3 * tt + 1], x, y, z, gx0 + x, gy0 + y, gz0 + z);
+      const float4 p2 =
+          mc_vertex<false>(S, S.tri[ci][3 * tt + 2], x, y, z, gx0 + x, gy0 + y, gz0 + z);
+      if (!(same_pos(p0, p1) || same_pos(p1, p2))) {
+        vmask |= 1u << m;
+        ++nvalid_mine;
       }
-      uint32_t total;
-      const uint32_t pre = cta_scan(S, tcount, &total);
-      S.prefix[t] = pre;
-      S.tmask[t] = tm;
-      if (t == 0) {
-        S.prefix[kMcThreads] = total;
-        S.base = total ? atomicAdd(&V.st->tri_count, total) : 0u;
-      }
-      __syncthreads();
-      // cooperative, contiguous write of this round's triangles (float4 units);
-      // each output vertex is recomputed from the staged corners
-      const uint32_t base = S.base;
-      for (uint32_t q = t; q < 3u * total; q += kMcThreads) {
-        const uint32_t k = q / 3u, j = q - 3u * k;
-        int lo = 0, hi = kMcThreads;  // owner: last thread with prefix <= k
-        while (hi - lo > 1) {
-          const int mid = (lo + hi) >> 1;
-          if (S.prefix[mid] <= k) lo = mid; else hi = mid;
-        }
-        const uint32_t tmk = S.tmask[lo];
-        uint32_t m = tmk & 0x1Fu;
-        for (uint32_t skip = k - S.prefix[lo]; skip; --skip) m &= m - 1u;
-        const int tt = __ffs(m) - 1;
-        const int ci = (int)((tmk >> 8) & 0xFFu), c = (int)(tmk >> 16);
-        const int x = c & 7, y = (c >> 3) & 7, z = c >> 6;
-        const uint32_t out = base + k;
-        if (out < tri_cap)
-          tris[3 * (size_t)out + j] =
-              edge_vertex(S, S.tri[ci][3 * tt + (int)j], x, y, z, gx0 + x, gy0 + y, gz0 + z);
-        else if (j == 0)
-          atomicOr(&V.st->error, kErrTriCap);
-      }
+    }
+    uint32_t nvalid;
+    off = cta_scan(S, nvalid_mine, &nvalid);
+    for (uint32_t mm = vmask; mm; mm &= mm - 1u) {
+      const uint32_t m = __ffs(mm) - 1;
+      S.valid[off++] = S.cand[t + kMcThreads * m];
+    }
+    if (t == 0) S.base = nvalid ? atomicAdd(&V.st->tri_count, nvalid) : 0u;
+    __syncthreads();
+    // 3. contiguous write, one float4 (vertex) per thread
+    const uint32_t base = S.base;
+    for (uint32_t q = t; q < 3u * nvalid; q += kMcThreads) {
+      const uint32_t k = q / 3u, j = q - 3u * k;
+      const uint32_t ent = S.valid[k];
+      const int c = (int)(ent & 511u), tt = (int)(ent >> 9);
+      const int x = c & 7, y = (c >> 3) & 7, z = c >> 6;
+      const int ci = S.cases[c];
+      const uint32_t out = base + k;
+      if (out < tri_cap)
+        tris[3 * (size_t)out + j] =
+            mc_vertex<true>(S, S.tri[ci][3 * tt + (int)j], x, y, z, gx0 + x, gy0 + y, gz0 + z);
+      else if (j == 0)
+        atomicOr(&V.st->error, kErrTriCap);
     }
   }
 }
@@ -871,9 +935,12 @@ void launch_allocate(const VolumeView &V, const CamParams &C, const void *depth,
     k_allocate<float><<<grid, 256, 0, s>>>(V, C, (const float *)depth, rgb, pose, pix);
 }
 
-int integrate_ctas_per_sm() {
+int integrate_ctas_per_sm(int variant) {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_integrate, 128, 0);
+  if (variant == 1)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_integrate<true>, 128, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_integrate<false>, 128, 0);
   return n > 0 ? n : 1;
 }
 
@@ -884,8 +951,11 @@ int mc_ctas_per_sm() {
 }
 
 void launch_integrate(const VolumeView &V, const CamParams &C, const uint2 *pix, const float *pose,
-                      int grid, cudaStream_t s) {
-  k_integrate<<<grid, 128, 0, s>>>(V, C, pix, pose);
+                      int grid, int variant, cudaStream_t s) {
+  if (variant == 1)
+    k_integrate<true><<<grid, 128, 0, s>>>(V, C, pix, pose);
+  else
+    k_integrate<false><<<grid, 128, 0, s>>>(V, C, pix, pose);
 }
 
 void launch_mc(const VolumeView &V, int scope_all, float min_weight, float4 *tris,

@@ -61,6 +61,11 @@ class VhStats(C.Structure):
     ]
 
 
+class VhTuning(C.Structure):
+    _fields_ = [("integrate_variant", C.c_int32), ("integrate_ctas_per_sm", C.c_int32),
+                ("mc_ctas_per_sm", C.c_int32), ("reserved", C.c_int32)]
+
+
 class VhMeshView(C.Structure):
     _fields_ = [("vertices", C.c_void_p), ("num_triangles", C.c_int64),
                 ("voxel_size", C.c_float)]
@@ -99,6 +104,9 @@ SIGNATURES = {
     "vh_save": (I32, [P, C.c_char_p]),
     "vh_load": (I32, [P, C.c_char_p]),
     "vh_get_stats": (I32, [P, C.POINTER(VhStats)]),
+    "vh_get_tuning": (I32, [P, C.POINTER(VhTuning)]),
+    "vh_set_tuning": (I32, [P, C.POINTER(VhTuning)]),
+    "vh_autotune": (I32, [P, P, I32, P, P, I32, C.POINTER(VhTuning)]),
 }
 
 _lib = None

@@ -109,6 +109,25 @@ class Volume:
         self._check(self._L.vh_process_frame(self._h, d.ptr, _depth_fmt(d.dtype, depth_format),
                                              c.ptr, pose.ctypes.data, d.mem, None))
 
+    # ---- launch tuning ----
+    def tuning(self):
+        t = N.VhTuning()
+        self._check(self._L.vh_get_tuning(self._h, C.byref(t)))
+        return {f: getattr(t, f) for f, _ in N.VhTuning._fields_ if f != "reserved"}
+
+    def set_tuning(self, integrate_variant=0, integrate_ctas_per_sm=0, mc_ctas_per_sm=0):
+        t = N.VhTuning(integrate_variant, integrate_ctas_per_sm, mc_ctas_per_sm, 0)
+        self._check(self._L.vh_set_tuning(self._h, C.byref(t)))
+
+    def autotune(self, depth, rgb, c2w, depth_format=None):
+        """Times the launch configurations on this frame (scratch volume) and
+        applies the fastest; returns it."""
+        d, c, pose = self._frame_args(depth, rgb, c2w)
+        t = N.VhTuning()
+        self._check(self._L.vh_autotune(self._h, d.ptr, _depth_fmt(d.dtype, depth_format), c.ptr,
+                                        pose.ctypes.data, d.mem, C.byref(t)))
+        return {f: getattr(t, f) for f, _ in N.VhTuning._fields_ if f != "reserved"}
+
     def extract(self, scope="frame"):
         """Runs marching cubes; returns (device pointer, triangle count)."""
         view = N.VhMeshView()
