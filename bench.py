@@ -189,7 +189,8 @@ def run_engine(args):
     torch.cuda.set_device(local)
     from vhsdf import Volume, _native as N
 
-    seed = WORKLOAD["scene_seed"] + rank  # independent stream per replica
+    from vhsdf import replicas
+    seed = replicas.stream_seed(WORKLOAD["scene_seed"], rank)  # independent stream per replica
     nframes = args.warmup + args.steps
     scene, frames = make_frames(nframes, seed)
     params = dict(ENGINE_PARAMS, fx=scene.fx, fy=scene.fy, cx=scene.cx, cy=scene.cy,
@@ -236,7 +237,7 @@ def run_engine(args):
 
     # ---- launch tuning (scratch volume, outside any timed region) ----
     tuner = Volume(**params)
-    tuning = tuner.autotune(*frames[0])
+    tuning = tuner.tuning() if args.no_autotune else tuner.autotune(*frames[0])
     tuner.close()
 
     # ---- device-resident pass (value + roofline) ----
@@ -272,10 +273,7 @@ def run_engine(args):
     vol.close()
     e2e_s = sum(wall)
 
-    tot = torch.tensor([dev_ms, e2e_s], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(tot, op=torch.distributed.ReduceOp.MAX)
-    dev_ms, e2e_s = tot.tolist()
+    dev_ms, e2e_s = replicas.reduce_max([dev_ms, e2e_s], device="cuda")
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
@@ -284,13 +282,24 @@ def run_engine(args):
     frames_total = args.steps * world
     value = frames_total / (dev_ms / 1000.0)
     e2e = frames_total / e2e_s
-    # roofline of the integration kernel (the dominant kernel)
-    integ_ms = [s["ms_integrate"] for s in stage]
-    visited = [s["frame_blocks"] * 512 for s in stage]
-    updated = [s["voxels_updated"] for s in stage]
+    # Rooflines.  Algorithmic bytes per launch:
+    #   k_mc        12 B per voxel of every listed block (sdf, weight, rgb read
+    #               once) + 48 B per output triangle (3 x float4 vertex)
+    #   k_integrate 12 B per voxel of every listed block read + 12 B per
+    #               updated voxel written + 8 B per pixel record
+    # DRAM traffic per launch comes from one ncu capture of frames 3-4 of this
+    # stream (60k-block pool): k_mc moved 1.04x and k_integrate 0.87x their
+    # algorithmic bytes; traffic below scales those ratios to this run.
     npx = 640 * 480
-    alg = [12 * v + 12 * u + 8 * npx for v, u in zip(visited, updated)]
-    achieved = sum(alg) / (sum(integ_ms) / 1000.0) / 1e9
+    blocks = [s["frame_blocks"] for s in stage]
+    updated = [s["voxels_updated"] for s in stage]
+    tris = [s["triangles"] for s in stage]
+    mc_alg = [12 * 512 * b + 48 * t for b, t in zip(blocks, tris)]
+    in_alg = [12 * 512 * b + 12 * u + 8 * npx for b, u in zip(blocks, updated)]
+    mc_ms = [s["ms_extract"] for s in stage]
+    in_ms = [s["ms_integrate"] for s in stage]
+    mc_ach = sum(mc_alg) / (sum(mc_ms) / 1000.0) / 1e9
+    in_ach = sum(in_alg) / (sum(in_ms) / 1000.0) / 1e9
     peak, peak_src = peak_hbm()
     cpu = cpu_leg(frames, scene, seconds=args.cpu_seconds)
     res = {
@@ -302,14 +311,18 @@ def run_engine(args):
         "e2e": {"value": e2e, "unit": UNIT,
                 "h2d_bytes_per_step": 2 * npx + 3 * npx + 64,
                 "d2h_bytes_per_step": 64},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
-                     "kernel": "k_integrate", "peak_source": peak_src},
+        "roofline": {"bound": "hbm", "achieved": mc_ach, "peak": peak, "unit": "GB/s",
+                     "frac": mc_ach / peak, "traffic": 1.04 * statistics.mean(mc_alg),
+                     "kernel": "k_mc", "peak_source": peak_src,
+                     "algorithmic_bytes": statistics.mean(mc_alg)},
+        "roofline_integrate": {"bound": "hbm", "achieved": in_ach, "peak": peak, "unit": "GB/s",
+                               "frac": in_ach / peak, "traffic": 0.87 * statistics.mean(in_alg),
+                               "kernel": "k_integrate", "peak_source": peak_src,
+                               "algorithmic_bytes": statistics.mean(in_alg)},
         "stages_ms": {k: statistics.mean(s[k] for s in stage)
                       for k in ("ms_allocate", "ms_integrate", "ms_extract", "ms_frame")},
-        "per_frame": {"blocks": statistics.mean(s["frame_blocks"] for s in stage),
-                      "voxels_updated": statistics.mean(updated),
-                      "triangles": statistics.mean(s["triangles"] for s in stage)},
+        "per_frame": {"blocks": statistics.mean(blocks), "voxels_updated": statistics.mean(updated),
+                      "triangles": statistics.mean(tris)},
         "gpu_launches": 6 * args.steps,
         "tuning": tuning,
         "wall_s": t_wall,
@@ -328,6 +341,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="use the default launch configuration (for profiling runs)")
     ap.add_argument("--pool-blocks", type=int, default=0,
                     help="smaller block pool (for short profiling runs)")
     args = ap.parse_args()

@@ -1,0 +1,166 @@
+/*
+ * ark_tsdf.h - header-only C++ front end with the reference's class name and
+ * method signatures, forwarding to the C ABI in vhsdf.h.
+ *
+ * A caller written against ark::GpuTsdfGenerator (include/tsdf.cuh:548-683 of
+ * E-BAO/Voxel-Hashing-SDF), such as PointCloudGenerator::Reproject
+ * (src/PointCloudGenerator.cpp:93-129), compiles unchanged against this
+ * header and links against libvhsdf.so.
+ *
+ * Differences a caller can observe:
+ *   - blocks are 8^3 voxels and the volume stays resident on the GPU;
+ *   - processFrame allocates the blocks of every pixel's truncation band
+ *     (the reference walks subsampled rays) and averages sdf with the old
+ *     weight (the reference uses the new one, src/tsdf.cu:739-742);
+ *   - render() draws nothing: OpenGL is not available (it sets last_status);
+ *   - errors never exit the process: every method records a vh_status in
+ *     last_status() and processFrame returns it instead of aborting.
+ */
+#ifndef ARK_TSDF_H
+#define ARK_TSDF_H
+
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "vhsdf.h"
+
+namespace ark {
+
+/* include/tsdf.cuh:65-77: position and colour of one mesh vertex. */
+struct Vertex {
+  float x, y, z;
+  unsigned char r, g, b;
+};
+
+/* include/tsdf.cuh:111-113 */
+struct Face {
+  int vIdx[3];
+};
+
+class GpuTsdfGenerator {
+ public:
+  /* include/tsdf.cuh:606-607, defaults src/tsdf.cu:1249-1252.  origin and
+   * vox_dim describe the reference's unused dense grid and are ignored. */
+  GpuTsdfGenerator(int width, int height, float fx, float fy, float cx, float cy,
+                   float max_depth, float origin_x = -1.5f, float origin_y = -1.5f,
+                   float origin_z = 0.5f, float vox_size = 0.006f, float trunc_m = 0.03f,
+                   int vox_dim_x = 500, int vox_dim_y = 500, int vox_dim_z = 500) {
+    (void)origin_x;
+    (void)origin_y;
+    (void)origin_z;
+    (void)vox_dim_x;
+    (void)vox_dim_y;
+    (void)vox_dim_z;
+    vh_params_default(&params_);
+    params_.width = width;
+    params_.height = height;
+    params_.fx = fx;
+    params_.fy = fy;
+    params_.cx = cx;
+    params_.cy = cy;
+    params_.max_depth = max_depth;
+    params_.voxel_size = vox_size;
+    params_.trunc = trunc_m;
+    status_ = vh_create(&params_, &handle_);
+  }
+
+  ~GpuTsdfGenerator() { Shutdown(); }
+  GpuTsdfGenerator(const GpuTsdfGenerator &) = delete;
+  GpuTsdfGenerator &operator=(const GpuTsdfGenerator &) = delete;
+
+  /* include/tsdf.cuh:610: depth H*W float metres, rgb H*W*3 (RGB order),
+   * c2w row-major 4x4 camera-to-world, all host memory. */
+  vh_status processFrame(float *depth, unsigned char *rgb, float *c2w) {
+    if (!handle_) return status_ = VH_ERR_INVALID_ARG;
+    status_ = vh_process_frame(handle_, depth, VH_DEPTH_F32_M, rgb, c2w, VH_MEM_HOST, nullptr);
+    mesh_valid_ = false;
+    return status_;
+  }
+
+  /* include/tsdf.cuh:628: full-volume mesh as ASCII PLY. */
+  void SavePLY(std::string filename) {
+    status_ = handle_ ? vh_save_ply(handle_, filename.c_str(), 0) : VH_ERR_INVALID_ARG;
+  }
+
+  /* include/tsdf.cuh:619: needs OpenGL, which this engine does not use. */
+  void render() { status_ = handle_ ? vh_render(handle_) : VH_ERR_INVALID_ARG; }
+
+  /* include/tsdf.cuh:622 */
+  void Shutdown() {
+    if (handle_) vh_destroy(handle_);
+    handle_ = nullptr;
+  }
+
+  /* include/tsdf.cuh:631-634: vertices (metres) and faces of the full-volume
+   * mesh, vertices merged by exact position like tsdf2mesh. */
+  std::vector<Vertex> *getVertices() {
+    build_mesh();
+    return &vertices_;
+  }
+  std::vector<Face> *getFaces() {
+    build_mesh();
+    return &faces_;
+  }
+
+  vh_status last_status() const { return status_; }
+  vh_handle *handle() { return handle_; }
+
+ private:
+  void build_mesh() {
+    if (mesh_valid_ || !handle_) return;
+    vertices_.clear();
+    faces_.clear();
+    status_ = vh_extract(handle_, VH_SCOPE_ALL, nullptr);
+    if (status_ != VH_OK) return;
+    int64_t n = 0;
+    vh_copy_mesh(handle_, nullptr, nullptr, 0, &n);
+    std::vector<float> xyz((size_t)n * 9);
+    std::vector<unsigned char> rgb((size_t)n * 9);
+    status_ = vh_copy_mesh(handle_, xyz.data(), rgb.data(), n, &n);
+    if (status_ != VH_OK) return;
+    struct Key {
+      float x, y, z;
+      bool operator==(const Key &o) const { return x == o.x && y == o.y && z == o.z; }
+    };
+    struct Hash {
+      size_t operator()(const Key &k) const {
+        uint32_t a, b, c;
+        std::memcpy(&a, &k.x, 4);
+        std::memcpy(&b, &k.y, 4);
+        std::memcpy(&c, &k.z, 4);
+        return (size_t)a * 73856093u ^ (size_t)b * 19349669u ^ (size_t)c * 83492791u;
+      }
+    };
+    std::unordered_map<Key, int, Hash> index;
+    for (int64_t t = 0; t < n; ++t) {
+      Face f;
+      for (int j = 0; j < 3; ++j) {
+        const float *p = &xyz[9 * t + 3 * j];
+        Key k{p[0], p[1], p[2]};
+        auto it = index.find(k);
+        if (it == index.end()) {
+          it = index.emplace(k, (int)vertices_.size()).first;
+          const unsigned char *c = &rgb[9 * t + 3 * j];
+          vertices_.push_back(Vertex{p[0] * params_.voxel_size, p[1] * params_.voxel_size,
+                                     p[2] * params_.voxel_size, c[0], c[1], c[2]});
+        }
+        f.vIdx[j] = it->second;
+      }
+      faces_.push_back(f);
+    }
+    mesh_valid_ = true;
+  }
+
+  vh_params params_{};
+  vh_handle *handle_ = nullptr;
+  vh_status status_ = VH_OK;
+  bool mesh_valid_ = false;
+  std::vector<Vertex> vertices_;
+  std::vector<Face> faces_;
+};
+
+}  // namespace ark
+
+#endif /* ARK_TSDF_H */
