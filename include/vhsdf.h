@@ -203,6 +203,23 @@ vh_status vh_alloc_keys(vh_handle *h, const int32_t *xyz, int64_t n,
  * (include/vhashing.h:128-131). */
 vh_status vh_find_keys(vh_handle *h, const int32_t *xyz, int64_t n,
                        int32_t *out_block, int32_t mem);
+/* Maximum keys per vh_find_keys_noalloc call. */
+#define VH_FIND_NOALLOC_MAX_KEYS 65536
+
+/* vh_find_keys for host buffers that allocates no device memory; it has no
+ * counterpart in the reference.  For callers that must not call cudaMalloc
+ * or cudaFree (a latency-bound loop cannot take cudaFree's device-wide
+ * synchronisation; a plugin whose host owns all device memory may not
+ * allocate).  xyz and out_block are host memory; out_block[i] is the pool
+ * index of key i or -1, as vh_find_keys.  At most VH_FIND_NOALLOC_MAX_KEYS
+ * keys per call, else VH_ERR_CAPACITY.  Its scratch is a fixed 1 MiB array
+ * that every GPU loading this library holds until the process exits; the
+ * first call on a device looks up that array's address, so make the first
+ * call before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU (other threads, other handles on the same GPU) race and
+ * must be serialised by the caller.  The call waits for its result. */
+vh_status vh_find_keys_noalloc(vh_handle *h, const int32_t *xyz, int64_t n,
+                               int32_t *out_block);
 /* Erases n keys and recycles their blocks (zeroed): replaces
  * HashTable::erase (include/vhashing.h:244-256). */
 vh_status vh_erase_keys(vh_handle *h, const int32_t *xyz, int64_t n,

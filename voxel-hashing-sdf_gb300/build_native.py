@@ -31,8 +31,9 @@ ENGINE_SOURCES = [
     ("vh_kernels.cu", KERNEL_FLAGS),
     ("vh_api.cpp", []),
     ("vh_mesh.cpp", []),
+    ("vh_noalloc.cu", []),
 ]
-ENGINE_HEADERS = ["vh_common.cuh", "vh_mc_tables.h", "vh_mesh.h"]
+ENGINE_HEADERS = ["vh_common.cuh", "vh_mc_tables.h", "vh_mesh.h", "vh_internal.h"]
 
 ENGINE_LIB = os.path.join(LIB, "libvhsdf.so")
 SYNTH_LIB = os.path.join(LIB, "libvhsynth.so")

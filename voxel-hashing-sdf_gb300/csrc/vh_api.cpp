@@ -23,6 +23,7 @@
 
 #include "../../include/vhsdf.h"
 #include "vh_common.cuh"
+#include "vh_internal.h"
 #include "vh_mesh.h"
 
 using namespace vh;
@@ -343,6 +344,14 @@ vh_status grow_tris(vh_handle *h, int64_t need) {
 }
 
 }  // namespace
+
+namespace vh {
+VolumeView handle_view(const vh_handle *h) { return h->V; }
+cudaStream_t handle_stream(const vh_handle *h) { return h->stream; }
+int handle_device(const vh_handle *h) { return h->p.device; }
+vh_status handle_fail(vh_handle *h, vh_status s, const char *msg) { return fail(h, s, msg); }
+vh_status handle_sync(vh_handle *h) { return sync_and_check(h); }
+}  // namespace vh
 
 extern "C" {
 

@@ -1,0 +1,15 @@
+// vh_internal.h - handle accessors for entry points implemented outside
+// vh_api.cpp (host code only).
+#pragma once
+#include "../../include/vhsdf.h"
+#include "vh_common.cuh"
+
+namespace vh {
+VolumeView handle_view(const vh_handle *h);
+cudaStream_t handle_stream(const vh_handle *h);
+int handle_device(const vh_handle *h);
+// Records `msg` as the handle's last error and returns `s`.
+vh_status handle_fail(vh_handle *h, vh_status s, const char *msg);
+// Waits for the handle's stream and reports sticky device errors.
+vh_status handle_sync(vh_handle *h);
+}  // namespace vh

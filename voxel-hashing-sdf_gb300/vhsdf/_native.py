@@ -95,6 +95,7 @@ SIGNATURES = {
     "vh_render": (I32, [P]),
     "vh_alloc_keys": (I32, [P, P, I64, I32]),
     "vh_find_keys": (I32, [P, P, I64, P, I32]),
+    "vh_find_keys_noalloc": (I32, [P, P, I64, P]),
     "vh_erase_keys": (I32, [P, P, I64, PI64, I32]),
     "vh_clear_block_list": (I32, [P]),
     "vh_block_list": (I32, [P, P, I64, PI64]),
