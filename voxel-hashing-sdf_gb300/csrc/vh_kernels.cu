@@ -309,12 +309,49 @@ __global__ void __launch_bounds__(256) k_allocate(VolumeView V, CamParams C,
 }
 
 // ---- integration ---------------------------------------------------------------
+// Colour running average of IntegrateHashKernel (src/tsdf.cu:743-745):
+// per channel trunc(fp32((c_old * w_old + c_new) / w_new)).  While
+// w_old <= 65536 the numerator n = c_old * w_old + c_new is an integer below
+// 2^24, exact in fp32, and the fp32 quotient of two integers with divisor
+// w <= 131072 truncates to floor(n / w): it cannot round up to the next
+// integer (that needs n / w within 2^-17 of it, but it differs from any
+// integer by at least 1 / w) nor down past one.  floor(n / w) is then taken
+// from a reciprocal estimate (error < 1) corrected by one exact integer
+// remainder test.  Larger weights use the fp32 formula itself.
+__device__ __forceinline__ uint32_t blend_colour(uint32_t old_rgb, uint32_t new_rgb, float w_old,
+                                                 float w_new) {
+  uint32_t out = 0;
+  if (w_old <= 65536.0f) {
+    const uint32_t wo = (uint32_t)w_old, wn = wo + 1u;
+    const float r = __fdividef(1.0f, w_new);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const uint32_t n = ((old_rgb >> (8 * c)) & 0xFFu) * wo + ((new_rgb >> (8 * c)) & 0xFFu);
+      uint32_t q = __float2uint_rz((float)n * r);
+      const int rem = (int)(n - q * wn);
+      q = rem < 0 ? q - 1u : (rem >= (int)wn ? q + 1u : q);
+      out |= (q & 0xFFu) << (8 * c);
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float old_c = (float)((old_rgb >> (8 * c)) & 0xFFu);
+      const float new_c = (float)((new_rgb >> (8 * c)) & 0xFFu);
+      const float v = (old_c * w_old + new_c) / w_new;
+      out |= (__float2uint_rz(v) & 0xFFu) << (8 * c);
+    }
+  }
+  return out;
+}
+
 // One voxel of IntegrateHashKernel (src/tsdf.cu:690-745), sdf averaged with
 // the old weight.
-__device__ __forceinline__ bool update_voxel(const CamParams &C, const float P[12],
-                                             const uint2 *__restrict__ pix, float wx, float wy,
-                                             float wz, float &sdf, float &wt, uint32_t &rgb) {
-  // base2cam (src/tsdf.cu:81-93)
+// Projection of one voxel centre (base2cam src/tsdf.cu:81-93, cam2frame
+// src/tsdf.cu:75-79): returns the pixel index or -1 (behind the camera or
+// outside the image), and the camera-frame z.  Branch-free so that the
+// pixel gathers of a thread's four voxels can be issued together.
+__device__ __forceinline__ int project_voxel(const CamParams &C, const float P[12], float wx,
+                                             float wy, float wz, float &z_out) {
   const float t0 = wx - P[3], t1 = wy - P[7], t2 = wz - P[11];
   float x = P[0] * t0;
   x = x + P[4] * t1;
@@ -325,12 +362,17 @@ __device__ __forceinline__ bool update_voxel(const CamParams &C, const float P[1
   float z = P[2] * t0;
   z = z + P[6] * t1;
   z = z + P[10] * t2;
-  if (!(z > 0.0f)) return false;
-  // cam2frame (src/tsdf.cu:75-79)
+  z_out = z;
   const float uf = roundf(C.fx * (x / z) + C.cx);
   const float vf = roundf(C.fy * (y / z) + C.cy);
-  if (!(uf >= 0.0f && uf < C.wf && vf >= 0.0f && vf < C.hf)) return false;
-  const uint2 px = __ldg(pix + (int)vf * C.width + (int)uf);
+  const bool ok = z > 0.0f && uf >= 0.0f && uf < C.wf && vf >= 0.0f && vf < C.hf;
+  return ok ? (int)vf * C.width + (int)uf : -1;
+}
+
+// Update of one voxel from its pixel (src/tsdf.cu:715-745), sdf averaged
+// with the old weight.
+__device__ __forceinline__ bool update_voxel(const CamParams &C, uint2 px, float z, float &sdf,
+                                             float &wt, uint32_t &rgb) {
   const float d = __uint_as_float(px.x);
   if (!(d > 0.0f && d <= C.max_depth)) return false;
   const float diff = d - z;
@@ -339,17 +381,32 @@ __device__ __forceinline__ bool update_voxel(const CamParams &C, const float P[1
   const float w_old = wt;
   const float w_new = w_old + 1.0f;
   sdf = (sdf * w_old + dist) / w_new;
-  uint32_t out = 0;
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    const float old_c = (float)((rgb >> (8 * c)) & 0xFFu);
-    const float new_c = (float)((px.y >> (8 * c)) & 0xFFu);
-    const float v = (old_c * w_old + new_c) / w_new;
-    out |= (__float2uint_rz(v) & 0xFFu) << (8 * c);
-  }
-  rgb = out;
+  rgb = blend_colour(rgb, px.y, w_old, w_new);
   wt = w_new;
   return true;
+}
+
+// One thread's quad of 4 voxels along x: project all, gather all pixels,
+// then update.  Returns the number of voxels updated.
+__device__ __forceinline__ uint32_t update_quad(const CamParams &C, const float P[12],
+                                                const uint2 *__restrict__ pix, int ix, float wy,
+                                                float wz, float4 &sdf, float4 &wt, uint4 &rgb) {
+  float z0, z1, z2, z3;
+  const int i0 = project_voxel(C, P, (float)(ix + 0) * C.voxel, wy, wz, z0);
+  const int i1 = project_voxel(C, P, (float)(ix + 1) * C.voxel, wy, wz, z1);
+  const int i2 = project_voxel(C, P, (float)(ix + 2) * C.voxel, wy, wz, z2);
+  const int i3 = project_voxel(C, P, (float)(ix + 3) * C.voxel, wy, wz, z3);
+  const uint2 none = make_uint2(0u, 0u);  // depth 0 = invalid
+  const uint2 p0 = i0 >= 0 ? __ldg(pix + i0) : none;
+  const uint2 p1 = i1 >= 0 ? __ldg(pix + i1) : none;
+  const uint2 p2 = i2 >= 0 ? __ldg(pix + i2) : none;
+  const uint2 p3 = i3 >= 0 ? __ldg(pix + i3) : none;
+  uint32_t n = 0;
+  n += update_voxel(C, p0, z0, sdf.x, wt.x, rgb.x);
+  n += update_voxel(C, p1, z1, sdf.y, wt.y, rgb.y);
+  n += update_voxel(C, p2, z2, sdf.z, wt.z, rgb.z);
+  n += update_voxel(C, p3, z3, sdf.w, wt.w, rgb.w);
+  return n;
 }
 
 // Loads the slot of frame-list entry i and the block's voxel quad of thread t.
@@ -417,12 +474,8 @@ __global__ void __launch_bounds__(128) k_integrate(VolumeView V, CamParams C,
       unpack_key(cur.key, bx, by, bz);
       const float wy = (float)(by * kB + y) * C.voxel;
       const float wz = (float)(bz * kB + z) * C.voxel;
-      const int ix = bx * kB + x0;
-      const bool a0 = update_voxel(C, P, pix, (float)(ix + 0) * C.voxel, wy, wz, cur.sdf.x, cur.wt.x, cur.rgb.x);
-      const bool a1 = update_voxel(C, P, pix, (float)(ix + 1) * C.voxel, wy, wz, cur.sdf.y, cur.wt.y, cur.rgb.y);
-      const bool a2 = update_voxel(C, P, pix, (float)(ix + 2) * C.voxel, wy, wz, cur.sdf.z, cur.wt.z, cur.rgb.z);
-      const bool a3 = update_voxel(C, P, pix, (float)(ix + 3) * C.voxel, wy, wz, cur.sdf.w, cur.wt.w, cur.rgb.w);
-      const uint32_t nu = (uint32_t)a0 + a1 + a2 + a3;
+      const uint32_t nu =
+          update_quad(C, P, pix, bx * kB + x0, wy, wz, cur.sdf, cur.wt, cur.rgb);
       if (nu) {
         float *base = V.pool + (size_t)cur.block * kBlockWords;
         reinterpret_cast<float4 *>(base)[t] = cur.sdf;
@@ -448,12 +501,13 @@ constexpr int kMaxCand = kB3 * 5;  // at most 5 triangles per cube
 struct McShared {
   float sdf[kH3];  // NaN = corner unusable (absent block or low weight)
   uint32_t rgb[kH3];
-  int8_t tri[256][16];
+  uint16_t tri[256][5];  // triangle t of a case: edges e0 | e1 << 4 | e2 << 8
   uint16_t edge[256];
   uint8_t ntri[256];
+  uint32_t einfo[12];    // per edge, see edge_info()
   uint8_t cases[kB3];        // cube case, 0 when the cube emits nothing
   uint16_t cand[kMaxCand];   // candidate triangles: cube | triangle << 9
-  uint16_t valid[kMaxCand];  // candidates that survive the degenerate test
+  uint32_t halo[kHalo];      // halo voxel: staged index | neighbour << 10 | voxel << 13
   uint32_t nb[8];
   uint32_t warp_sum[kMcThreads / 32];
   int key[3];
@@ -465,29 +519,21 @@ __device__ __forceinline__ int corner_dx(int k) { return (kMcCornerBitsX >> k) &
 __device__ __forceinline__ int corner_dy(int k) { return (kMcCornerBitsY >> k) & 1; }
 __device__ __forceinline__ int corner_dz(int k) { return (kMcCornerBitsZ >> k) & 1; }
 
-// Corners a -> b of edge e of the cube with staged corner 0 at (x, y, z).
-struct EdgeEnds {
-  int ia, ib;     // staged indices
-  int ax, ay, az; // offset of corner a
-  int axis;       // axis along which b differs from a
-  int dir;        // +1 or -1
-};
-
-__device__ __forceinline__ EdgeEnds edge_ends(int e, int x, int y, int z) {
+// Per-edge constants, packed: staged-index offset of corner a (7 bits) and
+// of corner b (7 bits), corner a's offset bits x | y << 1 | z << 2 (3 bits),
+// the axis along which the edge runs (2 bits) and whether it runs towards
+// -axis (1 bit).
+__device__ __forceinline__ uint32_t edge_info(int e) {
   const uint32_t code =
       (uint32_t)((e < 8 ? kMcEdgeCodeLo >> (8 * e) : kMcEdgeCodeHi >> (8 * (e - 8))) & 0x3Fu);
   const int a = (int)(code & 7u), b = (int)(code >> 3);
-  EdgeEnds r;
-  r.ax = corner_dx(a);
-  r.ay = corner_dy(a);
-  r.az = corner_dz(a);
+  const int ax = corner_dx(a), ay = corner_dy(a), az = corner_dz(a);
   const int bx = corner_dx(b), by = corner_dy(b), bz = corner_dz(b);
-  r.ia = hidx(x + r.ax, y + r.ay, z + r.az);
-  r.ib = hidx(x + bx, y + by, z + bz);
-  r.axis = bx != r.ax ? 0 : (by != r.ay ? 1 : 2);
-  const int d = (bx - r.ax) + (by - r.ay) + (bz - r.az);
-  r.dir = d;
-  return r;
+  const uint32_t oa = (uint32_t)hidx(ax, ay, az), ob = (uint32_t)hidx(bx, by, bz);
+  const uint32_t axis = bx != ax ? 0u : (by != ay ? 1u : 2u);
+  const uint32_t neg = (bx - ax) + (by - ay) + (bz - az) < 0 ? 1u : 0u;
+  return oa | (ob << 7) | ((uint32_t)(ax | (ay << 1) | (az << 2)) << 14) | (axis << 17) |
+         (neg << 19);
 }
 
 // Vertex of edge e: VertexInterp(p[a], p[b], val[a], val[b])
@@ -498,45 +544,41 @@ __device__ __forceinline__ EdgeEnds edge_ends(int e, int x, int y, int z) {
 // With `colour`, the colour is interpolated and truncated like the
 // reference's float-to-uchar store.
 template <bool colour>
-__device__ __forceinline__ float4 mc_vertex(const McShared &S, int e, int x, int y, int z,
-                                           int gx, int gy, int gz) {
-  const EdgeEnds E = edge_ends(e, x, y, z);
-  const float v1 = S.sdf[E.ia], v2 = S.sdf[E.ib];
-  float px = (float)(gx + E.ax), py = (float)(gy + E.ay), pz = (float)(gz + E.az);
-  uint32_t c1 = 0, c2 = 0;
-  if (colour) {
-    c1 = S.rgb[E.ia];
-    c2 = S.rgb[E.ib];
-  }
-  float mu;
+__device__ __forceinline__ float4 mc_vertex(const McShared &S, int e, int h0, int gx, int gy,
+                                           int gz) {
+  const uint32_t info = S.einfo[e];
+  const int ia = h0 + (int)(info & 127u), ib = h0 + (int)((info >> 7) & 127u);
+  const float v1 = S.sdf[ia], v2 = S.sdf[ib];
+  float p[3] = {(float)(gx + (int)((info >> 14) & 1u)), (float)(gy + (int)((info >> 15) & 1u)),
+                (float)(gz + (int)((info >> 16) & 1u))};
+  const int axis = (int)((info >> 17) & 3u);
+  const float step = (info >> 19) ? -1.0f : 1.0f;  // p2 - p1 along the axis
+  float mu = 0.0f;
   bool interp = false;
+  bool to_b = false;
   if (fabsf(0.0f - v1) < kSnap) {
-    mu = 0.0f;  // p1
+    // p1
   } else if (fabsf(0.0f - v2) < kSnap) {
-    mu = 1.0f;  // p2
+    to_b = true;  // p2
   } else if (fabsf(v1 - v2) < kSnap) {
-    mu = 0.0f;  // p1
+    // p1
   } else {
     mu = (0.0f - v1) / (v2 - v1);
     interp = true;
   }
-  // snapped: move to the chosen corner exactly (integer coordinates)
-  const float step = (float)E.dir;  // p2 - p1 along the axis
-  float moved;
-  if (E.axis == 0) moved = px;
-  else if (E.axis == 1) moved = py;
-  else moved = pz;
+  float moved = axis == 0 ? p[0] : (axis == 1 ? p[1] : p[2]);
   if (interp)
     moved = moved + mu * step;
-  else if (mu == 1.0f)
+  else if (to_b)
     moved = moved + step;
-  if (E.axis == 0) px = moved;
-  else if (E.axis == 1) py = moved;
-  else pz = moved;
+  const float px = axis == 0 ? moved : p[0];
+  const float py = axis == 1 ? moved : p[1];
+  const float pz = axis == 2 ? moved : p[2];
   uint32_t out = 0;
   if (colour) {
+    const uint32_t c1 = S.rgb[ia], c2 = S.rgb[ib];
     if (!interp) {
-      out = mu == 1.0f ? c2 : c1;
+      out = to_b ? c2 : c1;
     } else {
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
@@ -598,12 +640,35 @@ __global__ void __launch_bounds__(kMcThreads, 8) k_mc(VolumeView V, int scope_al
                                                       float4 *__restrict__ tris, uint32_t tri_cap) {
   __shared__ McShared S;
   const int t = threadIdx.x;
-  for (int i = t; i < 256 * 16; i += kMcThreads) (&S.tri[0][0])[i] = kMcTri[i >> 4][i & 15];
   for (int i = t; i < 256; i += kMcThreads) {
     S.edge[i] = kMcEdgeMask[i];
     int n = 0;
-    while (n < 5 && kMcTri[i][3 * n] >= 0) ++n;
+    for (; n < 5 && kMcTri[i][3 * n] >= 0; ++n)
+      S.tri[i][n] = (uint16_t)(kMcTri[i][3 * n] | (kMcTri[i][3 * n + 1] << 4) |
+                               (kMcTri[i][3 * n + 2] << 8));
+    for (int m = n; m < 5; ++m) S.tri[i][m] = 0;
     S.ntri[i] = (uint8_t)n;
+  }
+  if (t < 12) S.einfo[t] = edge_info(t);
+  // halo: x == 8 (81), then y == 8 with x < 8 (72), then z == 8 with x, y < 8 (64)
+  for (int hh = t; hh < kHalo; hh += kMcThreads) {
+    int x, y, z;
+    if (hh < 81) {
+      x = 8;
+      y = hh % 9;
+      z = hh / 9;
+    } else if (hh < 153) {
+      x = (hh - 81) & 7;
+      y = 8;
+      z = (hh - 81) >> 3;
+    } else {
+      x = (hh - 153) & 7;
+      y = (hh - 153) >> 3;
+      z = 8;
+    }
+    const uint32_t nbi = (uint32_t)((x >> 3) | ((y >> 3) << 1) | ((z >> 3) << 2));
+    const uint32_t li = (uint32_t)((x & 7) + 8 * (y & 7) + 64 * (z & 7));
+    S.halo[hh] = (uint32_t)hidx(x, y, z) | (nbi << 10) | (li << 13);
   }
   const uint32_t n = scope_all ? V.st->pool_top : min(V.st->frame_count, V.frame_cap);
   const float nanv = __int_as_float(0x7FC00000);
@@ -652,35 +717,19 @@ __global__ void __launch_bounds__(kMcThreads, 8) k_mc(VolumeView V, int scope_al
       S.rgb[h + 3] = cl.w;
     }
     __syncthreads();  // S.nb complete
-    // halo: x == 8 (81), then y == 8 with x < 8 (72), then z == 8 with x, y < 8 (64)
     for (int hh = t; hh < kHalo; hh += kMcThreads) {
-      int x, y, z;
-      if (hh < 81) {
-        x = 8;
-        y = hh % 9;
-        z = hh / 9;
-      } else if (hh < 153) {
-        const int q = hh - 81;
-        x = q & 7;
-        y = 8;
-        z = q >> 3;
-      } else {
-        const int q = hh - 153;
-        x = q & 7;
-        y = q >> 3;
-        z = 8;
-      }
-      const uint32_t blk = S.nb[(x >> 3) | ((y >> 3) << 1) | ((z >> 3) << 2)];
+      const uint32_t info = S.halo[hh];
+      const uint32_t blk = S.nb[(info >> 10) & 7u];
+      const int h = (int)(info & 1023u), li = (int)(info >> 13);
       float v = nanv;
       uint32_t c = 0;
       if (blk != kNoBlock) {
         const float *base = V.pool + (size_t)blk * kBlockWords;
-        const int li = (x & 7) + 8 * (y & 7) + 64 * (z & 7);
         v = __ldg(base + kB3 + li) >= min_weight ? __ldg(base + li) : nanv;
         c = __ldg(reinterpret_cast<const uint32_t *>(base + 2 * kB3) + li);
       }
-      S.sdf[hidx(x, y, z)] = v;
-      S.rgb[hidx(x, y, z)] = c;
+      S.sdf[h] = v;
+      S.rgb[h] = c;
     }
     __syncthreads();
     // 1. classify this thread's 4 cubes; count their candidate triangles
@@ -705,47 +754,42 @@ __global__ void __launch_bounds__(kMcThreads, 8) k_mc(VolumeView V, int scope_al
       for (int tt = 0; tt < nt; ++tt) S.cand[off++] = (uint16_t)(c | (tt << 9));
     }
     __syncthreads();
-    // 2. one thread per candidate: the reference drops p0 == p1 || p1 == p2
-    //    (src/tsdf.cu:1055-1057)
+    // 2. candidates in rounds of one per thread: the thread computes its
+    //    candidate's three vertices once, the reference's degenerate test
+    //    drops p0 == p1 || p1 == p2 (src/tsdf.cu:1055-1057), a CTA scan over
+    //    the survivors gives each a slot in one contiguous range reserved
+    //    with a single atomic, and the thread writes its 48-byte triangle.
     const int gx0 = bx * kB, gy0 = by * kB, gz0 = bz * kB;
-    uint32_t vmask = 0, nvalid_mine = 0;
-    for (uint32_t k = t, m = 0; k < ncand; k += kMcThreads, ++m) {
-      const uint32_t ent = S.cand[k];
-      const int c = (int)(ent & 511u), tt = (int)(ent >> 9);
-      const int x = c & 7, y = (c >> 3) & 7, z = c >> 6;
-      const int ci = S.cases[c];
-      const float4 p0 = mc_vertex<false>(S, S.tri[ci][3 * tt], x, y, z, gx0 + x, gy0 + y, gz0 + z);
-      const float4 p1 =
-          mc_vertex<false>(S, S.tri[ci][3 * tt + 1], x, y, z, gx0 + x, gy0 + y, gz0 + z);
-      const float4 p2 =
-          mc_vertex<false>(S, S.tri[ci][3 * tt + 2], x, y, z, gx0 + x, gy0 + y, gz0 + z);
-      if (!(same_pos(p0, p1) || same_pos(p1, p2))) {
-        vmask |= 1u << m;
-        ++nvalid_mine;
+    for (uint32_t r0 = 0; r0 < ncand; r0 += kMcThreads) {
+      const uint32_t k = r0 + t;
+      float4 p0, p1, p2;
+      uint32_t ok = 0;
+      if (k < ncand) {
+        const uint32_t ent = S.cand[k];
+        const int c = (int)(ent & 511u), tt = (int)(ent >> 9);
+        const int x = c & 7, y = (c >> 3) & 7, z = c >> 6;
+        const uint32_t tri = S.tri[S.cases[c]][tt];
+        const int h0 = hidx(x, y, z);
+        p0 = mc_vertex<true>(S, (int)(tri & 15u), h0, gx0 + x, gy0 + y, gz0 + z);
+        p1 = mc_vertex<true>(S, (int)((tri >> 4) & 15u), h0, gx0 + x, gy0 + y, gz0 + z);
+        p2 = mc_vertex<true>(S, (int)(tri >> 8), h0, gx0 + x, gy0 + y, gz0 + z);
+        ok = !(same_pos(p0, p1) || same_pos(p1, p2));
       }
-    }
-    uint32_t nvalid;
-    off = cta_scan(S, nvalid_mine, &nvalid);
-    for (uint32_t mm = vmask; mm; mm &= mm - 1u) {
-      const uint32_t m = __ffs(mm) - 1;
-      S.valid[off++] = S.cand[t + kMcThreads * m];
-    }
-    if (t == 0) S.base = nvalid ? atomicAdd(&V.st->tri_count, nvalid) : 0u;
-    __syncthreads();
-    // 3. contiguous write, one float4 (vertex) per thread
-    const uint32_t base = S.base;
-    for (uint32_t q = t; q < 3u * nvalid; q += kMcThreads) {
-      const uint32_t k = q / 3u, j = q - 3u * k;
-      const uint32_t ent = S.valid[k];
-      const int c = (int)(ent & 511u), tt = (int)(ent >> 9);
-      const int x = c & 7, y = (c >> 3) & 7, z = c >> 6;
-      const int ci = S.cases[c];
-      const uint32_t out = base + k;
-      if (out < tri_cap)
-        tris[3 * (size_t)out + j] =
-            mc_vertex<true>(S, S.tri[ci][3 * tt + (int)j], x, y, z, gx0 + x, gy0 + y, gz0 + z);
-      else if (j == 0)
-        atomicOr(&V.st->error, kErrTriCap);
+      uint32_t nvalid;
+      const uint32_t pre = cta_scan(S, ok, &nvalid);
+      if (t == 0) S.base = nvalid ? atomicAdd(&V.st->tri_count, nvalid) : 0u;
+      __syncthreads();
+      if (ok) {
+        const uint32_t out = S.base + pre;
+        if (out < tri_cap) {
+          float4 *dst = tris + 3 * (size_t)out;
+          dst[0] = p0;
+          dst[1] = p1;
+          dst[2] = p2;
+        } else {
+          atomicOr(&V.st->error, kErrTriCap);
+        }
+      }
     }
   }
 }
