@@ -323,7 +323,7 @@ def run_engine(args):
                       for k in ("ms_allocate", "ms_integrate", "ms_extract", "ms_frame")},
         "per_frame": {"blocks": statistics.mean(blocks), "voxels_updated": statistics.mean(updated),
                       "triangles": statistics.mean(tris)},
-        "gpu_launches": 6 * args.steps,
+        "gpu_launches": 7 * args.steps,  # frame_begin, allocate, epoch_end, resolve, integrate, mc_begin, mc
         "tuning": tuning,
         "wall_s": t_wall,
         "clocks": clk.summary(),

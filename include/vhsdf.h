@@ -126,7 +126,8 @@ typedef struct vh_tuning {
                                  /* 1: next block's voxels prefetched        */
   int32_t integrate_ctas_per_sm; /* resident CTAs per SM (0 = occupancy max) */
   int32_t mc_ctas_per_sm;        /* resident CTAs per SM (0 = occupancy max) */
-  int32_t reserved;
+  int32_t mc_variant;            /* 0: register budget for 8 CTAs per SM,    */
+                                 /* 1: for 12 CTAs per SM                    */
 } vh_tuning;
 
 typedef struct vh_handle vh_handle;

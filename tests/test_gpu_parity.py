@@ -212,7 +212,7 @@ def test_every_launch_configuration_is_bit_exact(scene):
     """The tuner only changes speed: each configuration reproduces the oracle."""
     orc = None
     results = []
-    configs = [(0, 0, 0), (1, 0, 0), (0, 2, 3), (1, 1, 1)]
+    configs = [(0, 0, 0, 0), (1, 0, 0, 1), (0, 2, 3, 1), (1, 1, 1, 0)]
     for cfg in configs:
         vol = volume_for(scene)
         vol.set_tuning(*cfg)
@@ -237,7 +237,7 @@ def test_autotune_picks_a_valid_configuration(scene, tmp_path, monkeypatch):
     vol = volume_for(scene)
     d, c, p = scene.render(0)
     t = vol.autotune(d, c, p)
-    assert t["integrate_variant"] in (0, 1)
+    assert t["integrate_variant"] in (0, 1) and t["mc_variant"] in (0, 1)
     assert t["integrate_ctas_per_sm"] >= 1 and t["mc_ctas_per_sm"] >= 1
     assert vol.stats()["blocks_allocated"] == 0  # the handle's volume is untouched
     assert vol.tuning() == t

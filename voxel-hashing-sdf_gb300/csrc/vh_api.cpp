@@ -174,13 +174,15 @@ void enqueue_frame(vh_handle *h, int fmt, bool with_mc, bool events, bool captur
   launch_frame_begin(h->V, s);
   launch_allocate(h->V, h->C, h->d_depth, fmt, h->d_rgb, h->d_pose, h->d_pix, s);
   launch_epoch_end(h->V, s);
+  launch_frame_resolve(h->V, h->sm_count * 2, s);
   if (events) stage_event(h->ev[1], s, capturing);
   launch_integrate(h->V, h->C, h->d_pix, h->d_pose, integrate_grid(h),
                    h->tuning.integrate_variant, s);
   if (events) stage_event(h->ev[2], s, capturing);
   if (with_mc) {
     launch_mc_begin(h->V, s);
-    launch_mc(h->V, 0, h->C.mc_min_weight, h->d_tris, (uint32_t)h->tri_cap, mc_grid(h), s);
+    launch_mc(h->V, 0, h->C.mc_min_weight, h->d_tris, (uint32_t)h->tri_cap, mc_grid(h),
+              h->tuning.mc_variant, s);
     if (events) stage_event(h->ev[3], s, capturing);
   }
 }
@@ -198,8 +200,9 @@ void drop_graphs(vh_handle *h) {
 void apply_tuning(vh_handle *h, const vh_tuning &t) {
   h->tuning = t;
   h->tuning.integrate_variant = t.integrate_variant == 1 ? 1 : 0;
+  h->tuning.mc_variant = t.mc_variant == 1 ? 1 : 0;
   const int imax = integrate_ctas_per_sm(h->tuning.integrate_variant);
-  const int mmax = mc_ctas_per_sm();
+  const int mmax = mc_ctas_per_sm(h->tuning.mc_variant);
   h->integrate_per_sm =
       t.integrate_ctas_per_sm > 0 && t.integrate_ctas_per_sm < imax ? t.integrate_ctas_per_sm : imax;
   h->mc_per_sm = t.mc_ctas_per_sm > 0 && t.mc_ctas_per_sm < mmax ? t.mc_ctas_per_sm : mmax;
@@ -270,6 +273,7 @@ void free_all(vh_handle *h) {
   cudaFree(h->V.free_list);
   cudaFree(h->V.frame_list);
   cudaFree(h->V.frame_nb);
+  cudaFree(h->V.frame_res);
   cudaFree(h->V.st);
   cudaFree(h->d_depth);
   cudaFree(h->d_rgb);
@@ -454,6 +458,7 @@ vh_status vh_create(const vh_params *p, vh_handle **out) {
             cudaMalloc(&h->V.free_list, sizeof(uint32_t) * p->pool_blocks) == cudaSuccess &&
             cudaMalloc(&h->V.frame_list, sizeof(uint32_t) * p->max_frame_blocks) == cudaSuccess &&
             cudaMalloc(&h->V.frame_nb, 8 * sizeof(uint32_t) * p->max_frame_blocks) == cudaSuccess &&
+            cudaMalloc(&h->V.frame_res, sizeof(ulonglong2) * p->max_frame_blocks) == cudaSuccess &&
             cudaMalloc(&h->V.st, sizeof(DevState)) == cudaSuccess &&
             cudaMalloc(&h->d_depth, 4 * npx) == cudaSuccess &&
             cudaMalloc(&h->d_rgb, 3 * npx) == cudaSuccess &&
@@ -546,7 +551,7 @@ vh_status vh_extract(vh_handle *h, int32_t scope, vh_mesh_view *out) {
   for (int attempt = 0; attempt < 2; ++attempt) {
     launch_mc_begin(h->V, h->stream);
     launch_mc(h->V, scope == VH_SCOPE_ALL, h->C.mc_min_weight, h->d_tris, (uint32_t)h->tri_cap,
-              mc_grid(h), h->stream);
+              mc_grid(h), h->tuning.mc_variant, h->stream);
     VH_CUDA(h, cudaGetLastError());
     h->ev_pending = false;
     if (scope == VH_SCOPE_FRAME && !out && !(h->p.flags & VH_FLAG_SYNC)) return VH_OK;
@@ -864,8 +869,8 @@ vh_status vh_get_tuning(vh_handle *h, vh_tuning *out) {
 }
 
 vh_status vh_set_tuning(vh_handle *h, const vh_tuning *t) {
-  if (!h || !t || t->integrate_variant < 0 || t->integrate_variant > 1 ||
-      t->integrate_ctas_per_sm < 0 || t->mc_ctas_per_sm < 0)
+  if (!h || !t || t->integrate_variant < 0 || t->integrate_variant > 1 || t->mc_variant < 0 ||
+      t->mc_variant > 1 || t->integrate_ctas_per_sm < 0 || t->mc_ctas_per_sm < 0)
     return VH_ERR_INVALID_ARG;
   VH_CUDA(h, cudaStreamSynchronize(h->stream));
   apply_tuning(h, *t);
@@ -904,7 +909,8 @@ bool cache_lookup(const std::string &key, vh_tuning *t) {
   std::ifstream f(path);
   std::string k;
   vh_tuning v{};
-  while (f >> k >> v.integrate_variant >> v.integrate_ctas_per_sm >> v.mc_ctas_per_sm) {
+  while (f >> k >> v.integrate_variant >> v.integrate_ctas_per_sm >> v.mc_ctas_per_sm >>
+         v.mc_variant) {
     if (k == key) {
       g_tune_cache[key] = v;
       *t = v;
@@ -921,7 +927,7 @@ void cache_store(const std::string &key, const vh_tuning &t) {
   if (!path) return;
   std::ofstream f(path, std::ios::app);
   f << key << " " << t.integrate_variant << " " << t.integrate_ctas_per_sm << " "
-    << t.mc_ctas_per_sm << "\n";
+    << t.mc_ctas_per_sm << " " << t.mc_variant << "\n";
 }
 
 float median(std::vector<float> v) {
@@ -981,16 +987,20 @@ extern "C" vh_status vh_autotune(vh_handle *h, const void *depth, int32_t depth_
       }
     }
   }
-  const int mocc = mc_ctas_per_sm();
-  const int mopts[3] = {mocc, std::max(1, mocc * 2 / 3), std::max(1, mocc / 2)};
-  for (int o = 0; o < 3 && s == VH_OK; ++o) {
-    if (o > 0 && mopts[o] == mopts[o - 1]) continue;
-    vh_tuning t = best;
-    t.mc_ctas_per_sm = mopts[o];
-    s = run(t, &mi, &mm);
-    if (s == VH_OK && mm < best_mc) {
-      best_mc = mm;
-      best.mc_ctas_per_sm = mopts[o];
+  for (int variant = 0; variant < 2 && s == VH_OK; ++variant) {
+    const int mocc = mc_ctas_per_sm(variant);
+    const int mopts[3] = {mocc, std::max(1, mocc * 2 / 3), std::max(1, mocc / 2)};
+    for (int o = 0; o < 3 && s == VH_OK; ++o) {
+      if (o > 0 && mopts[o] == mopts[o - 1]) continue;
+      vh_tuning t = best;
+      t.mc_variant = variant;
+      t.mc_ctas_per_sm = mopts[o];
+      s = run(t, &mi, &mm);
+      if (s == VH_OK && mm < best_mc) {
+        best_mc = mm;
+        best.mc_variant = variant;
+        best.mc_ctas_per_sm = mopts[o];
+      }
     }
   }
   vh_destroy(sc);

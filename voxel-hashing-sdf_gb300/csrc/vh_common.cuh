@@ -8,6 +8,8 @@
 //   block_keys  N x 8 B     packed key of every pool block (EMPTY if free)
 //   free_list   N x 4 B     recycled (already zeroed) block ids
 //   frame_list  M x 4 B     slot ids touched by the current frame
+//   frame_res   M x 16 B    {key, pool id} of each listed slot (one load instead
+//                           of list -> slot)
 //   frame_nb    M x 32 B    pool ids of each listed block and of its +x/+y/+z
 //                           neighbours (written by integration, read by MC)
 //   state       one DevState of counters and sticky error bits
@@ -74,6 +76,7 @@ struct VolumeView {
   uint32_t *free_list;
   uint32_t *frame_list;
   uint32_t *frame_nb;  // per frame-list entry: the block and its 7 +x/+y/+z neighbours
+  ulonglong2 *frame_res;  // per frame-list entry: {key, pool block} (resolved slot)
   uint32_t frame_cap;
   uint32_t pool_cap;
   DevState *st;
@@ -132,15 +135,17 @@ void launch_allocate(const VolumeView &V, const CamParams &C, const void *depth,
 void launch_integrate(const VolumeView &V, const CamParams &C, const uint2 *pix,
                       const float *pose, int grid, int variant, cudaStream_t s);
 void launch_mc(const VolumeView &V, int scope_all, float min_weight, float4 *tris,
-               uint32_t tri_cap, int grid, cudaStream_t s);
+               uint32_t tri_cap, int grid, int variant, cudaStream_t s);
 // Resident CTAs per SM of the persistent kernels (for grid sizing).
 int integrate_ctas_per_sm(int variant);
-int mc_ctas_per_sm();
+int mc_ctas_per_sm(int variant);
 void launch_alloc_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, cudaStream_t s);
 void launch_find_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, int32_t *out,
                       cudaStream_t s);
 void launch_erase_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, cudaStream_t s);
 void launch_frame_nb(const VolumeView &V, cudaStream_t s);
+// Writes frame_res for the current block list (after allocation).
+void launch_frame_resolve(const VolumeView &V, int grid, cudaStream_t s);
 void launch_list_keys(const VolumeView &V, int32_t *xyz, uint32_t n, cudaStream_t s);
 void launch_scatter_blocks(const VolumeView &V, const int32_t *xyz, const float *sdf,
                            const float *w, const uint8_t *rgb, uint32_t n, cudaStream_t s);

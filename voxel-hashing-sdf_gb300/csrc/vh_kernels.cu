@@ -418,10 +418,9 @@ struct BlockQuad {
 };
 
 __device__ __forceinline__ void load_quad(const VolumeView &V, uint32_t i, int t, BlockQuad &q) {
-  const uint32_t s = __ldg(V.frame_list + i);
-  const ulonglong2 sl = __ldg(reinterpret_cast<const ulonglong2 *>(V.slots) + s);
-  q.key = sl.x;
-  q.block = (uint32_t)sl.y;
+  const ulonglong2 r = __ldg(V.frame_res + i);
+  q.key = r.x;
+  q.block = (uint32_t)r.y;
   if (q.key >= kTombKey || q.block == kNoBlock) return;
   const float *base = V.pool + (size_t)q.block * kBlockWords;
   q.sdf = reinterpret_cast<const float4 *>(base)[t];
@@ -510,7 +509,6 @@ struct McShared {
   uint32_t halo[kHalo];      // halo voxel: staged index | neighbour << 10 | voxel << 13
   uint32_t nb[8];
   uint32_t warp_sum[kMcThreads / 32];
-  int key[3];
   uint32_t base;
 };
 
@@ -636,7 +634,8 @@ __device__ __forceinline__ uint32_t cta_scan(McShared &S, uint32_t v, uint32_t *
 //   triangles (scan) -> one thread per candidate tests the reference's
 //   degenerate-triangle rule -> compact (scan) -> one atomic per block ->
 //   one thread per output float4, contiguous stores.
-__global__ void __launch_bounds__(kMcThreads, 8) k_mc(VolumeView V, int scope_all, float min_weight,
+template <int kMinCtas>
+__global__ void __launch_bounds__(kMcThreads, kMinCtas) k_mc(VolumeView V, int scope_all, float min_weight,
                                                       float4 *__restrict__ tris, uint32_t tri_cap) {
   __shared__ McShared S;
   const int t = threadIdx.x;
@@ -674,34 +673,28 @@ __global__ void __launch_bounds__(kMcThreads, 8) k_mc(VolumeView V, int scope_al
   const float nanv = __int_as_float(0x7FC00000);
   for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
     __syncthreads();  // previous iteration done with S
-    if (t == 0) {
-      unsigned long long key;
-      uint32_t b;
-      if (scope_all) {
-        key = V.block_keys[i];
-        b = key < kTombKey ? i : kNoBlock;
-      } else {
-        const Slot sl = V.slots[V.frame_list[i]];
-        key = sl.key;
-        b = key < kTombKey ? sl.block : kNoBlock;
-      }
-      int x = 0, y = 0, z = 0;
-      if (b != kNoBlock) unpack_key(key, x, y, z);
-      S.key[0] = x;
-      S.key[1] = y;
-      S.key[2] = z;
-      if (scope_all) S.nb[0] = b;
+    // Every thread reads the block's key and id itself (broadcast loads), so
+    // the voxel loads below start without waiting for a barrier.
+    unsigned long long key;
+    uint32_t own;
+    if (scope_all) {
+      key = __ldg(V.block_keys + i);
+      own = key < kTombKey ? i : kNoBlock;
+    } else {
+      const ulonglong2 r = __ldg(V.frame_res + i);
+      key = r.x;
+      own = key < kTombKey ? (uint32_t)r.y : kNoBlock;
     }
-    if (!scope_all && t >= 32 && t < 40) S.nb[t - 32] = __ldg(V.frame_nb + 8 * (size_t)i + (t - 32));
-    __syncthreads();
-    if (S.nb[0] == kNoBlock) continue;
-    const int bx = S.key[0], by = S.key[1], bz = S.key[2];
-    if (scope_all && t >= 1 && t < 8) {
+    if (own == kNoBlock) continue;  // same entry for every thread: uniform
+    int bx, by, bz;
+    unpack_key(key, bx, by, bz);
+    if (scope_all && t < 8) {
       const int nx = bx + (t & 1), ny = by + ((t >> 1) & 1), nz = bz + (t >> 2);
-      S.nb[t] = key_in_range(nx, ny, nz) ? block_of(V, pack_key(nx, ny, nz)) : kNoBlock;
+      S.nb[t] = t == 0 ? own
+                       : (key_in_range(nx, ny, nz) ? block_of(V, pack_key(nx, ny, nz)) : kNoBlock);
     }
     {  // own block: 4 voxels per thread, 16-byte loads
-      const float *base = V.pool + (size_t)S.nb[0] * kBlockWords;
+      const float *base = V.pool + (size_t)own * kBlockWords;
       const float4 sd = reinterpret_cast<const float4 *>(base)[t];
       const float4 wt = reinterpret_cast<const float4 *>(base + kB3)[t];
       const uint4 cl = reinterpret_cast<const uint4 *>(base + 2 * kB3)[t];
@@ -716,20 +709,36 @@ __global__ void __launch_bounds__(kMcThreads, 8) k_mc(VolumeView V, int scope_al
       S.rgb[h + 2] = cl.z;
       S.rgb[h + 3] = cl.w;
     }
-    __syncthreads();  // S.nb complete
-    for (int hh = t; hh < kHalo; hh += kMcThreads) {
-      const uint32_t info = S.halo[hh];
-      const uint32_t blk = S.nb[(info >> 10) & 7u];
-      const int h = (int)(info & 1023u), li = (int)(info >> 13);
-      float v = nanv;
-      uint32_t c = 0;
-      if (blk != kNoBlock) {
-        const float *base = V.pool + (size_t)blk * kBlockWords;
-        v = __ldg(base + kB3 + li) >= min_weight ? __ldg(base + li) : nanv;
-        c = __ldg(reinterpret_cast<const uint32_t *>(base + 2 * kB3) + li);
+    if (scope_all) __syncthreads();  // S.nb complete (uniform condition)
+    {  // halo: every thread owns at most two entries; all loads issued together
+      const int h1 = t + kMcThreads;
+      const uint32_t info0 = S.halo[t];
+      const uint32_t info1 = h1 < kHalo ? S.halo[h1] : 0u;
+      const uint32_t nb0 = (info0 >> 10) & 7u, nb1 = (info1 >> 10) & 7u;
+      const uint32_t blk0 = scope_all ? S.nb[nb0] : __ldg(V.frame_nb + 8 * (size_t)i + nb0);
+      uint32_t blk1 = scope_all ? S.nb[nb1] : __ldg(V.frame_nb + 8 * (size_t)i + nb1);
+      if (h1 >= kHalo) blk1 = kNoBlock;
+      const int li0 = (int)(info0 >> 13), li1 = (int)(info1 >> 13);
+      float w0 = 0.f, s0 = nanv, w1 = 0.f, s1 = nanv;
+      uint32_t c0 = 0, c1 = 0;
+      if (blk0 != kNoBlock) {
+        const float *base = V.pool + (size_t)blk0 * kBlockWords;
+        w0 = __ldg(base + kB3 + li0);
+        s0 = __ldg(base + li0);
+        c0 = __ldg(reinterpret_cast<const uint32_t *>(base + 2 * kB3) + li0);
       }
-      S.sdf[h] = v;
-      S.rgb[h] = c;
+      if (blk1 != kNoBlock) {
+        const float *base = V.pool + (size_t)blk1 * kBlockWords;
+        w1 = __ldg(base + kB3 + li1);
+        s1 = __ldg(base + li1);
+        c1 = __ldg(reinterpret_cast<const uint32_t *>(base + 2 * kB3) + li1);
+      }
+      S.sdf[info0 & 1023u] = blk0 != kNoBlock && w0 >= min_weight ? s0 : nanv;
+      S.rgb[info0 & 1023u] = c0;
+      if (h1 < kHalo) {
+        S.sdf[info1 & 1023u] = blk1 != kNoBlock && w1 >= min_weight ? s1 : nanv;
+        S.rgb[info1 & 1023u] = c1;
+      }
     }
     __syncthreads();
     // 1. classify this thread's 4 cubes; count their candidate triangles
@@ -916,6 +925,7 @@ __global__ void __launch_bounds__(256) k_frame_nb(VolumeView V) {
   const uint32_t i = idx >> 3, k = idx & 7u;
   if (i >= n) return;
   const Slot sl = V.slots[V.frame_list[i]];
+  if (k == 0) V.frame_res[i] = make_ulonglong2(sl.key, (unsigned long long)sl.block);
   uint32_t nbid = kNoBlock;
   if (sl.key < kTombKey && sl.block != kNoBlock) {
     int bx, by, bz;
@@ -925,6 +935,15 @@ __global__ void __launch_bounds__(256) k_frame_nb(VolumeView V) {
                   : (key_in_range(nx, ny, nz) ? block_of(V, pack_key(nx, ny, nz)) : kNoBlock);
   }
   V.frame_nb[8 * (size_t)i + k] = nbid;
+}
+
+// frame_res[i] = {key, block} of frame-list entry i (grid-stride).
+__global__ void __launch_bounds__(256) k_frame_resolve(VolumeView V) {
+  const uint32_t n = min(V.st->frame_count, V.frame_cap);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const ulonglong2 sl = __ldg(reinterpret_cast<const ulonglong2 *>(V.slots) + V.frame_list[i]);
+    V.frame_res[i] = make_ulonglong2(sl.x, sl.y & 0xFFFFFFFFull);
+  }
 }
 
 __global__ void k_list_keys(VolumeView V, int32_t *__restrict__ xyz, uint32_t n) {
@@ -988,9 +1007,14 @@ int integrate_ctas_per_sm(int variant) {
   return n > 0 ? n : 1;
 }
 
-int mc_ctas_per_sm() {
+// MC variants differ only in the register budget: 0 targets 8 resident CTAs
+// per SM, 1 targets 12 (fewer registers, more warps to hide latency).
+int mc_ctas_per_sm(int variant) {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mc, kMcThreads, 0);
+  if (variant == 1)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mc<12>, kMcThreads, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mc<8>, kMcThreads, 0);
   return n > 0 ? n : 1;
 }
 
@@ -1003,8 +1027,11 @@ void launch_integrate(const VolumeView &V, const CamParams &C, const uint2 *pix,
 }
 
 void launch_mc(const VolumeView &V, int scope_all, float min_weight, float4 *tris,
-               uint32_t tri_cap, int grid, cudaStream_t s) {
-  k_mc<<<grid, kMcThreads, 0, s>>>(V, scope_all, min_weight, tris, tri_cap);
+               uint32_t tri_cap, int grid, int variant, cudaStream_t s) {
+  if (variant == 1)
+    k_mc<12><<<grid, kMcThreads, 0, s>>>(V, scope_all, min_weight, tris, tri_cap);
+  else
+    k_mc<8><<<grid, kMcThreads, 0, s>>>(V, scope_all, min_weight, tris, tri_cap);
 }
 
 void launch_alloc_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, cudaStream_t s) {
@@ -1016,6 +1043,9 @@ void launch_find_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, int32
 }
 void launch_erase_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, cudaStream_t s) {
   if (n) k_erase_keys<<<grid_for(n, 256), 256, 0, s>>>(V, xyz, n);
+}
+void launch_frame_resolve(const VolumeView &V, int grid, cudaStream_t s) {
+  k_frame_resolve<<<grid, 256, 0, s>>>(V);
 }
 void launch_frame_nb(const VolumeView &V, cudaStream_t s) {
   k_frame_nb<<<grid_for(V.frame_cap * 8u, 256), 256, 0, s>>>(V);

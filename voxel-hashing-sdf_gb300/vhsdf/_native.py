@@ -63,7 +63,7 @@ class VhStats(C.Structure):
 
 class VhTuning(C.Structure):
     _fields_ = [("integrate_variant", C.c_int32), ("integrate_ctas_per_sm", C.c_int32),
-                ("mc_ctas_per_sm", C.c_int32), ("reserved", C.c_int32)]
+                ("mc_ctas_per_sm", C.c_int32), ("mc_variant", C.c_int32)]
 
 
 class VhMeshView(C.Structure):

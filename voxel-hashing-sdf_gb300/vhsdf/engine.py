@@ -113,10 +113,11 @@ class Volume:
     def tuning(self):
         t = N.VhTuning()
         self._check(self._L.vh_get_tuning(self._h, C.byref(t)))
-        return {f: getattr(t, f) for f, _ in N.VhTuning._fields_ if f != "reserved"}
+        return {f: getattr(t, f) for f, _ in N.VhTuning._fields_}
 
-    def set_tuning(self, integrate_variant=0, integrate_ctas_per_sm=0, mc_ctas_per_sm=0):
-        t = N.VhTuning(integrate_variant, integrate_ctas_per_sm, mc_ctas_per_sm, 0)
+    def set_tuning(self, integrate_variant=0, integrate_ctas_per_sm=0, mc_ctas_per_sm=0,
+                   mc_variant=0):
+        t = N.VhTuning(integrate_variant, integrate_ctas_per_sm, mc_ctas_per_sm, mc_variant)
         self._check(self._L.vh_set_tuning(self._h, C.byref(t)))
 
     def autotune(self, depth, rgb, c2w, depth_format=None):
@@ -126,7 +127,7 @@ class Volume:
         t = N.VhTuning()
         self._check(self._L.vh_autotune(self._h, d.ptr, _depth_fmt(d.dtype, depth_format), c.ptr,
                                         pose.ctypes.data, d.mem, C.byref(t)))
-        return {f: getattr(t, f) for f, _ in N.VhTuning._fields_ if f != "reserved"}
+        return {f: getattr(t, f) for f, _ in N.VhTuning._fields_}
 
     def extract(self, scope="frame"):
         """Runs marching cubes; returns (device pointer, triangle count)."""
