@@ -267,6 +267,50 @@ vh_status vh_set_tuning(vh_handle *h, const vh_tuning *t);
 vh_status vh_autotune(vh_handle *h, const void *depth, int32_t depth_fmt, const uint8_t *rgb,
                       const float *c2w, int32_t mem, vh_tuning *chosen);
 
+/* ---- gradients and pose refinement (no reference counterpart: the
+ * reference has no derivatives) ------------------------------------------- */
+
+#define VH_REFINE_ADJOINT 0 /* analytic Jacobians from the sampling adjoint    */
+#define VH_REFINE_FD 1      /* forward-only central differences (13 residual   */
+                            /* evaluations per Gauss-Newton step)              */
+
+typedef struct vh_refine_stats {
+  int32_t iterations;    /* Gauss-Newton steps taken                         */
+  int32_t valid_pixels;  /* residuals in the last linearisation              */
+  float initial_rmse;    /* metres, at the initial pose                      */
+  float final_rmse;      /* metres, at the last linearised pose              */
+  float ms;              /* device + host time of the call                   */
+} vh_refine_stats;
+
+/* Trilinear TSDF value (units of the truncation distance) at n world points
+ * (x, y, z in metres) and, if grad != NULL, its gradient d sdf / d point
+ * (per metre): the adjoint of sampling.  valid[i] = 0 where a corner voxel
+ * is unallocated or unobserved (phi and grad are then 0).  All arrays in
+ * `mem`. */
+vh_status vh_sdf_sample(vh_handle *h, const float *xyz, int64_t n, float *phi, float *grad,
+                        uint8_t *valid, int32_t mem);
+/* Gauss-Newton normal equations of the SDF residuals r = T * sdf(c2w * X_p)
+ * of every `stride`-th pixel of a depth image (truncated samples skipped),
+ * for the left perturbation c2w -> exp(xi) c2w, xi = (v, w).  terms[29]:
+ * the upper triangle of J^T J row by row (21), J^T r (6), sum r^2, count. */
+vh_status vh_pose_normal_equations(vh_handle *h, const void *depth, int32_t depth_fmt,
+                                   int32_t mem, const float *c2w, int32_t stride,
+                                   int32_t method, double *terms);
+/* `iterations` Gauss-Newton steps from c2w_init against the fused volume;
+ * writes the refined pose to c2w_out (both row-major 4x4, host). */
+vh_status vh_pose_refine(vh_handle *h, const void *depth, int32_t depth_fmt, int32_t mem,
+                         const float *c2w_init, int32_t iterations, int32_t stride,
+                         int32_t method, float *c2w_out, vh_refine_stats *stats);
+/* Vector-Jacobian product of the last integration update (depth image and
+ * pose c2w of that frame): given dL/dsdf for every voxel of the frame's
+ * block list (vh_block_list order, 512 values per block, index x + 8y +
+ * 64z), writes dL/ddepth per pixel (H*W floats, metres) and dL/dxi (6
+ * floats, host) for the left pose perturbation.  Recomputed from the volume;
+ * no per-frame state is kept.  grad_sdf, grad_depth and depth in `mem`. */
+vh_status vh_integrate_vjp(vh_handle *h, const void *depth, int32_t depth_fmt, const float *c2w,
+                           const float *grad_sdf, float *grad_depth, float *grad_pose,
+                           int32_t mem);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

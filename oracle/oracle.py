@@ -51,6 +51,8 @@ def lib():
         L.vho_mc.argtypes = [P, C.c_int32]
         L.vho_mc_copy.restype = C.c_int64
         L.vho_mc_copy.argtypes = [P, P, P, P, P, C.c_int64]
+        L.vho_sample.argtypes = [P, P, C.c_int64, C.c_double, P, P, P]
+        L.vho_pose_terms.argtypes = [P, P, P, C.c_int32, C.c_double, P]
         _lib = L
     return _lib
 
@@ -171,3 +173,23 @@ class Oracle:
         self._L.vho_mc_copy(self._h, xyz.ctypes.data, rgb.ctypes.data, xyz64.ctypes.data,
                             cube.ctypes.data, n)
         return {"xyz": xyz, "rgb": rgb, "xyz64": xyz64, "cube": cube}
+
+    def sample(self, xyz, min_weight=1.0):
+        """FP64 trilinear sdf and gradient at world points (n x 3)."""
+        xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1, 3)
+        n = xyz.shape[0]
+        phi = np.empty(n, np.float64)
+        grad = np.empty((n, 3), np.float64)
+        valid = np.empty(n, np.uint8)
+        self._L.vho_sample(self._h, xyz.ctypes.data, n, float(min_weight), phi.ctypes.data,
+                           grad.ctypes.data, valid.ctypes.data)
+        return phi, grad, valid.astype(bool)
+
+    def pose_terms(self, depth, c2w, stride=1, min_weight=1.0):
+        """FP64 Gauss-Newton terms of the SDF residuals of a depth image."""
+        d = depth_to_metres(depth, self.depth_scale)
+        P = np.ascontiguousarray(np.asarray(c2w, np.float64).reshape(4, 4)[:3].reshape(12))
+        out = np.empty(29, np.float64)
+        self._L.vho_pose_terms(self._h, d.ctypes.data, P.ctypes.data, int(stride),
+                               float(min_weight), out.ctypes.data)
+        return out

@@ -755,3 +755,106 @@ void vho_vertex_interp(const float *p, const uint8_t *c, float v1, float v2, flo
 }
 
 }  // extern "C"
+
+// ---- differentiable queries (no reference counterpart) ------------------------
+namespace {
+
+// Trilinear TSDF value and gradient at a world point, in double precision,
+// over the oracle's stored voxels (corners need weight >= min_w).
+template <typename Acc>
+bool sample64(const Volume<Acc> &V, double x, double y, double z, double min_w, double *phi,
+              double g[3]) {
+  const double vs = V.p.voxel_size;
+  const double q[3] = {x / vs, y / vs, z / vs};
+  long b[3];
+  double f[3];
+  for (int a = 0; a < 3; ++a) {
+    const double fl = std::floor(q[a]);
+    b[a] = (long)fl;
+    f[a] = q[a] - fl;
+  }
+  double val[8];
+  for (int c = 0; c < 8; ++c) {
+    const long ix = b[0] + (c & 1), iy = b[1] + ((c >> 1) & 1), iz = b[2] + (c >> 2);
+    const long bx = ix >= 0 ? ix / 8 : -((-ix + 7) / 8), by = iy >= 0 ? iy / 8 : -((-iy + 7) / 8),
+               bz = iz >= 0 ? iz / 8 : -((-iz + 7) / 8);
+    const int32_t id = V.find(okey((int)bx, (int)by, (int)bz));
+    if (id < 0) return false;
+    const int li = (int)(ix - 8 * bx) + 8 * (int)(iy - 8 * by) + 64 * (int)(iz - 8 * bz);
+    if ((double)V.blocks[id].w[li] < min_w) return false;
+    val[c] = (double)V.blocks[id].sdf[li];
+  }
+  double p = 0, gx = 0, gy = 0, gz = 0;
+  for (int c = 0; c < 8; ++c) {
+    const int dx = c & 1, dy = (c >> 1) & 1, dz = c >> 2;
+    const double wx = dx ? f[0] : 1 - f[0], wy = dy ? f[1] : 1 - f[1], wz = dz ? f[2] : 1 - f[2];
+    p += wx * wy * wz * val[c];
+    gx += (dx ? 1.0 : -1.0) * wy * wz * val[c];
+    gy += wx * (dy ? 1.0 : -1.0) * wz * val[c];
+    gz += wx * wy * (dz ? 1.0 : -1.0) * val[c];
+  }
+  *phi = p;
+  g[0] = gx / vs;
+  g[1] = gy / vs;
+  g[2] = gz / vs;
+  return true;
+}
+
+template <typename Acc>
+void pose_terms64(const Volume<Acc> &V, const float *depth, const double *P, int stride,
+                  double min_w, double *out) {
+  for (int k = 0; k < 29; ++k) out[k] = 0;
+  const OParams &p = V.p;
+  for (int v = 0; v < p.height; v += stride)
+    for (int u = 0; u < p.width; u += stride) {
+      const double d = depth[(size_t)v * p.width + u];
+      if (!(d > p.min_depth && d <= p.max_depth)) continue;
+      const double cx = (u - (double)p.cx) * d / p.fx, cy = (v - (double)p.cy) * d / p.fy;
+      double X[3];
+      for (int r = 0; r < 3; ++r) X[r] = cx * P[4 * r] + cy * P[4 * r + 1] + d * P[4 * r + 2] + P[4 * r + 3];
+      double phi, g[3];
+      if (!sample64(V, X[0], X[1], X[2], min_w, &phi, g) || !(std::fabs(phi) < 1.0)) continue;
+      const double T = p.trunc;
+      const double J[6] = {T * g[0], T * g[1], T * g[2], T * (X[1] * g[2] - X[2] * g[1]),
+                           T * (X[2] * g[0] - X[0] * g[2]), T * (X[0] * g[1] - X[1] * g[0])};
+      const double r = T * phi;
+      int k = 0;
+      for (int a = 0; a < 6; ++a)
+        for (int b = a; b < 6; ++b) out[k++] += J[a] * J[b];
+      for (int a = 0; a < 6; ++a) out[21 + a] += J[a] * r;
+      out[27] += r * r;
+      out[28] += 1;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+// phi (units of T) and d phi / d point at n world points; valid[i] = 0/1.
+void vho_sample(void *hp, const double *xyz, int64_t n, double min_w, double *phi, double *grad,
+                uint8_t *valid) {
+  Handle *h = (Handle *)hp;
+  for (int64_t i = 0; i < n; ++i) {
+    double g[3] = {0, 0, 0}, f = 0;
+    const bool ok = h->precision == 64
+                        ? sample64(*h->v64, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], min_w, &f, g)
+                        : sample64(*h->v32, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], min_w, &f, g);
+    phi[i] = ok ? f : 0;
+    for (int a = 0; a < 3; ++a) grad[3 * i + a] = ok ? g[a] : 0;
+    valid[i] = ok;
+  }
+}
+
+// Normal-equation terms (same layout as the engine) in double precision;
+// P: 12 doubles, row-major camera-to-world 3x4.
+void vho_pose_terms(void *hp, const float *depth, const double *P, int32_t stride, double min_w,
+                    double *out29) {
+  Handle *h = (Handle *)hp;
+  if (h->precision == 64)
+    pose_terms64(*h->v64, depth, P, stride, min_w, out29);
+  else
+    pose_terms64(*h->v32, depth, P, stride, min_w, out29);
+}
+
+}  // extern "C"

@@ -1,0 +1,208 @@
+"""Gradients on the GPU against FP64 references: the sampling adjoint, the
+pose normal equations, Gauss-Newton pose refinement (adjoint vs the plain
+FD-Jacobian method) and the vector-Jacobian product of integration."""
+import numpy as np
+import pytest
+import torch
+
+from helpers import oracle_for, small_scene, volume_for
+
+pytestmark = pytest.mark.gpu
+
+
+def fused_room(w=320, h=240, frames=20, voxel=0.01, trunc=0.1):
+    scene = small_scene(w=w, h=h, frames=frames)
+    vol = volume_for(scene, voxel=voxel, trunc=trunc, pool_blocks=1 << 17,
+                     max_frame_blocks=1 << 17, max_triangles=1 << 22)
+    for f in range(frames):
+        vol.integrate(*scene.render(f))
+    orc = oracle_for(vol, 64)
+    e = vol.export_blocks()
+    orc.import_blocks(e["xyz"], e["sdf"], e["weight"], e["rgb"])
+    return scene, vol, orc, e
+
+
+@pytest.fixture(scope="module")
+def room(gpu):
+    return fused_room()
+
+
+def interior_points(e, voxel, n, seed=0):
+    """World points strictly inside voxel cells of observed blocks."""
+    rng = np.random.default_rng(seed)
+    blocks = e["xyz"][rng.integers(0, len(e["xyz"]), n)]
+    local = rng.integers(0, 8, (n, 3))
+    frac = rng.uniform(0.05, 0.95, (n, 3))
+    q = blocks * 8 + local + frac
+    return (q * voxel).astype(np.float32)
+
+
+def test_sampling_matches_fp64(room):
+    scene, vol, orc, e = room
+    pts = interior_points(e, vol.params.voxel_size, 20000)
+    phi, grad, valid = vol.sdf_sample(pts)
+    ophi, ograd, ovalid = orc.sample(pts.astype(np.float64))
+    assert valid.sum() > 5000
+    assert np.array_equal(valid, ovalid)
+    # fp32 world coordinates ~200 voxels from the origin quantise the in-cell
+    # position at ~1.5e-5 voxel; |grad| <= ~1 per voxel bounds the sdf error
+    assert np.max(np.abs(phi[valid] - ophi[valid])) < 5e-5
+    scale = np.abs(ograd[valid]).max()
+    assert np.max(np.abs(grad[valid] - ograd[valid])) < 1e-4 * scale
+
+
+def test_gradient_against_fp64_finite_differences(room):
+    scene, vol, orc, e = room
+    voxel = vol.params.voxel_size
+    pts = interior_points(e, voxel, 3000, seed=1)
+    phi, grad, valid = vol.sdf_sample(pts)
+    p = pts[valid].astype(np.float64)
+    h = 1e-4 * voxel  # stays inside the cell: points are >= 0.05 voxel from faces
+    fd = np.zeros_like(p)
+    for a in range(3):
+        dp = np.zeros(3)
+        dp[a] = h
+        fp, _, vp = orc.sample(p + dp)
+        fm, _, vm = orc.sample(p - dp)
+        assert vp.all() and vm.all()
+        fd[:, a] = (fp - fm) / (2 * h)
+    scale = np.abs(fd).max()
+    assert np.max(np.abs(grad[valid] - fd)) < 1e-4 * scale
+
+
+def test_autograd_binding(room):
+    from sdf_autograd import sdf_sample
+    scene, vol, orc, e = room
+    pts = torch.from_numpy(interior_points(e, vol.params.voxel_size, 4000, seed=2)).cuda()
+    pts.requires_grad_(True)
+    phi, valid = sdf_sample(pts, vol)
+    loss = (phi[valid] ** 2).sum()
+    loss.backward()
+    p = pts.detach().cpu().numpy().astype(np.float64)
+    ophi, ograd, ovalid = orc.sample(p)
+    want = np.where(ovalid[:, None], 2 * ophi[:, None] * ograd, 0.0)
+    got = pts.grad.cpu().numpy()
+    assert np.max(np.abs(got - want)) < 1e-4 * np.abs(want).max()
+
+
+def test_normal_equations_match_fp64(room):
+    scene, vol, orc, e = room
+    d, c, p = scene.render(7)
+    t = vol.pose_normal_equations(d, p, stride=2)
+    o = orc.pose_terms(d, p, stride=2)
+    assert abs(t[28] - o[28]) <= 1e-3 * o[28] + 5  # samples at |sdf| == 1 may differ
+    assert np.allclose(t[:27], o[:27], rtol=2e-3, atol=2e-3 * np.abs(o[:21]).max())
+    fd = vol.pose_normal_equations(d, p, stride=2, method="fd")
+    # forward central differences approximate the same Jacobian
+    assert np.allclose(fd[:21], t[:21], rtol=0.05, atol=0.05 * np.abs(t[:21]).max())
+
+
+def perturb(pose, deg, metres, seed):
+    rng = np.random.default_rng(seed)
+    axis = rng.normal(size=3)
+    axis /= np.linalg.norm(axis)
+    th = np.deg2rad(deg)
+    K = np.array([[0, -axis[2], axis[1]], [axis[2], 0, -axis[0]], [-axis[1], axis[0], 0]])
+    R = np.eye(3) + np.sin(th) * K + (1 - np.cos(th)) * K @ K
+    dirn = rng.normal(size=3)
+    dirn /= np.linalg.norm(dirn)
+    out = pose.astype(np.float64).copy()
+    out[:3, :3] = R @ out[:3, :3]
+    out[:3, 3] = R @ out[:3, 3] + metres * dirn
+    return out.astype(np.float32)
+
+
+def pose_error(a, b):
+    dt = np.linalg.norm(a[:3, 3].astype(np.float64) - b[:3, 3])
+    dR = a[:3, :3].astype(np.float64) @ b[:3, :3].T.astype(np.float64)
+    ang = np.degrees(np.arccos(np.clip((np.trace(dR) - 1) / 2, -1, 1)))
+    return dt, ang
+
+
+@pytest.mark.parametrize("method", ["adjoint", "fd"])
+def test_pose_refinement_converges(room, method):
+    scene, vol, orc, e = room
+    for f, seed in ((5, 11), (13, 12)):
+        d, c, gt = scene.render(f)
+        init = perturb(gt, 2.0, 0.02, seed)
+        out, st = vol.pose_refine(d, init, iterations=20, stride=2, method=method)
+        dt, ang = pose_error(out, gt)
+        assert dt < 2e-3 and ang < 0.1, (method, f, dt, ang, st)
+        assert st["final_rmse"] < st["initial_rmse"]
+
+
+def test_integration_vjp_against_fp64_finite_differences(gpu):
+    """Plane scene (constant depth), so pixel re-assignment under a pose
+    perturbation cannot change any sample."""
+    from vhsdf import Volume
+    from oracle.oracle import Oracle
+    W, H, f = 64, 48, 50.0
+    params = dict(width=W, height=H, fx=f, fy=f, cx=31.5, cy=23.5, min_depth=0.1, max_depth=4.0,
+                  voxel_size=0.01, trunc=0.04, table_log2=16, pool_blocks=1 << 14,
+                  max_frame_blocks=1 << 14, max_triangles=1 << 18)
+    vol = Volume(**params)
+    rgb = np.full((H, W, 3), 100, np.uint8)
+    pose0 = np.eye(4, dtype=np.float32)
+    vol.integrate(np.full((H, W), 1.0, np.float32), rgb, pose0)
+    pre = vol.export_blocks()
+    pose1 = perturb(pose0, 1.0, 0.005, 3)
+    d1 = np.full((H, W), 1.013, np.float32)
+    vol.integrate(d1, rgb, pose1)
+    lst = vol.block_list()
+    rng = np.random.default_rng(5)
+    G = rng.normal(size=(len(lst), 512)).astype(np.float32)
+    # The update has jumps where d - z crosses -T (voxel skipped) or +T (dist
+    # clamped); finite differences across them measure the jump, not the
+    # derivative.  Voxels within 2 mm of either boundary get no upstream
+    # gradient, so the loss is smooth over the perturbations below.
+    li = np.arange(512)
+    vox = (lst[:, None, :] * 8 + np.stack([li & 7, (li >> 3) & 7, li >> 6], -1)[None]) * 0.01
+    R, t = pose1[:3, :3].astype(np.float64), pose1[:3, 3].astype(np.float64)
+    cam = (vox.reshape(-1, 3) - t) @ R
+    zc = cam[:, 2]
+    diff = (1.013 - zc).reshape(len(lst), 512)
+    G[(np.abs(diff + 0.04) < 2e-3) | (np.abs(diff - 0.04) < 2e-3)] = 0.0
+    # voxels whose projection sits on the image border switch in and out too
+    u = (f * cam[:, 0] / zc + 31.5).reshape(len(lst), 512)
+    v = (f * cam[:, 1] / zc + 23.5).reshape(len(lst), 512)
+    near = lambda a, b: np.abs(a - b) < 0.1
+    G[near(u, -0.5) | near(u, W - 0.5) | near(v, -0.5) | near(v, H - 0.5)] = 0.0
+    gd, gp = vol.integrate_vjp(d1, pose1, G)
+
+    key = {tuple(k): i for i, k in enumerate(lst.tolist())}
+
+    def loss(depth, pose):
+        o = Oracle(W, H, f, f, 31.5, 23.5, 0.1, 4.0, 0.01, 0.04, precision=64)
+        o.import_blocks(pre["xyz"], pre["sdf"], pre["weight"], pre["rgb"])
+        o.integrate(depth, rgb, pose)
+        ex = o.export(fp64=True)
+        total = 0.0
+        for i, k in enumerate(ex["xyz"].tolist()):
+            j = key.get(tuple(k))
+            if j is not None:
+                total += float(np.dot(G[j].astype(np.float64), ex["sdf64"][i]))
+        return total
+
+    # depth: directional derivative along a random per-pixel direction
+    delta = rng.normal(size=(H, W)).astype(np.float32)
+    h = 2e-4
+    fd = (loss(d1 + h * delta, pose1) - loss(d1 - h * delta, pose1)) / (2 * h)
+    an = float(np.sum(gd.astype(np.float64) * delta))
+    assert abs(fd - an) < 2e-3 * max(1.0, abs(fd)), (fd, an)
+    # pose: directional derivative along a random se(3) direction
+    xi = rng.normal(size=6)
+    xi /= np.linalg.norm(xi)
+
+    def moved(sign):
+        out = pose1.astype(np.float64).copy()
+        w, v = sign * h * xi[3:], sign * h * xi[:3]
+        th = np.linalg.norm(w)
+        K = np.array([[0, -w[2], w[1]], [w[2], 0, -w[0]], [-w[1], w[0], 0]]) / max(th, 1e-30)
+        R = np.eye(3) + np.sin(th) * K + (1 - np.cos(th)) * K @ K
+        out[:3, :3] = R @ out[:3, :3]
+        out[:3, 3] = R @ out[:3, 3] + v
+        return out.astype(np.float32)
+
+    fdp = (loss(d1, moved(1)) - loss(d1, moved(-1))) / (2 * h)
+    anp = float(np.dot(gp.astype(np.float64), xi))
+    assert abs(fdp - anp) < 2e-2 * max(1.0, abs(fdp)), (fdp, anp)

@@ -32,8 +32,9 @@ ENGINE_SOURCES = [
     ("vh_api.cpp", []),
     ("vh_mesh.cpp", []),
     ("vh_noalloc.cu", []),
+    ("vh_adjoint.cu", []),
 ]
-ENGINE_HEADERS = ["vh_common.cuh", "vh_mc_tables.h", "vh_mesh.h", "vh_internal.h"]
+ENGINE_HEADERS = ["vh_common.cuh", "vh_device.cuh", "vh_mc_tables.h", "vh_mesh.h", "vh_internal.h"]
 
 ENGINE_LIB = os.path.join(LIB, "libvhsdf.so")
 SYNTH_LIB = os.path.join(LIB, "libvhsynth.so")

@@ -57,6 +57,8 @@ struct vh_handle {
   cudaEvent_t ev[kNumEvents] = {};
   bool ev_pending = false;
   bool ev_has_mc = false;
+  void *d_work = nullptr;  // workspace of the gradient / refinement calls
+  size_t work_bytes = 0;
   int64_t frames = 0;
   bool nb_valid = false;  // frame_nb matches the current block list
   std::string last_error;
@@ -280,6 +282,7 @@ void free_all(vh_handle *h) {
   cudaFree(h->d_pose);
   cudaFree(h->d_pix);
   cudaFree(h->d_tris);
+  cudaFree(h->d_work);
   if (h->h_pose_ring) cudaFreeHost(h->h_pose_ring);
   if (h->h_state) cudaFreeHost(h->h_state);
   for (auto &e : h->ring_ev)
@@ -355,6 +358,31 @@ cudaStream_t handle_stream(const vh_handle *h) { return h->stream; }
 int handle_device(const vh_handle *h) { return h->p.device; }
 vh_status handle_fail(vh_handle *h, vh_status s, const char *msg) { return fail(h, s, msg); }
 vh_status handle_sync(vh_handle *h) { return sync_and_check(h); }
+CamParams handle_cam(const vh_handle *h) { return h->C; }
+int handle_sm_count(const vh_handle *h) { return h->sm_count; }
+vh_status handle_stage_depth(vh_handle *h, const void *depth, int fmt, int mem, const void **dev) {
+  if (!depth || (fmt != VH_DEPTH_U16_MM && fmt != VH_DEPTH_F32_M) ||
+      (mem != VH_MEM_HOST && mem != VH_MEM_DEVICE))
+    return fail(h, VH_ERR_INVALID_ARG, "bad depth argument");
+  const size_t bytes = (size_t)h->p.width * h->p.height * (fmt == VH_DEPTH_U16_MM ? 2 : 4);
+  VH_CUDA(h, cudaMemcpyAsync(h->d_depth, depth, bytes,
+                             mem == VH_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                             h->stream));
+  *dev = h->d_depth;
+  return VH_OK;
+}
+vh_status handle_workspace(vh_handle *h, size_t bytes, void **ptr) {
+  if (bytes > h->work_bytes) {
+    VH_CUDA(h, cudaStreamSynchronize(h->stream));
+    cudaFree(h->d_work);
+    h->d_work = nullptr;
+    h->work_bytes = 0;
+    VH_CUDA(h, cudaMalloc(&h->d_work, bytes));
+    h->work_bytes = bytes;
+  }
+  *ptr = h->d_work;
+  return VH_OK;
+}
 }  // namespace vh
 
 extern "C" {

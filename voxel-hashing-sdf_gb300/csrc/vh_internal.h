@@ -12,4 +12,11 @@ int handle_device(const vh_handle *h);
 vh_status handle_fail(vh_handle *h, vh_status s, const char *msg);
 // Waits for the handle's stream and reports sticky device errors.
 vh_status handle_sync(vh_handle *h);
+CamParams handle_cam(const vh_handle *h);
+int handle_sm_count(const vh_handle *h);
+// Copies one depth image into the handle's staging buffer (stream-ordered)
+// and returns its device address.
+vh_status handle_stage_depth(vh_handle *h, const void *depth, int fmt, int mem, const void **dev);
+// Device workspace owned by the handle, grown on demand, freed with it.
+vh_status handle_workspace(vh_handle *h, size_t bytes, void **ptr);
 }  // namespace vh

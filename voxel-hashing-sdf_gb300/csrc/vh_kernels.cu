@@ -26,6 +26,7 @@
 // distance between its end blocks); no kernel waits on another thread.
 
 #include "vh_common.cuh"
+#include "vh_device.cuh"
 #include "vh_mc_tables.h"
 
 namespace vh {
@@ -76,23 +77,6 @@ __device__ uint32_t slot_insert(const VolumeView &V, unsigned long long key, boo
   atomicOr(&V.st->error, kErrTableFull);
   *created = false;
   return kNoBlock;
-}
-
-// Slot of `key` or kNoBlock.  Only valid between kernels that insert.
-__device__ __forceinline__ uint32_t slot_find(const VolumeView &V, unsigned long long key) {
-  const uint32_t h = (uint32_t)mix64(key) & V.slot_mask;
-  for (int i = 0; i < V.max_probe; ++i) {
-    const uint32_t s = (h + (uint32_t)i) & V.slot_mask;
-    const unsigned long long k = __ldg(&V.slots[s].key);
-    if (k == key) return s;
-    if (k == kEmptyKey) return kNoBlock;
-  }
-  return kNoBlock;
-}
-
-__device__ __forceinline__ uint32_t block_of(const VolumeView &V, unsigned long long key) {
-  const uint32_t s = slot_find(V, key);
-  return s == kNoBlock ? kNoBlock : __ldg(&V.slots[s].block);
 }
 
 // Block id for allocation ticket t of the open epoch (free list first).

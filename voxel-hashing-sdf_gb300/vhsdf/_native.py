@@ -33,6 +33,8 @@ VH_SCOPE_ALL = 1
 VH_FLAG_SYNC = 0x1
 VH_FLAG_NO_GRAPH = 0x2
 VH_FLAG_PROFILE = 0x4
+VH_REFINE_ADJOINT = 0
+VH_REFINE_FD = 1
 BLOCK_EDGE = 8
 BLOCK_VOXELS = 512
 
@@ -64,6 +66,11 @@ class VhStats(C.Structure):
 class VhTuning(C.Structure):
     _fields_ = [("integrate_variant", C.c_int32), ("integrate_ctas_per_sm", C.c_int32),
                 ("mc_ctas_per_sm", C.c_int32), ("mc_variant", C.c_int32)]
+
+
+class VhRefineStats(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("valid_pixels", C.c_int32),
+                ("initial_rmse", C.c_float), ("final_rmse", C.c_float), ("ms", C.c_float)]
 
 
 class VhMeshView(C.Structure):
@@ -108,6 +115,10 @@ SIGNATURES = {
     "vh_get_tuning": (I32, [P, C.POINTER(VhTuning)]),
     "vh_set_tuning": (I32, [P, C.POINTER(VhTuning)]),
     "vh_autotune": (I32, [P, P, I32, P, P, I32, C.POINTER(VhTuning)]),
+    "vh_sdf_sample": (I32, [P, P, I64, P, P, P, I32]),
+    "vh_pose_normal_equations": (I32, [P, P, I32, I32, P, I32, I32, P]),
+    "vh_pose_refine": (I32, [P, P, I32, I32, P, I32, I32, I32, P, C.POINTER(VhRefineStats)]),
+    "vh_integrate_vjp": (I32, [P, P, I32, P, P, P, P, I32]),
 }
 
 _lib = None

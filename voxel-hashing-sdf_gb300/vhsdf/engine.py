@@ -191,6 +191,64 @@ class Volume:
         self._check(self._L.vh_block_list(self._h, out.ctypes.data, n.value, C.byref(n)))
         return out
 
+    # ---- gradients and pose refinement ----
+    def sdf_sample(self, xyz):
+        """Trilinear sdf (units of T), gradient (per metre) and validity at
+        world points; numpy in, numpy out (torch CUDA tensors: device path)."""
+        if _is_cuda_tensor(xyz):
+            import torch
+            n = xyz.numel() // 3
+            phi = torch.empty(n, dtype=torch.float32, device=xyz.device)
+            grad = torch.empty((n, 3), dtype=torch.float32, device=xyz.device)
+            valid = torch.empty(n, dtype=torch.uint8, device=xyz.device)
+            self._check(self._L.vh_sdf_sample(self._h, xyz.data_ptr(), n, phi.data_ptr(),
+                                              grad.data_ptr(), valid.data_ptr(), N.VH_MEM_DEVICE))
+            return phi, grad, valid.bool()
+        pts = np.ascontiguousarray(np.asarray(xyz, np.float32).reshape(-1, 3))
+        n = pts.shape[0]
+        phi = np.empty(n, np.float32)
+        grad = np.empty((n, 3), np.float32)
+        valid = np.empty(n, np.uint8)
+        self._check(self._L.vh_sdf_sample(self._h, pts.ctypes.data, n, phi.ctypes.data,
+                                          grad.ctypes.data, valid.ctypes.data, N.VH_MEM_HOST))
+        return phi, grad, valid.astype(bool)
+
+    def pose_normal_equations(self, depth, c2w, stride=1, method="adjoint"):
+        d = _Arg(depth)
+        pose = np.ascontiguousarray(np.asarray(c2w, np.float32).reshape(16))
+        out = np.empty(29, np.float64)
+        m = N.VH_REFINE_FD if method == "fd" else N.VH_REFINE_ADJOINT
+        self._check(self._L.vh_pose_normal_equations(self._h, d.ptr, _depth_fmt(d.dtype), d.mem,
+                                                     pose.ctypes.data, stride, m,
+                                                     out.ctypes.data))
+        return out
+
+    def pose_refine(self, depth, c2w, iterations=20, stride=1, method="adjoint"):
+        """Gauss-Newton refinement of a camera pose against the volume;
+        returns (refined 4x4 c2w, stats dict)."""
+        d = _Arg(depth)
+        pose = np.ascontiguousarray(np.asarray(c2w, np.float32).reshape(16))
+        out = np.empty(16, np.float32)
+        st = N.VhRefineStats()
+        m = N.VH_REFINE_FD if method == "fd" else N.VH_REFINE_ADJOINT
+        self._check(self._L.vh_pose_refine(self._h, d.ptr, _depth_fmt(d.dtype), d.mem,
+                                           pose.ctypes.data, iterations, stride, m,
+                                           out.ctypes.data, C.byref(st)))
+        return out.reshape(4, 4), {f: getattr(st, f) for f, _ in N.VhRefineStats._fields_}
+
+    def integrate_vjp(self, depth, c2w, grad_sdf):
+        """dL/ddepth (H x W) and dL/dxi (6) of the last integration, given
+        dL/dsdf per voxel of the block list (n_blocks x 512, host arrays)."""
+        d = _Arg(depth)
+        pose = np.ascontiguousarray(np.asarray(c2w, np.float32).reshape(16))
+        g = np.ascontiguousarray(grad_sdf, np.float32)
+        gd = np.empty((self.params.height, self.params.width), np.float32)
+        gp = np.empty(6, np.float32)
+        self._check(self._L.vh_integrate_vjp(self._h, d.ptr, _depth_fmt(d.dtype),
+                                             pose.ctypes.data, g.ctypes.data, gd.ctypes.data,
+                                             gp.ctypes.data, N.VH_MEM_HOST))
+        return gd, gp
+
     # ---- volume I/O ----
     def export_blocks(self):
         n = C.c_int64()
