@@ -279,7 +279,9 @@ typedef struct vh_refine_stats {
   int32_t valid_pixels;  /* residuals in the last linearisation              */
   float initial_rmse;    /* metres, at the initial pose                      */
   float final_rmse;      /* metres, at the last linearised pose              */
-  float ms;              /* device + host time of the call                   */
+  float ms;              /* whole call: depth staging, pose upload, steps,   */
+                         /* result download                                  */
+  float ms_steps;        /* the Gauss-Newton steps alone (device events)     */
 } vh_refine_stats;
 
 /* Trilinear TSDF value (units of the truncation distance) at n world points
@@ -297,7 +299,11 @@ vh_status vh_pose_normal_equations(vh_handle *h, const void *depth, int32_t dept
                                    int32_t mem, const float *c2w, int32_t stride,
                                    int32_t method, double *terms);
 /* `iterations` Gauss-Newton steps from c2w_init against the fused volume;
- * writes the refined pose to c2w_out (both row-major 4x4, host). */
+ * writes the refined pose to c2w_out (both row-major 4x4, host).  The steps
+ * run on the device without host round trips: each is one kernel launch
+ * whose last CTA solves the 6x6 system in FP64 and composes the pose (the
+ * launches of a call are replayed as one CUDA graph).  A step whose system is
+ * singular or has fewer than 6 residuals ends the refinement early. */
 vh_status vh_pose_refine(vh_handle *h, const void *depth, int32_t depth_fmt, int32_t mem,
                          const float *c2w_init, int32_t iterations, int32_t stride,
                          int32_t method, float *c2w_out, vh_refine_stats *stats);

@@ -98,6 +98,8 @@ def test_normal_equations_match_fp64(room):
 
 
 def perturb(pose, deg, metres, seed):
+    """Rotates the camera by `deg` about a random axis through its centre and
+    moves the centre by `metres` along a random direction."""
     rng = np.random.default_rng(seed)
     axis = rng.normal(size=3)
     axis /= np.linalg.norm(axis)
@@ -108,8 +110,34 @@ def perturb(pose, deg, metres, seed):
     dirn /= np.linalg.norm(dirn)
     out = pose.astype(np.float64).copy()
     out[:3, :3] = R @ out[:3, :3]
-    out[:3, 3] = R @ out[:3, 3] + metres * dirn
+    out[:3, 3] = out[:3, 3] + metres * dirn
     return out.astype(np.float32)
+
+
+def se3_left_exp(xi, P):
+    """exp(xi) @ P in FP64 for xi = (v, w)."""
+    v, w = np.asarray(xi[:3], np.float64), np.asarray(xi[3:], np.float64)
+    th = np.linalg.norm(w)
+    K = np.array([[0, -w[2], w[1]], [w[2], 0, -w[0]], [-w[1], w[0], 0]])
+    if th < 1e-12:
+        A, B, Cc = 1.0, 0.5, 1.0 / 6.0
+    else:
+        A, B, Cc = np.sin(th) / th, (1 - np.cos(th)) / th**2, (th - np.sin(th)) / th**3
+    R = np.eye(3) + A * K + B * K @ K
+    V = np.eye(3) + B * K + Cc * K @ K
+    out = np.eye(4)
+    out[:3, :3] = R @ P[:3, :3]
+    out[:3, 3] = R @ P[:3, 3] + V @ v
+    return out
+
+
+def gn_step(terms, damp=1e-6):
+    H = np.zeros((6, 6))
+    iu = np.triu_indices(6)
+    H[iu] = terms[:21]
+    H = H + np.triu(H, 1).T
+    H[np.diag_indices(6)] *= 1 + damp
+    return -np.linalg.solve(H, terms[21:27])
 
 
 def pose_error(a, b):
@@ -129,6 +157,37 @@ def test_pose_refinement_converges(room, method):
         dt, ang = pose_error(out, gt)
         assert dt < 2e-3 and ang < 0.1, (method, f, dt, ang, st)
         assert st["final_rmse"] < st["initial_rmse"]
+
+
+@pytest.mark.parametrize("method", ["adjoint", "fd"])
+def test_device_step_matches_host_solve(room, method):
+    """One device step (reduce, FP64 Cholesky, exp) equals the host solve of
+    the normal equations at the same pose."""
+    scene, vol, orc, e = room
+    d, c, gt = scene.render(9)
+    init = perturb(gt, 1.0, 0.01, 21)
+    terms = vol.pose_normal_equations(d, init, stride=2, method=method)
+    want = se3_left_exp(gn_step(terms), init.astype(np.float64))
+    got, st = vol.pose_refine(d, init, iterations=1, stride=2, method=method)
+    assert st["iterations"] == 1 and abs(st["valid_pixels"] - terms[28]) <= 2
+    assert np.allclose(got, want, atol=2e-6), np.abs(got - want).max()
+    # determinism: the same call gives the same bits
+    again, _ = vol.pose_refine(d, init, iterations=1, stride=2, method=method)
+    assert np.array_equal(got, again)
+
+
+def test_refine_stops_without_residuals(room):
+    scene, vol, orc, e = room
+    d, c, gt = scene.render(3)
+    init = perturb(gt, 1.0, 0.01, 5)
+    ref, _ = vol.pose_refine(d, init, iterations=20, stride=2)
+    empty = np.zeros_like(d)
+    out, st = vol.pose_refine(empty, gt, iterations=5, stride=1)
+    assert st["iterations"] == 0 and st["valid_pixels"] == 0
+    assert np.array_equal(out, gt)
+    # the next call on the same handle starts afresh
+    again, st = vol.pose_refine(d, init, iterations=20, stride=2)
+    assert st["iterations"] == 20 and np.array_equal(again, ref)
 
 
 def test_integration_vjp_against_fp64_finite_differences(gpu):

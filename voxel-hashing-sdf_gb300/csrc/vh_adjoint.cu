@@ -6,7 +6,9 @@
 //     analytic gradient (the adjoint of sampling);
 //   * per-pixel SDF residuals of a back-projected depth frame and their
 //     Jacobians with respect to a left se(3) perturbation of the camera pose,
-//     reduced on the GPU to 6x6 Gauss-Newton normal equations;
+//     reduced on the GPU to 6x6 Gauss-Newton normal equations, solved and
+//     composed with the pose on the device (FP64) so that a refinement runs
+//     its steps without host round trips;
 //   * the same normal equations from forward-only central differences (the
 //     plain FD-Jacobian method: 13 residual evaluations per step), for
 //     comparison;
@@ -20,8 +22,8 @@
 // metres (T * sdf).
 
 #include <cmath>
+#include <cstdint>
 #include <cstring>
-#include <vector>
 
 #include "vh_device.cuh"
 #include "vh_internal.h"
@@ -44,9 +46,12 @@ __device__ __forceinline__ uint32_t nb_block(const VolumeView &V, int bx, int by
 
 // Trilinear interpolation of the TSDF at world point (x, y, z) and its
 // gradient.  Fails when any of the 8 corner voxels is unallocated or has a
-// weight below min_w.
-__device__ Sample sample_tsdf(const VolumeView &V, float inv_voxel, float min_w, float x, float y,
-                              float z) {
+// weight below min_w.  The corner blocks are resolved first (one hash lookup,
+// more only where the cell crosses a block face); then all 16 loads are
+// issued together, without a branch between them (a missing block reads
+// block 0, which always exists, and fails the sample afterwards).
+__device__ __forceinline__ Sample sample_tsdf(const VolumeView &V, float inv_voxel, float min_w,
+                                              float x, float y, float z) {
   Sample s;
   s.ok = false;
   const float qx = x * inv_voxel, qy = y * inv_voxel, qz = z * inv_voxel;
@@ -66,17 +71,21 @@ __device__ Sample sample_tsdf(const VolumeView &V, float inv_voxel, float min_w,
   b[5] = cz ? (cx ? nb_block(V, bx + 1, by, bz + 1) : b[4]) : b[1];
   b[6] = cz ? (cy ? nb_block(V, bx, by + 1, bz + 1) : b[4]) : b[2];
   b[7] = cz ? ((cx || cy) ? nb_block(V, bx + cx, by + cy, bz + 1) : b[4]) : b[3];
-  float val[8];
+  float val[8], w[8];
+  bool found = true;
 #pragma unroll
   for (int c = 0; c < 8; ++c) {
     const int dx = c & 1, dy = (c >> 1) & 1, dz = c >> 2;
-    if (b[c] == kNoBlock) return s;
+    found = found && b[c] != kNoBlock;
     const int li = ((lx + dx) & 7) + 8 * ((ly + dy) & 7) + 64 * ((lz + dz) & 7);
-    const float *base = V.pool + (size_t)b[c] * kBlockWords;
-    const float w = __ldg(base + kB3 + li);
-    if (w < min_w) return s;
+    const float *base = V.pool + (size_t)(b[c] == kNoBlock ? 0u : b[c]) * kBlockWords;
+    w[c] = __ldg(base + kB3 + li);
     val[c] = __ldg(base + li);
   }
+  bool observed = true;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) observed = observed && !(w[c] < min_w);
+  if (!found || !observed) return s;
   const float gx0 = 1.0f - fx, gy0 = 1.0f - fy, gz0 = 1.0f - fz;
   // phi = sum_c w_c val_c, w_c = (dx ? fx : 1-fx)(dy ? fy : 1-fy)(dz ? fz : 1-fz)
   const float c00 = val[0] * gx0 + val[1] * fx, c10 = val[2] * gx0 + val[3] * fx;
@@ -136,24 +145,43 @@ __device__ __forceinline__ Px backproject(const CamParams &C, const float *P, in
   return r;
 }
 
-// Sums the kTerms values of every thread of the CTA into out[kTerms].
-template <int kThreads>
-__device__ __forceinline__ void cta_sum_terms(float (&v)[kTerms], float *out) {
-  __shared__ float part[kThreads / 32][kTerms];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+// Warp sum of 32 values per lane by a transposing butterfly: at offset o a
+// lane keeps the half of its remaining values selected by bit o of its lane
+// index and adds its partner's copy of that half, so 16 + 8 + 4 + 2 + 1
+// shuffles leave lane l with the warp sum of value l (in a fixed order).
+__device__ __forceinline__ float warp_transpose_sum(float (&a)[32]) {
+  const int lane = threadIdx.x & 31;
 #pragma unroll
-  for (int k = 0; k < kTerms; ++k) {
-    float x = v[k];
+  for (int o = 16; o > 0; o >>= 1) {
+    const bool up = lane & o;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(kFull, x, o);
-    if (lane == 0) part[warp][k] = x;
+    for (int i = 0; i < o; ++i) {
+      const float send = up ? a[i] : a[i + o];
+      const float keep = up ? a[i + o] : a[i];
+      a[i] = keep + __shfl_xor_sync(kFull, send, o);
+    }
   }
-  __syncthreads();
-  if (threadIdx.x < kTerms) {
-    float x = 0.0f;
+  return a[0];
+}
+
+// Sums the kTerms values of every thread of the CTA into out[k * stride]:
+// a transposing warp sum, then the warps' sums by warp 0 the same way.
+template <int kThreads>
+__device__ __forceinline__ void cta_sum_terms(float (&v)[kTerms], float *out, int stride = 1) {
+  constexpr int kWarps = kThreads / 32;
+  static_assert(kWarps <= 32, "one value per lane in the second stage");
+  __shared__ float part[kWarps][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float a[32];
 #pragma unroll
-    for (int w = 0; w < kThreads / 32; ++w) x += part[w][threadIdx.x];
-    out[threadIdx.x] = x;
+  for (int k = 0; k < 32; ++k) a[k] = k < kTerms ? v[k] : 0.0f;
+  part[warp][lane] = warp_transpose_sum(a);
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < 32; ++k) a[k] = lane < kWarps ? part[lane][k] : 0.0f;
+    const float x = warp_transpose_sum(a);
+    if (lane < kTerms) out[lane * stride] = x;
   }
 }
 
@@ -170,88 +198,343 @@ __device__ __forceinline__ void add_terms(float (&v)[kTerms], float r, const flo
   v[28] += 1.0f;
 }
 
-// Adjoint normal equations: per sampled pixel, r = T * sdf(X_w) and
-// J = dr / d(v, w) for X_w -> X_w + v + w x X_w, i.e. T * [g ; X_w x g].
-// Pixels whose sample is invalid or truncated (|sdf| >= 1) are skipped.
-__global__ void __launch_bounds__(256) k_pose_terms(VolumeView V, CamParams C, const void *depth,
-                                                    int fmt, const float *__restrict__ pose,
-                                                    int stride, float inv_voxel,
-                                                    float *__restrict__ partials) {
-  float P[12];
+// ---- Gauss-Newton pose refinement on the device -----------------------------
+//
+// A pose is a row-major 3x4 camera-to-world matrix.  The master copy is FP64
+// (pose composition); the kernels back-project with an FP32 copy.
+
+__host__ __device__ constexpr double inv_factorial(int n) {
+  double f = 1.0;
+  for (int i = 2; i <= n; ++i) f *= i;
+  return 1.0 / f;
+}
+
+// Coefficients A = sin t / t, B = (1 - cos t) / t^2, C = (t - sin t) / t^3 of
+// the SE(3) exponential, t^2 = th2 (host, FP64).  Below t = 0.25 rad they are
+// summed from their Taylor series, sum_n (-1)^n t^2n / (2n + k)! for
+// k = 1, 2, 3, to seven terms (the first term left out is below 1e-20);
+// larger angles use sin and cos.
+inline void exp_coeffs(double th2, double &A, double &B, double &C) {
+  if (th2 < 0.0625) {
+    // coefficients fixed at compile time: (-1)^n / (2n + k)!
+    constexpr double a0 = inv_factorial(1), a1 = -inv_factorial(3), a2 = inv_factorial(5),
+                     a3 = -inv_factorial(7), a4 = inv_factorial(9), a5 = -inv_factorial(11),
+                     a6 = inv_factorial(13);
+    constexpr double b0 = inv_factorial(2), b1 = -inv_factorial(4), b2 = inv_factorial(6),
+                     b3 = -inv_factorial(8), b4 = inv_factorial(10), b5 = -inv_factorial(12),
+                     b6 = inv_factorial(14);
+    constexpr double c0 = inv_factorial(3), c1 = -inv_factorial(5), c2 = inv_factorial(7),
+                     c3 = -inv_factorial(9), c4 = inv_factorial(11), c5 = -inv_factorial(13),
+                     c6 = inv_factorial(15);
+    const double x = th2;
+    A = a0 + x * (a1 + x * (a2 + x * (a3 + x * (a4 + x * (a5 + x * a6)))));
+    B = b0 + x * (b1 + x * (b2 + x * (b3 + x * (b4 + x * (b5 + x * b6)))));
+    C = c0 + x * (c1 + x * (c2 + x * (c3 + x * (c4 + x * (c5 + x * c6)))));
+  } else {
+    const double th = sqrt(th2);
+    A = sin(th) / th;
+    B = (1.0 - cos(th)) / th2;
+    C = (th - sin(th)) / (th2 * th);
+  }
+}
+
+// exp(xi) * P for xi = (v, w) (host, FP64): Rodrigues for the rotation, the
+// left Jacobian of SO(3) for the translation, with W^2 = w w^T - |w|^2 I.
+inline void se3_left_exp(const double xi[6], const double P[12], double Q[12]) {
+  const double w[3] = {xi[3], xi[4], xi[5]};
+  const double th2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+  double A, B, Cc;
+  exp_coeffs(th2, A, B, Cc);
+  const double W[3][3] = {{0, -w[2], w[1]}, {w[2], 0, -w[0]}, {-w[1], w[0], 0}};
+  double dR[3][3], Vm[3][3];
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) {
+      const double w2 = w[r] * w[c] - (r == c ? th2 : 0.0);
+      const double I = r == c ? 1.0 : 0.0;
+      dR[r][c] = I + A * W[r][c] + B * w2;
+      Vm[r][c] = I + B * W[r][c] + Cc * w2;
+    }
+  for (int r = 0; r < 3; ++r) {
+    for (int c = 0; c < 4; ++c)
+      Q[4 * r + c] = dR[r][0] * P[c] + dR[r][1] * P[4 + c] + dR[r][2] * P[8 + c];
+    Q[4 * r + 3] += Vm[r][0] * xi[0] + Vm[r][1] * xi[1] + Vm[r][2] * xi[2];
+  }
+}
+
+// Solves (H + damp * diag(H)) x = -g for the 6x6 system of the kTerms layout
+// (upper triangle row by row, then g) by Cholesky of the Jacobi-scaled matrix
+// (unit diagonal), in FP32: a Gauss-Newton step needs no more, and FP64
+// arithmetic is slow on this GPU.  False if the matrix is not positive
+// definite or the step is not finite.
+__device__ __forceinline__ bool solve6(const float *terms, float damp, float x[6]) {
+  float H[6][6], L[6][6], inv[6], sc[6], y[6];
+  int k = 0;
 #pragma unroll
-  for (int k = 0; k < 12; ++k) P[k] = __ldg(pose + k);
-  float acc[kTerms];
+  for (int a = 0; a < 6; ++a)
 #pragma unroll
-  for (int k = 0; k < kTerms; ++k) acc[k] = 0.0f;
-  const int ws = (C.width + stride - 1) / stride, hs = (C.height + stride - 1) / stride;
-  const int npx = ws * hs;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < npx; q += gridDim.x * blockDim.x) {
-    const int u = (q % ws) * stride, v = (q / ws) * stride;
-    const float d = pixel_depth(depth, fmt, v * C.width + u, C.depth_scale);
-    const Px X = backproject(C, P, u, v, d);
-    if (!X.ok) continue;
+    for (int b = a; b < 6; ++b) H[a][b] = H[b][a] = terms[k++];
+  bool ok = true;
+#pragma unroll
+  for (int a = 0; a < 6; ++a) {
+    H[a][a] *= 1.0f + damp;
+    ok = ok && H[a][a] > 0.0f;
+    sc[a] = rsqrtf(H[a][a]);
+  }
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = 0; j <= i; ++j) {
+      float s = H[i][j] * sc[i] * sc[j];
+#pragma unroll
+      for (int m = 0; m < j; ++m) s -= L[i][m] * L[j][m];
+      if (i == j) {
+        ok = ok && s > 0.0f;
+        inv[i] = rsqrtf(s);
+        L[i][i] = s * inv[i];
+      } else {
+        L[i][j] = s * inv[j];
+      }
+    }
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    float s = -terms[21 + i] * sc[i];
+#pragma unroll
+    for (int m = 0; m < i; ++m) s -= L[i][m] * y[m];
+    y[i] = s * inv[i];
+  }
+#pragma unroll
+  for (int i = 5; i >= 0; --i) {
+    float s = y[i];
+#pragma unroll
+    for (int m = i + 1; m < 6; ++m) s -= L[m][i] * x[m];
+    x[i] = s * inv[i];
+  }
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    x[i] *= sc[i];
+    ok = ok && fabsf(x[i]) < 1e30f;
+  }
+  return ok;
+}
+
+// Increment of exp(xi) for xi = (v, w) in FP32: D = dR - I (entries of the
+// order of |w|, so FP32 keeps them to ~1e-9 absolute) and t = V v, with
+// dR = I + A W + B W^2, V = I + B W + C W^2, W^2 = w w^T - |w|^2 I.
+__device__ inline void exp_increment(const float xi[6], float D[9], float t[3]) {
+  const float w[3] = {xi[3], xi[4], xi[5]};
+  const float th2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+  float A, B, Cc;
+  if (th2 < 0.0625f) {
+    constexpr float a1 = (float)-inv_factorial(3), a2 = (float)inv_factorial(5),
+                    a3 = (float)-inv_factorial(7), a4 = (float)inv_factorial(9);
+    constexpr float b0 = (float)inv_factorial(2), b1 = (float)-inv_factorial(4),
+                    b2 = (float)inv_factorial(6), b3 = (float)-inv_factorial(8),
+                    b4 = (float)inv_factorial(10);
+    constexpr float c0 = (float)inv_factorial(3), c1 = (float)-inv_factorial(5),
+                    c2 = (float)inv_factorial(7), c3 = (float)-inv_factorial(9),
+                    c4 = (float)inv_factorial(11);
+    // five terms: the first one left out is below 1e-10 for |w| < 0.25
+    A = 1.0f + th2 * (a1 + th2 * (a2 + th2 * (a3 + th2 * a4)));
+    B = b0 + th2 * (b1 + th2 * (b2 + th2 * (b3 + th2 * b4)));
+    Cc = c0 + th2 * (c1 + th2 * (c2 + th2 * (c3 + th2 * c4)));
+  } else {
+    const float th = sqrtf(th2);
+    A = sinf(th) / th;
+    B = (1.0f - cosf(th)) / th2;
+    Cc = (th - sinf(th)) / (th2 * th);
+  }
+  const float W[3][3] = {{0, -w[2], w[1]}, {w[2], 0, -w[0]}, {-w[1], w[0], 0}};
+  for (int r = 0; r < 3; ++r) {
+    float tr = 0.0f;
+    for (int c = 0; c < 3; ++c) {
+      const float w2 = w[r] * w[c] - (r == c ? th2 : 0.0f);
+      D[3 * r + c] = A * W[r][c] + B * w2;
+      tr += ((r == c ? 1.0f : 0.0f) + B * W[r][c] + Cc * w2) * xi[c];
+    }
+    t[r] = tr;
+  }
+}
+
+constexpr int kFdPoses = 13;  // current pose, then +/- a step along each coordinate
+
+// Device state of one refinement (or one linearisation), in HBM.
+struct RefineState {
+  double pose[12];            // master pose, FP64
+  double terms[kTerms];       // last reduced normal-equation terms
+  float fd_step[6];           // FD step per coordinate
+  float inv2eps[6];           // 1 / (2 fd_step)
+  float rows[kFdPoses * 12];  // FP32 poses: [0] current, [1 + 2k] / [2 + 2k] = +/- step k
+  uint32_t counter;           // CTAs of the current launch that finished
+  int32_t updates;            // pose updates applied
+  int32_t stopped;            // a solve failed: later launches do nothing
+  int32_t iter;               // launches that linearised
+};
+
+// SDF residual of one back-projected pixel under pose P: T * sdf, NaN when the
+// sample is invalid or truncated.
+__device__ __forceinline__ float pixel_residual(const VolumeView &V, const CamParams &C,
+                                                const float *P, int u, int v, float d,
+                                                float inv_voxel) {
+  const Px X = backproject(C, P, u, v, d);
+  if (X.ok) {
     const Sample s = sample_tsdf(V, inv_voxel, C.mc_min_weight, X.x, X.y, X.z);
-    if (!s.ok || !(fabsf(s.phi) < 1.0f)) continue;
-    const float T = C.trunc;
-    const float J[6] = {T * s.gx, T * s.gy, T * s.gz, T * (X.y * s.gz - X.z * s.gy),
-                        T * (X.z * s.gx - X.x * s.gz), T * (X.x * s.gy - X.y * s.gx)};
-    add_terms(acc, T * s.phi, J);
+    if (s.ok && fabsf(s.phi) < 1.0f) return C.trunc * s.phi;
   }
-  cta_sum_terms<256>(acc, partials + (size_t)blockIdx.x * kTerms);
+  return __int_as_float(0x7FC00000);
 }
 
-// Residuals of every sampled pixel under `np` poses (forward only): r = T *
-// sdf, NaN where invalid or truncated.
-__global__ void __launch_bounds__(256) k_pose_residuals(VolumeView V, CamParams C,
-                                                        const void *depth, int fmt,
-                                                        const float *__restrict__ poses, int np,
-                                                        int stride, float inv_voxel,
-                                                        float *__restrict__ res) {
+// Threads per CTA of the refinement step: one CTA per SM for the adjoint (so
+// that the last CTA reduces only one partial per SM); the FD variant needs
+// more registers per thread and runs three 256-thread CTAs per SM.
+template <bool kFD>
+struct RefineShape {
+  static constexpr int kThreads = kFD ? 256 : 1024;
+  static constexpr int kMinCtas = kFD ? 3 : 1;
+};
+
+// One Gauss-Newton step.  Every CTA accumulates the 29 normal-equation terms
+// of its pixels (analytic Jacobians T [g ; X x g] from the sampling adjoint,
+// or, for kFD, central differences of 13 residual evaluations per pixel) and
+// stores them in partials[k * gridDim.x + blockIdx.x]; the last CTA to finish
+// sums the partials in a fixed order (deterministic), and with kSolve solves
+// the 6x6 system and composes exp(xi) * pose (the pose itself in FP64).  No
+// CTA waits for another.
+template <bool kFD, bool kSolve>
+__global__ void __launch_bounds__(RefineShape<kFD>::kThreads, RefineShape<kFD>::kMinCtas)
+    k_refine_step(VolumeView V, CamParams C, const void *depth, int fmt, int stride,
+                  float inv_voxel, RefineState *S, float *__restrict__ partials,
+                  float2 *__restrict__ hist, int hist_cap) {
+  constexpr int kThreads = RefineShape<kFD>::kThreads;
+  constexpr int kRows = kFD ? kFdPoses : 1;
+  __shared__ float rows[kRows * 12];
+  __shared__ float inv2eps[6];
+  __shared__ float tot[kTerms];
+  __shared__ int last;
+  // Thread i of the grid takes pixels i, i + threads, ...; the next depth
+  // value is loaded while the current pixel is sampled.
   const int ws = (C.width + stride - 1) / stride, hs = (C.height + stride - 1) / stride;
   const int npx = ws * hs;
-  const int pi = blockIdx.y;
-  if (pi >= np) return;
-  float P[12];
-#pragma unroll
-  for (int k = 0; k < 12; ++k) P[k] = __ldg(poses + 12 * pi + k);
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < npx; q += gridDim.x * blockDim.x) {
-    const int u = (q % ws) * stride, v = (q / ws) * stride;
-    const float d = pixel_depth(depth, fmt, v * C.width + u, C.depth_scale);
-    const Px X = backproject(C, P, u, v, d);
-    float r = __int_as_float(0x7FC00000);
-    if (X.ok) {
-      const Sample s = sample_tsdf(V, inv_voxel, C.mc_min_weight, X.x, X.y, X.z);
-      if (s.ok && fabsf(s.phi) < 1.0f) r = C.trunc * s.phi;
-    }
-    res[(size_t)pi * npx + q] = r;
-  }
-}
-
-// Normal equations from the 13 residual vectors of the FD method: pose 0 is
-// the current estimate, poses 1 + 2k and 2 + 2k are the +/- steps of
-// coordinate k; pixels valid under all 13 poses contribute.
-__global__ void __launch_bounds__(256) k_fd_terms(const float *__restrict__ res, int npx,
-                                                  const float *__restrict__ inv2eps,
-                                                  float *__restrict__ partials) {
+  const int lane = threadIdx.x & 31;
+  const int wstride = gridDim.x * blockDim.x;
+  const int q_first = blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+  auto depth_at = [&](int q) {
+    return q < npx ? pixel_depth(depth, fmt, ((q / ws) * stride) * C.width + (q % ws) * stride,
+                                 C.depth_scale)
+                   : 0.0f;
+  };
+  float d_next = depth_at(q_first + lane);
+  if (S->stopped) return;  // uniform: written only between launches
+  for (int i = threadIdx.x; i < kRows * 12; i += blockDim.x) rows[i] = S->rows[i];
+  if (kFD && threadIdx.x < 6) inv2eps[threadIdx.x] = S->inv2eps[threadIdx.x];
+  __syncthreads();
   float acc[kTerms];
 #pragma unroll
   for (int k = 0; k < kTerms; ++k) acc[k] = 0.0f;
-  float ie[6];
+  for (int q0 = q_first; q0 < npx; q0 += wstride) {
+    const int q = q0 + lane;
+    const float d = d_next;
+    d_next = depth_at(q + wstride);
+    const int u = (q % ws) * stride, v = (q / ws) * stride;
+    if (!(q < npx && d > C.min_depth && d <= C.max_depth)) continue;
+    if constexpr (kFD) {
+      const float r0 = pixel_residual(V, C, rows, u, v, d, inv_voxel);
+      if (r0 != r0) continue;
+      float J[6];
+      bool ok = true;
 #pragma unroll
-  for (int k = 0; k < 6; ++k) ie[k] = __ldg(inv2eps + k);
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < npx; q += gridDim.x * blockDim.x) {
-    const float r0 = res[q];
-    bool ok = r0 == r0;
-    float J[6];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      const float rp = res[(size_t)(1 + 2 * k) * npx + q], rm = res[(size_t)(2 + 2 * k) * npx + q];
-      ok = ok && rp == rp && rm == rm;
-      J[k] = (rp - rm) * ie[k];
+      for (int k = 0; k < 6; ++k) {
+        const float rp = pixel_residual(V, C, rows + 12 * (1 + 2 * k), u, v, d, inv_voxel);
+        const float rm = pixel_residual(V, C, rows + 12 * (2 + 2 * k), u, v, d, inv_voxel);
+        ok = ok && rp == rp && rm == rm;
+        J[k] = (rp - rm) * inv2eps[k];
+      }
+      if (ok) add_terms(acc, r0, J);
+    } else {
+      const Px X = backproject(C, rows, u, v, d);
+      const Sample s = sample_tsdf(V, inv_voxel, C.mc_min_weight, X.x, X.y, X.z);
+      if (!s.ok || !(fabsf(s.phi) < 1.0f)) continue;
+      const float T = C.trunc;
+      const float J[6] = {T * s.gx, T * s.gy, T * s.gz, T * (X.y * s.gz - X.z * s.gy),
+                          T * (X.z * s.gx - X.x * s.gz), T * (X.x * s.gy - X.y * s.gx)};
+      add_terms(acc, T * s.phi, J);
     }
-    if (ok) add_terms(acc, r0, J);
   }
-  cta_sum_terms<256>(acc, partials + (size_t)blockIdx.x * kTerms);
+  const int G = (int)gridDim.x;
+  cta_sum_terms<kThreads>(acc, partials + blockIdx.x, G);
+  __threadfence();  // this CTA's partials before its count
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(&S->counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // Last CTA: warp w sums terms w, w + nwarps, ...; lane l adds partials
+  // l, l + 32, ... in order, then a fixed shuffle tree (deterministic).
+  const int t = threadIdx.x;
+  for (int k = t >> 5; k < kTerms; k += kThreads / 32) {
+    const float *pk = partials + (size_t)k * G;
+    float x = 0.0f;
+#pragma unroll 8
+    for (int i = lane; i < G; i += 32) x += __ldcg(pk + i);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(kFull, x, o);
+    if (lane == 0) tot[k] = x;
+  }
+  __syncthreads();
+  if (t < kTerms) S->terms[t] = (double)tot[t];
+  if (!kSolve) {
+    if (t == 0) {
+      S->iter += 1;
+      S->counter = 0;
+    }
+    return;
+  }
+  // Solve (one thread, FP32), then compose exp(xi) * pose in FP64 with one
+  // thread per entry: pose + D * pose (+ t in the last column).
+  __shared__ float inc[12];  // D (3x3 row-major), t
+  __shared__ int solved;
+  if (t == 0) {
+    const int it = S->iter;
+    if (it < hist_cap) hist[it] = make_float2(tot[27], tot[28]);
+    float xi[6];
+    solved = tot[28] >= 6.0f && solve6(tot, 1e-6f, xi);
+    if (solved) {
+      exp_increment(xi, inc, inc + 9);
+      S->updates += 1;
+    } else {
+      S->stopped = 1;
+    }
+    S->iter = it + 1;
+    S->counter = 0;
+  }
+  __syncthreads();
+  if (!solved) return;
+  __shared__ float newrows[12];
+  if (t < 12) {
+    const int r = t >> 2, c = t & 3;
+    const double *P = S->pose;
+    double q = P[t];
+    q += (double)inc[3 * r] * P[c] + (double)inc[3 * r + 1] * P[4 + c] +
+         (double)inc[3 * r + 2] * P[8 + c];
+    if (c == 3) q += (double)inc[9 + r];
+    __syncwarp(0xFFFu);  // every entry read the old pose before any is replaced
+    S->pose[t] = q;
+    S->rows[t] = (float)q;
+    newrows[t] = (float)q;
+  }
+  if (!kFD) return;
+  __syncthreads();
+  if (t < 12) {  // FD pose t: exp(+/- step along coordinate t / 2) * pose, in FP32
+    const int k = t >> 1;
+    float xi[6] = {0, 0, 0, 0, 0, 0}, D[9], tt[3];
+    xi[k] = (t & 1) ? -S->fd_step[k] : S->fd_step[k];
+    exp_increment(xi, D, tt);
+    float *out = S->rows + 12 * (1 + t);
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 4; ++c)
+        out[4 * r + c] = newrows[4 * r + c] + (D[3 * r] * newrows[c] + D[3 * r + 1] * newrows[4 + c] +
+                                               D[3 * r + 2] * newrows[8 + c]) +
+                         (c == 3 ? tt[r] : 0.0f);
+  }
 }
 
 // Sums `n` CTA partials in a fixed order (deterministic) into out[kTerms].
@@ -332,186 +615,139 @@ __global__ void __launch_bounds__(128) k_integrate_vjp(VolumeView V, CamParams C
 // ---- host side ----------------------------------------------------------------
 using namespace vh;
 
+namespace vh {
+
+// Per-handle refinement buffers and the graph of the last refine call.
+struct RefineCtx {
+  int device = 0;
+  RefineState *d_state = nullptr;
+  RefineState *h_state = nullptr;  // pinned mirror
+  float *d_partials = nullptr;
+  int partial_cap = 0;
+  float2 *d_hist = nullptr;
+  float2 *h_hist = nullptr;  // pinned
+  int hist_cap = 0;
+  cudaEvent_t ev[4] = {};
+  cudaGraphExec_t graph = nullptr;
+  long long key[7] = {};  // method, stride, iterations, fmt, grid, stream, partial buffer
+};
+
+void refine_ctx_free(RefineCtx *c) {
+  if (!c) return;
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  cudaFree(c->d_state);
+  cudaFree(c->d_partials);
+  cudaFree(c->d_hist);
+  if (c->h_state) cudaFreeHost(c->h_state);
+  if (c->h_hist) cudaFreeHost(c->h_hist);
+  for (auto &e : c->ev)
+    if (e) cudaEventDestroy(e);
+  delete c;
+}
+
+}  // namespace vh
+
 namespace {
 
-// Rigid transform in double precision (pose composition happens here).
-struct Pose {
-  double R[3][3];
-  double t[3];
-};
+const double kFdStep = 1e-4;  // FD step per se(3) coordinate (metres / radians)
 
-Pose pose_from(const float *c2w) {
-  Pose p;
-  for (int r = 0; r < 3; ++r) {
-    for (int c = 0; c < 3; ++c) p.R[r][c] = c2w[4 * r + c];
-    p.t[r] = c2w[4 * r + 3];
-  }
-  return p;
-}
-
-void pose_to(const Pose &p, float *c2w) {
-  for (int r = 0; r < 3; ++r) {
-    for (int c = 0; c < 3; ++c) c2w[4 * r + c] = (float)p.R[r][c];
-    c2w[4 * r + 3] = (float)p.t[r];
-  }
-  c2w[12] = c2w[13] = c2w[14] = 0.0f;
-  c2w[15] = 1.0f;
-}
-
-// exp(xi) * p for xi = (v, w): the SE(3) exponential (Rodrigues for the
-// rotation, the left Jacobian for the translation).
-Pose left_exp(const double xi[6], const Pose &p) {
-  const double wx = xi[3], wy = xi[4], wz = xi[5];
-  const double th2 = wx * wx + wy * wy + wz * wz, th = std::sqrt(th2);
-  double A, B, Cc;
-  if (th < 1e-6) {
-    A = 1.0 - th2 / 6.0;
-    B = 0.5 - th2 / 24.0;
-    Cc = 1.0 / 6.0 - th2 / 120.0;
-  } else {
-    A = std::sin(th) / th;
-    B = (1.0 - std::cos(th)) / th2;
-    Cc = (th - std::sin(th)) / (th2 * th);
-  }
-  const double W[3][3] = {{0, -wz, wy}, {wz, 0, -wx}, {-wy, wx, 0}};
-  double W2[3][3];
-  for (int r = 0; r < 3; ++r)
-    for (int c = 0; c < 3; ++c) {
-      W2[r][c] = 0;
-      for (int k = 0; k < 3; ++k) W2[r][c] += W[r][k] * W[k][c];
-    }
-  double dR[3][3], Vm[3][3];
-  for (int r = 0; r < 3; ++r)
-    for (int c = 0; c < 3; ++c) {
-      const double I = r == c ? 1.0 : 0.0;
-      dR[r][c] = I + A * W[r][c] + B * W2[r][c];
-      Vm[r][c] = I + B * W[r][c] + Cc * W2[r][c];
-    }
-  double dt[3];
-  for (int r = 0; r < 3; ++r) dt[r] = Vm[r][0] * xi[0] + Vm[r][1] * xi[1] + Vm[r][2] * xi[2];
-  Pose q;
-  for (int r = 0; r < 3; ++r) {
-    for (int c = 0; c < 3; ++c)
-      q.R[r][c] = dR[r][0] * p.R[0][c] + dR[r][1] * p.R[1][c] + dR[r][2] * p.R[2][c];
-    q.t[r] = dR[r][0] * p.t[0] + dR[r][1] * p.t[1] + dR[r][2] * p.t[2] + dt[r];
-  }
-  return q;
-}
-
-void pose_rows(const Pose &p, float *out12) {
-  for (int r = 0; r < 3; ++r) {
-    for (int c = 0; c < 3; ++c) out12[4 * r + c] = (float)p.R[r][c];
-    out12[4 * r + 3] = (float)p.t[r];
-  }
-}
-
-// Solves (H + damp * diag(H)) x = -g for the 6x6 system given by the 29
-// terms (upper triangle row by row, then g).  Returns false if singular.
-bool solve_step(const double terms[29], double damp, double x[6]) {
-  double H[6][6], g[6];
-  int k = 0;
-  for (int a = 0; a < 6; ++a)
-    for (int b = a; b < 6; ++b) H[a][b] = H[b][a] = terms[k++];
-  for (int a = 0; a < 6; ++a) g[a] = terms[21 + a];
-  for (int a = 0; a < 6; ++a) H[a][a] *= 1.0 + damp;
-  double L[6][6] = {};
-  for (int i = 0; i < 6; ++i) {
-    for (int j = 0; j <= i; ++j) {
-      double s = H[i][j];
-      for (int m = 0; m < j; ++m) s -= L[i][m] * L[j][m];
-      if (i == j) {
-        if (!(s > 0.0)) return false;
-        L[i][i] = std::sqrt(s);
-      } else {
-        L[i][j] = s / L[j][j];
-      }
-    }
-  }
-  double y[6];
-  for (int i = 0; i < 6; ++i) {
-    double s = -g[i];
-    for (int m = 0; m < i; ++m) s -= L[i][m] * y[m];
-    y[i] = s / L[i][i];
-  }
-  for (int i = 5; i >= 0; --i) {
-    double s = y[i];
-    for (int m = i + 1; m < 6; ++m) s -= L[m][i] * x[m];
-    x[i] = s / L[i][i];
-  }
-  return true;
-}
-
-struct RefineWork {
-  float *poses;     // 13 x 12
-  float *inv2eps;   // 6
-  float *partials;  // grid x kTerms
-  float *terms;     // kTerms
-  float *res;       // 13 x npx (FD method)
-  int grid;
-  int npx;
-};
-
-vh_status refine_work(vh_handle *h, int stride, bool fd, RefineWork *w) {
+int refine_grid(vh_handle *h, int stride, bool fd) {
   const CamParams C = vh::handle_cam(h);
   const int ws = (C.width + stride - 1) / stride, hs = (C.height + stride - 1) / stride;
-  w->npx = ws * hs;
-  w->grid = vh::handle_sm_count(h) * 4;
-  const size_t floats = 13 * 12 + 8 + (size_t)w->grid * kTerms + 32 + (fd ? 13 * (size_t)w->npx : 0);
-  void *p = nullptr;
-  vh_status s = vh::handle_workspace(h, floats * sizeof(float), &p);
-  if (s != VH_OK) return s;
-  float *f = static_cast<float *>(p);
-  w->poses = f;
-  w->inv2eps = f + 13 * 12;
-  w->partials = w->inv2eps + 8;
-  w->terms = w->partials + (size_t)w->grid * kTerms;
-  w->res = fd ? w->terms + 32 : nullptr;
+  const int threads = fd ? RefineShape<true>::kThreads : RefineShape<false>::kThreads;
+  int per_sm = 0;
+  const cudaError_t e =
+      fd ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_refine_step<true, true>, threads, 0)
+         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_refine_step<false, true>, threads, 0);
+  if (e != cudaSuccess || per_sm < 1) per_sm = 1;
+  const int need = (ws * hs + threads - 1) / threads;
+  const int full = vh::handle_sm_count(h) * per_sm;
+  return need < 1 ? 1 : (need < full ? need : full);
+}
+
+// Creates / grows the handle's refinement buffers.
+vh_status refine_ctx(vh_handle *h, int grid, int iterations, RefineCtx **out) {
+  RefineCtx *&c = vh::handle_refine(h);
+  if (!c) {
+    c = new RefineCtx();
+    c->device = vh::handle_device(h);
+    bool ok = cudaMalloc(&c->d_state, sizeof(RefineState)) == cudaSuccess &&
+              cudaMallocHost(&c->h_state, sizeof(RefineState)) == cudaSuccess;
+    for (auto &e : c->ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+    if (!ok) {
+      refine_ctx_free(c);
+      c = nullptr;
+      return vh::handle_fail(h, VH_ERR_CUDA, "refinement state allocation failed");
+    }
+  }
+  if (grid > c->partial_cap || iterations > c->hist_cap) {
+    if (cudaStreamSynchronize(vh::handle_stream(h)) != cudaSuccess)
+      return vh::handle_fail(h, VH_ERR_CUDA, "stream failed");
+    if (c->graph) {
+      cudaGraphExecDestroy(c->graph);  // holds the old buffer addresses
+      c->graph = nullptr;
+    }
+  }
+  if (grid > c->partial_cap) {
+    cudaFree(c->d_partials);
+    c->d_partials = nullptr;
+    c->partial_cap = 0;
+    if (cudaMalloc(&c->d_partials, sizeof(float) * kTerms * (size_t)grid) != cudaSuccess)
+      return vh::handle_fail(h, VH_ERR_CUDA, "refinement partials allocation failed");
+    c->partial_cap = grid;
+  }
+  if (iterations > c->hist_cap) {
+    const int cap = iterations < 64 ? 64 : iterations;
+    cudaFree(c->d_hist);
+    if (c->h_hist) cudaFreeHost(c->h_hist);
+    c->d_hist = nullptr;
+    c->h_hist = nullptr;
+    c->hist_cap = 0;
+    if (cudaMalloc(&c->d_hist, sizeof(float2) * cap) != cudaSuccess ||
+        cudaMallocHost(&c->h_hist, sizeof(float2) * cap) != cudaSuccess)
+      return vh::handle_fail(h, VH_ERR_CUDA, "refinement history allocation failed");
+    c->hist_cap = cap;
+  }
+  *out = c;
   return VH_OK;
 }
 
-const double kFdStep[6] = {1e-4, 1e-4, 1e-4, 1e-4, 1e-4, 1e-4};
+// Initial state: FP64 pose from the caller's c2w, its FP32 rows (and FD steps).
+void init_state(RefineState *S, const float *c2w, bool fd) {
+  std::memset(S, 0, sizeof(*S));
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 4; ++c) S->pose[4 * r + c] = c2w[4 * r + c];
+  for (int k = 0; k < 6; ++k) {
+    S->fd_step[k] = (float)kFdStep;
+    S->inv2eps[k] = (float)(0.5 / kFdStep);
+  }
+  for (int c = 0; c < 12; ++c) S->rows[c] = (float)S->pose[c];
+  if (fd)
+    for (int k = 0; k < 6; ++k)
+      for (int sgn = 0; sgn < 2; ++sgn) {
+        double xi[6] = {0, 0, 0, 0, 0, 0}, Q[12];
+        xi[k] = sgn == 0 ? kFdStep : -kFdStep;
+        se3_left_exp(xi, S->pose, Q);
+        for (int c = 0; c < 12; ++c) S->rows[12 * (1 + 2 * k + sgn) + c] = (float)Q[c];
+      }
+}
 
-// One linearisation at `pose`: normal-equation terms in double.
-vh_status linearise(vh_handle *h, const void *depth, int fmt, const Pose &pose, int stride,
-                    int method, const RefineWork &w, double out[29]) {
+// Enqueues `n` step launches of one method.
+template <bool kSolve>
+void enqueue_steps(vh_handle *h, RefineCtx *c, const void *depth, int fmt, int stride, bool fd,
+                   int grid, int n, cudaStream_t st) {
   const VolumeView V = vh::handle_view(h);
   CamParams C = vh::handle_cam(h);
   C.mc_min_weight = C.mc_min_weight < 1.0f ? 1.0f : C.mc_min_weight;  // observed corners only
-  const cudaStream_t st = vh::handle_stream(h);
   const float inv_voxel = 1.0f / C.voxel;
-  float host[13 * 12];
-  if (method == VH_REFINE_FD) {
-    pose_rows(pose, host);
-    for (int k = 0; k < 6; ++k)
-      for (int sgn = 0; sgn < 2; ++sgn) {
-        double xi[6] = {0, 0, 0, 0, 0, 0};
-        xi[k] = sgn == 0 ? kFdStep[k] : -kFdStep[k];
-        pose_rows(left_exp(xi, pose), host + 12 * (1 + 2 * k + sgn));
-      }
-    float ie[8];
-    for (int k = 0; k < 6; ++k) ie[k] = (float)(0.5 / kFdStep[k]);
-    if (cudaMemcpyAsync(w.poses, host, sizeof(host), cudaMemcpyHostToDevice, st) != cudaSuccess ||
-        cudaMemcpyAsync(w.inv2eps, ie, 6 * sizeof(float), cudaMemcpyHostToDevice, st) != cudaSuccess)
-      return vh::handle_fail(h, VH_ERR_CUDA, "pose upload failed");
-    const int gx = (w.npx + 255) / 256 < w.grid ? (w.npx + 255) / 256 : w.grid;
-    k_pose_residuals<<<dim3(gx, 13), 256, 0, st>>>(V, C, depth, fmt, w.poses, 13, stride,
-                                                     inv_voxel, w.res);
-    k_fd_terms<<<w.grid, 256, 0, st>>>(w.res, w.npx, w.inv2eps, w.partials);
-  } else {
-    pose_rows(pose, host);
-    if (cudaMemcpyAsync(w.poses, host, 12 * sizeof(float), cudaMemcpyHostToDevice, st) !=
-        cudaSuccess)
-      return vh::handle_fail(h, VH_ERR_CUDA, "pose upload failed");
-    k_pose_terms<<<w.grid, 256, 0, st>>>(V, C, depth, fmt, w.poses, stride, inv_voxel, w.partials);
+  for (int i = 0; i < n; ++i) {
+    if (fd)
+      k_refine_step<true, kSolve><<<grid, RefineShape<true>::kThreads, 0, st>>>(
+          V, C, depth, fmt, stride, inv_voxel, c->d_state, c->d_partials, c->d_hist, c->hist_cap);
+    else
+      k_refine_step<false, kSolve><<<grid, RefineShape<false>::kThreads, 0, st>>>(
+          V, C, depth, fmt, stride, inv_voxel, c->d_state, c->d_partials, c->d_hist, c->hist_cap);
   }
-  k_sum_partials<<<1, 32, 0, st>>>(w.partials, w.grid, w.terms);
-  float t[kTerms];
-  if (cudaGetLastError() != cudaSuccess ||
-      cudaMemcpyAsync(t, w.terms, sizeof(t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-      cudaStreamSynchronize(st) != cudaSuccess)
-    return vh::handle_fail(h, VH_ERR_CUDA, "normal equations failed");
-  for (int k = 0; k < kTerms; ++k) out[k] = t[k];
-  return VH_OK;
 }
 
 }  // namespace
@@ -562,61 +798,102 @@ extern "C" vh_status vh_pose_normal_equations(vh_handle *h, const void *depth, i
     return VH_ERR_INVALID_ARG;
   for (int i = 0; i < 16; ++i)
     if (!std::isfinite(c2w[i])) return VH_ERR_NOT_FINITE;
+  const bool fd = method == VH_REFINE_FD;
+  const cudaStream_t st = vh::handle_stream(h);
   const void *d = nullptr;
   vh_status s = vh::handle_stage_depth(h, depth, depth_fmt, mem, &d);
   if (s != VH_OK) return s;
-  RefineWork w;
-  if ((s = refine_work(h, stride, method == VH_REFINE_FD, &w)) != VH_OK) return s;
-  return linearise(h, d, depth_fmt, pose_from(c2w), stride, method, w, terms);
+  const int grid = refine_grid(h, stride, fd);
+  RefineCtx *c = nullptr;
+  if ((s = refine_ctx(h, grid, 1, &c)) != VH_OK) return s;
+  init_state(c->h_state, c2w, fd);
+  if (cudaMemcpyAsync(c->d_state, c->h_state, sizeof(RefineState), cudaMemcpyHostToDevice, st) !=
+      cudaSuccess)
+    return vh::handle_fail(h, VH_ERR_CUDA, "pose upload failed");
+  enqueue_steps<false>(h, c, d, depth_fmt, stride, fd, grid, 1, st);
+  if (cudaGetLastError() != cudaSuccess ||
+      cudaMemcpyAsync(c->h_state, c->d_state, sizeof(RefineState), cudaMemcpyDeviceToHost, st) !=
+          cudaSuccess)
+    return vh::handle_fail(h, VH_ERR_CUDA, "normal equations failed");
+  s = vh::handle_sync(h);
+  for (int k = 0; k < kTerms; ++k) terms[k] = c->h_state->terms[k];
+  return s;
 }
 
 extern "C" vh_status vh_pose_refine(vh_handle *h, const void *depth, int32_t depth_fmt, int32_t mem,
                                     const float *c2w_init, int32_t iterations, int32_t stride,
                                     int32_t method, float *c2w_out, vh_refine_stats *stats) {
-  if (!h || !c2w_init || !c2w_out || iterations < 0 || stride < 1 ||
+  if (!h || !c2w_init || !c2w_out || iterations < 0 || iterations > (1 << 16) || stride < 1 ||
       (method != VH_REFINE_ADJOINT && method != VH_REFINE_FD))
     return VH_ERR_INVALID_ARG;
   for (int i = 0; i < 16; ++i)
     if (!std::isfinite(c2w_init[i])) return VH_ERR_NOT_FINITE;
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
+  const bool fd = method == VH_REFINE_FD;
   const cudaStream_t st = vh::handle_stream(h);
-  cudaEventRecord(e0, st);
+  const int grid = refine_grid(h, stride, fd);
+  RefineCtx *c = nullptr;
+  vh_status s = refine_ctx(h, grid, iterations, &c);
+  if (s != VH_OK) return s;
+  cudaEventRecord(c->ev[0], st);
   const void *d = nullptr;
-  vh_status s = vh::handle_stage_depth(h, depth, depth_fmt, mem, &d);
-  RefineWork w;
-  if (s == VH_OK) s = refine_work(h, stride, method == VH_REFINE_FD, &w);
-  Pose pose = pose_from(c2w_init);
-  double terms[29] = {0};
-  double rmse0 = 0.0, rmse = 0.0;
-  int valid = 0, done = 0;
-  for (int it = 0; it < iterations && s == VH_OK; ++it) {
-    s = linearise(h, d, depth_fmt, pose, stride, method, w, terms);
-    if (s != VH_OK) break;
-    valid = (int)terms[28];
-    rmse = valid ? std::sqrt(terms[27] / valid) : 0.0;
-    if (it == 0) rmse0 = rmse;
-    double xi[6];
-    if (valid < 6 || !solve_step(terms, 1e-6, xi)) break;
-    pose = left_exp(xi, pose);
-    ++done;
+  if ((s = vh::handle_stage_depth(h, depth, depth_fmt, mem, &d)) != VH_OK) return s;
+  init_state(c->h_state, c2w_init, fd);
+  if (cudaMemcpyAsync(c->d_state, c->h_state, sizeof(RefineState), cudaMemcpyHostToDevice, st) !=
+      cudaSuccess)
+    return vh::handle_fail(h, VH_ERR_CUDA, "pose upload failed");
+  const long long key[7] = {method, stride, iterations, depth_fmt, grid, (long long)(uintptr_t)st,
+                            (long long)(uintptr_t)c->d_partials};
+  if (c->graph && std::memcmp(key, c->key, sizeof(key)) != 0) {
+    cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
   }
-  cudaEventRecord(e1, st);
-  cudaEventSynchronize(e1);
-  float ms = 0.0f;
-  cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  pose_to(pose, c2w_out);
+  if (!c->graph && iterations > 0) {
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+      return vh::handle_fail(h, VH_ERR_CUDA, "refinement capture failed");
+    enqueue_steps<true>(h, c, d, depth_fmt, stride, fd, grid, iterations, st);
+    const cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (e != cudaSuccess || cudaGraphInstantiate(&c->graph, g, 0) != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      c->graph = nullptr;
+      return vh::handle_fail(h, VH_ERR_CUDA, "refinement graph failed");
+    }
+    cudaGraphDestroy(g);
+    std::memcpy(c->key, key, sizeof(key));
+  }
+  cudaEventRecord(c->ev[1], st);
+  if (iterations > 0 && cudaGraphLaunch(c->graph, st) != cudaSuccess)
+    return vh::handle_fail(h, VH_ERR_CUDA, "refinement launch failed");
+  cudaEventRecord(c->ev[2], st);
+  if (cudaMemcpyAsync(c->h_state, c->d_state, sizeof(RefineState), cudaMemcpyDeviceToHost, st) !=
+          cudaSuccess ||
+      (iterations > 0 && cudaMemcpyAsync(c->h_hist, c->d_hist, sizeof(float2) * iterations,
+                                         cudaMemcpyDeviceToHost, st) != cudaSuccess))
+    return vh::handle_fail(h, VH_ERR_CUDA, "refinement download failed");
+  cudaEventRecord(c->ev[3], st);
+  if ((s = vh::handle_sync(h)) != VH_OK) return s;
+  const RefineState &S = *c->h_state;
+  for (int r = 0; r < 3; ++r)
+    for (int k = 0; k < 4; ++k) c2w_out[4 * r + k] = (float)S.pose[4 * r + k];
+  c2w_out[12] = c2w_out[13] = c2w_out[14] = 0.0f;
+  c2w_out[15] = 1.0f;
   if (stats) {
-    stats->iterations = done;
-    stats->valid_pixels = valid;
-    stats->initial_rmse = (float)rmse0;
-    stats->final_rmse = (float)rmse;
+    const int lin = S.iter < iterations ? S.iter : iterations;  // linearisations recorded
+    auto rmse = [&](int i) {
+      const float2 v = c->h_hist[i];
+      return v.y > 0.0f ? std::sqrt(v.x / v.y) : 0.0f;
+    };
+    stats->iterations = S.updates;
+    stats->valid_pixels = lin > 0 ? (int32_t)c->h_hist[lin - 1].y : 0;
+    stats->initial_rmse = lin > 0 ? rmse(0) : 0.0f;
+    stats->final_rmse = lin > 0 ? rmse(lin - 1) : 0.0f;
+    float ms = 0.0f, ms_steps = 0.0f;
+    cudaEventElapsedTime(&ms, c->ev[0], c->ev[3]);
+    cudaEventElapsedTime(&ms_steps, c->ev[1], c->ev[2]);
     stats->ms = ms;
+    stats->ms_steps = ms_steps;
   }
-  return s;
+  return VH_OK;
 }
 
 extern "C" vh_status vh_integrate_vjp(vh_handle *h, const void *depth, int32_t depth_fmt,
@@ -653,7 +930,7 @@ extern "C" vh_status vh_integrate_vjp(vh_handle *h, const void *depth, int32_t d
     dg = tmp;
   }
   float rows[12];
-  pose_rows(pose_from(c2w), rows);
+  std::memcpy(rows, c2w, sizeof(rows));  // rows 0-2 of the row-major 4x4
   if (cudaMemcpyAsync(dpose, rows, sizeof(rows), cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemsetAsync(dgd, 0, sizeof(float) * npx, st) != cudaSuccess)
     return vh::handle_fail(h, VH_ERR_CUDA, "vjp set-up failed");

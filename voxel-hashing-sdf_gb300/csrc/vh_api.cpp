@@ -57,8 +57,9 @@ struct vh_handle {
   cudaEvent_t ev[kNumEvents] = {};
   bool ev_pending = false;
   bool ev_has_mc = false;
-  void *d_work = nullptr;  // workspace of the gradient / refinement calls
+  void *d_work = nullptr;  // workspace of the gradient calls
   size_t work_bytes = 0;
+  RefineCtx *refine = nullptr;  // device state of pose refinement (vh_adjoint.cu)
   int64_t frames = 0;
   bool nb_valid = false;  // frame_nb matches the current block list
   std::string last_error;
@@ -269,6 +270,8 @@ vh_status stage_inputs(vh_handle *h, const void *depth, int32_t fmt, const uint8
 
 void free_all(vh_handle *h) {
   drop_graphs(h);
+  refine_ctx_free(h->refine);
+  h->refine = nullptr;
   cudaFree(h->V.slots);
   cudaFree(h->V.pool);
   cudaFree(h->V.block_keys);
@@ -371,6 +374,8 @@ vh_status handle_stage_depth(vh_handle *h, const void *depth, int fmt, int mem, 
   *dev = h->d_depth;
   return VH_OK;
 }
+RefineCtx *&handle_refine(vh_handle *h) { return h->refine; }
+
 vh_status handle_workspace(vh_handle *h, size_t bytes, void **ptr) {
   if (bytes > h->work_bytes) {
     VH_CUDA(h, cudaStreamSynchronize(h->stream));

@@ -19,4 +19,9 @@ int handle_sm_count(const vh_handle *h);
 vh_status handle_stage_depth(vh_handle *h, const void *depth, int fmt, int mem, const void **dev);
 // Device workspace owned by the handle, grown on demand, freed with it.
 vh_status handle_workspace(vh_handle *h, size_t bytes, void **ptr);
+// Pose-refinement state (buffers, cached graph) created on first use by
+// vh_adjoint.cu and released with the handle.
+struct RefineCtx;
+RefineCtx *&handle_refine(vh_handle *h);
+void refine_ctx_free(RefineCtx *ctx);
 }  // namespace vh

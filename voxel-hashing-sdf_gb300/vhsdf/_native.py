@@ -70,7 +70,8 @@ class VhTuning(C.Structure):
 
 class VhRefineStats(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("valid_pixels", C.c_int32),
-                ("initial_rmse", C.c_float), ("final_rmse", C.c_float), ("ms", C.c_float)]
+                ("initial_rmse", C.c_float), ("final_rmse", C.c_float), ("ms", C.c_float),
+                ("ms_steps", C.c_float)]
 
 
 class VhMeshView(C.Structure):
