@@ -183,7 +183,7 @@ def adjoint_leg(num_frames, local, iterations=20):
     s = synth.Scene(kind=1, seed=0, num_frames=100)
     vol = Volume(width=640, height=480, fx=s.fx, fy=s.fy, cx=s.cx, cy=s.cy, min_depth=0.1,
                  max_depth=4.5, voxel_size=0.005, trunc=0.1, table_log2=22,
-                 pool_blocks=1_200_000, max_frame_blocks=400_000, max_triangles=1 << 22,
+                 pool_blocks=400_000, max_frame_blocks=200_000, max_triangles=1 << 20,
                  device=local)
     frames = [s.render(f) for f in range(100)]
     for d, c, p in frames:
@@ -382,7 +382,8 @@ def run_engine(args):
     in_ach = sum(in_alg) / (sum(in_ms) / 1000.0) / 1e9
     peak, peak_src = peak_hbm()
     cpu = cpu_leg(frames, scene, seconds=args.cpu_seconds)
-    adjoint = adjoint_leg(args.adjoint_frames, local) if args.adjoint_frames > 0 else None
+    adjoint = (adjoint_leg(args.adjoint_frames, local, args.adjoint_iterations)
+               if args.adjoint_frames > 0 and rank == 0 else None)
     res = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
@@ -425,6 +426,10 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--adjoint-frames", type=int, default=100,
                     help="poses refined in the pose-refinement leg (0 = skip)")
+    ap.add_argument("--adjoint-iterations", type=int, default=20,
+                    help="Gauss-Newton steps per pose in the pose-refinement leg")
+    ap.add_argument("--only-pose-refinement", action="store_true",
+                    help="run only the pose-refinement leg and print its JSON (profiling)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="use the default launch configuration (for profiling runs)")
     ap.add_argument("--pool-blocks", type=int, default=0,
@@ -433,6 +438,11 @@ def main():
     args.warmup = max(args.warmup, 0)
     if args.impl == "reference":
         run_reference(args)
+    elif args.only_pose_refinement:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps({"pose_refinement": adjoint_leg(max(args.adjoint_frames, 1), 0,
+                                                         args.adjoint_iterations)}), flush=True)
     else:
         run_engine(args)
 
