@@ -228,6 +228,110 @@ def adjoint_leg(num_frames, local, iterations=20):
             "speedup": out["adjoint"]["pose_steps_per_s"] / out["fd"]["pose_steps_per_s"]}
 
 
+BATCH_RES = [(320, 240), (640, 480), (960, 720), (1280, 960)]
+
+
+def batch_specs(num_scenes, small=False):
+    """The batched-scenes workload: scene s (seed 100 + s) is a seeded room
+    of extent U[1, 8] m with voxel U[4, 20] mm, truncation max(4 voxels,
+    30 mm) (the depth noise reaches 1.5e-3 z^2 = 24 mm at 4 m), U[10, 200]
+    frames and one of four depth resolutions; hash table and pool are sized
+    from the room's surface (table 2^16 .. 2^22).  small: scenes of seeds
+    1000 + s at 160x120 with voxels U[10, 20] mm (a launch-bound batch)."""
+    from vhsdf import synth
+    out = []
+    for s in range(num_scenes):
+        seed = (1000 if small else 100) + s
+        rng = np.random.default_rng(seed)
+        vox = float(rng.uniform(0.010, 0.020) if small else rng.uniform(0.004, 0.020))
+        nf = int(rng.integers(10, 201))
+        w, h = (160, 120) if small else BATCH_RES[int(rng.integers(0, 4))]
+        sc = synth.Scene(kind=3, seed=seed, num_frames=nf, width=w, height=h)
+        lo, hi = sc.bounds()
+        ext = hi - lo
+        area = 2 * ext[0] * ext[1] + 2 * (ext[0] + ext[1]) * ext[2]
+        blocks = int(4 * area / (8 * vox) ** 2) + 4096
+        tlog = int(min(22, max(16, np.ceil(np.log2(2 * blocks)))))
+        prm = dict(width=w, height=h, fx=sc.fx, fy=sc.fy, cx=sc.cx, cy=sc.cy, min_depth=0.1,
+                   max_depth=8.0, voxel_size=vox, trunc=max(4 * vox, 0.03), table_log2=tlog,
+                   pool_blocks=min(blocks, (1 << tlog) - (1 << (tlog - 3))),
+                   max_frame_blocks=min(blocks, 400_000), max_triangles=16 * w * h, flags=0)
+        out.append((sc, nf, prm))
+    return out
+
+
+def batched_leg(num_scenes, steps, local, small=False):
+    """Many uneven scenes in one persistent launch per stage (vh_batch) vs the
+    same frames through one handle per scene (one per-frame graph each).
+    Frames are resident on the device; both runs are timed by the host clock
+    between device synchronisations, allocate -> integrate per frame (a
+    single noisy frame at 4 mm voxels flips sign across the whole band, so
+    per-frame meshes grow beyond 16 triangles per pixel: fusion is timed,
+    extraction is not)."""
+    import torch
+    from vhsdf import Batch, Volume
+    specs = batch_specs(num_scenes, small)
+    frames = []
+    for sc, nf, prm in specs:
+        fr = []
+        for f in range(min(nf, steps)):
+            d, c, p = sc.render(f)
+            fr.append((torch.from_numpy(d.astype(np.int16)).cuda(local),
+                       torch.from_numpy(c).cuda(local), p))
+        frames.append(fr)
+    total = sum(len(fr) for fr in frames)
+    pixels = sum(prm["width"] * prm["height"] * len(fr) for (_, _, prm), fr in zip(specs, frames))
+    torch.cuda.synchronize()
+    batch = Batch([dict(prm, device=local) for _, _, prm in specs])
+    # warm-up (graph capture) on the first frames, then start from empty volumes
+    batch.process([fr[0] for fr in frames], with_mesh=False, depth_format="u16")
+    batch.sync()
+    for i in range(num_scenes):
+        batch.scene(i).reset()
+    batch.sync()
+    t0 = time.perf_counter()
+    for k in range(steps):
+        batch.process([fr[k] if k < len(fr) else None for fr in frames], with_mesh=False,
+                      depth_format="u16")
+    status, bstats = batch.sync()
+    t_batch = time.perf_counter() - t0
+    batch.close()
+    vols = [Volume(**dict(prm, device=local)) for _, _, prm in specs]
+    for v, fr in zip(vols, frames):
+        v.integrate(*fr[0], depth_format="u16")
+    for v in vols:
+        v.sync()
+        v.reset()
+    for v in vols:
+        v.sync()
+    t0 = time.perf_counter()
+    for k in range(steps):
+        for v, fr in zip(vols, frames):
+            if k < len(fr):
+                v.integrate(*fr[k], depth_format="u16")
+    for v in vols:
+        v.sync()
+    t_seq = time.perf_counter() - t0
+    sstats = [v.stats() for v in vols]
+    same = all(b["blocks_allocated"] == q["blocks_allocated"]
+               and b["voxels_updated"] == q["voxels_updated"] for b, q in zip(bstats, sstats))
+    for v in vols:
+        v.close()
+    first = 1000 if small else 100
+    shape = ("160x120, voxel U[10, 20] mm" if small else
+             "320x240 .. 1280x960, voxel U[4, 20] mm")
+    return {"workload": f"{num_scenes} seeded rooms (seeds {first}..{first + num_scenes - 1}): "
+                        f"extent U[1, 8] m, {shape}, truncation max(4 voxels, 30 mm), "
+                        "U[10, 200] frames, tables 2^16 .. 2^22; first "
+                        f"{steps} frames of each, allocate -> integrate per frame",
+            "frames": total, "megapixels": pixels / 1e6,
+            "batched_frames_per_s": total / t_batch, "per_scene_graphs_frames_per_s": total / t_seq,
+            "speedup": t_seq / t_batch, "status_ok": all(x == 0 for x in status),
+            "counts_equal_per_scene": same,
+            "voxel_updates_per_s": sum(b["voxels_updated"] for b in bstats) / t_batch,
+            "launches_per_step": {"batched": 5, "per_scene_graphs": 5 * num_scenes}}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -384,6 +488,10 @@ def run_engine(args):
     cpu = cpu_leg(frames, scene, seconds=args.cpu_seconds)
     adjoint = (adjoint_leg(args.adjoint_frames, local, args.adjoint_iterations)
                if args.adjoint_frames > 0 and rank == 0 else None)
+    batched = (batched_leg(args.batch_scenes, args.batch_steps, local)
+               if args.batch_scenes > 0 and rank == 0 else None)
+    batched_small = (batched_leg(4 * args.batch_scenes, args.batch_steps, local, small=True)
+                     if args.batch_scenes > 0 and rank == 0 else None)
     res = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
@@ -411,6 +519,8 @@ def run_engine(args):
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
         "pose_refinement": adjoint,
+        "batched_scenes": batched,
+        "batched_small_scenes": batched_small,
     }
     print(json.dumps(res), flush=True)
     if world > 1:
@@ -428,6 +538,12 @@ def main():
                     help="poses refined in the pose-refinement leg (0 = skip)")
     ap.add_argument("--adjoint-iterations", type=int, default=20,
                     help="Gauss-Newton steps per pose in the pose-refinement leg")
+    ap.add_argument("--batch-scenes", type=int, default=64,
+                    help="scenes in the batched-scenes leg (0 = skip)")
+    ap.add_argument("--batch-steps", type=int, default=12,
+                    help="frames per scene in the batched-scenes leg")
+    ap.add_argument("--only-batched", action="store_true",
+                    help="run only the batched-scenes leg and print its JSON (profiling)")
     ap.add_argument("--only-pose-refinement", action="store_true",
                     help="run only the pose-refinement leg and print its JSON (profiling)")
     ap.add_argument("--no-autotune", action="store_true",
@@ -438,6 +554,13 @@ def main():
     args.warmup = max(args.warmup, 0)
     if args.impl == "reference":
         run_reference(args)
+    elif args.only_batched:
+        import torch
+        torch.cuda.set_device(0)
+        n = max(args.batch_scenes, 1)
+        print(json.dumps({"batched_scenes": batched_leg(n, args.batch_steps, 0),
+                          "batched_small_scenes": batched_leg(4 * n, args.batch_steps, 0,
+                                                              small=True)}), flush=True)
     elif args.only_pose_refinement:
         import torch
         torch.cuda.set_device(0)

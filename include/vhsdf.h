@@ -267,6 +267,43 @@ vh_status vh_set_tuning(vh_handle *h, const vh_tuning *t);
 vh_status vh_autotune(vh_handle *h, const void *depth, int32_t depth_fmt, const uint8_t *rgb,
                       const float *c2w, int32_t mem, vh_tuning *chosen);
 
+/* ---- batches of independent scenes (no reference counterpart: the
+ * reference runs one scene per process) ------------------------------------ */
+
+typedef struct vh_batch vh_batch;
+
+#define VH_BATCH_MAX_SCENES 1024
+
+/* n independent scenes (1..VH_BATCH_MAX_SCENES) on params[0].device; scene i
+ * has params[i]: image size, intrinsics, voxel size, truncation, table and
+ * pool sizes may all differ.  Every scene is a full handle
+ * (vh_batch_scene) that shares the batch's stream. */
+vh_status vh_batch_create(const vh_params *params, int32_t n, vh_batch **out);
+vh_status vh_batch_destroy(vh_batch *b);
+int32_t vh_batch_size(const vh_batch *b);
+/* Scene i as an ordinary handle (extract, export, save, stats, hash calls),
+ * owned by the batch; NULL if i is out of range. */
+vh_handle *vh_batch_scene(vh_batch *b, int32_t i);
+/* One frame for every scene i with depth[i] != NULL (the other scenes keep
+ * their state): allocation, integration and, with with_mesh, the
+ * marching cubes of the frame's blocks.  Each stage is ONE launch over the
+ * work of all those scenes (flattened scene x item index), and the stages of
+ * a step replay as one CUDA graph.  depth[i] (format depth_fmt, shared) and
+ * rgb[i] are in `mem`: host frames are copied into the scene's staging
+ * buffers, device frames are read in place by the step (leave them unchanged
+ * until it completes); c2w holds n row-major 4x4 poses (host; entries of
+ * scenes without a frame are ignored).  Asynchronous unless params[0].flags
+ * has VH_FLAG_SYNC, which waits and returns the first scene error (without
+ * clearing it); per-scene errors are reported by vh_batch_sync. */
+vh_status vh_batch_process(vh_batch *b, const void *const *depth, int32_t depth_fmt,
+                           const uint8_t *const *rgb, const float *c2w, int32_t mem,
+                           int32_t with_mesh);
+/* Waits for the batch; status[i] (may be NULL) receives scene i's sticky
+ * device errors as a status (then cleared); stats[i] (may be NULL) its
+ * counters after the last step.  One device gather for all scenes.  Returns
+ * the first non-OK scene status. */
+vh_status vh_batch_sync(vh_batch *b, vh_status *status, vh_stats *stats);
+
 /* ---- gradients and pose refinement (no reference counterpart: the
  * reference has no derivatives) ------------------------------------------- */
 

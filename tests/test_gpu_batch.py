@@ -1,0 +1,115 @@
+"""Batched scenes on the GPU: a batch of uneven scenes stepped together must
+leave every scene exactly as the same frames do through its own handle
+(block set, voxels and the per-frame meshes bit for bit), and one scene is
+checked against the FP32 oracle directly."""
+import numpy as np
+import pytest
+
+from helpers import assert_same_blocks, oracle_for, sort_rows, tri_rows
+from vhsdf import Batch, VhError, Volume, synth
+
+pytestmark = pytest.mark.gpu
+
+# (kind, seed, width, height, voxel, table_log2, frames): uneven sizes,
+# pixel counts that are not multiples of 32, scenes that stop early
+SCENES = [
+    (1, 0, 160, 120, 0.02, 16, 6),
+    (3, 101, 200, 150, 0.015, 17, 4),
+    (3, 102, 96, 72, 0.03, 14, 6),
+    (2, 2, 320, 240, 0.01, 18, 3),
+    (3, 103, 130, 98, 0.025, 15, 5),
+]
+
+
+def scene_params(kind, seed, w, h, voxel, tlog, frames):
+    sc = synth.Scene(kind=kind, seed=seed, num_frames=frames, width=w, height=h)
+    prm = dict(width=w, height=h, fx=sc.fx, fy=sc.fy, cx=sc.cx, cy=sc.cy, min_depth=0.1,
+               max_depth=4.5, voxel_size=voxel, trunc=4 * voxel, table_log2=tlog,
+               pool_blocks=1 << (tlog - 1), max_frame_blocks=1 << (tlog - 1),
+               max_triangles=1 << 20)
+    return sc, prm
+
+
+@pytest.fixture(scope="module")
+def runs(gpu):
+    scenes = [scene_params(*s) for s in SCENES]
+    frames = [[sc.render(f) for f in range(s[-1])] for (sc, _), s in zip(scenes, SCENES)]
+    steps = max(s[-1] for s in SCENES)
+    batch = Batch([prm for _, prm in scenes])
+    batch_meshes = [[] for _ in SCENES]
+    for k in range(steps):
+        step = [fr[k] if k < len(fr) else None for fr in frames]
+        batch.process(step, with_mesh=True)
+        status, stats = batch.sync()
+        assert all(s == 0 for s in status), status
+        for i, fr in enumerate(step):
+            if fr is not None:
+                batch_meshes[i].append(batch.scene(i).mesh())
+                assert stats[i]["frames"] == k + 1
+    singles, single_meshes = [], []
+    for (sc, prm), fr in zip(scenes, frames):
+        vol = Volume(**prm)
+        ms = []
+        for d, c, p in fr:
+            vol.process_frame(d, c, p)
+            ms.append(vol.mesh())
+        singles.append(vol)
+        single_meshes.append(ms)
+    return scenes, frames, batch, batch_meshes, singles, single_meshes
+
+
+def test_blocks_equal_single_scene_runs(runs):
+    scenes, frames, batch, _, singles, _ = runs
+    for i in range(len(SCENES)):
+        assert_same_blocks(batch.scene(i).export_blocks(), singles[i].export_blocks())
+
+
+def test_frame_meshes_equal_single_scene_runs(runs):
+    _, frames, _, batch_meshes, _, single_meshes = runs
+    for i in range(len(SCENES)):
+        assert len(batch_meshes[i]) == len(single_meshes[i]) == len(frames[i])
+        for (bx, bc), (sx, scol) in zip(batch_meshes[i], single_meshes[i]):
+            assert len(bx) == len(sx)
+            assert np.array_equal(sort_rows(tri_rows(bx, bc)), sort_rows(tri_rows(sx, scol)))
+
+
+def test_one_scene_against_fp32_oracle(runs):
+    scenes, frames, batch, _, _, _ = runs
+    i = 1
+    vol = batch.scene(i)
+    orc = oracle_for(vol, 32)
+    for d, c, p in frames[i]:
+        orc.integrate(d, c, p)
+    assert_same_blocks(vol.export_blocks(), orc.export())
+
+
+def test_scene_handles_stay_usable(runs):
+    """After batched steps a scene is an ordinary handle: full-volume
+    extraction and stats work and agree with the single-scene run."""
+    _, _, batch, _, singles, _ = runs
+    for i in (0, 3):
+        vol = batch.scene(i)
+        vol.extract("all")
+        singles[i].extract("all")
+        bx, bc = vol.mesh()
+        sx, scol = singles[i].mesh()
+        assert np.array_equal(sort_rows(tri_rows(bx, bc)), sort_rows(tri_rows(sx, scol)))
+        assert vol.stats()["blocks_allocated"] == singles[i].stats()["blocks_allocated"]
+
+
+def test_pool_overflow_is_reported_per_scene(gpu):
+    sc_a, prm_a = scene_params(1, 0, 160, 120, 0.02, 16, 2)
+    sc_b, prm_b = scene_params(3, 104, 160, 120, 0.02, 16, 2)
+    prm_b["pool_blocks"] = 64  # far too small
+    batch = Batch([prm_a, prm_b])
+    with pytest.raises(VhError) as err:  # synchronous handles: the step reports the first error
+        batch.process([sc_a.render(0), sc_b.render(0)], with_mesh=False)
+    assert err.value.status == 4  # VH_ERR_POOL_FULL
+    status, stats = batch.sync()
+    assert status[0] == 0
+    assert status[1] != 0 and stats[1]["device_error"] != 0
+    # the error was cleared; the healthy scene keeps going
+    batch.process([sc_a.render(1), None])
+    status, _ = batch.sync()
+    assert status == [0, 0]
+    batch.close()

@@ -33,6 +33,7 @@ ENGINE_SOURCES = [
     ("vh_mesh.cpp", []),
     ("vh_noalloc.cu", []),
     ("vh_adjoint.cu", []),
+    ("vh_batch.cpp", []),
 ]
 ENGINE_HEADERS = ["vh_common.cuh", "vh_device.cuh", "vh_mc_tables.h", "vh_mesh.h", "vh_internal.h"]
 

@@ -376,6 +376,28 @@ vh_status handle_stage_depth(vh_handle *h, const void *depth, int fmt, int mem, 
 }
 RefineCtx *&handle_refine(vh_handle *h) { return h->refine; }
 
+FrameBuffers handle_frame_buffers(const vh_handle *h) {
+  return FrameBuffers{h->d_depth, h->d_rgb, h->d_pix, h->d_tris, h->tri_cap,
+                      h->integrate_per_sm, h->mc_per_sm, h->tuning.mc_variant};
+}
+
+const vh_params &handle_params(const vh_handle *h) { return h->p; }
+
+int64_t handle_frames(const vh_handle *h) { return h->frames; }
+
+void handle_note_frame(vh_handle *h) {
+  h->frames++;
+  h->nb_valid = true;
+  h->ev_pending = false;
+}
+
+vh_status handle_status_of_bits(vh_handle *h, uint32_t bits) {
+  if (!bits) return VH_OK;
+  std::string msg;
+  const vh_status st = status_of_bits(bits, msg);
+  return fail(h, st, msg);
+}
+
 vh_status handle_workspace(vh_handle *h, size_t bytes, void **ptr) {
   if (bytes > h->work_bytes) {
     VH_CUDA(h, cudaStreamSynchronize(h->stream));

@@ -1,0 +1,316 @@
+// vh_batch.cpp - many independent scenes stepped together (include/vhsdf.h,
+// vh_batch_*).
+//
+// Each scene is an ordinary handle (own hash table, pool, staging buffers).
+// A batched step runs the per-frame stages of every scene that has a frame
+// as one launch per stage: the kernels walk a flattened (scene, item) index
+// (pixels for allocation, listed blocks for integration and marching cubes)
+// and apply the single-scene bodies with that scene's volume and camera.
+// Per step the host fills one pinned block - the scene descriptors, the
+// poses and the active flags - and sends it with one copy; the stage
+// launches replay as one CUDA graph whose arguments never change.
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/vhsdf.h"
+#include "vh_common.cuh"
+#include "vh_internal.h"
+
+using namespace vh;
+
+namespace {
+constexpr int kRing = 4;  // per-step upload blocks in flight
+}
+
+struct vh_batch {
+  int n = 0;
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<vh_handle *> scenes;
+  // per-step upload block: SceneDesc[n] | float pose[16 n] | uint8 active[n]
+  size_t desc_bytes = 0, pose_bytes = 0, block_bytes = 0;
+  unsigned char *d_block = nullptr;
+  unsigned char *h_block = nullptr;  // pinned, kRing blocks
+  cudaEvent_t ring_ev[kRing] = {};
+  int ring_pos = 0;
+  uint32_t *d_px_start = nullptr;  // n + 1
+  uint32_t total_px = 0;
+  uint32_t *d_prefix = nullptr;  // n + 1
+  DevState *d_states = nullptr;  // n
+  DevState *h_states = nullptr;  // pinned, n
+  cudaGraphExec_t graphs[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  std::string last_error;
+
+  SceneDesc *desc() const { return reinterpret_cast<SceneDesc *>(d_block); }
+  const float *pose(int i) const {
+    return reinterpret_cast<const float *>(d_block + desc_bytes) + 16 * (size_t)i;
+  }
+  const uint8_t *active() const { return d_block + desc_bytes + pose_bytes; }
+};
+
+namespace {
+
+void free_batch(vh_batch *b) {
+  for (auto &row : b->graphs)
+    for (auto &g : row)
+      if (g) cudaGraphExecDestroy(g);
+  for (vh_handle *h : b->scenes)
+    if (h) vh_destroy(h);
+  cudaFree(b->d_block);
+  cudaFree(b->d_px_start);
+  cudaFree(b->d_prefix);
+  cudaFree(b->d_states);
+  if (b->h_block) cudaFreeHost(b->h_block);
+  if (b->h_states) cudaFreeHost(b->h_states);
+  for (auto &e : b->ring_ev)
+    if (e) cudaEventDestroy(e);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+// Launch shapes: the first scene's tuning, capped by the batched kernels'
+// own occupancy.
+int batch_grid(const vh_batch *b, int per_sm) { return b->sm_count * std::max(1, per_sm); }
+
+void enqueue_step(vh_batch *b, int fmt, bool with_mesh) {
+  const FrameBuffers f0 = handle_frame_buffers(b->scenes[0]);
+  const SceneDesc *d = b->desc();
+  const uint8_t *act = b->active();
+  cudaStream_t s = b->stream;
+  launch_batch_frame_begin(d, act, b->n, s);
+  launch_batch_allocate(d, act, b->d_px_start, b->total_px, b->n, fmt, s);
+  launch_batch_epoch_end(d, act, b->n, b->d_prefix, s);
+  launch_batch_resolve(d, b->d_prefix, b->n, b->sm_count * 2, s);
+  launch_batch_integrate(d, b->d_prefix, b->n,
+                         batch_grid(b, std::min(f0.integrate_per_sm, batch_integrate_ctas_per_sm())),
+                         s);
+  if (with_mesh) {
+    launch_batch_mc_begin(d, act, b->n, s);
+    launch_batch_mc(d, b->d_prefix, b->n,
+                    batch_grid(b, std::min(f0.mc_per_sm, batch_mc_ctas_per_sm(f0.mc_variant))),
+                    f0.mc_variant, s);
+  }
+}
+
+vh_status fail(vh_batch *b, vh_status s, const std::string &msg) {
+  b->last_error = msg;
+  return s;
+}
+
+vh_status check_batch(vh_batch *b, vh_status *status, vh_stats *stats, bool clear);
+
+}  // namespace
+
+extern "C" {
+
+vh_status vh_batch_create(const vh_params *params, int32_t n, vh_batch **out) {
+  if (!out) return VH_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (!params || n < 1 || n > VH_BATCH_MAX_SCENES) return VH_ERR_INVALID_ARG;
+  for (int i = 0; i < n; ++i) {
+    const vh_status s = vh_params_validate(params + i);
+    if (s != VH_OK) return s;
+    if (params[i].device != params[0].device) return VH_ERR_INVALID_ARG;
+  }
+  vh_batch *b = new vh_batch();
+  b->n = n;
+  b->device = params[0].device;
+  b->scenes.assign(n, nullptr);
+  for (int i = 0; i < n; ++i) {
+    const vh_status s = vh_create(params + i, &b->scenes[i]);
+    if (s != VH_OK) {
+      free_batch(b);
+      return s;
+    }
+  }
+  if (cudaSetDevice(b->device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, b->device) !=
+          cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    free_batch(b);
+    return VH_ERR_CUDA;
+  }
+  for (vh_handle *h : b->scenes) vh_set_stream(h, b->stream);
+  b->desc_bytes = sizeof(SceneDesc) * (size_t)n;
+  b->pose_bytes = 16 * sizeof(float) * (size_t)n;
+  b->block_bytes = (b->desc_bytes + b->pose_bytes + (size_t)n + 15) & ~(size_t)15;
+  std::vector<uint32_t> px(n + 1, 0);
+  for (int i = 0; i < n; ++i) {
+    const uint64_t npx = (uint64_t)params[i].width * (uint64_t)params[i].height;
+    // whole allocation CTAs per scene
+    px[i + 1] = px[i] + (uint32_t)((npx + kBatchPixelThreads - 1) / kBatchPixelThreads *
+                                   kBatchPixelThreads);
+  }
+  b->total_px = px[n];
+  bool ok = cudaMalloc(&b->d_block, b->block_bytes) == cudaSuccess &&
+            cudaMallocHost(&b->h_block, b->block_bytes * kRing) == cudaSuccess &&
+            cudaMalloc(&b->d_px_start, sizeof(uint32_t) * (n + 1)) == cudaSuccess &&
+            cudaMalloc(&b->d_prefix, sizeof(uint32_t) * (n + 1)) == cudaSuccess &&
+            cudaMalloc(&b->d_states, sizeof(DevState) * n) == cudaSuccess &&
+            cudaMallocHost(&b->h_states, sizeof(DevState) * n) == cudaSuccess;
+  for (auto &e : b->ring_ev)
+    ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+  ok = ok && cudaMemcpy(b->d_px_start, px.data(), sizeof(uint32_t) * (n + 1),
+                        cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemset(b->d_block, 0, b->block_bytes) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    free_batch(b);
+    return VH_ERR_CUDA;
+  }
+  for (auto &e : b->ring_ev) cudaEventRecord(e, b->stream);
+  *out = b;
+  return VH_OK;
+}
+
+vh_status vh_batch_destroy(vh_batch *b) {
+  if (!b) return VH_ERR_INVALID_ARG;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  free_batch(b);
+  return VH_OK;
+}
+
+int32_t vh_batch_size(const vh_batch *b) { return b ? b->n : 0; }
+
+vh_handle *vh_batch_scene(vh_batch *b, int32_t i) {
+  return b && i >= 0 && i < b->n ? b->scenes[i] : nullptr;
+}
+
+vh_status vh_batch_process(vh_batch *b, const void *const *depth, int32_t depth_fmt,
+                           const uint8_t *const *rgb, const float *c2w, int32_t mem,
+                           int32_t with_mesh) {
+  if (!b || !depth || !rgb || !c2w) return VH_ERR_INVALID_ARG;
+  if (depth_fmt != VH_DEPTH_U16_MM && depth_fmt != VH_DEPTH_F32_M)
+    return fail(b, VH_ERR_INVALID_ARG, "unknown depth format");
+  if (mem != VH_MEM_HOST && mem != VH_MEM_DEVICE)
+    return fail(b, VH_ERR_INVALID_ARG, "unknown memory kind");
+  for (int i = 0; i < b->n; ++i) {
+    if (!depth[i]) continue;
+    if (!rgb[i]) return fail(b, VH_ERR_INVALID_ARG, "scene with depth but no colour");
+    for (int k = 0; k < 16; ++k)
+      if (!std::isfinite(c2w[16 * i + k]))
+        return fail(b, VH_ERR_NOT_FINITE, "camera pose has a non-finite entry");
+  }
+  // the upload block of this step (reused only after its copy ran)
+  unsigned char *blk = b->h_block + b->block_bytes * b->ring_pos;
+  if (cudaEventSynchronize(b->ring_ev[b->ring_pos]) != cudaSuccess)
+    return fail(b, VH_ERR_CUDA, "upload ring wait failed");
+  SceneDesc *hd = reinterpret_cast<SceneDesc *>(blk);
+  float *hp = reinterpret_cast<float *>(blk + b->desc_bytes);
+  uint8_t *ha = blk + b->desc_bytes + b->pose_bytes;
+  for (int i = 0; i < b->n; ++i) {
+    vh_handle *h = b->scenes[i];
+    const FrameBuffers fb = handle_frame_buffers(h);
+    SceneDesc &sd = hd[i];
+    std::memset(&sd, 0, sizeof(sd));
+    sd.V = handle_view(h);
+    sd.C = handle_cam(h);
+    sd.depth = fb.depth;
+    sd.rgb = fb.rgb;
+    sd.pose = b->pose(i);
+    sd.pix = fb.pix;
+    sd.tris = fb.tris;
+    sd.tri_cap = (uint32_t)std::min<int64_t>(fb.tri_cap, 0xFFFFFFFFll);
+    ha[i] = depth[i] ? 1 : 0;
+    std::memcpy(hp + 16 * (size_t)i, c2w + 16 * (size_t)i, 16 * sizeof(float));
+    if (!depth[i]) continue;
+    if (mem == VH_MEM_DEVICE) {  // read in place: no staging copy
+      sd.depth = depth[i];
+      sd.rgb = rgb[i];
+      continue;
+    }
+    const vh_params &p = handle_params(h);
+    const size_t npx = (size_t)p.width * p.height;
+    const size_t dbytes = npx * (depth_fmt == VH_DEPTH_U16_MM ? 2 : 4);
+    if (cudaMemcpyAsync(fb.depth, depth[i], dbytes, cudaMemcpyHostToDevice, b->stream) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(fb.rgb, rgb[i], 3 * npx, cudaMemcpyHostToDevice, b->stream) != cudaSuccess)
+      return fail(b, VH_ERR_CUDA, "frame staging failed");
+  }
+  if (cudaMemcpyAsync(b->d_block, blk, b->block_bytes, cudaMemcpyHostToDevice, b->stream) !=
+          cudaSuccess ||
+      cudaEventRecord(b->ring_ev[b->ring_pos], b->stream) != cudaSuccess)
+    return fail(b, VH_ERR_CUDA, "descriptor upload failed");
+  b->ring_pos = (b->ring_pos + 1) % kRing;
+  const bool graphs_ok = !(handle_params(b->scenes[0]).flags & VH_FLAG_NO_GRAPH);
+  if (graphs_ok) {
+    cudaGraphExec_t &g = b->graphs[depth_fmt][with_mesh ? 1 : 0];
+    if (!g) {
+      cudaGraph_t graph = nullptr;
+      if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        return fail(b, VH_ERR_CUDA, "capture failed");
+      enqueue_step(b, depth_fmt, with_mesh != 0);
+      cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&g, graph, 0);
+      if (graph) cudaGraphDestroy(graph);
+      if (e != cudaSuccess) {
+        g = nullptr;
+        return fail(b, VH_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(e));
+      }
+    }
+    if (cudaGraphLaunch(g, b->stream) != cudaSuccess) return fail(b, VH_ERR_CUDA, "graph launch");
+  } else {
+    enqueue_step(b, depth_fmt, with_mesh != 0);
+    if (cudaGetLastError() != cudaSuccess) return fail(b, VH_ERR_CUDA, "batch launch failed");
+  }
+  for (int i = 0; i < b->n; ++i)
+    if (depth[i]) handle_note_frame(b->scenes[i]);
+  if (handle_params(b->scenes[0]).flags & VH_FLAG_SYNC) return check_batch(b, nullptr, nullptr, false);
+  return VH_OK;
+}
+
+vh_status vh_batch_sync(vh_batch *b, vh_status *status, vh_stats *stats) {
+  if (!b) return VH_ERR_INVALID_ARG;
+  return check_batch(b, status, stats, true);
+}
+
+}  // extern "C"
+
+namespace {
+
+// Waits for the batch and maps every scene's sticky error bits to a status;
+// `clear` resets them afterwards.
+vh_status check_batch(vh_batch *b, vh_status *status, vh_stats *stats, bool clear) {
+  launch_batch_gather_state(b->desc(), b->n, b->d_states, b->stream);
+  if (cudaMemcpyAsync(b->h_states, b->d_states, sizeof(DevState) * b->n, cudaMemcpyDeviceToHost,
+                      b->stream) != cudaSuccess ||
+      cudaStreamSynchronize(b->stream) != cudaSuccess)
+    return fail(b, VH_ERR_CUDA, std::string("batch sync: ") + cudaGetErrorString(cudaGetLastError()));
+  vh_status first = VH_OK;
+  bool any_error = false;
+  for (int i = 0; i < b->n; ++i) {
+    const DevState &st = b->h_states[i];
+    vh_handle *h = b->scenes[i];
+    const vh_status s = handle_status_of_bits(h, st.error);
+    any_error = any_error || st.error;
+    if (status) status[i] = s;
+    if (s != VH_OK && first == VH_OK) first = s;
+    if (stats) {
+      const vh_params &p = handle_params(h);
+      vh_stats &o = stats[i];
+      std::memset(&o, 0, sizeof(o));
+      o.frames = handle_frames(h);
+      o.blocks_allocated = (int64_t)st.pool_top - (int64_t)st.free_count;
+      o.frame_blocks = std::min<int64_t>(st.frame_count, p.max_frame_blocks);
+      o.new_blocks = st.new_blocks;
+      o.voxels_updated = (int64_t)st.voxels_updated;
+      o.triangles = st.tri_count;
+      o.pool_capacity = p.pool_blocks;
+      o.table_slots = (int64_t)1 << p.table_log2;
+      o.tombstones = st.tombstones;
+      o.device_error = st.error;
+    }
+  }
+  if (any_error && clear) {
+    launch_batch_clear_errors(b->desc(), b->n, b->stream);
+    if (cudaStreamSynchronize(b->stream) != cudaSuccess) return fail(b, VH_ERR_CUDA, "clear failed");
+  }
+  return first;
+}
+
+}  // namespace

@@ -123,6 +123,23 @@ __host__ __device__ inline unsigned long long ref_block_hash(int x, int y, int z
          ((unsigned long long)(long long)z * 83492791ull);
 }
 
+// One scene of a batch: everything the batched kernels need to reach the
+// scene's volume and its staged frame (device array built by vh_batch.cpp).
+struct SceneDesc {
+  VolumeView V;
+  CamParams C;
+  const void *depth;  // staged depth (format shared by the batch)
+  const uint8_t *rgb;
+  const float *pose;  // row-major camera-to-world, rows 0-2 used
+  uint2 *pix;
+  float4 *tris;
+  uint32_t tri_cap;
+  uint32_t pad;
+};
+
+constexpr int kMaxBatchScenes = 1024;
+constexpr int kBatchPixelThreads = 256;  // threads of a batched allocation CTA
+
 // ---- host-side launchers (vh_kernels.cu) ----------------------------------
 void launch_frame_begin(const VolumeView &V, cudaStream_t s);
 void launch_epoch_end(const VolumeView &V, cudaStream_t s);
@@ -149,5 +166,28 @@ void launch_frame_resolve(const VolumeView &V, int grid, cudaStream_t s);
 void launch_list_keys(const VolumeView &V, int32_t *xyz, uint32_t n, cudaStream_t s);
 void launch_scatter_blocks(const VolumeView &V, const int32_t *xyz, const float *sdf,
                            const float *w, const uint8_t *rgb, uint32_t n, cudaStream_t s);
+
+// Batched stages: one launch covers the work of every active scene.
+// active[i] != 0: scene i has a frame this step.  px_start: first global
+// pixel of each scene (multiples of kBatchPixelThreads; n + 1 entries).  prefix: per-scene
+// work prefix (n + 1 entries) written by launch_batch_epoch_end (frame
+// lists) and read by the later stages.
+void launch_batch_frame_begin(const SceneDesc *d, const uint8_t *active, int n, cudaStream_t s);
+void launch_batch_allocate(const SceneDesc *d, const uint8_t *active, const uint32_t *px_start,
+                           uint32_t total_px, int n, int fmt, cudaStream_t s);
+void launch_batch_epoch_end(const SceneDesc *d, const uint8_t *active, int n, uint32_t *prefix,
+                            cudaStream_t s);
+void launch_batch_resolve(const SceneDesc *d, const uint32_t *prefix, int n, int grid,
+                          cudaStream_t s);
+void launch_batch_integrate(const SceneDesc *d, const uint32_t *prefix, int n, int grid,
+                            cudaStream_t s);
+void launch_batch_mc_begin(const SceneDesc *d, const uint8_t *active, int n, cudaStream_t s);
+void launch_batch_mc(const SceneDesc *d, const uint32_t *prefix, int n, int grid, int variant,
+                     cudaStream_t s);
+void launch_batch_gather_state(const SceneDesc *d, int n, DevState *out, cudaStream_t s);
+// Resident CTAs per SM of the batched persistent kernels.
+int batch_integrate_ctas_per_sm();
+int batch_mc_ctas_per_sm(int variant);
+void launch_batch_clear_errors(const SceneDesc *d, int n, cudaStream_t s);
 
 }  // namespace vh

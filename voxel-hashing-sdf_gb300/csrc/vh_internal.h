@@ -19,6 +19,24 @@ int handle_sm_count(const vh_handle *h);
 vh_status handle_stage_depth(vh_handle *h, const void *depth, int fmt, int mem, const void **dev);
 // Device workspace owned by the handle, grown on demand, freed with it.
 vh_status handle_workspace(vh_handle *h, size_t bytes, void **ptr);
+// Frame buffers and launch shapes of a handle, for the batched frame step.
+struct FrameBuffers {
+  void *depth;
+  uint8_t *rgb;
+  uint2 *pix;
+  float4 *tris;
+  int64_t tri_cap;
+  int integrate_per_sm;
+  int mc_per_sm;
+  int mc_variant;
+};
+FrameBuffers handle_frame_buffers(const vh_handle *h);
+const vh_params &handle_params(const vh_handle *h);
+// Bookkeeping after a batched frame step ran on the handle's volume.
+void handle_note_frame(vh_handle *h);
+int64_t handle_frames(const vh_handle *h);
+// Reports sticky device error bits as a status (and records the message).
+vh_status handle_status_of_bits(vh_handle *h, uint32_t bits);
 // Pose-refinement state (buffers, cached graph) created on first use by
 // vh_adjoint.cu and released with the handle.
 struct RefineCtx;

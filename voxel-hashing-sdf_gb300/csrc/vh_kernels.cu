@@ -232,14 +232,15 @@ __device__ __forceinline__ float load_depth<float>(const float *d, int i, float)
 }
 
 // ---- allocation ----------------------------------------------------------------
+// Pixel idx of one frame (all 32 lanes of the warp take part: the band walk
+// is de-duplicated per warp).  Lanes with idx >= npx only follow the warp.
 template <typename DepthT>
-__global__ void __launch_bounds__(256) k_allocate(VolumeView V, CamParams C,
-                                                  const DepthT *__restrict__ depth,
-                                                  const uint8_t *__restrict__ rgb,
-                                                  const float *__restrict__ pose,
-                                                  uint2 *__restrict__ pix) {
+__device__ __forceinline__ void allocate_pixel(const VolumeView &V, const CamParams &C,
+                                               const DepthT *__restrict__ depth,
+                                               const uint8_t *__restrict__ rgb,
+                                               const float *__restrict__ pose,
+                                               uint2 *__restrict__ pix, int idx) {
   const int npx = C.width * C.height;
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   float P[12];
 #pragma unroll
@@ -290,6 +291,15 @@ __global__ void __launch_bounds__(256) k_allocate(VolumeView V, CamParams C,
     stamp_and_append(V, leader, slot, frame);
     if (active) active = walk_next(w);
   }
+}
+
+template <typename DepthT>
+__global__ void __launch_bounds__(256) k_allocate(VolumeView V, CamParams C,
+                                                  const DepthT *__restrict__ depth,
+                                                  const uint8_t *__restrict__ rgb,
+                                                  const float *__restrict__ pose,
+                                                  uint2 *__restrict__ pix) {
+  allocate_pixel<DepthT>(V, C, depth, rgb, pose, pix, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ---- integration ---------------------------------------------------------------
@@ -412,6 +422,44 @@ __device__ __forceinline__ void load_quad(const VolumeView &V, uint32_t i, int t
   q.rgb = reinterpret_cast<const uint4 *>(base + 2 * kB3)[t];
 }
 
+// Frame-list entry i whose voxel quad (thread t = threadIdx.x) is loaded in
+// `cur`: threads 0..7 record the block's +x/+y/+z neighbour ids for MC
+// (lane 0: the block itself; lane k: the block at +(k & 1, k >> 1 & 1,
+// k >> 2)), every thread updates and stores its 4 voxels.  Returns the
+// number of voxels this thread updated.
+__device__ __forceinline__ uint32_t integrate_loaded(const VolumeView &V, const CamParams &C,
+                                                     const float (&P)[12],
+                                                     const uint2 *__restrict__ pix, uint32_t i,
+                                                     BlockQuad &cur) {
+  const int t = threadIdx.x;
+  const int x0 = (t & 1) * 4, y = (t >> 1) & 7, z = t >> 4;
+  const bool live = cur.key < kTombKey && cur.block != kNoBlock;
+  if (t < 8) {
+    uint32_t nbid = kNoBlock;
+    if (live) {
+      int bx, by, bz;
+      unpack_key(cur.key, bx, by, bz);
+      const int nx = bx + (t & 1), ny = by + ((t >> 1) & 1), nz = bz + (t >> 2);
+      nbid = t == 0 ? cur.block
+                    : (key_in_range(nx, ny, nz) ? block_of(V, pack_key(nx, ny, nz)) : kNoBlock);
+    }
+    V.frame_nb[8 * (size_t)i + t] = nbid;
+  }
+  if (!live) return 0;
+  int bx, by, bz;
+  unpack_key(cur.key, bx, by, bz);
+  const float wy = (float)(by * kB + y) * C.voxel;
+  const float wz = (float)(bz * kB + z) * C.voxel;
+  const uint32_t nu = update_quad(C, P, pix, bx * kB + x0, wy, wz, cur.sdf, cur.wt, cur.rgb);
+  if (nu) {
+    float *base = V.pool + (size_t)cur.block * kBlockWords;
+    reinterpret_cast<float4 *>(base)[t] = cur.sdf;
+    reinterpret_cast<float4 *>(base + kB3)[t] = cur.wt;
+    reinterpret_cast<uint4 *>(base + 2 * kB3)[t] = cur.rgb;
+  }
+  return nu;
+}
+
 // Persistent CTAs of 128 threads, one voxel block per iteration, 4 voxels
 // per thread.  kPrefetch: the next block's loads are issued before the
 // current block is computed (two blocks in flight per thread, more
@@ -426,7 +474,6 @@ __global__ void __launch_bounds__(128) k_integrate(VolumeView V, CamParams C,
 #pragma unroll
   for (int k = 0; k < 12; ++k) P[k] = __ldg(pose + k);
   const int t = threadIdx.x;
-  const int x0 = (t & 1) * 4, y = (t >> 1) & 7, z = t >> 4;
   uint32_t updated = 0;
   uint32_t i = blockIdx.x;
   BlockQuad cur;
@@ -439,34 +486,7 @@ __global__ void __launch_bounds__(128) k_integrate(VolumeView V, CamParams C,
     } else {
       load_quad(V, i, t, cur);
     }
-    const bool live = cur.key < kTombKey && cur.block != kNoBlock;
-    if (t < 8) {
-      // lane 0: the block itself; lane k: the block at +(k & 1, k >> 1 & 1, k >> 2)
-      uint32_t nbid = kNoBlock;
-      if (live) {
-        int bx, by, bz;
-        unpack_key(cur.key, bx, by, bz);
-        const int nx = bx + (t & 1), ny = by + ((t >> 1) & 1), nz = bz + (t >> 2);
-        nbid = t == 0 ? cur.block
-                      : (key_in_range(nx, ny, nz) ? block_of(V, pack_key(nx, ny, nz)) : kNoBlock);
-      }
-      V.frame_nb[8 * (size_t)i + t] = nbid;
-    }
-    if (live) {
-      int bx, by, bz;
-      unpack_key(cur.key, bx, by, bz);
-      const float wy = (float)(by * kB + y) * C.voxel;
-      const float wz = (float)(bz * kB + z) * C.voxel;
-      const uint32_t nu =
-          update_quad(C, P, pix, bx * kB + x0, wy, wz, cur.sdf, cur.wt, cur.rgb);
-      if (nu) {
-        float *base = V.pool + (size_t)cur.block * kBlockWords;
-        reinterpret_cast<float4 *>(base)[t] = cur.sdf;
-        reinterpret_cast<float4 *>(base + kB3)[t] = cur.wt;
-        reinterpret_cast<uint4 *>(base + 2 * kB3)[t] = cur.rgb;
-      }
-      updated += nu;
-    }
+    updated += integrate_loaded(V, C, P, pix, i, cur);
     if (kPrefetch) cur = nxt;
   }
 #pragma unroll
@@ -618,10 +638,8 @@ __device__ __forceinline__ uint32_t cta_scan(McShared &S, uint32_t v, uint32_t *
 //   triangles (scan) -> one thread per candidate tests the reference's
 //   degenerate-triangle rule -> compact (scan) -> one atomic per block ->
 //   one thread per output float4, contiguous stores.
-template <int kMinCtas>
-__global__ void __launch_bounds__(kMcThreads, kMinCtas) k_mc(VolumeView V, int scope_all, float min_weight,
-                                                      float4 *__restrict__ tris, uint32_t tri_cap) {
-  __shared__ McShared S;
+// Tables and halo map of the MC shared state (once per CTA).
+__device__ __forceinline__ void mc_init_shared(McShared &S) {
   const int t = threadIdx.x;
   for (int i = t; i < 256; i += kMcThreads) {
     S.edge[i] = kMcEdgeMask[i];
@@ -653,137 +671,154 @@ __global__ void __launch_bounds__(kMcThreads, kMinCtas) k_mc(VolumeView V, int s
     const uint32_t li = (uint32_t)((x & 7) + 8 * (y & 7) + 64 * (z & 7));
     S.halo[hh] = (uint32_t)hidx(x, y, z) | (nbi << 10) | (li << 13);
   }
-  const uint32_t n = scope_all ? V.st->pool_top : min(V.st->frame_count, V.frame_cap);
+}
+
+// One block of the list (scope_all: pool block i; else frame-list entry i):
+// stage, classify, expand, test, compact and write its triangles.  Every
+// thread of the CTA calls it with the same i; S must be free on entry.
+__device__ __forceinline__ void mc_block(McShared &S, const VolumeView &V, int scope_all,
+                                         float min_weight, float4 *__restrict__ tris,
+                                         uint32_t tri_cap, uint32_t i) {
+  const int t = threadIdx.x;
   const float nanv = __int_as_float(0x7FC00000);
+  // Every thread reads the block's key and id itself (broadcast loads), so
+  // the voxel loads below start without waiting for a barrier.
+  unsigned long long key;
+  uint32_t own;
+  if (scope_all) {
+    key = __ldg(V.block_keys + i);
+    own = key < kTombKey ? i : kNoBlock;
+  } else {
+    const ulonglong2 r = __ldg(V.frame_res + i);
+    key = r.x;
+    own = key < kTombKey ? (uint32_t)r.y : kNoBlock;
+  }
+  if (own == kNoBlock) return;  // same entry for every thread: uniform
+  int bx, by, bz;
+  unpack_key(key, bx, by, bz);
+  if (scope_all && t < 8) {
+    const int nx = bx + (t & 1), ny = by + ((t >> 1) & 1), nz = bz + (t >> 2);
+    S.nb[t] = t == 0 ? own
+                     : (key_in_range(nx, ny, nz) ? block_of(V, pack_key(nx, ny, nz)) : kNoBlock);
+  }
+  {  // own block: 4 voxels per thread, 16-byte loads
+    const float *base = V.pool + (size_t)own * kBlockWords;
+    const float4 sd = reinterpret_cast<const float4 *>(base)[t];
+    const float4 wt = reinterpret_cast<const float4 *>(base + kB3)[t];
+    const uint4 cl = reinterpret_cast<const uint4 *>(base + 2 * kB3)[t];
+    const int li = 4 * t, x = li & 7, y = (li >> 3) & 7, z = li >> 6;
+    const int h = hidx(x, y, z);
+    S.sdf[h + 0] = wt.x >= min_weight ? sd.x : nanv;
+    S.sdf[h + 1] = wt.y >= min_weight ? sd.y : nanv;
+    S.sdf[h + 2] = wt.z >= min_weight ? sd.z : nanv;
+    S.sdf[h + 3] = wt.w >= min_weight ? sd.w : nanv;
+    S.rgb[h + 0] = cl.x;
+    S.rgb[h + 1] = cl.y;
+    S.rgb[h + 2] = cl.z;
+    S.rgb[h + 3] = cl.w;
+  }
+  if (scope_all) __syncthreads();  // S.nb complete (uniform condition)
+  {  // halo: every thread owns at most two entries; all loads issued together
+    const int h1 = t + kMcThreads;
+    const uint32_t info0 = S.halo[t];
+    const uint32_t info1 = h1 < kHalo ? S.halo[h1] : 0u;
+    const uint32_t nb0 = (info0 >> 10) & 7u, nb1 = (info1 >> 10) & 7u;
+    const uint32_t blk0 = scope_all ? S.nb[nb0] : __ldg(V.frame_nb + 8 * (size_t)i + nb0);
+    uint32_t blk1 = scope_all ? S.nb[nb1] : __ldg(V.frame_nb + 8 * (size_t)i + nb1);
+    if (h1 >= kHalo) blk1 = kNoBlock;
+    const int li0 = (int)(info0 >> 13), li1 = (int)(info1 >> 13);
+    float w0 = 0.f, s0 = nanv, w1 = 0.f, s1 = nanv;
+    uint32_t c0 = 0, c1 = 0;
+    if (blk0 != kNoBlock) {
+      const float *base = V.pool + (size_t)blk0 * kBlockWords;
+      w0 = __ldg(base + kB3 + li0);
+      s0 = __ldg(base + li0);
+      c0 = __ldg(reinterpret_cast<const uint32_t *>(base + 2 * kB3) + li0);
+    }
+    if (blk1 != kNoBlock) {
+      const float *base = V.pool + (size_t)blk1 * kBlockWords;
+      w1 = __ldg(base + kB3 + li1);
+      s1 = __ldg(base + li1);
+      c1 = __ldg(reinterpret_cast<const uint32_t *>(base + 2 * kB3) + li1);
+    }
+    S.sdf[info0 & 1023u] = blk0 != kNoBlock && w0 >= min_weight ? s0 : nanv;
+    S.rgb[info0 & 1023u] = c0;
+    if (h1 < kHalo) {
+      S.sdf[info1 & 1023u] = blk1 != kNoBlock && w1 >= min_weight ? s1 : nanv;
+      S.rgb[info1 & 1023u] = c1;
+    }
+  }
+  __syncthreads();
+  // 1. classify this thread's 4 cubes; count their candidate triangles
+  uint32_t ncand_mine = 0;
+  int cs[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int c = t + kMcThreads * j;
+    int ci = cube_case(S, c & 7, (c >> 3) & 7, c >> 6);
+    if (ci < 0 || S.edge[ci] == 0) ci = 0;
+    cs[j] = ci;
+    S.cases[c] = (uint8_t)ci;
+    ncand_mine += S.ntri[ci];
+  }
+  uint32_t ncand;
+  uint32_t off = cta_scan(S, ncand_mine, &ncand);
+  if (ncand == 0) return;  // uniform: nothing to emit in this block
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int c = t + kMcThreads * j;
+    const int nt = S.ntri[cs[j]];
+    for (int tt = 0; tt < nt; ++tt) S.cand[off++] = (uint16_t)(c | (tt << 9));
+  }
+  __syncthreads();
+  // 2. candidates in rounds of one per thread: the thread computes its
+  //    candidate's three vertices once, the reference's degenerate test
+  //    drops p0 == p1 || p1 == p2 (src/tsdf.cu:1055-1057), a CTA scan over
+  //    the survivors gives each a slot in one contiguous range reserved
+  //    with a single atomic, and the thread writes its 48-byte triangle.
+  const int gx0 = bx * kB, gy0 = by * kB, gz0 = bz * kB;
+  for (uint32_t r0 = 0; r0 < ncand; r0 += kMcThreads) {
+    const uint32_t k = r0 + t;
+    float4 p0, p1, p2;
+    uint32_t ok = 0;
+    if (k < ncand) {
+      const uint32_t ent = S.cand[k];
+      const int c = (int)(ent & 511u), tt = (int)(ent >> 9);
+      const int x = c & 7, y = (c >> 3) & 7, z = c >> 6;
+      const uint32_t tri = S.tri[S.cases[c]][tt];
+      const int h0 = hidx(x, y, z);
+      p0 = mc_vertex<true>(S, (int)(tri & 15u), h0, gx0 + x, gy0 + y, gz0 + z);
+      p1 = mc_vertex<true>(S, (int)((tri >> 4) & 15u), h0, gx0 + x, gy0 + y, gz0 + z);
+      p2 = mc_vertex<true>(S, (int)(tri >> 8), h0, gx0 + x, gy0 + y, gz0 + z);
+      ok = !(same_pos(p0, p1) || same_pos(p1, p2));
+    }
+    uint32_t nvalid;
+    const uint32_t pre = cta_scan(S, ok, &nvalid);
+    if (t == 0) S.base = nvalid ? atomicAdd(&V.st->tri_count, nvalid) : 0u;
+    __syncthreads();
+    if (ok) {
+      const uint32_t out = S.base + pre;
+      if (out < tri_cap) {
+        float4 *dst = tris + 3 * (size_t)out;
+        dst[0] = p0;
+        dst[1] = p1;
+        dst[2] = p2;
+      } else {
+        atomicOr(&V.st->error, kErrTriCap);
+      }
+    }
+  }
+}
+
+template <int kMinCtas>
+__global__ void __launch_bounds__(kMcThreads, kMinCtas) k_mc(VolumeView V, int scope_all, float min_weight,
+                                                      float4 *__restrict__ tris, uint32_t tri_cap) {
+  __shared__ McShared S;
+  mc_init_shared(S);
+  const uint32_t n = scope_all ? V.st->pool_top : min(V.st->frame_count, V.frame_cap);
   for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
     __syncthreads();  // previous iteration done with S
-    // Every thread reads the block's key and id itself (broadcast loads), so
-    // the voxel loads below start without waiting for a barrier.
-    unsigned long long key;
-    uint32_t own;
-    if (scope_all) {
-      key = __ldg(V.block_keys + i);
-      own = key < kTombKey ? i : kNoBlock;
-    } else {
-      const ulonglong2 r = __ldg(V.frame_res + i);
-      key = r.x;
-      own = key < kTombKey ? (uint32_t)r.y : kNoBlock;
-    }
-    if (own == kNoBlock) continue;  // same entry for every thread: uniform
-    int bx, by, bz;
-    unpack_key(key, bx, by, bz);
-    if (scope_all && t < 8) {
-      const int nx = bx + (t & 1), ny = by + ((t >> 1) & 1), nz = bz + (t >> 2);
-      S.nb[t] = t == 0 ? own
-                       : (key_in_range(nx, ny, nz) ? block_of(V, pack_key(nx, ny, nz)) : kNoBlock);
-    }
-    {  // own block: 4 voxels per thread, 16-byte loads
-      const float *base = V.pool + (size_t)own * kBlockWords;
-      const float4 sd = reinterpret_cast<const float4 *>(base)[t];
-      const float4 wt = reinterpret_cast<const float4 *>(base + kB3)[t];
-      const uint4 cl = reinterpret_cast<const uint4 *>(base + 2 * kB3)[t];
-      const int li = 4 * t, x = li & 7, y = (li >> 3) & 7, z = li >> 6;
-      const int h = hidx(x, y, z);
-      S.sdf[h + 0] = wt.x >= min_weight ? sd.x : nanv;
-      S.sdf[h + 1] = wt.y >= min_weight ? sd.y : nanv;
-      S.sdf[h + 2] = wt.z >= min_weight ? sd.z : nanv;
-      S.sdf[h + 3] = wt.w >= min_weight ? sd.w : nanv;
-      S.rgb[h + 0] = cl.x;
-      S.rgb[h + 1] = cl.y;
-      S.rgb[h + 2] = cl.z;
-      S.rgb[h + 3] = cl.w;
-    }
-    if (scope_all) __syncthreads();  // S.nb complete (uniform condition)
-    {  // halo: every thread owns at most two entries; all loads issued together
-      const int h1 = t + kMcThreads;
-      const uint32_t info0 = S.halo[t];
-      const uint32_t info1 = h1 < kHalo ? S.halo[h1] : 0u;
-      const uint32_t nb0 = (info0 >> 10) & 7u, nb1 = (info1 >> 10) & 7u;
-      const uint32_t blk0 = scope_all ? S.nb[nb0] : __ldg(V.frame_nb + 8 * (size_t)i + nb0);
-      uint32_t blk1 = scope_all ? S.nb[nb1] : __ldg(V.frame_nb + 8 * (size_t)i + nb1);
-      if (h1 >= kHalo) blk1 = kNoBlock;
-      const int li0 = (int)(info0 >> 13), li1 = (int)(info1 >> 13);
-      float w0 = 0.f, s0 = nanv, w1 = 0.f, s1 = nanv;
-      uint32_t c0 = 0, c1 = 0;
-      if (blk0 != kNoBlock) {
-        const float *base = V.pool + (size_t)blk0 * kBlockWords;
-        w0 = __ldg(base + kB3 + li0);
-        s0 = __ldg(base + li0);
-        c0 = __ldg(reinterpret_cast<const uint32_t *>(base + 2 * kB3) + li0);
-      }
-      if (blk1 != kNoBlock) {
-        const float *base = V.pool + (size_t)blk1 * kBlockWords;
-        w1 = __ldg(base + kB3 + li1);
-        s1 = __ldg(base + li1);
-        c1 = __ldg(reinterpret_cast<const uint32_t *>(base + 2 * kB3) + li1);
-      }
-      S.sdf[info0 & 1023u] = blk0 != kNoBlock && w0 >= min_weight ? s0 : nanv;
-      S.rgb[info0 & 1023u] = c0;
-      if (h1 < kHalo) {
-        S.sdf[info1 & 1023u] = blk1 != kNoBlock && w1 >= min_weight ? s1 : nanv;
-        S.rgb[info1 & 1023u] = c1;
-      }
-    }
-    __syncthreads();
-    // 1. classify this thread's 4 cubes; count their candidate triangles
-    uint32_t ncand_mine = 0;
-    int cs[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int c = t + kMcThreads * j;
-      int ci = cube_case(S, c & 7, (c >> 3) & 7, c >> 6);
-      if (ci < 0 || S.edge[ci] == 0) ci = 0;
-      cs[j] = ci;
-      S.cases[c] = (uint8_t)ci;
-      ncand_mine += S.ntri[ci];
-    }
-    uint32_t ncand;
-    uint32_t off = cta_scan(S, ncand_mine, &ncand);
-    if (ncand == 0) continue;  // uniform: nothing to emit in this block
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int c = t + kMcThreads * j;
-      const int nt = S.ntri[cs[j]];
-      for (int tt = 0; tt < nt; ++tt) S.cand[off++] = (uint16_t)(c | (tt << 9));
-    }
-    __syncthreads();
-    // 2. candidates in rounds of one per thread: the thread computes its
-    //    candidate's three vertices once, the reference's degenerate test
-    //    drops p0 == p1 || p1 == p2 (src/tsdf.cu:1055-1057), a CTA scan over
-    //    the survivors gives each a slot in one contiguous range reserved
-    //    with a single atomic, and the thread writes its 48-byte triangle.
-    const int gx0 = bx * kB, gy0 = by * kB, gz0 = bz * kB;
-    for (uint32_t r0 = 0; r0 < ncand; r0 += kMcThreads) {
-      const uint32_t k = r0 + t;
-      float4 p0, p1, p2;
-      uint32_t ok = 0;
-      if (k < ncand) {
-        const uint32_t ent = S.cand[k];
-        const int c = (int)(ent & 511u), tt = (int)(ent >> 9);
-        const int x = c & 7, y = (c >> 3) & 7, z = c >> 6;
-        const uint32_t tri = S.tri[S.cases[c]][tt];
-        const int h0 = hidx(x, y, z);
-        p0 = mc_vertex<true>(S, (int)(tri & 15u), h0, gx0 + x, gy0 + y, gz0 + z);
-        p1 = mc_vertex<true>(S, (int)((tri >> 4) & 15u), h0, gx0 + x, gy0 + y, gz0 + z);
-        p2 = mc_vertex<true>(S, (int)(tri >> 8), h0, gx0 + x, gy0 + y, gz0 + z);
-        ok = !(same_pos(p0, p1) || same_pos(p1, p2));
-      }
-      uint32_t nvalid;
-      const uint32_t pre = cta_scan(S, ok, &nvalid);
-      if (t == 0) S.base = nvalid ? atomicAdd(&V.st->tri_count, nvalid) : 0u;
-      __syncthreads();
-      if (ok) {
-        const uint32_t out = S.base + pre;
-        if (out < tri_cap) {
-          float4 *dst = tris + 3 * (size_t)out;
-          dst[0] = p0;
-          dst[1] = p1;
-          dst[2] = p2;
-        } else {
-          atomicOr(&V.st->error, kErrTriCap);
-        }
-      }
-    }
+    mc_block(S, V, scope_all, min_weight, tris, tri_cap, i);
   }
 }
 
@@ -801,8 +836,7 @@ __device__ void reconcile(const VolumeView &V) {
   st->ticket = 0;
 }
 
-__global__ void k_frame_begin(VolumeView V) {
-  if (threadIdx.x != 0) return;
+__device__ void frame_begin_state(const VolumeView &V) {
   reconcile(V);
   DevState *st = V.st;
   uint32_t f = st->frame + 1u;
@@ -811,6 +845,15 @@ __global__ void k_frame_begin(VolumeView V) {
   st->frame_count = 0;
   st->new_blocks = 0;
   st->voxels_updated = 0;
+}
+
+__device__ void mc_begin_state(const VolumeView &V) {
+  reconcile(V);
+  V.st->tri_count = 0;
+}
+
+__global__ void k_frame_begin(VolumeView V) {
+  if (threadIdx.x == 0) frame_begin_state(V);
 }
 
 __global__ void k_epoch_end(VolumeView V) {
@@ -827,10 +870,188 @@ __global__ void k_clear_list(VolumeView V) {
 }
 
 __global__ void k_mc_begin(VolumeView V) {
-  if (threadIdx.x == 0) {
-    reconcile(V);
-    V.st->tri_count = 0;
+  if (threadIdx.x == 0) mc_begin_state(V);
+}
+
+// ---- batched scenes -----------------------------------------------------------------
+// The stages of one frame for many independent scenes, each stage one launch
+// over the work of all scenes (flattened (scene, item) index, items of a
+// scene contiguous).  Per item the bodies above run unchanged with that
+// scene's volume, camera and frame.
+
+// Scene s with prefix[s] <= g < prefix[s + 1] (prefix non-decreasing,
+// prefix[0] = 0 <= g < prefix[n]); empty scenes are skipped.
+__device__ __forceinline__ int scene_of(const uint32_t *__restrict__ prefix, int n, uint32_t g) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(prefix + mid) <= g)
+      lo = mid;
+    else
+      hi = mid;
   }
+  return lo;
+}
+
+// Copies scene s's descriptor into shared memory (whole CTA, then a barrier).
+__device__ __forceinline__ void load_scene(SceneDesc &dst, const SceneDesc *__restrict__ d, int s) {
+  static_assert(sizeof(SceneDesc) % 4 == 0, "word copy");
+  const uint32_t *src = reinterpret_cast<const uint32_t *>(d + s);
+  uint32_t *out = reinterpret_cast<uint32_t *>(&dst);
+  for (int k = threadIdx.x; k < (int)(sizeof(SceneDesc) / 4); k += blockDim.x) out[k] = __ldg(src + k);
+  __syncthreads();
+}
+
+__global__ void k_batch_frame_begin(const SceneDesc *__restrict__ d,
+                                    const uint8_t *__restrict__ active, int n) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n && active[s]) frame_begin_state(d[s].V);
+}
+
+// One thread per pixel of every scene; scene s owns global pixels
+// [px_start[s], px_start[s + 1]), a multiple of the CTA size, so that a CTA
+// (and a warp: the band walk de-duplicates keys per warp) never spans two
+// scenes and the scene's descriptor is read once per CTA.
+template <typename DepthT>
+__global__ void __launch_bounds__(kBatchPixelThreads) k_batch_allocate(
+    const SceneDesc *__restrict__ d, const uint8_t *__restrict__ active,
+    const uint32_t *__restrict__ px_start, int n) {
+  __shared__ SceneDesc sd;
+  const uint32_t g0 = blockIdx.x * blockDim.x;
+  if (g0 >= __ldg(px_start + n)) return;  // whole CTAs
+  const int s = scene_of(px_start, n, g0);
+  if (!active[s]) return;  // CTA-uniform
+  load_scene(sd, d, s);
+  allocate_pixel<DepthT>(sd.V, sd.C, static_cast<const DepthT *>(sd.depth), sd.rgb, sd.pose,
+                         sd.pix, (int)(g0 + threadIdx.x - __ldg(px_start + s)));
+}
+
+// Closes every active scene's allocation epoch and writes the prefix of the
+// frame-list lengths (one CTA of 1024 threads, n <= 1024).
+__global__ void __launch_bounds__(1024) k_batch_epoch_end(const SceneDesc *__restrict__ d,
+                                                          const uint8_t *__restrict__ active,
+                                                          int n, uint32_t *__restrict__ prefix) {
+  __shared__ uint32_t wsum[32];
+  const int s = threadIdx.x, lane = s & 31, warp = s >> 5;
+  uint32_t cnt = 0;
+  if (s < n && active[s]) {
+    const VolumeView &V = d[s].V;
+    reconcile(V);
+    cnt = min(V.st->frame_count, V.frame_cap);
+  }
+  uint32_t incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t u = __shfl_up_sync(kFull, incl, o);
+    if (lane >= o) incl += u;
+  }
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = wsum[lane], wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t u = __shfl_up_sync(kFull, wi, o);
+      if (lane >= o) wi += u;
+    }
+    wsum[lane] = wi - w;  // exclusive warp offsets
+  }
+  __syncthreads();
+  const uint32_t excl = wsum[warp] + incl - cnt;
+  if (s < n) prefix[s] = excl;
+  if (s == n - 1) prefix[n] = excl + cnt;
+}
+
+__global__ void __launch_bounds__(256) k_batch_resolve(const SceneDesc *__restrict__ d,
+                                                       const uint32_t *__restrict__ prefix, int n) {
+  const uint32_t total = __ldg(prefix + n);
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+    const int s = scene_of(prefix, n, g);
+    const VolumeView &V = d[s].V;
+    const uint32_t i = g - __ldg(prefix + s);
+    const ulonglong2 sl = __ldg(reinterpret_cast<const ulonglong2 *>(V.slots) + V.frame_list[i]);
+    V.frame_res[i] = make_ulonglong2(sl.x, sl.y & 0xFFFFFFFFull);
+  }
+}
+
+// Adds this CTA's count of updated voxels to scene `sd`'s counter.
+__device__ __forceinline__ void flush_updated(const SceneDesc &sd, uint32_t updated) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) updated += __shfl_xor_sync(kFull, updated, o);
+  if ((threadIdx.x & 31) == 0 && updated)
+    atomicAdd(&sd.V.st->voxels_updated, (unsigned long long)updated);
+}
+
+// Persistent CTAs over the listed blocks of every scene; the scene's
+// descriptor and pose live in shared memory while consecutive items stay in
+// that scene.
+__global__ void __launch_bounds__(128) k_batch_integrate(const SceneDesc *__restrict__ d,
+                                                         const uint32_t *__restrict__ prefix,
+                                                         int n) {
+  __shared__ SceneDesc sd;
+  __shared__ float sp[12];
+  const uint32_t total = __ldg(prefix + n);
+  const int t = threadIdx.x;
+  int cur = -1;
+  uint32_t updated = 0;
+  float P[12];
+  for (uint32_t g = blockIdx.x; g < total; g += gridDim.x) {
+    const int s = scene_of(prefix, n, g);
+    if (s != cur) {  // uniform: every thread computes the same s
+      if (cur >= 0) flush_updated(sd, updated);
+      updated = 0;
+      __syncthreads();  // sd free
+      load_scene(sd, d, s);
+      if (t < 12) sp[t] = __ldg(sd.pose + t);
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < 12; ++k) P[k] = sp[k];
+      cur = s;
+    }
+    const uint32_t i = g - __ldg(prefix + s);
+    BlockQuad q;
+    load_quad(sd.V, i, t, q);
+    updated += integrate_loaded(sd.V, sd.C, P, sd.pix, i, q);
+  }
+  if (cur >= 0) flush_updated(sd, updated);
+}
+
+__global__ void k_batch_mc_begin(const SceneDesc *__restrict__ d, const uint8_t *__restrict__ active,
+                                 int n) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n && active[s]) mc_begin_state(d[s].V);
+}
+
+// Per-frame marching cubes over the listed blocks of every scene.
+template <int kMinCtas>
+__global__ void __launch_bounds__(kMcThreads, kMinCtas) k_batch_mc(const SceneDesc *__restrict__ d,
+                                                            const uint32_t *__restrict__ prefix,
+                                                            int n) {
+  __shared__ McShared S;
+  __shared__ SceneDesc sd;
+  mc_init_shared(S);
+  const uint32_t total = __ldg(prefix + n);
+  int cur = -1;
+  for (uint32_t g = blockIdx.x; g < total; g += gridDim.x) {
+    __syncthreads();  // previous iteration done with S and sd
+    const int s = scene_of(prefix, n, g);
+    if (s != cur) {
+      load_scene(sd, d, s);
+      cur = s;
+    }
+    mc_block(S, sd.V, 0, sd.C.mc_min_weight, sd.tris, sd.tri_cap, g - __ldg(prefix + s));
+  }
+}
+
+__global__ void k_batch_gather_state(const SceneDesc *__restrict__ d, int n,
+                                     DevState *__restrict__ out) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) out[s] = *d[s].V.st;
+}
+
+__global__ void k_batch_clear_errors(const SceneDesc *__restrict__ d, int n) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) d[s].V.st->error = 0;
 }
 
 // ---- hash surface -----------------------------------------------------------------
@@ -1040,6 +1261,60 @@ void launch_list_keys(const VolumeView &V, int32_t *xyz, uint32_t n, cudaStream_
 void launch_scatter_blocks(const VolumeView &V, const int32_t *xyz, const float *sdf,
                            const float *w, const uint8_t *rgb, uint32_t n, cudaStream_t s) {
   if (n) k_scatter_blocks<<<n, 128, 0, s>>>(V, xyz, sdf, w, rgb, n);
+}
+
+void launch_batch_frame_begin(const SceneDesc *d, const uint8_t *active, int n, cudaStream_t s) {
+  k_batch_frame_begin<<<grid_for((uint32_t)n, 128), 128, 0, s>>>(d, active, n);
+}
+void launch_batch_allocate(const SceneDesc *d, const uint8_t *active, const uint32_t *px_start,
+                           uint32_t total_px, int n, int fmt, cudaStream_t s) {
+  const unsigned grid = grid_for(total_px, kBatchPixelThreads);
+  if (!grid) return;
+  if (fmt == 0)
+    k_batch_allocate<uint16_t><<<grid, kBatchPixelThreads, 0, s>>>(d, active, px_start, n);
+  else
+    k_batch_allocate<float><<<grid, kBatchPixelThreads, 0, s>>>(d, active, px_start, n);
+}
+void launch_batch_epoch_end(const SceneDesc *d, const uint8_t *active, int n, uint32_t *prefix,
+                            cudaStream_t s) {
+  k_batch_epoch_end<<<1, 1024, 0, s>>>(d, active, n, prefix);
+}
+void launch_batch_resolve(const SceneDesc *d, const uint32_t *prefix, int n, int grid,
+                          cudaStream_t s) {
+  k_batch_resolve<<<grid, 256, 0, s>>>(d, prefix, n);
+}
+void launch_batch_integrate(const SceneDesc *d, const uint32_t *prefix, int n, int grid,
+                            cudaStream_t s) {
+  k_batch_integrate<<<grid, 128, 0, s>>>(d, prefix, n);
+}
+void launch_batch_mc_begin(const SceneDesc *d, const uint8_t *active, int n, cudaStream_t s) {
+  k_batch_mc_begin<<<grid_for((uint32_t)n, 128), 128, 0, s>>>(d, active, n);
+}
+void launch_batch_mc(const SceneDesc *d, const uint32_t *prefix, int n, int grid, int variant,
+                     cudaStream_t s) {
+  if (variant == 1)
+    k_batch_mc<12><<<grid, kMcThreads, 0, s>>>(d, prefix, n);
+  else
+    k_batch_mc<8><<<grid, kMcThreads, 0, s>>>(d, prefix, n);
+}
+int batch_integrate_ctas_per_sm() {
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_integrate, 128, 0);
+  return n > 0 ? n : 1;
+}
+int batch_mc_ctas_per_sm(int variant) {
+  int n = 0;
+  if (variant == 1)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_mc<12>, kMcThreads, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_mc<8>, kMcThreads, 0);
+  return n > 0 ? n : 1;
+}
+void launch_batch_gather_state(const SceneDesc *d, int n, DevState *out, cudaStream_t s) {
+  k_batch_gather_state<<<grid_for((uint32_t)n, 128), 128, 0, s>>>(d, n, out);
+}
+void launch_batch_clear_errors(const SceneDesc *d, int n, cudaStream_t s) {
+  k_batch_clear_errors<<<grid_for((uint32_t)n, 128), 128, 0, s>>>(d, n);
 }
 
 }  // namespace vh

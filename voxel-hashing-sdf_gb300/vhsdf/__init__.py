@@ -5,5 +5,6 @@ behind a C ABI, include/vhsdf.h); this package only marshals arguments.
 """
 from ._native import VhError, BLOCK_EDGE, BLOCK_VOXELS  # noqa: F401
 from .engine import Volume, block_hash_ref  # noqa: F401
+from .batch import Batch  # noqa: F401
 from .generator import GpuTsdfGenerator, HashTable  # noqa: F401
 from . import synth  # noqa: F401

@@ -120,6 +120,12 @@ SIGNATURES = {
     "vh_pose_normal_equations": (I32, [P, P, I32, I32, P, I32, I32, P]),
     "vh_pose_refine": (I32, [P, P, I32, I32, P, I32, I32, I32, P, C.POINTER(VhRefineStats)]),
     "vh_integrate_vjp": (I32, [P, P, I32, P, P, P, P, I32]),
+    "vh_batch_create": (I32, [C.POINTER(VhParams), I32, C.POINTER(P)]),
+    "vh_batch_destroy": (I32, [P]),
+    "vh_batch_size": (I32, [P]),
+    "vh_batch_scene": (P, [P, I32]),
+    "vh_batch_process": (I32, [P, P, I32, P, P, I32, I32]),
+    "vh_batch_sync": (I32, [P, P, C.POINTER(VhStats)]),
 }
 
 _lib = None
