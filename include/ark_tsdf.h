@@ -21,7 +21,6 @@
 
 #include <cstring>
 #include <string>
-#include <unordered_map>
 #include <vector>
 
 #include "vhsdf.h"
@@ -112,44 +111,21 @@ class GpuTsdfGenerator {
     if (mesh_valid_ || !handle_) return;
     vertices_.clear();
     faces_.clear();
-    status_ = vh_extract(handle_, VH_SCOPE_ALL, nullptr);
+    int64_t nv = 0, nf = 0;
+    status_ = vh_mesh_indexed(handle_, nullptr, nullptr, 0, nullptr, 0, &nv, &nf);
     if (status_ != VH_OK) return;
-    int64_t n = 0;
-    vh_copy_mesh(handle_, nullptr, nullptr, 0, &n);
-    std::vector<float> xyz((size_t)n * 9);
-    std::vector<unsigned char> rgb((size_t)n * 9);
-    status_ = vh_copy_mesh(handle_, xyz.data(), rgb.data(), n, &n);
+    std::vector<float> xyz((size_t)nv * 3);
+    std::vector<unsigned char> rgb((size_t)nv * 3);
+    std::vector<int> idx((size_t)nf * 3);
+    status_ = vh_mesh_indexed(handle_, xyz.data(), rgb.data(), nv, idx.data(), nf, &nv, &nf);
     if (status_ != VH_OK) return;
-    struct Key {
-      float x, y, z;
-      bool operator==(const Key &o) const { return x == o.x && y == o.y && z == o.z; }
-    };
-    struct Hash {
-      size_t operator()(const Key &k) const {
-        uint32_t a, b, c;
-        std::memcpy(&a, &k.x, 4);
-        std::memcpy(&b, &k.y, 4);
-        std::memcpy(&c, &k.z, 4);
-        return (size_t)a * 73856093u ^ (size_t)b * 19349669u ^ (size_t)c * 83492791u;
-      }
-    };
-    std::unordered_map<Key, int, Hash> index;
-    for (int64_t t = 0; t < n; ++t) {
-      Face f;
-      for (int j = 0; j < 3; ++j) {
-        const float *p = &xyz[9 * t + 3 * j];
-        Key k{p[0], p[1], p[2]};
-        auto it = index.find(k);
-        if (it == index.end()) {
-          it = index.emplace(k, (int)vertices_.size()).first;
-          const unsigned char *c = &rgb[9 * t + 3 * j];
-          vertices_.push_back(Vertex{p[0] * params_.voxel_size, p[1] * params_.voxel_size,
-                                     p[2] * params_.voxel_size, c[0], c[1], c[2]});
-        }
-        f.vIdx[j] = it->second;
-      }
-      faces_.push_back(f);
-    }
+    vertices_.resize((size_t)nv);
+    for (int64_t i = 0; i < nv; ++i)
+      vertices_[i] = Vertex{xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], rgb[3 * i], rgb[3 * i + 1],
+                            rgb[3 * i + 2]};
+    faces_.resize((size_t)nf);
+    for (int64_t t = 0; t < nf; ++t)
+      for (int j = 0; j < 3; ++j) faces_[t].vIdx[j] = idx[3 * t + j];
     mesh_valid_ = true;
   }
 

@@ -187,8 +187,17 @@ vh_status vh_copy_mesh(vh_handle *h, float *xyz, uint8_t *rgb,
 /* Full-volume extraction written as PLY with vertices merged by exact
  * position, as GpuTsdfGenerator::SavePLY / tsdf2mesh
  * (src/tsdf.cu:1696-1708,1760-1888). binary = 0 writes the reference's
- * ASCII layout. */
+ * ASCII layout.  The merge runs on the GPU (see vh_mesh_indexed). */
 vh_status vh_save_ply(vh_handle *h, const char *path, int32_t binary);
+/* Full-volume extraction as an indexed mesh, the data of tsdf2mesh /
+ * getVertices / getFaces (src/tsdf.cu:1760-1888, include/tsdf.cuh:631-634):
+ * vertices merged by exact position on the GPU and numbered by first
+ * occurrence over the triangles sorted by their coordinates (so the result
+ * does not depend on GPU scheduling); vertices in metres (3 floats), colours
+ * 3 bytes, faces 3 vertex numbers.  NULL outputs: sizes only. */
+vh_status vh_mesh_indexed(vh_handle *h, float *vertices, uint8_t *colors, int64_t vertex_capacity,
+                          int32_t *faces, int64_t face_capacity, int64_t *num_vertices,
+                          int64_t *num_faces);
 /* GpuTsdfGenerator::render (src/tsdf.cu:1710-1758) draws with OpenGL; there
  * is no graphics stack here, so this returns VH_ERR_UNSUPPORTED. */
 vh_status vh_render(vh_handle *h);

@@ -102,3 +102,49 @@ def test_gpu_tsdf_generator_front_end(scene, tmp_path):
     table.AllocKeys(np.array([[500, 500, 500]], np.int32))
     assert table.heap_counter == 1 and table.erase(np.array([[500, 500, 500]], np.int32)) == 1
     gen.Shutdown()
+
+
+def merged_mesh_reference(xyz, rgb, voxel):
+    """The vertex merge of tsdf2mesh (src/tsdf.cu:1777,1810-1821) over the
+    triangles sorted by (vertex coordinates, colours): exact-position merge,
+    numbering and colour by first occurrence.  numpy restatement."""
+    n = len(xyz)
+    p = xyz.reshape(n, 9).astype(np.float32)
+    p = np.where(p == 0, np.float32(0), p)  # -0 == +0
+    c = (rgb.reshape(n, 3, 3).astype(np.uint32) * np.array([1, 256, 65536], np.uint32)).sum(-1)
+    keys = [c[:, 2], c[:, 1], c[:, 0]] + [p[:, k] for k in range(8, -1, -1)]
+    order = np.lexsort(keys)
+    occ = p[order].reshape(-1, 3)
+    occ_rgb = rgb[order].reshape(-1, 3)
+    view = np.ascontiguousarray(occ).view(np.dtype((np.void, 12))).ravel()
+    _, first, inverse = np.unique(view, return_index=True, return_inverse=True)
+    rank = np.empty(len(first), np.int64)
+    rank[np.argsort(first, kind="stable")] = np.arange(len(first))
+    faces = rank[inverse.ravel()].reshape(-1, 3).astype(np.int32)
+    fo = np.sort(first)
+    verts = occ[fo] * np.float32(voxel)
+    return verts.astype(np.float32), occ_rgb[fo], faces
+
+
+def test_gpu_vertex_merge_matches_reference_rule(scene, tmp_path):
+    vol = volume_for(scene)
+    for f in range(5):
+        vol.integrate(*scene.render(f))
+    v, c, faces = vol.mesh_indexed()
+    vol.extract("all")
+    xyz, rgb = vol.mesh()
+    rv, rc, rf = merged_mesh_reference(xyz, rgb, vol.params.voxel_size)
+    assert len(v) == len(rv) and len(faces) == len(rf) > 0
+    assert np.array_equal(v.view(np.uint32), rv.view(np.uint32))
+    assert np.array_equal(c, rc)
+    assert np.array_equal(faces, rf)
+    # the binary PLY carries exactly these arrays
+    path = tmp_path / "m.ply"
+    vol.save_ply(path, binary=True)
+    pv, pf, nper = read_ply(path)
+    assert np.array_equal(pv.astype(np.float32).view(np.uint32), v.view(np.uint32))
+    assert np.array_equal(pf, faces) and np.all(nper == 3)
+    # and repeated calls give the same bytes (no dependence on GPU scheduling)
+    path2 = tmp_path / "m2.ply"
+    vol.save_ply(path2, binary=True)
+    assert path.read_bytes() == path2.read_bytes()

@@ -34,6 +34,7 @@ ENGINE_SOURCES = [
     ("vh_noalloc.cu", []),
     ("vh_adjoint.cu", []),
     ("vh_batch.cpp", []),
+    ("vh_meshindex.cu", []),
 ]
 ENGINE_HEADERS = ["vh_common.cuh", "vh_device.cuh", "vh_mc_tables.h", "vh_mesh.h", "vh_internal.h"]
 

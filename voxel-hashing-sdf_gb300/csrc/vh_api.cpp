@@ -681,15 +681,46 @@ vh_status vh_copy_mesh(vh_handle *h, float *xyz, uint8_t *rgb, int64_t capacity,
   return VH_OK;
 }
 
-vh_status vh_save_ply(vh_handle *h, const char *path, int32_t binary) {
-  if (!h || !path) return VH_ERR_INVALID_ARG;
+// Full-volume extraction, then the GPU indexing of its triangle soup.
+static vh_status indexed_mesh(vh_handle *h, std::vector<float> &vert, std::vector<uint8_t> &col,
+                              std::vector<int32_t> &faces) {
   vh_status s = vh_extract(h, VH_SCOPE_ALL, nullptr);
   if (s != VH_OK) return s;
   const int64_t n = std::min<int64_t>(h->h_state->tri_count, h->tri_cap);
-  std::vector<float> buf((size_t)n * 12);
-  if (n) VH_CUDA(h, cudaMemcpy(buf.data(), h->d_tris, sizeof(float) * 12 * (size_t)n, cudaMemcpyDeviceToHost));
-  if (!write_ply(path, buf.data(), n, h->p.voxel_size, binary != 0))
+  return index_mesh(h, h->d_tris, n, h->p.voxel_size, vert, col, faces);
+}
+
+vh_status vh_save_ply(vh_handle *h, const char *path, int32_t binary) {
+  if (!h || !path) return VH_ERR_INVALID_ARG;
+  std::vector<float> vert;
+  std::vector<uint8_t> col;
+  std::vector<int32_t> faces;
+  vh_status s = indexed_mesh(h, vert, col, faces);
+  if (s != VH_OK) return s;
+  if (!write_ply(path, vert, col, faces, binary != 0))
     return fail(h, VH_ERR_IO, std::string("cannot write ") + path);
+  return VH_OK;
+}
+
+vh_status vh_mesh_indexed(vh_handle *h, float *vertices, uint8_t *colors, int64_t vertex_capacity,
+                          int32_t *faces, int64_t face_capacity, int64_t *num_vertices,
+                          int64_t *num_faces) {
+  if (!h || vertex_capacity < 0 || face_capacity < 0) return VH_ERR_INVALID_ARG;
+  std::vector<float> vert;
+  std::vector<uint8_t> col;
+  std::vector<int32_t> fc;
+  vh_status s = indexed_mesh(h, vert, col, fc);
+  if (s != VH_OK) return s;
+  const int64_t nv = (int64_t)(vert.size() / 3), nf = (int64_t)(fc.size() / 3);
+  if (num_vertices) *num_vertices = nv;
+  if (num_faces) *num_faces = nf;
+  const bool want = vertices || colors || faces;
+  if (!want) return VH_OK;
+  if (nv > vertex_capacity || nf > face_capacity)
+    return fail(h, VH_ERR_CAPACITY, "mesh larger than the output capacity");
+  if (vertices && nv) std::memcpy(vertices, vert.data(), sizeof(float) * 3 * (size_t)nv);
+  if (colors && nv) std::memcpy(colors, col.data(), 3 * (size_t)nv);
+  if (faces && nf) std::memcpy(faces, fc.data(), sizeof(int32_t) * 3 * (size_t)nf);
   return VH_OK;
 }
 

@@ -4,6 +4,8 @@
 #include "../../include/vhsdf.h"
 #include "vh_common.cuh"
 
+#include <vector>
+
 namespace vh {
 VolumeView handle_view(const vh_handle *h);
 cudaStream_t handle_stream(const vh_handle *h);
@@ -37,6 +39,11 @@ void handle_note_frame(vh_handle *h);
 int64_t handle_frames(const vh_handle *h);
 // Reports sticky device error bits as a status (and records the message).
 vh_status handle_status_of_bits(vh_handle *h, uint32_t bits);
+// Vertices merged by exact position and numbered by first occurrence over
+// the sorted triangles (vh_meshindex.cu); positions scaled to metres.
+vh_status index_mesh(vh_handle *h, const float4 *tris, int64_t n, float voxel,
+                     std::vector<float> &vert, std::vector<uint8_t> &col,
+                     std::vector<int32_t> &faces);
 // Pose-refinement state (buffers, cached graph) created on first use by
 // vh_adjoint.cu and released with the handle.
 struct RefineCtx;

@@ -5,9 +5,10 @@
 
 namespace vh {
 
-// Writes a triangle soup (12 floats per triangle: 3 x {x, y, z, rgb bits},
-// voxel units) as PLY with vertices merged by exact position.
-bool write_ply(const char *path, const float *tris, int64_t n, float voxel_size, bool binary);
+// Writes an indexed mesh (vertices in metres, 3 colour bytes each, 3 vertex
+// numbers per face) as PLY in the reference's layout.
+bool write_ply(const char *path, const std::vector<float> &vert, const std::vector<uint8_t> &col,
+               const std::vector<int32_t> &faces, bool binary);
 
 // Binary volume snapshot: header, keys, sdf, weight, rgb.
 bool write_snapshot(const char *path, float voxel, float trunc, const int32_t *xyz,

@@ -146,6 +146,19 @@ class Volume:
                                          C.byref(n)))
         return xyz, rgb
 
+    def mesh_indexed(self):
+        """Full-volume mesh with vertices merged on the GPU: (vertices [n,3]
+        metres float32, colours [n,3] uint8, faces [m,3] int32)."""
+        nv, nf = C.c_int64(), C.c_int64()
+        self._check(self._L.vh_mesh_indexed(self._h, None, None, 0, None, 0, C.byref(nv),
+                                            C.byref(nf)))
+        v = np.empty((nv.value, 3), np.float32)
+        c = np.empty((nv.value, 3), np.uint8)
+        f = np.empty((nf.value, 3), np.int32)
+        self._check(self._L.vh_mesh_indexed(self._h, v.ctypes.data, c.ctypes.data, nv.value,
+                                            f.ctypes.data, nf.value, C.byref(nv), C.byref(nf)))
+        return v, c, f
+
     def save_ply(self, path, binary=False):
         self._check(self._L.vh_save_ply(self._h, str(path).encode(), int(binary)))
 

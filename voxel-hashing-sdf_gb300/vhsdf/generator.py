@@ -46,13 +46,9 @@ class GpuTsdfGenerator:
 
     def _mesh(self):
         if self._vertices is None:
-            self.volume.extract("all")
-            xyz, rgb = self.volume.mesh()
-            flat = xyz.reshape(-1, 3)
-            uniq, first, inv = np.unique(flat, axis=0, return_index=True, return_inverse=True)
-            vs = self.volume.params.voxel_size
-            self._vertices = (uniq * np.float32(vs), rgb.reshape(-1, 3)[first])
-            self._faces = inv.reshape(-1, 3).astype(np.int32)
+            v, c, f = self.volume.mesh_indexed()
+            self._vertices = (v, c)
+            self._faces = f
         return self._vertices, self._faces
 
     def getVertices(self):
