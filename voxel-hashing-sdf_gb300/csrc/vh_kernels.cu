@@ -423,10 +423,8 @@ __device__ __forceinline__ void load_quad(const VolumeView &V, uint32_t i, int t
 }
 
 // Frame-list entry i whose voxel quad (thread t = threadIdx.x) is loaded in
-// `cur`: threads 0..7 record the block's +x/+y/+z neighbour ids for MC
-// (lane 0: the block itself; lane k: the block at +(k & 1, k >> 1 & 1,
-// k >> 2)), every thread updates and stores its 4 voxels.  Returns the
-// number of voxels this thread updated.
+// `cur`: every thread updates and stores its 4 voxels.  Returns the number
+// of voxels this thread updated.
 __device__ __forceinline__ uint32_t integrate_loaded(const VolumeView &V, const CamParams &C,
                                                      const float (&P)[12],
                                                      const uint2 *__restrict__ pix, uint32_t i,
@@ -434,17 +432,6 @@ __device__ __forceinline__ uint32_t integrate_loaded(const VolumeView &V, const 
   const int t = threadIdx.x;
   const int x0 = (t & 1) * 4, y = (t >> 1) & 7, z = t >> 4;
   const bool live = cur.key < kTombKey && cur.block != kNoBlock;
-  if (t < 8) {
-    uint32_t nbid = kNoBlock;
-    if (live) {
-      int bx, by, bz;
-      unpack_key(cur.key, bx, by, bz);
-      const int nx = bx + (t & 1), ny = by + ((t >> 1) & 1), nz = bz + (t >> 2);
-      nbid = t == 0 ? cur.block
-                    : (key_in_range(nx, ny, nz) ? block_of(V, pack_key(nx, ny, nz)) : kNoBlock);
-    }
-    V.frame_nb[8 * (size_t)i + t] = nbid;
-  }
   if (!live) return 0;
   int bx, by, bz;
   unpack_key(cur.key, bx, by, bz);
@@ -464,7 +451,6 @@ __device__ __forceinline__ uint32_t integrate_loaded(const VolumeView &V, const 
 // per thread.  kPrefetch: the next block's loads are issued before the
 // current block is computed (two blocks in flight per thread, more
 // registers); otherwise one block in flight and higher occupancy.
-// Threads 0..7 also record the block's +x/+y/+z neighbour ids for MC.
 template <bool kPrefetch>
 __global__ void __launch_bounds__(128) k_integrate(VolumeView V, CamParams C,
                                                    const uint2 *__restrict__ pix,
@@ -873,6 +859,24 @@ __global__ void k_mc_begin(VolumeView V) {
   if (threadIdx.x == 0) mc_begin_state(V);
 }
 
+// Frame-list entry i, lane k of its 8 threads: k = 0 writes frame_res[i] =
+// {key, block} and frame_nb[8 i] = the block; k > 0 writes frame_nb[8 i + k]
+// = the block at +(k & 1, k >> 1 & 1, k >> 2) (read by marching cubes).
+__device__ __forceinline__ void resolve_entry(const VolumeView &V, uint32_t i, uint32_t k) {
+  const ulonglong2 sl = __ldg(reinterpret_cast<const ulonglong2 *>(V.slots) + V.frame_list[i]);
+  const uint32_t blk = (uint32_t)(sl.y & 0xFFFFFFFFull);
+  if (k == 0) V.frame_res[i] = make_ulonglong2(sl.x, (unsigned long long)blk);
+  uint32_t nbid = kNoBlock;
+  if (sl.x < kTombKey && blk != kNoBlock) {
+    int bx, by, bz;
+    unpack_key(sl.x, bx, by, bz);
+    const int nx = bx + (int)(k & 1u), ny = by + (int)((k >> 1) & 1u), nz = bz + (int)(k >> 2);
+    nbid = k == 0 ? blk
+                  : (key_in_range(nx, ny, nz) ? block_of(V, pack_key(nx, ny, nz)) : kNoBlock);
+  }
+  V.frame_nb[8 * (size_t)i + k] = nbid;
+}
+
 // ---- batched scenes -----------------------------------------------------------------
 // The stages of one frame for many independent scenes, each stage one launch
 // over the work of all scenes (flattened (scene, item) index, items of a
@@ -964,13 +968,12 @@ __global__ void __launch_bounds__(1024) k_batch_epoch_end(const SceneDesc *__res
 
 __global__ void __launch_bounds__(256) k_batch_resolve(const SceneDesc *__restrict__ d,
                                                        const uint32_t *__restrict__ prefix, int n) {
-  const uint32_t total = __ldg(prefix + n);
-  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+  const uint32_t total8 = 8u * __ldg(prefix + n);
+  for (uint32_t g8 = blockIdx.x * blockDim.x + threadIdx.x; g8 < total8;
+       g8 += gridDim.x * blockDim.x) {
+    const uint32_t g = g8 >> 3;
     const int s = scene_of(prefix, n, g);
-    const VolumeView &V = d[s].V;
-    const uint32_t i = g - __ldg(prefix + s);
-    const ulonglong2 sl = __ldg(reinterpret_cast<const ulonglong2 *>(V.slots) + V.frame_list[i]);
-    V.frame_res[i] = make_ulonglong2(sl.x, sl.y & 0xFFFFFFFFull);
+    resolve_entry(d[s].V, g - __ldg(prefix + s), g8 & 7u);
   }
 }
 
@@ -1122,33 +1125,20 @@ __global__ void __launch_bounds__(256) k_erase_keys(VolumeView V, const int32_t 
   }
 }
 
-// Rebuilds frame_nb for the current block list (needed when the list changed
-// without an integration, e.g. after alloc_keys or erase).  8 threads per entry.
+// Rebuilds frame_res and frame_nb for the current block list (needed when
+// the list changed without a frame, e.g. after alloc_keys or erase).
 __global__ void __launch_bounds__(256) k_frame_nb(VolumeView V) {
   const uint32_t n = min(V.st->frame_count, V.frame_cap);
   const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t i = idx >> 3, k = idx & 7u;
-  if (i >= n) return;
-  const Slot sl = V.slots[V.frame_list[i]];
-  if (k == 0) V.frame_res[i] = make_ulonglong2(sl.key, (unsigned long long)sl.block);
-  uint32_t nbid = kNoBlock;
-  if (sl.key < kTombKey && sl.block != kNoBlock) {
-    int bx, by, bz;
-    unpack_key(sl.key, bx, by, bz);
-    const int nx = bx + (int)(k & 1u), ny = by + (int)((k >> 1) & 1u), nz = bz + (int)(k >> 2);
-    nbid = k == 0 ? sl.block
-                  : (key_in_range(nx, ny, nz) ? block_of(V, pack_key(nx, ny, nz)) : kNoBlock);
-  }
-  V.frame_nb[8 * (size_t)i + k] = nbid;
+  if ((idx >> 3) < n) resolve_entry(V, idx >> 3, idx & 7u);
 }
 
-// frame_res[i] = {key, block} of frame-list entry i (grid-stride).
+// frame_res and frame_nb of every frame-list entry, 8 threads per entry
+// (grid-stride), after allocation and before integration.
 __global__ void __launch_bounds__(256) k_frame_resolve(VolumeView V) {
-  const uint32_t n = min(V.st->frame_count, V.frame_cap);
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const ulonglong2 sl = __ldg(reinterpret_cast<const ulonglong2 *>(V.slots) + V.frame_list[i]);
-    V.frame_res[i] = make_ulonglong2(sl.x, sl.y & 0xFFFFFFFFull);
-  }
+  const uint32_t n8 = 8u * min(V.st->frame_count, V.frame_cap);
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < n8; g += gridDim.x * blockDim.x)
+    resolve_entry(V, g >> 3, g & 7u);
 }
 
 __global__ void k_list_keys(VolumeView V, int32_t *__restrict__ xyz, uint32_t n) {
