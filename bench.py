@@ -472,7 +472,7 @@ def run_engine(args):
     #   k_integrate 12 B per voxel of every listed block read + 12 B per
     #               updated voxel written + 8 B per pixel record
     # DRAM traffic per launch comes from one ncu capture of frames 3-4 of this
-    # stream (60k-block pool): k_mc moved 1.04x and k_integrate 0.87x their
+    # stream (60k-block pool): k_mc moved 0.99x and k_integrate 0.84x their
     # algorithmic bytes; traffic below scales those ratios to this run.
     npx = 640 * 480
     blocks = [s["frame_blocks"] for s in stage]
@@ -502,11 +502,11 @@ def run_engine(args):
                 "h2d_bytes_per_step": 2 * npx + 3 * npx + 64,
                 "d2h_bytes_per_step": 64},
         "roofline": {"bound": "hbm", "achieved": mc_ach, "peak": peak, "unit": "GB/s",
-                     "frac": mc_ach / peak, "traffic": 1.04 * statistics.mean(mc_alg),
+                     "frac": mc_ach / peak, "traffic": 0.99 * statistics.mean(mc_alg),
                      "kernel": "k_mc", "peak_source": peak_src,
                      "algorithmic_bytes": statistics.mean(mc_alg)},
         "roofline_integrate": {"bound": "hbm", "achieved": in_ach, "peak": peak, "unit": "GB/s",
-                               "frac": in_ach / peak, "traffic": 0.87 * statistics.mean(in_alg),
+                               "frac": in_ach / peak, "traffic": 0.84 * statistics.mean(in_alg),
                                "kernel": "k_integrate", "peak_source": peak_src,
                                "algorithmic_bytes": statistics.mean(in_alg)},
         "stages_ms": {k: statistics.mean(s[k] for s in stage)
