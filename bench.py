@@ -332,6 +332,94 @@ def batched_leg(num_scenes, steps, local, small=False):
             "launches_per_step": {"batched": 5, "per_scene_graphs": 5 * num_scenes}}
 
 
+def hbm_stress_leg(num_frames, local, keyframes=16, iterations=20):
+    """HBM stress: a 20x20x4 m floor of 4x4 rooms, num_frames frames of
+    1280x960 u16 depth walked through the rooms at 0.5 m/s, 30 Hz; voxel
+    4 mm, truncation 16 mm, 2^24 hash slots.  Frames are rendered on a host
+    thread while the GPU integrates; the fusion rate is the device time of
+    allocate + integrate per frame (per-stage CUDA events).  Then one
+    full-volume marching cubes, and Gauss-Newton refinement (adjoint) of
+    `keyframes` keyframe poses perturbed by 0.25 deg / 5 mm (keyframe drift;
+    with a 16 mm truncation band a larger error leaves the band)."""
+    import queue
+    import torch
+    from vhsdf import Volume, synth, _native as N
+    w, h = 1280, 960
+    sc = synth.Scene(kind=4, seed=5, num_frames=num_frames, width=w, height=h)
+    vol = Volume(width=w, height=h, fx=sc.fx, fy=sc.fy, cx=sc.cx, cy=sc.cy, min_depth=0.1,
+                 max_depth=4.0, voxel_size=0.004, trunc=0.016, table_log2=24,
+                 pool_blocks=8_000_000, max_frame_blocks=1_500_000, max_triangles=1 << 24,
+                 flags=N.VH_FLAG_PROFILE, device=local)
+    q = queue.Queue(maxsize=16)
+
+    def producer():
+        for f in range(num_frames):
+            q.put(sc.render(f))
+
+    th = threading.Thread(target=producer, daemon=True)
+    t0 = time.perf_counter()
+    th.start()
+    dev_ms = updates = alg = 0.0
+    peak_frame_blocks = 0
+    for f in range(num_frames):
+        d, c, p = q.get()
+        vol.integrate(d, c, p)
+        st = vol.stats()
+        dev_ms += st["ms_allocate"] + st["ms_integrate"]
+        updates += st["voxels_updated"]
+        alg += 12 * 512 * st["frame_blocks"] + 12 * st["voxels_updated"] + 8 * w * h
+        peak_frame_blocks = max(peak_frame_blocks, st["frame_blocks"])
+    wall = time.perf_counter() - t0
+    th.join()
+    st = vol.stats()
+    torch.cuda.synchronize(local)
+    t1 = time.perf_counter()
+    _, ntri = vol.extract("all")
+    t_mc = time.perf_counter() - t1
+    rng = np.random.default_rng(3)
+    picks = np.linspace(0, num_frames - 1, keyframes).astype(int)
+    ms_steps, errs, floor, gap = 0.0, [], [], []
+    for f in picks:
+        d, _, gt = sc.render(int(f))
+        init = perturb_pose(gt, 0.25, 0.005, np.random.default_rng(2000 + int(f)))
+        res, rs = vol.pose_refine(d, init, iterations=iterations, stride=1, method="adjoint")
+        ms_steps += rs["ms_steps"]
+        errs.append(pose_error(res, gt))
+        # the cost's own minimum: refinement started at the ground truth
+        res0, _ = vol.pose_refine(d, gt, iterations=iterations, stride=1, method="adjoint")
+        floor.append(pose_error(res0, gt))
+        gap.append(pose_error(res, res0))
+    peak, _ = peak_hbm()
+    e_mm = np.array([1000 * e[0] for e in errs])
+    e_deg = np.array([e[1] for e in errs])
+    out = {"workload": f"20x20x4 m floor of 4x4 rooms (seed 5), {num_frames} frames 1280x960 u16 "
+                       "depth at 0.5 m/s, 30 Hz; voxel 4 mm, truncation 16 mm, 2^24 hash slots",
+           "frames": num_frames,
+           "fusion_frames_per_s_device": num_frames / (dev_ms / 1000.0),
+           "voxel_updates_per_s": updates / (dev_ms / 1000.0),
+           "fusion_hbm_frac": alg / (dev_ms / 1000.0) / 1e9 / peak,
+           "wall_s_incl_host_render": wall,
+           "blocks_allocated": st["blocks_allocated"],
+           "block_pool_gb": st["blocks_allocated"] * 6144 / 1e9,
+           "table_load": st["blocks_allocated"] / float(1 << 24),
+           "peak_frame_blocks": peak_frame_blocks,
+           "full_volume_mc": {"triangles": int(ntri), "s": t_mc,
+                              "triangles_per_s": ntri / t_mc},
+           "keyframe_refinement": {"keyframes": int(keyframes), "iterations": iterations,
+                                   "pose_steps_per_s": keyframes * iterations / (ms_steps / 1000.0),
+                                   "err_mm_median": float(np.median(e_mm)),
+                                   "err_deg_median": float(np.median(e_deg)),
+                                   "perturbation": "0.25 deg about the camera centre + 5 mm",
+                                   "floor_mm_median": float(np.median([1000 * e[0] for e in floor])),
+                                   "floor_deg_median": float(np.median([e[1] for e in floor])),
+                                   "gap_to_floor_mm_median": float(np.median([1000 * e[0] for e in gap])),
+                                   "gap_to_floor_deg_median": float(np.median([e[1] for e in gap])),
+                                   "within_1mm_0.05deg": int(((e_mm <= 1) & (e_deg <= 0.05)).sum()),
+                                   "within_2mm_0.1deg": int(((e_mm <= 2) & (e_deg <= 0.1)).sum())}}
+    vol.close()
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -544,6 +632,8 @@ def main():
                     help="frames per scene in the batched-scenes leg")
     ap.add_argument("--only-batched", action="store_true",
                     help="run only the batched-scenes leg and print its JSON (profiling)")
+    ap.add_argument("--hbm-stress", type=int, default=0,
+                    help="run only the HBM-stress leg with this many frames (e.g. 2000)")
     ap.add_argument("--only-pose-refinement", action="store_true",
                     help="run only the pose-refinement leg and print its JSON (profiling)")
     ap.add_argument("--no-autotune", action="store_true",
@@ -554,6 +644,10 @@ def main():
     args.warmup = max(args.warmup, 0)
     if args.impl == "reference":
         run_reference(args)
+    elif args.hbm_stress > 0:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps({"hbm_stress": hbm_stress_leg(args.hbm_stress, 0)}), flush=True)
     elif args.only_batched:
         import torch
         torch.cuda.set_device(0)

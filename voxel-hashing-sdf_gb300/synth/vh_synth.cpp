@@ -20,6 +20,10 @@
 //      Catmull-Rom trajectory walked at 0.5 m/s and 30 Hz.
 //   3  room of seeded extent in [1, 8] m with 2..20 objects and a circular
 //      trajectory scaled to the room (one of many uneven batched scenes).
+//   4  20x20x4 m floor of 4x4 rooms (5x5 m): interior walls 0.1 m thick
+//      with a 1.2 m wide, 2.2 m high door in every wall between two rooms,
+//      4 seeded objects per room; the camera walks a closed loop through all
+//      16 rooms and their doors at 0.5 m/s and 30 Hz, 1.5 m high.
 
 #include <cmath>
 #include <cstdint>
@@ -160,6 +164,96 @@ void place_objects(Scene &s, SplitMix &r, int n, V3 lo, V3 hi, const std::vector
   }
 }
 
+// Arc-length parametrised closed Catmull-Rom loop through `ctrl`, sampled
+// densely; returns the samples and their cumulative lengths.
+void dense_loop(const std::vector<V3> &ctrl, int per, std::vector<V3> &dense,
+                std::vector<double> &cum) {
+  const size_t n = ctrl.size();
+  dense.clear();
+  for (size_t k = 0; k < n; ++k)
+    for (int i = 0; i < per; ++i)
+      dense.push_back(catmull(ctrl[(k + n - 1) % n], ctrl[k], ctrl[(k + 1) % n], ctrl[(k + 2) % n],
+                              (double)i / per));
+  cum.assign(dense.size() + 1, 0.0);
+  for (size_t i = 0; i < dense.size(); ++i) {
+    V3 d = dense[(i + 1) % dense.size()] - dense[i];
+    cum[i + 1] = cum[i] + std::sqrt(dot(d, d));
+  }
+}
+
+Prim wall_box(V3 lo, V3 hi, SplitMix &r) {
+  Prim p;
+  p.kind = kBox;
+  p.a = lo;
+  p.b = hi;
+  random_colour(r, p.col);
+  return p;
+}
+
+// Scene kind 4: the multi-room floor (see the kinds above).
+void build_floor(Scene &s, SplitMix &r, int num_frames) {
+  const double half = 10.0, room = 5.0, wall = 0.05, door = 0.6, door_h = 2.2, h = 4.0;
+  s.room_min = {-half, -half, 0};
+  s.room_max = {half, half, h};
+  // interior walls on x = -5, 0, 5 (running along y) and y = -5, 0, 5
+  for (int axis = 0; axis < 2; ++axis)
+    for (int k = 1; k < 4; ++k) {
+      const double c = -half + room * k;
+      double from = -half;
+      for (int j = 0; j < 4; ++j) {
+        const double dc = -half + room * (j + 0.5);  // door centre along the wall
+        const double seg[3][2] = {{from, dc - door}, {dc - door, dc + door}, {dc + door, 0}};
+        for (int q = 0; q < 2; ++q) {
+          const double a0 = seg[q][0], a1 = seg[q][1];
+          const double z0 = q == 0 ? 0.0 : door_h;  // q == 1: lintel above the door
+          V3 lo = axis == 0 ? V3{c - wall, a0, z0} : V3{a0, c - wall, z0};
+          V3 hi = axis == 0 ? V3{c + wall, a1, h} : V3{a1, c + wall, h};
+          s.prims.push_back(wall_box(lo, hi, r));
+        }
+        from = dc + door;
+      }
+      V3 lo = axis == 0 ? V3{c - wall, from, 0} : V3{from, c - wall, 0};
+      V3 hi = axis == 0 ? V3{c + wall, half, h} : V3{half, c + wall, h};
+      s.prims.push_back(wall_box(lo, hi, r));
+    }
+  // closed loop through all 16 rooms (a Hamiltonian cycle of the 4x4 grid),
+  // passing each shared wall through its door
+  const int cyc[16][2] = {{0, 0}, {1, 0}, {2, 0}, {3, 0}, {3, 1}, {2, 1}, {1, 1}, {1, 2},
+                          {2, 2}, {3, 2}, {3, 3}, {2, 3}, {1, 3}, {0, 3}, {0, 2}, {0, 1}};
+  const double cam_z = 1.5;
+  std::vector<V3> ctrl;
+  for (int k = 0; k < 16; ++k) {
+    const int *a = cyc[k], *b = cyc[(k + 1) % 16];
+    V3 ca = {-half + room * (a[0] + 0.5), -half + room * (a[1] + 0.5), cam_z};
+    V3 cb = {-half + room * (b[0] + 0.5), -half + room * (b[1] + 0.5), cam_z};
+    V3 mid = (ca + cb) * 0.5;
+    V3 dir = normalize(cb - ca);
+    ctrl.push_back(ca);
+    ctrl.push_back(mid - dir * 0.8);  // straight through the door
+    ctrl.push_back(mid + dir * 0.8);
+  }
+  std::vector<V3> dense;
+  std::vector<double> cum;
+  dense_loop(ctrl, 100, dense, cum);
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) {
+      V3 lo = {-half + room * i + 0.2, -half + room * j + 0.2, 0};
+      V3 hi = {-half + room * (i + 1) - 0.2, -half + room * (j + 1) - 0.2, h};
+      place_objects(s, r, 4, lo, hi, dense, 0.7);
+    }
+  const double total = cum.back(), ds = 0.5 / 30.0;
+  size_t seg = 0;
+  for (int f = 0; f < num_frames; ++f) {
+    double sarc = std::fmod(f * ds, total);
+    while (!(cum[seg] <= sarc && sarc < cum[seg + 1])) seg = (seg + 1) % dense.size();
+    double a = (sarc - cum[seg]) / (cum[seg + 1] - cum[seg]);
+    V3 p0 = dense[seg], p1 = dense[(seg + 1) % dense.size()];
+    V3 eye = p0 + (p1 - p0) * a;
+    V3 fwd = normalize(normalize(p1 - p0) + V3{0, 0, -0.25});
+    s.poses.push_back(look_at(eye, eye + fwd));
+  }
+}
+
 void build_scene(Scene &s, int kind, uint64_t seed, int num_frames) {
   SplitMix r(seed * 0x2545F4914F6CDD1Dull + 17);
   s.kind = kind;
@@ -182,6 +276,10 @@ void build_scene(Scene &s, int kind, uint64_t seed, int num_frames) {
       double th = 2.0 * M_PI * i / num_frames;
       s.poses.push_back(look_at({1.5 * std::cos(th), 1.5 * std::sin(th), 1.4}, centre));
     }
+    return;
+  }
+  if (kind == 4) {
+    build_floor(s, r, num_frames);
     return;
   }
   double ex = 8, ey = 8, ez = 3;
@@ -381,7 +479,7 @@ extern "C" {
 
 void *vhs_create(int32_t kind, uint64_t seed, int32_t width, int32_t height, float fx, float fy,
                  float cx, float cy, int32_t num_frames) {
-  if (kind < 1 || kind > 3 || width <= 0 || height <= 0 || num_frames <= 0) return nullptr;
+  if (kind < 1 || kind > 4 || width <= 0 || height <= 0 || num_frames <= 0) return nullptr;
   Scene *s = new Scene();
   s->width = width;
   s->height = height;
