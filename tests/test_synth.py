@@ -55,3 +55,20 @@ def test_batched_scene_kinds_vary():
         sizes.add(round(float(hi[0] - lo[0]), 2))
         assert 1.0 <= hi[0] - lo[0] <= 8.0
     assert len(sizes) == 8
+
+
+def test_multi_room_floor():
+    """Kind 4: 20x20x4 m, 4x4 rooms with doors; the camera stays inside the
+    floor at 1.5 m, moves at 0.5 m/s and passes from room to room."""
+    s = synth.Scene(kind=4, seed=5, num_frames=900, width=80, height=60)
+    lo, hi = s.bounds()
+    assert np.allclose(lo, [-10, -10, 0]) and np.allclose(hi, [10, 10, 4])
+    assert s.num_objects >= 54  # 54 wall pieces (segments and lintels) + objects
+    pos = np.array([s.render(f, noise=False)[2][:3, 3] for f in range(0, 900, 30)])
+    assert np.all(np.abs(pos[:, :2]) < 10) and np.allclose(pos[:, 2], 1.5, atol=1e-3)
+    step = np.linalg.norm(np.diff(pos, axis=0), axis=1)
+    assert np.all(step <= 0.5 + 1e-3) and np.all(step > 0.4)  # 30 frames = 0.5 m of arc
+    rooms = {(int((x + 10) // 5), int((y + 10) // 5)) for x, y in pos[:, :2]}
+    assert len(rooms) >= 3
+    d, _, _ = s.render(0)
+    assert (d > 0).mean() > 0.5
