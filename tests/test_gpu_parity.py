@@ -244,3 +244,48 @@ def test_autotune_picks_a_valid_configuration(scene, tmp_path, monkeypatch):
     assert (tmp_path / "tune.txt").read_text().strip()
     vol2 = volume_for(scene)
     assert vol2.autotune(d, c, p) == t  # served from the cache
+
+
+@pytest.mark.parametrize("mc_variant", [0, 1])
+def test_frame_meshes_of_each_mc_variant(scene, mc_variant):
+    """Per-frame marching cubes of each kernel variant equals the oracle's."""
+    vol = volume_for(scene)
+    vol.set_tuning(0, 0, 0, mc_variant)
+    orc = oracle_for(vol, 32)
+    for f in range(4):
+        d, c, p = scene.render(f)
+        vol.process_frame(d, c, p)
+        orc.integrate(d, c, p)
+        gx, gc = vol.mesh()
+        m = orc.marching_cubes("frame")
+        assert len(gx) > 0
+        assert np.array_equal(sort_rows(tri_rows(gx, gc)), sort_rows(tri_rows(m["xyz"], m["rgb"])))
+
+
+def test_mc_on_dense_sign_changes(scene):
+    """Random signs cut about half of every block's edges (up to five
+    triangles per cube, every candidate round full): the mesh still equals
+    the oracle's."""
+    rng = np.random.default_rng(9)
+    n = 40
+    xyz = np.stack([rng.integers(-3, 3, n), rng.integers(-3, 3, n), rng.integers(-3, 3, n)], -1)
+    xyz = np.unique(xyz, axis=0).astype(np.int32)
+    m = len(xyz)
+    sdf = rng.uniform(-1, 1, (m, 512)).astype(np.float32)
+    w = np.ones((m, 512), np.float32)
+    rgb = rng.integers(0, 256, (m, 512, 3)).astype(np.uint8)
+    want = None
+    for variant in (0, 1):
+        vol = volume_for(scene)
+        vol.set_tuning(0, 0, 0, variant)
+        vol.import_blocks(xyz, sdf, w, rgb)
+        vol.extract("all")
+        got = sort_rows(tri_rows(*vol.mesh()))
+        if want is None:
+            orc = oracle_for(vol, 32)
+            orc.import_blocks(xyz, sdf, w, rgb)
+            mm = orc.marching_cubes("all")
+            want = sort_rows(tri_rows(mm["xyz"], mm["rgb"]))
+        assert len(got) > 5000
+        assert np.array_equal(got, want)
+        vol.close()
