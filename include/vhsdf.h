@@ -276,6 +276,21 @@ vh_status vh_set_tuning(vh_handle *h, const vh_tuning *t);
 vh_status vh_autotune(vh_handle *h, const void *depth, int32_t depth_fmt, const uint8_t *rgb,
                       const float *c2w, int32_t mem, vh_tuning *chosen);
 
+/* ---- ray casting (no reference counterpart: the reference draws its mesh
+ * with OpenGL, src/tsdf.cu:1710-1758) ---------------------------------------- */
+
+/* Ray-casts the fused surface from camera pose c2w (row-major 4x4, host)
+ * with the handle's image size and intrinsics: depth[H*W] (camera z in
+ * metres, 0 where the ray misses), and if not NULL normal[H*W*3] (unit TSDF
+ * gradient at the hit, world frame, towards free space) and rgb[H*W*3] (the
+ * nearest voxel's colour).  A ray advances by T through unknown space, by
+ * 0.8 of the sampled distance (at least half a voxel) through known positive
+ * space and by half a voxel through negative space not entered from positive
+ * space; the first + -> - change is interpolated linearly.  Outputs in
+ * `mem`. */
+vh_status vh_raycast(vh_handle *h, const float *c2w, float *depth, float *normal, uint8_t *rgb,
+                     int32_t mem);
+
 /* ---- batches of independent scenes (no reference counterpart: the
  * reference runs one scene per process) ------------------------------------ */
 

@@ -53,6 +53,7 @@ def lib():
         L.vho_mc_copy.argtypes = [P, P, P, P, P, C.c_int64]
         L.vho_sample.argtypes = [P, P, C.c_int64, C.c_double, P, P, P]
         L.vho_pose_terms.argtypes = [P, P, P, C.c_int32, C.c_double, P]
+        L.vho_raycast.argtypes = [P, P, C.c_double, P, P]
         _lib = L
     return _lib
 
@@ -184,6 +185,16 @@ class Oracle:
         self._L.vho_sample(self._h, xyz.ctypes.data, n, float(min_weight), phi.ctypes.data,
                            grad.ctypes.data, valid.ctypes.data)
         return phi, grad, valid.astype(bool)
+
+    def raycast(self, c2w, min_weight=1.0):
+        """FP64 ray cast of the fused surface: (depth [H,W], normals [H,W,3])."""
+        P = np.ascontiguousarray(np.asarray(c2w, np.float64).reshape(4, 4)[:3].reshape(12))
+        h, w = int(self.ip[1]), int(self.ip[0])
+        depth = np.empty((h, w), np.float64)
+        normal = np.empty((h, w, 3), np.float64)
+        self._L.vho_raycast(self._h, P.ctypes.data, float(min_weight), depth.ctypes.data,
+                            normal.ctypes.data)
+        return depth, normal
 
     def pose_terms(self, depth, c2w, stride=1, min_weight=1.0):
         """FP64 Gauss-Newton terms of the SDF residuals of a depth image."""

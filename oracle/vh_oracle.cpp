@@ -530,6 +530,65 @@ void import_blocks(Volume<Acc> &V, const int32_t *xyz, const float *sdf, const f
   }
 }
 
+// Ray casting of the fused surface, the same march as the engine's
+// vh_raycast in FP64 (no reference counterpart: the reference draws its
+// mesh with OpenGL, src/tsdf.cu:1710-1758): step T through unknown space,
+// 0.8 * T * phi (at least half a voxel) through known positive space, half
+// a voxel through negative space not entered from positive space, the first
+// + -> - change interpolated linearly; depth is camera z.
+template <typename Acc>
+void raycast64(const Volume<Acc> &V, const double *P, double min_w, double *depth, double *normal) {
+  const OParams &p = V.p;
+  const double T = p.trunc, vs = p.voxel_size;
+  for (int v = 0; v < p.height; ++v)
+    for (int u = 0; u < p.width; ++u) {
+      const double dx = (u - (double)p.cx) / p.fx, dy = (v - (double)p.cy) / p.fy;
+      const double w[3] = {P[0] * dx + P[1] * dy + P[2], P[4] * dx + P[5] * dy + P[6],
+                           P[8] * dx + P[9] * dy + P[10]};
+      const double len = std::sqrt(dx * dx + dy * dy + 1.0);
+      const double far_step = T / len, min_step = 0.5 * vs / len;
+      const int max_steps = (int)((p.max_depth - p.min_depth) / min_step) + 2;
+      double t = p.min_depth, prev_t = 0, prev_phi = 0, t_hit = 0, g[3] = {0, 0, 0};
+      bool prev_ok = false, hit = false;
+      for (int it = 0; it < max_steps && t <= p.max_depth; ++it) {
+        double phi, gs[3];
+        if (!sample64(V, P[3] + t * w[0], P[7] + t * w[1], P[11] + t * w[2], min_w, &phi, gs)) {
+          prev_ok = false;
+          t += far_step;
+          continue;
+        }
+        if (phi <= 0) {
+          if (prev_ok) {
+            t_hit = prev_t + (t - prev_t) * (prev_phi / (prev_phi - phi));
+            hit = true;
+            std::memcpy(g, gs, sizeof(g));
+            break;
+          }
+          t += min_step;  // negative space not entered from positive space: cross it
+          continue;
+        }
+        prev_ok = true;
+        prev_phi = phi;
+        prev_t = t;
+        std::memcpy(g, gs, sizeof(g));
+        t += std::max(0.8 * phi * T / len, min_step);
+      }
+      const size_t i = (size_t)v * p.width + u;
+      depth[i] = hit ? t_hit : 0.0;
+      double n[3] = {0, 0, 0};
+      if (hit) {
+        double phi, gs[3];
+        if (sample64(V, P[3] + t_hit * w[0], P[7] + t_hit * w[1], P[11] + t_hit * w[2], min_w, &phi,
+                     gs))
+          std::memcpy(g, gs, sizeof(g));
+        const double gn = std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+        if (gn > 0)
+          for (int a = 0; a < 3; ++a) n[a] = g[a] / gn;
+      }
+      for (int a = 0; a < 3; ++a) normal[3 * i + a] = n[a];
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -848,6 +907,14 @@ void vho_sample(void *hp, const double *xyz, int64_t n, double min_w, double *ph
 
 // Normal-equation terms (same layout as the engine) in double precision;
 // P: 12 doubles, row-major camera-to-world 3x4.
+void vho_raycast(void *hp, const double *P, double min_w, double *depth, double *normal) {
+  Handle *h = (Handle *)hp;
+  if (h->precision == 64)
+    raycast64(*h->v64, P, min_w, depth, normal);
+  else
+    raycast64(*h->v32, P, min_w, depth, normal);
+}
+
 void vho_pose_terms(void *hp, const float *depth, const double *P, int32_t stride, double min_w,
                     double *out29) {
   Handle *h = (Handle *)hp;

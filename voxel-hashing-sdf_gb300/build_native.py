@@ -35,6 +35,7 @@ ENGINE_SOURCES = [
     ("vh_adjoint.cu", []),
     ("vh_batch.cpp", []),
     ("vh_meshindex.cu", []),
+    ("vh_raycast.cu", []),
 ]
 ENGINE_HEADERS = ["vh_common.cuh", "vh_device.cuh", "vh_mc_tables.h", "vh_mesh.h", "vh_internal.h"]
 

@@ -35,75 +35,6 @@ namespace {
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr int kTerms = 29;  // 21 (upper H) + 6 (J^T r) + sum r^2 + count
 
-struct Sample {
-  bool ok;
-  float phi, gx, gy, gz;  // sdf (units of T) and d sdf / d world (per metre)
-};
-
-__device__ __forceinline__ uint32_t nb_block(const VolumeView &V, int bx, int by, int bz) {
-  return key_in_range(bx, by, bz) ? block_of(V, pack_key(bx, by, bz)) : kNoBlock;
-}
-
-// Trilinear interpolation of the TSDF at world point (x, y, z) and its
-// gradient.  Fails when any of the 8 corner voxels is unallocated or has a
-// weight below min_w.  The corner blocks are resolved first (one hash lookup,
-// more only where the cell crosses a block face); then all 16 loads are
-// issued together, without a branch between them (a missing block reads
-// block 0, which always exists, and fails the sample afterwards).
-__device__ __forceinline__ Sample sample_tsdf(const VolumeView &V, float inv_voxel, float min_w,
-                                              float x, float y, float z) {
-  Sample s;
-  s.ok = false;
-  const float qx = x * inv_voxel, qy = y * inv_voxel, qz = z * inv_voxel;
-  if (!(fabsf(qx) < 8.0e6f && fabsf(qy) < 8.0e6f && fabsf(qz) < 8.0e6f)) return s;
-  const float fxb = floorf(qx), fyb = floorf(qy), fzb = floorf(qz);
-  const int ix = (int)fxb, iy = (int)fyb, iz = (int)fzb;
-  const float fx = qx - fxb, fy = qy - fyb, fz = qz - fzb;
-  const int bx = ix >> 3, by = iy >> 3, bz = iz >> 3;  // floor division
-  const int lx = ix & 7, ly = iy & 7, lz = iz & 7;
-  const bool cx = lx == 7, cy = ly == 7, cz = lz == 7;  // corners cross into +1 blocks
-  uint32_t b[8];
-  b[0] = nb_block(V, bx, by, bz);
-  b[1] = cx ? nb_block(V, bx + 1, by, bz) : b[0];
-  b[2] = cy ? nb_block(V, bx, by + 1, bz) : b[0];
-  b[3] = cx && cy ? nb_block(V, bx + 1, by + 1, bz) : (cx ? b[1] : b[2]);
-  b[4] = cz ? nb_block(V, bx, by, bz + 1) : b[0];
-  b[5] = cz ? (cx ? nb_block(V, bx + 1, by, bz + 1) : b[4]) : b[1];
-  b[6] = cz ? (cy ? nb_block(V, bx, by + 1, bz + 1) : b[4]) : b[2];
-  b[7] = cz ? ((cx || cy) ? nb_block(V, bx + cx, by + cy, bz + 1) : b[4]) : b[3];
-  float val[8], w[8];
-  bool found = true;
-#pragma unroll
-  for (int c = 0; c < 8; ++c) {
-    const int dx = c & 1, dy = (c >> 1) & 1, dz = c >> 2;
-    found = found && b[c] != kNoBlock;
-    const int li = ((lx + dx) & 7) + 8 * ((ly + dy) & 7) + 64 * ((lz + dz) & 7);
-    const float *base = V.pool + (size_t)(b[c] == kNoBlock ? 0u : b[c]) * kBlockWords;
-    w[c] = __ldg(base + kB3 + li);
-    val[c] = __ldg(base + li);
-  }
-  bool observed = true;
-#pragma unroll
-  for (int c = 0; c < 8; ++c) observed = observed && !(w[c] < min_w);
-  if (!found || !observed) return s;
-  const float gx0 = 1.0f - fx, gy0 = 1.0f - fy, gz0 = 1.0f - fz;
-  // phi = sum_c w_c val_c, w_c = (dx ? fx : 1-fx)(dy ? fy : 1-fy)(dz ? fz : 1-fz)
-  const float c00 = val[0] * gx0 + val[1] * fx, c10 = val[2] * gx0 + val[3] * fx;
-  const float c01 = val[4] * gx0 + val[5] * fx, c11 = val[6] * gx0 + val[7] * fx;
-  const float c0 = c00 * gy0 + c10 * fy, c1 = c01 * gy0 + c11 * fy;
-  s.phi = c0 * gz0 + c1 * fz;
-  const float d00 = val[1] - val[0], d10 = val[3] - val[2];
-  const float d01 = val[5] - val[4], d11 = val[7] - val[6];
-  const float dphidx = (d00 * gy0 + d10 * fy) * gz0 + (d01 * gy0 + d11 * fy) * fz;
-  const float dphidy = (c10 - c00) * gz0 + (c11 - c01) * fz;
-  const float dphidz = c1 - c0;
-  s.gx = dphidx * inv_voxel;
-  s.gy = dphidy * inv_voxel;
-  s.gz = dphidz * inv_voxel;
-  s.ok = true;
-  return s;
-}
-
 __global__ void __launch_bounds__(256) k_sdf_sample(VolumeView V, float inv_voxel, float min_w,
                                                     const float *__restrict__ xyz, uint32_t n,
                                                     float *__restrict__ phi,

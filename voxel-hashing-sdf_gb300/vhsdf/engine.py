@@ -146,6 +146,18 @@ class Volume:
                                          C.byref(n)))
         return xyz, rgb
 
+    def raycast(self, c2w):
+        """Ray-cast (depth [H,W] metres (0 = miss), normals [H,W,3] world
+        frame, colours [H,W,3]) of the fused surface from pose c2w."""
+        p = self.params
+        pose = np.ascontiguousarray(np.asarray(c2w, np.float32).reshape(16))
+        depth = np.empty((p.height, p.width), np.float32)
+        normal = np.empty((p.height, p.width, 3), np.float32)
+        rgb = np.empty((p.height, p.width, 3), np.uint8)
+        self._check(self._L.vh_raycast(self._h, pose.ctypes.data, depth.ctypes.data,
+                                       normal.ctypes.data, rgb.ctypes.data, N.VH_MEM_HOST))
+        return depth, normal, rgb
+
     def mesh_indexed(self):
         """Full-volume mesh with vertices merged on the GPU: (vertices [n,3]
         metres float32, colours [n,3] uint8, faces [m,3] int32)."""
