@@ -276,6 +276,25 @@ vh_status vh_set_tuning(vh_handle *h, const vh_tuning *t);
 vh_status vh_autotune(vh_handle *h, const void *depth, int32_t depth_fmt, const uint8_t *rgb,
                       const float *c2w, int32_t mem, vh_tuning *chosen);
 
+/* ---- out-of-core blocks (the reference streams 128^3-voxel chunks between
+ * host and device every frame, src/tsdf.cu:118-596; here the volume stays
+ * resident and streaming is explicit) ---------------------------------------- */
+
+/* Moves every GPU block whose centre is farther than `radius` metres from
+ * centre[3] (world, host) into the handle's host store (pool layout, bit-
+ * identical), freeing its pool block; *moved receives the count (may be
+ * NULL).  Blocks moved out are not seen by integration, extraction, export
+ * or ray casting until they are moved back in; integrating a frame that
+ * reaches them first starts them afresh (a later move-out then replaces the
+ * stored copy). */
+vh_status vh_stream_out(vh_handle *h, const float *centre, float radius, int64_t *moved);
+/* Moves every stored block whose centre is within `radius` of centre[3]
+ * back into the volume (radius = INFINITY: all of them).  The keys join the
+ * current block list, as vh_alloc_keys does. */
+vh_status vh_stream_in(vh_handle *h, const float *centre, float radius, int64_t *moved);
+/* Blocks currently in the host store. */
+int64_t vh_host_blocks(const vh_handle *h);
+
 /* ---- ray casting (no reference counterpart: the reference draws its mesh
  * with OpenGL, src/tsdf.cu:1710-1758) ---------------------------------------- */
 

@@ -60,6 +60,7 @@ struct vh_handle {
   void *d_work = nullptr;  // workspace of the gradient calls
   size_t work_bytes = 0;
   RefineCtx *refine = nullptr;  // device state of pose refinement (vh_adjoint.cu)
+  StreamStore *stream_store = nullptr;  // streamed-out blocks (vh_stream.cu)
   int64_t frames = 0;
   bool nb_valid = false;  // frame_nb matches the current block list
   std::string last_error;
@@ -272,6 +273,8 @@ void free_all(vh_handle *h) {
   drop_graphs(h);
   refine_ctx_free(h->refine);
   h->refine = nullptr;
+  stream_store_free(h->stream_store);
+  h->stream_store = nullptr;
   cudaFree(h->V.slots);
   cudaFree(h->V.pool);
   cudaFree(h->V.block_keys);
@@ -375,6 +378,9 @@ vh_status handle_stage_depth(vh_handle *h, const void *depth, int fmt, int mem, 
   return VH_OK;
 }
 RefineCtx *&handle_refine(vh_handle *h) { return h->refine; }
+StreamStore *&handle_stream_store(vh_handle *h) { return h->stream_store; }
+const DevState &handle_state(const vh_handle *h) { return *h->h_state; }
+void handle_invalidate_nb(vh_handle *h) { h->nb_valid = false; }
 
 FrameBuffers handle_frame_buffers(const vh_handle *h) {
   return FrameBuffers{h->d_depth, h->d_rgb, h->d_pix, h->d_tris, h->tri_cap,

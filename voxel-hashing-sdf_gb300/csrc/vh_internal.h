@@ -44,6 +44,14 @@ vh_status handle_status_of_bits(vh_handle *h, uint32_t bits);
 vh_status index_mesh(vh_handle *h, const float4 *tris, int64_t n, float voxel,
                      std::vector<float> &vert, std::vector<uint8_t> &col,
                      std::vector<int32_t> &faces);
+// Host store of streamed-out blocks (vh_stream.cu), released with the handle.
+struct StreamStore;
+StreamStore *&handle_stream_store(vh_handle *h);
+void stream_store_free(StreamStore *s);
+// The device state as of the last synchronising call.
+const DevState &handle_state(const vh_handle *h);
+// The frame list's neighbour table no longer matches the hash table.
+void handle_invalidate_nb(vh_handle *h);
 // Pose-refinement state (buffers, cached graph) created on first use by
 // vh_adjoint.cu and released with the handle.
 struct RefineCtx;

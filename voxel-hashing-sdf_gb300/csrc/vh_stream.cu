@@ -1,0 +1,297 @@
+// vh_stream.cu - out-of-core blocks: moving parts of the volume between HBM
+// and a host store.
+//
+// The reference keeps its volume on the host in 128^3-voxel chunks and every
+// frame streams the chunks near the camera in and everything back out
+// (src/tsdf.cu:118-596, GpuTsdfGenerator::processFrame :1484-1598).  Here
+// the volume stays resident and streaming is explicit and selective: blocks
+// whose centre is farther than a radius from a point (typically the camera)
+// leave HBM for a host store in the handle, and come back when the caller
+// asks for a region.  Blocks travel in their pool layout (sdf | weight |
+// rgba, 6 KiB), so a block that goes out and comes back is bit-identical.
+//   out: one kernel lists the far blocks (key, pool id) of the pool; the
+//        blocks are gathered into a contiguous buffer, copied to the host
+//        store, and erased (slot tombstoned, block zeroed and freed);
+//   in:  the store's blocks within the radius are copied up, their keys
+//        inserted (joining the current block list, as vh_alloc_keys does)
+//        and their voxels written into the new pool blocks.
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <unordered_map>
+#include <vector>
+
+#include "vh_device.cuh"
+#include "vh_internal.h"
+
+namespace vh {
+
+struct StreamStore {
+  std::unordered_map<unsigned long long, size_t> index;  // key -> entry
+  std::vector<unsigned long long> keys;                   // per entry (kEmptyKey: free)
+  std::vector<float> data;                                // kBlockWords per entry
+  std::vector<size_t> free_entries;
+};
+
+void stream_store_free(StreamStore *s) { delete s; }
+
+namespace {
+
+constexpr uint32_t kChunk = 1u << 16;  // blocks per transfer (384 MiB)
+
+// Far blocks of the pool: key and pool id of every live block whose centre
+// is farther than sqrt(r2) from (cx, cy, cz).
+__global__ void __launch_bounds__(256) k_select_far(VolumeView V, float voxel, float cx, float cy,
+                                                    float cz, float r2,
+                                                    uint32_t *__restrict__ count,
+                                                    unsigned long long *__restrict__ keys,
+                                                    uint32_t *__restrict__ ids, uint32_t cap) {
+  const uint32_t top = min(V.st->pool_top, V.pool_cap);
+  for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < top; b += gridDim.x * blockDim.x) {
+    const unsigned long long key = V.block_keys[b];
+    if (key >= kTombKey) continue;
+    int bx, by, bz;
+    unpack_key(key, bx, by, bz);
+    const float x = ((float)(bx * kB) + 3.5f) * voxel - cx;
+    const float y = ((float)(by * kB) + 3.5f) * voxel - cy;
+    const float z = ((float)(bz * kB) + 3.5f) * voxel - cz;
+    if (x * x + y * y + z * z <= r2) continue;
+    const uint32_t slot = atomicAdd(count, 1u);
+    if (slot < cap) {
+      keys[slot] = key;
+      ids[slot] = b;
+    }
+  }
+}
+
+// One CTA per block: out[i] = pool block ids[i] (16-byte copies).
+__global__ void __launch_bounds__(128) k_gather_blocks(const float *__restrict__ pool,
+                                                       const uint32_t *__restrict__ ids,
+                                                       uint32_t n, float *__restrict__ out) {
+  const uint32_t i = blockIdx.x;
+  if (i >= n) return;
+  const float4 *src = reinterpret_cast<const float4 *>(pool + (size_t)ids[i] * kBlockWords);
+  float4 *dst = reinterpret_cast<float4 *>(out + (size_t)i * kBlockWords);
+  for (int k = threadIdx.x; k < kBlockWords / 4; k += blockDim.x) dst[k] = src[k];
+}
+
+__global__ void k_keys_to_xyz(const unsigned long long *__restrict__ keys, uint32_t n,
+                              int32_t *__restrict__ xyz) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int x, y, z;
+  unpack_key(keys[i], x, y, z);
+  xyz[3 * i] = x;
+  xyz[3 * i + 1] = y;
+  xyz[3 * i + 2] = z;
+}
+
+// One CTA per block: writes data[i] (pool layout) into the block of key xyz[i].
+__global__ void __launch_bounds__(128) k_scatter_raw(VolumeView V, const int32_t *__restrict__ xyz,
+                                                     const float *__restrict__ data, uint32_t n) {
+  const uint32_t i = blockIdx.x;
+  if (i >= n) return;
+  const int x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+  if (!key_in_range(x, y, z)) return;
+  const uint32_t b = block_of(V, pack_key(x, y, z));
+  if (b == kNoBlock) return;  // the insert failed (pool or table full): reported by the state
+  const float4 *src = reinterpret_cast<const float4 *>(data + (size_t)i * kBlockWords);
+  float4 *dst = reinterpret_cast<float4 *>(V.pool + (size_t)b * kBlockWords);
+  for (int k = threadIdx.x; k < kBlockWords / 4; k += blockDim.x) dst[k] = src[k];
+}
+
+// Device scratch freed on scope exit.
+struct Scratch {
+  std::vector<void *> ptrs;
+  ~Scratch() {
+    for (void *p : ptrs) cudaFree(p);
+  }
+  template <typename T>
+  bool alloc(T **p, size_t count) {
+    void *q = nullptr;
+    if (cudaMalloc(&q, sizeof(T) * (count ? count : 1)) != cudaSuccess) return false;
+    ptrs.push_back(q);
+    *p = static_cast<T *>(q);
+    return true;
+  }
+};
+
+StreamStore &store_of(vh_handle *h) {
+  StreamStore *&s = handle_stream_store(h);
+  if (!s) s = new StreamStore();
+  return *s;
+}
+
+bool far_enough(unsigned long long key, float voxel, const float c[3], double r2) {
+  int bx, by, bz;
+  unpack_key(key, bx, by, bz);
+  const double x = ((double)bx * kB + 3.5) * voxel - c[0];
+  const double y = ((double)by * kB + 3.5) * voxel - c[1];
+  const double z = ((double)bz * kB + 3.5) * voxel - c[2];
+  return x * x + y * y + z * z > r2;
+}
+
+}  // namespace
+}  // namespace vh
+
+using namespace vh;
+
+extern "C" vh_status vh_stream_out(vh_handle *h, const float *centre, float radius,
+                                   int64_t *moved) {
+  if (moved) *moved = 0;
+  if (!h || !centre || !(radius >= 0.0f)) return VH_ERR_INVALID_ARG;
+  for (int a = 0; a < 3; ++a)
+    if (!std::isfinite(centre[a])) return VH_ERR_NOT_FINITE;
+  const VolumeView V = handle_view(h);
+  const CamParams C = handle_cam(h);
+  const cudaStream_t st = handle_stream(h);
+  launch_epoch_end(V, st);
+  vh_status s = handle_sync(h);
+  if (s != VH_OK) return s;
+  const uint32_t top = handle_state(h).pool_top;
+  if (!top) return VH_OK;
+  Scratch sc;
+  uint32_t *d_count, *d_ids;
+  unsigned long long *d_keys;
+  if (!sc.alloc(&d_count, 1) || !sc.alloc(&d_keys, top) || !sc.alloc(&d_ids, top))
+    return handle_fail(h, VH_ERR_CUDA, "stream out: device allocation failed");
+  uint32_t n = 0;
+  const float r2 = radius * radius;
+  if (cudaMemsetAsync(d_count, 0, sizeof(uint32_t), st) != cudaSuccess)
+    return handle_fail(h, VH_ERR_CUDA, "stream out failed");
+  k_select_far<<<std::min<uint32_t>((top + 255) / 256, 4096), 256, 0, st>>>(
+      V, C.voxel, centre[0], centre[1], centre[2], std::isfinite(r2) ? r2 : 3.0e38f, d_count,
+      d_keys, d_ids, top);
+  if (cudaGetLastError() != cudaSuccess ||
+      cudaMemcpyAsync(&n, d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return handle_fail(h, VH_ERR_CUDA, "stream out: selection failed");
+  n = std::min(n, top);
+  if (!n) return VH_OK;
+  StreamStore &S = store_of(h);
+  float *d_data;
+  int32_t *d_xyz;
+  if (!sc.alloc(&d_data, (size_t)std::min(n, kChunk) * kBlockWords) || !sc.alloc(&d_xyz, 3 * (size_t)n))
+    return handle_fail(h, VH_ERR_CUDA, "stream out: device allocation failed");
+  std::vector<unsigned long long> keys(n);
+  if (cudaMemcpyAsync(keys.data(), d_keys, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost,
+                      st) != cudaSuccess)
+    return handle_fail(h, VH_ERR_CUDA, "stream out: key copy failed");
+  for (uint32_t c0 = 0; c0 < n; c0 += kChunk) {
+    const uint32_t cnt = std::min(kChunk, n - c0);
+    k_gather_blocks<<<cnt, 128, 0, st>>>(V.pool, d_ids + c0, cnt, d_data);
+    const size_t base = S.data.size();
+    // the host entries of this chunk go contiguously at the end
+    S.data.resize(base + (size_t)cnt * kBlockWords);
+    S.keys.resize(S.data.size() / kBlockWords, kEmptyKey);
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpyAsync(S.data.data() + base, d_data, sizeof(float) * kBlockWords * cnt,
+                        cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return handle_fail(h, VH_ERR_CUDA, "stream out: block copy failed");
+    for (uint32_t j = 0; j < cnt; ++j) {
+      const unsigned long long k = keys[c0 + j];
+      const size_t e = base / kBlockWords + j;
+      S.keys[e] = k;
+      auto it = S.index.find(k);
+      if (it != S.index.end()) {  // a stale copy of the same key: replace it
+        S.keys[it->second] = kEmptyKey;
+        S.free_entries.push_back(it->second);
+        it->second = e;
+      } else {
+        S.index.emplace(k, e);
+      }
+    }
+  }
+  k_keys_to_xyz<<<(n + 255) / 256, 256, 0, st>>>(d_keys, n, d_xyz);
+  int64_t erased = 0;
+  if (cudaGetLastError() != cudaSuccess) return handle_fail(h, VH_ERR_CUDA, "stream out failed");
+  s = vh_erase_keys(h, d_xyz, n, &erased, VH_MEM_DEVICE);
+  if (s != VH_OK) return s;
+  if (moved) *moved = erased;
+  return VH_OK;
+}
+
+extern "C" vh_status vh_stream_in(vh_handle *h, const float *centre, float radius, int64_t *moved) {
+  if (moved) *moved = 0;
+  if (!h || !centre || !(radius >= 0.0f)) return VH_ERR_INVALID_ARG;
+  for (int a = 0; a < 3; ++a)
+    if (!std::isfinite(centre[a])) return VH_ERR_NOT_FINITE;
+  StreamStore *Sp = handle_stream_store(h);
+  if (!Sp || Sp->index.empty()) return VH_OK;
+  StreamStore &S = *Sp;
+  const CamParams C = handle_cam(h);
+  const double r2 = std::isfinite(radius) ? (double)radius * radius : 1e300;
+  std::vector<size_t> pick;
+  for (const auto &kv : S.index)
+    if (!far_enough(kv.first, C.voxel, centre, r2)) pick.push_back(kv.second);
+  if (pick.empty()) return VH_OK;
+  std::sort(pick.begin(), pick.end());
+  const VolumeView V = handle_view(h);
+  const cudaStream_t st = handle_stream(h);
+  Scratch sc;
+  const uint32_t total = (uint32_t)pick.size();
+  int32_t *d_xyz;
+  float *d_data;
+  if (!sc.alloc(&d_xyz, 3 * (size_t)std::min(total, kChunk)) ||
+      !sc.alloc(&d_data, (size_t)std::min(total, kChunk) * kBlockWords))
+    return handle_fail(h, VH_ERR_CUDA, "stream in: device allocation failed");
+  std::vector<int32_t> xyz;
+  std::vector<float> buf;
+  int64_t done = 0;
+  for (uint32_t c0 = 0; c0 < total; c0 += kChunk) {
+    const uint32_t cnt = std::min(kChunk, total - c0);
+    xyz.resize(3 * (size_t)cnt);
+    buf.resize((size_t)cnt * kBlockWords);
+    for (uint32_t j = 0; j < cnt; ++j) {
+      const size_t e = pick[c0 + j];
+      int x, y, z;
+      unpack_key(S.keys[e], x, y, z);
+      xyz[3 * j] = x;
+      xyz[3 * j + 1] = y;
+      xyz[3 * j + 2] = z;
+      std::memcpy(&buf[(size_t)j * kBlockWords], &S.data[e * kBlockWords], sizeof(float) * kBlockWords);
+    }
+    if (cudaMemcpyAsync(d_xyz, xyz.data(), sizeof(int32_t) * 3 * cnt, cudaMemcpyHostToDevice, st) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(d_data, buf.data(), sizeof(float) * kBlockWords * cnt,
+                        cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return handle_fail(h, VH_ERR_CUDA, "stream in: copy failed");
+    launch_epoch_end(V, st);
+    launch_alloc_keys(V, d_xyz, cnt, st);
+    launch_epoch_end(V, st);
+    k_scatter_raw<<<cnt, 128, 0, st>>>(V, d_xyz, d_data, cnt);
+    if (cudaGetLastError() != cudaSuccess) return handle_fail(h, VH_ERR_CUDA, "stream in failed");
+    handle_invalidate_nb(h);
+    vh_status s = handle_sync(h);  // pool / table full surface here; the store keeps the blocks
+    if (s != VH_OK) return s;
+    for (uint32_t j = 0; j < cnt; ++j) {
+      const size_t e = pick[c0 + j];
+      S.index.erase(S.keys[e]);
+      S.keys[e] = kEmptyKey;
+      S.free_entries.push_back(e);
+    }
+    done += cnt;
+  }
+  // compact the store when most of it is free
+  if (S.free_entries.size() > 1024 && S.free_entries.size() * 2 > S.keys.size()) {
+    StreamStore T;
+    for (const auto &kv : S.index) {
+      const size_t e = T.keys.size();
+      T.keys.push_back(kv.first);
+      T.data.insert(T.data.end(), S.data.begin() + kv.second * kBlockWords,
+                    S.data.begin() + (kv.second + 1) * kBlockWords);
+      T.index.emplace(kv.first, e);
+    }
+    S = std::move(T);
+  }
+  if (moved) *moved = done;
+  return VH_OK;
+}
+
+extern "C" int64_t vh_host_blocks(const vh_handle *h) {
+  if (!h) return 0;
+  StreamStore *s = handle_stream_store(const_cast<vh_handle *>(h));
+  return s ? (int64_t)s->index.size() : 0;
+}

@@ -146,6 +146,24 @@ class Volume:
                                          C.byref(n)))
         return xyz, rgb
 
+    def stream_out(self, centre, radius):
+        """Moves blocks farther than `radius` from `centre` to the host store;
+        returns how many moved."""
+        c = np.ascontiguousarray(np.asarray(centre, np.float32).reshape(3))
+        n = C.c_int64()
+        self._check(self._L.vh_stream_out(self._h, c.ctypes.data, float(radius), C.byref(n)))
+        return n.value
+
+    def stream_in(self, centre, radius=float("inf")):
+        """Moves stored blocks within `radius` of `centre` back; returns how many."""
+        c = np.ascontiguousarray(np.asarray(centre, np.float32).reshape(3))
+        n = C.c_int64()
+        self._check(self._L.vh_stream_in(self._h, c.ctypes.data, float(radius), C.byref(n)))
+        return n.value
+
+    def host_blocks(self):
+        return int(self._L.vh_host_blocks(self._h))
+
     def raycast(self, c2w):
         """Ray-cast (depth [H,W] metres (0 = miss), normals [H,W,3] world
         frame, colours [H,W,3]) of the fused surface from pose c2w."""
