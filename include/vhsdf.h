@@ -62,6 +62,9 @@ typedef enum vh_scope {
 #define VH_FLAG_SYNC 0x1u      /* wait for device work inside every call     */
 #define VH_FLAG_NO_GRAPH 0x2u  /* launch kernels directly, no CUDA graphs    */
 #define VH_FLAG_PROFILE 0x4u   /* record per-stage CUDA events               */
+#define VH_FLAG_DEPTH_FILTER 0x8u /* bilateral pre-filter of every depth    */
+                                  /* frame (not the reference's rule; see    */
+                                  /* vh_filter_depth)                        */
 
 /*
  * Volume and camera parameters.  Replaces the arguments of
@@ -275,6 +278,14 @@ vh_status vh_set_tuning(vh_handle *h, const vh_tuning *t);
  * file, in that file, keyed by GPU, image size and volume parameters. */
 vh_status vh_autotune(vh_handle *h, const void *depth, int32_t depth_fmt, const uint8_t *rgb,
                       const float *c2w, int32_t mem, vh_tuning *chosen);
+
+/* The depth pre-filter of VH_FLAG_DEPTH_FILTER applied to one image: an
+ * edge-preserving bilateral filter over 5x5 pixels (spatial sigma 2 px,
+ * range sigma 5 mm + 1.5e-3 d^2 x 3, neighbours beyond 3 range sigmas or
+ * invalid left out); out[H*W] float metres, 0 where the input is invalid.
+ * depth and out in `mem`. */
+vh_status vh_filter_depth(vh_handle *h, const void *depth, int32_t depth_fmt, float *out,
+                          int32_t mem);
 
 /* ---- out-of-core blocks (the reference streams 128^3-voxel chunks between
  * host and device every frame, src/tsdf.cu:118-596; here the volume stays

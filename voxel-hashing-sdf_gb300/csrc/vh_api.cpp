@@ -44,6 +44,7 @@ struct vh_handle {
   VolumeView V{};
   CamParams C{};
   void *d_depth = nullptr;
+  float *d_depth_f = nullptr;  // filtered depth (VH_FLAG_DEPTH_FILTER)
   uint8_t *d_rgb = nullptr;
   float *d_pose = nullptr;
   uint2 *d_pix = nullptr;
@@ -176,7 +177,13 @@ void enqueue_frame(vh_handle *h, int fmt, bool with_mc, bool events, bool captur
   cudaStream_t s = h->stream;
   if (events) stage_event(h->ev[0], s, capturing);
   launch_frame_begin(h->V, s);
-  launch_allocate(h->V, h->C, h->d_depth, fmt, h->d_rgb, h->d_pose, h->d_pix, s);
+  const void *depth = h->d_depth;
+  if (h->p.flags & VH_FLAG_DEPTH_FILTER) {
+    launch_depth_filter(h->C, h->d_depth, fmt, h->d_depth_f, s);
+    depth = h->d_depth_f;
+    fmt = VH_DEPTH_F32_M;
+  }
+  launch_allocate(h->V, h->C, depth, fmt, h->d_rgb, h->d_pose, h->d_pix, s);
   launch_epoch_end(h->V, s);
   launch_frame_resolve(h->V, h->sm_count * 2, s);
   if (events) stage_event(h->ev[1], s, capturing);
@@ -284,6 +291,7 @@ void free_all(vh_handle *h) {
   cudaFree(h->V.frame_res);
   cudaFree(h->V.st);
   cudaFree(h->d_depth);
+  cudaFree(h->d_depth_f);
   cudaFree(h->d_rgb);
   cudaFree(h->d_pose);
   cudaFree(h->d_pix);
@@ -480,7 +488,8 @@ vh_status vh_params_validate(const vh_params *p) {
   if (p->max_frame_blocks < 1 || p->max_frame_blocks > 0x7FFFFFFF) return VH_ERR_INVALID_ARG;
   if (p->max_triangles < 0 || p->max_triangles > 0x7FFFFFFF / 3) return VH_ERR_INVALID_ARG;
   if (p->device < 0) return VH_ERR_INVALID_ARG;
-  if (p->flags & ~(uint32_t)(VH_FLAG_SYNC | VH_FLAG_NO_GRAPH | VH_FLAG_PROFILE))
+  if (p->flags &
+      ~(uint32_t)(VH_FLAG_SYNC | VH_FLAG_NO_GRAPH | VH_FLAG_PROFILE | VH_FLAG_DEPTH_FILTER))
     return VH_ERR_INVALID_ARG;
   return VH_OK;
 }
@@ -522,6 +531,7 @@ vh_status vh_create(const vh_params *p, vh_handle **out) {
             cudaMalloc(&h->V.frame_res, sizeof(ulonglong2) * p->max_frame_blocks) == cudaSuccess &&
             cudaMalloc(&h->V.st, sizeof(DevState)) == cudaSuccess &&
             cudaMalloc(&h->d_depth, 4 * npx) == cudaSuccess &&
+            cudaMalloc(&h->d_depth_f, 4 * npx) == cudaSuccess &&
             cudaMalloc(&h->d_rgb, 3 * npx) == cudaSuccess &&
             cudaMalloc(&h->d_pose, 16 * sizeof(float)) == cudaSuccess &&
             cudaMalloc(&h->d_pix, sizeof(uint2) * npx) == cudaSuccess &&
@@ -728,6 +738,21 @@ vh_status vh_mesh_indexed(vh_handle *h, float *vertices, uint8_t *colors, int64_
   if (colors && nv) std::memcpy(colors, col.data(), 3 * (size_t)nv);
   if (faces && nf) std::memcpy(faces, fc.data(), sizeof(int32_t) * 3 * (size_t)nf);
   return VH_OK;
+}
+
+vh_status vh_filter_depth(vh_handle *h, const void *depth, int32_t depth_fmt, float *out,
+                          int32_t mem) {
+  if (!h || !out) return VH_ERR_INVALID_ARG;
+  const void *d = nullptr;
+  vh_status s = handle_stage_depth(h, depth, depth_fmt, mem, &d);
+  if (s != VH_OK) return s;
+  float *dst = mem == VH_MEM_DEVICE ? out : h->d_depth_f;
+  launch_depth_filter(h->C, d, depth_fmt, dst, h->stream);
+  VH_CUDA(h, cudaGetLastError());
+  if (mem == VH_MEM_HOST)
+    VH_CUDA(h, cudaMemcpyAsync(out, dst, sizeof(float) * (size_t)h->p.width * h->p.height,
+                               cudaMemcpyDeviceToHost, h->stream));
+  return sync_and_check(h);
 }
 
 vh_status vh_render(vh_handle *h) {

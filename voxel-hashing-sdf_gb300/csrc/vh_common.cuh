@@ -167,6 +167,10 @@ void launch_list_keys(const VolumeView &V, int32_t *xyz, uint32_t n, cudaStream_
 void launch_scatter_blocks(const VolumeView &V, const int32_t *xyz, const float *sdf,
                            const float *w, const uint8_t *rgb, uint32_t n, cudaStream_t s);
 
+// Bilateral pre-filter of one depth image into float metres (vh_filter.cu).
+void launch_depth_filter(const CamParams &C, const void *depth, int fmt, float *out,
+                         cudaStream_t s);
+
 // Batched stages: one launch covers the work of every active scene.
 // active[i] != 0: scene i has a frame this step.  px_start: first global
 // pixel of each scene (multiples of kBatchPixelThreads; n + 1 entries).  prefix: per-scene

@@ -33,6 +33,7 @@ VH_SCOPE_ALL = 1
 VH_FLAG_SYNC = 0x1
 VH_FLAG_NO_GRAPH = 0x2
 VH_FLAG_PROFILE = 0x4
+VH_FLAG_DEPTH_FILTER = 0x8
 VH_REFINE_ADJOINT = 0
 VH_REFINE_FD = 1
 BLOCK_EDGE = 8
@@ -121,6 +122,7 @@ SIGNATURES = {
     "vh_pose_refine": (I32, [P, P, I32, I32, P, I32, I32, I32, P, C.POINTER(VhRefineStats)]),
     "vh_integrate_vjp": (I32, [P, P, I32, P, P, P, P, I32]),
     "vh_raycast": (I32, [P, P, P, P, P, I32]),
+    "vh_filter_depth": (I32, [P, P, I32, P, I32]),
     "vh_stream_out": (I32, [P, P, C.c_float, PI64]),
     "vh_stream_in": (I32, [P, P, C.c_float, PI64]),
     "vh_host_blocks": (I64, [P]),

@@ -164,6 +164,15 @@ class Volume:
     def host_blocks(self):
         return int(self._L.vh_host_blocks(self._h))
 
+    def filter_depth(self, depth, depth_format=None):
+        """The VH_FLAG_DEPTH_FILTER pre-filter of one depth image (float metres)."""
+        d = _Arg(depth)
+        p = self.params
+        out = np.empty((p.height, p.width), np.float32)
+        self._check(self._L.vh_filter_depth(self._h, d.ptr, _depth_fmt(d.dtype, depth_format),
+                                            out.ctypes.data, N.VH_MEM_HOST))
+        return out
+
     def raycast(self, c2w):
         """Ray-cast (depth [H,W] metres (0 = miss), normals [H,W,3] world
         frame, colours [H,W,3]) of the fused surface from pose c2w."""
