@@ -305,6 +305,11 @@ vh_status vh_stream_out(vh_handle *h, const float *centre, float radius, int64_t
 vh_status vh_stream_in(vh_handle *h, const float *centre, float radius, int64_t *moved);
 /* Blocks currently in the host store. */
 int64_t vh_host_blocks(const vh_handle *h);
+/* Rebuilds the hash table from the pool's live blocks, dropping the
+ * tombstones that erased keys leave (inserts do not reuse them); the
+ * current block list is emptied.  vh_stream_out calls it once tombstones
+ * fill an eighth of the table. */
+vh_status vh_compact_table(vh_handle *h);
 
 /* ---- ray casting (no reference counterpart: the reference draws its mesh
  * with OpenGL, src/tsdf.cu:1710-1758) ---------------------------------------- */
@@ -330,8 +335,10 @@ typedef struct vh_batch vh_batch;
 
 /* n independent scenes (1..VH_BATCH_MAX_SCENES) on params[0].device; scene i
  * has params[i]: image size, intrinsics, voxel size, truncation, table and
- * pool sizes may all differ.  Every scene is a full handle
- * (vh_batch_scene) that shares the batch's stream. */
+ * pool sizes may all differ (VH_FLAG_DEPTH_FILTER is not supported in a
+ * batch: VH_ERR_UNSUPPORTED).  Every scene is a full handle (vh_batch_scene)
+ * that shares the batch's stream; the launch shapes follow the first
+ * scene's tuning (vh_set_tuning / vh_autotune on vh_batch_scene(b, 0)). */
 vh_status vh_batch_create(const vh_params *params, int32_t n, vh_batch **out);
 vh_status vh_batch_destroy(vh_batch *b);
 int32_t vh_batch_size(const vh_batch *b);

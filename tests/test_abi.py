@@ -75,3 +75,13 @@ def test_missing_library_fails_loudly(monkeypatch):
     monkeypatch.setattr(N, "ENGINE_PATH", "/nonexistent/libvhsdf.so")
     with pytest.raises(ImportError):
         N.lib()
+
+
+def test_batch_rejects_unsupported_parameters_on_the_host():
+    from vhsdf import Batch, VhError, _native as N
+    with pytest.raises(VhError) as err:
+        Batch([dict(width=64, height=48), dict(width=64, height=48, flags=N.VH_FLAG_DEPTH_FILTER)])
+    assert err.value.status == N.VH_ERR_UNSUPPORTED
+    with pytest.raises(VhError) as err:
+        Batch([dict(width=64, height=48, voxel_size=0.0)])
+    assert err.value.status == N.VH_ERR_INVALID_ARG

@@ -113,3 +113,21 @@ def test_pool_overflow_is_reported_per_scene(gpu):
     status, _ = batch.sync()
     assert status == [0, 0]
     batch.close()
+
+
+def test_retuning_scene_zero_rebuilds_the_batch_graph(gpu):
+    specs = [scene_params(*s) for s in SCENES[:3]]
+    frames = [[sc.render(f) for f in range(3)] for sc, _ in specs]
+    batch = Batch([prm for _, prm in specs])
+    singles = [Volume(**prm) for _, prm in specs]
+    for k in range(3):
+        if k == 1:
+            batch.scene(0).set_tuning(1, 2, 3, 1)  # other launch shapes from now on
+        batch.process([fr[k] for fr in frames], with_mesh=True)
+        status, _ = batch.sync()
+        assert status == [0, 0, 0]
+        for v, fr in zip(singles, frames):
+            v.process_frame(*fr[k])
+    for i, v in enumerate(singles):
+        assert_same_blocks(batch.scene(i).export_blocks(), v.export_blocks())
+    batch.close()

@@ -83,3 +83,26 @@ def test_stream_in_reports_a_full_pool(gpu):
         vol.stream_in([0, 0, 0])
     assert err.value.status == 4  # VH_ERR_POOL_FULL
     assert vol.host_blocks() == need
+
+
+def test_repeated_streaming_keeps_the_table_usable(gpu):
+    """Every move-out leaves tombstones; a small table stays usable because
+    the table is rebuilt once they fill an eighth of it, and the volume
+    round-trips unchanged."""
+    s, frames = room_stream(6)
+    vol = volume_for(s, voxel=0.02, trunc=0.08, max_depth=MAX_DEPTH, table_log2=10,
+                     max_probe=256, pool_blocks=1 << 12, max_frame_blocks=1 << 12)
+    for d, c, p in frames:
+        vol.integrate(d, c, p)
+    before = vol.export_blocks()
+    n = len(before["xyz"])
+    assert n > 40
+    for _ in range(12):  # 12 x n erased keys: far more tombstones than slots / 8
+        assert vol.stream_out([0, 0, 0], 0.0) == n
+        assert vol.stream_in([0, 0, 0]) == n
+        assert vol.stats()["tombstones"] <= (1 << 10) // 8 + n
+    assert_same_blocks(vol.export_blocks(), before)
+    vol.compact_table()
+    assert vol.stats()["tombstones"] == 0
+    assert_same_blocks(vol.export_blocks(), before)
+    vol.integrate(*frames[0])  # integration goes on after a rebuild

@@ -44,6 +44,7 @@ struct vh_batch {
   DevState *d_states = nullptr;  // n
   DevState *h_states = nullptr;  // pinned, n
   cudaGraphExec_t graphs[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  int graph_shape[3] = {0, 0, -1};  // integrate grid, MC grid, MC variant the graphs hold
   std::string last_error;
 
   SceneDesc *desc() const { return reinterpret_cast<SceneDesc *>(d_block); }
@@ -74,11 +75,15 @@ void free_batch(vh_batch *b) {
 }
 
 // Launch shapes: the first scene's tuning, capped by the batched kernels'
-// own occupancy.
-int batch_grid(const vh_batch *b, int per_sm) { return b->sm_count * std::max(1, per_sm); }
-
-void enqueue_step(vh_batch *b, int fmt, bool with_mesh) {
+// own occupancy.  {integrate grid, MC grid, MC variant}.
+void batch_shape(const vh_batch *b, int out[3]) {
   const FrameBuffers f0 = handle_frame_buffers(b->scenes[0]);
+  out[0] = b->sm_count * std::max(1, std::min(f0.integrate_per_sm, batch_integrate_ctas_per_sm()));
+  out[1] = b->sm_count * std::max(1, std::min(f0.mc_per_sm, batch_mc_ctas_per_sm(f0.mc_variant)));
+  out[2] = f0.mc_variant;
+}
+
+void enqueue_step(vh_batch *b, int fmt, bool with_mesh, const int shape[3]) {
   const SceneDesc *d = b->desc();
   const uint8_t *act = b->active();
   cudaStream_t s = b->stream;
@@ -86,14 +91,10 @@ void enqueue_step(vh_batch *b, int fmt, bool with_mesh) {
   launch_batch_allocate(d, act, b->d_px_start, b->total_px, b->n, fmt, s);
   launch_batch_epoch_end(d, act, b->n, b->d_prefix, s);
   launch_batch_resolve(d, b->d_prefix, b->n, b->sm_count * 2, s);
-  launch_batch_integrate(d, b->d_prefix, b->n,
-                         batch_grid(b, std::min(f0.integrate_per_sm, batch_integrate_ctas_per_sm())),
-                         s);
+  launch_batch_integrate(d, b->d_prefix, b->n, shape[0], s);
   if (with_mesh) {
     launch_batch_mc_begin(d, act, b->n, s);
-    launch_batch_mc(d, b->d_prefix, b->n,
-                    batch_grid(b, std::min(f0.mc_per_sm, batch_mc_ctas_per_sm(f0.mc_variant))),
-                    f0.mc_variant, s);
+    launch_batch_mc(d, b->d_prefix, b->n, shape[1], shape[2], s);
   }
 }
 
@@ -116,6 +117,7 @@ vh_status vh_batch_create(const vh_params *params, int32_t n, vh_batch **out) {
     const vh_status s = vh_params_validate(params + i);
     if (s != VH_OK) return s;
     if (params[i].device != params[0].device) return VH_ERR_INVALID_ARG;
+    if (params[i].flags & VH_FLAG_DEPTH_FILTER) return VH_ERR_UNSUPPORTED;  // not in batches
   }
   vh_batch *b = new vh_batch();
   b->n = n;
@@ -238,13 +240,24 @@ vh_status vh_batch_process(vh_batch *b, const void *const *depth, int32_t depth_
     return fail(b, VH_ERR_CUDA, "descriptor upload failed");
   b->ring_pos = (b->ring_pos + 1) % kRing;
   const bool graphs_ok = !(handle_params(b->scenes[0]).flags & VH_FLAG_NO_GRAPH);
+  int shape[3];
+  batch_shape(b, shape);
+  if (std::memcmp(shape, b->graph_shape, sizeof(shape)) != 0) {  // tuning changed
+    for (auto &row : b->graphs)
+      for (auto &g : row)
+        if (g) {
+          cudaGraphExecDestroy(g);
+          g = nullptr;
+        }
+    std::memcpy(b->graph_shape, shape, sizeof(shape));
+  }
   if (graphs_ok) {
     cudaGraphExec_t &g = b->graphs[depth_fmt][with_mesh ? 1 : 0];
     if (!g) {
       cudaGraph_t graph = nullptr;
       if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
         return fail(b, VH_ERR_CUDA, "capture failed");
-      enqueue_step(b, depth_fmt, with_mesh != 0);
+      enqueue_step(b, depth_fmt, with_mesh != 0, shape);
       cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
       if (e == cudaSuccess) e = cudaGraphInstantiate(&g, graph, 0);
       if (graph) cudaGraphDestroy(graph);
@@ -255,7 +268,7 @@ vh_status vh_batch_process(vh_batch *b, const void *const *depth, int32_t depth_
     }
     if (cudaGraphLaunch(g, b->stream) != cudaSuccess) return fail(b, VH_ERR_CUDA, "graph launch");
   } else {
-    enqueue_step(b, depth_fmt, with_mesh != 0);
+    enqueue_step(b, depth_fmt, with_mesh != 0, shape);
     if (cudaGetLastError() != cudaSuccess) return fail(b, VH_ERR_CUDA, "batch launch failed");
   }
   for (int i = 0; i < b->n; ++i)

@@ -101,6 +101,34 @@ __global__ void __launch_bounds__(128) k_scatter_raw(VolumeView V, const int32_t
   for (int k = threadIdx.x; k < kBlockWords / 4; k += blockDim.x) dst[k] = src[k];
 }
 
+// Table rebuild: every slot emptied, then the key of every live pool block
+// inserted again with its block id (keys are unique, so plain CAS claims).
+__global__ void __launch_bounds__(256) k_clear_slots(Slot *__restrict__ slots, uint32_t n) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    slots[i].key = kEmptyKey;
+    slots[i].block = kNoBlock;
+    slots[i].stamp = 0xFFFFFFFFu;  // never stamped
+  }
+}
+
+__global__ void __launch_bounds__(256) k_reinsert(VolumeView V) {
+  const uint32_t top = min(V.st->pool_top, V.pool_cap);
+  for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < top; b += gridDim.x * blockDim.x) {
+    const unsigned long long key = V.block_keys[b];
+    if (key >= kTombKey) continue;
+    const uint32_t h = (uint32_t)mix64(key) & V.slot_mask;
+    bool placed = false;
+    for (int i = 0; i < V.max_probe && !placed; ++i) {
+      const uint32_t s = (h + (uint32_t)i) & V.slot_mask;
+      if (atomicCAS(&V.slots[s].key, kEmptyKey, key) == kEmptyKey) {
+        V.slots[s].block = b;
+        placed = true;
+      }
+    }
+    if (!placed) atomicOr(&V.st->error, kErrTableFull);
+  }
+}
+
 // Device scratch freed on scope exit.
 struct Scratch {
   std::vector<void *> ptrs;
@@ -136,6 +164,23 @@ bool far_enough(unsigned long long key, float voxel, const float c[3], double r2
 }  // namespace vh
 
 using namespace vh;
+
+extern "C" vh_status vh_compact_table(vh_handle *h) {
+  if (!h) return VH_ERR_INVALID_ARG;
+  const VolumeView V = handle_view(h);
+  const cudaStream_t st = handle_stream(h);
+  const uint32_t slots = V.slot_mask + 1u;
+  launch_epoch_end(V, st);
+  k_clear_slots<<<std::min<uint32_t>((slots + 255) / 256, 8192), 256, 0, st>>>(V.slots, slots);
+  k_reinsert<<<std::min<uint32_t>((V.pool_cap + 255) / 256, 8192), 256, 0, st>>>(V);
+  // the block list held slot ids: start an empty one
+  launch_clear_list(V, st);
+  if (cudaGetLastError() != cudaSuccess ||
+      cudaMemsetAsync(&V.st->tombstones, 0, sizeof(uint32_t), st) != cudaSuccess)
+    return handle_fail(h, VH_ERR_CUDA, "table rebuild failed");
+  handle_invalidate_nb(h);
+  return handle_sync(h);
+}
 
 extern "C" vh_status vh_stream_out(vh_handle *h, const float *centre, float radius,
                                    int64_t *moved) {
@@ -210,6 +255,9 @@ extern "C" vh_status vh_stream_out(vh_handle *h, const float *centre, float radi
   s = vh_erase_keys(h, d_xyz, n, &erased, VH_MEM_DEVICE);
   if (s != VH_OK) return s;
   if (moved) *moved = erased;
+  // erased slots stay tombstones (inserts do not reuse them): rebuild the
+  // table once they fill an eighth of it
+  if (handle_state(h).tombstones > (V.slot_mask + 1u) / 8u) return vh_compact_table(h);
   return VH_OK;
 }
 

@@ -126,6 +126,7 @@ SIGNATURES = {
     "vh_stream_out": (I32, [P, P, C.c_float, PI64]),
     "vh_stream_in": (I32, [P, P, C.c_float, PI64]),
     "vh_host_blocks": (I64, [P]),
+    "vh_compact_table": (I32, [P]),
     "vh_mesh_indexed": (I32, [P, P, P, I64, P, I64, PI64, PI64]),
     "vh_batch_create": (I32, [C.POINTER(VhParams), I32, C.POINTER(P)]),
     "vh_batch_destroy": (I32, [P]),

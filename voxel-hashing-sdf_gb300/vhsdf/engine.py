@@ -161,6 +161,9 @@ class Volume:
         self._check(self._L.vh_stream_in(self._h, c.ctypes.data, float(radius), C.byref(n)))
         return n.value
 
+    def compact_table(self):
+        self._check(self._L.vh_compact_table(self._h))
+
     def host_blocks(self):
         return int(self._L.vh_host_blocks(self._h))
 
