@@ -40,7 +40,7 @@ struct vh_batch {
   int ring_pos = 0;
   uint32_t *d_px_start = nullptr;  // n + 1
   uint32_t total_px = 0;
-  uint32_t *d_prefix = nullptr;  // n + 1
+  uint32_t *d_prefix = nullptr;  // n + 1 prefix words, then the MC block counter
   DevState *d_states = nullptr;  // n
   DevState *h_states = nullptr;  // pinned, n
   cudaGraphExec_t graphs[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
@@ -152,7 +152,7 @@ vh_status vh_batch_create(const vh_params *params, int32_t n, vh_batch **out) {
   bool ok = cudaMalloc(&b->d_block, b->block_bytes) == cudaSuccess &&
             cudaMallocHost(&b->h_block, b->block_bytes * kRing) == cudaSuccess &&
             cudaMalloc(&b->d_px_start, sizeof(uint32_t) * (n + 1)) == cudaSuccess &&
-            cudaMalloc(&b->d_prefix, sizeof(uint32_t) * (n + 1)) == cudaSuccess &&
+            cudaMalloc(&b->d_prefix, sizeof(uint32_t) * (n + 2)) == cudaSuccess &&
             cudaMalloc(&b->d_states, sizeof(DevState) * n) == cudaSuccess &&
             cudaMallocHost(&b->h_states, sizeof(DevState) * n) == cudaSuccess;
   for (auto &e : b->ring_ev)

@@ -63,7 +63,8 @@ struct DevState {
   unsigned long long voxels_updated;  // by the last integration
   uint32_t tombstones;   // erased slots
   uint32_t erased;       // keys erased by the last erase call
-  uint32_t pad[4];
+  uint32_t mc_next;      // marching cubes: blocks handed out past the first grid
+  uint32_t pad[3];
 };
 
 // Everything a kernel needs to reach the volume; passed by value.
@@ -186,7 +187,7 @@ void launch_batch_resolve(const SceneDesc *d, const uint32_t *prefix, int n, int
 void launch_batch_integrate(const SceneDesc *d, const uint32_t *prefix, int n, int grid,
                             cudaStream_t s);
 void launch_batch_mc_begin(const SceneDesc *d, const uint8_t *active, int n, cudaStream_t s);
-void launch_batch_mc(const SceneDesc *d, const uint32_t *prefix, int n, int grid, int variant,
+void launch_batch_mc(const SceneDesc *d, uint32_t *prefix, int n, int grid, int variant,
                      cudaStream_t s);
 void launch_batch_gather_state(const SceneDesc *d, int n, DevState *out, cudaStream_t s);
 // Resident CTAs per SM of the batched persistent kernels.

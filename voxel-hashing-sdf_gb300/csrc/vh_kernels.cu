@@ -500,6 +500,7 @@ struct McShared {
   uint32_t nb[8];
   uint32_t warp_sum[kMcThreads / 32];
   uint32_t base;
+  uint32_t next[2];  // the block after the current one (double-buffered)
 };
 
 __device__ __forceinline__ int hidx(int x, int y, int z) { return x + kH * (y + kH * z); }
@@ -802,9 +803,17 @@ __global__ void __launch_bounds__(kMcThreads, kMinCtas) k_mc(VolumeView V, int s
   __shared__ McShared S;
   mc_init_shared(S);
   const uint32_t n = scope_all ? V.st->pool_top : min(V.st->frame_count, V.frame_cap);
-  for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
-    __syncthreads();  // previous iteration done with S
+  // A block emits anything from nothing to hundreds of triangles, so blocks
+  // are handed out dynamically: a CTA's first block is its index, every
+  // further one comes from a counter, fetched while the current block is
+  // processed so the atomic's latency stays hidden.
+  __syncthreads();
+  uint32_t i = blockIdx.x;
+  for (int par = 0; i < n; par ^= 1) {
+    if (threadIdx.x == 0) S.next[par] = gridDim.x + atomicAdd(&V.st->mc_next, 1u);
     mc_block(S, V, scope_all, min_weight, tris, tri_cap, i);
+    __syncthreads();  // S.next[par] visible; this block done with S
+    i = S.next[par];
   }
 }
 
@@ -836,6 +845,7 @@ __device__ void frame_begin_state(const VolumeView &V) {
 __device__ void mc_begin_state(const VolumeView &V) {
   reconcile(V);
   V.st->tri_count = 0;
+  V.st->mc_next = 0;
 }
 
 __global__ void k_frame_begin(VolumeView V) {
@@ -931,7 +941,8 @@ __global__ void __launch_bounds__(kBatchPixelThreads) k_batch_allocate(
 }
 
 // Closes every active scene's allocation epoch and writes the prefix of the
-// frame-list lengths (one CTA of 1024 threads, n <= 1024).
+// frame-list lengths (one CTA of 1024 threads, n <= 1024); prefix holds
+// n + 2 words, the last one k_batch_mc's block counter.
 __global__ void __launch_bounds__(1024) k_batch_epoch_end(const SceneDesc *__restrict__ d,
                                                           const uint8_t *__restrict__ active,
                                                           int n, uint32_t *__restrict__ prefix) {
@@ -964,6 +975,7 @@ __global__ void __launch_bounds__(1024) k_batch_epoch_end(const SceneDesc *__res
   const uint32_t excl = wsum[warp] + incl - cnt;
   if (s < n) prefix[s] = excl;
   if (s == n - 1) prefix[n] = excl + cnt;
+  if (s == 0) prefix[n + 1] = 0;  // k_batch_mc's hand-out counter
 }
 
 __global__ void __launch_bounds__(256) k_batch_resolve(const SceneDesc *__restrict__ d,
@@ -1029,20 +1041,24 @@ __global__ void k_batch_mc_begin(const SceneDesc *__restrict__ d, const uint8_t 
 template <int kMinCtas>
 __global__ void __launch_bounds__(kMcThreads, kMinCtas) k_batch_mc(const SceneDesc *__restrict__ d,
                                                             const uint32_t *__restrict__ prefix,
-                                                            int n) {
+                                                            int n, uint32_t *__restrict__ next) {
   __shared__ McShared S;
   __shared__ SceneDesc sd;
   mc_init_shared(S);
   const uint32_t total = __ldg(prefix + n);
   int cur = -1;
-  for (uint32_t g = blockIdx.x; g < total; g += gridDim.x) {
-    __syncthreads();  // previous iteration done with S and sd
+  __syncthreads();
+  uint32_t g = blockIdx.x;
+  for (int par = 0; g < total; par ^= 1) {  // dynamic hand-out, as in k_mc
+    if (threadIdx.x == 0) S.next[par] = gridDim.x + atomicAdd(next, 1u);
     const int s = scene_of(prefix, n, g);
-    if (s != cur) {
+    if (s != cur) {  // the barrier closing the previous block freed sd
       load_scene(sd, d, s);
       cur = s;
     }
     mc_block(S, sd.V, 0, sd.C.mc_min_weight, sd.tris, sd.tri_cap, g - __ldg(prefix + s));
+    __syncthreads();
+    g = S.next[par];
   }
 }
 
@@ -1280,12 +1296,13 @@ void launch_batch_integrate(const SceneDesc *d, const uint32_t *prefix, int n, i
 void launch_batch_mc_begin(const SceneDesc *d, const uint8_t *active, int n, cudaStream_t s) {
   k_batch_mc_begin<<<grid_for((uint32_t)n, 128), 128, 0, s>>>(d, active, n);
 }
-void launch_batch_mc(const SceneDesc *d, const uint32_t *prefix, int n, int grid, int variant,
+void launch_batch_mc(const SceneDesc *d, uint32_t *prefix, int n, int grid, int variant,
                      cudaStream_t s) {
+  uint32_t *next = prefix + n + 1;  // reset by k_batch_epoch_end
   if (variant == 1)
-    k_batch_mc<12><<<grid, kMcThreads, 0, s>>>(d, prefix, n);
+    k_batch_mc<12><<<grid, kMcThreads, 0, s>>>(d, prefix, n, next);
   else
-    k_batch_mc<8><<<grid, kMcThreads, 0, s>>>(d, prefix, n);
+    k_batch_mc<8><<<grid, kMcThreads, 0, s>>>(d, prefix, n, next);
 }
 int batch_integrate_ctas_per_sm() {
   int n = 0;
