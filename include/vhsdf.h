@@ -125,11 +125,12 @@ typedef struct vh_mesh_view {
 /* Launch configuration of the per-frame kernels.  Every configuration
  * computes identical results; only the speed differs. */
 typedef struct vh_tuning {
-  int32_t integrate_variant;     /* 0: one block in flight per CTA,          */
+  int32_t integrate_variant;     /* 0: one block in flight per CTA, register */
+                                 /*    budget for 12 CTAs per SM,            */
                                  /* 1: next block's voxels prefetched        */
   int32_t integrate_ctas_per_sm; /* resident CTAs per SM (0 = occupancy max) */
   int32_t mc_ctas_per_sm;        /* resident CTAs per SM (0 = occupancy max) */
-  int32_t mc_variant;            /* 0: register budget for 8 CTAs per SM,    */
+  int32_t mc_variant;            /* 0: register budget for 10 CTAs per SM,   */
                                  /* 1: for 12 CTAs per SM                    */
 } vh_tuning;
 

@@ -184,14 +184,12 @@ void enqueue_frame(vh_handle *h, int fmt, bool with_mc, bool events, bool captur
     fmt = VH_DEPTH_F32_M;
   }
   launch_allocate(h->V, h->C, depth, fmt, h->d_rgb, h->d_pose, h->d_pix, s);
-  launch_epoch_end(h->V, s);
-  launch_frame_resolve(h->V, h->sm_count * 2, s);
+  launch_frame_resolve(h->V, h->sm_count * 2, with_mc, s);
   if (events) stage_event(h->ev[1], s, capturing);
   launch_integrate(h->V, h->C, h->d_pix, h->d_pose, integrate_grid(h),
                    h->tuning.integrate_variant, s);
   if (events) stage_event(h->ev[2], s, capturing);
   if (with_mc) {
-    launch_mc_begin(h->V, s);
     launch_mc(h->V, 0, h->C.mc_min_weight, h->d_tris, (uint32_t)h->tri_cap, mc_grid(h),
               h->tuning.mc_variant, s);
     if (events) stage_event(h->ev[3], s, capturing);

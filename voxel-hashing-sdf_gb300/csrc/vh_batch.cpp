@@ -89,13 +89,10 @@ void enqueue_step(vh_batch *b, int fmt, bool with_mesh, const int shape[3]) {
   cudaStream_t s = b->stream;
   launch_batch_frame_begin(d, act, b->n, s);
   launch_batch_allocate(d, act, b->d_px_start, b->total_px, b->n, fmt, s);
-  launch_batch_epoch_end(d, act, b->n, b->d_prefix, s);
+  launch_batch_epoch_end(d, act, b->n, b->d_prefix, with_mesh, s);
   launch_batch_resolve(d, b->d_prefix, b->n, b->sm_count * 2, s);
   launch_batch_integrate(d, b->d_prefix, b->n, shape[0], s);
-  if (with_mesh) {
-    launch_batch_mc_begin(d, act, b->n, s);
-    launch_batch_mc(d, b->d_prefix, b->n, shape[1], shape[2], s);
-  }
+  if (with_mesh) launch_batch_mc(d, b->d_prefix, b->n, shape[1], shape[2], s);
 }
 
 vh_status fail(vh_batch *b, vh_status s, const std::string &msg) {

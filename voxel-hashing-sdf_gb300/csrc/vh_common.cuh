@@ -162,8 +162,10 @@ void launch_find_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, int32
                       cudaStream_t s);
 void launch_erase_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, cudaStream_t s);
 void launch_frame_nb(const VolumeView &V, cudaStream_t s);
-// Writes frame_res for the current block list (after allocation).
-void launch_frame_resolve(const VolumeView &V, int grid, cudaStream_t s);
+// Writes frame_res and frame_nb for the current block list (after
+// allocation); also closes the allocation epoch and, with mc_follows, resets
+// the marching-cubes counters (what launch_mc_begin does).
+void launch_frame_resolve(const VolumeView &V, int grid, bool mc_follows, cudaStream_t s);
 void launch_list_keys(const VolumeView &V, int32_t *xyz, uint32_t n, cudaStream_t s);
 void launch_scatter_blocks(const VolumeView &V, const int32_t *xyz, const float *sdf,
                            const float *w, const uint8_t *rgb, uint32_t n, cudaStream_t s);
@@ -180,13 +182,13 @@ void launch_depth_filter(const CamParams &C, const void *depth, int fmt, float *
 void launch_batch_frame_begin(const SceneDesc *d, const uint8_t *active, int n, cudaStream_t s);
 void launch_batch_allocate(const SceneDesc *d, const uint8_t *active, const uint32_t *px_start,
                            uint32_t total_px, int n, int fmt, cudaStream_t s);
+// with_mesh: also resets every active scene's marching-cubes counters.
 void launch_batch_epoch_end(const SceneDesc *d, const uint8_t *active, int n, uint32_t *prefix,
-                            cudaStream_t s);
+                            bool with_mesh, cudaStream_t s);
 void launch_batch_resolve(const SceneDesc *d, const uint32_t *prefix, int n, int grid,
                           cudaStream_t s);
 void launch_batch_integrate(const SceneDesc *d, const uint32_t *prefix, int n, int grid,
                             cudaStream_t s);
-void launch_batch_mc_begin(const SceneDesc *d, const uint8_t *active, int n, cudaStream_t s);
 void launch_batch_mc(const SceneDesc *d, uint32_t *prefix, int n, int grid, int variant,
                      cudaStream_t s);
 void launch_batch_gather_state(const SceneDesc *d, int n, DevState *out, cudaStream_t s);

@@ -452,7 +452,7 @@ __device__ __forceinline__ uint32_t integrate_loaded(const VolumeView &V, const 
 // current block is computed (two blocks in flight per thread, more
 // registers); otherwise one block in flight and higher occupancy.
 template <bool kPrefetch>
-__global__ void __launch_bounds__(128) k_integrate(VolumeView V, CamParams C,
+__global__ void __launch_bounds__(128, kPrefetch ? 8 : 12) k_integrate(VolumeView V, CamParams C,
                                                    const uint2 *__restrict__ pix,
                                                    const float *__restrict__ pose) {
   const uint32_t n = min(V.st->frame_count, V.frame_cap);
@@ -945,13 +945,17 @@ __global__ void __launch_bounds__(kBatchPixelThreads) k_batch_allocate(
 // n + 2 words, the last one k_batch_mc's block counter.
 __global__ void __launch_bounds__(1024) k_batch_epoch_end(const SceneDesc *__restrict__ d,
                                                           const uint8_t *__restrict__ active,
-                                                          int n, uint32_t *__restrict__ prefix) {
+                                                          int n, uint32_t *__restrict__ prefix,
+                                                          int with_mesh) {
   __shared__ uint32_t wsum[32];
   const int s = threadIdx.x, lane = s & 31, warp = s >> 5;
   uint32_t cnt = 0;
   if (s < n && active[s]) {
     const VolumeView &V = d[s].V;
-    reconcile(V);
+    if (with_mesh)
+      mc_begin_state(V);
+    else
+      reconcile(V);
     cnt = min(V.st->frame_count, V.frame_cap);
   }
   uint32_t incl = cnt;
@@ -1029,12 +1033,6 @@ __global__ void __launch_bounds__(128) k_batch_integrate(const SceneDesc *__rest
     updated += integrate_loaded(sd.V, sd.C, P, sd.pix, i, q);
   }
   if (cur >= 0) flush_updated(sd, updated);
-}
-
-__global__ void k_batch_mc_begin(const SceneDesc *__restrict__ d, const uint8_t *__restrict__ active,
-                                 int n) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < n && active[s]) mc_begin_state(d[s].V);
 }
 
 // Per-frame marching cubes over the listed blocks of every scene.
@@ -1150,8 +1148,16 @@ __global__ void __launch_bounds__(256) k_frame_nb(VolumeView V) {
 }
 
 // frame_res and frame_nb of every frame-list entry, 8 threads per entry
-// (grid-stride), after allocation and before integration.
-__global__ void __launch_bounds__(256) k_frame_resolve(VolumeView V) {
+// (grid-stride), after allocation and before integration.  Thread 0 also
+// closes the allocation epoch and, when marching cubes follows in this
+// frame, resets its counters (no other thread reads those fields).
+__global__ void __launch_bounds__(256) k_frame_resolve(VolumeView V, int mc_follows) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (mc_follows)
+      mc_begin_state(V);
+    else
+      reconcile(V);
+  }
   const uint32_t n8 = 8u * min(V.st->frame_count, V.frame_cap);
   for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < n8; g += gridDim.x * blockDim.x)
     resolve_entry(V, g >> 3, g & 7u);
@@ -1218,14 +1224,15 @@ int integrate_ctas_per_sm(int variant) {
   return n > 0 ? n : 1;
 }
 
-// MC variants differ only in the register budget: 0 targets 8 resident CTAs
-// per SM, 1 targets 12 (fewer registers, more warps to hide latency).
+// MC variants differ only in the register budget: 0 targets 10 resident
+// CTAs per SM (48 registers, no spills), 1 targets 12 (40 registers, a few
+// spilled).
 int mc_ctas_per_sm(int variant) {
   int n = 0;
   if (variant == 1)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mc<12>, kMcThreads, 0);
   else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mc<8>, kMcThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mc<10>, kMcThreads, 0);
   return n > 0 ? n : 1;
 }
 
@@ -1242,7 +1249,7 @@ void launch_mc(const VolumeView &V, int scope_all, float min_weight, float4 *tri
   if (variant == 1)
     k_mc<12><<<grid, kMcThreads, 0, s>>>(V, scope_all, min_weight, tris, tri_cap);
   else
-    k_mc<8><<<grid, kMcThreads, 0, s>>>(V, scope_all, min_weight, tris, tri_cap);
+    k_mc<10><<<grid, kMcThreads, 0, s>>>(V, scope_all, min_weight, tris, tri_cap);
 }
 
 void launch_alloc_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, cudaStream_t s) {
@@ -1255,8 +1262,8 @@ void launch_find_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, int32
 void launch_erase_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, cudaStream_t s) {
   if (n) k_erase_keys<<<grid_for(n, 256), 256, 0, s>>>(V, xyz, n);
 }
-void launch_frame_resolve(const VolumeView &V, int grid, cudaStream_t s) {
-  k_frame_resolve<<<grid, 256, 0, s>>>(V);
+void launch_frame_resolve(const VolumeView &V, int grid, bool mc_follows, cudaStream_t s) {
+  k_frame_resolve<<<grid, 256, 0, s>>>(V, mc_follows ? 1 : 0);
 }
 void launch_frame_nb(const VolumeView &V, cudaStream_t s) {
   k_frame_nb<<<grid_for(V.frame_cap * 8u, 256), 256, 0, s>>>(V);
@@ -1282,8 +1289,8 @@ void launch_batch_allocate(const SceneDesc *d, const uint8_t *active, const uint
     k_batch_allocate<float><<<grid, kBatchPixelThreads, 0, s>>>(d, active, px_start, n);
 }
 void launch_batch_epoch_end(const SceneDesc *d, const uint8_t *active, int n, uint32_t *prefix,
-                            cudaStream_t s) {
-  k_batch_epoch_end<<<1, 1024, 0, s>>>(d, active, n, prefix);
+                            bool with_mesh, cudaStream_t s) {
+  k_batch_epoch_end<<<1, 1024, 0, s>>>(d, active, n, prefix, with_mesh ? 1 : 0);
 }
 void launch_batch_resolve(const SceneDesc *d, const uint32_t *prefix, int n, int grid,
                           cudaStream_t s) {
@@ -1293,16 +1300,13 @@ void launch_batch_integrate(const SceneDesc *d, const uint32_t *prefix, int n, i
                             cudaStream_t s) {
   k_batch_integrate<<<grid, 128, 0, s>>>(d, prefix, n);
 }
-void launch_batch_mc_begin(const SceneDesc *d, const uint8_t *active, int n, cudaStream_t s) {
-  k_batch_mc_begin<<<grid_for((uint32_t)n, 128), 128, 0, s>>>(d, active, n);
-}
 void launch_batch_mc(const SceneDesc *d, uint32_t *prefix, int n, int grid, int variant,
                      cudaStream_t s) {
   uint32_t *next = prefix + n + 1;  // reset by k_batch_epoch_end
   if (variant == 1)
     k_batch_mc<12><<<grid, kMcThreads, 0, s>>>(d, prefix, n, next);
   else
-    k_batch_mc<8><<<grid, kMcThreads, 0, s>>>(d, prefix, n, next);
+    k_batch_mc<10><<<grid, kMcThreads, 0, s>>>(d, prefix, n, next);
 }
 int batch_integrate_ctas_per_sm() {
   int n = 0;
@@ -1314,7 +1318,7 @@ int batch_mc_ctas_per_sm(int variant) {
   if (variant == 1)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_mc<12>, kMcThreads, 0);
   else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_mc<8>, kMcThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_mc<10>, kMcThreads, 0);
   return n > 0 ? n : 1;
 }
 void launch_batch_gather_state(const SceneDesc *d, int n, DevState *out, cudaStream_t s) {
