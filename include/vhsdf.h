@@ -168,7 +168,13 @@ const char *vh_last_error(const vh_handle *h);
  * (src/tsdf.cu:1484-1533, kernels src/tsdf.cu:2088-2238 and 599-751).
  * depth: H*W row-major in `depth_fmt`; rgb: H*W*3 interleaved RGB bytes;
  * c2w: 16 floats, row-major camera-to-world, host memory
- * (PointCloudGenerator.cpp:118-127 builds it this way). */
+ * (PointCloudGenerator.cpp:118-127 builds it this way).
+ * VH_MEM_DEVICE images are read in place by the frame's kernels: without
+ * VH_FLAG_SYNC they must stay unchanged until the handle's stream has run
+ * the frame.  VH_MEM_HOST images are copied on the handle's copy stream
+ * into one of two staging slots, overlapping the previous frame's kernels;
+ * pinned host memory keeps the call asynchronous (pageable memory is copied
+ * before the call returns). */
 vh_status vh_integrate(vh_handle *h, const void *depth, int32_t depth_fmt,
                        const uint8_t *rgb, const float *c2w, int32_t mem);
 /* Marching cubes over `scope`: replaces marchingCubeHashKernel

@@ -43,16 +43,25 @@ struct vh_handle {
   cudaStream_t own_stream = nullptr;
   VolumeView V{};
   CamParams C{};
-  void *d_depth = nullptr;
+  void *d_depth = nullptr;      // staging of single images (refinement, batches)
   float *d_depth_f = nullptr;  // filtered depth (VH_FLAG_DEPTH_FILTER)
   uint8_t *d_rgb = nullptr;
-  float *d_pose = nullptr;
+  FrameIn *d_fin = nullptr;    // the current frame's pose and image pointers
   uint2 *d_pix = nullptr;
   float4 *d_tris = nullptr;
   int64_t tri_cap = 0;
-  float *h_pose_ring = nullptr;
+  FrameIn *h_fin_ring = nullptr;  // pinned upload slots of d_fin
   cudaEvent_t ring_ev[kPoseRing] = {};
   int ring_pos = 0;
+  // Host frames: two device slots filled on copy_stream, so the upload of a
+  // frame overlaps the kernels of the one before.  in_copied[k] follows the
+  // upload into slot k, in_consumed[k] the kernels of the frame that read it.
+  cudaStream_t copy_stream = nullptr;
+  void *d_in_depth[2] = {nullptr, nullptr};
+  uint8_t *d_in_rgb[2] = {nullptr, nullptr};
+  cudaEvent_t in_copied[2] = {}, in_consumed[2] = {};
+  int in_pos = 0;
+  int in_used = -1;  // slot read by the frame being enqueued (-1: device inputs)
   DevState *h_state = nullptr;
   cudaGraphExec_t graphs[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
   cudaEvent_t ev[kNumEvents] = {};
@@ -177,16 +186,16 @@ void enqueue_frame(vh_handle *h, int fmt, bool with_mc, bool events, bool captur
   cudaStream_t s = h->stream;
   if (events) stage_event(h->ev[0], s, capturing);
   launch_frame_begin(h->V, s);
-  const void *depth = h->d_depth;
+  const void *depth = nullptr;  // the frame's own image, found through d_fin
   if (h->p.flags & VH_FLAG_DEPTH_FILTER) {
-    launch_depth_filter(h->C, h->d_depth, fmt, h->d_depth_f, s);
+    launch_depth_filter(h->C, nullptr, h->d_fin, fmt, h->d_depth_f, s);
     depth = h->d_depth_f;
     fmt = VH_DEPTH_F32_M;
   }
-  launch_allocate(h->V, h->C, depth, fmt, h->d_rgb, h->d_pose, h->d_pix, s);
+  launch_allocate(h->V, h->C, h->d_fin, depth, fmt, h->d_pix, s);
   launch_frame_resolve(h->V, h->sm_count * 2, with_mc, s);
   if (events) stage_event(h->ev[1], s, capturing);
-  launch_integrate(h->V, h->C, h->d_pix, h->d_pose, integrate_grid(h),
+  launch_integrate(h->V, h->C, h->d_pix, h->d_fin->pose, integrate_grid(h),
                    h->tuning.integrate_variant, s);
   if (events) stage_event(h->ev[2], s, capturing);
   if (with_mc) {
@@ -221,6 +230,8 @@ void apply_tuning(vh_handle *h, const vh_tuning &t) {
 }
 
 // Runs the frame chain as a CUDA graph (captured on first use) or directly.
+vh_status inputs_consumed(vh_handle *h);
+
 vh_status run_frame(vh_handle *h, int fmt, bool with_mc) {
   const bool events = (h->p.flags & VH_FLAG_PROFILE) != 0;
   const bool graphs_ok = !(h->p.flags & VH_FLAG_NO_GRAPH) && h->stream != nullptr;
@@ -246,10 +257,21 @@ vh_status run_frame(vh_handle *h, int fmt, bool with_mc) {
   }
   h->ev_pending = events;
   h->ev_has_mc = with_mc;
+  vh_status s = inputs_consumed(h);
+  if (s != VH_OK) return s;
+  // Without VH_FLAG_SYNC the frame's counters still come back to the host
+  // mirror (64 bytes, pinned) at the end of every frame.
+  if (!(h->p.flags & VH_FLAG_SYNC))
+    VH_CUDA(h, cudaMemcpyAsync(h->h_state, h->V.st, sizeof(DevState), cudaMemcpyDeviceToHost,
+                               h->stream));
   return VH_OK;
 }
 
-// Stages depth, colour and pose of one frame into the fixed device buffers.
+// Makes one frame's inputs visible to the frame kernels through d_fin:
+// device images are read in place (the caller keeps them unchanged until the
+// frame's work on the handle's stream has run), host images are uploaded
+// into a staging slot on the copy stream, which the handle's stream waits
+// for.  The caller records inputs_consumed() after the frame's kernels.
 vh_status stage_inputs(vh_handle *h, const void *depth, int32_t fmt, const uint8_t *rgb,
                        const float *c2w, int32_t mem) {
   if (!depth || !rgb || !c2w) return fail(h, VH_ERR_INVALID_ARG, "null input pointer");
@@ -259,22 +281,44 @@ vh_status stage_inputs(vh_handle *h, const void *depth, int32_t fmt, const uint8
     return fail(h, VH_ERR_INVALID_ARG, "unknown memory kind");
   if (!finite_pose(c2w)) return fail(h, VH_ERR_NOT_FINITE, "camera pose has a non-finite entry");
   const size_t npx = (size_t)h->p.width * h->p.height;
-  // pose: host ring of pinned slots, each reused only after its copy ran
-  float *slot = h->h_pose_ring + 16 * h->ring_pos;
+  // descriptor: host ring of pinned slots, each reused only after its copy ran
+  FrameIn *slot = h->h_fin_ring + h->ring_pos;
   VH_CUDA(h, cudaEventSynchronize(h->ring_ev[h->ring_pos]));
-  std::memcpy(slot, c2w, 16 * sizeof(float));
-  VH_CUDA(h, cudaMemcpyAsync(h->d_pose, slot, 16 * sizeof(float), cudaMemcpyHostToDevice,
-                             h->stream));
+  std::memcpy(slot->pose, c2w, 16 * sizeof(float));
+  h->in_used = -1;
+  if (mem == VH_MEM_DEVICE) {
+    slot->depth = depth;
+    slot->rgb = rgb;
+  } else {
+    const int k = h->in_pos;  // last read by the frame two host frames back
+    const size_t dbytes = npx * (fmt == VH_DEPTH_U16_MM ? 2 : 4);
+    VH_CUDA(h, cudaStreamWaitEvent(h->copy_stream, h->in_consumed[k], 0));
+    VH_CUDA(h, cudaMemcpyAsync(h->d_in_depth[k], depth, dbytes, cudaMemcpyHostToDevice,
+                               h->copy_stream));
+    VH_CUDA(h, cudaMemcpyAsync(h->d_in_rgb[k], rgb, 3 * npx, cudaMemcpyHostToDevice,
+                               h->copy_stream));
+    VH_CUDA(h, cudaEventRecord(h->in_copied[k], h->copy_stream));
+    VH_CUDA(h, cudaStreamWaitEvent(h->stream, h->in_copied[k], 0));
+    slot->depth = h->d_in_depth[k];
+    slot->rgb = h->d_in_rgb[k];
+    h->in_used = k;
+    h->in_pos ^= 1;
+  }
+  VH_CUDA(h, cudaMemcpyAsync(h->d_fin, slot, sizeof(FrameIn), cudaMemcpyHostToDevice, h->stream));
   VH_CUDA(h, cudaEventRecord(h->ring_ev[h->ring_pos], h->stream));
   h->ring_pos = (h->ring_pos + 1) % kPoseRing;
-  const cudaMemcpyKind kind = mem == VH_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
-  const size_t dbytes = npx * (fmt == VH_DEPTH_U16_MM ? 2 : 4);
-  VH_CUDA(h, cudaMemcpyAsync(h->d_depth, depth, dbytes, kind, h->stream));
-  VH_CUDA(h, cudaMemcpyAsync(h->d_rgb, rgb, 3 * npx, kind, h->stream));
+  return VH_OK;
+}
+
+// After the frame's kernels: its host staging slot may be refilled.
+vh_status inputs_consumed(vh_handle *h) {
+  if (h->in_used >= 0) VH_CUDA(h, cudaEventRecord(h->in_consumed[h->in_used], h->stream));
+  h->in_used = -1;
   return VH_OK;
 }
 
 void free_all(vh_handle *h) {
+  if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
   drop_graphs(h);
   refine_ctx_free(h->refine);
   h->refine = nullptr;
@@ -291,11 +335,18 @@ void free_all(vh_handle *h) {
   cudaFree(h->d_depth);
   cudaFree(h->d_depth_f);
   cudaFree(h->d_rgb);
-  cudaFree(h->d_pose);
+  cudaFree(h->d_fin);
+  for (int k = 0; k < 2; ++k) {
+    cudaFree(h->d_in_depth[k]);
+    cudaFree(h->d_in_rgb[k]);
+    if (h->in_copied[k]) cudaEventDestroy(h->in_copied[k]);
+    if (h->in_consumed[k]) cudaEventDestroy(h->in_consumed[k]);
+  }
+  if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
   cudaFree(h->d_pix);
   cudaFree(h->d_tris);
   cudaFree(h->d_work);
-  if (h->h_pose_ring) cudaFreeHost(h->h_pose_ring);
+  if (h->h_fin_ring) cudaFreeHost(h->h_fin_ring);
   if (h->h_state) cudaFreeHost(h->h_state);
   for (auto &e : h->ring_ev)
     if (e) cudaEventDestroy(e);
@@ -531,10 +582,14 @@ vh_status vh_create(const vh_params *p, vh_handle **out) {
             cudaMalloc(&h->d_depth, 4 * npx) == cudaSuccess &&
             cudaMalloc(&h->d_depth_f, 4 * npx) == cudaSuccess &&
             cudaMalloc(&h->d_rgb, 3 * npx) == cudaSuccess &&
-            cudaMalloc(&h->d_pose, 16 * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&h->d_fin, sizeof(FrameIn)) == cudaSuccess &&
+            cudaMalloc(&h->d_in_depth[0], 4 * npx) == cudaSuccess &&
+            cudaMalloc(&h->d_in_depth[1], 4 * npx) == cudaSuccess &&
+            cudaMalloc(&h->d_in_rgb[0], 3 * npx) == cudaSuccess &&
+            cudaMalloc(&h->d_in_rgb[1], 3 * npx) == cudaSuccess &&
             cudaMalloc(&h->d_pix, sizeof(uint2) * npx) == cudaSuccess &&
             cudaMalloc(&h->d_tris, sizeof(float4) * 3 * (size_t)(h->tri_cap ? h->tri_cap : 1)) == cudaSuccess &&
-            cudaMallocHost(&h->h_pose_ring, sizeof(float) * 16 * kPoseRing) == cudaSuccess &&
+            cudaMallocHost(&h->h_fin_ring, sizeof(FrameIn) * kPoseRing) == cudaSuccess &&
             cudaMallocHost(&h->h_state, sizeof(DevState)) == cudaSuccess;
   if (!ok) {
     cudaGetLastError();
@@ -543,6 +598,12 @@ vh_status vh_create(const vh_params *p, vh_handle **out) {
   }
   for (auto &e : h->ring_ev)
     if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return bail(VH_ERR_CUDA);
+  for (int k = 0; k < 2; ++k)
+    if (cudaEventCreateWithFlags(&h->in_copied[k], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->in_consumed[k], cudaEventDisableTiming) != cudaSuccess)
+      return bail(VH_ERR_CUDA);
+  if (cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(VH_ERR_CUDA);
   for (auto &e : h->ev)
     if (cudaEventCreate(&e) != cudaSuccess) return bail(VH_ERR_CUDA);
   for (int i = 0; i < kPoseRing; ++i) cudaEventRecord(h->ring_ev[i], h->stream);
@@ -745,7 +806,7 @@ vh_status vh_filter_depth(vh_handle *h, const void *depth, int32_t depth_fmt, fl
   vh_status s = handle_stage_depth(h, depth, depth_fmt, mem, &d);
   if (s != VH_OK) return s;
   float *dst = mem == VH_MEM_DEVICE ? out : h->d_depth_f;
-  launch_depth_filter(h->C, d, depth_fmt, dst, h->stream);
+  launch_depth_filter(h->C, d, nullptr, depth_fmt, dst, h->stream);
   VH_CUDA(h, cudaGetLastError());
   if (mem == VH_MEM_HOST)
     VH_CUDA(h, cudaMemcpyAsync(out, dst, sizeof(float) * (size_t)h->p.width * h->p.height,

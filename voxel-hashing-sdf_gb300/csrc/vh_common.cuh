@@ -146,9 +146,20 @@ void launch_frame_begin(const VolumeView &V, cudaStream_t s);
 void launch_epoch_end(const VolumeView &V, cudaStream_t s);
 void launch_clear_list(const VolumeView &V, cudaStream_t s);
 void launch_mc_begin(const VolumeView &V, cudaStream_t s);
-// fmt: 0 = uint16 scaled by depth_scale, 1 = float metres
-void launch_allocate(const VolumeView &V, const CamParams &C, const void *depth, int fmt,
-                     const uint8_t *rgb, const float *pose, uint2 *pix, cudaStream_t s);
+// The inputs of one frame as the kernels find them on the device: the
+// camera pose and where the depth and colour images live (the caller's own
+// device buffers, or the handle's staging copy of host images).  Uploaded
+// per frame, so a captured frame graph serves every frame.
+struct FrameIn {
+  float pose[16];  // row-major camera-to-world; the kernels read rows 0-2
+  const void *depth;
+  const uint8_t *rgb;
+};
+
+// fmt: 0 = uint16 scaled by depth_scale, 1 = float metres.  depth (when not
+// null) replaces fin->depth, e.g. by the filtered copy.
+void launch_allocate(const VolumeView &V, const CamParams &C, const FrameIn *fin,
+                     const void *depth, int fmt, uint2 *pix, cudaStream_t s);
 // variant 0: one block in flight per CTA; 1: next block prefetched
 void launch_integrate(const VolumeView &V, const CamParams &C, const uint2 *pix,
                       const float *pose, int grid, int variant, cudaStream_t s);
@@ -170,9 +181,10 @@ void launch_list_keys(const VolumeView &V, int32_t *xyz, uint32_t n, cudaStream_
 void launch_scatter_blocks(const VolumeView &V, const int32_t *xyz, const float *sdf,
                            const float *w, const uint8_t *rgb, uint32_t n, cudaStream_t s);
 
-// Bilateral pre-filter of one depth image into float metres (vh_filter.cu).
-void launch_depth_filter(const CamParams &C, const void *depth, int fmt, float *out,
-                         cudaStream_t s);
+// Bilateral pre-filter of one depth image into float metres (vh_filter.cu);
+// depth == nullptr reads the image of fin.
+void launch_depth_filter(const CamParams &C, const void *depth, const FrameIn *fin, int fmt,
+                         float *out, cudaStream_t s);
 
 // Batched stages: one launch covers the work of every active scene.
 // active[i] != 0: scene i has a frame this step.  px_start: first global

@@ -26,10 +26,12 @@ __device__ __forceinline__ float depth_at<float>(const float *d, int i, float) {
 }
 
 template <typename DepthT>
-__global__ void __launch_bounds__(256) k_depth_filter(CamParams C, const DepthT *__restrict__ in,
+__global__ void __launch_bounds__(256) k_depth_filter(CamParams C, const DepthT *__restrict__ depth,
+                                                      const FrameIn *__restrict__ fin,
                                                       float *__restrict__ out) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= C.width * C.height) return;
+  const DepthT *in = depth ? depth : static_cast<const DepthT *>(fin->depth);
   const int u = idx % C.width, v = idx / C.width;
   const float d0 = depth_at<DepthT>(in, idx, C.depth_scale);
   if (!(d0 > C.min_depth && d0 <= C.max_depth)) {
@@ -56,13 +58,13 @@ __global__ void __launch_bounds__(256) k_depth_filter(CamParams C, const DepthT 
 
 }  // namespace
 
-void launch_depth_filter(const CamParams &C, const void *depth, int fmt, float *out,
-                         cudaStream_t s) {
+void launch_depth_filter(const CamParams &C, const void *depth, const FrameIn *fin, int fmt,
+                         float *out, cudaStream_t s) {
   const unsigned grid = (unsigned)(((size_t)C.width * C.height + 255) / 256);
   if (fmt == 0)
-    k_depth_filter<uint16_t><<<grid, 256, 0, s>>>(C, static_cast<const uint16_t *>(depth), out);
+    k_depth_filter<uint16_t><<<grid, 256, 0, s>>>(C, static_cast<const uint16_t *>(depth), fin, out);
   else
-    k_depth_filter<float><<<grid, 256, 0, s>>>(C, static_cast<const float *>(depth), out);
+    k_depth_filter<float><<<grid, 256, 0, s>>>(C, static_cast<const float *>(depth), fin, out);
 }
 
 }  // namespace vh

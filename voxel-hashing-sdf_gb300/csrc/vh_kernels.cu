@@ -295,11 +295,11 @@ __device__ __forceinline__ void allocate_pixel(const VolumeView &V, const CamPar
 
 template <typename DepthT>
 __global__ void __launch_bounds__(256) k_allocate(VolumeView V, CamParams C,
+                                                  const FrameIn *__restrict__ fin,
                                                   const DepthT *__restrict__ depth,
-                                                  const uint8_t *__restrict__ rgb,
-                                                  const float *__restrict__ pose,
                                                   uint2 *__restrict__ pix) {
-  allocate_pixel<DepthT>(V, C, depth, rgb, pose, pix, blockIdx.x * blockDim.x + threadIdx.x);
+  const DepthT *d = depth ? depth : static_cast<const DepthT *>(fin->depth);
+  allocate_pixel<DepthT>(V, C, d, fin->rgb, fin->pose, pix, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ---- integration ---------------------------------------------------------------
@@ -1206,13 +1206,13 @@ void launch_epoch_end(const VolumeView &V, cudaStream_t s) { k_epoch_end<<<1, 32
 void launch_clear_list(const VolumeView &V, cudaStream_t s) { k_clear_list<<<1, 32, 0, s>>>(V); }
 void launch_mc_begin(const VolumeView &V, cudaStream_t s) { k_mc_begin<<<1, 32, 0, s>>>(V); }
 
-void launch_allocate(const VolumeView &V, const CamParams &C, const void *depth, int fmt,
-                     const uint8_t *rgb, const float *pose, uint2 *pix, cudaStream_t s) {
+void launch_allocate(const VolumeView &V, const CamParams &C, const FrameIn *fin,
+                     const void *depth, int fmt, uint2 *pix, cudaStream_t s) {
   const unsigned grid = grid_for((uint32_t)C.width * (uint32_t)C.height, 256);
   if (fmt == 0)
-    k_allocate<uint16_t><<<grid, 256, 0, s>>>(V, C, (const uint16_t *)depth, rgb, pose, pix);
+    k_allocate<uint16_t><<<grid, 256, 0, s>>>(V, C, fin, (const uint16_t *)depth, pix);
   else
-    k_allocate<float><<<grid, 256, 0, s>>>(V, C, (const float *)depth, rgb, pose, pix);
+    k_allocate<float><<<grid, 256, 0, s>>>(V, C, fin, (const float *)depth, pix);
 }
 
 int integrate_ctas_per_sm(int variant) {
