@@ -29,7 +29,6 @@
 using namespace vh;
 
 namespace {
-constexpr int kPoseRing = 64;
 constexpr int kNumEvents = 5;
 }  // namespace
 
@@ -47,12 +46,10 @@ struct vh_handle {
   float *d_depth_f = nullptr;  // filtered depth (VH_FLAG_DEPTH_FILTER)
   uint8_t *d_rgb = nullptr;
   FrameIn *d_fin = nullptr;    // the current frame's pose and image pointers
+  FrameIn fin{};               // the next frame's, passed to k_frame_begin
   uint2 *d_pix = nullptr;
   float4 *d_tris = nullptr;
   int64_t tri_cap = 0;
-  FrameIn *h_fin_ring = nullptr;  // pinned upload slots of d_fin
-  cudaEvent_t ring_ev[kPoseRing] = {};
-  int ring_pos = 0;
   // Host frames: two device slots filled on copy_stream, so the upload of a
   // frame overlaps the kernels of the one before.  in_copied[k] follows the
   // upload into slot k, in_consumed[k] the kernels of the frame that read it.
@@ -62,8 +59,11 @@ struct vh_handle {
   cudaEvent_t in_copied[2] = {}, in_consumed[2] = {};
   int in_pos = 0;
   int in_used = -1;  // slot read by the frame being enqueued (-1: device inputs)
-  DevState *h_state = nullptr;
+  DevState *h_state = nullptr;    // pinned, mapped
+  DevState *h_state_dev = nullptr;  // its device address (k_state_out)
   cudaGraphExec_t graphs[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  cudaGraph_t graph_src[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  cudaGraphNode_t graph_fb[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // k_frame_begin
   cudaEvent_t ev[kNumEvents] = {};
   bool ev_pending = false;
   bool ev_has_mc = false;
@@ -185,7 +185,7 @@ void stage_event(cudaEvent_t ev, cudaStream_t s, bool capturing) {
 void enqueue_frame(vh_handle *h, int fmt, bool with_mc, bool events, bool capturing) {
   cudaStream_t s = h->stream;
   if (events) stage_event(h->ev[0], s, capturing);
-  launch_frame_begin(h->V, s);
+  launch_frame_begin(h->V, &h->fin, h->d_fin, s);
   const void *depth = nullptr;  // the frame's own image, found through d_fin
   if (h->p.flags & VH_FLAG_DEPTH_FILTER) {
     launch_depth_filter(h->C, nullptr, h->d_fin, fmt, h->d_depth_f, s);
@@ -203,15 +203,20 @@ void enqueue_frame(vh_handle *h, int fmt, bool with_mc, bool events, bool captur
               h->tuning.mc_variant, s);
     if (events) stage_event(h->ev[3], s, capturing);
   }
+  // Without VH_FLAG_SYNC every frame still brings its counters to the host
+  // mirror (a 64-byte in-stream write to mapped memory, no copy on the stream).
+  if (!(h->p.flags & VH_FLAG_SYNC)) launch_state_out(h->V, h->h_state_dev, s);
 }
 
 void drop_graphs(vh_handle *h) {
-  for (auto &row : h->graphs)
-    for (auto &g : row)
-      if (g) {
-        cudaGraphExecDestroy(g);
-        g = nullptr;
-      }
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b) {
+      if (h->graphs[a][b]) cudaGraphExecDestroy(h->graphs[a][b]);
+      if (h->graph_src[a][b]) cudaGraphDestroy(h->graph_src[a][b]);
+      h->graphs[a][b] = nullptr;
+      h->graph_src[a][b] = nullptr;
+      h->graph_fb[a][b] = nullptr;
+    }
 }
 
 // Resolves a requested configuration against the occupancy limits.
@@ -236,19 +241,29 @@ vh_status run_frame(vh_handle *h, int fmt, bool with_mc) {
   const bool events = (h->p.flags & VH_FLAG_PROFILE) != 0;
   const bool graphs_ok = !(h->p.flags & VH_FLAG_NO_GRAPH) && h->stream != nullptr;
   if (graphs_ok) {
-    cudaGraphExec_t &g = h->graphs[fmt][with_mc ? 1 : 0];
-    if (!g) {
+    const int m = with_mc ? 1 : 0;
+    cudaGraphExec_t &g = h->graphs[fmt][m];
+    if (!g) {  // captured with this frame's descriptor
       cudaGraph_t graph = nullptr;
       VH_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
       enqueue_frame(h, fmt, with_mc, events, true);
       cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
       if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
       e = cudaGraphInstantiate(&g, graph, 0);
-      cudaGraphDestroy(graph);
       if (e != cudaSuccess) {
+        cudaGraphDestroy(graph);
         g = nullptr;
         return cuda_fail(h, e, "cudaGraphInstantiate");
       }
+      h->graph_src[fmt][m] = graph;  // its nodes address the parameter updates
+      h->graph_fb[fmt][m] = find_frame_begin_node(graph);
+      if (!h->graph_fb[fmt][m]) {
+        drop_graphs(h);
+        return fail(h, VH_ERR_CUDA, "frame graph without its begin node");
+      }
+    } else {
+      const cudaError_t e = update_frame_begin(g, h->graph_fb[fmt][m], h->V, h->fin, h->d_fin);
+      if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphExecKernelNodeSetParams");
     }
     VH_CUDA(h, cudaGraphLaunch(g, h->stream));
   } else {
@@ -257,21 +272,15 @@ vh_status run_frame(vh_handle *h, int fmt, bool with_mc) {
   }
   h->ev_pending = events;
   h->ev_has_mc = with_mc;
-  vh_status s = inputs_consumed(h);
-  if (s != VH_OK) return s;
-  // Without VH_FLAG_SYNC the frame's counters still come back to the host
-  // mirror (64 bytes, pinned) at the end of every frame.
-  if (!(h->p.flags & VH_FLAG_SYNC))
-    VH_CUDA(h, cudaMemcpyAsync(h->h_state, h->V.st, sizeof(DevState), cudaMemcpyDeviceToHost,
-                               h->stream));
-  return VH_OK;
+  return inputs_consumed(h);
 }
 
-// Makes one frame's inputs visible to the frame kernels through d_fin:
-// device images are read in place (the caller keeps them unchanged until the
-// frame's work on the handle's stream has run), host images are uploaded
-// into a staging slot on the copy stream, which the handle's stream waits
-// for.  The caller records inputs_consumed() after the frame's kernels.
+// Prepares one frame's descriptor (h->fin, written to d_fin by the frame's
+// first kernel): device images are read in place (the caller keeps them
+// unchanged until the frame's work on the handle's stream has run), host
+// images are uploaded into a staging slot on the copy stream, which the
+// handle's stream waits for.  run_frame records inputs_consumed() after the
+// frame's kernels.
 vh_status stage_inputs(vh_handle *h, const void *depth, int32_t fmt, const uint8_t *rgb,
                        const float *c2w, int32_t mem) {
   if (!depth || !rgb || !c2w) return fail(h, VH_ERR_INVALID_ARG, "null input pointer");
@@ -281,9 +290,7 @@ vh_status stage_inputs(vh_handle *h, const void *depth, int32_t fmt, const uint8
     return fail(h, VH_ERR_INVALID_ARG, "unknown memory kind");
   if (!finite_pose(c2w)) return fail(h, VH_ERR_NOT_FINITE, "camera pose has a non-finite entry");
   const size_t npx = (size_t)h->p.width * h->p.height;
-  // descriptor: host ring of pinned slots, each reused only after its copy ran
-  FrameIn *slot = h->h_fin_ring + h->ring_pos;
-  VH_CUDA(h, cudaEventSynchronize(h->ring_ev[h->ring_pos]));
+  FrameIn *slot = &h->fin;
   std::memcpy(slot->pose, c2w, 16 * sizeof(float));
   h->in_used = -1;
   if (mem == VH_MEM_DEVICE) {
@@ -304,9 +311,6 @@ vh_status stage_inputs(vh_handle *h, const void *depth, int32_t fmt, const uint8
     h->in_used = k;
     h->in_pos ^= 1;
   }
-  VH_CUDA(h, cudaMemcpyAsync(h->d_fin, slot, sizeof(FrameIn), cudaMemcpyHostToDevice, h->stream));
-  VH_CUDA(h, cudaEventRecord(h->ring_ev[h->ring_pos], h->stream));
-  h->ring_pos = (h->ring_pos + 1) % kPoseRing;
   return VH_OK;
 }
 
@@ -346,10 +350,7 @@ void free_all(vh_handle *h) {
   cudaFree(h->d_pix);
   cudaFree(h->d_tris);
   cudaFree(h->d_work);
-  if (h->h_fin_ring) cudaFreeHost(h->h_fin_ring);
   if (h->h_state) cudaFreeHost(h->h_state);
-  for (auto &e : h->ring_ev)
-    if (e) cudaEventDestroy(e);
   for (auto &e : h->ev)
     if (e) cudaEventDestroy(e);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
@@ -589,15 +590,13 @@ vh_status vh_create(const vh_params *p, vh_handle **out) {
             cudaMalloc(&h->d_in_rgb[1], 3 * npx) == cudaSuccess &&
             cudaMalloc(&h->d_pix, sizeof(uint2) * npx) == cudaSuccess &&
             cudaMalloc(&h->d_tris, sizeof(float4) * 3 * (size_t)(h->tri_cap ? h->tri_cap : 1)) == cudaSuccess &&
-            cudaMallocHost(&h->h_fin_ring, sizeof(FrameIn) * kPoseRing) == cudaSuccess &&
-            cudaMallocHost(&h->h_state, sizeof(DevState)) == cudaSuccess;
+            cudaHostAlloc(&h->h_state, sizeof(DevState), cudaHostAllocMapped) == cudaSuccess &&
+            cudaHostGetDevicePointer(&h->h_state_dev, h->h_state, 0) == cudaSuccess;
   if (!ok) {
     cudaGetLastError();
     h->last_error = "device allocation failed";
     return bail(VH_ERR_CUDA);
   }
-  for (auto &e : h->ring_ev)
-    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return bail(VH_ERR_CUDA);
   for (int k = 0; k < 2; ++k)
     if (cudaEventCreateWithFlags(&h->in_copied[k], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->in_consumed[k], cudaEventDisableTiming) != cudaSuccess)
@@ -606,7 +605,6 @@ vh_status vh_create(const vh_params *p, vh_handle **out) {
     return bail(VH_ERR_CUDA);
   for (auto &e : h->ev)
     if (cudaEventCreate(&e) != cudaSuccess) return bail(VH_ERR_CUDA);
-  for (int i = 0; i < kPoseRing; ++i) cudaEventRecord(h->ring_ev[i], h->stream);
   h->V.slot_mask = (uint32_t)(slots - 1);
   h->V.max_probe = p->max_probe;
   h->V.frame_cap = (uint32_t)p->max_frame_blocks;

@@ -141,20 +141,30 @@ struct SceneDesc {
 constexpr int kMaxBatchScenes = 1024;
 constexpr int kBatchPixelThreads = 256;  // threads of a batched allocation CTA
 
-// ---- host-side launchers (vh_kernels.cu) ----------------------------------
-void launch_frame_begin(const VolumeView &V, cudaStream_t s);
-void launch_epoch_end(const VolumeView &V, cudaStream_t s);
-void launch_clear_list(const VolumeView &V, cudaStream_t s);
-void launch_mc_begin(const VolumeView &V, cudaStream_t s);
 // The inputs of one frame as the kernels find them on the device: the
 // camera pose and where the depth and colour images live (the caller's own
-// device buffers, or the handle's staging copy of host images).  Uploaded
-// per frame, so a captured frame graph serves every frame.
+// device buffers, or the handle's staging copy of host images).  Written per
+// frame by k_frame_begin from its parameters, so a captured frame graph
+// serves every frame.
 struct FrameIn {
   float pose[16];  // row-major camera-to-world; the kernels read rows 0-2
   const void *depth;
   const uint8_t *rgb;
 };
+
+// ---- host-side launchers (vh_kernels.cu) ----------------------------------
+// fin (optional): the frame's descriptor, written to d_fin by the kernel.
+void launch_frame_begin(const VolumeView &V, const FrameIn *fin, FrameIn *d_fin, cudaStream_t s);
+// Copies the device counters to `host` (mapped pinned memory) in-stream.
+void launch_state_out(const VolumeView &V, DevState *host, cudaStream_t s);
+// The k_frame_begin node of a captured frame graph (nullptr if it has none),
+// and the per-launch update of its descriptor parameter.
+cudaGraphNode_t find_frame_begin_node(cudaGraph_t g);
+cudaError_t update_frame_begin(cudaGraphExec_t e, cudaGraphNode_t n, const VolumeView &V,
+                               const FrameIn &fin, FrameIn *d_fin);
+void launch_epoch_end(const VolumeView &V, cudaStream_t s);
+void launch_clear_list(const VolumeView &V, cudaStream_t s);
+void launch_mc_begin(const VolumeView &V, cudaStream_t s);
 
 // fmt: 0 = uint16 scaled by depth_scale, 1 = float metres.  depth (when not
 // null) replaces fin->depth, e.g. by the filtered copy.

@@ -25,6 +25,8 @@
 // Every loop is bounded (probe length <= max_probe, band walk <= the key
 // distance between its end blocks); no kernel waits on another thread.
 
+#include <vector>
+
 #include "vh_common.cuh"
 #include "vh_device.cuh"
 #include "vh_mc_tables.h"
@@ -848,8 +850,25 @@ __device__ void mc_begin_state(const VolumeView &V) {
   V.st->mc_next = 0;
 }
 
-__global__ void k_frame_begin(VolumeView V) {
+// Opens a frame: stamp and counters (thread 0) and, with d_fin set, the
+// frame's descriptor, passed by value so that a graph launch carries it in
+// its kernel parameters instead of a copy on the stream.
+__global__ void k_frame_begin(VolumeView V, FrameIn fin, FrameIn *d_fin) {
   if (threadIdx.x == 0) frame_begin_state(V);
+  if (d_fin) {
+    static_assert(sizeof(FrameIn) % 4 == 0, "word copy");
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(&fin);
+    uint32_t *dst = reinterpret_cast<uint32_t *>(d_fin);
+    for (int k = threadIdx.x; k < (int)(sizeof(FrameIn) / 4); k += blockDim.x) dst[k] = src[k];
+  }
+}
+
+// The device counters into host-mapped memory, at the end of a frame.
+__global__ void k_state_out(const DevState *__restrict__ st, DevState *host) {
+  static_assert(sizeof(DevState) % 4 == 0 && sizeof(DevState) / 4 <= 32, "one warp");
+  if (threadIdx.x < sizeof(DevState) / 4)
+    reinterpret_cast<volatile uint32_t *>(host)[threadIdx.x] =
+        reinterpret_cast<const uint32_t *>(st)[threadIdx.x];
 }
 
 __global__ void k_epoch_end(VolumeView V) {
@@ -1201,7 +1220,43 @@ inline unsigned grid_for(uint32_t n, unsigned threads) { return (n + threads - 1
 
 }  // namespace
 
-void launch_frame_begin(const VolumeView &V, cudaStream_t s) { k_frame_begin<<<1, 32, 0, s>>>(V); }
+void launch_frame_begin(const VolumeView &V, const FrameIn *fin, FrameIn *d_fin, cudaStream_t s) {
+  k_frame_begin<<<1, 32, 0, s>>>(V, fin ? *fin : FrameIn{}, fin ? d_fin : nullptr);
+}
+void launch_state_out(const VolumeView &V, DevState *host, cudaStream_t s) {
+  k_state_out<<<1, 32, 0, s>>>(V.st, host);
+}
+
+cudaGraphNode_t find_frame_begin_node(cudaGraph_t g) {
+  size_t n = 0;
+  if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess || n == 0) return nullptr;
+  std::vector<cudaGraphNode_t> nodes(n);
+  if (cudaGraphGetNodes(g, nodes.data(), &n) != cudaSuccess) return nullptr;
+  for (cudaGraphNode_t nd : nodes) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nd, &t) != cudaSuccess || t != cudaGraphNodeTypeKernel) continue;
+    cudaKernelNodeParams p{};
+    if (cudaGraphKernelNodeGetParams(nd, &p) != cudaSuccess) continue;
+    if (p.func == reinterpret_cast<void *>(k_frame_begin)) return nd;
+  }
+  return nullptr;
+}
+
+cudaError_t update_frame_begin(cudaGraphExec_t e, cudaGraphNode_t n, const VolumeView &V,
+                               const FrameIn &fin, FrameIn *d_fin) {
+  VolumeView v = V;
+  FrameIn f = fin;
+  FrameIn *d = d_fin;
+  void *args[3] = {&v, &f, &d};
+  cudaKernelNodeParams p{};
+  p.func = reinterpret_cast<void *>(k_frame_begin);
+  p.gridDim = dim3(1);
+  p.blockDim = dim3(32);
+  p.sharedMemBytes = 0;
+  p.kernelParams = args;
+  p.extra = nullptr;
+  return cudaGraphExecKernelNodeSetParams(e, n, &p);
+}
 void launch_epoch_end(const VolumeView &V, cudaStream_t s) { k_epoch_end<<<1, 32, 0, s>>>(V); }
 void launch_clear_list(const VolumeView &V, cudaStream_t s) { k_clear_list<<<1, 32, 0, s>>>(V); }
 void launch_mc_begin(const VolumeView &V, cudaStream_t s) { k_mc_begin<<<1, 32, 0, s>>>(V); }
