@@ -484,14 +484,19 @@ __global__ void __launch_bounds__(128, kPrefetch ? 8 : 12) k_integrate(VolumeVie
 
 // ---- marching cubes --------------------------------------------------------------
 constexpr int kH = 9;              // staged edge: 8 voxels + 1 halo
-constexpr int kH3 = kH * kH * kH;  // 729
+constexpr int kH3 = kH * kH * kH;  // 729 staged corners
 constexpr int kHalo = kH3 - kB3;   // 217
+// Staged layout x + 9 y + 88 z: the z pitch is 8 (mod 32) banks, so the 32
+// lanes of a warp, which classify 8 x by 4 z cubes of one y row, read 32
+// distinct banks for every corner.
+constexpr int kZPitch = 88;
+constexpr int kStaged = kZPitch * kH;  // 792 words
 constexpr int kMcThreads = 128;
 constexpr int kMaxCand = kB3 * 5;  // at most 5 triangles per cube
 
 struct McShared {
-  float sdf[kH3];  // NaN = corner unusable (absent block or low weight)
-  uint32_t rgb[kH3];
+  float sdf[kStaged];  // NaN = corner unusable (absent block or low weight)
+  uint32_t rgb[kStaged];
   uint16_t tri[256][5];  // triangle t of a case: edges e0 | e1 << 4 | e2 << 8
   uint16_t edge[256];
   uint8_t ntri[256];
@@ -505,7 +510,14 @@ struct McShared {
   uint32_t next[2];  // the block after the current one (double-buffered)
 };
 
-__device__ __forceinline__ int hidx(int x, int y, int z) { return x + kH * (y + kH * z); }
+__device__ __forceinline__ int hidx(int x, int y, int z) { return x + kH * y + kZPitch * z; }
+
+// Cube j (0..3) of thread t: x = t & 7, z = (t >> 3 & 3) + 4 (j >> 1),
+// y = (t >> 5) + 4 (j & 1); returns x + 8 y + 64 z.  All 512 cubes once.
+__device__ __forceinline__ int mc_cube(int t, int j) {
+  const int x = t & 7, z = ((t >> 3) & 3) + 4 * (j >> 1), y = (t >> 5) + 4 * (j & 1);
+  return x + 8 * y + 64 * z;
+}
 __device__ __forceinline__ int corner_dx(int k) { return (kMcCornerBitsX >> k) & 1; }
 __device__ __forceinline__ int corner_dy(int k) { return (kMcCornerBitsY >> k) & 1; }
 __device__ __forceinline__ int corner_dz(int k) { return (kMcCornerBitsZ >> k) & 1; }
@@ -743,7 +755,7 @@ __device__ __forceinline__ void mc_block(McShared &S, const VolumeView &V, int s
   int cs[4];
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    const int c = t + kMcThreads * j;
+    const int c = mc_cube(t, j);
     int ci = cube_case(S, c & 7, (c >> 3) & 7, c >> 6);
     if (ci < 0 || S.edge[ci] == 0) ci = 0;
     cs[j] = ci;
@@ -755,7 +767,7 @@ __device__ __forceinline__ void mc_block(McShared &S, const VolumeView &V, int s
   if (ncand == 0) return;  // uniform: nothing to emit in this block
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    const int c = t + kMcThreads * j;
+    const int c = mc_cube(t, j);
     const int nt = S.ntri[cs[j]];
     for (int tt = 0; tt < nt; ++tt) S.cand[off++] = (uint16_t)(c | (tt << 9));
   }
