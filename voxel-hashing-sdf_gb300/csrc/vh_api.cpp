@@ -193,7 +193,7 @@ void enqueue_frame(vh_handle *h, int fmt, bool with_mc, bool events, bool captur
     fmt = VH_DEPTH_F32_M;
   }
   launch_allocate(h->V, h->C, h->d_fin, depth, fmt, h->d_pix, s);
-  launch_frame_resolve(h->V, h->sm_count * 2, with_mc, s);
+  launch_frame_resolve(h->V, h->sm_count * 8, with_mc, s);  // probes in flight: many CTAs
   if (events) stage_event(h->ev[1], s, capturing);
   launch_integrate(h->V, h->C, h->d_pix, h->d_fin->pose, integrate_grid(h),
                    h->tuning.integrate_variant, s);

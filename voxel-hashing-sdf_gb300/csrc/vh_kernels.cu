@@ -54,14 +54,28 @@ __device__ __forceinline__ uint32_t ld_volatile(const uint32_t *p) {
   return *(volatile const uint32_t *)p;
 }
 
-// Claims or finds `key`. Returns the slot index or kNoBlock (table full).
-__device__ uint32_t slot_insert(const VolumeView &V, unsigned long long key, bool *created) {
+// Whole slot in one 16-byte access: {key, block | stamp << 32}.
+__device__ __forceinline__ ulonglong2 ld_volatile_slot(const Slot *p) {
+  ulonglong2 r;
+  asm volatile("ld.volatile.global.v2.u64 {%0, %1}, [%2];" : "=l"(r.x), "=l"(r.y) : "l"(p));
+  return r;
+}
+
+// Claims or finds `key`. Returns the slot index or kNoBlock (table full);
+// *stamp is the slot's frame stamp as the probe saw it (kNoBlock for a slot
+// claimed here or not found), so a caller can skip the stamp exchange when
+// the slot already carries the current frame.
+__device__ uint32_t slot_insert(const VolumeView &V, unsigned long long key, bool *created,
+                                uint32_t *stamp) {
   const uint32_t h = (uint32_t)mix64(key) & V.slot_mask;
+  *stamp = kNoBlock;
   for (int i = 0; i < V.max_probe; ++i) {
     const uint32_t s = (h + (uint32_t)i) & V.slot_mask;
-    unsigned long long k = ld_volatile(&V.slots[s].key);
+    const ulonglong2 sl = ld_volatile_slot(V.slots + s);
+    const unsigned long long k = sl.x;
     if (k == key) {
       *created = false;
+      *stamp = (uint32_t)(sl.y >> 32);
       return s;
     }
     if (k == kEmptyKey) {
@@ -114,13 +128,13 @@ __device__ __forceinline__ void assign_blocks(const VolumeView &V, bool created,
 
 // Called by every lane: stamps `slot` for this frame and appends it to the
 // frame list if this lane is the first to touch it (one atomic per warp).
+// `seen`: the slot's stamp as the probe read it (stamps only move forward
+// within a frame, so seen == frame means another lane already appended it).
 __device__ __forceinline__ void stamp_and_append(const VolumeView &V, bool leader, uint32_t slot,
-                                                 uint32_t frame) {
+                                                 uint32_t frame, uint32_t seen) {
   bool app = false;
-  if (leader && slot != kNoBlock) {
-    if (ld_volatile(&V.slots[slot].stamp) != frame)
-      app = atomicExch(&V.slots[slot].stamp, frame) != frame;
-  }
+  if (leader && slot != kNoBlock && seen != frame)
+    app = atomicExch(&V.slots[slot].stamp, frame) != frame;
   const unsigned am = __ballot_sync(kFull, app);
   if (!am) return;
   const int lane = threadIdx.x & 31;
@@ -287,16 +301,16 @@ __device__ __forceinline__ void allocate_pixel(const VolumeView &V, const CamPar
     const unsigned peers = __match_any_sync(kFull, key);
     const bool leader = active && (__ffs(peers) - 1) == lane;
     bool created = false;
-    uint32_t slot = kNoBlock;
-    if (leader) slot = slot_insert(V, key, &created);
+    uint32_t slot = kNoBlock, seen = kNoBlock;
+    if (leader) slot = slot_insert(V, key, &created, &seen);
     assign_blocks(V, created, slot, key, free0, top0);
-    stamp_and_append(V, leader, slot, frame);
+    stamp_and_append(V, leader, slot, frame, seen);
     if (active) active = walk_next(w);
   }
 }
 
 template <typename DepthT>
-__global__ void __launch_bounds__(256) k_allocate(VolumeView V, CamParams C,
+__global__ void __launch_bounds__(256, 8) k_allocate(VolumeView V, CamParams C,
                                                   const FrameIn *__restrict__ fin,
                                                   const DepthT *__restrict__ depth,
                                                   uint2 *__restrict__ pix) {
@@ -1122,10 +1136,10 @@ __global__ void __launch_bounds__(256) k_alloc_keys(VolumeView V, const int32_t 
   const unsigned peers = __match_any_sync(kFull, key);
   const bool leader = active && (__ffs(peers) - 1) == (int)(threadIdx.x & 31);
   bool created = false;
-  uint32_t slot = kNoBlock;
-  if (leader) slot = slot_insert(V, key, &created);
+  uint32_t slot = kNoBlock, seen = kNoBlock;
+  if (leader) slot = slot_insert(V, key, &created, &seen);
   assign_blocks(V, created, slot, key, free0, top0);
-  stamp_and_append(V, leader, slot, frame);
+  stamp_and_append(V, leader, slot, frame, seen);
 }
 
 __global__ void __launch_bounds__(256) k_find_keys(VolumeView V, const int32_t *__restrict__ xyz,
