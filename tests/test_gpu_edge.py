@@ -114,3 +114,40 @@ def test_external_stream(scene):
     for f in range(4):
         orc.integrate(*scene.render(f))
     assert vol.stats()["blocks_allocated"] == orc.num_blocks()
+
+
+def test_pipelined_frames_equal_synchronous_ones(scene):
+    """Asynchronous mode, frames submitted back to back: host frames go
+    through the two upload slots of the copy stream (pinned buffers, one per
+    frame), device frames are read in place; the volume, the last frame's
+    mesh and the counters (written to the host mirror in-stream) equal a
+    synchronous run of the same frames."""
+    import torch
+    from helpers import sorted_blocks
+    n = 12
+    frames = [scene.render(f) for f in range(n)]
+    ref = volume_for(scene)  # VH_FLAG_SYNC
+    for d, c, p in frames:
+        ref.process_frame(d, c, p)
+    want_st = ref.stats()
+    want_tris = sort_rows(tri_rows(*ref.mesh()))
+    vol = volume_for(scene, flags=0)
+    fmt = "u16" if frames[0][0].dtype == np.uint16 else "f32"
+    signed = np.int16 if fmt == "u16" else np.float32  # torch-friendly view of the bytes
+    keep = []
+    for f, (d, c, p) in enumerate(frames):
+        td, tc = torch.from_numpy(d.view(signed)), torch.from_numpy(c)
+        if f % 3 == 2:  # a device frame among host frames
+            dd, cc = td.cuda(), tc.cuda()
+        else:
+            dd, cc = td.pin_memory().numpy().view(d.dtype), tc.pin_memory().numpy()
+        keep.append((dd, cc))
+        vol.process_frame(dd, cc, p, depth_format=fmt)
+    vol.sync()
+    st = vol.stats()
+    for k in ("frames", "frame_blocks", "blocks_allocated", "voxels_updated", "triangles"):
+        assert st[k] == want_st[k], (k, st[k], want_st[k])
+    a, b = sorted_blocks(ref.export_blocks()), sorted_blocks(vol.export_blocks())
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+    assert np.array_equal(sort_rows(tri_rows(*vol.mesh())), want_tris)
