@@ -251,7 +251,7 @@ __device__ __forceinline__ bool solve6(const float *terms, float damp, float x[6
 // Increment of exp(xi) for xi = (v, w) in FP32: D = dR - I (entries of the
 // order of |w|, so FP32 keeps them to ~1e-9 absolute) and t = V v, with
 // dR = I + A W + B W^2, V = I + B W + C W^2, W^2 = w w^T - |w|^2 I.
-__device__ inline void exp_increment(const float xi[6], float D[9], float t[3]) {
+__device__ __forceinline__ void exp_increment(const float xi[6], float D[9], float t[3]) {
   const float w[3] = {xi[3], xi[4], xi[5]};
   const float th2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
   float A, B, Cc;
@@ -354,6 +354,10 @@ __global__ void __launch_bounds__(RefineShape<kFD>::kThreads, RefineShape<kFD>::
                    : 0.0f;
   };
   float d_next = depth_at(q_first + lane);
+  // Launched as a programmatic dependent of the previous step: everything
+  // above (the depth prefetch) may overlap that step's last CTA; the state
+  // and the partials are touched only after it has completed.
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   if (S->stopped) return;  // uniform: written only between launches
   for (int i = threadIdx.x; i < kRows * 12; i += blockDim.x) rows[i] = S->rows[i];
   if (kFD && threadIdx.x < 6) inv2eps[threadIdx.x] = S->inv2eps[threadIdx.x];
@@ -390,6 +394,8 @@ __global__ void __launch_bounds__(RefineShape<kFD>::kThreads, RefineShape<kFD>::
       add_terms(acc, T * s.phi, J);
     }
   }
+  // the next step may start its CTAs on the SMs this grid releases
+  asm volatile("griddepcontrol.launch_dependents;");
   const int G = (int)gridDim.x;
   cta_sum_terms<kThreads>(acc, partials + blockIdx.x, G);
   __threadfence();  // this CTA's partials before its count
@@ -663,22 +669,36 @@ void init_state(RefineState *S, const float *c2w, bool fd) {
       }
 }
 
-// Enqueues `n` step launches of one method.
+// Enqueues `n` step launches of one method; every step after the first is a
+// programmatic dependent launch of the one before (same stream; inside a
+// capture it becomes a programmatic graph edge), so its CTAs start as the
+// previous step's CTAs exit and wait in-kernel for that step to complete.
 template <bool kSolve>
-void enqueue_steps(vh_handle *h, RefineCtx *c, const void *depth, int fmt, int stride, bool fd,
-                   int grid, int n, cudaStream_t st) {
+cudaError_t enqueue_steps(vh_handle *h, RefineCtx *c, const void *depth, int fmt, int stride,
+                          bool fd, int grid, int n, cudaStream_t st) {
   const VolumeView V = vh::handle_view(h);
   CamParams C = vh::handle_cam(h);
   C.mc_min_weight = C.mc_min_weight < 1.0f ? 1.0f : C.mc_min_weight;  // observed corners only
   const float inv_voxel = 1.0f / C.voxel;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
   for (int i = 0; i < n; ++i) {
-    if (fd)
-      k_refine_step<true, kSolve><<<grid, RefineShape<true>::kThreads, 0, st>>>(
-          V, C, depth, fmt, stride, inv_voxel, c->d_state, c->d_partials, c->d_hist, c->hist_cap);
-    else
-      k_refine_step<false, kSolve><<<grid, RefineShape<false>::kThreads, 0, st>>>(
-          V, C, depth, fmt, stride, inv_voxel, c->d_state, c->d_partials, c->d_hist, c->hist_cap);
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(fd ? RefineShape<true>::kThreads : RefineShape<false>::kThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = i > 0 ? 1u : 0u;
+    const cudaError_t e =
+        fd ? cudaLaunchKernelEx(&cfg, k_refine_step<true, kSolve>, V, C, depth, fmt, stride,
+                                inv_voxel, c->d_state, c->d_partials, c->d_hist, c->hist_cap)
+           : cudaLaunchKernelEx(&cfg, k_refine_step<false, kSolve>, V, C, depth, fmt, stride,
+                                inv_voxel, c->d_state, c->d_partials, c->d_hist, c->hist_cap);
+    if (e != cudaSuccess) return e;
   }
+  return cudaSuccess;
 }
 
 }  // namespace
@@ -741,8 +761,8 @@ extern "C" vh_status vh_pose_normal_equations(vh_handle *h, const void *depth, i
   if (cudaMemcpyAsync(c->d_state, c->h_state, sizeof(RefineState), cudaMemcpyHostToDevice, st) !=
       cudaSuccess)
     return vh::handle_fail(h, VH_ERR_CUDA, "pose upload failed");
-  enqueue_steps<false>(h, c, d, depth_fmt, stride, fd, grid, 1, st);
-  if (cudaGetLastError() != cudaSuccess ||
+  if (enqueue_steps<false>(h, c, d, depth_fmt, stride, fd, grid, 1, st) != cudaSuccess ||
+      cudaGetLastError() != cudaSuccess ||
       cudaMemcpyAsync(c->h_state, c->d_state, sizeof(RefineState), cudaMemcpyDeviceToHost, st) !=
           cudaSuccess)
     return vh::handle_fail(h, VH_ERR_CUDA, "normal equations failed");
@@ -782,9 +802,9 @@ extern "C" vh_status vh_pose_refine(vh_handle *h, const void *depth, int32_t dep
     cudaGraph_t g = nullptr;
     if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
       return vh::handle_fail(h, VH_ERR_CUDA, "refinement capture failed");
-    enqueue_steps<true>(h, c, d, depth_fmt, stride, fd, grid, iterations, st);
+    const cudaError_t le = enqueue_steps<true>(h, c, d, depth_fmt, stride, fd, grid, iterations, st);
     const cudaError_t e = cudaStreamEndCapture(st, &g);
-    if (e != cudaSuccess || cudaGraphInstantiate(&c->graph, g, 0) != cudaSuccess) {
+    if (le != cudaSuccess || e != cudaSuccess || cudaGraphInstantiate(&c->graph, g, 0) != cudaSuccess) {
       if (g) cudaGraphDestroy(g);
       c->graph = nullptr;
       return vh::handle_fail(h, VH_ERR_CUDA, "refinement graph failed");
