@@ -248,14 +248,40 @@ __device__ __forceinline__ float load_depth<float>(const float *d, int i, float)
 }
 
 // ---- allocation ----------------------------------------------------------------
+constexpr int kAllocChunk = 4;  // band steps of a warp collected before one resolve pass
+
+// Resolves the warp's collected keys (wkeys[0, nkeys), shared, warp-private)
+// in rounds of 32: probe or claim, hand out pool blocks, stamp and append.
+// All rounds' probes are independent, so a warp pays one dependent chain per
+// round instead of one per band step.  A key listed twice (two band steps
+// of different lanes) is settled by the claim CAS and the stamp exchange.
+__device__ __forceinline__ void resolve_keys(const VolumeView &V, const unsigned long long *wkeys,
+                                             int nkeys, uint32_t frame, uint32_t free0,
+                                             uint32_t top0) {
+  const int lane = threadIdx.x & 31;
+  for (int base = 0; base < nkeys; base += 32) {  // warp-uniform
+    const bool has = base + lane < nkeys;
+    const unsigned long long key = has ? wkeys[base + lane] : kEmptyKey;
+    const unsigned peers = __match_any_sync(kFull, key);
+    const bool leader = has && (__ffs(peers) - 1) == lane;
+    bool created = false;
+    uint32_t slot = kNoBlock, seen = kNoBlock;
+    if (leader) slot = slot_insert(V, key, &created, &seen);
+    assign_blocks(V, created, slot, key, free0, top0);
+    stamp_and_append(V, leader, slot, frame, seen);
+  }
+}
+
 // Pixel idx of one frame (all 32 lanes of the warp take part: the band walk
 // is de-duplicated per warp).  Lanes with idx >= npx only follow the warp.
+// wkeys: this warp's 32 * kAllocChunk key slots in shared memory.
 template <typename DepthT>
 __device__ __forceinline__ void allocate_pixel(const VolumeView &V, const CamParams &C,
                                                const DepthT *__restrict__ depth,
                                                const uint8_t *__restrict__ rgb,
                                                const float *__restrict__ pose,
-                                               uint2 *__restrict__ pix, int idx) {
+                                               uint2 *__restrict__ pix, int idx,
+                                               unsigned long long *wkeys) {
   const int npx = C.width * C.height;
   const int lane = threadIdx.x & 31;
   float P[12];
@@ -296,26 +322,35 @@ __device__ __forceinline__ void allocate_pixel(const VolumeView &V, const CamPar
       }
     }
   }
+  // Collect each band step's warp-unique keys; resolve them when the list
+  // could not take another step's 32, and at the end.
+  int nkeys = 0;  // warp-uniform
   while (__any_sync(kFull, active)) {
     const unsigned long long key = active ? pack_key(w.cx, w.cy, w.cz) : kEmptyKey;
     const unsigned peers = __match_any_sync(kFull, key);
     const bool leader = active && (__ffs(peers) - 1) == lane;
-    bool created = false;
-    uint32_t slot = kNoBlock, seen = kNoBlock;
-    if (leader) slot = slot_insert(V, key, &created, &seen);
-    assign_blocks(V, created, slot, key, free0, top0);
-    stamp_and_append(V, leader, slot, frame, seen);
+    const unsigned lm = __ballot_sync(kFull, leader);
+    if (leader) wkeys[nkeys + __popc(lm & lanemask_lt())] = key;
+    nkeys += __popc(lm);
     if (active) active = walk_next(w);
+    if (nkeys > 32 * (kAllocChunk - 1) || !__any_sync(kFull, active)) {
+      __syncwarp();
+      resolve_keys(V, wkeys, nkeys, frame, free0, top0);
+      __syncwarp();
+      nkeys = 0;
+    }
   }
 }
 
 template <typename DepthT>
-__global__ void __launch_bounds__(256, 8) k_allocate(VolumeView V, CamParams C,
+__global__ void __launch_bounds__(256, 6) k_allocate(VolumeView V, CamParams C,
                                                   const FrameIn *__restrict__ fin,
                                                   const DepthT *__restrict__ depth,
                                                   uint2 *__restrict__ pix) {
+  __shared__ unsigned long long keys[256 / 32][32 * kAllocChunk];
   const DepthT *d = depth ? depth : static_cast<const DepthT *>(fin->depth);
-  allocate_pixel<DepthT>(V, C, d, fin->rgb, fin->pose, pix, blockIdx.x * blockDim.x + threadIdx.x);
+  allocate_pixel<DepthT>(V, C, d, fin->rgb, fin->pose, pix, blockIdx.x * blockDim.x + threadIdx.x,
+                         keys[threadIdx.x >> 5]);
 }
 
 // ---- integration ---------------------------------------------------------------
@@ -981,8 +1016,10 @@ __global__ void __launch_bounds__(kBatchPixelThreads) k_batch_allocate(
   const int s = scene_of(px_start, n, g0);
   if (!active[s]) return;  // CTA-uniform
   load_scene(sd, d, s);
+  __shared__ unsigned long long keys[kBatchPixelThreads / 32][32 * kAllocChunk];
   allocate_pixel<DepthT>(sd.V, sd.C, static_cast<const DepthT *>(sd.depth), sd.rgb, sd.pose,
-                         sd.pix, (int)(g0 + threadIdx.x - __ldg(px_start + s)));
+                         sd.pix, (int)(g0 + threadIdx.x - __ldg(px_start + s)),
+                         keys[threadIdx.x >> 5]);
 }
 
 // Closes every active scene's allocation epoch and writes the prefix of the
