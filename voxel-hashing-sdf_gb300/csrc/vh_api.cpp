@@ -3,11 +3,15 @@
 // The reference's processFrame (src/tsdf.cu:1484-1598) rebuilds two hash
 // tables, streams host chunks in, runs three kernels with blocking copies in
 // between and streams everything back out every frame.  Here the volume stays
-// resident in HBM; a frame is three host->device copies into fixed staging
-// buffers followed by one CUDA graph:
-//     frame_begin -> allocate -> epoch_end -> integrate [-> mc_begin -> mc]
-// All counts stay on the device; the host reads the state block only when a
-// call has to report something (VH_FLAG_SYNC, stats, mesh copies).
+// resident in HBM; a frame is one CUDA graph
+//     frame_begin -> allocate -> resolve -> integrate [-> mc] [-> state_out]
+// whose first kernel carries the frame's descriptor (pose, image addresses)
+// as a parameter updated per launch.  Device images are read in place; host
+// images are uploaded on a copy stream into one of two staging slots,
+// overlapping the previous frame.  All counts stay on the device; the host
+// reads the state block only when a call has to report something
+// (VH_FLAG_SYNC, stats, mesh copies), and without VH_FLAG_SYNC state_out
+// writes it to mapped host memory at the end of every frame.
 
 #include <algorithm>
 #include <cmath>

@@ -2,19 +2,23 @@
 //
 //   k_allocate   one thread per pixel: walks the blocks of the pixel's
 //                truncation band, de-duplicates keys across the warp with
-//                __match_any_sync, claims new keys with one atomicCAS, hands
-//                out pool blocks with one warp-aggregated atomic, stamps each
-//                touched slot once per frame and appends it to the frame list
-//                (replaces HashAssignKernel, src/tsdf.cu:2088-2238, and the
-//                locked insert of include/vhashing.h:205-239,394-484).
+//                __match_any_sync, collects the warp's keys in shared memory
+//                and resolves them in rounds of 32: claims new keys with one
+//                atomicCAS, hands out pool blocks with one warp-aggregated
+//                atomic, stamps each touched slot once per frame and appends
+//                it to the frame list (replaces HashAssignKernel,
+//                src/tsdf.cu:2088-2238, and the locked insert of
+//                include/vhashing.h:205-239,394-484).
+//   k_frame_resolve  the frame list's slots and +x/+y/+z neighbours, 8 threads
+//                per entry; also closes the allocation epoch.
 //   k_integrate  persistent CTAs of 128 threads, one voxel block per CTA
 //                iteration, four voxels per thread with 16-byte loads and
 //                stores of sdf, weight and colour (replaces
 //                IntegrateHashKernel, src/tsdf.cu:599-751).
-//   k_mc         persistent CTAs: one block plus its +x/+y/+z halo staged in
-//                shared memory (7 hash probes per block instead of up to 16
-//                per voxel), cube cases counted, a CTA-wide scan compacts the
-//                triangles into one output range (replaces
+//   k_mc         persistent CTAs, blocks handed out by a counter: one block
+//                plus its +x/+y/+z halo staged in shared memory (no hash
+//                probe per voxel), cube cases counted, CTA-wide scans compact
+//                the triangles into one output range per round (replaces
 //                marchingCubeHashKernel, src/tsdf.cu:884-1110).
 //
 // This file is compiled with -fmad=false: every fp32 operation that decides a
