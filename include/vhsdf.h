@@ -412,6 +412,17 @@ vh_status vh_pose_normal_equations(vh_handle *h, const void *depth, int32_t dept
 vh_status vh_pose_refine(vh_handle *h, const void *depth, int32_t depth_fmt, int32_t mem,
                          const float *c2w_init, int32_t iterations, int32_t stride,
                          int32_t method, float *c2w_out, vh_refine_stats *stats);
+/* Batched refinement (keyframe windows): n poses, each against its own depth
+ * image (depth[i], all in `mem` and one format), refined together by the
+ * adjoint method - one launch per Gauss-Newton step for all n, the GPU's
+ * CTAs split evenly among them, each pose solved by its own last CTA.
+ * c2w_init / c2w_out: n * 16 floats (host); stats: n entries or NULL (ms and
+ * ms_steps are the whole batch's).  With n = 1 the result equals
+ * vh_pose_refine(..., VH_REFINE_ADJOINT, ...) bit for bit. */
+#define VH_REFINE_BATCH_MAX 256
+vh_status vh_pose_refine_batch(vh_handle *h, const void *const *depth, int32_t depth_fmt,
+                               int32_t mem, int32_t n, const float *c2w_init, int32_t iterations,
+                               int32_t stride, float *c2w_out, vh_refine_stats *stats);
 /* Vector-Jacobian product of the last integration update (depth image and
  * pose c2w of that frame): given dL/dsdf for every voxel of the frame's
  * block list (vh_block_list order, 512 values per block, index x + 8y +

@@ -269,3 +269,39 @@ def test_integration_vjp_against_fp64_finite_differences(gpu):
     fdp = (loss(d1, moved(1)) - loss(d1, moved(-1))) / (2 * h)
     anp = float(np.dot(gp.astype(np.float64), xi))
     assert abs(fdp - anp) < 2e-2 * max(1.0, abs(fdp)), (fdp, anp)
+
+
+def test_batched_refinement(room):
+    """vh_pose_refine_batch: one pose equals vh_pose_refine bit for bit; four
+    keyframes refined in one launch per step land on their single-pose
+    results (the partial sums split over other CTAs, so float-close, not
+    bit-equal), repeat to the bit, and agree for host and device depths."""
+    import torch
+    scene, vol, orc, e = room
+    frames = [scene.render(f) for f in (3, 6, 10, 14)]
+    inits = [perturb(gt, 2.0, 0.02, 40 + i) for i, (_, _, gt) in enumerate(frames)]
+    d0 = frames[0][0]
+    one, st1 = vol.pose_refine_batch([d0], [inits[0]], iterations=20, stride=2)
+    ref, st_ref = vol.pose_refine(d0, inits[0], iterations=20, stride=2, method="adjoint")
+    assert np.array_equal(one[0], ref)
+    assert st1[0]["iterations"] == st_ref["iterations"]
+    assert st1[0]["final_rmse"] == st_ref["final_rmse"]
+    depths = [d for d, _, _ in frames]
+    got, st = vol.pose_refine_batch(depths, inits, iterations=20, stride=2)
+    again, _ = vol.pose_refine_batch(depths, inits, iterations=20, stride=2)
+    assert np.array_equal(got, again)
+    u16 = depths[0].dtype == np.uint16  # int16 tensors carry the uint16 bytes
+    dev = [torch.from_numpy(d.view(np.int16) if u16 else d).cuda() for d in depths]
+    got_d, _ = vol.pose_refine_batch(dev, inits, iterations=20, stride=2,
+                                     depth_format="u16" if u16 else None)
+    assert np.array_equal(got, got_d)
+    for i, (d, _, gt) in enumerate(frames):
+        single, _ = vol.pose_refine(d, inits[i], iterations=20, stride=2, method="adjoint")
+        dt = np.linalg.norm(got[i][:3, 3].astype(np.float64) - single[:3, 3])
+        # small rotation differences from the skew part (arccos of the trace
+        # has a ~0.02 deg floor for float32 matrices)
+        dR = got[i][:3, :3].astype(np.float64) @ single[:3, :3].T.astype(np.float64)
+        w = 0.5 * np.array([dR[2, 1] - dR[1, 2], dR[0, 2] - dR[2, 0], dR[1, 0] - dR[0, 1]])
+        ang = np.degrees(np.arcsin(min(1.0, np.linalg.norm(w))))
+        assert dt < 1e-4 and ang < 5e-3, (i, dt, ang)
+        assert st[i]["final_rmse"] < st[i]["initial_rmse"]

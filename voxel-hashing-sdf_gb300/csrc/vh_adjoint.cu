@@ -326,15 +326,22 @@ struct RefineShape {
 // One Gauss-Newton step.  Every CTA accumulates the 29 normal-equation terms
 // of its pixels (analytic Jacobians T [g ; X x g] from the sampling adjoint,
 // or, for kFD, central differences of 13 residual evaluations per pixel) and
-// stores them in partials[k * gridDim.x + blockIdx.x]; the last CTA to finish
-// sums the partials in a fixed order (deterministic), and with kSolve solves
-// the 6x6 system and composes exp(xi) * pose (the pose itself in FP64).  No
-// CTA waits for another.
+// stores them in partials[k * G + cta]; the last CTA to finish sums the
+// partials in a fixed order (deterministic), and with kSolve solves the 6x6
+// system and composes exp(xi) * pose (the pose itself in FP64).  No CTA waits
+// for another.
+//
+// Jobs: with job_ctas > 0 the grid refines gridDim.x / job_ctas independent
+// poses (keyframes) at once: CTA b works for job b / job_ctas as its CTA
+// b % job_ctas of G = job_ctas, with the job's depth image depth_tab[job],
+// state S[job], partials and history; the job's last CTA solves its pose.
+// job_ctas = 0 is the single pose (G = gridDim.x, `depth`).
 template <bool kFD, bool kSolve>
 __global__ void __launch_bounds__(RefineShape<kFD>::kThreads, RefineShape<kFD>::kMinCtas)
-    k_refine_step(VolumeView V, CamParams C, const void *depth, int fmt, int stride,
-                  float inv_voxel, RefineState *S, float *__restrict__ partials,
-                  float2 *__restrict__ hist, int hist_cap) {
+    k_refine_step(VolumeView V, CamParams C, const void *depth, const void *const *depth_tab,
+                  int fmt, int stride, float inv_voxel, RefineState *S,
+                  float *__restrict__ partials, float2 *__restrict__ hist, int hist_cap,
+                  int job_ctas) {
   constexpr int kThreads = RefineShape<kFD>::kThreads;
   constexpr int kRows = kFD ? kFdPoses : 1;
   __shared__ float rows[kRows * 12];
@@ -346,8 +353,15 @@ __global__ void __launch_bounds__(RefineShape<kFD>::kThreads, RefineShape<kFD>::
   const int ws = (C.width + stride - 1) / stride, hs = (C.height + stride - 1) / stride;
   const int npx = ws * hs;
   const int lane = threadIdx.x & 31;
-  const int wstride = gridDim.x * blockDim.x;
-  const int q_first = blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+  const int job = job_ctas ? (int)blockIdx.x / job_ctas : 0;
+  const int cta = job_ctas ? (int)blockIdx.x % job_ctas : (int)blockIdx.x;
+  const int G = job_ctas ? job_ctas : (int)gridDim.x;
+  if (depth_tab) depth = depth_tab[job];
+  S += job;
+  partials += (size_t)job * kTerms * G;
+  if (hist) hist += (size_t)job * hist_cap;
+  const int wstride = G * blockDim.x;
+  const int q_first = cta * blockDim.x + (threadIdx.x & ~31);
   auto depth_at = [&](int q) {
     return q < npx ? pixel_depth(depth, fmt, ((q / ws) * stride) * C.width + (q % ws) * stride,
                                  C.depth_scale)
@@ -396,11 +410,10 @@ __global__ void __launch_bounds__(RefineShape<kFD>::kThreads, RefineShape<kFD>::
   }
   // the next step may start its CTAs on the SMs this grid releases
   asm volatile("griddepcontrol.launch_dependents;");
-  const int G = (int)gridDim.x;
-  cta_sum_terms<kThreads>(acc, partials + blockIdx.x, G);
+  cta_sum_terms<kThreads>(acc, partials + cta, G);
   __threadfence();  // this CTA's partials before its count
   __syncthreads();
-  if (threadIdx.x == 0) last = atomicAdd(&S->counter, 1u) == gridDim.x - 1;
+  if (threadIdx.x == 0) last = atomicAdd(&S->counter, 1u) == (uint32_t)G - 1u;
   __syncthreads();
   if (!last) return;
   __threadfence();
@@ -567,11 +580,30 @@ struct RefineCtx {
   cudaEvent_t ev[4] = {};
   cudaGraphExec_t graph = nullptr;
   long long key[7] = {};  // method, stride, iterations, fmt, grid, stream, partial buffer
+  // batched refinement (vh_pose_refine_batch): per-job states, partials,
+  // histories, depth staging and the device table of depth images
+  RefineState *d_bstate = nullptr, *h_bstate = nullptr;
+  float *d_bpartials = nullptr;
+  float2 *d_bhist = nullptr, *h_bhist = nullptr;
+  const void **d_btab = nullptr, **h_btab = nullptr;
+  char *d_bdepth = nullptr;
+  size_t bstate_cap = 0, bpartial_cap = 0, bhist_cap = 0, btab_cap = 0, bdepth_cap = 0;
+  cudaGraphExec_t bgraph = nullptr;
+  long long bkey[9] = {};
 };
 
 void refine_ctx_free(RefineCtx *c) {
   if (!c) return;
   if (c->graph) cudaGraphExecDestroy(c->graph);
+  if (c->bgraph) cudaGraphExecDestroy(c->bgraph);
+  cudaFree(c->d_bstate);
+  cudaFree(c->d_bpartials);
+  cudaFree(c->d_bhist);
+  cudaFree(c->d_btab);
+  cudaFree(c->d_bdepth);
+  if (c->h_bstate) cudaFreeHost(c->h_bstate);
+  if (c->h_bhist) cudaFreeHost(c->h_bhist);
+  if (c->h_btab) cudaFreeHost(c->h_btab);
   cudaFree(c->d_state);
   cudaFree(c->d_partials);
   cudaFree(c->d_hist);
@@ -692,13 +724,123 @@ cudaError_t enqueue_steps(vh_handle *h, RefineCtx *c, const void *depth, int fmt
     cfg.attrs = attr;
     cfg.numAttrs = i > 0 ? 1u : 0u;
     const cudaError_t e =
-        fd ? cudaLaunchKernelEx(&cfg, k_refine_step<true, kSolve>, V, C, depth, fmt, stride,
-                                inv_voxel, c->d_state, c->d_partials, c->d_hist, c->hist_cap)
-           : cudaLaunchKernelEx(&cfg, k_refine_step<false, kSolve>, V, C, depth, fmt, stride,
-                                inv_voxel, c->d_state, c->d_partials, c->d_hist, c->hist_cap);
+        fd ? cudaLaunchKernelEx(&cfg, k_refine_step<true, kSolve>, V, C, depth,
+                                (const void *const *)nullptr, fmt, stride, inv_voxel, c->d_state,
+                                c->d_partials, c->d_hist, c->hist_cap, 0)
+           : cudaLaunchKernelEx(&cfg, k_refine_step<false, kSolve>, V, C, depth,
+                                (const void *const *)nullptr, fmt, stride, inv_voxel, c->d_state,
+                                c->d_partials, c->d_hist, c->hist_cap, 0);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
+}
+
+// Enqueues `n` batched adjoint steps (jobs of job_ctas CTAs each), chained
+// as programmatic dependent launches like enqueue_steps.
+cudaError_t enqueue_batch_steps(vh_handle *h, RefineCtx *c, int fmt, int stride, int grid,
+                                int job_ctas, int hist_cap, int n, cudaStream_t st) {
+  const VolumeView V = vh::handle_view(h);
+  CamParams C = vh::handle_cam(h);
+  C.mc_min_weight = C.mc_min_weight < 1.0f ? 1.0f : C.mc_min_weight;
+  const float inv_voxel = 1.0f / C.voxel;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  for (int i = 0; i < n; ++i) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(RefineShape<false>::kThreads);
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = i > 0 ? 1u : 0u;
+    const cudaError_t e = cudaLaunchKernelEx(
+        &cfg, k_refine_step<false, true>, V, C, (const void *)nullptr,
+        (const void *const *)c->d_btab, fmt, stride, inv_voxel, c->d_bstate, c->d_bpartials,
+        c->d_bhist, hist_cap, job_ctas);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// Grows the batched-refinement buffers (the cached batch graph holds their
+// addresses, so it goes when one is reallocated).
+vh_status refine_batch_buffers(vh_handle *h, RefineCtx *c, size_t jobs, size_t partials,
+                               size_t hist, size_t depth_bytes) {
+  const bool grow = jobs > c->bstate_cap || partials > c->bpartial_cap || hist > c->bhist_cap ||
+                    jobs > c->btab_cap || depth_bytes > c->bdepth_cap;
+  if (!grow) return VH_OK;
+  if (cudaStreamSynchronize(vh::handle_stream(h)) != cudaSuccess)
+    return vh::handle_fail(h, VH_ERR_CUDA, "stream failed");
+  if (c->bgraph) {
+    cudaGraphExecDestroy(c->bgraph);
+    c->bgraph = nullptr;
+  }
+  bool ok = true;
+  if (jobs > c->bstate_cap) {
+    cudaFree(c->d_bstate);
+    if (c->h_bstate) cudaFreeHost(c->h_bstate);
+    c->d_bstate = nullptr;
+    c->h_bstate = nullptr;
+    c->bstate_cap = 0;
+    ok = ok && cudaMalloc(&c->d_bstate, sizeof(RefineState) * jobs) == cudaSuccess &&
+         cudaMallocHost(&c->h_bstate, sizeof(RefineState) * jobs) == cudaSuccess;
+    if (ok) c->bstate_cap = jobs;
+  }
+  if (ok && jobs > c->btab_cap) {
+    cudaFree(c->d_btab);
+    if (c->h_btab) cudaFreeHost(c->h_btab);
+    c->d_btab = nullptr;
+    c->h_btab = nullptr;
+    c->btab_cap = 0;
+    ok = cudaMalloc(&c->d_btab, sizeof(void *) * jobs) == cudaSuccess &&
+         cudaMallocHost(&c->h_btab, sizeof(void *) * jobs) == cudaSuccess;
+    if (ok) c->btab_cap = jobs;
+  }
+  if (ok && partials > c->bpartial_cap) {
+    cudaFree(c->d_bpartials);
+    c->d_bpartials = nullptr;
+    c->bpartial_cap = 0;
+    ok = cudaMalloc(&c->d_bpartials, sizeof(float) * partials) == cudaSuccess;
+    if (ok) c->bpartial_cap = partials;
+  }
+  if (ok && hist > c->bhist_cap) {
+    cudaFree(c->d_bhist);
+    if (c->h_bhist) cudaFreeHost(c->h_bhist);
+    c->d_bhist = nullptr;
+    c->h_bhist = nullptr;
+    c->bhist_cap = 0;
+    ok = cudaMalloc(&c->d_bhist, sizeof(float2) * hist) == cudaSuccess &&
+         cudaMallocHost(&c->h_bhist, sizeof(float2) * hist) == cudaSuccess;
+    if (ok) c->bhist_cap = hist;
+  }
+  if (ok && depth_bytes > c->bdepth_cap) {
+    cudaFree(c->d_bdepth);
+    c->d_bdepth = nullptr;
+    c->bdepth_cap = 0;
+    ok = cudaMalloc(&c->d_bdepth, depth_bytes) == cudaSuccess;
+    if (ok) c->bdepth_cap = depth_bytes;
+  }
+  if (!ok) {
+    cudaGetLastError();
+    return vh::handle_fail(h, VH_ERR_CUDA, "batched refinement allocation failed");
+  }
+  return VH_OK;
+}
+
+// Stats of one refinement from its final state and linearisation history.
+void fill_refine_stats(const RefineState &S, const float2 *hist, int iterations, float ms,
+                       float ms_steps, vh_refine_stats *stats) {
+  const int lin = S.iter < iterations ? S.iter : iterations;  // linearisations recorded
+  auto rmse = [&](int i) {
+    const float2 v = hist[i];
+    return v.y > 0.0f ? std::sqrt(v.x / v.y) : 0.0f;
+  };
+  stats->iterations = S.updates;
+  stats->valid_pixels = lin > 0 ? (int32_t)hist[lin - 1].y : 0;
+  stats->initial_rmse = lin > 0 ? rmse(0) : 0.0f;
+  stats->final_rmse = lin > 0 ? rmse(lin - 1) : 0.0f;
+  stats->ms = ms;
+  stats->ms_steps = ms_steps;
 }
 
 }  // namespace
@@ -829,20 +971,104 @@ extern "C" vh_status vh_pose_refine(vh_handle *h, const void *depth, int32_t dep
   c2w_out[12] = c2w_out[13] = c2w_out[14] = 0.0f;
   c2w_out[15] = 1.0f;
   if (stats) {
-    const int lin = S.iter < iterations ? S.iter : iterations;  // linearisations recorded
-    auto rmse = [&](int i) {
-      const float2 v = c->h_hist[i];
-      return v.y > 0.0f ? std::sqrt(v.x / v.y) : 0.0f;
-    };
-    stats->iterations = S.updates;
-    stats->valid_pixels = lin > 0 ? (int32_t)c->h_hist[lin - 1].y : 0;
-    stats->initial_rmse = lin > 0 ? rmse(0) : 0.0f;
-    stats->final_rmse = lin > 0 ? rmse(lin - 1) : 0.0f;
     float ms = 0.0f, ms_steps = 0.0f;
     cudaEventElapsedTime(&ms, c->ev[0], c->ev[3]);
     cudaEventElapsedTime(&ms_steps, c->ev[1], c->ev[2]);
-    stats->ms = ms;
-    stats->ms_steps = ms_steps;
+    fill_refine_stats(S, c->h_hist, iterations, ms, ms_steps, stats);
+  }
+  return VH_OK;
+}
+
+extern "C" vh_status vh_pose_refine_batch(vh_handle *h, const void *const *depth,
+                                          int32_t depth_fmt, int32_t mem, int32_t n,
+                                          const float *c2w_init, int32_t iterations,
+                                          int32_t stride, float *c2w_out,
+                                          vh_refine_stats *stats) {
+  if (!h || !depth || !c2w_init || !c2w_out || n < 1 || n > VH_REFINE_BATCH_MAX ||
+      iterations < 0 || iterations > (1 << 16) || stride < 1)
+    return VH_ERR_INVALID_ARG;
+  if (depth_fmt != VH_DEPTH_U16_MM && depth_fmt != VH_DEPTH_F32_M) return VH_ERR_INVALID_ARG;
+  if (mem != VH_MEM_HOST && mem != VH_MEM_DEVICE) return VH_ERR_INVALID_ARG;
+  for (int i = 0; i < n; ++i)
+    if (!depth[i]) return VH_ERR_INVALID_ARG;
+  for (int i = 0; i < 16 * n; ++i)
+    if (!std::isfinite(c2w_init[i])) return VH_ERR_NOT_FINITE;
+  const cudaStream_t st = vh::handle_stream(h);
+  const CamParams C = vh::handle_cam(h);
+  const size_t img = (size_t)C.width * C.height * (depth_fmt == VH_DEPTH_U16_MM ? 2 : 4);
+  const int full = refine_grid(h, stride, false);
+  const int job_ctas = full / n > 0 ? full / n : 1;
+  const int grid = n * job_ctas;
+  const int hcap = iterations > 0 ? iterations : 1;  // per-job history entries
+  RefineCtx *c = nullptr;
+  vh_status s = refine_ctx(h, full, iterations, &c);
+  if (s != VH_OK) return s;
+  s = refine_batch_buffers(h, c, (size_t)n, (size_t)kTerms * grid, (size_t)n * hcap,
+                           mem == VH_MEM_HOST ? img * n : 0);
+  if (s != VH_OK) return s;
+  cudaEventRecord(c->ev[0], st);
+  // depth images: the caller's device buffers, or staged host images
+  for (int i = 0; i < n; ++i) {
+    if (mem == VH_MEM_DEVICE) {
+      c->h_btab[i] = depth[i];
+    } else {
+      if (cudaMemcpyAsync(c->d_bdepth + img * i, depth[i], img, cudaMemcpyHostToDevice, st) !=
+          cudaSuccess)
+        return vh::handle_fail(h, VH_ERR_CUDA, "depth upload failed");
+      c->h_btab[i] = c->d_bdepth + img * i;
+    }
+    init_state(c->h_bstate + i, c2w_init + 16 * i, false);
+  }
+  if (cudaMemcpyAsync(c->d_btab, c->h_btab, sizeof(void *) * n, cudaMemcpyHostToDevice, st) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(c->d_bstate, c->h_bstate, sizeof(RefineState) * n, cudaMemcpyHostToDevice,
+                      st) != cudaSuccess)
+    return vh::handle_fail(h, VH_ERR_CUDA, "pose upload failed");
+  const long long key[9] = {n, stride, iterations, depth_fmt, grid, (long long)(uintptr_t)st,
+                            (long long)(uintptr_t)c->d_bpartials,
+                            (long long)(uintptr_t)c->d_bstate, (long long)(uintptr_t)c->d_bhist};
+  if (c->bgraph && std::memcmp(key, c->bkey, sizeof(key)) != 0) {
+    cudaGraphExecDestroy(c->bgraph);
+    c->bgraph = nullptr;
+  }
+  if (!c->bgraph && iterations > 0) {
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+      return vh::handle_fail(h, VH_ERR_CUDA, "refinement capture failed");
+    const cudaError_t le =
+        enqueue_batch_steps(h, c, depth_fmt, stride, grid, job_ctas, hcap, iterations, st);
+    const cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (le != cudaSuccess || e != cudaSuccess ||
+        cudaGraphInstantiate(&c->bgraph, g, 0) != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      c->bgraph = nullptr;
+      return vh::handle_fail(h, VH_ERR_CUDA, "refinement graph failed");
+    }
+    cudaGraphDestroy(g);
+    std::memcpy(c->bkey, key, sizeof(key));
+  }
+  cudaEventRecord(c->ev[1], st);
+  if (iterations > 0 && cudaGraphLaunch(c->bgraph, st) != cudaSuccess)
+    return vh::handle_fail(h, VH_ERR_CUDA, "refinement launch failed");
+  cudaEventRecord(c->ev[2], st);
+  if (cudaMemcpyAsync(c->h_bstate, c->d_bstate, sizeof(RefineState) * n, cudaMemcpyDeviceToHost,
+                      st) != cudaSuccess ||
+      cudaMemcpyAsync(c->h_bhist, c->d_bhist, sizeof(float2) * n * hcap, cudaMemcpyDeviceToHost,
+                      st) != cudaSuccess)
+    return vh::handle_fail(h, VH_ERR_CUDA, "refinement download failed");
+  cudaEventRecord(c->ev[3], st);
+  if ((s = vh::handle_sync(h)) != VH_OK) return s;
+  float ms = 0.0f, ms_steps = 0.0f;
+  cudaEventElapsedTime(&ms, c->ev[0], c->ev[3]);
+  cudaEventElapsedTime(&ms_steps, c->ev[1], c->ev[2]);
+  for (int i = 0; i < n; ++i) {
+    const RefineState &S = c->h_bstate[i];
+    float *out = c2w_out + 16 * i;
+    for (int r = 0; r < 3; ++r)
+      for (int k = 0; k < 4; ++k) out[4 * r + k] = (float)S.pose[4 * r + k];
+    out[12] = out[13] = out[14] = 0.0f;
+    out[15] = 1.0f;
+    if (stats) fill_refine_stats(S, c->h_bhist + (size_t)i * hcap, iterations, ms, ms_steps, stats + i);
   }
   return VH_OK;
 }

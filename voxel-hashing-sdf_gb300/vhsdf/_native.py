@@ -34,6 +34,7 @@ VH_FLAG_SYNC = 0x1
 VH_FLAG_NO_GRAPH = 0x2
 VH_FLAG_PROFILE = 0x4
 VH_FLAG_DEPTH_FILTER = 0x8
+VH_REFINE_BATCH_MAX = 256
 VH_REFINE_ADJOINT = 0
 VH_REFINE_FD = 1
 BLOCK_EDGE = 8
@@ -120,6 +121,7 @@ SIGNATURES = {
     "vh_sdf_sample": (I32, [P, P, I64, P, P, P, I32]),
     "vh_pose_normal_equations": (I32, [P, P, I32, I32, P, I32, I32, P]),
     "vh_pose_refine": (I32, [P, P, I32, I32, P, I32, I32, I32, P, C.POINTER(VhRefineStats)]),
+    "vh_pose_refine_batch": (I32, [P, P, I32, I32, I32, P, I32, I32, P, C.POINTER(VhRefineStats)]),
     "vh_integrate_vjp": (I32, [P, P, I32, P, P, P, P, I32]),
     "vh_raycast": (I32, [P, P, P, P, P, I32]),
     "vh_filter_depth": (I32, [P, P, I32, P, I32]),

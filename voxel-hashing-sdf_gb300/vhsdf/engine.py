@@ -291,6 +291,26 @@ class Volume:
                                            out.ctypes.data, C.byref(st)))
         return out.reshape(4, 4), {f: getattr(st, f) for f, _ in N.VhRefineStats._fields_}
 
+    def pose_refine_batch(self, depths, c2ws, iterations=20, stride=1, depth_format=None):
+        """Adjoint refinement of n poses together, pose i against depths[i]
+        (all host arrays or all CUDA tensors, one dtype; depth_format as in
+        process_frame); returns (n x 4 x 4 refined c2w, list of n stats)."""
+        args = [_Arg(d) for d in depths]
+        n = len(args)
+        if n == 0 or any(a.mem != args[0].mem or a.dtype != args[0].dtype for a in args):
+            raise ValueError("depths must be one memory kind and dtype, at least one image")
+        tab = (C.c_void_p * n)(*[a.ptr for a in args])
+        poses = np.ascontiguousarray(np.asarray(c2ws, np.float32).reshape(n, 16))
+        out = np.empty((n, 16), np.float32)
+        st = (N.VhRefineStats * n)()
+        self._check(self._L.vh_pose_refine_batch(self._h, C.cast(tab, C.c_void_p),
+                                                 _depth_fmt(args[0].dtype, depth_format),
+                                                 args[0].mem, n,
+                                                 poses.ctypes.data, iterations, stride,
+                                                 out.ctypes.data, st))
+        stats = [{f: getattr(x, f) for f, _ in N.VhRefineStats._fields_} for x in st]
+        return out.reshape(n, 4, 4), stats
+
     def integrate_vjp(self, depth, c2w, grad_sdf):
         """dL/ddepth (H x W) and dL/dxi (6) of the last integration, given
         dL/dsdf per voxel of the block list (n_blocks x 512, host arrays)."""
