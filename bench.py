@@ -261,12 +261,36 @@ def adjoint_leg(num_frames, local, iterations=20):
                        "err_mm_p90": float(np.percentile(e_mm, 90)),
                        "err_deg_p90": float(np.percentile(e_deg, 90))}
     gap = [pose_error(a, b) for a, b in zip(poses["adjoint"], poses["fd"])]
+    # the same poses through vh_pose_refine_batch, 16 per call (one launch per
+    # Gauss-Newton step for all 16)
+    vol.pose_refine_batch([frames[int(f)][0] for f in picks[:16]],
+                          [inits[int(f)] for f in picks[:16]], iterations=iterations)
+    ms_b, errs_b, res_b = 0.0, [], []
+    for i in range(0, len(picks), 16):
+        group = picks[i:i + 16]
+        r, st = vol.pose_refine_batch([frames[int(f)][0] for f in group],
+                                      [inits[int(f)] for f in group], iterations=iterations)
+        ms_b += st[0]["ms_steps"]
+        for k, f in enumerate(group):
+            errs_b.append(pose_error(r[k], frames[int(f)][2]))
+            res_b.append(r[k])
+    eb_mm = np.array([1000 * e[0] for e in errs_b])
+    eb_deg = np.array([e[1] for e in errs_b])
+    out["adjoint_batched"] = {
+        "poses_per_call": 16,
+        "pose_steps_per_s": iterations * len(picks) / (ms_b / 1000.0),
+        "within_1mm_0.05deg": int(((eb_mm <= 1.0) & (eb_deg <= 0.05)).sum()),
+        "err_mm_median": float(np.median(eb_mm)),
+        "err_deg_median": float(np.median(eb_deg)),
+        "gap_to_one_at_a_time_mm_median": float(np.median(
+            [1000 * pose_error(a, b)[0] for a, b in zip(res_b, poses["adjoint"])]))}
     extras = volume_extras(vol, [frames[int(f)][2] for f in picks], local)
     vol.close()
     return {"workload": "4x4x3 m room, 3 spheres, 100 frames 640x480 fused at 5 mm (T 0.1 m); "
                         f"{len(picks)} poses perturbed 2 deg about the camera centre + 20 mm "
                         f"(seeded); {iterations} Gauss-Newton steps, all 307200 pixels",
             "adjoint": out["adjoint"], "fd_jacobian": out["fd"],
+            "adjoint_batched": out["adjoint_batched"],
             "adjoint_vs_fd_pose_gap_mm_median": float(np.median([1000 * g[0] for g in gap])),
             "speedup": out["adjoint"]["pose_steps_per_s"] / out["fd"]["pose_steps_per_s"],
             "same_volume": extras}
