@@ -4,14 +4,14 @@
 // tables, streams host chunks in, runs three kernels with blocking copies in
 // between and streams everything back out every frame.  Here the volume stays
 // resident in HBM; a frame is one CUDA graph
-//     frame_begin -> allocate -> resolve -> integrate [-> mc] [-> state_out]
+//     frame_begin -> allocate -> resolve -> integrate [-> mc]
 // whose first kernel carries the frame's descriptor (pose, image addresses)
 // as a parameter updated per launch.  Device images are read in place; host
 // images are uploaded on a copy stream into one of two staging slots,
 // overlapping the previous frame.  All counts stay on the device; the host
 // reads the state block only when a call has to report something
-// (VH_FLAG_SYNC, stats, mesh copies), and without VH_FLAG_SYNC state_out
-// writes it to mapped host memory at the end of every frame.
+// (VH_FLAG_SYNC, stats, mesh copies), and without VH_FLAG_SYNC the frame's
+// last kernel writes it to mapped host memory at the end of every frame.
 
 #include <algorithm>
 #include <cmath>
@@ -202,14 +202,17 @@ void enqueue_frame(vh_handle *h, int fmt, bool with_mc, bool events, bool captur
   launch_integrate(h->V, h->C, h->d_pix, h->d_fin->pose, integrate_grid(h),
                    h->tuning.integrate_variant, s);
   if (events) stage_event(h->ev[2], s, capturing);
+  // Without VH_FLAG_SYNC every frame still brings its counters to the host
+  // mirror (a 64-byte in-stream write to mapped memory, no copy on the
+  // stream): by the last MC CTA, or by k_state_out after an integration.
+  DevState *mirror = (h->p.flags & VH_FLAG_SYNC) ? nullptr : h->h_state_dev;
   if (with_mc) {
     launch_mc(h->V, 0, h->C.mc_min_weight, h->d_tris, (uint32_t)h->tri_cap, mc_grid(h),
-              h->tuning.mc_variant, s);
+              h->tuning.mc_variant, mirror, s);
     if (events) stage_event(h->ev[3], s, capturing);
+  } else if (mirror) {
+    launch_state_out(h->V, mirror, s);
   }
-  // Without VH_FLAG_SYNC every frame still brings its counters to the host
-  // mirror (a 64-byte in-stream write to mapped memory, no copy on the stream).
-  if (!(h->p.flags & VH_FLAG_SYNC)) launch_state_out(h->V, h->h_state_dev, s);
 }
 
 void drop_graphs(vh_handle *h) {
@@ -683,7 +686,7 @@ vh_status vh_extract(vh_handle *h, int32_t scope, vh_mesh_view *out) {
   for (int attempt = 0; attempt < 2; ++attempt) {
     launch_mc_begin(h->V, h->stream);
     launch_mc(h->V, scope == VH_SCOPE_ALL, h->C.mc_min_weight, h->d_tris, (uint32_t)h->tri_cap,
-              mc_grid(h), h->tuning.mc_variant, h->stream);
+              mc_grid(h), h->tuning.mc_variant, nullptr, h->stream);
     VH_CUDA(h, cudaGetLastError());
     h->ev_pending = false;
     if (scope == VH_SCOPE_FRAME && !out && !(h->p.flags & VH_FLAG_SYNC)) return VH_OK;

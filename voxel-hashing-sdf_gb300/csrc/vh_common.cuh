@@ -64,7 +64,8 @@ struct DevState {
   uint32_t tombstones;   // erased slots
   uint32_t erased;       // keys erased by the last erase call
   uint32_t mc_next;      // marching cubes: blocks handed out past the first grid
-  uint32_t pad[3];
+  uint32_t mc_done;      // marching cubes: CTAs finished (state copy-out)
+  uint32_t pad[2];
 };
 
 // Everything a kernel needs to reach the volume; passed by value.
@@ -173,8 +174,10 @@ void launch_allocate(const VolumeView &V, const CamParams &C, const FrameIn *fin
 // variant 0: one block in flight per CTA; 1: next block prefetched
 void launch_integrate(const VolumeView &V, const CamParams &C, const uint2 *pix,
                       const float *pose, int grid, int variant, cudaStream_t s);
+// host_state (optional, mapped host memory): the last CTA copies the device
+// counters there, as launch_state_out would after the kernel.
 void launch_mc(const VolumeView &V, int scope_all, float min_weight, float4 *tris,
-               uint32_t tri_cap, int grid, int variant, cudaStream_t s);
+               uint32_t tri_cap, int grid, int variant, DevState *host_state, cudaStream_t s);
 // Resident CTAs per SM of the persistent kernels (for grid sizing).
 int integrate_ctas_per_sm(int variant);
 int mc_ctas_per_sm(int variant);

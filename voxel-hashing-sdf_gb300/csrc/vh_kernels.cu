@@ -866,7 +866,8 @@ __device__ __forceinline__ void mc_block(McShared &S, const VolumeView &V, int s
 
 template <int kMinCtas>
 __global__ void __launch_bounds__(kMcThreads, kMinCtas) k_mc(VolumeView V, int scope_all, float min_weight,
-                                                      float4 *__restrict__ tris, uint32_t tri_cap) {
+                                                      float4 *__restrict__ tris, uint32_t tri_cap,
+                                                      DevState *host_state) {
   __shared__ McShared S;
   mc_init_shared(S);
   const uint32_t n = scope_all ? V.st->pool_top : min(V.st->frame_count, V.frame_cap);
@@ -881,6 +882,25 @@ __global__ void __launch_bounds__(kMcThreads, kMinCtas) k_mc(VolumeView V, int s
     mc_block(S, V, scope_all, min_weight, tris, tri_cap, i);
     __syncthreads();  // S.next[par] visible; this block done with S
     i = S.next[par];
+  }
+  if (host_state) {  // the last CTA to finish copies the counters out
+    __shared__ int last_cta;
+    if (threadIdx.x == 0) {
+      __threadfence();  // this CTA's counter updates before its arrival
+      last_cta = atomicAdd(&V.st->mc_done, 1u) == gridDim.x - 1u;
+    }
+    __syncthreads();
+    if (last_cta && threadIdx.x < 32) {
+      if (threadIdx.x == 0) {
+        __threadfence();
+        V.st->mc_done = 0u;
+      }
+      __syncwarp();
+      static_assert(sizeof(DevState) % 4 == 0 && sizeof(DevState) / 4 <= 32, "one warp");
+      if (threadIdx.x < sizeof(DevState) / 4)
+        reinterpret_cast<volatile uint32_t *>(host_state)[threadIdx.x] =
+            reinterpret_cast<volatile const uint32_t *>(V.st)[threadIdx.x];
+    }
   }
 }
 
@@ -1367,11 +1387,11 @@ void launch_integrate(const VolumeView &V, const CamParams &C, const uint2 *pix,
 }
 
 void launch_mc(const VolumeView &V, int scope_all, float min_weight, float4 *tris,
-               uint32_t tri_cap, int grid, int variant, cudaStream_t s) {
+               uint32_t tri_cap, int grid, int variant, DevState *host_state, cudaStream_t s) {
   if (variant == 1)
-    k_mc<12><<<grid, kMcThreads, 0, s>>>(V, scope_all, min_weight, tris, tri_cap);
+    k_mc<12><<<grid, kMcThreads, 0, s>>>(V, scope_all, min_weight, tris, tri_cap, host_state);
   else
-    k_mc<10><<<grid, kMcThreads, 0, s>>>(V, scope_all, min_weight, tris, tri_cap);
+    k_mc<10><<<grid, kMcThreads, 0, s>>>(V, scope_all, min_weight, tris, tri_cap, host_state);
 }
 
 void launch_alloc_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, cudaStream_t s) {
