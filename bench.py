@@ -669,7 +669,7 @@ def run_engine(args):
     #   k_integrate 12 B per voxel of every listed block read + 12 B per
     #               updated voxel written + 8 B per pixel record
     # DRAM traffic per launch comes from one ncu capture of frames 3-4 of this
-    # stream (60k-block pool): k_mc moved 1.01x and k_integrate 0.86x their
+    # stream (60k-block pool): k_mc moved 0.91x and k_integrate 0.85x their
     # algorithmic bytes; traffic below scales those ratios to this run.
     npx = 640 * 480
     blocks = [s["frame_blocks"] for s in stage]
@@ -703,11 +703,11 @@ def run_engine(args):
                         "working set (listed blocks read, triangles written) exceeds L2",
                 "sync_per_frame": e2e_sync},
         "roofline": {"bound": "hbm", "achieved": mc_ach, "peak": peak, "unit": "GB/s",
-                     "frac": mc_ach / peak, "traffic": 1.01 * statistics.mean(mc_alg),
+                     "frac": mc_ach / peak, "traffic": 0.91 * statistics.mean(mc_alg),
                      "kernel": "k_mc", "peak_source": peak_src,
                      "algorithmic_bytes": statistics.mean(mc_alg)},
         "roofline_integrate": {"bound": "hbm", "achieved": in_ach, "peak": peak, "unit": "GB/s",
-                               "frac": in_ach / peak, "traffic": 0.86 * statistics.mean(in_alg),
+                               "frac": in_ach / peak, "traffic": 0.85 * statistics.mean(in_alg),
                                "kernel": "k_integrate", "peak_source": peak_src,
                                "algorithmic_bytes": statistics.mean(in_alg)},
         "stages_ms": {k: statistics.mean(s[k] for s in stage)
