@@ -56,6 +56,14 @@ def test_status_strings_and_null_handles():
     assert L.vh_sync(None) == N.VH_ERR_INVALID_ARG
     assert L.vh_render(None) == N.VH_ERR_UNSUPPORTED
     assert L.vh_last_error(None) == b"null handle"
+    # argument checks come before any device work
+    poses = (C.c_float * 16)()
+    out = (C.c_float * 16)()
+    tab = (C.c_void_p * 1)(None)
+    assert L.vh_pose_refine_batch(None, C.cast(tab, C.c_void_p), N.VH_DEPTH_U16_MM,
+                                  N.VH_MEM_HOST, 1, poses, 20, 1, out, None) == N.VH_ERR_INVALID_ARG
+    assert L.vh_pose_refine(None, None, N.VH_DEPTH_U16_MM, N.VH_MEM_HOST, poses, 20, 1,
+                            N.VH_REFINE_ADJOINT, out, None) == N.VH_ERR_INVALID_ARG
 
 
 @pytest.mark.skipif(cuda_available(), reason="checks the no-device path")
