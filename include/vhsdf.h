@@ -253,6 +253,12 @@ vh_status vh_block_list(vh_handle *h, int32_t *xyz, int64_t capacity,
                         int64_t *n);
 /* The reference's BlockHasher (include/tsdf.cuh:144-156) value of a key. */
 uint64_t vh_block_hash_ref(int32_t x, int32_t y, int32_t z);
+/* The marching-cubes tables the engine uses, i.e. the reference's
+ * MarchingCubeParam idxMap / edgeTable / triTable (include/tsdf.cuh:234-534):
+ * corner[8 * 3] voxel offsets of the cube corners, edge_mask[256] cut edges
+ * per case, tri[256 * 16] edge triplets per case (-1 padded).  Any output
+ * may be NULL. */
+vh_status vh_mc_tables(int32_t *corner, int32_t *edge_mask, int32_t *tri);
 
 /* ---- volume I/O ------------------------------------------------------------ */
 

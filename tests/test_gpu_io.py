@@ -91,9 +91,13 @@ def test_gpu_tsdf_generator_front_end(scene, tmp_path):
     assert verts.shape[1] == 3 and cols.shape == verts.shape and faces.max() < len(verts)
     mc = gen.getMarchingCubeParam()
     assert abs(mc["block_size"] - 0.16) < 1e-7
+    assert mc["edgeTable"][1] == 0x109 and list(mc["triTable"][1][:3]) == [0, 8, 3]
+    assert mc["idxMap"].tolist()[1] == [0, 1, 0]  # the reference's corner order
+    vmap = gen.getHashMap()
+    assert sorted(i for bucket in vmap for _, i in bucket) == list(range(len(verts)))
     with pytest.raises(VhError):
         gen.render()
-    table = gen.getHashMap()
+    table = gen.hash_table()
     assert isinstance(table, HashTable)
     keys = gen.volume.export_blocks()["xyz"][:5]
     assert np.all(table.find(keys) >= 0)

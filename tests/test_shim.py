@@ -31,7 +31,11 @@ int main(int argc, char **argv) {
   for (int f = 0; f < 3; ++f)
     if (gen->processFrame(depth.data(), rgb.data(), cam2base) != VH_OK) return 2;
   if (argc > 1) gen->SavePLY(argv[1]);
-  std::printf("ok %zu %zu\n", gen->getVertices()->size(), gen->getFaces()->size());
+  size_t mapped = 0;
+  for (const auto &bucket : *gen->getHashMap()) mapped += bucket.size();
+  const ark::MarchingCubeParam *mc = gen->getMarchingCubeParam();
+  std::printf("ok %zu %zu %zu %d %d %g\n", gen->getVertices()->size(), gen->getFaces()->size(),
+              mapped, mc->edgeTable[1], mc->triTable[1][2], mc->block_size);
   gen->Shutdown();
   delete gen;
   return 0;
@@ -63,7 +67,9 @@ def test_shim_fuses_a_plane(tmp_path, gpu):
     ply = tmp_path / "plane.ply"
     out = subprocess.run([str(exe), str(ply)], capture_output=True, text=True, timeout=120)
     assert out.returncode == 0, out.stdout + out.stderr
-    _, nv, nf = out.stdout.split()
+    _, nv, nf, nm, e1, t12, bs = out.stdout.split()
     assert int(nv) > 100 and int(nf) > 100
+    assert int(nm) == int(nv)  # every merged vertex in the vertex hash
+    assert int(e1) == 0x109 and int(t12) == 3 and abs(float(bs) - 0.08) < 1e-6  # tables, 8 voxels
     header = ply.read_bytes().split(b"end_header")[0].decode()
     assert f"element face {nf}" in header

@@ -28,6 +28,7 @@
 #include "../../include/vhsdf.h"
 #include "vh_common.cuh"
 #include "vh_internal.h"
+#include "vh_mc_tables.h"
 #include "vh_mesh.h"
 
 using namespace vh;
@@ -905,6 +906,15 @@ vh_status vh_block_list(vh_handle *h, int32_t *xyz, int64_t capacity, int64_t *n
 }
 
 uint64_t vh_block_hash_ref(int32_t x, int32_t y, int32_t z) { return ref_block_hash(x, y, z); }
+
+vh_status vh_mc_tables(int32_t *corner, int32_t *edge_mask, int32_t *tri) {
+  for (int k = 0; corner && k < 8; ++k)
+    for (int a = 0; a < 3; ++a) corner[3 * k + a] = kMcCorner[k][a];
+  for (int i = 0; edge_mask && i < 256; ++i) edge_mask[i] = kMcEdgeMask[i];
+  for (int i = 0; tri && i < 256; ++i)
+    for (int j = 0; j < 16; ++j) tri[16 * i + j] = kMcTri[i][j];
+  return VH_OK;
+}
 
 vh_status vh_export_blocks(vh_handle *h, int32_t *xyz, float *sdf, float *weight, uint8_t *rgb,
                            int64_t capacity, int64_t *n) {

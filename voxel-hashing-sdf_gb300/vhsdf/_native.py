@@ -110,6 +110,7 @@ SIGNATURES = {
     "vh_clear_block_list": (I32, [P]),
     "vh_block_list": (I32, [P, P, I64, PI64]),
     "vh_block_hash_ref": (C.c_uint64, [I32, I32, I32]),
+    "vh_mc_tables": (I32, [P, P, P]),
     "vh_export_blocks": (I32, [P, P, P, P, P, I64, PI64]),
     "vh_import_blocks": (I32, [P, P, P, P, P, I64]),
     "vh_save": (I32, [P, C.c_char_p]),

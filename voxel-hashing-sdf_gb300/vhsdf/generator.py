@@ -59,14 +59,37 @@ class GpuTsdfGenerator:
         return self._mesh()[1]
 
     def getHashMap(self):
+        """The vertex hash of the mesh export (include/tsdf.cuh:637): buckets of
+        ((x, y, z, r, g, b), vertex index) keyed by the vertex's voxel cell.
+        The reference's insert_vertex works on a copy of the bucket
+        (src/tsdf.cu:1935) and leaves its map empty; here it holds every
+        merged vertex."""
+        (v, c), _ = self._mesh()
+        nb = max(1, len(v))
+        cells = np.floor(v / self.volume.params.voxel_size).astype(np.int64)
+        keys = (cells[:, 0] * 73856093) ^ (cells[:, 1] * 19349669) ^ (cells[:, 2] * 83492791)
+        buckets = [[] for _ in range(nb)]
+        for i, k in enumerate((keys % nb).tolist()):
+            buckets[k].append((tuple(v[i].tolist()) + tuple(c[i].tolist()), i))
+        return buckets
+
+    def hash_table(self):
+        """The block hash of the volume in the shape of vhashing::HashTable."""
         return HashTable(self.volume)
 
     def getMarchingCubeParam(self):
+        """MarchingCubeParam (include/tsdf.cuh:220-534) as a dict, tables included."""
         p = self.volume.params
+        corner = np.zeros((8, 3), np.int32)
+        edge = np.zeros(256, np.int32)
+        tri = np.zeros((256, 16), np.int32)
+        N.lib().vh_mc_tables(corner.ctypes.data, edge.ctypes.data, tri.ctypes.data)
         return {"vox_size": p.voxel_size, "trunc_margin": p.trunc, "max_depth": p.max_depth,
                 "min_depth": p.min_depth, "block_size": N.BLOCK_EDGE * p.voxel_size,
                 "im_width": p.width, "im_height": p.height, "fx": p.fx, "fy": p.fy,
-                "cx": p.cx, "cy": p.cy, "vox_origin": self.origin, "vox_dim": self.vox_dim}
+                "cx": p.cx, "cy": p.cy, "vox_origin": self.origin, "vox_dim": self.vox_dim,
+                "total_vox": int(np.prod(self.vox_dim)), "idxMap": corner, "edgeTable": edge,
+                "triTable": tri}
 
 
 class HashTable:
