@@ -14,6 +14,7 @@ PROGRAM = r"""
 #include <cstdio>
 #include <vector>
 #include "ark_tsdf.h"
+#include "vhashing_table.h"
 
 int main(int argc, char **argv) {
   const int w = 64, h = 48;
@@ -36,6 +37,18 @@ int main(int argc, char **argv) {
   const ark::MarchingCubeParam *mc = gen->getMarchingCubeParam();
   std::printf("ok %zu %zu %zu %d %d %g\n", gen->getVertices()->size(), gen->getFaces()->size(),
               mapped, mc->edgeTable[1], mc->triTable[1][2], mc->block_size);
+  // the block hash in vhashing::HashTable's shape
+  vhashing::BlockHashTable table(gen->handle());
+  const std::vector<vhashing::BlockKey> heap = table.key_heap();
+  int found = 0;
+  for (int id : table.find(heap)) found += id >= 0;
+  table.clearheap();
+  const long long cleared = table.heap_counter();
+  table.AllocKeys({{500, 500, 500}});
+  const long long allocated = table.heap_counter();
+  const long long erased = table.erase({{500, 500, 500}});
+  std::printf("hash %zu %d %lld %lld %lld %d\n", heap.size(), found, cleared, allocated, erased,
+              (int)table.last_status());
   gen->Shutdown();
   delete gen;
   return 0;
@@ -67,9 +80,13 @@ def test_shim_fuses_a_plane(tmp_path, gpu):
     ply = tmp_path / "plane.ply"
     out = subprocess.run([str(exe), str(ply)], capture_output=True, text=True, timeout=120)
     assert out.returncode == 0, out.stdout + out.stderr
-    _, nv, nf, nm, e1, t12, bs = out.stdout.split()
+    first, second = out.stdout.strip().splitlines()
+    _, nv, nf, nm, e1, t12, bs = first.split()
     assert int(nv) > 100 and int(nf) > 100
     assert int(nm) == int(nv)  # every merged vertex in the vertex hash
     assert int(e1) == 0x109 and int(t12) == 3 and abs(float(bs) - 0.08) < 1e-6  # tables, 8 voxels
+    _, heap, found, cleared, allocated, erased, status = second.split()
+    assert int(heap) > 0 and int(found) == int(heap)
+    assert (int(cleared), int(allocated), int(erased), int(status)) == (0, 1, 1, 0)
     header = ply.read_bytes().split(b"end_header")[0].decode()
     assert f"element face {nf}" in header
