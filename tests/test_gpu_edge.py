@@ -116,22 +116,23 @@ def test_external_stream(scene):
     assert vol.stats()["blocks_allocated"] == orc.num_blocks()
 
 
-def test_pipelined_frames_equal_synchronous_ones(scene):
+@pytest.mark.parametrize("extra", [0, N.VH_FLAG_DEPTH_FILTER])
+def test_pipelined_frames_equal_synchronous_ones(scene, extra):
     """Asynchronous mode, frames submitted back to back: host frames go
     through the two upload slots of the copy stream (pinned buffers, one per
-    frame), device frames are read in place; the volume, the last frame's
-    mesh and the counters (written to the host mirror in-stream) equal a
-    synchronous run of the same frames."""
+    frame), device frames are read in place (with the depth pre-filter, the
+    filter reads them the same way); the volume, the last frame's mesh and
+    the counters equal a synchronous run of the same frames."""
     import torch
     from helpers import sorted_blocks
     n = 12
     frames = [scene.render(f) for f in range(n)]
-    ref = volume_for(scene)  # VH_FLAG_SYNC
+    ref = volume_for(scene, flags=N.VH_FLAG_SYNC | extra)
     for d, c, p in frames:
         ref.process_frame(d, c, p)
     want_st = ref.stats()
     want_tris = sort_rows(tri_rows(*ref.mesh()))
-    vol = volume_for(scene, flags=0)
+    vol = volume_for(scene, flags=extra)
     fmt = "u16" if frames[0][0].dtype == np.uint16 else "f32"
     signed = np.int16 if fmt == "u16" else np.float32  # torch-friendly view of the bytes
     keep = []
