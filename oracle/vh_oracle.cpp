@@ -905,8 +905,8 @@ void vho_sample(void *hp, const double *xyz, int64_t n, double min_w, double *ph
   }
 }
 
-// Normal-equation terms (same layout as the engine) in double precision;
-// P: 12 doubles, row-major camera-to-world 3x4.
+// FP64 ray cast of the fused surface: camera-z depth (0 = no hit) and unit
+// normals per pixel; P: 12 doubles, row-major camera-to-world 3x4.
 void vho_raycast(void *hp, const double *P, double min_w, double *depth, double *normal) {
   Handle *h = (Handle *)hp;
   if (h->precision == 64)
@@ -915,6 +915,8 @@ void vho_raycast(void *hp, const double *P, double min_w, double *depth, double 
     raycast64(*h->v32, P, min_w, depth, normal);
 }
 
+// Normal-equation terms (same layout as the engine) in double precision;
+// P: 12 doubles, row-major camera-to-world 3x4.
 void vho_pose_terms(void *hp, const float *depth, const double *P, int32_t stride, double min_w,
                     double *out29) {
   Handle *h = (Handle *)hp;

@@ -121,3 +121,46 @@ def test_mc_vertices_stay_in_their_cube_and_fp64_agrees():
     lo = m["cube"][:, None, :3].astype(np.float32)
     assert np.all(m["xyz"] >= lo - 1e-4) and np.all(m["xyz"] <= lo + 1 + 1e-4)
     assert np.max(np.abs(m["xyz"] - m["xyz64"])) < 1e-3
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_raycast_of_a_plane_returns_its_depth(precision):
+    """The truncated SDF of a fronto-parallel plane is linear in z inside the
+    band, so trilinear sampling and the march's linear crossing are exact:
+    the cast depth is the plane's depth and the normal faces the camera."""
+    d = 1.2345
+    o = Oracle(W, H, FX, FY, CX, CY, min_depth=0.1, max_depth=4.0, voxel_size=V, trunc=T,
+               precision=precision)
+    depth, rgb, pose = plane_frame(d)
+    o.integrate(depth, rgb, pose)
+    cast, normal = o.raycast(pose)
+    inner = (slice(8, H - 8), slice(8, W - 8))
+    assert np.all(cast[inner] > 0)
+    assert np.max(np.abs(cast[inner] - np.float64(np.float32(d)))) < 1e-5
+    assert np.max(np.abs(normal[inner] - np.array([0.0, 0.0, -1.0]))) < 1e-6
+    # rays that leave the observed frustum's band before crossing miss
+    assert np.all((cast == 0) | (np.abs(cast - d) < 1e-4))
+
+
+def test_pose_terms_of_a_plane_have_closed_form():
+    """A depth image offset by delta from the fused plane: every residual is
+    T * phi = -delta, the Jacobian row is (0, 0, -1, -y, x, 0), so the sums
+    are count, count * delta and count * delta^2."""
+    d, delta = 1.2345, 0.005
+    o = Oracle(W, H, FX, FY, CX, CY, min_depth=0.1, max_depth=4.0, voxel_size=V, trunc=T,
+               precision=64)
+    depth, rgb, pose = plane_frame(d)
+    o.integrate(depth, rgb, pose)
+    obs = np.full((H, W), np.float32(d + delta), np.float32)
+    t = o.pose_terms(obs, pose)
+    n = t[28]
+    assert n > 0.5 * W * H
+    row = {a: 6 * a - a * (a - 1) // 2 for a in range(6)}   # packed upper triangle
+    dz = np.float64(np.float32(d + delta)) - np.float64(np.float32(d))
+    # the gradient is a difference of fp32-stored sdf values over a voxel
+    assert abs(t[row[2]] - n) < 1e-5 * n                    # J_tz . J_tz
+    assert abs(t[21 + 2] - n * dz) < 1e-4 * n * dz          # J_tz . r
+    assert abs(t[27] - n * dz * dz) < 2e-4 * n * dz * dz     # r . r
+    for a in (0, 1):                                         # no in-plane gradient
+        assert abs(t[row[a]]) < 1e-9 and abs(t[21 + a]) < 1e-9
+    assert abs(t[row[5]]) < 1e-9                             # J_rz vanishes
