@@ -12,6 +12,8 @@
  *
  * Threading: calls on one handle must be serialised by the caller; different
  * handles are independent.  Work is enqueued on the handle's CUDA stream.
+ * Every call works on the handle's GPU (vh_params.device) whatever device
+ * the calling thread has current, and leaves that setting unchanged.
  * With VH_FLAG_SYNC set (the default) every call that enqueues work waits
  * for it and reports device-side errors before returning, like the
  * reference's processFrame, which ends in blocking copies.

@@ -847,6 +847,7 @@ void fill_refine_stats(const RefineState &S, const float2 *hist, int iterations,
 
 extern "C" vh_status vh_sdf_sample(vh_handle *h, const float *xyz, int64_t n, float *phi,
                                    float *grad, uint8_t *valid, int32_t mem) {
+  VH_HANDLE_DEVICE(h);
   if (!h || n < 0 || (n && (!xyz || !phi)) || n > (1ll << 30)) return VH_ERR_INVALID_ARG;
   if (mem != VH_MEM_HOST && mem != VH_MEM_DEVICE) return VH_ERR_INVALID_ARG;
   if (!n) return VH_OK;
@@ -887,6 +888,7 @@ extern "C" vh_status vh_sdf_sample(vh_handle *h, const float *xyz, int64_t n, fl
 extern "C" vh_status vh_pose_normal_equations(vh_handle *h, const void *depth, int32_t depth_fmt,
                                               int32_t mem, const float *c2w, int32_t stride,
                                               int32_t method, double *terms) {
+  VH_HANDLE_DEVICE(h);
   if (!h || !c2w || !terms || stride < 1 || (method != VH_REFINE_ADJOINT && method != VH_REFINE_FD))
     return VH_ERR_INVALID_ARG;
   for (int i = 0; i < 16; ++i)
@@ -916,6 +918,7 @@ extern "C" vh_status vh_pose_normal_equations(vh_handle *h, const void *depth, i
 extern "C" vh_status vh_pose_refine(vh_handle *h, const void *depth, int32_t depth_fmt, int32_t mem,
                                     const float *c2w_init, int32_t iterations, int32_t stride,
                                     int32_t method, float *c2w_out, vh_refine_stats *stats) {
+  VH_HANDLE_DEVICE(h);
   if (!h || !c2w_init || !c2w_out || iterations < 0 || iterations > (1 << 16) || stride < 1 ||
       (method != VH_REFINE_ADJOINT && method != VH_REFINE_FD))
     return VH_ERR_INVALID_ARG;
@@ -984,6 +987,7 @@ extern "C" vh_status vh_pose_refine_batch(vh_handle *h, const void *const *depth
                                           const float *c2w_init, int32_t iterations,
                                           int32_t stride, float *c2w_out,
                                           vh_refine_stats *stats) {
+  VH_HANDLE_DEVICE(h);
   if (!h || !depth || !c2w_init || !c2w_out || n < 1 || n > VH_REFINE_BATCH_MAX ||
       iterations < 0 || iterations > (1 << 16) || stride < 1)
     return VH_ERR_INVALID_ARG;
@@ -1076,6 +1080,7 @@ extern "C" vh_status vh_pose_refine_batch(vh_handle *h, const void *const *depth
 extern "C" vh_status vh_integrate_vjp(vh_handle *h, const void *depth, int32_t depth_fmt,
                                       const float *c2w, const float *grad_sdf, float *grad_depth,
                                       float *grad_pose, int32_t mem) {
+  VH_HANDLE_DEVICE(h);
   if (!h || !c2w || !grad_sdf || !grad_depth || !grad_pose) return VH_ERR_INVALID_ARG;
   if (mem != VH_MEM_HOST && mem != VH_MEM_DEVICE) return VH_ERR_INVALID_ARG;
   const cudaStream_t st = vh::handle_stream(h);

@@ -563,6 +563,8 @@ vh_status vh_create(const vh_params *p, vh_handle **out) {
     return VH_ERR_NO_DEVICE;
   }
   if (p->device >= ndev) return VH_ERR_INVALID_ARG;
+  DeviceScope on_device(p->device);  // the caller's current device is restored
+  if (!on_device.ok()) return VH_ERR_CUDA;
   vh_handle *h = new vh_handle();
   h->p = *p;
   auto bail = [&](vh_status s) {
@@ -570,7 +572,6 @@ vh_status vh_create(const vh_params *p, vh_handle **out) {
     delete h;
     return s;
   };
-  if (cudaSetDevice(p->device) != cudaSuccess) return bail(VH_ERR_CUDA);
   if (cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess)
     return bail(VH_ERR_CUDA);
   if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess)
@@ -638,6 +639,7 @@ vh_status vh_create(const vh_params *p, vh_handle **out) {
 }
 
 vh_status vh_destroy(vh_handle *h) {
+  VH_HANDLE_DEVICE(h);
   if (!h) return VH_ERR_INVALID_ARG;
   if (h->stream) cudaStreamSynchronize(h->stream);
   free_all(h);
@@ -646,11 +648,13 @@ vh_status vh_destroy(vh_handle *h) {
 }
 
 vh_status vh_reset(vh_handle *h) {
+  VH_HANDLE_DEVICE(h);
   if (!h) return VH_ERR_INVALID_ARG;
   return clear_volume(h, true);
 }
 
 vh_status vh_set_stream(vh_handle *h, void *stream) {
+  VH_HANDLE_DEVICE(h);
   if (!h) return VH_ERR_INVALID_ARG;
   VH_CUDA(h, cudaStreamSynchronize(h->stream));
   h->stream = stream ? (cudaStream_t)stream : h->own_stream;
@@ -658,6 +662,7 @@ vh_status vh_set_stream(vh_handle *h, void *stream) {
 }
 
 vh_status vh_sync(vh_handle *h) {
+  VH_HANDLE_DEVICE(h);
   if (!h) return VH_ERR_INVALID_ARG;
   return sync_and_check(h);
 }
@@ -666,6 +671,7 @@ const char *vh_last_error(const vh_handle *h) { return h ? h->last_error.c_str()
 
 vh_status vh_integrate(vh_handle *h, const void *depth, int32_t depth_fmt, const uint8_t *rgb,
                        const float *c2w, int32_t mem) {
+  VH_HANDLE_DEVICE(h);
   if (!h) return VH_ERR_INVALID_ARG;
   vh_status s = stage_inputs(h, depth, depth_fmt, rgb, c2w, mem);
   if (s != VH_OK) return s;
@@ -677,6 +683,7 @@ vh_status vh_integrate(vh_handle *h, const void *depth, int32_t depth_fmt, const
 }
 
 vh_status vh_extract(vh_handle *h, int32_t scope, vh_mesh_view *out) {
+  VH_HANDLE_DEVICE(h);
   if (!h) return VH_ERR_INVALID_ARG;
   if (scope != VH_SCOPE_FRAME && scope != VH_SCOPE_ALL)
     return fail(h, VH_ERR_INVALID_ARG, "unknown extraction scope");
@@ -714,6 +721,7 @@ vh_status vh_extract(vh_handle *h, int32_t scope, vh_mesh_view *out) {
 
 vh_status vh_process_frame(vh_handle *h, const void *depth, int32_t depth_fmt, const uint8_t *rgb,
                            const float *c2w, int32_t mem, vh_mesh_view *out) {
+  VH_HANDLE_DEVICE(h);
   if (!h) return VH_ERR_INVALID_ARG;
   vh_status s = stage_inputs(h, depth, depth_fmt, rgb, c2w, mem);
   if (s != VH_OK) return s;
@@ -733,6 +741,7 @@ vh_status vh_process_frame(vh_handle *h, const void *depth, int32_t depth_fmt, c
 
 vh_status vh_copy_mesh(vh_handle *h, float *xyz, uint8_t *rgb, int64_t capacity,
                        int64_t *num_triangles) {
+  VH_HANDLE_DEVICE(h);
   if (!h || capacity < 0) return VH_ERR_INVALID_ARG;
   vh_status s = pull_state(h);
   if (s != VH_OK) return s;
@@ -772,6 +781,7 @@ static vh_status indexed_mesh(vh_handle *h, std::vector<float> &vert, std::vecto
 }
 
 vh_status vh_save_ply(vh_handle *h, const char *path, int32_t binary) {
+  VH_HANDLE_DEVICE(h);
   if (!h || !path) return VH_ERR_INVALID_ARG;
   std::vector<float> vert;
   std::vector<uint8_t> col;
@@ -786,6 +796,7 @@ vh_status vh_save_ply(vh_handle *h, const char *path, int32_t binary) {
 vh_status vh_mesh_indexed(vh_handle *h, float *vertices, uint8_t *colors, int64_t vertex_capacity,
                           int32_t *faces, int64_t face_capacity, int64_t *num_vertices,
                           int64_t *num_faces) {
+  VH_HANDLE_DEVICE(h);
   if (!h || vertex_capacity < 0 || face_capacity < 0) return VH_ERR_INVALID_ARG;
   std::vector<float> vert;
   std::vector<uint8_t> col;
@@ -807,6 +818,7 @@ vh_status vh_mesh_indexed(vh_handle *h, float *vertices, uint8_t *colors, int64_
 
 vh_status vh_filter_depth(vh_handle *h, const void *depth, int32_t depth_fmt, float *out,
                           int32_t mem) {
+  VH_HANDLE_DEVICE(h);
   if (!h || !out) return VH_ERR_INVALID_ARG;
   const void *d = nullptr;
   vh_status s = handle_stage_depth(h, depth, depth_fmt, mem, &d);
@@ -825,6 +837,7 @@ vh_status vh_render(vh_handle *h) {
 }
 
 vh_status vh_alloc_keys(vh_handle *h, const int32_t *xyz, int64_t n, int32_t mem) {
+  VH_HANDLE_DEVICE(h);
   if (h) h->nb_valid = false;
   if (!h || n < 0 || (n && !xyz) || n > 0x7FFFFFFF / 3) return VH_ERR_INVALID_ARG;
   if (!n) return VH_OK;
@@ -841,6 +854,7 @@ vh_status vh_alloc_keys(vh_handle *h, const int32_t *xyz, int64_t n, int32_t mem
 
 vh_status vh_find_keys(vh_handle *h, const int32_t *xyz, int64_t n, int32_t *out_block,
                        int32_t mem) {
+  VH_HANDLE_DEVICE(h);
   if (!h || n < 0 || (n && (!xyz || !out_block)) || n > 0x7FFFFFFF / 3) return VH_ERR_INVALID_ARG;
   if (!n) return VH_OK;
   DevBuf<int32_t> tmp, res;
@@ -861,6 +875,7 @@ vh_status vh_find_keys(vh_handle *h, const int32_t *xyz, int64_t n, int32_t *out
 
 vh_status vh_erase_keys(vh_handle *h, const int32_t *xyz, int64_t n, int64_t *num_erased,
                         int32_t mem) {
+  VH_HANDLE_DEVICE(h);
   if (h) h->nb_valid = false;
   if (!h || n < 0 || (n && !xyz) || n > 0x7FFFFFFF / 3) return VH_ERR_INVALID_ARG;
   if (num_erased) *num_erased = 0;
@@ -879,6 +894,7 @@ vh_status vh_erase_keys(vh_handle *h, const int32_t *xyz, int64_t n, int64_t *nu
 }
 
 vh_status vh_clear_block_list(vh_handle *h) {
+  VH_HANDLE_DEVICE(h);
   if (h) h->nb_valid = false;
   if (!h) return VH_ERR_INVALID_ARG;
   launch_clear_list(h->V, h->stream);
@@ -887,6 +903,7 @@ vh_status vh_clear_block_list(vh_handle *h) {
 }
 
 vh_status vh_block_list(vh_handle *h, int32_t *xyz, int64_t capacity, int64_t *n) {
+  VH_HANDLE_DEVICE(h);
   if (!h || capacity < 0) return VH_ERR_INVALID_ARG;
   vh_status s = pull_state(h);
   if (s != VH_OK) return s;
@@ -918,6 +935,7 @@ vh_status vh_mc_tables(int32_t *corner, int32_t *edge_mask, int32_t *tri) {
 
 vh_status vh_export_blocks(vh_handle *h, int32_t *xyz, float *sdf, float *weight, uint8_t *rgb,
                            int64_t capacity, int64_t *n) {
+  VH_HANDLE_DEVICE(h);
   if (!h || capacity < 0) return VH_ERR_INVALID_ARG;
   launch_epoch_end(h->V, h->stream);
   vh_status s = pull_state(h);
@@ -973,6 +991,7 @@ vh_status vh_export_blocks(vh_handle *h, int32_t *xyz, float *sdf, float *weight
 
 vh_status vh_import_blocks(vh_handle *h, const int32_t *xyz, const float *sdf, const float *weight,
                            const uint8_t *rgb, int64_t n) {
+  VH_HANDLE_DEVICE(h);
   if (h) h->nb_valid = false;
   if (!h || n < 0 || (n && (!xyz || !sdf || !weight || !rgb)) || n > (1ll << 24))
     return VH_ERR_INVALID_ARG;
@@ -997,6 +1016,7 @@ vh_status vh_import_blocks(vh_handle *h, const int32_t *xyz, const float *sdf, c
 }
 
 vh_status vh_save(vh_handle *h, const char *path) {
+  VH_HANDLE_DEVICE(h);
   if (!h || !path) return VH_ERR_INVALID_ARG;
   int64_t n = 0;
   vh_status s = vh_export_blocks(h, nullptr, nullptr, nullptr, nullptr, 0, &n);
@@ -1013,6 +1033,7 @@ vh_status vh_save(vh_handle *h, const char *path) {
 }
 
 vh_status vh_load(vh_handle *h, const char *path) {
+  VH_HANDLE_DEVICE(h);
   if (!h || !path) return VH_ERR_INVALID_ARG;
   std::vector<int32_t> xyz;
   std::vector<float> sdf, w;
@@ -1031,6 +1052,7 @@ vh_status vh_load(vh_handle *h, const char *path) {
 }
 
 vh_status vh_get_stats(vh_handle *h, vh_stats *out) {
+  VH_HANDLE_DEVICE(h);
   if (!h || !out) return VH_ERR_INVALID_ARG;
   launch_epoch_end(h->V, h->stream);
   vh_status s = sync_and_check(h);
@@ -1060,6 +1082,7 @@ vh_status vh_get_tuning(vh_handle *h, vh_tuning *out) {
 }
 
 vh_status vh_set_tuning(vh_handle *h, const vh_tuning *t) {
+  VH_HANDLE_DEVICE(h);
   if (!h || !t || t->integrate_variant < 0 || t->integrate_variant > 1 || t->mc_variant < 0 ||
       t->mc_variant > 1 || t->integrate_ctas_per_sm < 0 || t->mc_ctas_per_sm < 0)
     return VH_ERR_INVALID_ARG;
@@ -1131,6 +1154,7 @@ float median(std::vector<float> v) {
 extern "C" vh_status vh_autotune(vh_handle *h, const void *depth, int32_t depth_fmt,
                                  const uint8_t *rgb, const float *c2w, int32_t mem,
                                  vh_tuning *chosen) {
+  VH_HANDLE_DEVICE(h);
   if (!h) return VH_ERR_INVALID_ARG;
   const std::string key = tune_key(h);
   vh_tuning best{};

@@ -149,6 +149,8 @@ vh_status vh_batch_create(const vh_params *params, int32_t n, vh_batch **out) {
     if (params[i].device != params[0].device) return VH_ERR_INVALID_ARG;
     if (params[i].flags & VH_FLAG_DEPTH_FILTER) return VH_ERR_UNSUPPORTED;  // not in batches
   }
+  DeviceScope on_device(params[0].device);  // the caller's current device is restored
+  if (!on_device.ok()) return VH_ERR_CUDA;
   vh_batch *b = new vh_batch();
   b->n = n;
   b->device = params[0].device;
@@ -160,8 +162,7 @@ vh_status vh_batch_create(const vh_params *params, int32_t n, vh_batch **out) {
       return s;
     }
   }
-  if (cudaSetDevice(b->device) != cudaSuccess ||
-      cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, b->device) !=
+  if (cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, b->device) !=
           cudaSuccess ||
       cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
     free_batch(b);
@@ -227,6 +228,8 @@ vh_status vh_batch_create(const vh_params *params, int32_t n, vh_batch **out) {
 }
 
 vh_status vh_batch_destroy(vh_batch *b) {
+  DeviceScope on_device(b ? b->device : -1);
+  if (!on_device.ok()) return VH_ERR_CUDA;
   if (!b) return VH_ERR_INVALID_ARG;
   if (b->stream) cudaStreamSynchronize(b->stream);
   free_batch(b);
@@ -242,6 +245,8 @@ vh_handle *vh_batch_scene(vh_batch *b, int32_t i) {
 vh_status vh_batch_process(vh_batch *b, const void *const *depth, int32_t depth_fmt,
                            const uint8_t *const *rgb, const float *c2w, int32_t mem,
                            int32_t with_mesh) {
+  DeviceScope on_device(b ? b->device : -1);
+  if (!on_device.ok()) return VH_ERR_CUDA;
   if (!b || !depth || !rgb || !c2w) return VH_ERR_INVALID_ARG;
   if (depth_fmt != VH_DEPTH_U16_MM && depth_fmt != VH_DEPTH_F32_M)
     return fail(b, VH_ERR_INVALID_ARG, "unknown depth format");
@@ -334,6 +339,8 @@ vh_status vh_batch_process(vh_batch *b, const void *const *depth, int32_t depth_
 }
 
 vh_status vh_batch_sync(vh_batch *b, vh_status *status, vh_stats *stats) {
+  DeviceScope on_device(b ? b->device : -1);
+  if (!on_device.ok()) return VH_ERR_CUDA;
   if (!b) return VH_ERR_INVALID_ARG;
   return check_batch(b, status, stats, true);
 }

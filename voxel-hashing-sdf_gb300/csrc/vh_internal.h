@@ -58,3 +58,35 @@ struct RefineCtx;
 RefineCtx *&handle_refine(vh_handle *h);
 void refine_ctx_free(RefineCtx *ctx);
 }  // namespace vh
+
+namespace vh {
+// Makes `device` the calling thread's current GPU for the scope's lifetime
+// and restores the caller's device after it, so that an entry point works on
+// its handle's GPU whatever device the caller has current, and leaves that
+// setting as it found it.  device < 0: no change (a null handle).
+class DeviceScope {
+ public:
+  explicit DeviceScope(int device) {
+    if (device < 0) return;
+    ok_ = cudaGetDevice(&prev_) == cudaSuccess;
+    if (ok_ && prev_ != device) ok_ = switched_ = cudaSetDevice(device) == cudaSuccess;
+  }
+  ~DeviceScope() {
+    if (switched_) cudaSetDevice(prev_);
+  }
+  DeviceScope(const DeviceScope &) = delete;
+  DeviceScope &operator=(const DeviceScope &) = delete;
+  bool ok() const { return ok_; }
+
+ private:
+  int prev_ = 0;
+  bool ok_ = true, switched_ = false;
+};
+}  // namespace vh
+
+// First statement of an entry point that works on a handle's GPU (the
+// handle may be null; the argument checks that follow report that).
+#define VH_HANDLE_DEVICE(h)                                                   \
+  vh::DeviceScope vh_device_scope_((h) ? vh::handle_device(h) : -1);          \
+  if (!vh_device_scope_.ok())                                                 \
+  return vh::handle_fail((h), VH_ERR_CUDA, "cannot make the handle's GPU current")

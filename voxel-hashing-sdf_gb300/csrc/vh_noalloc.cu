@@ -54,6 +54,7 @@ cudaError_t scratch_for(int device, int32_t **out) {
 
 extern "C" vh_status vh_find_keys_noalloc(vh_handle *h, const int32_t *xyz, int64_t n,
                                           int32_t *out_block) {
+  VH_HANDLE_DEVICE(h);
   if (!h || n < 0 || (n && (!xyz || !out_block))) return VH_ERR_INVALID_ARG;
   if (n > kMaxKeys)
     return vh::handle_fail(h, VH_ERR_CAPACITY,

@@ -166,6 +166,7 @@ bool far_enough(unsigned long long key, float voxel, const float c[3], double r2
 using namespace vh;
 
 extern "C" vh_status vh_compact_table(vh_handle *h) {
+  VH_HANDLE_DEVICE(h);
   if (!h) return VH_ERR_INVALID_ARG;
   const VolumeView V = handle_view(h);
   const cudaStream_t st = handle_stream(h);
@@ -184,6 +185,7 @@ extern "C" vh_status vh_compact_table(vh_handle *h) {
 
 extern "C" vh_status vh_stream_out(vh_handle *h, const float *centre, float radius,
                                    int64_t *moved) {
+  VH_HANDLE_DEVICE(h);
   if (moved) *moved = 0;
   if (!h || !centre || !(radius >= 0.0f)) return VH_ERR_INVALID_ARG;
   for (int a = 0; a < 3; ++a)
@@ -262,6 +264,7 @@ extern "C" vh_status vh_stream_out(vh_handle *h, const float *centre, float radi
 }
 
 extern "C" vh_status vh_stream_in(vh_handle *h, const float *centre, float radius, int64_t *moved) {
+  VH_HANDLE_DEVICE(h);
   if (moved) *moved = 0;
   if (!h || !centre || !(radius >= 0.0f)) return VH_ERR_INVALID_ARG;
   for (int a = 0; a < 3; ++a)
