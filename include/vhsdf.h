@@ -272,7 +272,9 @@ vh_status vh_export_blocks(vh_handle *h, int32_t *xyz, float *sdf,
                            float *weight, uint8_t *rgb, int64_t capacity,
                            int64_t *n);
 /* Inserts the given blocks and overwrites their voxels. Replaces the
- * stream-in copy of streamInCPU2GPU (src/tsdf.cu:277-457). */
+ * stream-in copy of streamInCPU2GPU (src/tsdf.cu:277-457).  Weights are
+ * observation counts, as integration makes them: whole numbers in
+ * [0, 2^24], else VH_ERR_INVALID_ARG and nothing is changed. */
 vh_status vh_import_blocks(vh_handle *h, const int32_t *xyz, const float *sdf,
                            const float *weight, const uint8_t *rgb, int64_t n);
 /* Binary snapshot of the volume (header, keys, voxel payload). */

@@ -88,6 +88,26 @@ def test_bad_arguments(scene):
     assert e.value.status == N.VH_ERR_UNSUPPORTED
 
 
+@pytest.mark.parametrize("bad", [2.5, -1.0, np.nan, 2.0 ** 25])
+def test_import_rejects_weights_that_are_not_counts(scene, bad):
+    """Weights are observation counts (whole numbers); anything else is
+    refused before the volume changes."""
+    vol = volume_for(scene)
+    xyz = np.array([[0, 0, 0], [1, 0, 0]], np.int32)
+    sdf = np.zeros((2, 512), np.float32)
+    w = np.ones((2, 512), np.float32)
+    rgb = np.zeros((2, 512, 3), np.uint8)
+    w[1, 17] = bad
+    with pytest.raises(VhError) as e:
+        vol.import_blocks(xyz, sdf, w, rgb)
+    assert e.value.status == N.VH_ERR_INVALID_ARG
+    assert len(vol.export_blocks()["xyz"]) == 0
+    w[1, 17] = 3.0
+    vol.import_blocks(xyz, sdf, w, rgb)
+    assert len(vol.export_blocks()["xyz"]) == 2
+    vol.close()
+
+
 def test_reset_clears_volume(scene):
     vol = volume_for(scene)
     vol.integrate(*scene.render(0))

@@ -996,6 +996,11 @@ vh_status vh_import_blocks(vh_handle *h, const int32_t *xyz, const float *sdf, c
   if (!h || n < 0 || (n && (!xyz || !sdf || !weight || !rgb)) || n > (1ll << 24))
     return VH_ERR_INVALID_ARG;
   if (!n) return VH_OK;
+  // Weights are observation counts: integration adds 1 per update, and its
+  // exact colour average relies on whole weights.
+  for (size_t i = 0, m = (size_t)n * kB3; i < m; ++i)
+    if (!(weight[i] >= 0.0f && weight[i] <= 16777216.0f && weight[i] == std::floor(weight[i])))
+      return fail(h, VH_ERR_INVALID_ARG, "block weights must be whole numbers in [0, 2^24]");
   DevBuf<int32_t> dk;
   DevBuf<float> ds, dw;
   DevBuf<uint8_t> dc;
