@@ -212,19 +212,21 @@ def test_integration_vjp_against_fp64_finite_differences(gpu):
     G = rng.normal(size=(len(lst), 512)).astype(np.float32)
     # The update has jumps where d - z crosses -T (voxel skipped) or +T (dist
     # clamped); finite differences across them measure the jump, not the
-    # derivative.  Voxels within 2 mm of either boundary get no upstream
-    # gradient, so the loss is smooth over the perturbations below.
+    # derivative.  Voxels within 3 mm of either boundary get no upstream
+    # gradient, so the loss is smooth over the perturbations below (the
+    # pose step moves a voxel by at most 2.4 mm).
     li = np.arange(512)
     vox = (lst[:, None, :] * 8 + np.stack([li & 7, (li >> 3) & 7, li >> 6], -1)[None]) * 0.01
     R, t = pose1[:3, :3].astype(np.float64), pose1[:3, 3].astype(np.float64)
     cam = (vox.reshape(-1, 3) - t) @ R
     zc = cam[:, 2]
     diff = (1.013 - zc).reshape(len(lst), 512)
-    G[(np.abs(diff + 0.04) < 2e-3) | (np.abs(diff - 0.04) < 2e-3)] = 0.0
+    G[(np.abs(diff + 0.04) < 3e-3) | (np.abs(diff - 0.04) < 3e-3)] = 0.0
     # voxels whose projection sits on the image border switch in and out too
+    # (the pose step moves a projection by at most 0.21 px)
     u = (f * cam[:, 0] / zc + 31.5).reshape(len(lst), 512)
     v = (f * cam[:, 1] / zc + 23.5).reshape(len(lst), 512)
-    near = lambda a, b: np.abs(a - b) < 0.1
+    near = lambda a, b: np.abs(a - b) < 0.25
     G[near(u, -0.5) | near(u, W - 0.5) | near(v, -0.5) | near(v, H - 0.5)] = 0.0
     gd, gp = vol.integrate_vjp(d1, pose1, G)
 
@@ -252,13 +254,19 @@ def test_integration_vjp_against_fp64_finite_differences(gpu):
     step = (dp.astype(np.float64) - dm.astype(np.float64)) / (2 * h)
     an = float(np.sum(gd.astype(np.float64) * step))
     assert abs(fd - an) < 2e-3 * max(1.0, abs(fd)), (fd, an)
-    # pose: directional derivative along a random se(3) direction
+    # pose: directional derivative along a random se(3) direction.  The
+    # oracle takes camera z in fp32 (its decisions are the reference's fp32
+    # operations), so every voxel's sdf carries a rounding of ~6e-8 m / T
+    # that the difference quotient divides by 2h: summed over the volume's
+    # voxels that is ~1 on this loss at h = 2e-4 and ~0.15 at the pose step
+    # used here, well inside the tolerance.
+    hp = 1.5e-3
     xi = rng.normal(size=6)
     xi /= np.linalg.norm(xi)
 
     def moved(sign):
         out = pose1.astype(np.float64).copy()
-        w, v = sign * h * xi[3:], sign * h * xi[:3]
+        w, v = sign * hp * xi[3:], sign * hp * xi[:3]
         th = np.linalg.norm(w)
         K = np.array([[0, -w[2], w[1]], [w[2], 0, -w[0]], [-w[1], w[0], 0]]) / max(th, 1e-30)
         R = np.eye(3) + np.sin(th) * K + (1 - np.cos(th)) * K @ K
@@ -266,7 +274,7 @@ def test_integration_vjp_against_fp64_finite_differences(gpu):
         out[:3, 3] = R @ out[:3, 3] + v
         return out.astype(np.float32)
 
-    fdp = (loss(d1, moved(1)) - loss(d1, moved(-1))) / (2 * h)
+    fdp = (loss(d1, moved(1)) - loss(d1, moved(-1))) / (2 * hp)
     anp = float(np.dot(gp.astype(np.float64), xi))
     assert abs(fdp - anp) < 2e-2 * max(1.0, abs(fdp)), (fdp, anp)
 
