@@ -289,3 +289,35 @@ def test_mc_on_dense_sign_changes(scene):
         assert len(got) > 5000
         assert np.array_equal(got, want)
         vol.close()
+
+
+def test_colour_average_at_every_weight_range(scene):
+    """Voxels imported with weights at the edges of the colour average's
+    paths (first observation; umulhi up to w_old 2047; corrected reciprocal
+    up to 65536; the fp32 formula beyond) and random colours: one integrated
+    frame equals the fp32 oracle bit for bit."""
+    vol = volume_for(scene)
+    seed_orc = oracle_for(vol, 32)
+    seed_orc.integrate(*scene.render(0))
+    e = seed_orc.export()
+    rng = np.random.default_rng(11)
+    levels = np.array([0, 1, 2, 3, 254, 255, 256, 1023, 2046, 2047, 2048, 2049, 65535, 65536,
+                       65537, 1e6, 2 ** 24], np.float32)
+    w = levels[rng.integers(0, len(levels), e["weight"].shape)]
+    rgb = rng.integers(0, 256, e["rgb"].shape).astype(np.uint8)
+    vol.import_blocks(e["xyz"], e["sdf"], w, rgb)
+    orc = oracle_for(vol, 32)
+    orc.import_blocks(e["xyz"], e["sdf"], w, rgb)
+    for f in (1, 2):
+        d, c, p = scene.render(f)
+        vol.integrate(d, c, p)
+        orc.integrate(d, c, p)
+    g = vol.export_blocks()
+    assert_same_blocks(g, orc.export())
+    # every weight range was updated (w_old = 2^24 stays: 2^24 + 1 rounds back)
+    pos = {k: i for i, k in enumerate(map(tuple, g["xyz"].tolist()))}
+    idx = np.array([pos[k] for k in map(tuple, e["xyz"].tolist())])
+    changed = g["weight"][idx] != w
+    for lv in levels[:-1]:
+        assert np.any(changed & (w == lv)), lv
+    vol.close()

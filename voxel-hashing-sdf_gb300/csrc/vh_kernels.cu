@@ -364,12 +364,33 @@ __global__ void __launch_bounds__(256, 6) k_allocate(VolumeView V, CamParams C,
 // 2^24, exact in fp32, and the fp32 quotient of two integers with divisor
 // w <= 131072 truncates to floor(n / w): it cannot round up to the next
 // integer (that needs n / w within 2^-17 of it, but it differs from any
-// integer by at least 1 / w) nor down past one.  floor(n / w) is then taken
-// from a reciprocal estimate (error < 1) corrected by one exact integer
-// remainder test.  Larger weights use the fp32 formula itself.
+// integer by at least 1 / w) nor down past one.  So any exact floor(n / w)
+// will do:
+//  * w <= 2048: floor(n / w) = umulhi(n, m) for any m in
+//    [2^32 / w, 2^32 / w + 2^32 / (255 w^2)), since n <= 255 w keeps
+//    n (m - 2^32 / w) / 2^32 below 1 / w, the distance from n / w to the
+//    next integer.  m = trunc(rcp(w) * 2^32 (1 + 2^-21)) + 1 with the
+//    approximate reciprocal (__fdividef: at most 2 ulp, 2^-22 relative) lies
+//    in that range: the 2^-21 bias covers the reciprocal's and the
+//    product's rounding from below and stays inside the upper margin
+//    (tests/blend_bound_check.c checks every n at both ends of the possible
+//    m range for every w).  w_old = 0 keeps the new colour.
+//  * w <= 65537: a reciprocal estimate (error < 1) corrected by one exact
+//    integer remainder test.
+// Larger weights use the fp32 formula itself.
 __device__ __forceinline__ uint32_t blend_colour(uint32_t old_rgb, uint32_t new_rgb, float w_old,
                                                  float w_new) {
   uint32_t out = 0;
+  if (w_old <= 2047.0f) {
+    const uint32_t wo = (uint32_t)w_old;
+    const uint32_t m = __float2uint_rz(__fdividef(1.0f, w_new) * 4294969344.0f) + 1u;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const uint32_t n = ((old_rgb >> (8 * c)) & 0xFFu) * wo + ((new_rgb >> (8 * c)) & 0xFFu);
+      out |= __umulhi(n, m) << (8 * c);
+    }
+    return wo ? out : new_rgb;
+  }
   if (w_old <= 65536.0f) {
     const uint32_t wo = (uint32_t)w_old, wn = wo + 1u;
     const float r = __fdividef(1.0f, w_new);
