@@ -11,7 +11,7 @@ import ctypes as C
 import numpy as np
 
 from . import _native as N
-from .engine import Volume, _Arg, _depth_fmt
+from .engine import Volume, _depth_arg, _rgb_arg
 
 
 class _Scene(Volume):
@@ -84,8 +84,8 @@ class Batch:
         for i, fr in enumerate(frames):
             if fr is None:
                 continue
-            d, c = _Arg(fr[0]), _Arg(fr[1], np.uint8)
-            f = _depth_fmt(d.dtype, depth_format)
+            d, f = _depth_arg(fr[0], self._params[i], depth_format)
+            c = _rgb_arg(fr[1], self._params[i])
             if fmt is not None and (f != fmt or d.mem != mem):
                 raise ValueError("all frames of a step share depth format and memory kind")
             if d.mem != c.mem:

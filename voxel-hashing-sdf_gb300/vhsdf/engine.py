@@ -16,7 +16,9 @@ def _is_cuda_tensor(a):
 
 
 class _Arg:
-    """Pointer + memory kind of an input array, keeping host copies alive."""
+    """Pointer + memory kind of an input array, keeping host copies alive.
+    The library reads as many bytes as the volume's parameters say, so the
+    size (and for device tensors the GPU) is checked here, before the call."""
 
     def __init__(self, a, dtype=None):
         if _is_cuda_tensor(a):
@@ -26,12 +28,47 @@ class _Arg:
             self.ptr = a.data_ptr()
             self.mem = N.VH_MEM_DEVICE
             self.dtype = str(a.dtype).replace("torch.", "")
+            self.nbytes = a.numel() * a.element_size()
+            self.device = a.device.index
         else:
             arr = np.ascontiguousarray(a if dtype is None else np.asarray(a, dtype=dtype))
             self.keep = arr
             self.ptr = arr.ctypes.data
             self.mem = N.VH_MEM_HOST
             self.dtype = str(arr.dtype)
+            self.nbytes = arr.nbytes
+            self.device = None
+
+
+def _check_image(arg, params, bytes_per_px, what):
+    """`arg` holds exactly one width x height image of `bytes_per_px` bytes
+    per pixel, on the volume's GPU if it is a device tensor."""
+    want = int(params.width) * int(params.height) * bytes_per_px
+    if arg.nbytes != want:
+        raise ValueError(f"{what} must hold {params.width}x{params.height} pixels of "
+                         f"{bytes_per_px} bytes ({want} bytes), got {arg.nbytes} bytes")
+    if arg.mem == N.VH_MEM_DEVICE and arg.device != int(params.device):
+        raise ValueError(f"{what} is on cuda:{arg.device}, the volume on cuda:{params.device}")
+
+
+def _depth_bytes(fmt):
+    return 2 if fmt == N.VH_DEPTH_U16_MM else 4
+
+
+def _depth_arg(depth, params, depth_format=None):
+    """A checked depth image and its format."""
+    d = _Arg(depth)
+    fmt = _depth_fmt(d.dtype, depth_format)
+    _check_image(d, params, _depth_bytes(fmt), "depth")
+    return d, fmt
+
+
+def _rgb_arg(rgb, params):
+    c = _Arg(rgb, np.uint8)
+    if c.mem == N.VH_MEM_DEVICE and c.dtype != "uint8":
+        raise TypeError(f"rgb must be uint8, got {c.dtype}")
+    _check_image(c, params, 3, "rgb")
+    return c
 
 
 def _depth_fmt(dtype, override=None):
@@ -91,23 +128,22 @@ class Volume:
         self._check(self._L.vh_set_stream(self._h, C.c_void_p(stream_ptr)))
 
     # ---- per-frame path ----
-    def _frame_args(self, depth, rgb, c2w):
-        d = _Arg(depth)
-        c = _Arg(rgb, np.uint8)
+    def _frame_args(self, depth, rgb, c2w, depth_format=None):
+        d, fmt = _depth_arg(depth, self.params, depth_format)
+        c = _rgb_arg(rgb, self.params)
         if d.mem != c.mem:
             raise ValueError("depth and rgb must both be host or both be device arrays")
         pose = np.ascontiguousarray(np.asarray(c2w, dtype=np.float32).reshape(16))
-        return d, c, pose
+        return d, fmt, c, pose
 
     def integrate(self, depth, rgb, c2w, depth_format=None):
-        d, c, pose = self._frame_args(depth, rgb, c2w)
-        self._check(self._L.vh_integrate(self._h, d.ptr, _depth_fmt(d.dtype, depth_format), c.ptr,
-                                         pose.ctypes.data, d.mem))
+        d, fmt, c, pose = self._frame_args(depth, rgb, c2w, depth_format)
+        self._check(self._L.vh_integrate(self._h, d.ptr, fmt, c.ptr, pose.ctypes.data, d.mem))
 
     def process_frame(self, depth, rgb, c2w, depth_format=None):
-        d, c, pose = self._frame_args(depth, rgb, c2w)
-        self._check(self._L.vh_process_frame(self._h, d.ptr, _depth_fmt(d.dtype, depth_format),
-                                             c.ptr, pose.ctypes.data, d.mem, None))
+        d, fmt, c, pose = self._frame_args(depth, rgb, c2w, depth_format)
+        self._check(self._L.vh_process_frame(self._h, d.ptr, fmt, c.ptr, pose.ctypes.data, d.mem,
+                                             None))
 
     # ---- launch tuning ----
     def tuning(self):
@@ -123,10 +159,10 @@ class Volume:
     def autotune(self, depth, rgb, c2w, depth_format=None):
         """Times the launch configurations on this frame (scratch volume) and
         applies the fastest; returns it."""
-        d, c, pose = self._frame_args(depth, rgb, c2w)
+        d, fmt, c, pose = self._frame_args(depth, rgb, c2w, depth_format)
         t = N.VhTuning()
-        self._check(self._L.vh_autotune(self._h, d.ptr, _depth_fmt(d.dtype, depth_format), c.ptr,
-                                        pose.ctypes.data, d.mem, C.byref(t)))
+        self._check(self._L.vh_autotune(self._h, d.ptr, fmt, c.ptr, pose.ctypes.data, d.mem,
+                                        C.byref(t)))
         return {f: getattr(t, f) for f, _ in N.VhTuning._fields_}
 
     def extract(self, scope="frame"):
@@ -169,11 +205,13 @@ class Volume:
 
     def filter_depth(self, depth, depth_format=None):
         """The VH_FLAG_DEPTH_FILTER pre-filter of one depth image (float metres)."""
-        d = _Arg(depth)
+        if _is_cuda_tensor(depth):
+            raise TypeError("filter_depth takes a host image (the frame path filters device "
+                            "images itself with VH_FLAG_DEPTH_FILTER)")
+        d, fmt = _depth_arg(depth, self.params, depth_format)
         p = self.params
         out = np.empty((p.height, p.width), np.float32)
-        self._check(self._L.vh_filter_depth(self._h, d.ptr, _depth_fmt(d.dtype, depth_format),
-                                            out.ctypes.data, N.VH_MEM_HOST))
+        self._check(self._L.vh_filter_depth(self._h, d.ptr, fmt, out.ctypes.data, N.VH_MEM_HOST))
         return out
 
     def raycast(self, c2w):
@@ -208,10 +246,15 @@ class Volume:
         self._check(self._L.vh_render(self._h))
 
     # ---- hash surface ----
-    @staticmethod
-    def _keys(keys):
+    def _keys(self, keys):
         if _is_cuda_tensor(keys):
-            return _Arg(keys), keys.numel() // 3
+            a = _Arg(keys)
+            if a.dtype != "int32" or keys.numel() % 3:
+                raise TypeError("device keys must be an int32 tensor of (x, y, z) triples")
+            if a.device != int(self.params.device):
+                raise ValueError(f"keys are on cuda:{a.device}, the volume on "
+                                 f"cuda:{self.params.device}")
+            return a, keys.numel() // 3
         k = np.ascontiguousarray(np.asarray(keys, dtype=np.int32).reshape(-1, 3))
         return _Arg(k), k.shape[0]
 
@@ -252,6 +295,12 @@ class Volume:
         world points; numpy in, numpy out (torch CUDA tensors: device path)."""
         if _is_cuda_tensor(xyz):
             import torch
+            a = _Arg(xyz)
+            if a.dtype != "float32" or xyz.numel() % 3:
+                raise TypeError("device points must be a float32 tensor of (x, y, z) triples")
+            if a.device != int(self.params.device):
+                raise ValueError(f"points are on cuda:{a.device}, the volume on "
+                                 f"cuda:{self.params.device}")
             n = xyz.numel() // 3
             phi = torch.empty(n, dtype=torch.float32, device=xyz.device)
             grad = torch.empty((n, 3), dtype=torch.float32, device=xyz.device)
@@ -268,25 +317,26 @@ class Volume:
                                           grad.ctypes.data, valid.ctypes.data, N.VH_MEM_HOST))
         return phi, grad, valid.astype(bool)
 
-    def pose_normal_equations(self, depth, c2w, stride=1, method="adjoint"):
-        d = _Arg(depth)
+    def pose_normal_equations(self, depth, c2w, stride=1, method="adjoint", depth_format=None):
+        d, fmt = _depth_arg(depth, self.params, depth_format)
         pose = np.ascontiguousarray(np.asarray(c2w, np.float32).reshape(16))
         out = np.empty(29, np.float64)
         m = N.VH_REFINE_FD if method == "fd" else N.VH_REFINE_ADJOINT
-        self._check(self._L.vh_pose_normal_equations(self._h, d.ptr, _depth_fmt(d.dtype), d.mem,
+        self._check(self._L.vh_pose_normal_equations(self._h, d.ptr, fmt, d.mem,
                                                      pose.ctypes.data, stride, m,
                                                      out.ctypes.data))
         return out
 
-    def pose_refine(self, depth, c2w, iterations=20, stride=1, method="adjoint"):
+    def pose_refine(self, depth, c2w, iterations=20, stride=1, method="adjoint",
+                    depth_format=None):
         """Gauss-Newton refinement of a camera pose against the volume;
         returns (refined 4x4 c2w, stats dict)."""
-        d = _Arg(depth)
+        d, fmt = _depth_arg(depth, self.params, depth_format)
         pose = np.ascontiguousarray(np.asarray(c2w, np.float32).reshape(16))
         out = np.empty(16, np.float32)
         st = N.VhRefineStats()
         m = N.VH_REFINE_FD if method == "fd" else N.VH_REFINE_ADJOINT
-        self._check(self._L.vh_pose_refine(self._h, d.ptr, _depth_fmt(d.dtype), d.mem,
+        self._check(self._L.vh_pose_refine(self._h, d.ptr, fmt, d.mem,
                                            pose.ctypes.data, iterations, stride, m,
                                            out.ctypes.data, C.byref(st)))
         return out.reshape(4, 4), {f: getattr(st, f) for f, _ in N.VhRefineStats._fields_}
@@ -299,12 +349,14 @@ class Volume:
         n = len(args)
         if n == 0 or any(a.mem != args[0].mem or a.dtype != args[0].dtype for a in args):
             raise ValueError("depths must be one memory kind and dtype, at least one image")
+        fmt = _depth_fmt(args[0].dtype, depth_format)
+        for a in args:
+            _check_image(a, self.params, _depth_bytes(fmt), "depth")
         tab = (C.c_void_p * n)(*[a.ptr for a in args])
         poses = np.ascontiguousarray(np.asarray(c2ws, np.float32).reshape(n, 16))
         out = np.empty((n, 16), np.float32)
         st = (N.VhRefineStats * n)()
-        self._check(self._L.vh_pose_refine_batch(self._h, C.cast(tab, C.c_void_p),
-                                                 _depth_fmt(args[0].dtype, depth_format),
+        self._check(self._L.vh_pose_refine_batch(self._h, C.cast(tab, C.c_void_p), fmt,
                                                  args[0].mem, n,
                                                  poses.ctypes.data, iterations, stride,
                                                  out.ctypes.data, st))
@@ -314,12 +366,17 @@ class Volume:
     def integrate_vjp(self, depth, c2w, grad_sdf):
         """dL/ddepth (H x W) and dL/dxi (6) of the last integration, given
         dL/dsdf per voxel of the block list (n_blocks x 512, host arrays)."""
-        d = _Arg(depth)
+        d, fmt = _depth_arg(depth, self.params)
         pose = np.ascontiguousarray(np.asarray(c2w, np.float32).reshape(16))
         g = np.ascontiguousarray(grad_sdf, np.float32)
+        nb = C.c_int64()
+        self._check(self._L.vh_block_list(self._h, None, 0, C.byref(nb)))
+        if g.size != nb.value * N.BLOCK_VOXELS:
+            raise ValueError(f"grad_sdf must hold {nb.value} x {N.BLOCK_VOXELS} values (one per "
+                             f"voxel of the block list), got {g.size}")
         gd = np.empty((self.params.height, self.params.width), np.float32)
         gp = np.empty(6, np.float32)
-        self._check(self._L.vh_integrate_vjp(self._h, d.ptr, _depth_fmt(d.dtype),
+        self._check(self._L.vh_integrate_vjp(self._h, d.ptr, fmt,
                                              pose.ctypes.data, g.ctypes.data, gd.ctypes.data,
                                              gp.ctypes.data, N.VH_MEM_HOST))
         return gd, gp
@@ -338,10 +395,15 @@ class Volume:
         return {"xyz": xyz, "sdf": sdf, "weight": w, "rgb": rgb}
 
     def import_blocks(self, xyz, sdf, weight, rgb):
-        xyz = np.ascontiguousarray(xyz, np.int32)
+        xyz = np.ascontiguousarray(xyz, np.int32).reshape(-1, 3)
         sdf = np.ascontiguousarray(sdf, np.float32)
         weight = np.ascontiguousarray(weight, np.float32)
         rgb = np.ascontiguousarray(rgb, np.uint8)
+        n = xyz.shape[0]
+        for name, a, per in (("sdf", sdf, 1), ("weight", weight, 1), ("rgb", rgb, 3)):
+            if a.size != n * N.BLOCK_VOXELS * per:
+                raise ValueError(f"{name} must hold {n} x {N.BLOCK_VOXELS}"
+                                 f"{' x 3' if per == 3 else ''} values, got {a.size}")
         self._check(self._L.vh_import_blocks(self._h, xyz.ctypes.data, sdf.ctypes.data,
                                              weight.ctypes.data, rgb.ctypes.data, xyz.shape[0]))
 
