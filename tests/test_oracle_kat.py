@@ -164,3 +164,35 @@ def test_pose_terms_of_a_plane_have_closed_form():
     for a in (0, 1):                                         # no in-plane gradient
         assert abs(t[row[a]]) < 1e-9 and abs(t[21 + a]) < 1e-9
     assert abs(t[row[5]]) < 1e-9                             # J_rz vanishes
+
+
+@pytest.mark.parametrize("c", [7.3, 7.0, 0.5])
+def test_mc_of_a_plane_has_closed_form(c):
+    """sdf = (c - z) / T over 2x2x2 blocks (voxel units): every cube whose
+    eight corners exist (origins 0..14 on each axis) and whose z-span holds
+    the crossing emits two triangles, every vertex on z = c (the sdf is
+    linear, so the interpolation is exact; a corner exactly on the plane
+    is not negative and snaps the vertex onto itself)."""
+    o = Oracle(W, H, FX, FY, CX, CY, max_depth=4.0, voxel_size=V, trunc=T, precision=32)
+    bx, by, bz = np.meshgrid(range(2), range(2), range(2), indexing="ij")
+    xyz = np.stack([bx.ravel(), by.ravel(), bz.ravel()], -1).astype(np.int32)
+    li = np.arange(512)
+    z = (xyz[:, 2:3] * 8 + (li >> 6)[None, :]).astype(np.float32)
+    sdf = ((np.float32(c) - z) * np.float32(0.25)).astype(np.float32)  # T = 4 voxels
+    w = np.ones_like(sdf)
+    rgb = np.full((len(xyz), 512, 3), 9, np.uint8)
+    o.import_blocks(xyz, sdf, w, rgb)
+    m = o.marching_cubes("all")
+    k = int(np.floor(c))  # the cube layer whose z-span [k, k + 1) holds c
+    assert len(m["xyz"]) == 15 * 15 * 2
+    assert np.all(m["cube"][:, 2] == k)
+    assert np.max(np.abs(m["xyz"][..., 2] - np.float32(c))) < 1e-5
+    # the triangles tile the 15 x 15 voxel square exactly once
+    e1 = m["xyz64"][:, 1, :2] - m["xyz64"][:, 0, :2]
+    e2 = m["xyz64"][:, 2, :2] - m["xyz64"][:, 0, :2]
+    area = 0.5 * np.abs(e1[:, 0] * e2[:, 1] - e1[:, 1] * e2[:, 0])
+    assert abs(area.sum() - 15.0 * 15.0) < 1e-6
+    # one winding: every triangle faces the positive-sdf (observed) side, -z
+    n = np.cross(m["xyz64"][:, 1] - m["xyz64"][:, 0], m["xyz64"][:, 2] - m["xyz64"][:, 0])
+    assert np.all(n[:, 2] < 0)
+    assert np.all(m["rgb"] == 9)
