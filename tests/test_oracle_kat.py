@@ -196,3 +196,31 @@ def test_mc_of_a_plane_has_closed_form(c):
     n = np.cross(m["xyz64"][:, 1] - m["xyz64"][:, 0], m["xyz64"][:, 2] - m["xyz64"][:, 0])
     assert np.all(n[:, 2] < 0)
     assert np.all(m["rgb"] == 9)
+
+
+def test_mc_of_a_sphere_is_a_closed_genus_zero_surface():
+    """Truncated distance to a sphere (radius 5.2 voxels) over 2x2x2 blocks:
+    vertices merged by exact float equality (the reference's tsdf2mesh
+    rule) give a closed 2-manifold of Euler characteristic 2, every edge in
+    exactly two triangles, every vertex within 0.05 voxel of the sphere."""
+    o = Oracle(W, H, FX, FY, CX, CY, max_depth=4.0, voxel_size=V, trunc=T, precision=32)
+    bx, by, bz = np.meshgrid(range(2), range(2), range(2), indexing="ij")
+    xyz = np.stack([bx.ravel(), by.ravel(), bz.ravel()], -1).astype(np.int32)
+    li = np.arange(512)
+    pts = np.stack([xyz[:, None, 0] * 8 + (li & 7)[None], xyz[:, None, 1] * 8 + ((li >> 3) & 7)[None],
+                    xyz[:, None, 2] * 8 + (li >> 6)[None]], -1).astype(np.float64)
+    centre, r = np.array([8.3, 8.1, 7.9]), 5.2
+    sdf = np.clip((np.linalg.norm(pts - centre, axis=-1) - r) / 4.0, -1, 1).astype(np.float32)
+    o.import_blocks(xyz, sdf, np.ones_like(sdf), np.full((len(xyz), 512, 3), 9, np.uint8))
+    m = o.marching_cubes("all")
+    nf = len(m["xyz"])
+    assert nf > 500
+    bits = np.ascontiguousarray(m["xyz"].reshape(-1, 3)).view(np.uint32)
+    verts, faces = np.unique(bits, axis=0, return_inverse=True)
+    faces = faces.reshape(-1, 3)
+    edges = np.sort(np.concatenate([faces[:, [0, 1]], faces[:, [1, 2]], faces[:, [2, 0]]]), axis=1)
+    ue, count = np.unique(edges, axis=0, return_counts=True)
+    assert np.all(count == 2)
+    assert len(verts) - len(ue) + nf == 2
+    rad = np.linalg.norm(m["xyz64"].reshape(-1, 3) - centre, axis=1)
+    assert np.max(np.abs(rad - r)) < 0.05
