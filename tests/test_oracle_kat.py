@@ -200,9 +200,12 @@ def test_mc_of_a_plane_has_closed_form(c):
 
 def test_mc_of_a_sphere_is_a_closed_genus_zero_surface():
     """Truncated distance to a sphere (radius 5.2 voxels) over 2x2x2 blocks:
-    vertices merged by exact float equality (the reference's tsdf2mesh
-    rule) give a closed 2-manifold of Euler characteristic 2, every edge in
-    exactly two triangles, every vertex within 0.05 voxel of the sphere."""
+    with vertices merged by position (FP64 vertices) the mesh is a closed
+    2-manifold of Euler characteristic 2, every edge in exactly two
+    triangles, every vertex within 0.05 voxel of the sphere.  The fp32
+    vertices of one edge, interpolated from either end by the two cubes
+    that share it, differ by at most one ulp, so the reference's
+    exact-equality merge (tsdf2mesh) can split a vertex in two."""
     o = Oracle(W, H, FX, FY, CX, CY, max_depth=4.0, voxel_size=V, trunc=T, precision=32)
     bx, by, bz = np.meshgrid(range(2), range(2), range(2), indexing="ij")
     xyz = np.stack([bx.ravel(), by.ravel(), bz.ravel()], -1).astype(np.int32)
@@ -215,8 +218,8 @@ def test_mc_of_a_sphere_is_a_closed_genus_zero_surface():
     m = o.marching_cubes("all")
     nf = len(m["xyz"])
     assert nf > 500
-    bits = np.ascontiguousarray(m["xyz"].reshape(-1, 3)).view(np.uint32)
-    verts, faces = np.unique(bits, axis=0, return_inverse=True)
+    key = np.round(m["xyz64"].reshape(-1, 3) * 1e5).astype(np.int64)
+    verts, faces = np.unique(key, axis=0, return_inverse=True)
     faces = faces.reshape(-1, 3)
     edges = np.sort(np.concatenate([faces[:, [0, 1]], faces[:, [1, 2]], faces[:, [2, 0]]]), axis=1)
     ue, count = np.unique(edges, axis=0, return_counts=True)
@@ -224,3 +227,8 @@ def test_mc_of_a_sphere_is_a_closed_genus_zero_surface():
     assert len(verts) - len(ue) + nf == 2
     rad = np.linalg.norm(m["xyz64"].reshape(-1, 3) - centre, axis=1)
     assert np.max(np.abs(rad - r)) < 0.05
+    f32 = m["xyz"].reshape(-1, 3)
+    ulp = np.spacing(np.abs(f32).max())
+    for g in range(len(verts)):
+        same = f32[faces.ravel() == g]
+        assert np.max(np.abs(same - same[0])) <= ulp
