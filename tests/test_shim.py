@@ -90,3 +90,20 @@ def test_shim_fuses_a_plane(tmp_path, gpu):
     assert (int(cleared), int(allocated), int(erased), int(status)) == (0, 1, 1, 0)
     header = ply.read_bytes().split(b"end_header")[0].decode()
     assert f"element face {nf}" in header
+
+
+def test_headers_compile_without_warnings(tmp_path):
+    """vhsdf.h is plain C (C99); the C++ front ends compile warning-free
+    under strict flags, so they can be dropped into a caller's build."""
+    c_src = tmp_path / "c_api.c"
+    c_src.write_text('#include "vhsdf.h"\nint main(void) { vh_params p; '
+                     'return vh_params_default(&p) == VH_OK ? 0 : 1; }\n')
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Wpedantic", "-Werror", "-c",
+                    str(c_src), "-I", os.path.join(REPO, "include"), "-o",
+                    str(tmp_path / "c_api.o")], check=True)
+    cpp_src = tmp_path / "uses_shim.cpp"
+    cpp_src.write_text(PROGRAM)
+    subprocess.run(["g++", "-std=c++17", "-Wall", "-Wextra", "-Wpedantic", "-Wshadow",
+                    "-Wconversion", "-Werror", "-c", str(cpp_src), "-I",
+                    os.path.join(REPO, "include"), "-o", str(tmp_path / "uses_shim.o")],
+                   check=True)
