@@ -314,7 +314,8 @@ vh_status vh_filter_depth(vh_handle *h, const void *depth, int32_t depth_fmt, fl
  * NULL).  Blocks moved out are not seen by integration, extraction, export
  * or ray casting until they are moved back in; integrating a frame that
  * reaches them first starts them afresh (a later move-out then replaces the
- * stored copy). */
+ * stored copy).  Both directions wait for their copies before returning
+ * (the handle's stream is synchronised; they do not overlap frames). */
 vh_status vh_stream_out(vh_handle *h, const float *centre, float radius, int64_t *moved);
 /* Moves every stored block whose centre is within `radius` of centre[3]
  * back into the volume (radius = INFINITY: all of them).  The keys join the
