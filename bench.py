@@ -128,8 +128,10 @@ def make_frames(num, seed):
 
 
 def cpu_leg(frames, scene, seconds=15.0, threads=None):
-    """Times the oracle (all threads) on the first frames of the stream."""
+    """Times the oracle (all threads, or `threads`) on the first frames of
+    the stream."""
     from oracle.oracle import Oracle
+    all_threads = Oracle.max_threads()
     if threads:
         Oracle.set_threads(threads)
     cores = Oracle.max_threads()
@@ -144,9 +146,11 @@ def cpu_leg(frames, scene, seconds=15.0, threads=None):
         if time.perf_counter() - t0 > seconds:
             break
     dt = time.perf_counter() - t0
+    if threads:
+        Oracle.set_threads(all_threads)
     return {"value": n / dt, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"first {n} frames of the same stream (allocate+integrate+per-frame MC), "
-                      f"FP64 oracle, {cores} threads, {dt:.1f} s"}
+                      f"FP64 oracle, {cores} thread{'' if cores == 1 else 's'}, {dt:.1f} s"}
 
 
 def perturb_pose(pose, deg, metres, rng):
@@ -682,7 +686,11 @@ def run_engine(args):
     mc_ach = sum(mc_alg) / (sum(mc_ms) / 1000.0) / 1e9
     in_ach = sum(in_alg) / (sum(in_ms) / 1000.0) / 1e9
     peak, peak_src = peak_hbm()
-    cpu = cpu_leg(frames, scene, seconds=args.cpu_seconds)
+    cpu = None
+    if world == 1:  # the CPU baseline is rank 0's at N=1 only
+        cpu = cpu_leg(frames, scene, seconds=args.cpu_seconds)
+        one = cpu_leg(frames, scene, seconds=min(args.cpu_seconds, 5.0), threads=1)
+        cpu["single_thread"] = {"value": one["value"], "cores": 1, "sample": one["sample"]}
     adjoint = (adjoint_leg(args.adjoint_frames, local, args.adjoint_iterations)
                if args.adjoint_frames > 0 and rank == 0 else None)
     batched = (batched_leg(args.batch_scenes, args.batch_steps, local)
