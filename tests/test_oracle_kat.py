@@ -232,3 +232,34 @@ def test_mc_of_a_sphere_is_a_closed_genus_zero_surface():
     for g in range(len(verts)):
         same = f32[faces.ravel() == g]
         assert np.max(np.abs(same - same[0])) <= ulp
+
+
+def test_sample_gradient_equals_differences_of_the_sample():
+    """Within one trilinear cell the oracle's sdf sample is a polynomial, so
+    its reported gradient equals central differences of the sample (points
+    and steps chosen so that x +- h stays in the same cell)."""
+    from vhsdf import synth
+    s = synth.Scene(kind=1, seed=0, num_frames=4, width=160, height=120)
+    o = Oracle(160, 120, s.fx, s.fy, s.cx, s.cy, max_depth=4.5, voxel_size=0.02, trunc=0.08,
+               precision=64)
+    for f in range(3):
+        o.integrate(*s.render(f))
+    e = o.export()
+    rng = np.random.default_rng(3)
+    blk = e["xyz"][rng.integers(0, len(e["xyz"]), 400)]
+    cell = blk * 8 + rng.integers(0, 7, (400, 3))          # a cell inside the block
+    frac = rng.uniform(0.2, 0.8, (400, 3))
+    pts = (cell + frac) * 0.02
+    phi, grad, valid = o.sample(pts)
+    h = 1e-5
+    checked = 0
+    for a in range(3):
+        d = np.zeros(3)
+        d[a] = h
+        pp, _, vp = o.sample(pts + d)
+        pm, _, vm = o.sample(pts - d)
+        ok = valid & vp & vm
+        fd = (pp - pm) / (2 * h)
+        assert np.max(np.abs(fd[ok] - grad[ok, a])) < 1e-6 * max(1.0, np.max(np.abs(grad[ok, a])))
+        checked += ok.sum()
+    assert checked > 300
