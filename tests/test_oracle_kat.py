@@ -263,3 +263,44 @@ def test_sample_gradient_equals_differences_of_the_sample():
         assert np.max(np.abs(fd[ok] - grad[ok, a])) < 1e-6 * max(1.0, np.max(np.abs(grad[ok, a])))
         checked += ok.sum()
     assert checked > 300
+
+
+def _exp_se3(xi):
+    """exp of xi = (v, w): rotation by Rodrigues' formula, translation v."""
+    v, w = xi[:3], xi[3:]
+    th = np.linalg.norm(w)
+    K = np.array([[0, -w[2], w[1]], [w[2], 0, -w[0]], [-w[1], w[0], 0]])
+    R = np.eye(3) + K if th < 1e-300 else (np.eye(3) + np.sin(th) / th * K
+                                           + (1 - np.cos(th)) / th ** 2 * K @ K)
+    T = np.eye(4)
+    T[:3, :3], T[:3, 3] = R, v
+    return T
+
+
+def test_pose_terms_gradient_equals_differences_of_the_cost():
+    """For the left perturbation c2w -> exp(xi) c2w the oracle's J^T r is the
+    gradient of half the summed squared residuals: central differences of
+    that sum along random se(3) directions agree with (J^T r) . xi.  The
+    trilinear sample has slope jumps at cell faces; with ~18k residuals a
+    step of 1e-6 carries a few of them (errors ~1e-3), a step of 1e-8 none
+    here, and its rounding stays far below the tolerance."""
+    from vhsdf import synth
+    s = synth.Scene(kind=1, seed=0, num_frames=20, width=160, height=120)
+    o = Oracle(160, 120, s.fx, s.fy, s.cx, s.cy, max_depth=4.5, voxel_size=0.02, trunc=0.08,
+               precision=64)
+    for f in range(0, 8):
+        o.integrate(*s.render(f))
+    d, _, P = s.render(3)
+    P0 = _exp_se3(np.array([0.002, -0.001, 0.0015, 0.002, -0.001, 0.0005])) @ P.astype(np.float64)
+    t0 = o.pose_terms(d, P0)
+    assert t0[28] > 5000 and t0[27] > 0
+    rng = np.random.default_rng(1)
+    h = 1e-8
+    for _ in range(4):
+        xi = rng.normal(size=6)
+        xi /= np.linalg.norm(xi)
+        tp, tm = o.pose_terms(d, _exp_se3(h * xi) @ P0), o.pose_terms(d, _exp_se3(-h * xi) @ P0)
+        assert tp[28] == tm[28] == t0[28]  # same residual set on both sides
+        fd = (tp[27] - tm[27]) / (4 * h)
+        an = float(np.dot(t0[21:27], xi))
+        assert abs(fd - an) < 1e-5 * max(1.0, abs(an)), (fd, an)
