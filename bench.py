@@ -11,8 +11,10 @@ generator (no dataset is needed or present).
 
 Prints one JSON line (rank 0).  `value` is frames/s with the frames already
 in HBM (device time of each step, L2 flushed between steps); `e2e` is the
-same through the C ABI with host buffers (pinned), copies included, frames
-submitted back to back (`e2e.sync_per_frame`: one frame at a time).
+same through the C ABI with host buffers (pinned): each frame's depth and
+colour uploaded and its whole triangle mesh copied back to host memory,
+frames submitted back to back (`e2e.sync_per_frame`: one frame at a time;
+`e2e.mesh_left_on_device`: without the mesh copy).
 `--impl reference` times the CPU restatement of the reference's algorithm
 (oracle/) on all host cores on the same workload.
 """
@@ -534,10 +536,19 @@ def run_reference(args):
         "data": "synthetic", "config": WORKLOAD,
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{args.steps} timed frames after {args.warmup} warm-up "
-                                   f"frames, FP64 CPU restatement of the reference algorithm"},
+                                   f"frames: allocate + integrate + per-frame marching cubes "
+                                   f"of the FP64 CPU port in oracle/, canonical band rule"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "the reference's CUDA build cannot run this workload (400k-block table, "
-                "1e6-block staging buffer); the CPU restatement stands in for it",
+        "reference_class": "cpu_port_of_reference_algorithm",
+        "comparable_to_reference_cuda_build": False,
+        "note": "CPU port (oracle/vh_oracle.cpp, FP64) of the engine's rule, which is the "
+                "reference's camera math, integration update and marching cubes with the "
+                "benchmark's canonical band allocation and old-weight sdf average (not the "
+                "reference's DDA allocation or its w_new update).  The reference's CUDA build "
+                "is not run: it cannot hold this workload (400k-block per-frame tables, "
+                "1e6-block staging buffer), and on a shared GPU its table insert spins without "
+                "bound and its allocator traps when full; the comparison with it is "
+                "unmeasured",
     }), flush=True)
 
 
@@ -591,9 +602,14 @@ def run_engine(args):
                         stream.synchronize()
                     t0 = time.perf_counter()
                     starts[j].record(stream)
-                vol.process_frame(d, c, p, depth_format="u16")
+                if host:  # the frame's mesh comes back to pinned host memory
+                    vol.process_frame_mesh(d, c, p, mesh_bufs[0], one_count, depth_format="u16")
+                else:
+                    vol.process_frame(d, c, p, depth_format="u16")
                 if timed:
                     ends[j].record(stream)
+                    if host:
+                        vol.sync()  # the mesh copy-out is complete
                     st = vol.stats()  # synchronises; D2H of the frame's counters
                     wall.append(time.perf_counter() - t0)
                     stage.append(st)
@@ -634,15 +650,43 @@ def run_engine(args):
         cp = torch.empty(c.shape, dtype=torch.uint8, pin_memory=True).numpy()
         cp[...] = c
         pinned.append((dp, cp, p))
-    vol = Volume(**params)
+    cap = int(max(s["triangles"] for s in stage) * 1.25) + 4096
+    mesh_bufs = [torch.empty((cap, 12), dtype=torch.float32, pin_memory=True).numpy()
+                 for _ in range(3)]
+    one_count = np.zeros(1, np.int64)
+    vol = Volume(**dict(params, max_triangles=cap))
     vol.set_tuning(**tuning)
     vol.set_stream(stream.cuda_stream)
     _, _, wall = timed_pass(vol, host=True)  # one frame at a time: latency
     vol.close()
     e2e_sync_s = sum(wall)
-    # Throughput: frames submitted back to back (the engine's asynchronous
-    # mode), each with its host->device upload (overlapping the previous
-    # frame's kernels) and the 64-byte device->host copy of its counters.
+    # Throughput with the product result on the host: frames submitted back
+    # to back (the engine's asynchronous mode) through vh_process_frame_mesh,
+    # each with its host->device upload (overlapping the previous frame's
+    # kernels) and the device->host copy of its whole triangle mesh into
+    # pinned host memory (overlapping the next frame's kernels), as the
+    # reference's processFrame copies its triangles back every frame.
+    mesh_counts = [np.zeros(1, np.int64) for _ in range(nframes)]
+    vol = Volume(**dict(params, max_triangles=cap))
+    vol.set_tuning(**tuning)
+    vol.set_stream(stream.cuda_stream)
+    with torch.cuda.stream(stream):
+        for i in range(args.warmup):
+            vol.process_frame_mesh(*pinned[i], mesh_bufs[i % 3], mesh_counts[i],
+                                   depth_format="u16")
+        vol.sync()
+        t0 = time.perf_counter()
+        for i in range(args.warmup, nframes):
+            vol.process_frame_mesh(*pinned[i], mesh_bufs[i % 3], mesh_counts[i],
+                                   depth_format="u16")
+        vol.sync()
+        e2e_s = time.perf_counter() - t0
+    vol.close()
+    e2e_tris = [int(c[0]) for c in mesh_counts[args.warmup:]]
+    # the delivered counts are the device pass's, frame for frame
+    mesh_counts_match = e2e_tris == [int(s["triangles"]) for s in stage]
+    # The same with the mesh left on the device (vh_process_frame; only the
+    # 64-byte counters reach the host): what the copies cost.
     vol = Volume(**params)
     vol.set_tuning(**tuning)
     vol.set_stream(stream.cuda_stream)
@@ -654,10 +698,11 @@ def run_engine(args):
         for i in range(args.warmup, nframes):
             vol.process_frame(*pinned[i], depth_format="u16")
         vol.sync()
-        e2e_s = time.perf_counter() - t0
+        e2e_dev_s = time.perf_counter() - t0
     vol.close()
 
-    dev_ms, e2e_s, e2e_sync_s = replicas.reduce_max([dev_ms, e2e_s, e2e_sync_s], device="cuda")
+    dev_ms, e2e_s, e2e_sync_s, e2e_dev_s = replicas.reduce_max(
+        [dev_ms, e2e_s, e2e_sync_s, e2e_dev_s], device="cuda")
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
@@ -667,6 +712,7 @@ def run_engine(args):
     value = frames_total / (dev_ms / 1000.0)
     e2e = frames_total / e2e_s
     e2e_sync = frames_total / e2e_sync_s
+    e2e_dev = frames_total / e2e_dev_s
     # Rooflines.  Algorithmic bytes per launch:
     #   k_mc        12 B per voxel of every listed block (sdf, weight, rgb read
     #               once) + 48 B per output triangle (3 x float4 vertex)
@@ -701,15 +747,23 @@ def run_engine(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": dict(WORKLOAD, l2="flushed between steps (256 MiB memset), outside timing",
-                       parallelism="replicas" if world > 1 else "single"),
+        "config": WORKLOAD,
+        "l2": "flushed between steps (256 MiB memset), outside timing",
+        "parallelism": "replicas" if world > 1 else "single",
+        "voxel_updates_per_s": sum(updated) * world / (dev_ms / 1000.0),
         "e2e": {"value": e2e, "unit": UNIT,
                 "h2d_bytes_per_step": 2 * npx + 3 * npx + 80,
-                "d2h_bytes_per_step": 64,
-                "mode": "vh_process_frame on pinned host frames submitted back to back "
-                        "(asynchronous mode, one sync at the end); no L2 flush, the per-frame "
-                        "working set (listed blocks read, triangles written) exceeds L2",
-                "sync_per_frame": e2e_sync},
+                "d2h_bytes_per_step": 48 * statistics.mean(e2e_tris) + 64,
+                "mode": "vh_process_frame_mesh on pinned host frames submitted back to back "
+                        "(asynchronous mode, one sync at the end): per frame the depth + RGB "
+                        "upload and the copy of the frame's whole triangle mesh (48 B per "
+                        "triangle) into pinned host memory, plus the 64-byte counters; no L2 "
+                        "flush, the per-frame working set (listed blocks read, triangles "
+                        "written) exceeds L2",
+                "triangles_per_step": statistics.mean(e2e_tris),
+                "mesh_counts_match_device_pass": mesh_counts_match,
+                "sync_per_frame": e2e_sync,
+                "mesh_left_on_device": e2e_dev},
         "roofline": {"bound": "hbm", "achieved": mc_ach, "peak": peak, "unit": "GB/s",
                      "frac": mc_ach / peak, "traffic": 0.91 * statistics.mean(mc_alg),
                      "kernel": "k_mc", "peak_source": peak_src,
@@ -722,7 +776,9 @@ def run_engine(args):
                       for k in ("ms_allocate", "ms_integrate", "ms_extract", "ms_frame")},
         "per_frame": {"blocks": statistics.mean(blocks), "voxels_updated": statistics.mean(updated),
                       "triangles": statistics.mean(tris)},
-        "gpu_launches": 5 * args.steps,  # frame_begin, allocate, resolve, integrate, mc
+        # kernels of the timed frames as the engine counted them when it
+        # enqueued each frame (frame_begin, allocate, resolve, integrate, mc)
+        "gpu_launches": sum(s["frame_kernels"] for s in stage),
         "tuning": tuning,
         "wall_s": t_wall,
         "clocks": clk.summary(),

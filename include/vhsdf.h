@@ -108,7 +108,7 @@ typedef struct vh_stats {
   int64_t table_slots;
   int64_t tombstones;        /* erased hash slots not yet reclaimed         */
   uint32_t device_error;     /* sticky device error bits (0 = none)         */
-  uint32_t reserved;
+  uint32_t frame_kernels;    /* kernels launched by the last frame          */
   /* per-stage device time of the last frame in ms (VH_FLAG_PROFILE only)   */
   float ms_allocate, ms_integrate, ms_extract, ms_frame;
 } vh_stats;
@@ -188,6 +188,24 @@ vh_status vh_extract(vh_handle *h, int32_t scope, vh_mesh_view *out);
 vh_status vh_process_frame(vh_handle *h, const void *depth, int32_t depth_fmt,
                            const uint8_t *rgb, const float *c2w, int32_t mem,
                            vh_mesh_view *out);
+/* vh_process_frame with the frame's triangles delivered to host memory, as
+ * processFrame copies its triangle buffer back every frame
+ * (src/tsdf.cu:1554-1564): tris receives min(n, capacity) triangles in the
+ * vh_mesh_view layout (12 floats each) and *num_triangles the frame's count
+ * n.  With VH_FLAG_SYNC both are written before the call returns.
+ * Otherwise the call returns once the frame is enqueued: the next
+ * vh_process_frame_mesh call (after enqueuing its own frame, so the copy
+ * overlaps that frame's kernels) or vh_sync writes *num_triangles and issues
+ * the copy-out, and a frame's triangles are complete in `tris` once the
+ * second vh_process_frame_mesh call after it, or vh_sync, has returned.
+ * Until then `tris` and `num_triangles` must stay valid (three host buffers
+ * used in turn are enough for a stream of frames).  Pinned host memory keeps
+ * the copy asynchronous.  A mesh larger than `capacity` is truncated and
+ * reported as VH_ERR_CAPACITY (by vh_sync when asynchronous).  Two device
+ * triangle buffers of max_triangles each are added on first use. */
+vh_status vh_process_frame_mesh(vh_handle *h, const void *depth, int32_t depth_fmt,
+                                const uint8_t *rgb, const float *c2w, int32_t mem, float *tris,
+                                int64_t capacity, int64_t *num_triangles);
 /* Copies the last extraction to host: xyz (9 floats per triangle, voxel
  * units) and rgb (9 bytes per triangle).  Output copies and size queries
  * (all outputs NULL) follow one rule for every copy-out call here: the full
@@ -237,7 +255,10 @@ vh_status vh_find_keys(vh_handle *h, const int32_t *xyz, int64_t n,
  * keys per call, else VH_ERR_CAPACITY.  Its scratch is a fixed 1 MiB array
  * that every GPU loading this library holds until the process exits; the
  * first call on a device looks up that array's address, so make the first
- * call before any stream capture.  All calls share the array: calls that
+ * call before any stream capture.  The address is kept for the life of the
+ * process: a cudaDeviceReset of that device invalidates it (and every
+ * handle on the device), so do not reset a device this library is using.
+ * All calls share the array: calls that
  * overlap on the GPU (other threads, other handles on the same GPU) race and
  * must be serialised by the caller.  The call waits for its result. */
 vh_status vh_find_keys_noalloc(vh_handle *h, const int32_t *xyz, int64_t n,
@@ -313,13 +334,19 @@ vh_status vh_filter_depth(vh_handle *h, const void *depth, int32_t depth_fmt, fl
  * identical), freeing its pool block; *moved receives the count (may be
  * NULL).  Blocks moved out are not seen by integration, extraction, export
  * or ray casting until they are moved back in; integrating a frame that
- * reaches them first starts them afresh (a later move-out then replaces the
- * stored copy).  Both directions wait for their copies before returning
- * (the handle's stream is synchronised; they do not overlap frames). */
+ * reaches them first starts them afresh, and the two copies are merged when
+ * they meet again (moved in, or moved out once more): per voxel the weighted
+ * average of the two partial averages, sdf (a w_a + b w_b) / (w_a + w_b) in
+ * fp32 and colour floor((c_a w_a + c_b w_b) / (w_a + w_b)), weights added;
+ * a voxel observed by one copy only keeps that copy's values.  Both
+ * directions wait for their copies before returning (the handle's stream is
+ * synchronised; they do not overlap frames). */
 vh_status vh_stream_out(vh_handle *h, const float *centre, float radius, int64_t *moved);
 /* Moves every stored block whose centre is within `radius` of centre[3]
- * back into the volume (radius = INFINITY: all of them).  The keys join the
- * current block list, as vh_alloc_keys does. */
+ * back into the volume (radius = INFINITY: all of them): a block with no
+ * resident copy comes back bit-identical, one that a frame re-created is
+ * merged as vh_stream_out describes.  The keys join the current block list,
+ * as vh_alloc_keys does. */
 vh_status vh_stream_in(vh_handle *h, const float *centre, float radius, int64_t *moved);
 /* Blocks currently in the host store. */
 int64_t vh_host_blocks(const vh_handle *h);

@@ -2,10 +2,10 @@
 
 Builds oracle/ref_golden (the reference's unmodified src/tsdf.cu plus a
 host-side driver, outputs under oracle/_ref/) and runs it on the CPU.  Needs
-the reference checkout at /root/reference (or $VH_REFERENCE); the committed
+the reference checkout named by $VH_REFERENCE; the committed
 JSON is what the tests read, so the tests themselves never need the reference.
 
-    python tests/golden/make_golden.py
+    VH_REFERENCE=<reference checkout> python tests/golden/make_golden.py
 """
 import json
 import os
@@ -14,7 +14,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("VH_REFERENCE", "/root/reference")
+REF = os.environ.get("VH_REFERENCE", "")
 
 
 def build_and_run():
@@ -26,8 +26,8 @@ def build_and_run():
 
 
 def main():
-    if not os.path.isdir(REF):
-        print(f"reference not found at {REF}", file=sys.stderr)
+    if not REF or not os.path.isdir(REF):
+        print("set VH_REFERENCE to the reference checkout", file=sys.stderr)
         return 1
     data = build_and_run()
     data["_source"] = ("outputs of the reference's host code (include/tsdf.cuh, "

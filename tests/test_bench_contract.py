@@ -34,6 +34,12 @@ def test_reference_arm_prints_the_benchmark_line():
     assert cpu["value"] == d["value"] and cpu["unit"] == d["unit"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}
+    # labelled as the CPU port, and on exactly the engine arm's config
+    assert d["reference_class"] == "cpu_port_of_reference_algorithm"
+    assert d["comparable_to_reference_cuda_build"] is False
+    sys.path.insert(0, REPO)
+    import bench
+    assert d["config"] == json.loads(json.dumps(bench.WORKLOAD))
 
 
 def test_reference_arm_runs_on_rank_zero_only():

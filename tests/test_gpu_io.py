@@ -152,3 +152,34 @@ def test_gpu_vertex_merge_matches_reference_rule(scene, tmp_path):
     path2 = tmp_path / "m2.ply"
     vol.save_ply(path2, binary=True)
     assert path.read_bytes() == path2.read_bytes()
+
+
+def test_bad_snapshot_leaves_the_volume_unchanged(scene, tmp_path):
+    """A snapshot that the import would reject (a fractional weight, more
+    blocks than the pool holds) is refused before the volume is cleared."""
+    vol = volume_for(scene)
+    for f in range(3):
+        vol.integrate(*scene.render(f))
+    good = tmp_path / "good.vhs"
+    vol.save(good)
+    n = len(vol.export_blocks()["xyz"])
+    raw = bytearray(good.read_bytes())
+    header = 8 + 4 + 4 + 4 + 4 + 8
+    w_off = header + 12 * n + 2048 * n  # first weight of the first block
+    raw[w_off:w_off + 4] = np.float32(0.5).tobytes()
+    bad = tmp_path / "bad_weight.vhs"
+    bad.write_bytes(bytes(raw))
+
+    other = volume_for(scene)
+    other.integrate(*scene.render(5))
+    before = other.export_blocks()
+    with pytest.raises(VhError):
+        other.load(bad)
+    assert_same_blocks(other.export_blocks(), before)
+    small = volume_for(scene, pool_blocks=max(n // 2, 4))
+    small.alloc_keys(np.array([[0, 0, 0], [1, 0, 0]], np.int32))
+    before = small.export_blocks()
+    assert len(before["xyz"]) == 2
+    with pytest.raises(VhError):
+        small.load(good)
+    assert_same_blocks(small.export_blocks(), before)

@@ -106,3 +106,79 @@ def test_repeated_streaming_keeps_the_table_usable(gpu):
     assert vol.stats()["tombstones"] == 0
     assert_same_blocks(vol.export_blocks(), before)
     vol.integrate(*frames[0])  # integration goes on after a rebuild
+
+
+def merge_expected(old, new):
+    """numpy restatement of the documented merge of two copies of a volume:
+    per voxel (a w_a + b w_b) / (w_a + w_b) in float32 (older copy first),
+    colour floor((c_a w_a + c_b w_b) / (w_a + w_b)), weights added; a voxel
+    seen by one copy keeps that copy's values; keys in one copy only stay."""
+    old, new = sort_blocks(old), sort_blocks(new)
+    keys = {tuple(k): i for i, k in enumerate(old["xyz"].tolist())}
+    out = {k: [] for k in ("xyz", "sdf", "weight", "rgb")}
+    seen = set()
+    for j, k in enumerate(new["xyz"].tolist()):
+        seen.add(tuple(k))
+        sdf, w, c = new["sdf"][j].copy(), new["weight"][j].copy(), new["rgb"][j].copy()
+        i = keys.get(tuple(k))
+        if i is not None:
+            os_, ow, oc = old["sdf"][i], old["weight"][i], old["rgb"][i]
+            only_old = (w == 0) & (ow > 0)
+            both = (w > 0) & (ow > 0)
+            wn = (ow + w).astype(np.float32)
+            num = (os_ * ow).astype(np.float32) + (sdf * w).astype(np.float32)
+            merged = np.divide(num.astype(np.float32), wn, out=np.zeros_like(wn), where=wn > 0)
+            csum = oc.astype(np.int64) * ow.astype(np.int64)[:, None] + \
+                c.astype(np.int64) * w.astype(np.int64)[:, None]
+            cm = (csum // np.maximum(wn, 1).astype(np.int64)[:, None]).astype(np.uint8)
+            sdf = np.where(both, merged, np.where(only_old, os_, sdf))
+            c = np.where(both[:, None], cm, np.where(only_old[:, None], oc, c))
+            w = np.where(both, wn, np.where(only_old, ow, w))
+        out["xyz"].append(k)
+        out["sdf"].append(sdf)
+        out["weight"].append(w)
+        out["rgb"].append(c)
+    for i, k in enumerate(old["xyz"].tolist()):
+        if tuple(k) not in seen:
+            out["xyz"].append(k)
+            for f in ("sdf", "weight", "rgb"):
+                out[f].append(old[f][i])
+    return {"xyz": np.array(out["xyz"], np.int32), "sdf": np.array(out["sdf"], np.float32),
+            "weight": np.array(out["weight"], np.float32), "rgb": np.array(out["rgb"], np.uint8)}
+
+
+def sort_blocks(e):
+    order = np.lexsort(e["xyz"].T[::-1])
+    return {k: v[order] for k, v in e.items()}
+
+
+@pytest.mark.parametrize("back_by", ["stream_in", "stream_out_then_in"])
+def test_recreated_blocks_merge_with_their_stored_copies(gpu, back_by):
+    """A frame that reaches moved-out blocks re-creates them; when the stored
+    copy meets the resident one again (moved in, or the new one moved out as
+    well) the two are merged, so no observation is lost: the result equals
+    the merge of the oracle's two partial volumes."""
+    from helpers import oracle_for
+    s, frames = room_stream(8)
+    vol = make_volume(s, 1 << 16)
+    first, later = frames[:4], frames[4:]
+    for d, c, p in first:
+        vol.integrate(d, c, p)
+    n = vol.stream_out([0, 0, 0], 0.0)
+    assert n > 0 and vol.stats()["blocks_allocated"] == 0
+    for d, c, p in later:  # reaches (most of) the moved-out blocks again
+        vol.integrate(d, c, p)
+    o_old, o_new = oracle_for(vol, 32), oracle_for(vol, 32)
+    for d, c, p in first:
+        o_old.integrate(d, c, p)
+    for d, c, p in later:
+        o_new.integrate(d, c, p)
+    old, new = o_old.export(), o_new.export()
+    both = len(set(map(tuple, old["xyz"].tolist())) & set(map(tuple, new["xyz"].tolist())))
+    assert both > n // 2  # the later frames overlap the stored blocks
+    if back_by == "stream_out_then_in":
+        vol.stream_out([0, 0, 0], 0.0)  # merges on the host store
+        assert vol.host_blocks() == len(merge_expected(old, new)["xyz"])
+    vol.stream_in([0, 0, 0])
+    assert vol.host_blocks() == 0
+    assert_same_blocks(vol.export_blocks(), merge_expected(old, new))

@@ -35,6 +35,10 @@ using namespace vh;
 
 namespace {
 constexpr int kNumEvents = 5;
+// Marching-cubes mode of a frame graph: none, into the handle's triangle
+// buffer (vh_process_frame, vh_extract), or into mesh slot 0 / 1 of
+// vh_process_frame_mesh.
+enum { kMcNone = 0, kMcMain = 1, kMcSlot0 = 2, kMcSlot1 = 3, kMcModes = 4 };
 }  // namespace
 
 struct vh_handle {
@@ -66,9 +70,30 @@ struct vh_handle {
   int in_used = -1;  // slot read by the frame being enqueued (-1: device inputs)
   DevState *h_state = nullptr;    // pinned, mapped
   DevState *h_state_dev = nullptr;  // its device address (k_state_out)
-  cudaGraphExec_t graphs[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
-  cudaGraph_t graph_src[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
-  cudaGraphNode_t graph_fb[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // k_frame_begin
+  // Frame graphs per depth format and marching-cubes mode (kMc*).
+  cudaGraphExec_t graphs[2][kMcModes] = {};
+  cudaGraph_t graph_src[2][kMcModes] = {};
+  cudaGraphNode_t graph_fb[2][kMcModes] = {};  // k_frame_begin
+  int frame_kernels = 0;  // kernels one frame launches (counted when enqueued)
+  // Per-frame meshes to host (vh_process_frame_mesh): two device triangle
+  // buffers and two mapped counter mirrors, used by alternate frames, so that
+  // one frame's copy-out overlaps the next frame's kernels.
+  float4 *d_mtris[2] = {nullptr, nullptr};
+  int64_t mtri_cap = 0;
+  DevState *h_mstate = nullptr;      // 2 entries, pinned and mapped
+  DevState *h_mstate_dev = nullptr;  // their device address
+  cudaStream_t mesh_stream = nullptr;
+  cudaEvent_t mesh_done[2] = {}, mesh_copied[2] = {};
+  bool mesh_copy_issued[2] = {false, false};
+  int mesh_slot = 0;
+  struct PendingMesh {
+    bool valid = false;
+    int slot = 0;
+    float *tris = nullptr;
+    int64_t capacity = 0;
+    int64_t *count = nullptr;
+  } pending;
+  bool mesh_overflow = false;  // a frame had more triangles than its host buffer
   cudaEvent_t ev[kNumEvents] = {};
   bool ev_pending = false;
   bool ev_has_mc = false;
@@ -186,39 +211,57 @@ void stage_event(cudaEvent_t ev, cudaStream_t s, bool capturing) {
     cudaEventRecord(ev, s);
 }
 
-// Enqueues one frame's kernels (optionally with per-stage events).
-void enqueue_frame(vh_handle *h, int fmt, bool with_mc, bool events, bool capturing) {
+// Enqueues one frame's kernels (optionally with per-stage events); mc is a
+// kMc* mode.  Counts the kernels it launches into h->frame_kernels.
+void enqueue_frame(vh_handle *h, int fmt, int mc, bool events, bool capturing) {
   cudaStream_t s = h->stream;
+  int kernels = 0;
   if (events) stage_event(h->ev[0], s, capturing);
   launch_frame_begin(h->V, &h->fin, h->d_fin, s);
+  ++kernels;
   const void *depth = nullptr;  // the frame's own image, found through d_fin
   if (h->p.flags & VH_FLAG_DEPTH_FILTER) {
     launch_depth_filter(h->C, nullptr, h->d_fin, fmt, h->d_depth_f, s);
+    ++kernels;
     depth = h->d_depth_f;
     fmt = VH_DEPTH_F32_M;
   }
   launch_allocate(h->V, h->C, h->d_fin, depth, fmt, h->d_pix, s);
-  launch_frame_resolve(h->V, h->sm_count * 8, with_mc, s);  // probes in flight: many CTAs
+  launch_frame_resolve(h->V, h->sm_count * 8, mc != kMcNone, s);  // probes in flight: many CTAs
+  kernels += 2;
   if (events) stage_event(h->ev[1], s, capturing);
   launch_integrate(h->V, h->C, h->d_pix, h->d_fin->pose, integrate_grid(h),
                    h->tuning.integrate_variant, s);
+  ++kernels;
   if (events) stage_event(h->ev[2], s, capturing);
   // Without VH_FLAG_SYNC every frame still brings its counters to the host
   // mirror (a 64-byte in-stream write to mapped memory, no copy on the
   // stream): by the last MC CTA, or by k_state_out after an integration.
+  // Frames of vh_process_frame_mesh use their slot's own mirror and buffer.
   DevState *mirror = (h->p.flags & VH_FLAG_SYNC) ? nullptr : h->h_state_dev;
-  if (with_mc) {
-    launch_mc(h->V, 0, h->C.mc_min_weight, h->d_tris, (uint32_t)h->tri_cap, mc_grid(h),
-              h->tuning.mc_variant, mirror, s);
+  if (mc != kMcNone) {
+    float4 *tris = h->d_tris;
+    int64_t cap = h->tri_cap;
+    if (mc == kMcSlot0 || mc == kMcSlot1) {
+      const int k = mc - kMcSlot0;
+      tris = h->d_mtris[k];
+      cap = h->mtri_cap;
+      mirror = h->h_mstate_dev + k;
+    }
+    launch_mc(h->V, 0, h->C.mc_min_weight, tris, (uint32_t)cap, mc_grid(h), h->tuning.mc_variant,
+              mirror, s);
+    ++kernels;
     if (events) stage_event(h->ev[3], s, capturing);
   } else if (mirror) {
     launch_state_out(h->V, mirror, s);
+    ++kernels;
   }
+  h->frame_kernels = kernels;
 }
 
 void drop_graphs(vh_handle *h) {
   for (int a = 0; a < 2; ++a)
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < kMcModes; ++b) {
       if (h->graphs[a][b]) cudaGraphExecDestroy(h->graphs[a][b]);
       if (h->graph_src[a][b]) cudaGraphDestroy(h->graph_src[a][b]);
       h->graphs[a][b] = nullptr;
@@ -245,16 +288,16 @@ void apply_tuning(vh_handle *h, const vh_tuning &t) {
 // Runs the frame chain as a CUDA graph (captured on first use) or directly.
 vh_status inputs_consumed(vh_handle *h);
 
-vh_status run_frame(vh_handle *h, int fmt, bool with_mc) {
+vh_status run_frame(vh_handle *h, int fmt, int mc) {
   const bool events = (h->p.flags & VH_FLAG_PROFILE) != 0;
   const bool graphs_ok = !(h->p.flags & VH_FLAG_NO_GRAPH) && h->stream != nullptr;
   if (graphs_ok) {
-    const int m = with_mc ? 1 : 0;
+    const int m = mc;
     cudaGraphExec_t &g = h->graphs[fmt][m];
     if (!g) {  // captured with this frame's descriptor
       cudaGraph_t graph = nullptr;
       VH_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-      enqueue_frame(h, fmt, with_mc, events, true);
+      enqueue_frame(h, fmt, mc, events, true);
       cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
       if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
       e = cudaGraphInstantiate(&g, graph, 0);
@@ -275,11 +318,11 @@ vh_status run_frame(vh_handle *h, int fmt, bool with_mc) {
     }
     VH_CUDA(h, cudaGraphLaunch(g, h->stream));
   } else {
-    enqueue_frame(h, fmt, with_mc, events, false);
+    enqueue_frame(h, fmt, mc, events, false);
     VH_CUDA(h, cudaGetLastError());
   }
   h->ev_pending = events;
-  h->ev_has_mc = with_mc;
+  h->ev_has_mc = mc != kMcNone;
   return inputs_consumed(h);
 }
 
@@ -331,6 +374,14 @@ vh_status inputs_consumed(vh_handle *h) {
 
 void free_all(vh_handle *h) {
   if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
+  if (h->mesh_stream) cudaStreamSynchronize(h->mesh_stream);
+  for (int k = 0; k < 2; ++k) {
+    cudaFree(h->d_mtris[k]);
+    if (h->mesh_done[k]) cudaEventDestroy(h->mesh_done[k]);
+    if (h->mesh_copied[k]) cudaEventDestroy(h->mesh_copied[k]);
+  }
+  if (h->h_mstate) cudaFreeHost(h->h_mstate);
+  if (h->mesh_stream) cudaStreamDestroy(h->mesh_stream);
   drop_graphs(h);
   refine_ctx_free(h->refine);
   h->refine = nullptr;
@@ -419,6 +470,75 @@ vh_status grow_tris(vh_handle *h, int64_t need) {
   drop_graphs(h);  // captured graphs hold the old pointer
   VH_CUDA(h, cudaMalloc(&h->d_tris, sizeof(float4) * 3 * (size_t)cap));
   h->tri_cap = cap;
+  return VH_OK;
+}
+
+// First use of vh_process_frame_mesh: the two slot buffers, their mapped
+// counter mirrors, the copy-out stream and its events.
+vh_status mesh_setup(vh_handle *h) {
+  if (h->mesh_stream) return VH_OK;
+  const int64_t cap = h->tri_cap ? h->tri_cap : 1;
+  bool ok = cudaMalloc(&h->d_mtris[0], sizeof(float4) * 3 * (size_t)cap) == cudaSuccess &&
+            cudaMalloc(&h->d_mtris[1], sizeof(float4) * 3 * (size_t)cap) == cudaSuccess &&
+            cudaHostAlloc(&h->h_mstate, 2 * sizeof(DevState), cudaHostAllocMapped) == cudaSuccess &&
+            cudaHostGetDevicePointer(&h->h_mstate_dev, h->h_mstate, 0) == cudaSuccess;
+  for (int k = 0; ok && k < 2; ++k)
+    ok = cudaEventCreateWithFlags(&h->mesh_done[k], cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&h->mesh_copied[k], cudaEventDisableTiming) == cudaSuccess;
+  if (ok) ok = cudaStreamCreateWithFlags(&h->mesh_stream, cudaStreamNonBlocking) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    for (int k = 0; k < 2; ++k) {
+      cudaFree(h->d_mtris[k]);
+      h->d_mtris[k] = nullptr;
+      if (h->mesh_done[k]) cudaEventDestroy(h->mesh_done[k]);
+      if (h->mesh_copied[k]) cudaEventDestroy(h->mesh_copied[k]);
+      h->mesh_done[k] = h->mesh_copied[k] = nullptr;
+    }
+    if (h->h_mstate) cudaFreeHost(h->h_mstate);
+    h->h_mstate = h->h_mstate_dev = nullptr;
+    return fail(h, VH_ERR_CUDA, "per-frame mesh buffers: allocation failed");
+  }
+  std::memset(h->h_mstate, 0, 2 * sizeof(DevState));
+  h->mtri_cap = cap;
+  return VH_OK;
+}
+
+// Issues the copy-out of the pending mesh frame: waits (host) for that
+// frame's kernels, reads its triangle count from its slot's mirror and
+// copies the triangles into the caller's buffer on the mesh stream.
+vh_status mesh_flush(vh_handle *h) {
+  if (!h->pending.valid) return VH_OK;
+  vh_handle::PendingMesh p = h->pending;
+  h->pending.valid = false;
+  VH_CUDA(h, cudaEventSynchronize(h->mesh_done[p.slot]));
+  const int64_t n = h->h_mstate[p.slot].tri_count;
+  const int64_t m = std::min(std::min(n, p.capacity), h->mtri_cap);
+  if (m > 0)
+    VH_CUDA(h, cudaMemcpyAsync(p.tris, h->d_mtris[p.slot], sizeof(float4) * 3 * (size_t)m,
+                               cudaMemcpyDeviceToHost, h->mesh_stream));
+  VH_CUDA(h, cudaEventRecord(h->mesh_copied[p.slot], h->mesh_stream));
+  h->mesh_copy_issued[p.slot] = true;
+  if (p.count) *p.count = n;
+  if (n > p.capacity) h->mesh_overflow = true;
+  // the copy issued by the previous flush (the frame before) is complete
+  // when this returns: a caller may reuse that frame's buffer
+  const int q = p.slot ^ 1;
+  if (h->mesh_copy_issued[q]) VH_CUDA(h, cudaEventSynchronize(h->mesh_copied[q]));
+  return VH_OK;
+}
+
+// Every pending mesh copied out; a mesh larger than its host buffer is
+// reported (once) as VH_ERR_CAPACITY.
+vh_status mesh_drain(vh_handle *h) {
+  if (!h->mesh_stream) return VH_OK;
+  vh_status s = mesh_flush(h);
+  if (s != VH_OK) return s;
+  VH_CUDA(h, cudaStreamSynchronize(h->mesh_stream));
+  if (h->mesh_overflow) {
+    h->mesh_overflow = false;
+    return fail(h, VH_ERR_CAPACITY, "a frame's mesh was larger than its host buffer");
+  }
   return VH_OK;
 }
 
@@ -664,7 +784,9 @@ vh_status vh_set_stream(vh_handle *h, void *stream) {
 vh_status vh_sync(vh_handle *h) {
   VH_HANDLE_DEVICE(h);
   if (!h) return VH_ERR_INVALID_ARG;
-  return sync_and_check(h);
+  vh_status s = mesh_drain(h);
+  vh_status t = sync_and_check(h);
+  return s != VH_OK ? s : t;
 }
 
 const char *vh_last_error(const vh_handle *h) { return h ? h->last_error.c_str() : "null handle"; }
@@ -675,7 +797,7 @@ vh_status vh_integrate(vh_handle *h, const void *depth, int32_t depth_fmt, const
   if (!h) return VH_ERR_INVALID_ARG;
   vh_status s = stage_inputs(h, depth, depth_fmt, rgb, c2w, mem);
   if (s != VH_OK) return s;
-  s = run_frame(h, depth_fmt, false);
+  s = run_frame(h, depth_fmt, kMcNone);
   if (s != VH_OK) return s;
   h->frames++;
   h->nb_valid = true;
@@ -725,7 +847,7 @@ vh_status vh_process_frame(vh_handle *h, const void *depth, int32_t depth_fmt, c
   if (!h) return VH_ERR_INVALID_ARG;
   vh_status s = stage_inputs(h, depth, depth_fmt, rgb, c2w, mem);
   if (s != VH_OK) return s;
-  s = run_frame(h, depth_fmt, true);
+  s = run_frame(h, depth_fmt, kMcMain);
   if (s != VH_OK) return s;
   h->frames++;
   h->nb_valid = true;
@@ -736,6 +858,52 @@ vh_status vh_process_frame(vh_handle *h, const void *depth, int32_t depth_fmt, c
     out->num_triangles = std::min<int64_t>(h->h_state->tri_count, h->tri_cap);
     out->voxel_size = h->p.voxel_size;
   }
+  return s;
+}
+
+vh_status vh_process_frame_mesh(vh_handle *h, const void *depth, int32_t depth_fmt,
+                                const uint8_t *rgb, const float *c2w, int32_t mem, float *tris,
+                                int64_t capacity, int64_t *num_triangles) {
+  VH_HANDLE_DEVICE(h);
+  if (!h) return VH_ERR_INVALID_ARG;
+  if (capacity < 0 || (capacity > 0 && !tris) || !num_triangles)
+    return fail(h, VH_ERR_INVALID_ARG, "mesh output: null buffer or negative capacity");
+  vh_status s = stage_inputs(h, depth, depth_fmt, rgb, c2w, mem);
+  if (s != VH_OK) return s;
+  if (h->p.flags & VH_FLAG_SYNC) {  // the reference's blocking order
+    s = run_frame(h, depth_fmt, kMcMain);
+    if (s != VH_OK) return s;
+    h->frames++;
+    h->nb_valid = true;
+    s = sync_and_check(h);
+    const int64_t n = std::min<int64_t>(h->h_state->tri_count, h->tri_cap);
+    *num_triangles = h->h_state->tri_count;
+    const int64_t m = std::min(n, capacity);
+    if (m > 0)
+      VH_CUDA(h, cudaMemcpy(tris, h->d_tris, sizeof(float4) * 3 * (size_t)m,
+                            cudaMemcpyDeviceToHost));
+    if (s != VH_OK) return s;
+    if (n > capacity) return fail(h, VH_ERR_CAPACITY, "the frame's mesh is larger than its buffer");
+    return VH_OK;
+  }
+  s = mesh_setup(h);
+  if (s != VH_OK) return s;
+  const int k = h->mesh_slot;
+  // slot k's buffer was last read by the copy-out of the frame two back
+  if (h->mesh_copy_issued[k]) VH_CUDA(h, cudaStreamWaitEvent(h->stream, h->mesh_copied[k], 0));
+  s = run_frame(h, depth_fmt, kMcSlot0 + k);
+  if (s != VH_OK) return s;
+  h->frames++;
+  h->nb_valid = true;
+  VH_CUDA(h, cudaEventRecord(h->mesh_done[k], h->stream));
+  // this frame is queued behind the pending one: copy that one out now
+  s = mesh_flush(h);
+  h->pending.valid = true;
+  h->pending.slot = k;
+  h->pending.tris = tris;
+  h->pending.capacity = capacity;
+  h->pending.count = num_triangles;
+  h->mesh_slot = k ^ 1;
   return s;
 }
 
@@ -989,6 +1157,23 @@ vh_status vh_export_blocks(vh_handle *h, int32_t *xyz, float *sdf, float *weight
   return VH_OK;
 }
 
+// Host-side checks of a block set before anything on the device changes.
+// Weights are observation counts: integration adds 1 per update, and its
+// exact colour average relies on whole weights.  Keys must lie in the key
+// range; `replace`: the set will replace the volume, so it must fit the pool.
+static vh_status check_blocks(vh_handle *h, const int32_t *xyz, const float *weight, int64_t n,
+                              bool replace) {
+  for (size_t i = 0, m = (size_t)n * kB3; i < m; ++i)
+    if (!(weight[i] >= 0.0f && weight[i] <= 16777216.0f && weight[i] == std::floor(weight[i])))
+      return fail(h, VH_ERR_INVALID_ARG, "block weights must be whole numbers in [0, 2^24]");
+  for (int64_t i = 0; i < n; ++i)
+    if (!key_in_range(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]))
+      return fail(h, VH_ERR_OUT_OF_RANGE, "a block coordinate lies outside [-2^20, 2^20)");
+  if (replace && n > h->p.pool_blocks)
+    return fail(h, VH_ERR_POOL_FULL, "more blocks than the pool holds (raise pool_blocks)");
+  return VH_OK;
+}
+
 vh_status vh_import_blocks(vh_handle *h, const int32_t *xyz, const float *sdf, const float *weight,
                            const uint8_t *rgb, int64_t n) {
   VH_HANDLE_DEVICE(h);
@@ -996,11 +1181,8 @@ vh_status vh_import_blocks(vh_handle *h, const int32_t *xyz, const float *sdf, c
   if (!h || n < 0 || (n && (!xyz || !sdf || !weight || !rgb)) || n > (1ll << 24))
     return VH_ERR_INVALID_ARG;
   if (!n) return VH_OK;
-  // Weights are observation counts: integration adds 1 per update, and its
-  // exact colour average relies on whole weights.
-  for (size_t i = 0, m = (size_t)n * kB3; i < m; ++i)
-    if (!(weight[i] >= 0.0f && weight[i] <= 16777216.0f && weight[i] == std::floor(weight[i])))
-      return fail(h, VH_ERR_INVALID_ARG, "block weights must be whole numbers in [0, 2^24]");
+  vh_status cs = check_blocks(h, xyz, weight, n, false);
+  if (cs != VH_OK) return cs;
   DevBuf<int32_t> dk;
   DevBuf<float> ds, dw;
   DevBuf<uint8_t> dc;
@@ -1048,9 +1230,14 @@ vh_status vh_load(vh_handle *h, const char *path) {
     return fail(h, VH_ERR_IO, std::string("cannot read snapshot ") + path);
   if (voxel != h->p.voxel_size)
     return fail(h, VH_ERR_INVALID_ARG, "snapshot voxel size differs from the handle's");
-  vh_status s = clear_volume(h, true);
-  if (s != VH_OK) return s;
   const int64_t n = (int64_t)xyz.size() / 3;
+  // Everything the import would reject is rejected before the volume is
+  // cleared, so a bad snapshot leaves the caller's volume unchanged.
+  if (n > (1ll << 24)) return fail(h, VH_ERR_INVALID_ARG, "snapshot holds more than 2^24 blocks");
+  vh_status s = check_blocks(h, xyz.data(), w.data(), n, true);
+  if (s != VH_OK) return s;
+  s = clear_volume(h, true);
+  if (s != VH_OK) return s;
   s = vh_import_blocks(h, xyz.data(), sdf.data(), w.data(), rgb.data(), n);
   if (s != VH_OK) return s;
   return vh_clear_block_list(h);
@@ -1073,6 +1260,7 @@ vh_status vh_get_stats(vh_handle *h, vh_stats *out) {
   out->table_slots = (int64_t)h->V.slot_mask + 1;
   out->tombstones = d.tombstones;
   out->device_error = d.error;
+  out->frame_kernels = (uint32_t)h->frame_kernels;
   out->ms_allocate = h->stage.ms_allocate;
   out->ms_integrate = h->stage.ms_integrate;
   out->ms_extract = h->stage.ms_extract;

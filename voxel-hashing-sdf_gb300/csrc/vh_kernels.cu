@@ -378,6 +378,11 @@ __global__ void __launch_bounds__(256, 6) k_allocate(VolumeView V, CamParams C,
 //  * w <= 65537: a reciprocal estimate (error < 1) corrected by one exact
 //    integer remainder test.
 // Larger weights use the fp32 formula itself.
+// The equality holds for the rule with IEEE fp32 division (the oracle's).
+// The reference builds with -use_fast_math, whose '/' is an approximate
+// division: an exact quotient such as 300 / 3 can come out just below the
+// integer there and truncate one lower, so its GPU build may differ from
+// this by 1 on such voxels.
 __device__ __forceinline__ uint32_t blend_colour(uint32_t old_rgb, uint32_t new_rgb, float w_old,
                                                  float w_new) {
   uint32_t out = 0;

@@ -31,7 +31,10 @@ std::mutex g_setup_mu;
 int32_t *g_scratch_ptr[kMaxDevices] = {};
 
 // Device address of the scratch array on `device`, looked up once per device
-// with that device current (the caller's current device is restored).
+// with that device current (the caller's current device is restored).  The
+// address stays valid while the device's primary context lives, i.e. until
+// the process exits unless someone calls cudaDeviceReset on that device,
+// which also invalidates every handle there (documented in vhsdf.h).
 cudaError_t scratch_for(int device, int32_t **out) {
   std::lock_guard<std::mutex> lock(g_setup_mu);
   if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;

@@ -87,7 +87,41 @@ __global__ void k_keys_to_xyz(const unsigned long long *__restrict__ keys, uint3
   xyz[3 * i + 2] = z;
 }
 
-// One CTA per block: writes data[i] (pool layout) into the block of key xyz[i].
+// Weighted average of two partial averages of one voxel: a copy observed
+// w_a times with value a and one observed w_b times with value b combine to
+// (a w_a + b w_b) / (w_a + w_b) with weight w_a + w_b.  Explicit roundings
+// (no contraction), stored copy first.
+__device__ __forceinline__ void merge_voxel(float &sdf, float &w, uint32_t &rgb, float s_sdf,
+                                            float s_w, uint32_t s_rgb) {
+  if (s_w == 0.0f) return;  // the stored copy never saw this voxel
+  if (w == 0.0f) {          // only the stored copy did: exact copy
+    sdf = s_sdf;
+    w = s_w;
+    rgb = s_rgb;
+    return;
+  }
+  const float wn = __fadd_rn(s_w, w);
+  sdf = __fdiv_rn(__fadd_rn(__fmul_rn(s_sdf, s_w), __fmul_rn(sdf, w)), wn);
+  // colour: exact integer floor of the weighted sum (weights are whole
+  // numbers below 2^24, so every product fits in 64 bits)
+  const unsigned long long ws = (unsigned long long)s_w, wr = (unsigned long long)w,
+                           wt = ws + wr;
+  uint32_t out = 0;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const unsigned long long n =
+        ((s_rgb >> (8 * c)) & 0xFFu) * ws + ((rgb >> (8 * c)) & 0xFFu) * wr;
+    out |= (uint32_t)(n / wt) << (8 * c);
+  }
+  rgb = out;
+  w = wn;
+}
+
+// One CTA per block: brings data[i] (pool layout) into the block of key
+// xyz[i].  A block created by this stream-in is zero, so it receives an
+// exact copy; a block that a frame re-created after the key was moved out
+// holds the observations made since, and the two copies are merged voxel by
+// voxel (merge_voxel) so that neither set of observations is lost.
 __global__ void __launch_bounds__(128) k_scatter_raw(VolumeView V, const int32_t *__restrict__ xyz,
                                                      const float *__restrict__ data, uint32_t n) {
   const uint32_t i = blockIdx.x;
@@ -96,9 +130,22 @@ __global__ void __launch_bounds__(128) k_scatter_raw(VolumeView V, const int32_t
   if (!key_in_range(x, y, z)) return;
   const uint32_t b = block_of(V, pack_key(x, y, z));
   if (b == kNoBlock) return;  // the insert failed (pool or table full): reported by the state
-  const float4 *src = reinterpret_cast<const float4 *>(data + (size_t)i * kBlockWords);
-  float4 *dst = reinterpret_cast<float4 *>(V.pool + (size_t)b * kBlockWords);
-  for (int k = threadIdx.x; k < kBlockWords / 4; k += blockDim.x) dst[k] = src[k];
+  const float *src = data + (size_t)i * kBlockWords;
+  float *dst = V.pool + (size_t)b * kBlockWords;
+  const int t = threadIdx.x;  // voxels 4t .. 4t+3
+  const float4 ss = reinterpret_cast<const float4 *>(src)[t];
+  const float4 sw = reinterpret_cast<const float4 *>(src + kB3)[t];
+  const uint4 sc = reinterpret_cast<const uint4 *>(src + 2 * kB3)[t];
+  float4 ds = reinterpret_cast<const float4 *>(dst)[t];
+  float4 dw = reinterpret_cast<const float4 *>(dst + kB3)[t];
+  uint4 dc = reinterpret_cast<const uint4 *>(dst + 2 * kB3)[t];
+  merge_voxel(ds.x, dw.x, dc.x, ss.x, sw.x, sc.x);
+  merge_voxel(ds.y, dw.y, dc.y, ss.y, sw.y, sc.y);
+  merge_voxel(ds.z, dw.z, dc.z, ss.z, sw.z, sc.z);
+  merge_voxel(ds.w, dw.w, dc.w, ss.w, sw.w, sc.w);
+  reinterpret_cast<float4 *>(dst)[t] = ds;
+  reinterpret_cast<float4 *>(dst + kB3)[t] = dw;
+  reinterpret_cast<uint4 *>(dst + 2 * kB3)[t] = dc;
 }
 
 // Table rebuild: every slot emptied, then the key of every live pool block
@@ -149,6 +196,40 @@ StreamStore &store_of(vh_handle *h) {
   StreamStore *&s = handle_stream_store(h);
   if (!s) s = new StreamStore();
   return *s;
+}
+
+// merge_voxel on the host: `blk` (the newer copy) absorbs `old`, voxel by
+// voxel, with the same single roundings (volatile temporaries keep the
+// compiler from contracting or reordering them).
+void merge_block_host(float *blk, const float *old) {
+  float *sdf = blk, *w = blk + kB3;
+  uint32_t *rgb = reinterpret_cast<uint32_t *>(blk + 2 * kB3);
+  const float *o_sdf = old, *o_w = old + kB3;
+  const uint32_t *o_rgb = reinterpret_cast<const uint32_t *>(old + 2 * kB3);
+  for (int v = 0; v < kB3; ++v) {
+    if (o_w[v] == 0.0f) continue;
+    if (w[v] == 0.0f) {
+      sdf[v] = o_sdf[v];
+      w[v] = o_w[v];
+      rgb[v] = o_rgb[v];
+      continue;
+    }
+    volatile float wn = o_w[v] + w[v];
+    volatile float a = o_sdf[v] * o_w[v];
+    volatile float b = sdf[v] * w[v];
+    volatile float num = a + b;
+    sdf[v] = num / wn;
+    const unsigned long long ws = (unsigned long long)o_w[v], wr = (unsigned long long)w[v],
+                             wt = ws + wr;
+    uint32_t out = 0;
+    for (int c = 0; c < 3; ++c) {
+      const unsigned long long n =
+          ((o_rgb[v] >> (8 * c)) & 0xFFu) * ws + ((rgb[v] >> (8 * c)) & 0xFFu) * wr;
+      out |= (uint32_t)(n / wt) << (8 * c);
+    }
+    rgb[v] = out;
+    w[v] = wn;
+  }
 }
 
 bool far_enough(unsigned long long key, float voxel, const float c[3], double r2) {
@@ -242,7 +323,10 @@ extern "C" vh_status vh_stream_out(vh_handle *h, const float *centre, float radi
       const size_t e = base / kBlockWords + j;
       S.keys[e] = k;
       auto it = S.index.find(k);
-      if (it != S.index.end()) {  // a stale copy of the same key: replace it
+      if (it != S.index.end()) {
+        // an older copy of the same key (moved out before a frame re-created
+        // the block): merge it into the outgoing one, then drop it
+        merge_block_host(&S.data[e * kBlockWords], &S.data[it->second * kBlockWords]);
         S.keys[it->second] = kEmptyKey;
         S.free_entries.push_back(it->second);
         it->second = e;

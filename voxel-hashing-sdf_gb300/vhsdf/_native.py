@@ -59,7 +59,7 @@ class VhStats(C.Structure):
         ("frames", C.c_int64), ("blocks_allocated", C.c_int64), ("frame_blocks", C.c_int64),
         ("new_blocks", C.c_int64), ("voxels_updated", C.c_int64), ("triangles", C.c_int64),
         ("pool_capacity", C.c_int64), ("table_slots", C.c_int64), ("tombstones", C.c_int64),
-        ("device_error", C.c_uint32), ("reserved", C.c_uint32),
+        ("device_error", C.c_uint32), ("frame_kernels", C.c_uint32),
         ("ms_allocate", C.c_float), ("ms_integrate", C.c_float), ("ms_extract", C.c_float),
         ("ms_frame", C.c_float),
     ]
@@ -100,6 +100,7 @@ SIGNATURES = {
     "vh_integrate": (I32, [P, P, I32, P, P, I32]),
     "vh_extract": (I32, [P, I32, C.POINTER(VhMeshView)]),
     "vh_process_frame": (I32, [P, P, I32, P, P, I32, C.POINTER(VhMeshView)]),
+    "vh_process_frame_mesh": (I32, [P, P, I32, P, P, I32, P, I64, PI64]),
     "vh_copy_mesh": (I32, [P, P, P, I64, PI64]),
     "vh_save_ply": (I32, [P, C.c_char_p, I32]),
     "vh_render": (I32, [P]),

@@ -104,5 +104,5 @@ class Batch:
         st = (C.c_int32 * self.n)()
         stats = (N.VhStats * self.n)()
         self._L.vh_batch_sync(self._b, st, stats)
-        names = [f for f, _ in N.VhStats._fields_ if f != "reserved"]
+        names = [f for f, _ in N.VhStats._fields_]
         return list(st), [{f: getattr(s, f) for f in names} for s in stats]

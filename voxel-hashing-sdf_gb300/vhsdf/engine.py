@@ -93,6 +93,7 @@ class Volume:
                 raise TypeError(f"unknown parameter {k}")
             setattr(p, k, v)
         self.params = p
+        self._pending_meshes = []  # host outputs of vh_process_frame_mesh until sync()
         h = C.c_void_p()
         N.check(self._L.vh_create(C.byref(p), C.byref(h)))
         self._h = h
@@ -122,7 +123,10 @@ class Volume:
         self._check(self._L.vh_reset(self._h))
 
     def sync(self):
-        self._check(self._L.vh_sync(self._h))
+        try:
+            self._check(self._L.vh_sync(self._h))
+        finally:
+            self._pending_meshes = []
 
     def set_stream(self, stream_ptr):
         self._check(self._L.vh_set_stream(self._h, C.c_void_p(stream_ptr)))
@@ -144,6 +148,23 @@ class Volume:
         d, fmt, c, pose = self._frame_args(depth, rgb, c2w, depth_format)
         self._check(self._L.vh_process_frame(self._h, d.ptr, fmt, c.ptr, pose.ctypes.data, d.mem,
                                              None))
+
+    def process_frame_mesh(self, depth, rgb, c2w, out, count, depth_format=None):
+        """process_frame, and the frame's triangles delivered into `out`
+        (host float32 array of shape (capacity, 12), the device buffer's
+        layout) with the count in count[0] (host int64 array).  Without
+        VH_FLAG_SYNC the copy completes by the next sync(); the arrays are
+        kept alive until then."""
+        d, fmt, c, pose = self._frame_args(depth, rgb, c2w, depth_format)
+        if not (isinstance(out, np.ndarray) and out.dtype == np.float32 and out.ndim == 2
+                and out.shape[1] == 12 and out.flags.c_contiguous):
+            raise ValueError("out must be a C-contiguous float32 array of shape (capacity, 12)")
+        if not (isinstance(count, np.ndarray) and count.dtype == np.int64 and count.size >= 1):
+            raise ValueError("count must be an int64 array")
+        self._pending_meshes.append((out, count))
+        self._check(self._L.vh_process_frame_mesh(
+            self._h, d.ptr, fmt, c.ptr, pose.ctypes.data, d.mem, out.ctypes.data, out.shape[0],
+            count.ctypes.data))
 
     # ---- launch tuning ----
     def tuning(self):
@@ -416,7 +437,7 @@ class Volume:
     def stats(self):
         s = N.VhStats()
         self._check(self._L.vh_get_stats(self._h, C.byref(s)))
-        return {f: getattr(s, f) for f, _ in N.VhStats._fields_ if f != "reserved"}
+        return {f: getattr(s, f) for f, _ in N.VhStats._fields_}
 
 
 def block_hash_ref(x, y, z):
