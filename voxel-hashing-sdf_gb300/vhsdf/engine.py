@@ -164,7 +164,7 @@ class Volume:
         self._pending_meshes.append((out, count))
         self._check(self._L.vh_process_frame_mesh(
             self._h, d.ptr, fmt, c.ptr, pose.ctypes.data, d.mem, out.ctypes.data, out.shape[0],
-            count.ctypes.data))
+            count.ctypes.data_as(C.POINTER(C.c_int64))))
 
     # ---- launch tuning ----
     def tuning(self):
