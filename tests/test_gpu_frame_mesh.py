@@ -52,9 +52,11 @@ def test_frame_meshes_reach_the_host(gpu, flags):
         vol.process_frame_mesh(*scene.render(f), out, cnt)
     vol.sync()
     for (n, xyz, rgb), out, cnt in zip(ref, outs, counts):
-        assert cnt[0] == n > 0
+        assert cnt[0] == n == len(xyz)
         assert np.array_equal(as_rows(out, n), rows_from_mesh(xyz, rgb))
         assert np.all(np.isnan(out[n:]))  # nothing written past the frame's mesh
+    # frames 0-6 see the room; frame 7's depth is all invalid (an empty mesh)
+    assert all(n > 50_000 for n, _, _ in ref[:7]) and ref[7][0] == 0
     assert vol.stats()["frame_kernels"] == 5
 
 
@@ -83,6 +85,8 @@ def test_three_buffers_in_turn(gpu):
     bufs = [np.zeros((cap, 12), np.float32) for _ in range(3)]
     cnts = [np.zeros(1, np.int64) for _ in range(3)]
     checked = 0
+
+    assert sum(n > 0 for n, _, _ in ref) == 10  # frames 7 and 8 have no valid depth
 
     def check(i):
         n, xyz, rgb = ref[i]
