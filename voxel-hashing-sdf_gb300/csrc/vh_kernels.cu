@@ -565,38 +565,24 @@ __global__ void __launch_bounds__(128, kPrefetch ? 8 : 12) k_integrate(VolumeVie
 constexpr int kH = 9;              // staged edge: 8 voxels + 1 halo
 constexpr int kH3 = kH * kH * kH;  // 729 staged corners
 constexpr int kHalo = kH3 - kB3;   // 217
-// Staged layout x + 9 y + 88 z (a corner row (y, z) is 9 consecutive words).
+// Staged layout x + 9 y + 88 z: the z pitch is 8 (mod 32) banks, so the 32
+// lanes of a warp, which classify 8 x by 4 z cubes of one y row, read 32
+// distinct banks for every corner.
 constexpr int kZPitch = 88;
 constexpr int kStaged = kZPitch * kH;  // 792 words
 constexpr int kMcThreads = 128;
-constexpr int kRows = kH * kH;         // corner rows (y, z), y and z in 0..8
-constexpr int kEdgeRows = 3 * kRows;   // lattice-edge rows: axis * 81 + y + 9 z
-// Capacities of one pass over a block.  A block whose cube cases need more
-// is processed again in 8 passes of one cube layer each (at most 320
-// triangles and 369 cut edges per layer), so no block is ever dropped.
-constexpr int kCandCap = 1536;  // candidate triangles per pass
-constexpr int kEdgeCap = 512;   // cut lattice edges per pass
+constexpr int kMaxCand = kB3 * 5;  // at most 5 triangles per cube
 
 struct McShared {
   float sdf[kStaged];  // NaN = corner unusable (absent block or low weight)
   uint32_t rgb[kStaged];
-  // corner row (y, z): bit x (0..8) = sdf < 0, bit 16 + x = unusable
-  uint32_t row[kRows];
-  // lattice-edge row: bit x = the edge from corner (x, y, z) one voxel along
-  // the row's axis is cut (both corners usable, signs differ)
-  uint16_t cut[kEdgeRows];
-  uint16_t first[kEdgeRows];  // vertex slot of the row's first cut edge
-  uint16_t elist[kEdgeCap];   // cut edge of a slot: x | y << 4 | z << 8 | axis << 12
-  // vertex slot: the edge's vertex towards +axis and towards -axis (moved
-  // coordinate along the axis, global voxel units) and their colours
-  float4 vert[kEdgeCap];
   uint16_t tri[256][5];  // triangle t of a case: edges e0 | e1 << 4 | e2 << 8
   uint16_t edge[256];
   uint8_t ntri[256];
-  uint8_t einfo[12];    // per cube edge, see edge_info()
-  uint8_t cases[kB3];         // cube case, 0 when the cube emits nothing
-  uint16_t cand[kCandCap];    // candidate triangles: cube | triangle << 9
-  uint32_t halo[kHalo];       // halo voxel: staged index | neighbour << 10 | voxel << 13
+  uint32_t einfo[12];    // per edge, see edge_info()
+  uint8_t cases[kB3];        // cube case, 0 when the cube emits nothing
+  uint16_t cand[kMaxCand];   // candidate triangles: cube | triangle << 9
+  uint32_t halo[kHalo];      // halo voxel: staged index | neighbour << 10 | voxel << 13
   uint32_t nb[8];
   uint32_t warp_sum[kMcThreads / 32];
   uint32_t base;
@@ -604,33 +590,51 @@ struct McShared {
 };
 
 __device__ __forceinline__ int hidx(int x, int y, int z) { return x + kH * y + kZPitch * z; }
+
+// Cube j (0..3) of thread t: x = t & 7, z = (t >> 3 & 3) + 4 (j >> 1),
+// y = (t >> 5) + 4 (j & 1); returns x + 8 y + 64 z.  All 512 cubes once.
+__device__ __forceinline__ int mc_cube(int t, int j) {
+  const int x = t & 7, z = ((t >> 3) & 3) + 4 * (j >> 1), y = (t >> 5) + 4 * (j & 1);
+  return x + 8 * y + 64 * z;
+}
 __device__ __forceinline__ int corner_dx(int k) { return (kMcCornerBitsX >> k) & 1; }
 __device__ __forceinline__ int corner_dy(int k) { return (kMcCornerBitsY >> k) & 1; }
 __device__ __forceinline__ int corner_dz(int k) { return (kMcCornerBitsZ >> k) & 1; }
 
-// Cube edge e as a lattice edge: the offset bits x | y << 1 | z << 2 of its
-// lower corner (the one with the smaller coordinate along the edge), the
-// axis along which it runs (bits 3-4) and whether the reference's corner
-// order runs it towards -axis (bit 5: from the upper to the lower corner).
+// Per-edge constants, packed: staged-index offset of corner a (7 bits) and
+// of corner b (7 bits), corner a's offset bits x | y << 1 | z << 2 (3 bits),
+// the axis along which the edge runs (2 bits) and whether it runs towards
+// -axis (1 bit).
 __device__ __forceinline__ uint32_t edge_info(int e) {
   const uint32_t code =
       (uint32_t)((e < 8 ? kMcEdgeCodeLo >> (8 * e) : kMcEdgeCodeHi >> (8 * (e - 8))) & 0x3Fu);
   const int a = (int)(code & 7u), b = (int)(code >> 3);
   const int ax = corner_dx(a), ay = corner_dy(a), az = corner_dz(a);
   const int bx = corner_dx(b), by = corner_dy(b), bz = corner_dz(b);
+  const uint32_t oa = (uint32_t)hidx(ax, ay, az), ob = (uint32_t)hidx(bx, by, bz);
   const uint32_t axis = bx != ax ? 0u : (by != ay ? 1u : 2u);
   const uint32_t neg = (bx - ax) + (by - ay) + (bz - az) < 0 ? 1u : 0u;
-  const uint32_t lower = (uint32_t)((ax & bx) | ((ay & by) << 1) | ((az & bz) << 2));
-  return lower | (axis << 3) | (neg << 5);
+  return oa | (ob << 7) | ((uint32_t)(ax | (ay << 1) | (az << 2)) << 14) | (axis << 17) |
+         (neg << 19);
 }
 
-// VertexInterp(p1, p2, val1, val2) of src/tsdf.cu:1640-1660 for corners one
-// voxel apart along one axis: p1 + mu * (p2 - p1) moves only that coordinate
-// (the others stay exactly at p1's), so the vertex is `moved` (p1's
-// coordinate p, step = p2 - p1 = +-1).  The colour is interpolated and
-// truncated like the reference's float-to-uchar store.
-__device__ __forceinline__ void vertex_interp(float p, float step, float v1, float v2, uint32_t c1,
-                                              uint32_t c2, float &moved, uint32_t &col) {
+// Vertex of edge e: VertexInterp(p[a], p[b], val[a], val[b])
+// (src/tsdf.cu:1640-1660) in global voxel units; (gx, gy, gz) is the global
+// voxel of staged corner 0.  Corners are one voxel apart along one axis, so
+// p1 + mu * (p2 - p1) changes only that coordinate: the others are
+// p1 + mu * 0 = p1 exactly (mu is finite and >= 0 on a cut edge).
+// With `colour`, the colour is interpolated and truncated like the
+// reference's float-to-uchar store.
+template <bool colour>
+__device__ __forceinline__ float4 mc_vertex(const McShared &S, int e, int h0, int gx, int gy,
+                                           int gz) {
+  const uint32_t info = S.einfo[e];
+  const int ia = h0 + (int)(info & 127u), ib = h0 + (int)((info >> 7) & 127u);
+  const float v1 = S.sdf[ia], v2 = S.sdf[ib];
+  float p[3] = {(float)(gx + (int)((info >> 14) & 1u)), (float)(gy + (int)((info >> 15) & 1u)),
+                (float)(gz + (int)((info >> 16) & 1u))};
+  const int axis = (int)((info >> 17) & 3u);
+  const float step = (info >> 19) ? -1.0f : 1.0f;  // p2 - p1 along the axis
   float mu = 0.0f;
   bool interp = false;
   bool to_b = false;
@@ -644,23 +648,42 @@ __device__ __forceinline__ void vertex_interp(float p, float step, float v1, flo
     mu = (0.0f - v1) / (v2 - v1);
     interp = true;
   }
-  moved = p;
+  float moved = axis == 0 ? p[0] : (axis == 1 ? p[1] : p[2]);
   if (interp)
     moved = moved + mu * step;
   else if (to_b)
     moved = moved + step;
-  if (!interp) {
-    col = to_b ? c2 : c1;
-    return;
-  }
+  const float px = axis == 0 ? moved : p[0];
+  const float py = axis == 1 ? moved : p[1];
+  const float pz = axis == 2 ? moved : p[2];
   uint32_t out = 0;
+  if (colour) {
+    const uint32_t c1 = S.rgb[ia], c2 = S.rgb[ib];
+    if (!interp) {
+      out = to_b ? c2 : c1;
+    } else {
 #pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    const int q1 = (int)((c1 >> (8 * c)) & 0xFFu), q2 = (int)((c2 >> (8 * c)) & 0xFFu);
-    const float v = (float)q1 + mu * (float)(q2 - q1);
-    out |= (__float2uint_rz(v) & 0xFFu) << (8 * c);
+      for (int c = 0; c < 3; ++c) {
+        const int q1 = (int)((c1 >> (8 * c)) & 0xFFu), q2 = (int)((c2 >> (8 * c)) & 0xFFu);
+        const float v = (float)q1 + mu * (float)(q2 - q1);
+        out |= (__float2uint_rz(v) & 0xFFu) << (8 * c);
+      }
+    }
   }
-  col = out;
+  return make_float4(px, py, pz, __uint_as_float(out));
+}
+
+// Cube case of the cube with staged corner 0 at (x, y, z); -1 if a corner is
+// unusable (src/tsdf.cu:930-986).
+__device__ __forceinline__ int cube_case(const McShared &S, int x, int y, int z) {
+  int ci = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const float v = S.sdf[hidx(x + corner_dx(k), y + corner_dy(k), z + corner_dz(k))];
+    if (v != v) return -1;
+    if (v < 0.0f) ci |= 1 << k;
+  }
+  return ci;
 }
 
 __device__ __forceinline__ bool same_pos(const float4 &a, const float4 &b) {
@@ -690,6 +713,11 @@ __device__ __forceinline__ uint32_t cta_scan(McShared &S, uint32_t v, uint32_t *
   return before + incl - v;
 }
 
+// Persistent CTAs, one block (plus its +x/+y/+z halo) per iteration:
+//   stage 9^3 corners -> classify 512 cubes -> expand into candidate
+//   triangles (scan) -> one thread per candidate tests the reference's
+//   degenerate-triangle rule -> compact (scan) -> one atomic per block ->
+//   one thread per output float4, contiguous stores.
 // Tables and halo map of the MC shared state (once per CTA).
 __device__ __forceinline__ void mc_init_shared(McShared &S) {
   const int t = threadIdx.x;
@@ -702,7 +730,7 @@ __device__ __forceinline__ void mc_init_shared(McShared &S) {
     for (int m = n; m < 5; ++m) S.tri[i][m] = 0;
     S.ntri[i] = (uint8_t)n;
   }
-  if (t < 12) S.einfo[t] = (uint8_t)edge_info(t);
+  if (t < 12) S.einfo[t] = edge_info(t);
   // halo: x == 8 (81), then y == 8 with x < 8 (72), then z == 8 with x, y < 8 (64)
   for (int hh = t; hh < kHalo; hh += kMcThreads) {
     int x, y, z;
@@ -725,54 +753,8 @@ __device__ __forceinline__ void mc_init_shared(McShared &S) {
   }
 }
 
-// Cut-edge mask of lattice-edge row r (axis * 81 + y + 9 z) among the edges
-// that the cubes of layers [z0, z1) use.
-__device__ __forceinline__ uint32_t edge_row_mask(const McShared &S, int r, int z0, int z1) {
-  const int axis = r / kRows, rr = r - axis * kRows;
-  const int y = rr % kH, z = rr / kH;
-  const uint32_t w = S.row[rr];
-  const uint32_t n = w & 0x1FFu, q = w >> 16;
-  if (axis == 0) {  // x edges of layer z are used by cubes z - 1 and z
-    if (z < z0 || z > z1) return 0u;
-    return (n ^ (n >> 1)) & ~(q | (q >> 1)) & 0xFFu;
-  }
-  if (axis == 1) {
-    if (y == 8 || z < z0 || z > z1) return 0u;
-    const uint32_t w2 = S.row[rr + 1];
-    return (n ^ w2) & ~(q | (w2 >> 16)) & 0x1FFu;
-  }
-  if (z == 8 || z < z0 || z >= z1) return 0u;  // z edges of layer z: cubes of layer z
-  const uint32_t w2 = S.row[rr + kH];
-  return (n ^ w2) & ~(q | (w2 >> 16)) & 0x1FFu;
-}
-
-// Cube cases of cubes (x0 .. x0 + 3, y, z) from the corner-row words: bit k
-// of a case is corner k's sign (corner order of src/tsdf.cu's idxMap), 0
-// for a cube with an unusable corner or no cut edge (src/tsdf.cu:930-986).
-__device__ __forceinline__ void classify4(const McShared &S, int x0, int y, int z, int cs[4]) {
-  const uint32_t A = S.row[y + kH * z], B = S.row[y + 1 + kH * z];
-  const uint32_t C = S.row[y + kH * (z + 1)], D = S.row[y + 1 + kH * (z + 1)];
-  const uint32_t bad = (A | B | C | D) >> 16;
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const int x = x0 + j;
-    const uint32_t a = (A >> x) & 3u, b = (B >> x) & 3u, c = (C >> x) & 3u, d = (D >> x) & 3u;
-    // corners 0 (0,0,0) 3 (1,0,0) | 1 (0,1,0) 2 (1,1,0) | 4 (0,0,1) 7 (1,0,1) | 5 (0,1,1) 6 (1,1,1)
-    int ci = (int)((a & 1u) | ((a & 2u) << 2) | (b << 1) | ((c & 1u) << 4) | ((c & 2u) << 6) |
-                   (d << 5));
-    if (((bad >> x) & 3u) || S.edge[ci] == 0) ci = 0;
-    cs[j] = ci;
-  }
-}
-
 // One block of the list (scope_all: pool block i; else frame-list entry i):
-// stage its 9^3 corners, classify the 512 cubes, compute the vertex of every
-// cut lattice edge once (in both directions where the reference's corner
-// order traverses it both ways, so every vertex equals the per-cube
-// VertexInterp bit for bit), then assemble the candidate triangles, apply
-// the reference's degenerate test (p0 == p1 || p1 == p2,
-// src/tsdf.cu:1055-1057), compact the survivors with a CTA scan and write
-// them into one range reserved with a single atomic per round.  Every
+// stage, classify, expand, test, compact and write its triangles.  Every
 // thread of the CTA calls it with the same i; S must be free on entry.
 __device__ __forceinline__ void mc_block(McShared &S, const VolumeView &V, int scope_all,
                                          float min_weight, float4 *__restrict__ tris,
@@ -847,146 +829,64 @@ __device__ __forceinline__ void mc_block(McShared &S, const VolumeView &V, int s
     }
   }
   __syncthreads();
-  if (t < kRows) {  // corner-row words: sign and unusable bits of 9 corners
-    const float *r = S.sdf + hidx(0, t % kH, t / kH);
-    uint32_t w = 0;
+  // 1. classify this thread's 4 cubes; count their candidate triangles
+  uint32_t ncand_mine = 0;
+  int cs[4];
 #pragma unroll
-    for (int x = 0; x < kH; ++x) {
-      const float v = r[x];
-      w |= (v < 0.0f ? 1u : 0u) << x;
-      w |= (v != v ? 1u : 0u) << (16 + x);
-    }
-    S.row[t] = w;
+  for (int j = 0; j < 4; ++j) {
+    const int c = mc_cube(t, j);
+    int ci = cube_case(S, c & 7, (c >> 3) & 7, c >> 6);
+    if (ci < 0 || S.edge[ci] == 0) ci = 0;
+    cs[j] = ci;
+    S.cases[c] = (uint8_t)ci;
+    ncand_mine += S.ntri[ci];
+  }
+  uint32_t ncand;
+  uint32_t off = cta_scan(S, ncand_mine, &ncand);
+  if (ncand == 0) return;  // uniform: nothing to emit in this block
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int c = mc_cube(t, j);
+    const int nt = S.ntri[cs[j]];
+    for (int tt = 0; tt < nt; ++tt) S.cand[off++] = (uint16_t)(c | (tt << 9));
   }
   __syncthreads();
-
-  const int cy = (t >> 1) & 7, cz = t >> 4, cx0 = (t & 1) * 4;  // this thread's 4 cubes
+  // 2. candidates in rounds of one per thread: the thread computes its
+  //    candidate's three vertices once, the reference's degenerate test
+  //    drops p0 == p1 || p1 == p2 (src/tsdf.cu:1055-1057), a CTA scan over
+  //    the survivors gives each a slot in one contiguous range reserved
+  //    with a single atomic, and the thread writes its 48-byte triangle.
   const int gx0 = bx * kB, gy0 = by * kB, gz0 = bz * kB;
-  // One pass over layers [z0, z1): normally all 8; a block that exceeds the
-  // pass capacities goes again layer by layer.
-  int z0 = 0, z1 = kB;
-  bool layered = false;
-  for (;;) {
-    // 1. classify this thread's cubes and the cut masks of its edge rows
-    int cs[4];
-    classify4(S, cx0, cy, cz, cs);
-    uint32_t ntri_mine = 0;
-    const bool in_pass = cz >= z0 && cz < z1;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      if (!in_pass) cs[j] = 0;
-      S.cases[cx0 + j + kB * cy + kB * kB * cz] = (uint8_t)cs[j];
-      ntri_mine += S.ntri[cs[j]];
+  for (uint32_t r0 = 0; r0 < ncand; r0 += kMcThreads) {
+    const uint32_t k = r0 + t;
+    float4 p0, p1, p2;
+    uint32_t ok = 0;
+    if (k < ncand) {
+      const uint32_t ent = S.cand[k];
+      const int c = (int)(ent & 511u), tt = (int)(ent >> 9);
+      const int x = c & 7, y = (c >> 3) & 7, z = c >> 6;
+      const uint32_t tri = S.tri[S.cases[c]][tt];
+      const int h0 = hidx(x, y, z);
+      p0 = mc_vertex<true>(S, (int)(tri & 15u), h0, gx0 + x, gy0 + y, gz0 + z);
+      p1 = mc_vertex<true>(S, (int)((tri >> 4) & 15u), h0, gx0 + x, gy0 + y, gz0 + z);
+      p2 = mc_vertex<true>(S, (int)(tri >> 8), h0, gx0 + x, gy0 + y, gz0 + z);
+      ok = !(same_pos(p0, p1) || same_pos(p1, p2));
     }
-    const int r1 = t + kMcThreads;
-    const uint32_t m0 = edge_row_mask(S, t, z0, z1);
-    const uint32_t m1 = r1 < kEdgeRows ? edge_row_mask(S, r1, z0, z1) : 0u;
-    const uint32_t ncut_mine = (uint32_t)(__popc(m0) + __popc(m1));
-    uint32_t tot;
-    const uint32_t off = cta_scan(S, ntri_mine | (ncut_mine << 16), &tot);
-    const uint32_t ncand = tot & 0xFFFFu, ncut = tot >> 16;
-    if (!layered && (ncand > (uint32_t)kCandCap || ncut > (uint32_t)kEdgeCap)) {
-      layered = true;  // uniform: start again one layer at a time
-      z1 = 1;
-      __syncthreads();  // warp sums read before the next scan
-      continue;
-    }
-    if (ncand) {
-      // 2. expand candidate triangles and list the cut edges (slot order)
-      uint32_t ct = off & 0xFFFFu;
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int c = cx0 + j + kB * cy + kB * kB * cz;
-        const int nt = S.ntri[cs[j]];
-        for (int tt = 0; tt < nt; ++tt) S.cand[ct++] = (uint16_t)(c | (tt << 9));
-      }
-      uint32_t se = off >> 16;
-#pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        const int r = k ? r1 : t;
-        if (r >= kEdgeRows) break;
-        uint32_t m = k ? m1 : m0;
-        S.cut[r] = (uint16_t)m;
-        S.first[r] = (uint16_t)se;
-        const int axis = r / kRows, rr = r - axis * kRows;
-        const uint32_t yz = (uint32_t)((rr % kH) << 4 | (rr / kH) << 8 | axis << 12);
-        while (m) {
-          const int x = __ffs(m) - 1;
-          m &= m - 1u;
-          S.elist[se++] = (uint16_t)(yz | (uint32_t)x);
-        }
-      }
-      __syncthreads();
-      // 3. the vertices of the cut edges, one edge per thread per round:
-      //    towards +axis VertexInterp(lower, upper), towards -axis
-      //    VertexInterp(upper, lower) (z edges are only traversed upwards)
-      for (uint32_t s = (uint32_t)t; s < ncut; s += kMcThreads) {
-        const uint32_t ent = S.elist[s];
-        const int x = (int)(ent & 15u), y = (int)((ent >> 4) & 15u), z = (int)((ent >> 8) & 15u);
-        const int axis = (int)(ent >> 12);
-        const int lo = hidx(x, y, z);
-        const int hi = lo + (axis == 0 ? 1 : (axis == 1 ? kH : kZPitch));
-        const float vl = S.sdf[lo], vh = S.sdf[hi];
-        const uint32_t cl = S.rgb[lo], ch = S.rgb[hi];
-        const int g = axis == 0 ? gx0 + x : (axis == 1 ? gy0 + y : gz0 + z);
-        float up, down = 0.0f;
-        uint32_t cup, cdown = 0u;
-        vertex_interp((float)g, 1.0f, vl, vh, cl, ch, up, cup);
-        if (axis != 2) vertex_interp((float)(g + 1), -1.0f, vh, vl, ch, cl, down, cdown);
-        S.vert[s] = make_float4(up, down, __uint_as_float(cup), __uint_as_float(cdown));
-      }
-      __syncthreads();
-      // 4. candidates in rounds of one per thread: the three vertices from
-      //    the slots, the degenerate test, a CTA scan over the survivors, one
-      //    atomic per round, and each survivor's 48-byte triangle
-      for (uint32_t r0 = 0; r0 < ncand; r0 += kMcThreads) {
-        const uint32_t k = r0 + (uint32_t)t;
-        float4 p[3];
-        uint32_t ok = 0;
-        if (k < ncand) {
-          const uint32_t ent = S.cand[k];
-          const int c = (int)(ent & 511u), tt = (int)(ent >> 9);
-          const int x = c & 7, y = (c >> 3) & 7, z = c >> 6;
-          const uint32_t tri = S.tri[S.cases[c]][tt];
-#pragma unroll
-          for (int v = 0; v < 3; ++v) {
-            const uint32_t info = S.einfo[(tri >> (4 * v)) & 15u];
-            const int lx = x + (int)(info & 1u), ly = y + (int)((info >> 1) & 1u),
-                      lz = z + (int)((info >> 2) & 1u);
-            const int axis = (int)((info >> 3) & 3u);
-            const int r = axis * kRows + ly + kH * lz;
-            const uint32_t slot = S.first[r] + (uint32_t)__popc(S.cut[r] & ((1u << lx) - 1u));
-            const float4 sv = S.vert[slot];
-            const bool down = (info >> 5) & 1u;
-            const float moved = down ? sv.y : sv.x;
-            const float col = down ? sv.w : sv.z;
-            p[v] = make_float4(axis == 0 ? moved : (float)(gx0 + lx),
-                               axis == 1 ? moved : (float)(gy0 + ly),
-                               axis == 2 ? moved : (float)(gz0 + lz), col);
-          }
-          ok = !(same_pos(p[0], p[1]) || same_pos(p[1], p[2]));
-        }
-        uint32_t nvalid;
-        const uint32_t pre = cta_scan(S, ok, &nvalid);
-        if (t == 0) S.base = nvalid ? atomicAdd(&V.st->tri_count, nvalid) : 0u;
-        __syncthreads();
-        if (ok) {
-          const uint32_t out = S.base + pre;
-          if (out < tri_cap) {
-            float4 *dst = tris + 3 * (size_t)out;
-            dst[0] = p[0];
-            dst[1] = p[1];
-            dst[2] = p[2];
-          } else {
-            atomicOr(&V.st->error, kErrTriCap);
-          }
-        }
+    uint32_t nvalid;
+    const uint32_t pre = cta_scan(S, ok, &nvalid);
+    if (t == 0) S.base = nvalid ? atomicAdd(&V.st->tri_count, nvalid) : 0u;
+    __syncthreads();
+    if (ok) {
+      const uint32_t out = S.base + pre;
+      if (out < tri_cap) {
+        float4 *dst = tris + 3 * (size_t)out;
+        dst[0] = p0;
+        dst[1] = p1;
+        dst[2] = p2;
+      } else {
+        atomicOr(&V.st->error, kErrTriCap);
       }
     }
-    if (!layered || z1 == kB) return;
-    __syncthreads();  // this layer's slots, lists and warp sums are free
-    ++z0;
-    ++z1;
   }
 }
 
