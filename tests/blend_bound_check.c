@@ -1,8 +1,9 @@
 /* Exhaustive check of the integer colour average of k_integrate for weights
  * w = w_old + 1 in [2, 2048]: floor(n / w) = umulhi(n, m) for every
  * numerator n = c_old * w_old + c_new in [0, 255 w], where
- * m = trunc(r * (2^32 + 2^11)) + 1 and r is the approximate reciprocal of w
- * (within 2^-22 relative, i.e. 2 ulp) and the float product is rounded to
+ * m = trunc(r * (2^32 + 2^11)) + 1 and r is a reciprocal of w within 2^-22
+ * relative (2 ulp; the kernel's is correctly rounded, within 2^-24) and the
+ * float product is rounded to
  * nearest (2^-24 relative).  floor(n * m / 2^32) is monotone in m, so the
  * smallest and the largest m those roundings allow cover every case.
  * Prints the number of checks and failures; exits 1 on a failure. */

@@ -57,6 +57,7 @@ struct vh_handle {
   FrameIn *d_fin = nullptr;    // the current frame's pose and image pointers
   FrameIn fin{};               // the next frame's, passed to k_frame_begin
   uint2 *d_pix = nullptr;
+  float *d_rcp = nullptr;  // correctly rounded 1 / w for the integration update
   float4 *d_tris = nullptr;
   int64_t tri_cap = 0;
   // Host frames: two device slots filled on copy_stream, so the upload of a
@@ -123,6 +124,17 @@ vh_status cuda_fail(vh_handle *h, cudaError_t e, const char *what) {
     cudaError_t e__ = (expr);                              \
     if (e__ != cudaSuccess) return cuda_fail(h, e__, #expr); \
   } while (0)
+
+// 1 / b correctly rounded to float: the double quotient rounded once, then
+// the float neighbours checked in case that double rounding missed.
+float rn_reciprocal(float b) {
+  const double ex = 1.0 / (double)b;
+  float y = (float)ex;
+  const float up = std::nextafter(y, INFINITY), down = std::nextafter(y, -INFINITY);
+  if (std::fabs((double)up - ex) < std::fabs((double)y - ex)) y = up;
+  if (std::fabs((double)down - ex) < std::fabs((double)y - ex)) y = down;
+  return y;
+}
 
 bool finite_pose(const float *c2w) {
   for (int i = 0; i < 16; ++i)
@@ -407,6 +419,7 @@ void free_all(vh_handle *h) {
   }
   if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
   cudaFree(h->d_pix);
+  cudaFree(h->d_rcp);
   cudaFree(h->d_tris);
   cudaFree(h->d_work);
   if (h->h_state) cudaFreeHost(h->h_state);
@@ -718,6 +731,7 @@ vh_status vh_create(const vh_params *p, vh_handle **out) {
             cudaMalloc(&h->d_in_rgb[0], 3 * npx) == cudaSuccess &&
             cudaMalloc(&h->d_in_rgb[1], 3 * npx) == cudaSuccess &&
             cudaMalloc(&h->d_pix, sizeof(uint2) * npx) == cudaSuccess &&
+            cudaMalloc(&h->d_rcp, sizeof(float) * (kRcpMax + 1)) == cudaSuccess &&
             cudaMalloc(&h->d_tris, sizeof(float4) * 3 * (size_t)(h->tri_cap ? h->tri_cap : 1)) == cudaSuccess &&
             cudaHostAlloc(&h->h_state, sizeof(DevState), cudaHostAllocMapped) == cudaSuccess &&
             cudaHostGetDevicePointer(&h->h_state_dev, h->h_state, 0) == cudaSuccess;
@@ -752,6 +766,9 @@ vh_status vh_create(const vh_params *p, vh_handle **out) {
   h->C.voxel = p->voxel_size;
   h->C.trunc = p->trunc;
   h->C.mc_min_weight = p->mc_min_weight;
+  h->C.rtrunc = rn_reciprocal(p->trunc);
+  launch_rcp_table(h->d_rcp, h->stream);
+  h->C.rcp_w = h->d_rcp;
   vs = clear_volume(h, false);
   if (vs != VH_OK) return bail(vs);
   *out = h;

@@ -91,7 +91,12 @@ struct CamParams {
   float fx, fy, cx, cy;
   float min_depth, max_depth, depth_scale;
   float voxel, trunc, mc_min_weight;
+  float rtrunc;         // 1 / trunc correctly rounded (host-computed)
+  const float *rcp_w;   // device table: rcp_w[w] = 1 / w correctly rounded, w <= kRcpMax
 };
+
+// Weights up to this have a correctly rounded reciprocal in CamParams::rcp_w.
+constexpr int kRcpMax = 2048;
 
 __host__ __device__ inline bool key_in_range(int x, int y, int z) {
   return (uint32_t)(x + kKeyBias) < (1u << 21) && (uint32_t)(y + kKeyBias) < (1u << 21) &&
@@ -196,6 +201,9 @@ void launch_scatter_blocks(const VolumeView &V, const int32_t *xyz, const float 
 
 // Bilateral pre-filter of one depth image into float metres (vh_filter.cu);
 // depth == nullptr reads the image of fin.
+// rcp[w] = 1 / w correctly rounded for w in [1, kRcpMax] (rcp[0] = 0).
+void launch_rcp_table(float *rcp, cudaStream_t s);
+
 void launch_depth_filter(const CamParams &C, const void *depth, const FrameIn *fin, int fmt,
                          float *out, cudaStream_t s);
 

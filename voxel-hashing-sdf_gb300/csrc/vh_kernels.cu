@@ -384,11 +384,11 @@ __global__ void __launch_bounds__(256, 6) k_allocate(VolumeView V, CamParams C,
 // integer there and truncate one lower, so its GPU build may differ from
 // this by 1 on such voxels.
 __device__ __forceinline__ uint32_t blend_colour(uint32_t old_rgb, uint32_t new_rgb, float w_old,
-                                                 float w_new) {
+                                                 float w_new, float rcp_new) {
   uint32_t out = 0;
-  if (w_old <= 2047.0f) {
+  if (w_old <= 2047.0f) {  // rcp_new = 1 / w_new correctly rounded (within the bound above)
     const uint32_t wo = (uint32_t)w_old;
-    const uint32_t m = __float2uint_rz(__fdividef(1.0f, w_new) * 4294969344.0f) + 1u;
+    const uint32_t m = __float2uint_rz(rcp_new * 4294969344.0f) + 1u;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const uint32_t n = ((old_rgb >> (8 * c)) & 0xFFu) * wo + ((new_rgb >> (8 * c)) & 0xFFu);
@@ -444,19 +444,39 @@ __device__ __forceinline__ int project_voxel(const CamParams &C, const float P[1
   return ok ? (int)vf * C.width + (int)uf : -1;
 }
 
+// a / b from y = 1 / b correctly rounded: q = a y, then one exact residual
+// correction q + (a - b q) y (Markstein's theorem: with y correctly rounded
+// and q within an ulp of a / b the corrected quotient is the correctly
+// rounded a / b, barring overflow and underflow; tests/markstein_check.c
+// checks it exhaustively against IEEE division for the divisors and
+// dividend ranges of the integration update).  A zero dividend gives +0,
+// which is what IEEE division gives for the +0 dividends that occur here.
+__device__ __forceinline__ float div_by_rcp(float a, float b, float y) {
+  const float q = __fmul_rn(a, y);
+  return __fmaf_rn(__fmaf_rn(-b, q, a), y, q);
+}
+
 // Update of one voxel from its pixel (src/tsdf.cu:715-745), sdf averaged
-// with the old weight.
+// with the old weight.  The two divisions are the IEEE quotients, taken
+// from correctly rounded reciprocals of T (host) and of the weight (table).
 __device__ __forceinline__ bool update_voxel(const CamParams &C, uint2 px, float z, float &sdf,
                                              float &wt, uint32_t &rgb) {
   const float d = __uint_as_float(px.x);
   if (!(d > 0.0f && d <= C.max_depth)) return false;
   const float diff = d - z;
   if (diff <= -C.trunc) return false;
-  const float dist = fminf(1.0f, diff / C.trunc);
+  const float dist = fminf(1.0f, div_by_rcp(diff, C.trunc, C.rtrunc));  // diff / T
   const float w_old = wt;
   const float w_new = w_old + 1.0f;
-  sdf = (sdf * w_old + dist) / w_new;
-  rgb = blend_colour(rgb, px.y, w_old, w_new);
+  const float num = sdf * w_old + dist;
+  float r = 0.0f;
+  if (w_new <= (float)kRcpMax) {
+    r = __ldg(C.rcp_w + (int)w_new);
+    sdf = div_by_rcp(num, w_new, r);
+  } else {
+    sdf = num / w_new;
+  }
+  rgb = blend_colour(rgb, px.y, w_old, w_new, r);
   wt = w_new;
   return true;
 }
@@ -982,6 +1002,11 @@ __global__ void k_state_out(const DevState *__restrict__ st, DevState *host) {
         reinterpret_cast<const uint32_t *>(st)[threadIdx.x];
 }
 
+__global__ void k_rcp_table(float *__restrict__ rcp) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w <= kRcpMax) rcp[w] = w ? __frcp_rn((float)w) : 0.0f;
+}
+
 __global__ void k_epoch_end(VolumeView V) {
   if (threadIdx.x == 0) reconcile(V);
 }
@@ -1371,6 +1396,9 @@ cudaError_t update_frame_begin(cudaGraphExec_t e, cudaGraphNode_t n, const Volum
   return cudaGraphExecKernelNodeSetParams(e, n, &p);
 }
 void launch_epoch_end(const VolumeView &V, cudaStream_t s) { k_epoch_end<<<1, 32, 0, s>>>(V); }
+void launch_rcp_table(float *rcp, cudaStream_t s) {
+  k_rcp_table<<<(kRcpMax + 256) / 256, 256, 0, s>>>(rcp);
+}
 void launch_clear_list(const VolumeView &V, cudaStream_t s) { k_clear_list<<<1, 32, 0, s>>>(V); }
 void launch_mc_begin(const VolumeView &V, cudaStream_t s) { k_mc_begin<<<1, 32, 0, s>>>(V); }
 
