@@ -5,7 +5,9 @@
  *   mode 0 (truncation T): for 12 divisors b in [0.007, 3], every float a
  *           with |a| in [2^-30, 64] (both signs), every `step`-th one;
  *   mode 1 (weights): every whole b in [1, 4096], `samples` seeded random
- *           floats a with |a| in [2^-40, 8192] per b.
+ *           floats a with |a| in [2^-40, 8192] per b;
+ *   mode 2 (camera depth): `samples` seeded random pairs, b in [2^-10, 2^8]
+ *           and |a| in [2^-30, 2^8] (the projection's x / z and y / z).
  * y is formed as the engine's host code forms RN(1/T): the double quotient
  * rounded once, then checked against its float neighbours.
  * Usage: markstein_check <mode> <step|samples>.  Prints the number of checks
@@ -54,6 +56,18 @@ int main(int argc, char **argv) {
         check(f_of(u), b, y);
         check(f_of(u | 0x80000000u), b, y);
       }
+    }
+  } else if (mode == 2) {
+    uint64_t s = 0x9E3779B97F4A7C15ull;
+    const uint32_t blo = u_of(0x1p-10f), bhi = u_of(0x1p8f);
+    const uint32_t alo = u_of(0x1p-30f), ahi = u_of(0x1p8f);
+    for (long long i = 0; i < arg; ++i) {
+      s ^= s << 13; s ^= s >> 7; s ^= s << 17;
+      const float b = f_of(blo + (uint32_t)(s % (bhi - blo)));
+      const float y = rn_reciprocal(b);
+      const uint64_t t = s * 0x2545F4914F6CDD1Dull;
+      const float a = f_of((alo + (uint32_t)((t >> 8) % (ahi - alo))) | ((t & 1) ? 0x80000000u : 0));
+      check(a, b, y);
     }
   } else {
     uint64_t s = 88172645463325252ull;

@@ -1,9 +1,9 @@
 """The integration update divides by the truncation T and by the new weight
 through correctly rounded reciprocals plus one fused residual correction
 (Markstein's theorem); this checks in C that the result is the IEEE
-quotient, exhaustively over a stride of all dividends for 12 truncations
-and on seeded samples for every weight up to 4096 (the engine uses the
-table up to 2048).  The GPU parity tests then compare the kernel with the
+quotient, exhaustively over a stride of all dividends for 12 truncations,
+on seeded samples for every weight up to 4096 (the engine uses the table up
+to 2048), and on seeded samples of the projection's x / z and y / z.  The GPU parity tests then compare the kernel with the
 oracle's IEEE divisions bit for bit."""
 import os
 import platform
@@ -32,7 +32,7 @@ def checker(tmp_path_factory):
     return exe
 
 
-@pytest.mark.parametrize("mode,arg", [(0, 7), (1, 1 << 17)])
+@pytest.mark.parametrize("mode,arg", [(0, 7), (1, 1 << 17), (2, 1 << 29)])
 def test_reciprocal_division_is_ieee(checker, mode, arg):
     out = subprocess.run([checker, str(mode), str(arg)], capture_output=True, text=True,
                          timeout=600)
