@@ -348,7 +348,24 @@ vh_status vh_stream_out(vh_handle *h, const float *centre, float radius, int64_t
  * merged as vh_stream_out describes.  The keys join the current block list,
  * as vh_alloc_keys does. */
 vh_status vh_stream_in(vh_handle *h, const float *centre, float radius, int64_t *moved);
-/* Blocks currently in the host store. */
+/* vh_stream_out without waiting: the chunk streaming of processFrame
+ * (src/tsdf.cu:469-596) done as an eviction that overlaps later frames.  On
+ * the handle's stream, in order with the frames around the call, every GPU
+ * block whose centre is farther than `radius` metres from centre[3] (at most
+ * 32768 per call; the rest stay and a later call takes them) is gathered
+ * into a device staging buffer, its key leaves the hash table and its pool
+ * block is zeroed and returned to the free list, so frames enqueued after
+ * the call neither see the block nor lack its pool space.  A copy kernel on
+ * a separate stream then brings the gathered blocks into mapped pinned host
+ * memory while those frames run, and the blocks join the host store when a
+ * later call finds that copy finished (vh_host_blocks counts them then;
+ * vh_sync, vh_stream_in and vh_stream_out wait for it).  Stored copies are
+ * bit-identical and merge with re-created blocks as vh_stream_out
+ * describes.  Two evictions can be in flight; a third call waits for the
+ * older one.  The first call allocates two 192 MiB device staging buffers
+ * and two as large in pinned host memory. */
+vh_status vh_evict_async(vh_handle *h, const float *centre, float radius);
+/* Blocks currently in the host store (evictions whose copy has finished). */
 int64_t vh_host_blocks(const vh_handle *h);
 /* Rebuilds the hash table from the pool's live blocks, dropping the
  * tombstones that erased keys leave (inserts do not reuse them); the

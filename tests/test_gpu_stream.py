@@ -182,3 +182,44 @@ def test_recreated_blocks_merge_with_their_stored_copies(gpu, back_by):
     vol.stream_in([0, 0, 0])
     assert vol.host_blocks() == 0
     assert_same_blocks(vol.export_blocks(), merge_expected(old, new))
+
+
+def test_async_eviction_round_trip(gpu):
+    """vh_evict_async: the blocks leave the volume in stream order and reach
+    the host store bit-identical once the copy has finished."""
+    s, frames = room_stream(12)
+    vol = make_volume(s, 1 << 16)
+    for d, c, p in frames:
+        vol.integrate(d, c, p)
+    before = vol.export_blocks()
+    n = len(before["xyz"])
+    vol.evict_async([0, 0, 0], 0.0)
+    assert vol.stats()["blocks_allocated"] == 0  # gone in stream order
+    vol.sync()  # the copy has finished: the blocks are in the store
+    assert vol.host_blocks() == n
+    assert vol.stream_in([0, 0, 0]) == n
+    assert_same_blocks(vol.export_blocks(), before)
+
+
+def test_async_eviction_around_the_camera_equals_an_unlimited_pool(gpu):
+    """Frames submitted back to back (asynchronous mode) with an eviction
+    after each frame and the region of the next frame moved back in before
+    it: the volume equals an unlimited pool's bit for bit, while part of it
+    lived on the host."""
+    s, frames = room_stream(40)
+    radius = 1.3 * (MAX_DEPTH + 0.08) + 2 * np.sqrt(3) * 8 * 0.02
+    ref = make_volume(s, 1 << 16)
+    vol = volume_for(s, voxel=0.02, trunc=0.08, max_depth=MAX_DEPTH, table_log2=18,
+                     pool_blocks=1 << 16, max_frame_blocks=1 << 15, flags=0)
+    stored = 0
+    for d, c, p in frames:
+        ref.integrate(d, c, p)
+        centre = p[:3, 3]
+        vol.stream_in(centre, radius)  # waits for the pending evictions
+        stored = max(stored, vol.host_blocks())
+        vol.integrate(d, c, p)
+        vol.evict_async(centre, radius)
+    vol.sync()
+    assert stored > 0
+    vol.stream_in([0, 0, 0])
+    assert_same_blocks(vol.export_blocks(), ref.export_blocks())

@@ -803,7 +803,8 @@ vh_status vh_sync(vh_handle *h) {
   if (!h) return VH_ERR_INVALID_ARG;
   vh_status s = mesh_drain(h);
   vh_status t = sync_and_check(h);
-  return s != VH_OK ? s : t;
+  vh_status e = stream_store_settle(h);
+  return s != VH_OK ? s : (t != VH_OK ? t : e);
 }
 
 const char *vh_last_error(const vh_handle *h) { return h ? h->last_error.c_str() : "null handle"; }

@@ -48,6 +48,8 @@ vh_status index_mesh(vh_handle *h, const float4 *tris, int64_t n, float voxel,
 struct StreamStore;
 StreamStore *&handle_stream_store(vh_handle *h);
 void stream_store_free(StreamStore *s);
+// Waits for pending asynchronous evictions and moves them into the store.
+vh_status stream_store_settle(vh_handle *h);
 // The device state as of the last synchronising call.
 const DevState &handle_state(const vh_handle *h);
 // The frame list's neighbour table no longer matches the hash table.

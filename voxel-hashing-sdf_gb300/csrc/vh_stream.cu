@@ -27,11 +27,56 @@
 
 namespace vh {
 
+// Asynchronous eviction (vh_evict_async): one in-flight eviction per slot.
+// Device staging holds the gathered blocks once they have left the volume;
+// a copy kernel on the evictor's own stream writes them into mapped pinned
+// host memory while the handle's stream runs later frames.
+constexpr uint32_t kEvictCap = 1u << 15;  // blocks per call (192 MiB per slot)
+
+struct EvictSlot {
+  float *d_data = nullptr;              // kEvictCap blocks, device
+  unsigned long long *d_keys = nullptr;
+  uint32_t *d_ids = nullptr;
+  uint32_t *d_count = nullptr;          // selected blocks (may exceed kEvictCap)
+  float *h_data = nullptr;              // pinned and mapped: the copy's target
+  unsigned long long *h_keys = nullptr;
+  uint32_t *h_count = nullptr;
+  float *h_data_dev = nullptr;          // their device addresses
+  unsigned long long *h_keys_dev = nullptr;
+  uint32_t *h_count_dev = nullptr;
+  cudaEvent_t done = nullptr;           // the copy kernel has finished
+  bool busy = false;
+  uint64_t seq = 0;
+};
+
+struct Evictor {
+  cudaStream_t stream = nullptr;
+  EvictSlot slot[2];
+  uint64_t seq = 0;
+  uint64_t evicted_since_compaction = 0;
+  ~Evictor() {
+    if (stream) cudaStreamSynchronize(stream);
+    for (auto &e : slot) {
+      cudaFree(e.d_data);
+      cudaFree(e.d_keys);
+      cudaFree(e.d_ids);
+      cudaFree(e.d_count);
+      if (e.h_data) cudaFreeHost(e.h_data);
+      if (e.h_keys) cudaFreeHost(e.h_keys);
+      if (e.h_count) cudaFreeHost(e.h_count);
+      if (e.done) cudaEventDestroy(e.done);
+    }
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
 struct StreamStore {
   std::unordered_map<unsigned long long, size_t> index;  // key -> entry
   std::vector<unsigned long long> keys;                   // per entry (kEmptyKey: free)
   std::vector<float> data;                                // kBlockWords per entry
   std::vector<size_t> free_entries;
+  Evictor *evict = nullptr;                               // created on first use
+  ~StreamStore() { delete evict; }
 };
 
 void stream_store_free(StreamStore *s) { delete s; }
@@ -148,6 +193,66 @@ __global__ void __launch_bounds__(128) k_scatter_raw(VolumeView V, const int32_t
   reinterpret_cast<uint4 *>(dst + 2 * kB3)[t] = dc;
 }
 
+// Eviction, on the handle's stream: every selected block (keys[i], pool id
+// ids[i], i < min(*count, cap)) is copied into the device staging buffer,
+// then its slot becomes a tombstone and the block is zeroed and returned to
+// the free list, so that work enqueued after it no longer sees the block.
+// One CTA of 128 threads per block, grid-stride.
+__global__ void __launch_bounds__(128) k_evict(VolumeView V, const unsigned long long *__restrict__ keys,
+                                               const uint32_t *__restrict__ ids,
+                                               const uint32_t *__restrict__ count, uint32_t cap,
+                                               float *__restrict__ out) {
+  const uint32_t n = min(*count, cap);
+  const int t = threadIdx.x;
+  for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+    const uint32_t b = ids[i];
+    float4 *blk = reinterpret_cast<float4 *>(V.pool + (size_t)b * kBlockWords);
+    float4 *dst = reinterpret_cast<float4 *>(out + (size_t)i * kBlockWords);
+    for (int k = t; k < kBlockWords / 4; k += blockDim.x) dst[k] = blk[k];
+    __syncthreads();  // the block is in the staging buffer before it is cleared
+    for (int k = t; k < kBlockWords / 4; k += blockDim.x) blk[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+    if (t == 0) {
+      const unsigned long long key = keys[i];
+      const uint32_t h = (uint32_t)mix64(key) & V.slot_mask;
+      for (int p = 0; p < V.max_probe; ++p) {
+        const uint32_t s = (h + (uint32_t)p) & V.slot_mask;
+        const unsigned long long k = V.slots[s].key;
+        if (k == kEmptyKey) break;
+        if (k != key) continue;
+        V.slots[s].key = kTombKey;
+        V.slots[s].block = kNoBlock;
+        atomicAdd(&V.st->tombstones, 1u);
+        V.block_keys[b] = kEmptyKey;
+        __threadfence();
+        const uint32_t f = atomicAdd(&V.st->free_count, 1u);
+        V.free_list[f] = b;
+        break;
+      }
+    }
+  }
+}
+
+// The evicted blocks and their keys from device staging into mapped host
+// memory (on the evictor's stream, beside later frames); count last.
+__global__ void __launch_bounds__(256) k_evict_copy(const float *__restrict__ data,
+                                                    const unsigned long long *__restrict__ keys,
+                                                    const uint32_t *__restrict__ count, uint32_t cap,
+                                                    float *__restrict__ h_data,
+                                                    unsigned long long *__restrict__ h_keys,
+                                                    uint32_t *__restrict__ h_count) {
+  const uint32_t n = min(*count, cap);
+  const size_t words4 = (size_t)n * (kBlockWords / 4);
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const float4 *src = reinterpret_cast<const float4 *>(data);
+  float4 *dst = reinterpret_cast<float4 *>(h_data);
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < words4; k += stride)
+    dst[k] = src[k];
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride)
+    h_keys[k] = keys[k];
+  if (blockIdx.x == 0 && threadIdx.x == 0) *h_count = n;
+}
+
 // Table rebuild: every slot emptied, then the key of every live pool block
 // inserted again with its block id (keys are unique, so plain CAS claims).
 __global__ void __launch_bounds__(256) k_clear_slots(Slot *__restrict__ slots, uint32_t n) {
@@ -241,10 +346,144 @@ bool far_enough(unsigned long long key, float voxel, const float c[3], double r2
   return x * x + y * y + z * z > r2;
 }
 
+// Adds block `blk` of `key` to the host store; an older stored copy of the
+// same key is merged into it (merge_block_host) and dropped.
+void store_put(StreamStore &S, unsigned long long key, const float *blk) {
+  size_t e;
+  if (!S.free_entries.empty()) {
+    e = S.free_entries.back();
+    S.free_entries.pop_back();
+  } else {
+    e = S.keys.size();
+    S.keys.push_back(kEmptyKey);
+    S.data.resize(S.data.size() + kBlockWords);
+  }
+  std::memcpy(&S.data[e * kBlockWords], blk, sizeof(float) * kBlockWords);
+  S.keys[e] = key;
+  auto it = S.index.find(key);
+  if (it != S.index.end()) {
+    merge_block_host(&S.data[e * kBlockWords], &S.data[it->second * kBlockWords]);
+    S.keys[it->second] = kEmptyKey;
+    S.free_entries.push_back(it->second);
+    it->second = e;
+  } else {
+    S.index.emplace(key, e);
+  }
+}
+
+// Moves finished asynchronous evictions into the host store, oldest first:
+// with `wait`, every pending one (waiting for its copy); else those whose
+// copy has completed.
+vh_status evict_settle(vh_handle *h, bool wait) {
+  StreamStore *Sp = handle_stream_store(h);
+  if (!Sp || !Sp->evict) return VH_OK;
+  StreamStore &S = *Sp;
+  Evictor &E = *S.evict;
+  for (;;) {
+    EvictSlot *o = nullptr;
+    for (auto &e : E.slot)
+      if (e.busy && (!o || e.seq < o->seq)) o = &e;
+    if (!o) return VH_OK;
+    const cudaError_t q = wait ? cudaEventSynchronize(o->done) : cudaEventQuery(o->done);
+    if (q == cudaErrorNotReady) return VH_OK;
+    if (q != cudaSuccess) return handle_fail(h, VH_ERR_CUDA, "eviction copy failed");
+    const uint32_t n = *o->h_count;
+    for (uint32_t j = 0; j < n; ++j) store_put(S, o->h_keys[j], o->h_data + (size_t)j * kBlockWords);
+    E.evicted_since_compaction += n;
+    o->busy = false;
+  }
+}
+
+vh_status evictor_setup(vh_handle *h, Evictor **out) {
+  StreamStore &S = store_of(h);
+  if (S.evict) {
+    *out = S.evict;
+    return VH_OK;
+  }
+  Evictor *E = new Evictor();
+  bool ok = cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking) == cudaSuccess;
+  for (auto &e : E->slot) {
+    ok = ok && cudaMalloc(&e.d_data, sizeof(float) * kBlockWords * (size_t)kEvictCap) == cudaSuccess &&
+         cudaMalloc(&e.d_keys, sizeof(unsigned long long) * kEvictCap) == cudaSuccess &&
+         cudaMalloc(&e.d_ids, sizeof(uint32_t) * kEvictCap) == cudaSuccess &&
+         cudaMalloc(&e.d_count, sizeof(uint32_t)) == cudaSuccess &&
+         cudaHostAlloc(&e.h_data, sizeof(float) * kBlockWords * (size_t)kEvictCap,
+                       cudaHostAllocMapped) == cudaSuccess &&
+         cudaHostAlloc(&e.h_keys, sizeof(unsigned long long) * kEvictCap, cudaHostAllocMapped) ==
+             cudaSuccess &&
+         cudaHostAlloc(&e.h_count, sizeof(uint32_t), cudaHostAllocMapped) == cudaSuccess &&
+         cudaHostGetDevicePointer(&e.h_data_dev, e.h_data, 0) == cudaSuccess &&
+         cudaHostGetDevicePointer(&e.h_keys_dev, e.h_keys, 0) == cudaSuccess &&
+         cudaHostGetDevicePointer(&e.h_count_dev, e.h_count, 0) == cudaSuccess &&
+         cudaEventCreateWithFlags(&e.done, cudaEventDisableTiming) == cudaSuccess;
+  }
+  if (!ok) {
+    cudaGetLastError();
+    delete E;
+    return handle_fail(h, VH_ERR_CUDA, "asynchronous eviction: buffer allocation failed");
+  }
+  S.evict = E;
+  *out = E;
+  return VH_OK;
+}
+
 }  // namespace
 }  // namespace vh
 
 using namespace vh;
+
+extern "C" vh_status vh_evict_async(vh_handle *h, const float *centre, float radius) {
+  VH_HANDLE_DEVICE(h);
+  if (!h || !centre || !(radius >= 0.0f)) return VH_ERR_INVALID_ARG;
+  for (int a = 0; a < 3; ++a)
+    if (!std::isfinite(centre[a])) return VH_ERR_NOT_FINITE;
+  Evictor *E = nullptr;
+  vh_status s = evictor_setup(h, &E);
+  if (s != VH_OK) return s;
+  if ((s = evict_settle(h, false)) != VH_OK) return s;
+  const VolumeView V = handle_view(h);
+  // erased slots stay tombstones: rebuild the table (synchronously, rare)
+  // once the evictions since the last rebuild could fill an eighth of it
+  if (E->evicted_since_compaction + handle_state(h).tombstones > (V.slot_mask + 1u) / 8u) {
+    if ((s = evict_settle(h, true)) != VH_OK || (s = vh_compact_table(h)) != VH_OK) return s;
+    E->evicted_since_compaction = 0;
+  }
+  EvictSlot *slot = !E->slot[0].busy ? &E->slot[0] : (!E->slot[1].busy ? &E->slot[1] : nullptr);
+  if (!slot) {  // both in flight: finish the older one
+    EvictSlot *o = E->slot[0].seq < E->slot[1].seq ? &E->slot[0] : &E->slot[1];
+    if (cudaEventSynchronize(o->done) != cudaSuccess)
+      return handle_fail(h, VH_ERR_CUDA, "eviction copy failed");
+    if ((s = evict_settle(h, false)) != VH_OK) return s;
+    slot = o;
+  }
+  const CamParams C = handle_cam(h);
+  const cudaStream_t st = handle_stream(h);
+  const float r2 = radius * radius;
+  launch_epoch_end(V, st);  // allocation tickets settled before blocks are freed
+  if (cudaMemsetAsync(slot->d_count, 0, sizeof(uint32_t), st) != cudaSuccess)
+    return handle_fail(h, VH_ERR_CUDA, "eviction failed");
+  k_select_far<<<std::min<uint32_t>((V.pool_cap + 255) / 256, 4096), 256, 0, st>>>(
+      V, C.voxel, centre[0], centre[1], centre[2], std::isfinite(r2) ? r2 : 3.0e38f, slot->d_count,
+      slot->d_keys, slot->d_ids, kEvictCap);
+  k_evict<<<2048, 128, 0, st>>>(V, slot->d_keys, slot->d_ids, slot->d_count, kEvictCap,
+                                slot->d_data);
+  cudaEvent_t gathered = slot->done;  // reused: recorded on st, then waited by the copy
+  if (cudaGetLastError() != cudaSuccess || cudaEventRecord(gathered, st) != cudaSuccess ||
+      cudaStreamWaitEvent(E->stream, gathered, 0) != cudaSuccess)
+    return handle_fail(h, VH_ERR_CUDA, "eviction failed");
+  k_evict_copy<<<64, 256, 0, E->stream>>>(slot->d_data, slot->d_keys, slot->d_count, kEvictCap,
+                                          slot->h_data_dev, slot->h_keys_dev, slot->h_count_dev);
+  if (cudaGetLastError() != cudaSuccess || cudaEventRecord(slot->done, E->stream) != cudaSuccess)
+    return handle_fail(h, VH_ERR_CUDA, "eviction copy failed");
+  slot->busy = true;
+  slot->seq = ++E->seq;
+  handle_invalidate_nb(h);
+  return VH_OK;
+}
+
+namespace vh {
+vh_status stream_store_settle(vh_handle *h) { return evict_settle(h, true); }
+}  // namespace vh
 
 extern "C" vh_status vh_compact_table(vh_handle *h) {
   VH_HANDLE_DEVICE(h);
@@ -271,6 +510,8 @@ extern "C" vh_status vh_stream_out(vh_handle *h, const float *centre, float radi
   if (!h || !centre || !(radius >= 0.0f)) return VH_ERR_INVALID_ARG;
   for (int a = 0; a < 3; ++a)
     if (!std::isfinite(centre[a])) return VH_ERR_NOT_FINITE;
+  vh_status es = evict_settle(h, true);  // keeps the order of earlier evictions
+  if (es != VH_OK) return es;
   const VolumeView V = handle_view(h);
   const CamParams C = handle_cam(h);
   const cudaStream_t st = handle_stream(h);
@@ -353,6 +594,8 @@ extern "C" vh_status vh_stream_in(vh_handle *h, const float *centre, float radiu
   if (!h || !centre || !(radius >= 0.0f)) return VH_ERR_INVALID_ARG;
   for (int a = 0; a < 3; ++a)
     if (!std::isfinite(centre[a])) return VH_ERR_NOT_FINITE;
+  vh_status es = evict_settle(h, true);  // pending evictions reach the store first
+  if (es != VH_OK) return es;
   StreamStore *Sp = handle_stream_store(h);
   if (!Sp || Sp->index.empty()) return VH_OK;
   StreamStore &S = *Sp;
@@ -427,6 +670,10 @@ extern "C" vh_status vh_stream_in(vh_handle *h, const float *centre, float radiu
 
 extern "C" int64_t vh_host_blocks(const vh_handle *h) {
   if (!h) return 0;
+  {  // finished evictions count; pending ones are not waited for
+    DeviceScope on_device(handle_device(h));
+    evict_settle(const_cast<vh_handle *>(h), false);
+  }
   StreamStore *s = handle_stream_store(const_cast<vh_handle *>(h));
   return s ? (int64_t)s->index.size() : 0;
 }

@@ -129,6 +129,7 @@ SIGNATURES = {
     "vh_filter_depth": (I32, [P, P, I32, P, I32]),
     "vh_stream_out": (I32, [P, P, C.c_float, PI64]),
     "vh_stream_in": (I32, [P, P, C.c_float, PI64]),
+    "vh_evict_async": (I32, [P, P, C.c_float]),
     "vh_host_blocks": (I64, [P]),
     "vh_compact_table": (I32, [P]),
     "vh_mesh_indexed": (I32, [P, P, P, I64, P, I64, PI64, PI64]),

@@ -218,6 +218,12 @@ class Volume:
         self._check(self._L.vh_stream_in(self._h, c.ctypes.data, float(radius), C.byref(n)))
         return n.value
 
+    def evict_async(self, centre, radius):
+        """Moves blocks farther than `radius` from `centre` out of HBM without
+        waiting; they reach the host store while later frames run."""
+        c = np.ascontiguousarray(np.asarray(centre, np.float32).reshape(3))
+        self._check(self._L.vh_evict_async(self._h, c.ctypes.data, float(radius)))
+
     def compact_table(self):
         self._check(self._L.vh_compact_table(self._h))
 
