@@ -511,6 +511,40 @@ def hbm_stress_leg(num_frames, local, keyframes=16, iterations=20):
     return out
 
 
+def eviction_leg(params, tuning, dev, stream, radius=2.0):
+    """Out-of-core streaming beside the frames: the same device-resident
+    frames back to back, once plainly and once with vh_evict_async after
+    every frame (blocks farther than `radius` from the camera leave HBM for
+    the host store while the next frames run; re-observed blocks start
+    afresh).  Wall clock from the first submission to vh_sync."""
+    import torch
+    from vhsdf import Volume
+    out = {}
+    for mode in ("off", "on"):
+        vol = Volume(**params)
+        vol.set_tuning(**tuning)
+        vol.set_stream(stream.cuda_stream)
+        with torch.cuda.stream(stream):
+            vol.process_frame(*dev[0], depth_format="u16")  # graph capture
+            vol.sync()
+            vol.reset()
+            t0 = time.perf_counter()
+            for d, c, p in dev:
+                vol.process_frame(d, c, p, depth_format="u16")
+                if mode == "on":
+                    vol.evict_async(p[:3, 3], radius)
+            vol.sync()
+            dt = time.perf_counter() - t0
+        st = vol.stats()
+        out[mode] = {"frames_per_s": len(dev) / dt, "resident_blocks": st["blocks_allocated"],
+                     "host_blocks": vol.host_blocks()}
+        vol.close()
+    out["radius_m"] = radius
+    out["frames"] = len(dev)
+    out["slowdown"] = out["off"]["frames_per_s"] / out["on"]["frames_per_s"]
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -701,6 +735,7 @@ def run_engine(args):
         e2e_dev_s = time.perf_counter() - t0
     vol.close()
 
+    eviction = eviction_leg(params, tuning, dev, stream) if rank == 0 else None
     dev_ms, e2e_s, e2e_sync_s, e2e_dev_s = replicas.reduce_max(
         [dev_ms, e2e_s, e2e_sync_s, e2e_dev_s], device="cuda")
     if rank != 0:
@@ -783,6 +818,7 @@ def run_engine(args):
         "wall_s": t_wall,
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
+        "out_of_core": eviction,
         "pose_refinement": adjoint,
         "batched_scenes": batched,
         "batched_small_scenes": batched_small,

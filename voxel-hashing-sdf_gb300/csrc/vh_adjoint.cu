@@ -848,6 +848,7 @@ void fill_refine_stats(const RefineState &S, const float2 *hist, int iterations,
 extern "C" vh_status vh_sdf_sample(vh_handle *h, const float *xyz, int64_t n, float *phi,
                                    float *grad, uint8_t *valid, int32_t mem) {
   VH_HANDLE_DEVICE(h);
+  VH_NVTX("vh_sdf_sample");
   if (!h || n < 0 || (n && (!xyz || !phi)) || n > (1ll << 30)) return VH_ERR_INVALID_ARG;
   if (mem != VH_MEM_HOST && mem != VH_MEM_DEVICE) return VH_ERR_INVALID_ARG;
   if (!n) return VH_OK;
@@ -889,6 +890,7 @@ extern "C" vh_status vh_pose_normal_equations(vh_handle *h, const void *depth, i
                                               int32_t mem, const float *c2w, int32_t stride,
                                               int32_t method, double *terms) {
   VH_HANDLE_DEVICE(h);
+  VH_NVTX("vh_pose_normal_equations");
   if (!h || !c2w || !terms || stride < 1 || (method != VH_REFINE_ADJOINT && method != VH_REFINE_FD))
     return VH_ERR_INVALID_ARG;
   for (int i = 0; i < 16; ++i)
@@ -919,6 +921,7 @@ extern "C" vh_status vh_pose_refine(vh_handle *h, const void *depth, int32_t dep
                                     const float *c2w_init, int32_t iterations, int32_t stride,
                                     int32_t method, float *c2w_out, vh_refine_stats *stats) {
   VH_HANDLE_DEVICE(h);
+  VH_NVTX("vh_pose_refine");
   if (!h || !c2w_init || !c2w_out || iterations < 0 || iterations > (1 << 16) || stride < 1 ||
       (method != VH_REFINE_ADJOINT && method != VH_REFINE_FD))
     return VH_ERR_INVALID_ARG;
@@ -988,6 +991,7 @@ extern "C" vh_status vh_pose_refine_batch(vh_handle *h, const void *const *depth
                                           int32_t stride, float *c2w_out,
                                           vh_refine_stats *stats) {
   VH_HANDLE_DEVICE(h);
+  VH_NVTX("vh_pose_refine_batch");
   if (!h || !depth || !c2w_init || !c2w_out || n < 1 || n > VH_REFINE_BATCH_MAX ||
       iterations < 0 || iterations > (1 << 16) || stride < 1)
     return VH_ERR_INVALID_ARG;
@@ -1081,6 +1085,7 @@ extern "C" vh_status vh_integrate_vjp(vh_handle *h, const void *depth, int32_t d
                                       const float *c2w, const float *grad_sdf, float *grad_depth,
                                       float *grad_pose, int32_t mem) {
   VH_HANDLE_DEVICE(h);
+  VH_NVTX("vh_integrate_vjp");
   if (!h || !c2w || !grad_sdf || !grad_depth || !grad_pose) return VH_ERR_INVALID_ARG;
   if (mem != VH_MEM_HOST && mem != VH_MEM_DEVICE) return VH_ERR_INVALID_ARG;
   const cudaStream_t st = vh::handle_stream(h);

@@ -800,6 +800,7 @@ vh_status vh_set_stream(vh_handle *h, void *stream) {
 
 vh_status vh_sync(vh_handle *h) {
   VH_HANDLE_DEVICE(h);
+  VH_NVTX("vh_sync");
   if (!h) return VH_ERR_INVALID_ARG;
   vh_status s = mesh_drain(h);
   vh_status t = sync_and_check(h);
@@ -812,6 +813,7 @@ const char *vh_last_error(const vh_handle *h) { return h ? h->last_error.c_str()
 vh_status vh_integrate(vh_handle *h, const void *depth, int32_t depth_fmt, const uint8_t *rgb,
                        const float *c2w, int32_t mem) {
   VH_HANDLE_DEVICE(h);
+  VH_NVTX("vh_integrate");
   if (!h) return VH_ERR_INVALID_ARG;
   vh_status s = stage_inputs(h, depth, depth_fmt, rgb, c2w, mem);
   if (s != VH_OK) return s;
@@ -824,6 +826,7 @@ vh_status vh_integrate(vh_handle *h, const void *depth, int32_t depth_fmt, const
 
 vh_status vh_extract(vh_handle *h, int32_t scope, vh_mesh_view *out) {
   VH_HANDLE_DEVICE(h);
+  VH_NVTX("vh_extract");
   if (!h) return VH_ERR_INVALID_ARG;
   if (scope != VH_SCOPE_FRAME && scope != VH_SCOPE_ALL)
     return fail(h, VH_ERR_INVALID_ARG, "unknown extraction scope");
@@ -862,6 +865,7 @@ vh_status vh_extract(vh_handle *h, int32_t scope, vh_mesh_view *out) {
 vh_status vh_process_frame(vh_handle *h, const void *depth, int32_t depth_fmt, const uint8_t *rgb,
                            const float *c2w, int32_t mem, vh_mesh_view *out) {
   VH_HANDLE_DEVICE(h);
+  VH_NVTX("vh_process_frame");
   if (!h) return VH_ERR_INVALID_ARG;
   vh_status s = stage_inputs(h, depth, depth_fmt, rgb, c2w, mem);
   if (s != VH_OK) return s;
@@ -883,6 +887,7 @@ vh_status vh_process_frame_mesh(vh_handle *h, const void *depth, int32_t depth_f
                                 const uint8_t *rgb, const float *c2w, int32_t mem, float *tris,
                                 int64_t capacity, int64_t *num_triangles) {
   VH_HANDLE_DEVICE(h);
+  VH_NVTX("vh_process_frame_mesh");
   if (!h) return VH_ERR_INVALID_ARG;
   if (capacity < 0 || (capacity > 0 && !tris) || !num_triangles)
     return fail(h, VH_ERR_INVALID_ARG, "mesh output: null buffer or negative capacity");
@@ -968,6 +973,7 @@ static vh_status indexed_mesh(vh_handle *h, std::vector<float> &vert, std::vecto
 
 vh_status vh_save_ply(vh_handle *h, const char *path, int32_t binary) {
   VH_HANDLE_DEVICE(h);
+  VH_NVTX("vh_save_ply");
   if (!h || !path) return VH_ERR_INVALID_ARG;
   std::vector<float> vert;
   std::vector<uint8_t> col;
@@ -983,6 +989,7 @@ vh_status vh_mesh_indexed(vh_handle *h, float *vertices, uint8_t *colors, int64_
                           int32_t *faces, int64_t face_capacity, int64_t *num_vertices,
                           int64_t *num_faces) {
   VH_HANDLE_DEVICE(h);
+  VH_NVTX("vh_mesh_indexed");
   if (!h || vertex_capacity < 0 || face_capacity < 0) return VH_ERR_INVALID_ARG;
   std::vector<float> vert;
   std::vector<uint8_t> col;
@@ -1122,6 +1129,7 @@ vh_status vh_mc_tables(int32_t *corner, int32_t *edge_mask, int32_t *tri) {
 vh_status vh_export_blocks(vh_handle *h, int32_t *xyz, float *sdf, float *weight, uint8_t *rgb,
                            int64_t capacity, int64_t *n) {
   VH_HANDLE_DEVICE(h);
+  VH_NVTX("vh_export_blocks");
   if (!h || capacity < 0) return VH_ERR_INVALID_ARG;
   launch_epoch_end(h->V, h->stream);
   vh_status s = pull_state(h);
@@ -1195,6 +1203,7 @@ static vh_status check_blocks(vh_handle *h, const int32_t *xyz, const float *wei
 vh_status vh_import_blocks(vh_handle *h, const int32_t *xyz, const float *sdf, const float *weight,
                            const uint8_t *rgb, int64_t n) {
   VH_HANDLE_DEVICE(h);
+  VH_NVTX("vh_import_blocks");
   if (h) h->nb_valid = false;
   if (!h || n < 0 || (n && (!xyz || !sdf || !weight || !rgb)) || n > (1ll << 24))
     return VH_ERR_INVALID_ARG;

@@ -245,6 +245,7 @@ vh_handle *vh_batch_scene(vh_batch *b, int32_t i) {
 vh_status vh_batch_process(vh_batch *b, const void *const *depth, int32_t depth_fmt,
                            const uint8_t *const *rgb, const float *c2w, int32_t mem,
                            int32_t with_mesh) {
+  VH_NVTX("vh_batch_process");
   DeviceScope on_device(b ? b->device : -1);
   if (!on_device.ok()) return VH_ERR_CUDA;
   if (!b || !depth || !rgb || !c2w) return VH_ERR_INVALID_ARG;
@@ -339,6 +340,7 @@ vh_status vh_batch_process(vh_batch *b, const void *const *depth, int32_t depth_
 }
 
 vh_status vh_batch_sync(vh_batch *b, vh_status *status, vh_stats *stats) {
+  VH_NVTX("vh_batch_sync");
   DeviceScope on_device(b ? b->device : -1);
   if (!on_device.ok()) return VH_ERR_CUDA;
   if (!b) return VH_ERR_INVALID_ARG;

@@ -6,7 +6,19 @@
 
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 namespace vh {
+// NVTX range over one entry point (named after it): visible in Nsight
+// Systems timelines, a no-op without a profiler attached.
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
+#define VH_NVTX(name) ::vh::NvtxRange vh_nvtx_range__(name)
+
 VolumeView handle_view(const vh_handle *h);
 cudaStream_t handle_stream(const vh_handle *h);
 int handle_device(const vh_handle *h);

@@ -125,6 +125,7 @@ using namespace vh;
 extern "C" vh_status vh_raycast(vh_handle *h, const float *c2w, float *depth, float *normal,
                                 uint8_t *rgb, int32_t mem) {
   VH_HANDLE_DEVICE(h);
+  VH_NVTX("vh_raycast");
   if (!h || !c2w || !depth) return VH_ERR_INVALID_ARG;
   if (mem != VH_MEM_HOST && mem != VH_MEM_DEVICE) return VH_ERR_INVALID_ARG;
   for (int i = 0; i < 16; ++i)

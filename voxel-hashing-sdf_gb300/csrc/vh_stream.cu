@@ -434,6 +434,7 @@ using namespace vh;
 
 extern "C" vh_status vh_evict_async(vh_handle *h, const float *centre, float radius) {
   VH_HANDLE_DEVICE(h);
+  VH_NVTX("vh_evict_async");
   if (!h || !centre || !(radius >= 0.0f)) return VH_ERR_INVALID_ARG;
   for (int a = 0; a < 3; ++a)
     if (!std::isfinite(centre[a])) return VH_ERR_NOT_FINITE;
@@ -487,6 +488,7 @@ vh_status stream_store_settle(vh_handle *h) { return evict_settle(h, true); }
 
 extern "C" vh_status vh_compact_table(vh_handle *h) {
   VH_HANDLE_DEVICE(h);
+  VH_NVTX("vh_compact_table");
   if (!h) return VH_ERR_INVALID_ARG;
   const VolumeView V = handle_view(h);
   const cudaStream_t st = handle_stream(h);
@@ -506,6 +508,7 @@ extern "C" vh_status vh_compact_table(vh_handle *h) {
 extern "C" vh_status vh_stream_out(vh_handle *h, const float *centre, float radius,
                                    int64_t *moved) {
   VH_HANDLE_DEVICE(h);
+  VH_NVTX("vh_stream_out");
   if (moved) *moved = 0;
   if (!h || !centre || !(radius >= 0.0f)) return VH_ERR_INVALID_ARG;
   for (int a = 0; a < 3; ++a)
@@ -590,6 +593,7 @@ extern "C" vh_status vh_stream_out(vh_handle *h, const float *centre, float radi
 
 extern "C" vh_status vh_stream_in(vh_handle *h, const float *centre, float radius, int64_t *moved) {
   VH_HANDLE_DEVICE(h);
+  VH_NVTX("vh_stream_in");
   if (moved) *moved = 0;
   if (!h || !centre || !(radius >= 0.0f)) return VH_ERR_INVALID_ARG;
   for (int a = 0; a < 3; ++a)
