@@ -267,6 +267,21 @@ def adjoint_leg(num_frames, local, iterations=20):
                        "err_mm_p90": float(np.percentile(e_mm, 90)),
                        "err_deg_p90": float(np.percentile(e_deg, 90))}
     gap = [pose_error(a, b) for a, b in zip(poses["adjoint"], poses["fd"])]
+    # the data's floor: refinement started at the ground-truth pose
+    floor, to_floor = [], []
+    for f, r in zip(picks, poses["adjoint"]):
+        d, _, gt = frames[f]
+        r0, _ = vol.pose_refine(d, gt, iterations=iterations, stride=1, method="adjoint")
+        floor.append(pose_error(r0, gt))
+        to_floor.append(pose_error(r, r0))
+    out["floor"] = {
+        "from": "refinement started at the ground-truth pose (same steps, adjoint)",
+        "err_mm_median": float(np.median([1000 * e[0] for e in floor])),
+        "err_deg_median": float(np.median([e[1] for e in floor])),
+        "adjoint_gap_to_floor_mm_median": float(np.median([1000 * e[0] for e in to_floor])),
+        "adjoint_gap_to_floor_deg_median": float(np.median([e[1] for e in to_floor])),
+        "adjoint_within_1mm_0.05deg_of_floor": int(sum(1 for e in to_floor
+                                                        if 1000 * e[0] <= 1 and e[1] <= 0.05))}
     # the same poses through vh_pose_refine_batch, 16 per call (one launch per
     # Gauss-Newton step for all 16)
     vol.pose_refine_batch([frames[int(f)][0] for f in picks[:16]],
@@ -297,6 +312,7 @@ def adjoint_leg(num_frames, local, iterations=20):
                         f"(seeded); {iterations} Gauss-Newton steps, all 307200 pixels",
             "adjoint": out["adjoint"], "fd_jacobian": out["fd"],
             "adjoint_batched": out["adjoint_batched"],
+            "floor": out["floor"],
             "adjoint_vs_fd_pose_gap_mm_median": float(np.median([1000 * g[0] for g in gap])),
             "speedup": out["adjoint"]["pose_steps_per_s"] / out["fd"]["pose_steps_per_s"],
             "same_volume": extras}
