@@ -190,9 +190,12 @@ def test_refine_stops_without_residuals(room):
     assert st["iterations"] == 20 and np.array_equal(again, ref)
 
 
-def test_integration_vjp_against_fp64_finite_differences(gpu):
+@pytest.fixture(scope="module")
+def plane_vjp(gpu):
     """Plane scene (constant depth), so pixel re-assignment under a pose
-    perturbation cannot change any sample."""
+    perturbation cannot change any sample: the engine's VJP of the second
+    integration and FP64 finite differences of the oracle's update along a
+    random depth direction and a random se(3) direction."""
     from vhsdf import Volume
     from oracle.oracle import Oracle
     W, H, f = 64, 48, 50.0
@@ -252,8 +255,6 @@ def test_integration_vjp_against_fp64_finite_differences(gpu):
     # the float32 images carry the step rounded to float32 (~3e-4 of h per
     # pixel, ~0.5 on this loss): compare against the step actually taken
     step = (dp.astype(np.float64) - dm.astype(np.float64)) / (2 * h)
-    an = float(np.sum(gd.astype(np.float64) * step))
-    assert abs(fd - an) < 2e-3 * max(1.0, abs(fd)), (fd, an)
     # pose: directional derivative along a random se(3) direction.  The
     # oracle takes camera z in fp32 (its decisions are the reference's fp32
     # operations), so every voxel's sdf carries a rounding of ~6e-8 m / T
@@ -275,8 +276,38 @@ def test_integration_vjp_against_fp64_finite_differences(gpu):
         return out.astype(np.float32)
 
     fdp = (loss(d1, moved(1)) - loss(d1, moved(-1))) / (2 * hp)
-    anp = float(np.dot(gp.astype(np.float64), xi))
-    assert abs(fdp - anp) < 2e-2 * max(1.0, abs(fdp)), (fdp, anp)
+    return dict(vol=vol, pre=pre, d1=d1, pose1=pose1, rgb=rgb, G=G, lst=lst, gd=gd, gp=gp,
+                fd=fd, step=step, fdp=fdp, xi=xi)
+
+
+def check_against_fd(c, gd, gp):
+    an = float(np.sum(np.asarray(gd, np.float64) * c["step"]))
+    assert abs(c["fd"] - an) < 2e-3 * max(1.0, abs(c["fd"])), (c["fd"], an)
+    anp = float(np.dot(np.asarray(gp, np.float64), c["xi"]))
+    assert abs(c["fdp"] - anp) < 2e-2 * max(1.0, abs(c["fdp"])), (c["fdp"], anp)
+
+
+def test_integration_vjp_against_fp64_finite_differences(plane_vjp):
+    check_against_fd(plane_vjp, plane_vjp["gd"], plane_vjp["gp"])
+
+
+def test_integration_autograd_binding(plane_vjp):
+    """The test-only torch.autograd.Function over the integration update:
+    its backward (vh_integrate_vjp) gives the engine's VJP exactly and
+    matches the FP64 finite differences."""
+    from sdf_autograd import integrate_frame
+    c = plane_vjp
+    depth = torch.tensor(c["d1"], dtype=torch.float32, device="cuda", requires_grad=True)
+    delta = torch.zeros(6, dtype=torch.float64, device="cuda", requires_grad=True)
+    out = integrate_frame(depth, delta, c["vol"], c["pose1"], c["rgb"], c["pre"])
+    assert out.shape == c["G"].shape
+    G = c["G"][np.lexsort(c["lst"].T[::-1])]  # the binding's block order
+    (out * torch.from_numpy(G).cuda()).sum().backward()
+    gd = depth.grad.cpu().numpy()
+    gp = delta.grad.cpu().numpy()
+    assert np.array_equal(gd, c["gd"])
+    assert np.array_equal(gp.astype(np.float32), c["gp"])
+    check_against_fd(c, gd, gp)
 
 
 def test_batched_refinement(room):
