@@ -293,8 +293,8 @@ def test_integration_vjp_against_fp64_finite_differences(plane_vjp):
 
 def test_integration_autograd_binding(plane_vjp):
     """The test-only torch.autograd.Function over the integration update:
-    its backward (vh_integrate_vjp) gives the engine's VJP exactly and
-    matches the FP64 finite differences."""
+    its backward (vh_integrate_vjp) gives the engine's VJP (up to the order
+    of its float atomic sums) and matches the FP64 finite differences."""
     from sdf_autograd import integrate_frame
     c = plane_vjp
     depth = torch.tensor(c["d1"], dtype=torch.float32, device="cuda", requires_grad=True)
@@ -305,8 +305,9 @@ def test_integration_autograd_binding(plane_vjp):
     (out * torch.from_numpy(G).cuda()).sum().backward()
     gd = depth.grad.cpu().numpy()
     gp = delta.grad.cpu().numpy()
-    assert np.array_equal(gd, c["gd"])
-    assert np.array_equal(gp.astype(np.float32), c["gp"])
+    # the VJP sums pixel gradients with float atomics: equal up to summation order
+    assert np.allclose(gd, c["gd"], rtol=1e-5, atol=1e-3)
+    assert np.allclose(gp, c["gp"], rtol=1e-4, atol=1e-2)
     check_against_fd(c, gd, gp)
 
 
