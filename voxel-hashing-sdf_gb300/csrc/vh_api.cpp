@@ -231,14 +231,10 @@ void enqueue_frame(vh_handle *h, int fmt, int mc, bool events, bool capturing) {
   if (events) stage_event(h->ev[0], s, capturing);
   launch_frame_begin(h->V, &h->fin, h->d_fin, s);
   ++kernels;
-  const void *depth = nullptr;  // the frame's own image, found through d_fin
-  if (h->p.flags & VH_FLAG_DEPTH_FILTER) {
-    launch_depth_filter(h->C, nullptr, h->d_fin, fmt, h->d_depth_f, s);
-    ++kernels;
-    depth = h->d_depth_f;
-    fmt = VH_DEPTH_F32_M;
-  }
-  launch_allocate(h->V, h->C, h->d_fin, depth, fmt, h->d_pix, s);
+  // the frame's own image, found through d_fin; the depth pre-filter runs
+  // inside the allocation kernel, whose pixel records integration reads
+  launch_allocate(h->V, h->C, h->d_fin, nullptr, fmt, (h->p.flags & VH_FLAG_DEPTH_FILTER) != 0,
+                  h->d_pix, s);
   launch_frame_resolve(h->V, h->sm_count * 8, mc != kMcNone, s);  // probes in flight: many CTAs
   kernels += 2;
   if (events) stage_event(h->ev[1], s, capturing);

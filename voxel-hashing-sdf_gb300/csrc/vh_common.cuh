@@ -173,9 +173,10 @@ void launch_clear_list(const VolumeView &V, cudaStream_t s);
 void launch_mc_begin(const VolumeView &V, cudaStream_t s);
 
 // fmt: 0 = uint16 scaled by depth_scale, 1 = float metres.  depth (when not
-// null) replaces fin->depth, e.g. by the filtered copy.
+// null) replaces fin->depth.  filter: each pixel's depth goes through the
+// bilateral pre-filter (VH_FLAG_DEPTH_FILTER) inside the allocation kernel.
 void launch_allocate(const VolumeView &V, const CamParams &C, const FrameIn *fin,
-                     const void *depth, int fmt, uint2 *pix, cudaStream_t s);
+                     const void *depth, int fmt, bool filter, uint2 *pix, cudaStream_t s);
 // variant 0: one block in flight per CTA; 1: next block prefetched
 void launch_integrate(const VolumeView &V, const CamParams &C, const uint2 *pix,
                       const float *pose, int grid, int variant, cudaStream_t s);
@@ -199,8 +200,8 @@ void launch_list_keys(const VolumeView &V, int32_t *xyz, uint32_t n, cudaStream_
 void launch_scatter_blocks(const VolumeView &V, const int32_t *xyz, const float *sdf,
                            const float *w, const uint8_t *rgb, uint32_t n, cudaStream_t s);
 
-// Bilateral pre-filter of one depth image into float metres (vh_filter.cu);
-// depth == nullptr reads the image of fin.
+// Bilateral pre-filter of one depth image into float metres; depth ==
+// nullptr reads the image of fin.
 // rcp[w] = 1 / w correctly rounded for w in [1, kRcpMax] (rcp[0] = 0).
 void launch_rcp_table(float *rcp, cudaStream_t s);
 

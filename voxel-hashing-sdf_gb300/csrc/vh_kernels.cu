@@ -251,6 +251,52 @@ __device__ __forceinline__ float load_depth<float>(const float *d, int i, float)
   return __ldg(d + i);
 }
 
+// ---- depth pre-filter (VH_FLAG_DEPTH_FILTER) ---------------------------------------
+// The reference only scales its depth (SaveFrame::frameLoad,
+// src/SaveFrame.cpp:179-180).  With the flag set, each pixel's depth is
+// smoothed by an edge-preserving bilateral filter over a 5x5 window:
+// weights exp(-r^2 / (2 s^2)) exp(-(d - d0)^2 / (2 sr^2)) with s = 2 pixels
+// and sr = 5 mm + 3 * 1.5e-3 d0^2 (three standard deviations of
+// structured-light depth noise), neighbours that are invalid or farther than
+// 3 sr from the centre depth left out; an invalid centre pixel stays invalid
+// (0).  Allocation computes it for its own pixel from the raw image (the
+// filter is fused into the allocation kernel's depth read), and
+// vh_filter_depth writes the same values as an image; both come from this
+// function in this translation unit, so they agree bit for bit.
+template <typename DepthT>
+__device__ __forceinline__ float filtered_depth(const CamParams &C, const DepthT *__restrict__ in,
+                                                int idx) {
+  const int u = idx % C.width, v = idx / C.width;
+  const float d0 = load_depth<DepthT>(in, idx, C.depth_scale);
+  if (!(d0 > C.min_depth && d0 <= C.max_depth)) return 0.0f;
+  const float sr = 0.005f + 4.5e-3f * d0 * d0;
+  const float inv_2sr2 = 1.0f / (2.0f * sr * sr), inv_2ss2 = 1.0f / 8.0f;  // s = 2 px
+  float sum = 0.0f, wsum = 0.0f;
+#pragma unroll
+  for (int dy = -2; dy <= 2; ++dy)
+#pragma unroll
+    for (int dx = -2; dx <= 2; ++dx) {
+      const int x = u + dx, y = v + dy;
+      if (x < 0 || x >= C.width || y < 0 || y >= C.height) continue;
+      const float d = load_depth<DepthT>(in, y * C.width + x, C.depth_scale);
+      if (!(d > C.min_depth && d <= C.max_depth) || fabsf(d - d0) >= 3.0f * sr) continue;
+      const float w = expf(-(float)(dx * dx + dy * dy) * inv_2ss2 - (d - d0) * (d - d0) * inv_2sr2);
+      sum += w * d;
+      wsum += w;
+    }
+  return sum / wsum;  // the centre contributes weight 1
+}
+
+template <typename DepthT>
+__global__ void __launch_bounds__(256) k_depth_filter(CamParams C, const DepthT *__restrict__ depth,
+                                                      const FrameIn *__restrict__ fin,
+                                                      float *__restrict__ out) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= C.width * C.height) return;
+  const DepthT *in = depth ? depth : static_cast<const DepthT *>(fin->depth);
+  out[idx] = filtered_depth<DepthT>(C, in, idx);
+}
+
 // ---- allocation ----------------------------------------------------------------
 constexpr int kAllocChunk = 4;  // band steps of a warp collected before one resolve pass
 
@@ -279,7 +325,7 @@ __device__ __forceinline__ void resolve_keys(const VolumeView &V, const unsigned
 // Pixel idx of one frame (all 32 lanes of the warp take part: the band walk
 // is de-duplicated per warp).  Lanes with idx >= npx only follow the warp.
 // wkeys: this warp's 32 * kAllocChunk key slots in shared memory.
-template <typename DepthT>
+template <typename DepthT, bool kFilter = false>
 __device__ __forceinline__ void allocate_pixel(const VolumeView &V, const CamParams &C,
                                                const DepthT *__restrict__ depth,
                                                const uint8_t *__restrict__ rgb,
@@ -298,7 +344,8 @@ __device__ __forceinline__ void allocate_pixel(const VolumeView &V, const CamPar
   bool active = false;
   BandWalk w;
   if (idx < npx) {
-    const float d = load_depth<DepthT>(depth, idx, C.depth_scale);
+    const float d = kFilter ? filtered_depth<DepthT>(C, depth, idx)
+                            : load_depth<DepthT>(depth, idx, C.depth_scale);
     const uint32_t c = (uint32_t)__ldg(rgb + 3 * idx) | ((uint32_t)__ldg(rgb + 3 * idx + 1) << 8) |
                        ((uint32_t)__ldg(rgb + 3 * idx + 2) << 16);
     pix[idx] = make_uint2(__float_as_uint(d), c);
@@ -346,14 +393,14 @@ __device__ __forceinline__ void allocate_pixel(const VolumeView &V, const CamPar
   }
 }
 
-template <typename DepthT>
+template <typename DepthT, bool kFilter>
 __global__ void __launch_bounds__(256, 6) k_allocate(VolumeView V, CamParams C,
                                                   const FrameIn *__restrict__ fin,
                                                   const DepthT *__restrict__ depth,
                                                   uint2 *__restrict__ pix) {
   __shared__ unsigned long long keys[256 / 32][32 * kAllocChunk];
   const DepthT *d = depth ? depth : static_cast<const DepthT *>(fin->depth);
-  allocate_pixel<DepthT>(V, C, d, fin->rgb, fin->pose, pix, blockIdx.x * blockDim.x + threadIdx.x,
+  allocate_pixel<DepthT, kFilter>(V, C, d, fin->rgb, fin->pose, pix, blockIdx.x * blockDim.x + threadIdx.x,
                          keys[threadIdx.x >> 5]);
 }
 
@@ -1403,12 +1450,27 @@ void launch_clear_list(const VolumeView &V, cudaStream_t s) { k_clear_list<<<1, 
 void launch_mc_begin(const VolumeView &V, cudaStream_t s) { k_mc_begin<<<1, 32, 0, s>>>(V); }
 
 void launch_allocate(const VolumeView &V, const CamParams &C, const FrameIn *fin,
-                     const void *depth, int fmt, uint2 *pix, cudaStream_t s) {
+                     const void *depth, int fmt, bool filter, uint2 *pix, cudaStream_t s) {
+  const unsigned grid = grid_for((uint32_t)C.width * (uint32_t)C.height, 256);
+  const uint16_t *d16 = (const uint16_t *)depth;
+  const float *d32 = (const float *)depth;
+  if (fmt == 0 && filter)
+    k_allocate<uint16_t, true><<<grid, 256, 0, s>>>(V, C, fin, d16, pix);
+  else if (fmt == 0)
+    k_allocate<uint16_t, false><<<grid, 256, 0, s>>>(V, C, fin, d16, pix);
+  else if (filter)
+    k_allocate<float, true><<<grid, 256, 0, s>>>(V, C, fin, d32, pix);
+  else
+    k_allocate<float, false><<<grid, 256, 0, s>>>(V, C, fin, d32, pix);
+}
+
+void launch_depth_filter(const CamParams &C, const void *depth, const FrameIn *fin, int fmt,
+                         float *out, cudaStream_t s) {
   const unsigned grid = grid_for((uint32_t)C.width * (uint32_t)C.height, 256);
   if (fmt == 0)
-    k_allocate<uint16_t><<<grid, 256, 0, s>>>(V, C, fin, (const uint16_t *)depth, pix);
+    k_depth_filter<uint16_t><<<grid, 256, 0, s>>>(C, static_cast<const uint16_t *>(depth), fin, out);
   else
-    k_allocate<float><<<grid, 256, 0, s>>>(V, C, fin, (const float *)depth, pix);
+    k_depth_filter<float><<<grid, 256, 0, s>>>(C, static_cast<const float *>(depth), fin, out);
 }
 
 int integrate_ctas_per_sm(int variant) {
