@@ -50,6 +50,21 @@ ENGINE_PARAMS = dict(width=640, height=480, min_depth=0.1, max_depth=4.0, voxel_
 L2_BYTES = 129 * 1024 * 1024
 
 
+def traffic_ratios():
+    """DRAM traffic / algorithmic bytes per kernel launch from the committed
+    ncu capture (profiles/traffic_per_kernel_long_stream.txt), or {}."""
+    out = {}
+    try:
+        with open(os.path.join(REPO, "profiles", "traffic_per_kernel_long_stream.txt")) as f:
+            for line in f:
+                if line.startswith("traffic_ratio "):
+                    _, k, v = line.split()
+                    out[k] = float(v)
+    except OSError:
+        pass
+    return out
+
+
 def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -784,9 +799,9 @@ def run_engine(args):
     #               once) + 48 B per output triangle (3 x float4 vertex)
     #   k_integrate 12 B per voxel of every listed block read + 12 B per
     #               updated voxel written + 8 B per pixel record
-    # DRAM traffic per launch comes from one ncu capture of frames 3-4 of this
-    # stream (60k-block pool): k_mc moved 0.91x and k_integrate 0.85x their
-    # algorithmic bytes; traffic below scales those ratios to this run.
+    # DRAM traffic per launch: the traffic / algorithmic ratio that the
+    # committed warm-cache ncu capture of this stream measured per kernel
+    # (frames 3-4, one kernel per capture), scaled to this run's launches.
     npx = 640 * 480
     blocks = [s["frame_blocks"] for s in stage]
     updated = [s["voxels_updated"] for s in stage]
@@ -798,6 +813,7 @@ def run_engine(args):
     mc_ach = sum(mc_alg) / (sum(mc_ms) / 1000.0) / 1e9
     in_ach = sum(in_alg) / (sum(in_ms) / 1000.0) / 1e9
     peak, peak_src = peak_hbm()
+    ratios = traffic_ratios()
     cpu = None
     if world == 1:  # the CPU baseline is rank 0's at N=1 only
         cpu = cpu_leg(frames, scene, seconds=args.cpu_seconds)
@@ -831,11 +847,15 @@ def run_engine(args):
                 "sync_per_frame": e2e_sync,
                 "mesh_left_on_device": e2e_dev},
         "roofline": {"bound": "hbm", "achieved": mc_ach, "peak": peak, "unit": "GB/s",
-                     "frac": mc_ach / peak, "traffic": 0.91 * statistics.mean(mc_alg),
+                     "frac": mc_ach / peak,
+                     "traffic": (ratios["k_mc"] * statistics.mean(mc_alg)
+                                 if "k_mc" in ratios else None),
                      "kernel": "k_mc", "peak_source": peak_src,
                      "algorithmic_bytes": statistics.mean(mc_alg)},
         "roofline_integrate": {"bound": "hbm", "achieved": in_ach, "peak": peak, "unit": "GB/s",
-                               "frac": in_ach / peak, "traffic": 0.85 * statistics.mean(in_alg),
+                               "frac": in_ach / peak,
+                               "traffic": (ratios["k_integrate"] * statistics.mean(in_alg)
+                                           if "k_integrate" in ratios else None),
                                "kernel": "k_integrate", "peak_source": peak_src,
                                "algorithmic_bytes": statistics.mean(in_alg)},
         "stages_ms": {k: statistics.mean(s[k] for s in stage)
