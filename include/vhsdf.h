@@ -398,9 +398,13 @@ typedef struct vh_batch vh_batch;
 /* n independent scenes (1..VH_BATCH_MAX_SCENES) on params[0].device; scene i
  * has params[i]: image size, intrinsics, voxel size, truncation, table and
  * pool sizes may all differ (VH_FLAG_DEPTH_FILTER is not supported in a
- * batch: VH_ERR_UNSUPPORTED).  Every scene is a full handle (vh_batch_scene)
- * that shares the batch's stream; the launch shapes follow the first
- * scene's tuning (vh_set_tuning / vh_autotune on vh_batch_scene(b, 0)). */
+ * batch: VH_ERR_UNSUPPORTED).  Every scene is a full handle (vh_batch_scene).
+ * The scenes form up to 16 groups of about equal pixel count; each group has
+ * its own stream, which is also the stream of its scenes' handles, so calls
+ * on a scene handle are ordered with that scene's steps, and groups move
+ * from step to step independently (vh_batch_sync joins them).  The launch
+ * shapes follow the first scene's tuning (vh_set_tuning / vh_autotune on
+ * vh_batch_scene(b, 0)). */
 vh_status vh_batch_create(const vh_params *params, int32_t n, vh_batch **out);
 vh_status vh_batch_destroy(vh_batch *b);
 int32_t vh_batch_size(const vh_batch *b);
@@ -409,9 +413,10 @@ int32_t vh_batch_size(const vh_batch *b);
 vh_handle *vh_batch_scene(vh_batch *b, int32_t i);
 /* One frame for every scene i with depth[i] != NULL (the other scenes keep
  * their state): allocation, integration and, with with_mesh, the
- * marching cubes of the frame's blocks.  Each stage is ONE launch over the
- * work of all those scenes (flattened scene x item index), and the stages of
- * a step replay as one CUDA graph.  depth[i] (format depth_fmt, shared) and
+ * marching cubes of the frame's blocks.  Each stage is ONE launch per group
+ * over the work of all its scenes (flattened scene x item index), and a
+ * group's stages of a step replay as one CUDA graph on the group's stream.
+ * depth[i] (format depth_fmt, shared) and
  * rgb[i] are in `mem`: host frames are copied into the scene's staging
  * buffers, device frames are read in place by the step (leave them unchanged
  * until it completes); c2w holds n row-major 4x4 poses (host; entries of

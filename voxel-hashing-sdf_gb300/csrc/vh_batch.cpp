@@ -11,10 +11,13 @@
 // launches replay as one CUDA graph whose arguments never change.
 //
 // The scenes are split into a few contiguous groups of about equal pixel
-// count, each with its own stage launches on its own stream (forked from
-// and joined back into the batch stream, inside the graph): a scene's
-// integration needs only its own allocation, so one group's latency-bound
-// allocation overlaps another group's issue-bound integration.
+// count.  Each group has its own stream, which is also the stream of its
+// scenes' handles, and runs its stage launches there as one CUDA graph per
+// step: a scene depends only on its own earlier frames, so groups move on
+// from step to step independently (no step-wide join), one group's
+// latency-bound allocation overlapping another's issue-bound integration.
+// The per-step descriptor blocks live in a ring on the device; a block is
+// rewritten only after every group has finished the step that read it.
 
 #include <algorithm>
 #include <cmath>
@@ -43,7 +46,11 @@ struct BatchGroup {
   uint32_t *d_px_start = nullptr;  // n + 1, relative to the group
   uint32_t *d_prefix = nullptr;    // n + 1 prefix words, then the MC block counter
   cudaStream_t stream = nullptr;
-  cudaEvent_t done = nullptr;
+  cudaEvent_t done[kRing] = {};    // this group's step that read ring block k
+  bool used[kRing] = {};
+  cudaEvent_t last = nullptr;      // this group's latest work
+  // step graphs per depth format, mesh flag and ring block
+  cudaGraphExec_t graphs[2][2][kRing] = {};
 };
 }
 
@@ -51,45 +58,60 @@ struct vh_batch {
   int n = 0;
   int device = 0;
   int sm_count = 0;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;  // descriptor uploads and the state gather
   std::vector<vh_handle *> scenes;
   // per-step upload block: SceneDesc[n] | float pose[16 n] | uint8 active[n]
   size_t desc_bytes = 0, pose_bytes = 0, block_bytes = 0;
-  unsigned char *d_block = nullptr;
+  unsigned char *d_block = nullptr;  // kRing blocks
   unsigned char *h_block = nullptr;  // pinned, kRing blocks
-  cudaEvent_t ring_ev[kRing] = {};
+  cudaEvent_t ring_ev[kRing] = {};   // upload of ring block k done
   int ring_pos = 0;
+  SceneDesc *d_static = nullptr;     // n: every scene's volume view (state gather)
   std::vector<BatchGroup> groups;
-  cudaEvent_t fork = nullptr;
+  cudaEvent_t joined = nullptr;      // the batch stream after a state gather
   DevState *d_states = nullptr;  // n
   DevState *h_states = nullptr;  // pinned, n
-  cudaGraphExec_t graphs[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
   int graph_shape[3] = {0, 0, -1};  // integrate grid, MC grid, MC variant the graphs hold
   std::string last_error;
 
-  SceneDesc *desc() const { return reinterpret_cast<SceneDesc *>(d_block); }
-  const float *pose(int i) const {
-    return reinterpret_cast<const float *>(d_block + desc_bytes) + 16 * (size_t)i;
+  unsigned char *block(int k) const { return d_block + block_bytes * (size_t)k; }
+  SceneDesc *desc(int k) const { return reinterpret_cast<SceneDesc *>(block(k)); }
+  const float *pose(int k, int i) const {
+    return reinterpret_cast<const float *>(block(k) + desc_bytes) + 16 * (size_t)i;
   }
-  const uint8_t *active() const { return d_block + desc_bytes + pose_bytes; }
+  const uint8_t *active(int k) const { return block(k) + desc_bytes + pose_bytes; }
 };
 
 namespace {
 
+void drop_step_graphs(vh_batch *b) {
+  for (BatchGroup &g : b->groups)
+    for (auto &a : g.graphs)
+      for (auto &m : a)
+        for (auto &x : m)
+          if (x) {
+            cudaGraphExecDestroy(x);
+            x = nullptr;
+          }
+}
+
 void free_batch(vh_batch *b) {
-  for (auto &row : b->graphs)
-    for (auto &g : row)
-      if (g) cudaGraphExecDestroy(g);
+  drop_step_graphs(b);
+  for (BatchGroup &g : b->groups)
+    if (g.stream) cudaStreamSynchronize(g.stream);
   for (vh_handle *h : b->scenes)
     if (h) vh_destroy(h);
   cudaFree(b->d_block);
+  cudaFree(b->d_static);
   for (BatchGroup &g : b->groups) {
     cudaFree(g.d_px_start);
     cudaFree(g.d_prefix);
-    if (g.done) cudaEventDestroy(g.done);
+    for (auto &e : g.done)
+      if (e) cudaEventDestroy(e);
+    if (g.last) cudaEventDestroy(g.last);
     if (g.stream) cudaStreamDestroy(g.stream);
   }
-  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->joined) cudaEventDestroy(b->joined);
   cudaFree(b->d_states);
   if (b->h_block) cudaFreeHost(b->h_block);
   if (b->h_states) cudaFreeHost(b->h_states);
@@ -108,24 +130,19 @@ void batch_shape(const vh_batch *b, int out[3]) {
   out[2] = f0.mc_variant;
 }
 
-// One step: every group's stages on its own stream, forked from and joined
-// back into the batch stream (also inside a stream capture).
-void enqueue_step(vh_batch *b, int fmt, bool with_mesh, const int shape[3]) {
-  cudaEventRecord(b->fork, b->stream);
-  for (BatchGroup &g : b->groups) {
-    const SceneDesc *d = b->desc() + g.s0;
-    const uint8_t *act = b->active() + g.s0;
-    cudaStream_t s = g.stream;
-    cudaStreamWaitEvent(s, b->fork, 0);
-    launch_batch_frame_begin(d, act, g.n, s);
-    launch_batch_allocate(d, act, g.d_px_start, g.total_px, g.n, fmt, s);
-    launch_batch_epoch_end(d, act, g.n, g.d_prefix, with_mesh, s);
-    launch_batch_resolve(d, g.d_prefix, g.n, b->sm_count * 2, s);
-    launch_batch_integrate(d, g.d_prefix, g.n, shape[0], s);
-    if (with_mesh) launch_batch_mc(d, g.d_prefix, g.n, shape[1], shape[2], s);
-    cudaEventRecord(g.done, s);
-    cudaStreamWaitEvent(b->stream, g.done, 0);
-  }
+// One group's stages of one step, reading ring block k, on the group's
+// stream (also inside a stream capture).
+void enqueue_group_step(vh_batch *b, BatchGroup &g, int k, int fmt, bool with_mesh,
+                        const int shape[3]) {
+  const SceneDesc *d = b->desc(k) + g.s0;
+  const uint8_t *act = b->active(k) + g.s0;
+  cudaStream_t s = g.stream;
+  launch_batch_frame_begin(d, act, g.n, s);
+  launch_batch_allocate(d, act, g.d_px_start, g.total_px, g.n, fmt, s);
+  launch_batch_epoch_end(d, act, g.n, g.d_prefix, with_mesh, s);
+  launch_batch_resolve(d, g.d_prefix, g.n, b->sm_count * 2, s);
+  launch_batch_integrate(d, g.d_prefix, g.n, shape[0], s);
+  if (with_mesh) launch_batch_mc(d, g.d_prefix, g.n, shape[1], shape[2], s);
 }
 
 vh_status fail(vh_batch *b, vh_status s, const std::string &msg) {
@@ -168,7 +185,6 @@ vh_status vh_batch_create(const vh_params *params, int32_t n, vh_batch **out) {
     free_batch(b);
     return VH_ERR_CUDA;
   }
-  for (vh_handle *h : b->scenes) vh_set_stream(h, b->stream);
   b->desc_bytes = sizeof(SceneDesc) * (size_t)n;
   b->pose_bytes = 16 * sizeof(float) * (size_t)n;
   b->block_bytes = (b->desc_bytes + b->pose_bytes + (size_t)n + 15) & ~(size_t)15;
@@ -198,11 +214,12 @@ vh_status vh_batch_create(const vh_params *params, int32_t n, vh_batch **out) {
     }
     G.n = i - G.s0;
   }
-  bool ok = cudaMalloc(&b->d_block, b->block_bytes) == cudaSuccess &&
+  bool ok = cudaMalloc(&b->d_block, b->block_bytes * kRing) == cudaSuccess &&
             cudaMallocHost(&b->h_block, b->block_bytes * kRing) == cudaSuccess &&
+            cudaMalloc(&b->d_static, b->desc_bytes) == cudaSuccess &&
             cudaMalloc(&b->d_states, sizeof(DevState) * n) == cudaSuccess &&
             cudaMallocHost(&b->h_states, sizeof(DevState) * n) == cudaSuccess &&
-            cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess;
+            cudaEventCreateWithFlags(&b->joined, cudaEventDisableTiming) == cudaSuccess;
   for (auto &e : b->ring_ev)
     ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
   for (BatchGroup &G : b->groups) {
@@ -212,17 +229,30 @@ vh_status vh_batch_create(const vh_params *params, int32_t n, vh_batch **out) {
     ok = ok && cudaMalloc(&G.d_px_start, sizeof(uint32_t) * (G.n + 1)) == cudaSuccess &&
          cudaMalloc(&G.d_prefix, sizeof(uint32_t) * (G.n + 2)) == cudaSuccess &&
          cudaStreamCreateWithFlags(&G.stream, cudaStreamNonBlocking) == cudaSuccess &&
-         cudaEventCreateWithFlags(&G.done, cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&G.last, cudaEventDisableTiming) == cudaSuccess &&
          cudaMemcpy(G.d_px_start, px.data(), sizeof(uint32_t) * (G.n + 1),
                     cudaMemcpyHostToDevice) == cudaSuccess;
+    for (auto &e : G.done) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+    // a scene's own calls run on its group's stream, in order with its steps
+    for (int k = 0; ok && k < G.n; ++k) ok = vh_set_stream(b->scenes[G.s0 + k], G.stream) == VH_OK;
   }
-  ok = ok && cudaMemset(b->d_block, 0, b->block_bytes) == cudaSuccess;
+  if (ok) {  // every scene's volume view, for the state gather
+    std::vector<SceneDesc> sd((size_t)n);
+    std::memset(sd.data(), 0, b->desc_bytes);
+    for (int i = 0; i < n; ++i) {
+      sd[i].V = handle_view(b->scenes[i]);
+      sd[i].C = handle_cam(b->scenes[i]);
+    }
+    ok = cudaMemcpy(b->d_static, sd.data(), b->desc_bytes, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemset(b->d_block, 0, b->block_bytes * kRing) == cudaSuccess;
+  }
   if (!ok) {
     cudaGetLastError();
     free_batch(b);
     return VH_ERR_CUDA;
   }
   for (auto &e : b->ring_ev) cudaEventRecord(e, b->stream);
+  for (BatchGroup &G : b->groups) cudaEventRecord(G.last, G.stream);
   *out = b;
   return VH_OK;
 }
@@ -232,6 +262,7 @@ vh_status vh_batch_destroy(vh_batch *b) {
   if (!on_device.ok()) return VH_ERR_CUDA;
   if (!b) return VH_ERR_INVALID_ARG;
   if (b->stream) cudaStreamSynchronize(b->stream);
+  for (BatchGroup &g : b->groups) cudaStreamSynchronize(g.stream);
   free_batch(b);
   return VH_OK;
 }
@@ -260,10 +291,15 @@ vh_status vh_batch_process(vh_batch *b, const void *const *depth, int32_t depth_
       if (!std::isfinite(c2w[16 * i + k]))
         return fail(b, VH_ERR_NOT_FINITE, "camera pose has a non-finite entry");
   }
-  // the upload block of this step (reused only after its copy ran)
-  unsigned char *blk = b->h_block + b->block_bytes * b->ring_pos;
-  if (cudaEventSynchronize(b->ring_ev[b->ring_pos]) != cudaSuccess)
+  // the upload block of this step (host copy reused only after its upload
+  // ran; device copy only after every group's step that read it)
+  const int k = b->ring_pos;
+  unsigned char *blk = b->h_block + b->block_bytes * k;
+  if (cudaEventSynchronize(b->ring_ev[k]) != cudaSuccess)
     return fail(b, VH_ERR_CUDA, "upload ring wait failed");
+  for (BatchGroup &g : b->groups)
+    if (g.used[k] && cudaStreamWaitEvent(b->stream, g.done[k], 0) != cudaSuccess)
+      return fail(b, VH_ERR_CUDA, "upload ring wait failed");
   SceneDesc *hd = reinterpret_cast<SceneDesc *>(blk);
   float *hp = reinterpret_cast<float *>(blk + b->desc_bytes);
   uint8_t *ha = blk + b->desc_bytes + b->pose_bytes;
@@ -276,7 +312,7 @@ vh_status vh_batch_process(vh_batch *b, const void *const *depth, int32_t depth_
     sd.C = handle_cam(h);
     sd.depth = fb.depth;
     sd.rgb = fb.rgb;
-    sd.pose = b->pose(i);
+    sd.pose = b->pose(k, i);
     sd.pix = fb.pix;
     sd.tris = fb.tris;
     sd.tri_cap = (uint32_t)std::min<int64_t>(fb.tri_cap, 0xFFFFFFFFll);
@@ -288,50 +324,63 @@ vh_status vh_batch_process(vh_batch *b, const void *const *depth, int32_t depth_
       sd.rgb = rgb[i];
       continue;
     }
-    const vh_params &p = handle_params(h);
-    const size_t npx = (size_t)p.width * p.height;
-    const size_t dbytes = npx * (depth_fmt == VH_DEPTH_U16_MM ? 2 : 4);
-    if (cudaMemcpyAsync(fb.depth, depth[i], dbytes, cudaMemcpyHostToDevice, b->stream) !=
-            cudaSuccess ||
-        cudaMemcpyAsync(fb.rgb, rgb[i], 3 * npx, cudaMemcpyHostToDevice, b->stream) != cudaSuccess)
-      return fail(b, VH_ERR_CUDA, "frame staging failed");
   }
-  if (cudaMemcpyAsync(b->d_block, blk, b->block_bytes, cudaMemcpyHostToDevice, b->stream) !=
+  if (cudaMemcpyAsync(b->block(k), blk, b->block_bytes, cudaMemcpyHostToDevice, b->stream) !=
           cudaSuccess ||
-      cudaEventRecord(b->ring_ev[b->ring_pos], b->stream) != cudaSuccess)
+      cudaEventRecord(b->ring_ev[k], b->stream) != cudaSuccess)
     return fail(b, VH_ERR_CUDA, "descriptor upload failed");
-  b->ring_pos = (b->ring_pos + 1) % kRing;
+  b->ring_pos = (k + 1) % kRing;
   const bool graphs_ok = !(handle_params(b->scenes[0]).flags & VH_FLAG_NO_GRAPH);
   int shape[3];
   batch_shape(b, shape);
   if (std::memcmp(shape, b->graph_shape, sizeof(shape)) != 0) {  // tuning changed
-    for (auto &row : b->graphs)
-      for (auto &g : row)
-        if (g) {
-          cudaGraphExecDestroy(g);
-          g = nullptr;
-        }
+    drop_step_graphs(b);
     std::memcpy(b->graph_shape, shape, sizeof(shape));
   }
-  if (graphs_ok) {
-    cudaGraphExec_t &g = b->graphs[depth_fmt][with_mesh ? 1 : 0];
-    if (!g) {
-      cudaGraph_t graph = nullptr;
-      if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
-        return fail(b, VH_ERR_CUDA, "capture failed");
-      enqueue_step(b, depth_fmt, with_mesh != 0, shape);
-      cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
-      if (e == cudaSuccess) e = cudaGraphInstantiate(&g, graph, 0);
-      if (graph) cudaGraphDestroy(graph);
-      if (e != cudaSuccess) {
-        g = nullptr;
-        return fail(b, VH_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(e));
-      }
+  for (BatchGroup &g : b->groups) {
+    // the descriptors of this step have arrived; host frames are staged on
+    // the group's stream, after its previous step has read the staging
+    if (cudaStreamWaitEvent(g.stream, b->ring_ev[k], 0) != cudaSuccess)
+      return fail(b, VH_ERR_CUDA, "step wait failed");
+    bool any = false;
+    for (int j = g.s0; j < g.s0 + g.n; ++j) {
+      if (!depth[j]) continue;
+      any = true;
+      if (mem == VH_MEM_DEVICE) continue;
+      const FrameBuffers fb = handle_frame_buffers(b->scenes[j]);
+      const vh_params &p = handle_params(b->scenes[j]);
+      const size_t npx = (size_t)p.width * p.height;
+      const size_t dbytes = npx * (depth_fmt == VH_DEPTH_U16_MM ? 2 : 4);
+      if (cudaMemcpyAsync(fb.depth, depth[j], dbytes, cudaMemcpyHostToDevice, g.stream) !=
+              cudaSuccess ||
+          cudaMemcpyAsync(fb.rgb, rgb[j], 3 * npx, cudaMemcpyHostToDevice, g.stream) != cudaSuccess)
+        return fail(b, VH_ERR_CUDA, "frame staging failed");
     }
-    if (cudaGraphLaunch(g, b->stream) != cudaSuccess) return fail(b, VH_ERR_CUDA, "graph launch");
-  } else {
-    enqueue_step(b, depth_fmt, with_mesh != 0, shape);
-    if (cudaGetLastError() != cudaSuccess) return fail(b, VH_ERR_CUDA, "batch launch failed");
+    if (!any) continue;  // no scene of this group has a frame this step
+    if (graphs_ok) {
+      cudaGraphExec_t &x = g.graphs[depth_fmt][with_mesh ? 1 : 0][k];
+      if (!x) {
+        cudaGraph_t graph = nullptr;
+        if (cudaStreamBeginCapture(g.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+          return fail(b, VH_ERR_CUDA, "capture failed");
+        enqueue_group_step(b, g, k, depth_fmt, with_mesh != 0, shape);
+        cudaError_t e = cudaStreamEndCapture(g.stream, &graph);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&x, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+          x = nullptr;
+          return fail(b, VH_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(e));
+        }
+      }
+      if (cudaGraphLaunch(x, g.stream) != cudaSuccess) return fail(b, VH_ERR_CUDA, "graph launch");
+    } else {
+      enqueue_group_step(b, g, k, depth_fmt, with_mesh != 0, shape);
+      if (cudaGetLastError() != cudaSuccess) return fail(b, VH_ERR_CUDA, "batch launch failed");
+    }
+    if (cudaEventRecord(g.done[k], g.stream) != cudaSuccess ||
+        cudaEventRecord(g.last, g.stream) != cudaSuccess)
+      return fail(b, VH_ERR_CUDA, "step record failed");
+    g.used[k] = true;
   }
   for (int i = 0; i < b->n; ++i)
     if (depth[i]) handle_note_frame(b->scenes[i]);
@@ -354,7 +403,11 @@ namespace {
 // Waits for the batch and maps every scene's sticky error bits to a status;
 // `clear` resets them afterwards.
 vh_status check_batch(vh_batch *b, vh_status *status, vh_stats *stats, bool clear) {
-  launch_batch_gather_state(b->desc(), b->n, b->d_states, b->stream);
+  for (BatchGroup &g : b->groups)  // every group's latest work, including its scenes' calls
+    if (cudaEventRecord(g.last, g.stream) != cudaSuccess ||
+        cudaStreamWaitEvent(b->stream, g.last, 0) != cudaSuccess)
+      return fail(b, VH_ERR_CUDA, "batch join failed");
+  launch_batch_gather_state(b->d_static, b->n, b->d_states, b->stream);
   if (cudaMemcpyAsync(b->h_states, b->d_states, sizeof(DevState) * b->n, cudaMemcpyDeviceToHost,
                       b->stream) != cudaSuccess ||
       cudaStreamSynchronize(b->stream) != cudaSuccess)
@@ -385,7 +438,7 @@ vh_status check_batch(vh_batch *b, vh_status *status, vh_stats *stats, bool clea
     }
   }
   if (any_error && clear) {
-    launch_batch_clear_errors(b->desc(), b->n, b->stream);
+    launch_batch_clear_errors(b->d_static, b->n, b->stream);
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return fail(b, VH_ERR_CUDA, "clear failed");
   }
   return first;
