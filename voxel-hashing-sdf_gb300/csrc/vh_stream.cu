@@ -18,7 +18,11 @@
 
 #include <algorithm>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
+#include <deque>
+#include <mutex>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -49,12 +53,62 @@ struct EvictSlot {
   uint64_t seq = 0;
 };
 
+struct StreamStore;
+void store_put(StreamStore &S, unsigned long long key, const float *blk);
+
+// A host thread moves each finished eviction into the store, so the calling
+// thread only enqueues GPU work.  mu guards the store, the queue and the
+// slots' busy flags while the thread runs.
 struct Evictor {
   cudaStream_t stream = nullptr;
   EvictSlot slot[2];
   uint64_t seq = 0;
   uint64_t evicted_since_compaction = 0;
+  int device = 0;
+  StreamStore *store = nullptr;
+  std::thread worker;
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<int> queue;  // slots whose copy is awaited, oldest first
+  bool stop = false;
+  bool failed = false;
+
+  void run() {
+    cudaSetDevice(device);
+    for (;;) {
+      int k;
+      {
+        std::unique_lock<std::mutex> lock(mu);
+        cv.wait(lock, [&] { return stop || !queue.empty(); });
+        if (queue.empty()) return;
+        k = queue.front();
+      }
+      EvictSlot &e = slot[k];
+      const cudaError_t q = cudaEventSynchronize(e.done);
+      {
+        std::lock_guard<std::mutex> lock(mu);
+        if (q == cudaSuccess) {
+          const uint32_t n = *e.h_count;
+          for (uint32_t j = 0; j < n; ++j)
+            store_put(*store, e.h_keys[j], e.h_data + (size_t)j * kBlockWords);
+          evicted_since_compaction += n;
+        } else {
+          failed = true;
+        }
+        e.busy = false;
+        queue.pop_front();
+      }
+      cv.notify_all();
+    }
+  }
+
   ~Evictor() {
+    {
+      std::lock_guard<std::mutex> lock(mu);
+      stop = true;
+    }
+    cv.notify_all();
+    if (worker.joinable()) worker.join();
     if (stream) cudaStreamSynchronize(stream);
     for (auto &e : slot) {
       cudaFree(e.d_data);
@@ -346,6 +400,8 @@ bool far_enough(unsigned long long key, float voxel, const float c[3], double r2
   return x * x + y * y + z * z > r2;
 }
 
+}  // namespace
+
 // Adds block `blk` of `key` to the host store; an older stored copy of the
 // same key is merged into it (merge_block_host) and dropped.
 void store_put(StreamStore &S, unsigned long long key, const float *blk) {
@@ -371,27 +427,22 @@ void store_put(StreamStore &S, unsigned long long key, const float *blk) {
   }
 }
 
-// Moves finished asynchronous evictions into the host store, oldest first:
-// with `wait`, every pending one (waiting for its copy); else those whose
-// copy has completed.
-vh_status evict_settle(vh_handle *h, bool wait) {
+namespace {
+
+// Waits until the eviction thread has moved every pending eviction into the
+// host store (the store is then the calling thread's until the next
+// vh_evict_async).
+vh_status evict_settle(vh_handle *h) {
   StreamStore *Sp = handle_stream_store(h);
   if (!Sp || !Sp->evict) return VH_OK;
-  StreamStore &S = *Sp;
-  Evictor &E = *S.evict;
-  for (;;) {
-    EvictSlot *o = nullptr;
-    for (auto &e : E.slot)
-      if (e.busy && (!o || e.seq < o->seq)) o = &e;
-    if (!o) return VH_OK;
-    const cudaError_t q = wait ? cudaEventSynchronize(o->done) : cudaEventQuery(o->done);
-    if (q == cudaErrorNotReady) return VH_OK;
-    if (q != cudaSuccess) return handle_fail(h, VH_ERR_CUDA, "eviction copy failed");
-    const uint32_t n = *o->h_count;
-    for (uint32_t j = 0; j < n; ++j) store_put(S, o->h_keys[j], o->h_data + (size_t)j * kBlockWords);
-    E.evicted_since_compaction += n;
-    o->busy = false;
+  Evictor &E = *Sp->evict;
+  std::unique_lock<std::mutex> lock(E.mu);
+  E.cv.wait(lock, [&] { return E.queue.empty(); });
+  if (E.failed) {
+    E.failed = false;
+    return handle_fail(h, VH_ERR_CUDA, "eviction copy failed");
   }
+  return VH_OK;
 }
 
 vh_status evictor_setup(vh_handle *h, Evictor **out) {
@@ -422,6 +473,9 @@ vh_status evictor_setup(vh_handle *h, Evictor **out) {
     delete E;
     return handle_fail(h, VH_ERR_CUDA, "asynchronous eviction: buffer allocation failed");
   }
+  E->device = handle_device(h);
+  E->store = &S;
+  E->worker = std::thread([E] { E->run(); });
   S.evict = E;
   *out = E;
   return VH_OK;
@@ -441,21 +495,30 @@ extern "C" vh_status vh_evict_async(vh_handle *h, const float *centre, float rad
   Evictor *E = nullptr;
   vh_status s = evictor_setup(h, &E);
   if (s != VH_OK) return s;
-  if ((s = evict_settle(h, false)) != VH_OK) return s;
   const VolumeView V = handle_view(h);
+  uint64_t evicted = 0;
+  {
+    std::lock_guard<std::mutex> lock(E->mu);
+    evicted = E->evicted_since_compaction;
+  }
   // erased slots stay tombstones: rebuild the table (synchronously, rare)
   // once the evictions since the last rebuild could fill an eighth of it
-  if (E->evicted_since_compaction + handle_state(h).tombstones > (V.slot_mask + 1u) / 8u) {
-    if ((s = evict_settle(h, true)) != VH_OK || (s = vh_compact_table(h)) != VH_OK) return s;
+  if (evicted + handle_state(h).tombstones > (V.slot_mask + 1u) / 8u) {
+    if ((s = evict_settle(h)) != VH_OK || (s = vh_compact_table(h)) != VH_OK) return s;
+    std::lock_guard<std::mutex> lock(E->mu);
     E->evicted_since_compaction = 0;
   }
-  EvictSlot *slot = !E->slot[0].busy ? &E->slot[0] : (!E->slot[1].busy ? &E->slot[1] : nullptr);
-  if (!slot) {  // both in flight: finish the older one
-    EvictSlot *o = E->slot[0].seq < E->slot[1].seq ? &E->slot[0] : &E->slot[1];
-    if (cudaEventSynchronize(o->done) != cudaSuccess)
+  EvictSlot *slot = nullptr;
+  int k = 0;
+  {  // a free slot (both in flight: wait for the older one to be stored)
+    std::unique_lock<std::mutex> lock(E->mu);
+    E->cv.wait(lock, [&] { return !E->slot[0].busy || !E->slot[1].busy; });
+    k = E->slot[0].busy ? 1 : 0;
+    slot = &E->slot[k];
+    if (E->failed) {
+      E->failed = false;
       return handle_fail(h, VH_ERR_CUDA, "eviction copy failed");
-    if ((s = evict_settle(h, false)) != VH_OK) return s;
-    slot = o;
+    }
   }
   const CamParams C = handle_cam(h);
   const cudaStream_t st = handle_stream(h);
@@ -476,14 +539,19 @@ extern "C" vh_status vh_evict_async(vh_handle *h, const float *centre, float rad
                                           slot->h_data_dev, slot->h_keys_dev, slot->h_count_dev);
   if (cudaGetLastError() != cudaSuccess || cudaEventRecord(slot->done, E->stream) != cudaSuccess)
     return handle_fail(h, VH_ERR_CUDA, "eviction copy failed");
-  slot->busy = true;
-  slot->seq = ++E->seq;
+  {
+    std::lock_guard<std::mutex> lock(E->mu);
+    slot->busy = true;
+    slot->seq = ++E->seq;
+    E->queue.push_back(k);
+  }
+  E->cv.notify_all();
   handle_invalidate_nb(h);
   return VH_OK;
 }
 
 namespace vh {
-vh_status stream_store_settle(vh_handle *h) { return evict_settle(h, true); }
+vh_status stream_store_settle(vh_handle *h) { return evict_settle(h); }
 }  // namespace vh
 
 extern "C" vh_status vh_compact_table(vh_handle *h) {
@@ -513,7 +581,7 @@ extern "C" vh_status vh_stream_out(vh_handle *h, const float *centre, float radi
   if (!h || !centre || !(radius >= 0.0f)) return VH_ERR_INVALID_ARG;
   for (int a = 0; a < 3; ++a)
     if (!std::isfinite(centre[a])) return VH_ERR_NOT_FINITE;
-  vh_status es = evict_settle(h, true);  // keeps the order of earlier evictions
+  vh_status es = evict_settle(h);  // keeps the order of earlier evictions
   if (es != VH_OK) return es;
   const VolumeView V = handle_view(h);
   const CamParams C = handle_cam(h);
@@ -598,7 +666,7 @@ extern "C" vh_status vh_stream_in(vh_handle *h, const float *centre, float radiu
   if (!h || !centre || !(radius >= 0.0f)) return VH_ERR_INVALID_ARG;
   for (int a = 0; a < 3; ++a)
     if (!std::isfinite(centre[a])) return VH_ERR_NOT_FINITE;
-  vh_status es = evict_settle(h, true);  // pending evictions reach the store first
+  vh_status es = evict_settle(h);  // pending evictions reach the store first
   if (es != VH_OK) return es;
   StreamStore *Sp = handle_stream_store(h);
   if (!Sp || Sp->index.empty()) return VH_OK;
@@ -674,9 +742,10 @@ extern "C" vh_status vh_stream_in(vh_handle *h, const float *centre, float radiu
 
 extern "C" int64_t vh_host_blocks(const vh_handle *h) {
   if (!h) return 0;
-  {  // finished evictions count; pending ones are not waited for
-    DeviceScope on_device(handle_device(h));
-    evict_settle(const_cast<vh_handle *>(h), false);
+  StreamStore *Sp = handle_stream_store(const_cast<vh_handle *>(h));
+  if (Sp && Sp->evict) {  // finished evictions count; pending ones are not waited for
+    std::lock_guard<std::mutex> lock(Sp->evict->mu);
+    return (int64_t)Sp->index.size();
   }
   StreamStore *s = handle_stream_store(const_cast<vh_handle *>(h));
   return s ? (int64_t)s->index.size() : 0;
