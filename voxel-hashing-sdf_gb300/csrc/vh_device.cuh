@@ -101,4 +101,20 @@ __device__ __forceinline__ Sample sample_tsdf(const VolumeView &V, float inv_vox
   return s;
 }
 
+// Closes the open allocation epoch (one thread): the tickets handed out
+// since the last close become blocks taken from the free list first, then
+// from the bump pointer (capped at the pool's capacity).
+__device__ __forceinline__ void reconcile_epoch(const VolumeView &V) {
+  DevState *st = V.st;
+  const uint32_t t = st->ticket;
+  if (!t) return;
+  const uint32_t from_free = min(t, st->free_count);
+  st->free_count -= from_free;
+  const unsigned long long top = (unsigned long long)st->pool_top + (t - from_free);
+  const uint32_t new_top = (uint32_t)min(top, (unsigned long long)V.pool_cap);
+  st->new_blocks += from_free + (new_top - st->pool_top);
+  st->pool_top = new_top;
+  st->ticket = 0;
+}
+
 }  // namespace vh

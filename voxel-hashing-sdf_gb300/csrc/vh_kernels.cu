@@ -998,18 +998,7 @@ __global__ void __launch_bounds__(kMcThreads, kMinCtas) k_mc(VolumeView V, int s
 }
 
 // ---- small state kernels --------------------------------------------------------
-__device__ void reconcile(const VolumeView &V) {
-  DevState *st = V.st;
-  const uint32_t t = st->ticket;
-  if (!t) return;
-  const uint32_t from_free = min(t, st->free_count);
-  st->free_count -= from_free;
-  const unsigned long long top = (unsigned long long)st->pool_top + (t - from_free);
-  const uint32_t new_top = (uint32_t)min(top, (unsigned long long)V.pool_cap);
-  st->new_blocks += from_free + (new_top - st->pool_top);
-  st->pool_top = new_top;
-  st->ticket = 0;
-}
+__device__ __forceinline__ void reconcile(const VolumeView &V) { reconcile_epoch(V); }
 
 __device__ void frame_begin_state(const VolumeView &V) {
   reconcile(V);

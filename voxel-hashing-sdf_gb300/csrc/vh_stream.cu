@@ -55,6 +55,7 @@ struct EvictSlot {
 
 struct StreamStore;
 void store_put(StreamStore &S, unsigned long long key, const float *blk);
+void store_reserve(StreamStore &S, size_t more);
 
 // A host thread moves each finished eviction into the store, so the calling
 // thread only enqueues GPU work.  mu guards the store, the queue and the
@@ -89,6 +90,7 @@ struct Evictor {
         std::lock_guard<std::mutex> lock(mu);
         if (q == cudaSuccess) {
           const uint32_t n = *e.h_count;
+          store_reserve(*store, n);
           for (uint32_t j = 0; j < n; ++j)
             store_put(*store, e.h_keys[j], e.h_data + (size_t)j * kBlockWords);
           evicted_since_compaction += n;
@@ -287,6 +289,14 @@ __global__ void __launch_bounds__(128) k_evict(VolumeView V, const unsigned long
   }
 }
 
+// Opens an eviction: the allocation epoch closed (as k_epoch_end) and the
+// selection counter cleared.
+__global__ void k_evict_begin(VolumeView V, uint32_t *__restrict__ count) {
+  if (threadIdx.x != 0) return;
+  reconcile_epoch(V);
+  *count = 0u;
+}
+
 // The evicted blocks and their keys from device staging into mapped host
 // memory (on the evictor's stream, beside later frames); count last.
 __global__ void __launch_bounds__(256) k_evict_copy(const float *__restrict__ data,
@@ -404,6 +414,18 @@ bool far_enough(unsigned long long key, float voxel, const float c[3], double r2
 
 // Adds block `blk` of `key` to the host store; an older stored copy of the
 // same key is merged into it (merge_block_host) and dropped.
+// Room for `more` new entries, so that a batch of insertions reallocates
+// at most once (geometric growth).
+void store_reserve(StreamStore &S, size_t more) {
+  const size_t want = S.keys.size() + more;
+  if (want > S.keys.capacity()) {
+    const size_t cap = std::max(want, 2 * S.keys.capacity());
+    S.keys.reserve(cap);
+    S.data.reserve(cap * kBlockWords);
+  }
+  S.index.reserve(S.index.size() + more);
+}
+
 void store_put(StreamStore &S, unsigned long long key, const float *blk) {
   size_t e;
   if (!S.free_entries.empty()) {
@@ -466,7 +488,8 @@ vh_status evictor_setup(vh_handle *h, Evictor **out) {
          cudaHostGetDevicePointer(&e.h_data_dev, e.h_data, 0) == cudaSuccess &&
          cudaHostGetDevicePointer(&e.h_keys_dev, e.h_keys, 0) == cudaSuccess &&
          cudaHostGetDevicePointer(&e.h_count_dev, e.h_count, 0) == cudaSuccess &&
-         cudaEventCreateWithFlags(&e.done, cudaEventDisableTiming) == cudaSuccess;
+         cudaEventCreateWithFlags(&e.done, cudaEventDisableTiming | cudaEventBlockingSync) ==
+             cudaSuccess;
   }
   if (!ok) {
     cudaGetLastError();
@@ -523,9 +546,8 @@ extern "C" vh_status vh_evict_async(vh_handle *h, const float *centre, float rad
   const CamParams C = handle_cam(h);
   const cudaStream_t st = handle_stream(h);
   const float r2 = radius * radius;
-  launch_epoch_end(V, st);  // allocation tickets settled before blocks are freed
-  if (cudaMemsetAsync(slot->d_count, 0, sizeof(uint32_t), st) != cudaSuccess)
-    return handle_fail(h, VH_ERR_CUDA, "eviction failed");
+  // allocation tickets settled before blocks are freed; selection count 0
+  k_evict_begin<<<1, 32, 0, st>>>(V, slot->d_count);
   k_select_far<<<std::min<uint32_t>((V.pool_cap + 255) / 256, 4096), 256, 0, st>>>(
       V, C.voxel, centre[0], centre[1], centre[2], std::isfinite(r2) ? r2 : 3.0e38f, slot->d_count,
       slot->d_keys, slot->d_ids, kEvictCap);
