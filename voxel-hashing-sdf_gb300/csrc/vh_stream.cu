@@ -56,6 +56,7 @@ struct EvictSlot {
 struct StreamStore;
 void store_put(StreamStore &S, unsigned long long key, const float *blk);
 void store_reserve(StreamStore &S, size_t more);
+int64_t store_size(const StreamStore &S);
 
 // A host thread moves each finished eviction into the store, so the calling
 // thread only enqueues GPU work.  mu guards the store, the queue and the
@@ -73,6 +74,7 @@ struct Evictor {
   std::deque<int> queue;  // slots whose copy is awaited, oldest first
   bool stop = false;
   bool failed = false;
+  int64_t stored = 0;  // blocks in the store after the last finished eviction
 
   void run() {
     cudaSetDevice(device);
@@ -86,17 +88,21 @@ struct Evictor {
       }
       EvictSlot &e = slot[k];
       const cudaError_t q = cudaEventSynchronize(e.done);
+      // the store is this thread's while the queue is not empty (the API
+      // calls that use it wait for an empty queue first), so it is filled
+      // without holding mu and vh_evict_async never waits for it
+      uint32_t n = 0;
+      if (q == cudaSuccess) {
+        n = *e.h_count;
+        store_reserve(*store, n);
+        for (uint32_t j = 0; j < n; ++j)
+          store_put(*store, e.h_keys[j], e.h_data + (size_t)j * kBlockWords);
+      }
       {
         std::lock_guard<std::mutex> lock(mu);
-        if (q == cudaSuccess) {
-          const uint32_t n = *e.h_count;
-          store_reserve(*store, n);
-          for (uint32_t j = 0; j < n; ++j)
-            store_put(*store, e.h_keys[j], e.h_data + (size_t)j * kBlockWords);
-          evicted_since_compaction += n;
-        } else {
-          failed = true;
-        }
+        if (q != cudaSuccess) failed = true;
+        evicted_since_compaction += n;
+        stored = store_size(*store);
         e.busy = false;
         queue.pop_front();
       }
@@ -414,6 +420,8 @@ bool far_enough(unsigned long long key, float voxel, const float c[3], double r2
 
 // Adds block `blk` of `key` to the host store; an older stored copy of the
 // same key is merged into it (merge_block_host) and dropped.
+int64_t store_size(const StreamStore &S) { return (int64_t)S.index.size(); }
+
 // Room for `more` new entries, so that a batch of insertions reallocates
 // at most once (geometric growth).
 void store_reserve(StreamStore &S, size_t more) {
@@ -767,7 +775,7 @@ extern "C" int64_t vh_host_blocks(const vh_handle *h) {
   StreamStore *Sp = handle_stream_store(const_cast<vh_handle *>(h));
   if (Sp && Sp->evict) {  // finished evictions count; pending ones are not waited for
     std::lock_guard<std::mutex> lock(Sp->evict->mu);
-    return (int64_t)Sp->index.size();
+    return Sp->evict->queue.empty() ? (int64_t)Sp->index.size() : Sp->evict->stored;
   }
   StreamStore *s = handle_stream_store(const_cast<vh_handle *>(h));
   return s ? (int64_t)s->index.size() : 0;
