@@ -542,7 +542,7 @@ def hbm_stress_leg(num_frames, local, keyframes=16, iterations=20):
     return out
 
 
-def eviction_leg(params, tuning, stream, seed, num=50, every=10):
+def eviction_leg(params, tuning, stream, seed, num=60, every=3):
     """Out-of-core streaming beside the frames: every `every`-th frame of the
     long stream (the camera crosses the room), device-resident, back to back
     - plainly, with vh_evict_async after every frame (blocks farther than
