@@ -542,17 +542,20 @@ def hbm_stress_leg(num_frames, local, keyframes=16, iterations=20):
     return out
 
 
-def eviction_leg(params, tuning, stream, seed, num=60, every=3):
+def eviction_leg(params, tuning, stream, num=80, every=20):
     """Out-of-core streaming beside the frames: every `every`-th frame of the
-    long stream (the camera crosses the room), device-resident, back to back
-    - plainly, with vh_evict_async after every frame (blocks farther than
-    the frame's reach from the camera leave HBM for the host store while the
-    next frames run), and with the synchronous vh_stream_out at the same
-    radius.  Wall clock from the first submission to vh_sync (which waits
-    for the last eviction's copy)."""
+    walk through the 20x20 m floor of 4x4 rooms (640x480; the camera covers
+    ~27 m), device-resident, back to back - plainly, with vh_evict_async
+    after every frame (blocks farther than the frame's reach from the camera
+    leave HBM for the host store while the next frames run), and with the
+    synchronous vh_stream_out at the same radius.  Volume parameters as the
+    long stream's (5 mm, 20 mm, 2^22 slots).  Wall clock from the first
+    submission to vh_sync (which waits for the last eviction's copy)."""
     import torch
     from vhsdf import Volume, synth
-    sc = synth.Scene(kind=2, seed=seed, num_frames=num * every)
+    sc = synth.Scene(kind=4, seed=5, num_frames=num * every, width=params["width"],
+                     height=params["height"])
+    params = dict(params, fx=sc.fx, fy=sc.fy, cx=sc.cx, cy=sc.cy)
     dev = []
     for f in range(0, num * every, every):
         d, c, p = sc.render(f)
@@ -585,7 +588,8 @@ def eviction_leg(params, tuning, stream, seed, num=60, every=3):
                      "host_blocks": vol.host_blocks()}
         vol.close()
     out["radius_m"] = radius
-    out["frames"] = f"{len(dev)} (every {every}th of the long stream)"
+    out["frames"] = f"{len(dev)} (every {every}th of a {num * every}-frame walk through the rooms)"
+    out["evicted_blocks_per_frame"] = out["async"]["host_blocks"] / len(dev)
     out["async_vs_off"] = out["async"]["frames_per_s"] / out["off"]["frames_per_s"]
     out["async_vs_sync"] = out["async"]["frames_per_s"] / out["sync"]["frames_per_s"]
     return out
@@ -781,7 +785,7 @@ def run_engine(args):
         e2e_dev_s = time.perf_counter() - t0
     vol.close()
 
-    eviction = eviction_leg(params, tuning, stream, seed) if rank == 0 else None
+    eviction = eviction_leg(params, tuning, stream) if rank == 0 else None
     dev_ms, e2e_s, e2e_sync_s, e2e_dev_s = replicas.reduce_max(
         [dev_ms, e2e_s, e2e_sync_s, e2e_dev_s], device="cuda")
     if rank != 0:
