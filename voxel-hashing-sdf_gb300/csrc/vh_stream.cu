@@ -22,7 +22,11 @@
 #include <cstring>
 #include <deque>
 #include <mutex>
+#include <new>
 #include <thread>
+
+#include <stdlib.h>
+#include <sys/mman.h>
 #include <unordered_map>
 #include <vector>
 
@@ -92,15 +96,20 @@ struct Evictor {
       // calls that use it wait for an empty queue first), so it is filled
       // without holding mu and vh_evict_async never waits for it
       uint32_t n = 0;
-      if (q == cudaSuccess) {
+      bool stored_ok = q == cudaSuccess;
+      if (stored_ok) {
         n = *e.h_count;
-        store_reserve(*store, n);
-        for (uint32_t j = 0; j < n; ++j)
-          store_put(*store, e.h_keys[j], e.h_data + (size_t)j * kBlockWords);
+        try {
+          store_reserve(*store, n);
+          for (uint32_t j = 0; j < n; ++j)
+            store_put(*store, e.h_keys[j], e.h_data + (size_t)j * kBlockWords);
+        } catch (const std::bad_alloc &) {
+          stored_ok = false;
+        }
       }
       {
         std::lock_guard<std::mutex> lock(mu);
-        if (q != cudaSuccess) failed = true;
+        if (!stored_ok) failed = true;
         evicted_since_compaction += n;
         stored = store_size(*store);
         e.busy = false;
@@ -132,10 +141,46 @@ struct Evictor {
   }
 };
 
+// Host memory of the stored blocks: chunks of kChunkBlocks blocks, allocated
+// without zero fill (on huge pages where the OS grants them) and faulted in
+// when a chunk is added, so filing a block later costs one memcpy.
+class BlockArena {
+ public:
+  static constexpr size_t kChunkBlocks = 8192;  // 48 MiB per chunk
+  BlockArena() = default;
+  BlockArena(const BlockArena &) = delete;
+  BlockArena &operator=(const BlockArena &) = delete;
+  ~BlockArena() {
+    for (void *c : chunks_) std::free(c);
+  }
+  float *block(size_t e) const {
+    return static_cast<float *>(chunks_[e / kChunkBlocks]) + (e % kChunkBlocks) * kBlockWords;
+  }
+  // entries [0, n) addressable
+  bool reserve(size_t n) {
+    while (chunks_.size() * kChunkBlocks < n)
+      if (!add_chunk()) return false;
+    return true;
+  }
+  void swap(BlockArena &o) { chunks_.swap(o.chunks_); }
+
+ private:
+  bool add_chunk() {
+    const size_t bytes = kChunkBlocks * kBlockWords * sizeof(float);
+    void *p = nullptr;
+    if (posix_memalign(&p, (size_t)1 << 21, bytes) != 0) return false;
+    madvise(p, bytes, MADV_HUGEPAGE);  // a hint: fewer page faults if granted
+    for (size_t o = 0; o < bytes; o += 4096) static_cast<volatile char *>(p)[o] = 0;
+    chunks_.push_back(p);
+    return true;
+  }
+  std::vector<void *> chunks_;
+};
+
 struct StreamStore {
   std::unordered_map<unsigned long long, size_t> index;  // key -> entry
   std::vector<unsigned long long> keys;                   // per entry (kEmptyKey: free)
-  std::vector<float> data;                                // kBlockWords per entry
+  BlockArena arena;                                       // kBlockWords per entry
   std::vector<size_t> free_entries;
   Evictor *evict = nullptr;                               // created on first use
   ~StreamStore() { delete evict; }
@@ -426,11 +471,8 @@ int64_t store_size(const StreamStore &S) { return (int64_t)S.index.size(); }
 // at most once (geometric growth).
 void store_reserve(StreamStore &S, size_t more) {
   const size_t want = S.keys.size() + more;
-  if (want > S.keys.capacity()) {
-    const size_t cap = std::max(want, 2 * S.keys.capacity());
-    S.keys.reserve(cap);
-    S.data.reserve(cap * kBlockWords);
-  }
+  if (want > S.keys.capacity()) S.keys.reserve(std::max(want, 2 * S.keys.capacity()));
+  S.arena.reserve(want);
   S.index.reserve(S.index.size() + more);
 }
 
@@ -441,14 +483,14 @@ void store_put(StreamStore &S, unsigned long long key, const float *blk) {
     S.free_entries.pop_back();
   } else {
     e = S.keys.size();
+    if (!S.arena.reserve(e + 1)) throw std::bad_alloc();
     S.keys.push_back(kEmptyKey);
-    S.data.resize(S.data.size() + kBlockWords);
   }
-  std::memcpy(&S.data[e * kBlockWords], blk, sizeof(float) * kBlockWords);
+  std::memcpy(S.arena.block(e), blk, sizeof(float) * kBlockWords);
   S.keys[e] = key;
   auto it = S.index.find(key);
   if (it != S.index.end()) {
-    merge_block_host(&S.data[e * kBlockWords], &S.data[it->second * kBlockWords]);
+    merge_block_host(S.arena.block(e), S.arena.block(it->second));
     S.keys[it->second] = kEmptyKey;
     S.free_entries.push_back(it->second);
     it->second = e;
@@ -648,33 +690,23 @@ extern "C" vh_status vh_stream_out(vh_handle *h, const float *centre, float radi
   if (cudaMemcpyAsync(keys.data(), d_keys, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost,
                       st) != cudaSuccess)
     return handle_fail(h, VH_ERR_CUDA, "stream out: key copy failed");
+  std::vector<float> buf;
   for (uint32_t c0 = 0; c0 < n; c0 += kChunk) {
     const uint32_t cnt = std::min(kChunk, n - c0);
     k_gather_blocks<<<cnt, 128, 0, st>>>(V.pool, d_ids + c0, cnt, d_data);
-    const size_t base = S.data.size();
-    // the host entries of this chunk go contiguously at the end
-    S.data.resize(base + (size_t)cnt * kBlockWords);
-    S.keys.resize(S.data.size() / kBlockWords, kEmptyKey);
+    buf.resize((size_t)cnt * kBlockWords);
     if (cudaGetLastError() != cudaSuccess ||
-        cudaMemcpyAsync(S.data.data() + base, d_data, sizeof(float) * kBlockWords * cnt,
+        cudaMemcpyAsync(buf.data(), d_data, sizeof(float) * kBlockWords * cnt,
                         cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
       return handle_fail(h, VH_ERR_CUDA, "stream out: block copy failed");
-    for (uint32_t j = 0; j < cnt; ++j) {
-      const unsigned long long k = keys[c0 + j];
-      const size_t e = base / kBlockWords + j;
-      S.keys[e] = k;
-      auto it = S.index.find(k);
-      if (it != S.index.end()) {
-        // an older copy of the same key (moved out before a frame re-created
-        // the block): merge it into the outgoing one, then drop it
-        merge_block_host(&S.data[e * kBlockWords], &S.data[it->second * kBlockWords]);
-        S.keys[it->second] = kEmptyKey;
-        S.free_entries.push_back(it->second);
-        it->second = e;
-      } else {
-        S.index.emplace(k, e);
-      }
+    // an older stored copy of a key (moved out before a frame re-created the
+    // block) is merged into the outgoing one and dropped
+    try {
+      store_reserve(S, cnt);
+      for (uint32_t j = 0; j < cnt; ++j) store_put(S, keys[c0 + j], &buf[(size_t)j * kBlockWords]);
+    } catch (const std::bad_alloc &) {
+      return handle_fail(h, VH_ERR_CUDA, "stream out: host store allocation failed");
     }
   }
   k_keys_to_xyz<<<(n + 255) / 256, 256, 0, st>>>(d_keys, n, d_xyz);
@@ -731,7 +763,7 @@ extern "C" vh_status vh_stream_in(vh_handle *h, const float *centre, float radiu
       xyz[3 * j] = x;
       xyz[3 * j + 1] = y;
       xyz[3 * j + 2] = z;
-      std::memcpy(&buf[(size_t)j * kBlockWords], &S.data[e * kBlockWords], sizeof(float) * kBlockWords);
+      std::memcpy(&buf[(size_t)j * kBlockWords], S.arena.block(e), sizeof(float) * kBlockWords);
     }
     if (cudaMemcpyAsync(d_xyz, xyz.data(), sizeof(int32_t) * 3 * cnt, cudaMemcpyHostToDevice, st) !=
             cudaSuccess ||
@@ -756,15 +788,17 @@ extern "C" vh_status vh_stream_in(vh_handle *h, const float *centre, float radiu
   }
   // compact the store when most of it is free
   if (S.free_entries.size() > 1024 && S.free_entries.size() * 2 > S.keys.size()) {
-    StreamStore T;
-    for (const auto &kv : S.index) {
-      const size_t e = T.keys.size();
-      T.keys.push_back(kv.first);
-      T.data.insert(T.data.end(), S.data.begin() + kv.second * kBlockWords,
-                    S.data.begin() + (kv.second + 1) * kBlockWords);
-      T.index.emplace(kv.first, e);
+    StreamStore T;  // the live entries, packed (the evictor stays with S)
+    try {
+      store_reserve(T, S.index.size());
+      for (const auto &kv : S.index) store_put(T, kv.first, S.arena.block(kv.second));
+    } catch (const std::bad_alloc &) {
+      return handle_fail(h, VH_ERR_CUDA, "stream in: host store allocation failed");
     }
-    S = std::move(T);
+    S.index.swap(T.index);
+    S.keys.swap(T.keys);
+    S.free_entries.swap(T.free_entries);
+    S.arena.swap(T.arena);
   }
   if (moved) *moved = done;
   return VH_OK;
