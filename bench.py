@@ -555,7 +555,8 @@ def eviction_leg(params, tuning, stream, num=80, every=20):
     from vhsdf import Volume, synth
     sc = synth.Scene(kind=4, seed=5, num_frames=num * every, width=params["width"],
                      height=params["height"])
-    params = dict(params, fx=sc.fx, fy=sc.fy, cx=sc.cx, cy=sc.cy)
+    params = dict(params, fx=sc.fx, fy=sc.fy, cx=sc.cx, cy=sc.cy,
+                  pool_blocks=ENGINE_PARAMS["pool_blocks"])  # the walk needs ~300k blocks
     dev = []
     for f in range(0, num * every, every):
         d, c, p = sc.render(f)
@@ -785,7 +786,8 @@ def run_engine(args):
         e2e_dev_s = time.perf_counter() - t0
     vol.close()
 
-    eviction = eviction_leg(params, tuning, stream) if rank == 0 else None
+    eviction = (eviction_leg(params, tuning, stream, num=args.eviction_frames)
+                if rank == 0 and args.eviction_frames > 0 else None)
     dev_ms, e2e_s, e2e_sync_s, e2e_dev_s = replicas.reduce_max(
         [dev_ms, e2e_s, e2e_sync_s, e2e_dev_s], device="cuda")
     if rank != 0:
@@ -896,6 +898,8 @@ def main():
                     help="Gauss-Newton steps per pose in the pose-refinement leg")
     ap.add_argument("--batch-scenes", type=int, default=64,
                     help="scenes in the batched-scenes leg (0 = skip)")
+    ap.add_argument("--eviction-frames", type=int, default=80,
+                    help="frames of the out-of-core leg (0 = skip)")
     ap.add_argument("--batch-steps", type=int, default=12,
                     help="frames per scene in the batched-scenes leg")
     ap.add_argument("--only-batched", action="store_true",
