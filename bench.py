@@ -483,7 +483,9 @@ def batched_leg(num_scenes, steps, local, small=False):
                                         "speedup": t_seq_py / t_batch_py},
             "counts_equal_per_scene": same,
             "voxel_updates_per_s": sum(b["voxels_updated"] for b in bstats) / t_batch,
-            "launches_per_step": {"batched": 5, "per_scene_graphs": 5 * num_scenes}}
+            "launches_per_step": {
+                "batched": 4 * min(16, num_scenes),  # frame_begin, allocate, resolve, integrate per group
+                "per_scene_graphs": sum(int(q["frame_kernels"]) for q in sstats)}}
 
 
 def hbm_stress_leg(num_frames, local, keyframes=16, iterations=20):
@@ -755,7 +757,12 @@ def run_engine(args):
 
     # ---- launch tuning (scratch volume, outside any timed region) ----
     tuner = Volume(**params)
-    tuning = tuner.tuning() if args.no_autotune else tuner.autotune(*frames[0])
+    if args.tuning:
+        iv, ic, mcs, mv = (int(x) for x in args.tuning.split(","))
+        tuner.set_tuning(iv, ic, mcs, mv)
+        tuning = tuner.tuning()
+    else:
+        tuning = tuner.tuning() if args.no_autotune else tuner.autotune(*frames[0])
     tuner.close()
 
     # ---- device-resident pass (value + roofline) ----
@@ -959,6 +966,9 @@ def main():
                     help="run only the pose-refinement leg and print its JSON (profiling)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="use the default launch configuration (for profiling runs)")
+    ap.add_argument("--tuning", default="",
+                    help="explicit launch configuration integrate_variant,integrate_ctas_per_sm,"
+                         "mc_ctas_per_sm,mc_variant (0 = occupancy maximum; no autotuning)")
     ap.add_argument("--pool-blocks", type=int, default=0,
                     help="smaller block pool (for short profiling runs)")
     args = ap.parse_args()

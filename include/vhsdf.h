@@ -127,9 +127,12 @@ typedef struct vh_mesh_view {
 /* Launch configuration of the per-frame kernels.  Every configuration
  * computes identical results; only the speed differs. */
 typedef struct vh_tuning {
-  int32_t integrate_variant;     /* 0: one block in flight per CTA, register */
-                                 /*    budget for 12 CTAs per SM,            */
-                                 /* 1: next block's voxels prefetched        */
+  int32_t integrate_variant;     /* voxels per thread x threads per CTA,     */
+                                 /* register budget (CTAs per SM):           */
+                                 /* 0: 4 x 128, 12   1: 4 x 128, next block  */
+                                 /*    prefetched, 8   2: 8 x 64, 16         */
+                                 /* 3: 2 x 256, 6   4: 4 x 128, 10           */
+                                 /* 5: 8 x 64, 12                            */
   int32_t integrate_ctas_per_sm; /* resident CTAs per SM (0 = occupancy max) */
   int32_t mc_ctas_per_sm;        /* resident CTAs per SM (0 = occupancy max) */
   int32_t mc_variant;            /* 0: register budget for 10 CTAs per SM,   */
@@ -309,6 +312,9 @@ vh_status vh_get_stats(vh_handle *h, vh_stats *out);
 
 vh_status vh_get_tuning(vh_handle *h, vh_tuning *out);
 vh_status vh_set_tuning(vh_handle *h, const vh_tuning *t);
+/* Number of launch shapes: integrate_variant takes 0 .. *integrate - 1 and
+ * mc_variant 0 .. *mc - 1 (either pointer may be NULL).  Host only. */
+void vh_tuning_variants(int32_t *integrate, int32_t *mc);
 /* Times every candidate configuration on one frame in a scratch volume with
  * the handle's parameters (the handle's volume is not touched), applies the
  * fastest and returns it in `chosen` (may be NULL).  Results are cached per

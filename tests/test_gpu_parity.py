@@ -11,6 +11,7 @@ import torch
 
 from helpers import (assert_same_blocks, key_set, oracle_for, small_scene, sort_rows,
                      sorted_blocks, tri_rows, volume_for)
+from vhsdf import Volume
 
 pytestmark = pytest.mark.gpu
 
@@ -209,10 +210,13 @@ def test_frame_scope_mc_after_list_change_without_integration(scene):
 
 
 def test_every_launch_configuration_is_bit_exact(scene):
-    """The tuner only changes speed: each configuration reproduces the oracle."""
+    """The tuner only changes speed: each configuration (every integration
+    shape and every MC shape, some with reduced grids) reproduces the oracle."""
     orc = None
     results = []
-    configs = [(0, 0, 0, 0), (1, 0, 0, 1), (0, 2, 3, 1), (1, 1, 1, 0)]
+    ni, nm = Volume.tuning_variants()
+    assert ni >= 6 and nm >= 3
+    configs = [(iv, 0, 0, iv % nm) for iv in range(ni)] + [(0, 2, 3, 1), (1, 1, 1, 0), (3, 1, 2, 2)]
     for cfg in configs:
         vol = volume_for(scene)
         vol.set_tuning(*cfg)
@@ -237,7 +241,8 @@ def test_autotune_picks_a_valid_configuration(scene, tmp_path, monkeypatch):
     vol = volume_for(scene)
     d, c, p = scene.render(0)
     t = vol.autotune(d, c, p)
-    assert t["integrate_variant"] in (0, 1) and t["mc_variant"] in (0, 1)
+    ni, nm = Volume.tuning_variants()
+    assert 0 <= t["integrate_variant"] < ni and 0 <= t["mc_variant"] < nm
     assert t["integrate_ctas_per_sm"] >= 1 and t["mc_ctas_per_sm"] >= 1
     assert vol.stats()["blocks_allocated"] == 0  # the handle's volume is untouched
     assert vol.tuning() == t
@@ -246,7 +251,7 @@ def test_autotune_picks_a_valid_configuration(scene, tmp_path, monkeypatch):
     assert vol2.autotune(d, c, p) == t  # served from the cache
 
 
-@pytest.mark.parametrize("mc_variant", [0, 1])
+@pytest.mark.parametrize("mc_variant", [0, 1, 2])
 def test_frame_meshes_of_each_mc_variant(scene, mc_variant):
     """Per-frame marching cubes of each kernel variant equals the oracle's."""
     vol = volume_for(scene)
@@ -275,7 +280,7 @@ def test_mc_on_dense_sign_changes(scene):
     w = np.ones((m, 512), np.float32)
     rgb = rng.integers(0, 256, (m, 512, 3)).astype(np.uint8)
     want = None
-    for variant in (0, 1):
+    for variant in range(Volume.tuning_variants()[1]):
         vol = volume_for(scene)
         vol.set_tuning(0, 0, 0, variant)
         vol.import_blocks(xyz, sdf, w, rgb)

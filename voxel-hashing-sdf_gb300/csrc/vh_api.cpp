@@ -281,8 +281,9 @@ void drop_graphs(vh_handle *h) {
 // Resolves a requested configuration against the occupancy limits.
 void apply_tuning(vh_handle *h, const vh_tuning &t) {
   h->tuning = t;
-  h->tuning.integrate_variant = t.integrate_variant == 1 ? 1 : 0;
-  h->tuning.mc_variant = t.mc_variant == 1 ? 1 : 0;
+  h->tuning.integrate_variant =
+      t.integrate_variant > 0 && t.integrate_variant < integrate_variants() ? t.integrate_variant : 0;
+  h->tuning.mc_variant = t.mc_variant > 0 && t.mc_variant < mc_variants() ? t.mc_variant : 0;
   const int imax = integrate_ctas_per_sm(h->tuning.integrate_variant);
   const int mmax = mc_ctas_per_sm(h->tuning.mc_variant);
   h->integrate_per_sm =
@@ -1291,6 +1292,11 @@ vh_status vh_get_stats(vh_handle *h, vh_stats *out) {
   return s;
 }
 
+void vh_tuning_variants(int32_t *integrate, int32_t *mc) {
+  if (integrate) *integrate = integrate_variants();
+  if (mc) *mc = mc_variants();
+}
+
 vh_status vh_get_tuning(vh_handle *h, vh_tuning *out) {
   if (!h || !out) return VH_ERR_INVALID_ARG;
   *out = h->tuning;
@@ -1299,8 +1305,9 @@ vh_status vh_get_tuning(vh_handle *h, vh_tuning *out) {
 
 vh_status vh_set_tuning(vh_handle *h, const vh_tuning *t) {
   VH_HANDLE_DEVICE(h);
-  if (!h || !t || t->integrate_variant < 0 || t->integrate_variant > 1 || t->mc_variant < 0 ||
-      t->mc_variant > 1 || t->integrate_ctas_per_sm < 0 || t->mc_ctas_per_sm < 0)
+  if (!h || !t || t->integrate_variant < 0 || t->integrate_variant >= integrate_variants() ||
+      t->mc_variant < 0 || t->mc_variant >= mc_variants() || t->integrate_ctas_per_sm < 0 ||
+      t->mc_ctas_per_sm < 0)
     return VH_ERR_INVALID_ARG;
   VH_CUDA(h, cudaStreamSynchronize(h->stream));
   apply_tuning(h, *t);
@@ -1402,7 +1409,7 @@ extern "C" vh_status vh_autotune(vh_handle *h, const void *depth, int32_t depth_
   float mi = 0, mm = 0;
   s = run(vh_tuning{}, &mi, &mm);  // also allocates the frame's blocks
   float best_int = 1e30f, best_mc = 1e30f;
-  for (int variant = 0; variant < 2 && s == VH_OK; ++variant) {
+  for (int variant = 0; variant < integrate_variants() && s == VH_OK; ++variant) {
     const int occ = integrate_ctas_per_sm(variant);
     const int opts[3] = {occ, std::max(1, occ * 3 / 4), std::max(1, occ / 2)};
     for (int o = 0; o < 3 && s == VH_OK; ++o) {
@@ -1418,7 +1425,7 @@ extern "C" vh_status vh_autotune(vh_handle *h, const void *depth, int32_t depth_
       }
     }
   }
-  for (int variant = 0; variant < 2 && s == VH_OK; ++variant) {
+  for (int variant = 0; variant < mc_variants() && s == VH_OK; ++variant) {
     const int mocc = mc_ctas_per_sm(variant);
     const int mopts[3] = {mocc, std::max(1, mocc * 2 / 3), std::max(1, mocc / 2)};
     for (int o = 0; o < 3 && s == VH_OK; ++o) {

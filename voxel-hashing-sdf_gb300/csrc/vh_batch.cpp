@@ -139,8 +139,7 @@ void enqueue_group_step(vh_batch *b, BatchGroup &g, int k, int fmt, bool with_me
   cudaStream_t s = g.stream;
   launch_batch_frame_begin(d, act, g.n, s);
   launch_batch_allocate(d, act, g.d_px_start, g.total_px, g.n, fmt, s);
-  launch_batch_epoch_end(d, act, g.n, g.d_prefix, with_mesh, s);
-  launch_batch_resolve(d, g.d_prefix, g.n, b->sm_count * 2, s);
+  launch_batch_resolve(d, act, g.n, g.d_prefix, with_mesh, b->sm_count * 2, s);
   launch_batch_integrate(d, g.d_prefix, g.n, shape[0], s);
   if (with_mesh) launch_batch_mc(d, g.d_prefix, g.n, shape[1], shape[2], s);
 }

@@ -184,9 +184,12 @@ void launch_integrate(const VolumeView &V, const CamParams &C, const uint2 *pix,
 // counters there, as launch_state_out would after the kernel.
 void launch_mc(const VolumeView &V, int scope_all, float min_weight, float4 *tris,
                uint32_t tri_cap, int grid, int variant, DevState *host_state, cudaStream_t s);
-// Resident CTAs per SM of the persistent kernels (for grid sizing).
+// Resident CTAs per SM of the persistent kernels (for grid sizing), and the
+// number of launch shapes of each (variants 0 .. n - 1).
 int integrate_ctas_per_sm(int variant);
 int mc_ctas_per_sm(int variant);
+int integrate_variants();
+int mc_variants();
 void launch_alloc_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, cudaStream_t s);
 void launch_find_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, int32_t *out,
                       cudaStream_t s);
@@ -211,16 +214,16 @@ void launch_depth_filter(const CamParams &C, const void *depth, const FrameIn *f
 // Batched stages: one launch covers the work of every active scene.
 // active[i] != 0: scene i has a frame this step.  px_start: first global
 // pixel of each scene (multiples of kBatchPixelThreads; n + 1 entries).  prefix: per-scene
-// work prefix (n + 1 entries) written by launch_batch_epoch_end (frame
+// work prefix (n + 1 entries) written by launch_batch_resolve (frame
 // lists) and read by the later stages.
 void launch_batch_frame_begin(const SceneDesc *d, const uint8_t *active, int n, cudaStream_t s);
 void launch_batch_allocate(const SceneDesc *d, const uint8_t *active, const uint32_t *px_start,
                            uint32_t total_px, int n, int fmt, cudaStream_t s);
-// with_mesh: also resets every active scene's marching-cubes counters.
-void launch_batch_epoch_end(const SceneDesc *d, const uint8_t *active, int n, uint32_t *prefix,
-                            bool with_mesh, cudaStream_t s);
-void launch_batch_resolve(const SceneDesc *d, const uint32_t *prefix, int n, int grid,
-                          cudaStream_t s);
+// Closes every active scene's allocation epoch, writes prefix and resolves
+// the frame lists (one launch); with_mesh: also resets every active
+// scene's marching-cubes counters.
+void launch_batch_resolve(const SceneDesc *d, const uint8_t *active, int n, uint32_t *prefix,
+                          bool with_mesh, int grid, cudaStream_t s);
 void launch_batch_integrate(const SceneDesc *d, const uint32_t *prefix, int n, int grid,
                             cudaStream_t s);
 void launch_batch_mc(const SceneDesc *d, uint32_t *prefix, int n, int grid, int variant,

@@ -528,81 +528,129 @@ __device__ __forceinline__ bool update_voxel(const CamParams &C, uint2 px, float
   return true;
 }
 
-// One thread's quad of 4 voxels along x: project all, gather all pixels,
-// then update.  Returns the number of voxels updated.
-__device__ __forceinline__ uint32_t update_quad(const CamParams &C, const float P[12],
-                                                const uint2 *__restrict__ pix, int ix, float wy,
-                                                float wz, float4 &sdf, float4 &wt, uint4 &rgb) {
-  float z0, z1, z2, z3;
-  const int i0 = project_voxel(C, P, (float)(ix + 0) * C.voxel, wy, wz, z0);
-  const int i1 = project_voxel(C, P, (float)(ix + 1) * C.voxel, wy, wz, z1);
-  const int i2 = project_voxel(C, P, (float)(ix + 2) * C.voxel, wy, wz, z2);
-  const int i3 = project_voxel(C, P, (float)(ix + 3) * C.voxel, wy, wz, z3);
+// One thread's run of kV voxels along x (kV = 2, 4 or 8): project all,
+// gather all pixels, then update.  Returns the number of voxels updated.
+template <int kV>
+__device__ __forceinline__ uint32_t update_run(const CamParams &C, const float P[12],
+                                               const uint2 *__restrict__ pix, int ix, float wy,
+                                               float wz, float (&sdf)[kV], float (&wt)[kV],
+                                               uint32_t (&rgb)[kV]) {
+  float z[kV];
+  int idx[kV];
+#pragma unroll
+  for (int k = 0; k < kV; ++k) idx[k] = project_voxel(C, P, (float)(ix + k) * C.voxel, wy, wz, z[k]);
   const uint2 none = make_uint2(0u, 0u);  // depth 0 = invalid
-  const uint2 p0 = i0 >= 0 ? __ldg(pix + i0) : none;
-  const uint2 p1 = i1 >= 0 ? __ldg(pix + i1) : none;
-  const uint2 p2 = i2 >= 0 ? __ldg(pix + i2) : none;
-  const uint2 p3 = i3 >= 0 ? __ldg(pix + i3) : none;
+  uint2 px[kV];
+#pragma unroll
+  for (int k = 0; k < kV; ++k) px[k] = idx[k] >= 0 ? __ldg(pix + idx[k]) : none;
   uint32_t n = 0;
-  n += update_voxel(C, p0, z0, sdf.x, wt.x, rgb.x);
-  n += update_voxel(C, p1, z1, sdf.y, wt.y, rgb.y);
-  n += update_voxel(C, p2, z2, sdf.z, wt.z, rgb.z);
-  n += update_voxel(C, p3, z3, sdf.w, wt.w, rgb.w);
+#pragma unroll
+  for (int k = 0; k < kV; ++k) n += update_voxel(C, px[k], z[k], sdf[k], wt[k], rgb[k]);
   return n;
 }
 
-// Loads the slot of frame-list entry i and the block's voxel quad of thread t.
-struct BlockQuad {
+// Word <-> value of the pool's 4-byte fields (sdf and weight floats, colour).
+__device__ __forceinline__ void from_bits(uint32_t b, float &v) { v = __uint_as_float(b); }
+__device__ __forceinline__ void from_bits(uint32_t b, uint32_t &v) { v = b; }
+__device__ __forceinline__ uint32_t to_bits(float v) { return __float_as_uint(v); }
+__device__ __forceinline__ uint32_t to_bits(uint32_t v) { return v; }
+
+// kV consecutive words at p (p aligned to 4 kV bytes), with 16-byte
+// accesses (8-byte for kV = 2).
+template <int kV, typename T>
+__device__ __forceinline__ void load_words(const T *__restrict__ p, T (&v)[kV]) {
+  static_assert(sizeof(T) == 4 && (kV == 2 || kV == 4 || kV == 8), "2, 4 or 8 words");
+  if constexpr (kV == 2) {
+    const uint2 a = *reinterpret_cast<const uint2 *>(p);
+    from_bits(a.x, v[0]);
+    from_bits(a.y, v[1]);
+  } else {
+#pragma unroll
+    for (int h = 0; h < kV / 4; ++h) {
+      const uint4 a = reinterpret_cast<const uint4 *>(p)[h];
+      from_bits(a.x, v[4 * h + 0]);
+      from_bits(a.y, v[4 * h + 1]);
+      from_bits(a.z, v[4 * h + 2]);
+      from_bits(a.w, v[4 * h + 3]);
+    }
+  }
+}
+template <int kV, typename T>
+__device__ __forceinline__ void store_words(T *__restrict__ p, const T (&v)[kV]) {
+  if constexpr (kV == 2) {
+    *reinterpret_cast<uint2 *>(p) = make_uint2(to_bits(v[0]), to_bits(v[1]));
+  } else {
+#pragma unroll
+    for (int h = 0; h < kV / 4; ++h)
+      reinterpret_cast<uint4 *>(p)[h] = make_uint4(to_bits(v[4 * h + 0]), to_bits(v[4 * h + 1]),
+                                                   to_bits(v[4 * h + 2]), to_bits(v[4 * h + 3]));
+  }
+}
+
+// The slot of frame-list entry i and thread t's run of kV voxels of the
+// block (voxels kV t .. kV t + kV - 1).
+template <int kV>
+struct VoxelRun {
   unsigned long long key;
   uint32_t block;
-  float4 sdf, wt;
-  uint4 rgb;
+  float sdf[kV], wt[kV];
+  uint32_t rgb[kV];
 };
 
-__device__ __forceinline__ void load_quad(const VolumeView &V, uint32_t i, int t, BlockQuad &q) {
+template <int kV>
+__device__ __forceinline__ void load_run(const VolumeView &V, uint32_t i, int t, VoxelRun<kV> &q) {
   const ulonglong2 r = __ldg(V.frame_res + i);
   q.key = r.x;
   q.block = (uint32_t)r.y;
   if (q.key >= kTombKey || q.block == kNoBlock) return;
-  const float *base = V.pool + (size_t)q.block * kBlockWords;
-  q.sdf = reinterpret_cast<const float4 *>(base)[t];
-  q.wt = reinterpret_cast<const float4 *>(base + kB3)[t];
-  q.rgb = reinterpret_cast<const uint4 *>(base + 2 * kB3)[t];
+  const float *base = V.pool + (size_t)q.block * kBlockWords + kV * t;
+  load_words<kV>(base, q.sdf);
+  load_words<kV>(base + kB3, q.wt);
+  load_words<kV>(reinterpret_cast<const uint32_t *>(base + 2 * kB3), q.rgb);
 }
 
-// Frame-list entry i whose voxel quad (thread t = threadIdx.x) is loaded in
-// `cur`: every thread updates and stores its 4 voxels.  Returns the number
-// of voxels this thread updated.
-__device__ __forceinline__ uint32_t integrate_loaded(const VolumeView &V, const CamParams &C,
-                                                     const float (&P)[12],
-                                                     const uint2 *__restrict__ pix, uint32_t i,
-                                                     BlockQuad &cur) {
+// Frame-list entry i whose run (thread t = threadIdx.x) is loaded in `cur`:
+// every thread updates and stores its kV voxels.  Returns the number of
+// voxels this thread updated.
+template <int kV>
+__device__ __forceinline__ uint32_t integrate_run(const VolumeView &V, const CamParams &C,
+                                                  const float (&P)[12],
+                                                  const uint2 *__restrict__ pix, uint32_t i,
+                                                  VoxelRun<kV> &cur) {
   const int t = threadIdx.x;
-  const int x0 = (t & 1) * 4, y = (t >> 1) & 7, z = t >> 4;
+  const int li = kV * t, x0 = li & 7, y = (li >> 3) & 7, z = li >> 6;
   const bool live = cur.key < kTombKey && cur.block != kNoBlock;
   if (!live) return 0;
   int bx, by, bz;
   unpack_key(cur.key, bx, by, bz);
   const float wy = (float)(by * kB + y) * C.voxel;
   const float wz = (float)(bz * kB + z) * C.voxel;
-  const uint32_t nu = update_quad(C, P, pix, bx * kB + x0, wy, wz, cur.sdf, cur.wt, cur.rgb);
+  const uint32_t nu = update_run<kV>(C, P, pix, bx * kB + x0, wy, wz, cur.sdf, cur.wt, cur.rgb);
   if (nu) {
-    float *base = V.pool + (size_t)cur.block * kBlockWords;
-    reinterpret_cast<float4 *>(base)[t] = cur.sdf;
-    reinterpret_cast<float4 *>(base + kB3)[t] = cur.wt;
-    reinterpret_cast<uint4 *>(base + 2 * kB3)[t] = cur.rgb;
+    float *base = V.pool + (size_t)cur.block * kBlockWords + kV * t;
+    store_words<kV>(base, cur.sdf);
+    store_words<kV>(base + kB3, cur.wt);
+    store_words<kV>(reinterpret_cast<uint32_t *>(base + 2 * kB3), cur.rgb);
   }
   return nu;
 }
 
-// Persistent CTAs of 128 threads, one voxel block per iteration, 4 voxels
-// per thread.  kPrefetch: the next block's loads are issued before the
-// current block is computed (two blocks in flight per thread, more
-// registers); otherwise one block in flight and higher occupancy.
-template <bool kPrefetch>
-__global__ void __launch_bounds__(128, kPrefetch ? 8 : 12) k_integrate(VolumeView V, CamParams C,
-                                                   const uint2 *__restrict__ pix,
-                                                   const float *__restrict__ pose) {
+// Integration launch shapes (the tuning's integrate_variant): voxels per
+// thread, whether the next block's voxels are loaded before the current
+// block is computed (two blocks in flight per thread, more registers), and
+// the resident CTAs per SM the register budget is set for.
+//   0: 4 voxels x 128 threads, 12 CTAs per SM (40 registers)
+//   1: 4 voxels x 128 threads, prefetch, 8 CTAs per SM (64 registers)
+//   2: 8 voxels x  64 threads (a whole x row per thread), 16 CTAs per SM (64)
+//   3: 2 voxels x 256 threads, 6 CTAs per SM (40)
+//   4: 4 voxels x 128 threads, 10 CTAs per SM (48)
+//   5: 8 voxels x  64 threads, 12 CTAs per SM (80)
+constexpr int kIntegrateVariants = 6;
+// Persistent CTAs of 512 / kV threads, one voxel block per iteration, kV
+// voxels per thread.
+template <int kV, bool kPrefetch, int kMinCtas>
+__global__ void __launch_bounds__(kB3 / kV, kMinCtas) k_integrate(VolumeView V, CamParams C, const uint2 *__restrict__ pix,
+                const float *__restrict__ pose) {
   const uint32_t n = min(V.st->frame_count, V.frame_cap);
   float P[12];
 #pragma unroll
@@ -610,17 +658,17 @@ __global__ void __launch_bounds__(128, kPrefetch ? 8 : 12) k_integrate(VolumeVie
   const int t = threadIdx.x;
   uint32_t updated = 0;
   uint32_t i = blockIdx.x;
-  BlockQuad cur;
-  if (kPrefetch && i < n) load_quad(V, i, t, cur);
+  VoxelRun<kV> cur;
+  if (kPrefetch && i < n) load_run<kV>(V, i, t, cur);
   for (; i < n; i += gridDim.x) {
-    BlockQuad nxt;
+    VoxelRun<kV> nxt;
     if (kPrefetch) {
       const uint32_t j = i + gridDim.x;
-      if (j < n) load_quad(V, j, t, nxt);
+      if (j < n) load_run<kV>(V, j, t, nxt);
     } else {
-      load_quad(V, i, t, cur);
+      load_run<kV>(V, i, t, cur);
     }
-    updated += integrate_loaded(V, C, P, pix, i, cur);
+    updated += integrate_run<kV>(V, C, P, pix, i, cur);
     if (kPrefetch) cur = nxt;
   }
 #pragma unroll
@@ -637,7 +685,8 @@ constexpr int kHalo = kH3 - kB3;   // 217
 // distinct banks for every corner.
 constexpr int kZPitch = 88;
 constexpr int kStaged = kZPitch * kH;  // 792 words
-constexpr int kMcThreads = 128;
+constexpr int kMcThreads = 128;     // threads per CTA of the batched MC and MC variants 0, 1
+constexpr int kMcMaxThreads = 256;  // largest MC CTA (variant 2)
 constexpr int kMaxCand = kB3 * 5;  // at most 5 triangles per cube
 
 struct McShared {
@@ -651,17 +700,21 @@ struct McShared {
   uint16_t cand[kMaxCand];   // candidate triangles: cube | triangle << 9
   uint32_t halo[kHalo];      // halo voxel: staged index | neighbour << 10 | voxel << 13
   uint32_t nb[8];
-  uint32_t warp_sum[kMcThreads / 32];
+  uint32_t warp_sum[kMcMaxThreads / 32];
   uint32_t base;
   uint32_t next[2];  // the block after the current one (double-buffered)
 };
 
 __device__ __forceinline__ int hidx(int x, int y, int z) { return x + kH * y + kZPitch * z; }
 
-// Cube j (0..3) of thread t: x = t & 7, z = (t >> 3 & 3) + 4 (j >> 1),
-// y = (t >> 5) + 4 (j & 1); returns x + 8 y + 64 z.  All 512 cubes once.
+// Cube j (0 .. 512 / kThreads - 1) of thread t: a warp covers 8 x by 4 z
+// cubes of one y row per j, x = t & 7, z = (t >> 3 & 3) + 4 (j / R),
+// y = (t >> 5) + W (j % R) with W = kThreads / 32 warps and R = 8 / W;
+// returns x + 8 y + 64 z.  All 512 cubes once.
+template <int kThreads>
 __device__ __forceinline__ int mc_cube(int t, int j) {
-  const int x = t & 7, z = ((t >> 3) & 3) + 4 * (j >> 1), y = (t >> 5) + 4 * (j & 1);
+  constexpr int W = kThreads / 32, R = 8 / W;
+  const int x = t & 7, z = ((t >> 3) & 3) + 4 * (j / R), y = (t >> 5) + W * (j % R);
   return x + 8 * y + 64 * z;
 }
 __device__ __forceinline__ int corner_dx(int k) { return (kMcCornerBitsX >> k) & 1; }
@@ -759,6 +812,7 @@ __device__ __forceinline__ bool same_pos(const float4 &a, const float4 &b) {
 
 // Exclusive CTA-wide scan of `v`; returns the prefix, total in *total.
 // Contains one __syncthreads; the caller separates consecutive scans.
+template <int kThreads>
 __device__ __forceinline__ uint32_t cta_scan(McShared &S, uint32_t v, uint32_t *total) {
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   uint32_t incl = v;
@@ -771,7 +825,7 @@ __device__ __forceinline__ uint32_t cta_scan(McShared &S, uint32_t v, uint32_t *
   __syncthreads();
   uint32_t before = 0, tot = 0;
 #pragma unroll
-  for (int q = 0; q < kMcThreads / 32; ++q) {
+  for (int q = 0; q < kThreads / 32; ++q) {
     const uint32_t ws = S.warp_sum[q];
     before += q < warp ? ws : 0u;
     tot += ws;
@@ -785,10 +839,10 @@ __device__ __forceinline__ uint32_t cta_scan(McShared &S, uint32_t v, uint32_t *
 //   triangles (scan) -> one thread per candidate tests the reference's
 //   degenerate-triangle rule -> compact (scan) -> one atomic per block ->
 //   one thread per output float4, contiguous stores.
-// Tables and halo map of the MC shared state (once per CTA).
+// Tables and halo map of the MC shared state (once per CTA; any CTA size).
 __device__ __forceinline__ void mc_init_shared(McShared &S) {
   const int t = threadIdx.x;
-  for (int i = t; i < 256; i += kMcThreads) {
+  for (int i = t; i < 256; i += blockDim.x) {
     S.edge[i] = kMcEdgeMask[i];
     int n = 0;
     for (; n < 5 && kMcTri[i][3 * n] >= 0; ++n)
@@ -799,7 +853,7 @@ __device__ __forceinline__ void mc_init_shared(McShared &S) {
   }
   if (t < 12) S.einfo[t] = edge_info(t);
   // halo: x == 8 (81), then y == 8 with x < 8 (72), then z == 8 with x, y < 8 (64)
-  for (int hh = t; hh < kHalo; hh += kMcThreads) {
+  for (int hh = t; hh < kHalo; hh += blockDim.x) {
     int x, y, z;
     if (hh < 81) {
       x = 8;
@@ -821,8 +875,10 @@ __device__ __forceinline__ void mc_init_shared(McShared &S) {
 }
 
 // One block of the list (scope_all: pool block i; else frame-list entry i):
-// stage, classify, expand, test, compact and write its triangles.  Every
-// thread of the CTA calls it with the same i; S must be free on entry.
+// stage, classify, expand, test, compact and write its triangles, with a
+// CTA of kThreads (128 or 256) threads.  Every thread of the CTA calls it
+// with the same i; S must be free on entry.
+template <int kThreads>
 __device__ __forceinline__ void mc_block(McShared &S, const VolumeView &V, int scope_all,
                                          float min_weight, float4 *__restrict__ tris,
                                          uint32_t tri_cap, uint32_t i) {
@@ -848,30 +904,34 @@ __device__ __forceinline__ void mc_block(McShared &S, const VolumeView &V, int s
     S.nb[t] = t == 0 ? own
                      : (key_in_range(nx, ny, nz) ? block_of(V, pack_key(nx, ny, nz)) : kNoBlock);
   }
-  {  // own block: 4 voxels per thread, 16-byte loads
-    const float *base = V.pool + (size_t)own * kBlockWords;
-    const float4 sd = reinterpret_cast<const float4 *>(base)[t];
-    const float4 wt = reinterpret_cast<const float4 *>(base + kB3)[t];
-    const uint4 cl = reinterpret_cast<const uint4 *>(base + 2 * kB3)[t];
-    const int li = 4 * t, x = li & 7, y = (li >> 3) & 7, z = li >> 6;
+  {  // own block: kV voxels per thread, 16-byte (kV = 4) or 8-byte loads
+    constexpr int kV = kB3 / kThreads;
+    const int li = kV * t, x = li & 7, y = (li >> 3) & 7, z = li >> 6;
+    const float *base = V.pool + (size_t)own * kBlockWords + li;
+    float sd[kV], wt[kV];
+    uint32_t cl[kV];
+    load_words<kV>(base, sd);
+    load_words<kV>(base + kB3, wt);
+    load_words<kV>(reinterpret_cast<const uint32_t *>(base + 2 * kB3), cl);
     const int h = hidx(x, y, z);
-    S.sdf[h + 0] = wt.x >= min_weight ? sd.x : nanv;
-    S.sdf[h + 1] = wt.y >= min_weight ? sd.y : nanv;
-    S.sdf[h + 2] = wt.z >= min_weight ? sd.z : nanv;
-    S.sdf[h + 3] = wt.w >= min_weight ? sd.w : nanv;
-    S.rgb[h + 0] = cl.x;
-    S.rgb[h + 1] = cl.y;
-    S.rgb[h + 2] = cl.z;
-    S.rgb[h + 3] = cl.w;
+#pragma unroll
+    for (int k = 0; k < kV; ++k) {
+      S.sdf[h + k] = wt[k] >= min_weight ? sd[k] : nanv;
+      S.rgb[h + k] = cl[k];
+    }
   }
   if (scope_all) __syncthreads();  // S.nb complete (uniform condition)
-  {  // halo: every thread owns at most two entries; all loads issued together
-    const int h1 = t + kMcThreads;
-    const uint32_t info0 = S.halo[t];
+  {  // halo: every thread owns at most two entries (128 threads: t and
+     // t + 128; 256 threads: t only, none from t = kHalo on); all loads
+     // issued together
+    const int h1 = t + kThreads;
+    const bool has0 = kThreads <= kHalo || t < kHalo;
+    const uint32_t info0 = has0 ? S.halo[t] : 0u;
     const uint32_t info1 = h1 < kHalo ? S.halo[h1] : 0u;
     const uint32_t nb0 = (info0 >> 10) & 7u, nb1 = (info1 >> 10) & 7u;
-    const uint32_t blk0 = scope_all ? S.nb[nb0] : __ldg(V.frame_nb + 8 * (size_t)i + nb0);
+    uint32_t blk0 = scope_all ? S.nb[nb0] : __ldg(V.frame_nb + 8 * (size_t)i + nb0);
     uint32_t blk1 = scope_all ? S.nb[nb1] : __ldg(V.frame_nb + 8 * (size_t)i + nb1);
+    if (!has0) blk0 = kNoBlock;
     if (h1 >= kHalo) blk1 = kNoBlock;
     const int li0 = (int)(info0 >> 13), li1 = (int)(info1 >> 13);
     float w0 = 0.f, s0 = nanv, w1 = 0.f, s1 = nanv;
@@ -888,20 +948,23 @@ __device__ __forceinline__ void mc_block(McShared &S, const VolumeView &V, int s
       s1 = __ldg(base + li1);
       c1 = __ldg(reinterpret_cast<const uint32_t *>(base + 2 * kB3) + li1);
     }
-    S.sdf[info0 & 1023u] = blk0 != kNoBlock && w0 >= min_weight ? s0 : nanv;
-    S.rgb[info0 & 1023u] = c0;
+    if (has0) {
+      S.sdf[info0 & 1023u] = blk0 != kNoBlock && w0 >= min_weight ? s0 : nanv;
+      S.rgb[info0 & 1023u] = c0;
+    }
     if (h1 < kHalo) {
       S.sdf[info1 & 1023u] = blk1 != kNoBlock && w1 >= min_weight ? s1 : nanv;
       S.rgb[info1 & 1023u] = c1;
     }
   }
   __syncthreads();
-  // 1. classify this thread's 4 cubes; count their candidate triangles
+  // 1. classify this thread's cubes; count their candidate triangles
+  constexpr int kCubes = kB3 / kThreads;
   uint32_t ncand_mine = 0;
-  int cs[4];
+  int cs[kCubes];
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const int c = mc_cube(t, j);
+  for (int j = 0; j < kCubes; ++j) {
+    const int c = mc_cube<kThreads>(t, j);
     int ci = cube_case(S, c & 7, (c >> 3) & 7, c >> 6);
     if (ci < 0 || S.edge[ci] == 0) ci = 0;
     cs[j] = ci;
@@ -909,11 +972,11 @@ __device__ __forceinline__ void mc_block(McShared &S, const VolumeView &V, int s
     ncand_mine += S.ntri[ci];
   }
   uint32_t ncand;
-  uint32_t off = cta_scan(S, ncand_mine, &ncand);
+  uint32_t off = cta_scan<kThreads>(S, ncand_mine, &ncand);
   if (ncand == 0) return;  // uniform: nothing to emit in this block
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const int c = mc_cube(t, j);
+  for (int j = 0; j < kCubes; ++j) {
+    const int c = mc_cube<kThreads>(t, j);
     const int nt = S.ntri[cs[j]];
     for (int tt = 0; tt < nt; ++tt) S.cand[off++] = (uint16_t)(c | (tt << 9));
   }
@@ -924,7 +987,7 @@ __device__ __forceinline__ void mc_block(McShared &S, const VolumeView &V, int s
   //    the survivors gives each a slot in one contiguous range reserved
   //    with a single atomic, and the thread writes its 48-byte triangle.
   const int gx0 = bx * kB, gy0 = by * kB, gz0 = bz * kB;
-  for (uint32_t r0 = 0; r0 < ncand; r0 += kMcThreads) {
+  for (uint32_t r0 = 0; r0 < ncand; r0 += kThreads) {
     const uint32_t k = r0 + t;
     float4 p0, p1, p2;
     uint32_t ok = 0;
@@ -940,7 +1003,7 @@ __device__ __forceinline__ void mc_block(McShared &S, const VolumeView &V, int s
       ok = !(same_pos(p0, p1) || same_pos(p1, p2));
     }
     uint32_t nvalid;
-    const uint32_t pre = cta_scan(S, ok, &nvalid);
+    const uint32_t pre = cta_scan<kThreads>(S, ok, &nvalid);
     if (t == 0) S.base = nvalid ? atomicAdd(&V.st->tri_count, nvalid) : 0u;
     __syncthreads();
     if (ok) {
@@ -957,8 +1020,8 @@ __device__ __forceinline__ void mc_block(McShared &S, const VolumeView &V, int s
   }
 }
 
-template <int kMinCtas>
-__global__ void __launch_bounds__(kMcThreads, kMinCtas) k_mc(VolumeView V, int scope_all, float min_weight,
+template <int kThreads, int kMinCtas>
+__global__ void __launch_bounds__(kThreads, kMinCtas) k_mc(VolumeView V, int scope_all, float min_weight,
                                                       float4 *__restrict__ tris, uint32_t tri_cap,
                                                       DevState *host_state) {
   __shared__ McShared S;
@@ -972,7 +1035,7 @@ __global__ void __launch_bounds__(kMcThreads, kMinCtas) k_mc(VolumeView V, int s
   uint32_t i = blockIdx.x;
   for (int par = 0; i < n; par ^= 1) {
     if (threadIdx.x == 0) S.next[par] = gridDim.x + atomicAdd(&V.st->mc_next, 1u);
-    mc_block(S, V, scope_all, min_weight, tris, tri_cap, i);
+    mc_block<kThreads>(S, V, scope_all, min_weight, tris, tri_cap, i);
     __syncthreads();  // S.next[par] visible; this block done with S
     i = S.next[par];
   }
@@ -1133,56 +1196,71 @@ __global__ void __launch_bounds__(kBatchPixelThreads) k_batch_allocate(
                          keys[threadIdx.x >> 5]);
 }
 
-// Closes every active scene's allocation epoch and writes the prefix of the
-// frame-list lengths (one CTA of 1024 threads, n <= 1024); prefix holds
-// n + 2 words, the last one k_batch_mc's block counter.
-__global__ void __launch_bounds__(1024) k_batch_epoch_end(const SceneDesc *__restrict__ d,
-                                                          const uint8_t *__restrict__ active,
-                                                          int n, uint32_t *__restrict__ prefix,
-                                                          int with_mesh) {
-  __shared__ uint32_t wsum[32];
-  const int s = threadIdx.x, lane = s & 31, warp = s >> 5;
-  uint32_t cnt = 0;
-  if (s < n && active[s]) {
-    const VolumeView &V = d[s].V;
-    if (with_mesh)
-      mc_begin_state(V);
-    else
-      reconcile(V);
-    cnt = min(V.st->frame_count, V.frame_cap);
-  }
-  uint32_t incl = cnt;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t u = __shfl_up_sync(kFull, incl, o);
-    if (lane >= o) incl += u;
-  }
-  if (lane == 31) wsum[warp] = incl;
-  __syncthreads();
-  if (warp == 0) {
-    uint32_t w = wsum[lane], wi = w;
+// Closes every active scene's allocation epoch (CTA 0; with_mesh: also
+// resets its marching-cubes counters), writes the prefix of the frame-list
+// lengths for the later stages (CTA 0; prefix holds n + 2 words, the last
+// one k_batch_mc's block counter) and resolves the frame lists of all
+// scenes, 8 threads per entry (every CTA, from its own copy of the prefix
+// in shared memory, n <= 1024).  The epoch fields CTA 0 updates are not
+// the frame-list lengths the other CTAs read, as in k_frame_resolve.
+__global__ void __launch_bounds__(256) k_batch_resolve(const SceneDesc *__restrict__ d,
+                                                       const uint8_t *__restrict__ active, int n,
+                                                       uint32_t *__restrict__ prefix,
+                                                       int with_mesh) {
+  __shared__ uint32_t sp[1025];
+  __shared__ uint32_t wsum[8];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  uint32_t run = 0;
+  for (int s0 = 0; s0 < n; s0 += 256) {
+    const int s = s0 + t;
+    uint32_t cnt = 0;
+    if (s < n && active[s]) {
+      const VolumeView &V = d[s].V;
+      if (blockIdx.x == 0) {
+        if (with_mesh)
+          mc_begin_state(V);
+        else
+          reconcile(V);
+      }
+      cnt = min(V.st->frame_count, V.frame_cap);
+    }
+    uint32_t incl = cnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t u = __shfl_up_sync(kFull, wi, o);
-      if (lane >= o) wi += u;
+      const uint32_t u = __shfl_up_sync(kFull, incl, o);
+      if (lane >= o) incl += u;
     }
-    wsum[lane] = wi - w;  // exclusive warp offsets
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    uint32_t before = 0, tot = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const uint32_t w = wsum[q];
+      before += q < warp ? w : 0u;
+      tot += w;
+    }
+    if (s < n) sp[s] = run + before + incl - cnt;
+    run += tot;
+    __syncthreads();  // wsum free for the next chunk
   }
+  if (t == 0) sp[n] = run;
   __syncthreads();
-  const uint32_t excl = wsum[warp] + incl - cnt;
-  if (s < n) prefix[s] = excl;
-  if (s == n - 1) prefix[n] = excl + cnt;
-  if (s == 0) prefix[n + 1] = 0;  // k_batch_mc's hand-out counter
-}
-
-__global__ void __launch_bounds__(256) k_batch_resolve(const SceneDesc *__restrict__ d,
-                                                       const uint32_t *__restrict__ prefix, int n) {
-  const uint32_t total8 = 8u * __ldg(prefix + n);
-  for (uint32_t g8 = blockIdx.x * blockDim.x + threadIdx.x; g8 < total8;
-       g8 += gridDim.x * blockDim.x) {
+  if (blockIdx.x == 0) {
+    for (int s = t; s <= n; s += 256) prefix[s] = sp[s];
+    if (t == 0) prefix[n + 1] = 0;  // k_batch_mc's hand-out counter
+  }
+  const uint32_t total8 = 8u * run;
+  for (uint32_t g8 = blockIdx.x * blockDim.x + t; g8 < total8; g8 += gridDim.x * blockDim.x) {
     const uint32_t g = g8 >> 3;
-    const int s = scene_of(prefix, n, g);
-    resolve_entry(d[s].V, g - __ldg(prefix + s), g8 & 7u);
+    int lo = 0, hi = n;  // scene of entry g: the last s with sp[s] <= g
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (sp[mid] <= g)
+        lo = mid;
+      else
+        hi = mid;
+    }
+    resolve_entry(d[lo].V, g - sp[lo], g8 & 7u);
   }
 }
 
@@ -1221,9 +1299,9 @@ __global__ void __launch_bounds__(128) k_batch_integrate(const SceneDesc *__rest
       cur = s;
     }
     const uint32_t i = g - __ldg(prefix + s);
-    BlockQuad q;
-    load_quad(sd.V, i, t, q);
-    updated += integrate_loaded(sd.V, sd.C, P, sd.pix, i, q);
+    VoxelRun<4> q;
+    load_run<4>(sd.V, i, t, q);
+    updated += integrate_run<4>(sd.V, sd.C, P, sd.pix, i, q);
   }
   if (cur >= 0) flush_updated(sd, updated);
 }
@@ -1247,7 +1325,7 @@ __global__ void __launch_bounds__(kMcThreads, kMinCtas) k_batch_mc(const SceneDe
       load_scene(sd, d, s);
       cur = s;
     }
-    mc_block(S, sd.V, 0, sd.C.mc_min_weight, sd.tris, sd.tri_cap, g - __ldg(prefix + s));
+    mc_block<kMcThreads>(S, sd.V, 0, sd.C.mc_min_weight, sd.tris, sd.tri_cap, g - __ldg(prefix + s));
     __syncthreads();
     g = S.next[par];
   }
@@ -1462,41 +1540,72 @@ void launch_depth_filter(const CamParams &C, const void *depth, const FrameIn *f
     k_depth_filter<float><<<grid, 256, 0, s>>>(C, static_cast<const float *>(depth), fin, out);
 }
 
-int integrate_ctas_per_sm(int variant) {
+template <int kV, bool kPrefetch, int kMinCtas>
+int integrate_occupancy() {
   int n = 0;
-  if (variant == 1)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_integrate<true>, 128, 0);
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_integrate<false>, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_integrate<kV, kPrefetch, kMinCtas>, kB3 / kV,
+                                                0);
   return n > 0 ? n : 1;
 }
 
-// MC variants differ only in the register budget: 0 targets 10 resident
-// CTAs per SM (48 registers, no spills), 1 targets 12 (40 registers, a few
-// spilled).
+int integrate_ctas_per_sm(int variant) {
+  switch (variant) {
+    case 1: return integrate_occupancy<4, true, 8>();
+    case 2: return integrate_occupancy<8, false, 16>();
+    case 3: return integrate_occupancy<2, false, 6>();
+    case 4: return integrate_occupancy<4, false, 10>();
+    case 5: return integrate_occupancy<8, false, 12>();
+    default: return integrate_occupancy<4, false, 12>();
+  }
+}
+
+int integrate_variants() { return kIntegrateVariants; }
+
+// MC launch shapes (the tuning's mc_variant): 0: 128 threads, register
+// budget for 10 resident CTAs per SM; 1: 128 threads, 12 CTAs; 2: 256
+// threads (2 voxels and 2 cubes per thread, rounds of 256 candidates), 5
+// CTAs.
+int mc_variants() { return 3; }
+
 int mc_ctas_per_sm(int variant) {
   int n = 0;
-  if (variant == 1)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mc<12>, kMcThreads, 0);
+  if (variant == 2)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mc<256, 5>, 256, 0);
+  else if (variant == 1)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mc<kMcThreads, 12>, kMcThreads, 0);
   else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mc<10>, kMcThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mc<kMcThreads, 10>, kMcThreads, 0);
   return n > 0 ? n : 1;
+}
+
+template <int kV, bool kPrefetch, int kMinCtas>
+void launch_integrate_shape(const VolumeView &V, const CamParams &C, const uint2 *pix,
+                            const float *pose, int grid, cudaStream_t s) {
+  k_integrate<kV, kPrefetch, kMinCtas><<<grid, kB3 / kV, 0, s>>>(V, C, pix, pose);
 }
 
 void launch_integrate(const VolumeView &V, const CamParams &C, const uint2 *pix, const float *pose,
                       int grid, int variant, cudaStream_t s) {
-  if (variant == 1)
-    k_integrate<true><<<grid, 128, 0, s>>>(V, C, pix, pose);
-  else
-    k_integrate<false><<<grid, 128, 0, s>>>(V, C, pix, pose);
+  switch (variant) {
+    case 1: launch_integrate_shape<4, true, 8>(V, C, pix, pose, grid, s); break;
+    case 2: launch_integrate_shape<8, false, 16>(V, C, pix, pose, grid, s); break;
+    case 3: launch_integrate_shape<2, false, 6>(V, C, pix, pose, grid, s); break;
+    case 4: launch_integrate_shape<4, false, 10>(V, C, pix, pose, grid, s); break;
+    case 5: launch_integrate_shape<8, false, 12>(V, C, pix, pose, grid, s); break;
+    default: launch_integrate_shape<4, false, 12>(V, C, pix, pose, grid, s); break;
+  }
 }
 
 void launch_mc(const VolumeView &V, int scope_all, float min_weight, float4 *tris,
                uint32_t tri_cap, int grid, int variant, DevState *host_state, cudaStream_t s) {
-  if (variant == 1)
-    k_mc<12><<<grid, kMcThreads, 0, s>>>(V, scope_all, min_weight, tris, tri_cap, host_state);
+  if (variant == 2)
+    k_mc<256, 5><<<grid, 256, 0, s>>>(V, scope_all, min_weight, tris, tri_cap, host_state);
+  else if (variant == 1)
+    k_mc<kMcThreads, 12><<<grid, kMcThreads, 0, s>>>(V, scope_all, min_weight, tris, tri_cap,
+                                                      host_state);
   else
-    k_mc<10><<<grid, kMcThreads, 0, s>>>(V, scope_all, min_weight, tris, tri_cap, host_state);
+    k_mc<kMcThreads, 10><<<grid, kMcThreads, 0, s>>>(V, scope_all, min_weight, tris, tri_cap,
+                                                      host_state);
 }
 
 void launch_alloc_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, cudaStream_t s) {
@@ -1535,13 +1644,9 @@ void launch_batch_allocate(const SceneDesc *d, const uint8_t *active, const uint
   else
     k_batch_allocate<float><<<grid, kBatchPixelThreads, 0, s>>>(d, active, px_start, n);
 }
-void launch_batch_epoch_end(const SceneDesc *d, const uint8_t *active, int n, uint32_t *prefix,
-                            bool with_mesh, cudaStream_t s) {
-  k_batch_epoch_end<<<1, 1024, 0, s>>>(d, active, n, prefix, with_mesh ? 1 : 0);
-}
-void launch_batch_resolve(const SceneDesc *d, const uint32_t *prefix, int n, int grid,
-                          cudaStream_t s) {
-  k_batch_resolve<<<grid, 256, 0, s>>>(d, prefix, n);
+void launch_batch_resolve(const SceneDesc *d, const uint8_t *active, int n, uint32_t *prefix,
+                          bool with_mesh, int grid, cudaStream_t s) {
+  k_batch_resolve<<<grid, 256, 0, s>>>(d, active, n, prefix, with_mesh ? 1 : 0);
 }
 void launch_batch_integrate(const SceneDesc *d, const uint32_t *prefix, int n, int grid,
                             cudaStream_t s) {
@@ -1549,7 +1654,7 @@ void launch_batch_integrate(const SceneDesc *d, const uint32_t *prefix, int n, i
 }
 void launch_batch_mc(const SceneDesc *d, uint32_t *prefix, int n, int grid, int variant,
                      cudaStream_t s) {
-  uint32_t *next = prefix + n + 1;  // reset by k_batch_epoch_end
+  uint32_t *next = prefix + n + 1;  // reset by k_batch_resolve
   if (variant == 1)
     k_batch_mc<12><<<grid, kMcThreads, 0, s>>>(d, prefix, n, next);
   else

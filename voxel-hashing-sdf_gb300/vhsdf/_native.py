@@ -119,6 +119,7 @@ SIGNATURES = {
     "vh_get_stats": (I32, [P, C.POINTER(VhStats)]),
     "vh_get_tuning": (I32, [P, C.POINTER(VhTuning)]),
     "vh_set_tuning": (I32, [P, C.POINTER(VhTuning)]),
+    "vh_tuning_variants": (None, [C.POINTER(I32), C.POINTER(I32)]),
     "vh_autotune": (I32, [P, P, I32, P, P, I32, C.POINTER(VhTuning)]),
     "vh_sdf_sample": (I32, [P, P, I64, P, P, P, I32]),
     "vh_pose_normal_equations": (I32, [P, P, I32, I32, P, I32, I32, P]),

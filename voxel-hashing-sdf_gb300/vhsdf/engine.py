@@ -172,6 +172,14 @@ class Volume:
         self._check(self._L.vh_get_tuning(self._h, C.byref(t)))
         return {f: getattr(t, f) for f, _ in N.VhTuning._fields_}
 
+    @staticmethod
+    def tuning_variants():
+        """(integration shapes, MC shapes): the ranges of integrate_variant
+        and mc_variant."""
+        a, b = N.I32(), N.I32()
+        N.lib().vh_tuning_variants(C.byref(a), C.byref(b))
+        return a.value, b.value
+
     def set_tuning(self, integrate_variant=0, integrate_ctas_per_sm=0, mc_ctas_per_sm=0,
                    mc_variant=0):
         t = N.VhTuning(integrate_variant, integrate_ctas_per_sm, mc_ctas_per_sm, mc_variant)
