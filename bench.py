@@ -467,6 +467,12 @@ def batched_leg(num_scenes, steps, local, small=False):
                and b["voxels_updated"] == q["voxels_updated"] for b, q in zip(bstats, sstats))
     for v in vols:
         v.close()
+    extraction = None
+    if small:
+        try:
+            extraction = _batched_extraction(specs, frames, steps, local)
+        except Exception as e:  # a capacity error is reported, not fatal
+            extraction = {"unavailable": f"{type(e).__name__}: {e}"}
     first = 1000 if small else 100
     shape = ("160x120, voxel U[10, 20] mm" if small else
              "320x240 .. 1280x960, voxel U[4, 20] mm")
@@ -485,7 +491,80 @@ def batched_leg(num_scenes, steps, local, small=False):
             "voxel_updates_per_s": sum(b["voxels_updated"] for b in bstats) / t_batch,
             "launches_per_step": {
                 "batched": 4 * min(16, num_scenes),  # frame_begin, allocate, resolve, integrate per group
-                "per_scene_graphs": sum(int(q["frame_kernels"]) for q in sstats)}}
+                "per_scene_graphs": sum(int(q["frame_kernels"]) for q in sstats)},
+            "with_extraction": extraction}
+
+
+def _batched_extraction(specs, frames, steps, local):
+    """The same steps with per-frame marching cubes (meshes left on the
+    device): one vh_process_frame per scene and frame against batched steps
+    with the mesh flag; both through the C ABI with prepared arguments.
+    Single noisy frames mesh the whole band (up to ~25 triangles per pixel
+    on these scenes), so both arms get 64 triangles per pixel of room."""
+    import ctypes as C
+    from vhsdf import Batch, Volume
+    from vhsdf import _native as N
+    L = N.lib()
+    n = len(specs)
+    params = [dict(prm, device=local, max_triangles=64 * prm["width"] * prm["height"])
+              for _, _, prm in specs]
+    vols = [Volume(**prm) for prm in params]
+    for v, fr in zip(vols, frames):
+        v.process_frame(*fr[0], depth_format="u16")
+    for v in vols:
+        v.sync()
+        v.reset()
+    for v in vols:
+        v.sync()
+    rows = []
+    for k in range(steps):
+        row = []
+        for v, fr in zip(vols, frames):
+            if k < len(fr):
+                pose = np.ascontiguousarray(np.asarray(fr[k][2], np.float32).reshape(16))
+                row.append((v._h, fr[k][0].data_ptr(), fr[k][1].data_ptr(), pose))
+        rows.append(row)
+    t0 = time.perf_counter()
+    for row in rows:
+        for h, dptr, cptr, pose in row:
+            N.check(L.vh_process_frame(h, dptr, N.VH_DEPTH_U16_MM, cptr, pose.ctypes.data,
+                                       N.VH_MEM_DEVICE, None))
+    for v in vols:
+        v.sync()
+    t_seq = time.perf_counter() - t0
+    seq_tris = [int(v.stats()["triangles"]) for v in vols]
+    for v in vols:
+        v.close()
+    batch = Batch(params)
+    batch.process([fr[0] for fr in frames], with_mesh=True, depth_format="u16")
+    batch.sync()
+    for i in range(n):
+        batch.scene(i).reset()
+    batch.sync()
+    prepared = []
+    for k in range(steps):
+        dp, cp = (C.c_void_p * n)(), (C.c_void_p * n)()
+        poses = np.zeros((n, 16), np.float32)
+        for i, fr in enumerate(frames):
+            if k < len(fr):
+                dp[i], cp[i] = fr[k][0].data_ptr(), fr[k][1].data_ptr()
+                poses[i] = np.asarray(fr[k][2], np.float32).reshape(16)
+        prepared.append((dp, cp, poses))
+    t0 = time.perf_counter()
+    for dp, cp, poses in prepared:
+        N.check(L.vh_batch_process(batch._b, dp, N.VH_DEPTH_U16_MM, cp, poses.ctypes.data,
+                                   N.VH_MEM_DEVICE, 1))
+    status, bstats = batch.sync()
+    t_batch = time.perf_counter() - t0
+    batch.close()
+    total = sum(len(fr) for fr in frames)
+    return {"what": "allocate -> integrate -> per-frame marching cubes per frame, meshes left "
+                    "on the device",
+            "batched_frames_per_s": total / t_batch, "per_scene_graphs_frames_per_s": total / t_seq,
+            "speedup": t_seq / t_batch, "status_ok": all(x == 0 for x in status),
+            "last_mesh_triangles_equal_per_scene":
+                [int(b["triangles"]) for b in bstats] == seq_tris,
+            "triangles_last_step": sum(seq_tris)}
 
 
 def hbm_stress_leg(num_frames, local, keyframes=16, iterations=20):

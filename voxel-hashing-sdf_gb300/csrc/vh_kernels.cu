@@ -1275,7 +1275,7 @@ __device__ __forceinline__ void flush_updated(const SceneDesc &sd, uint32_t upda
 // Persistent CTAs over the listed blocks of every scene; the scene's
 // descriptor and pose live in shared memory while consecutive items stay in
 // that scene.
-__global__ void __launch_bounds__(128) k_batch_integrate(const SceneDesc *__restrict__ d,
+__global__ void __launch_bounds__(128, 12) k_batch_integrate(const SceneDesc *__restrict__ d,
                                                          const uint32_t *__restrict__ prefix,
                                                          int n) {
   __shared__ SceneDesc sd;
