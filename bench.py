@@ -937,7 +937,9 @@ def run_engine(args):
     e2e_dev = frames_total / e2e_dev_s
     # Rooflines.  Algorithmic bytes per launch:
     #   k_mc        12 B per voxel of every listed block (sdf, weight, rgb read
-    #               once) + 48 B per output triangle (3 x float4 vertex)
+    #               once) + 45 B per output triangle (3 vertices of xyz f32
+    #               and rgb u8; the kernel writes them as 3 x float4, 48 B,
+    #               the colour packed in the fourth word)
     #   k_integrate 12 B per voxel of every listed block read + 12 B per
     #               updated voxel written + 8 B per pixel record
     # DRAM traffic per launch: the traffic / algorithmic ratio that the
@@ -947,7 +949,8 @@ def run_engine(args):
     blocks = [s["frame_blocks"] for s in stage]
     updated = [s["voxels_updated"] for s in stage]
     tris = [s["triangles"] for s in stage]
-    mc_alg = [12 * 512 * b + 48 * t for b, t in zip(blocks, tris)]
+    mc_alg = [12 * 512 * b + 45 * t for b, t in zip(blocks, tris)]
+    mc_stored = [12 * 512 * b + 48 * t for b, t in zip(blocks, tris)]  # the ratio's base
     in_alg = [12 * 512 * b + 12 * u + 8 * npx for b, u in zip(blocks, updated)]
     mc_ms = [s["ms_extract"] for s in stage]
     in_ms = [s["ms_integrate"] for s in stage]
@@ -989,7 +992,7 @@ def run_engine(args):
                 "mesh_left_on_device": e2e_dev},
         "roofline": {"bound": "hbm", "achieved": mc_ach, "peak": peak, "unit": "GB/s",
                      "frac": mc_ach / peak,
-                     "traffic": (ratios["k_mc"] * statistics.mean(mc_alg)
+                     "traffic": (ratios["k_mc"] * statistics.mean(mc_stored)
                                  if "k_mc" in ratios else None),
                      "kernel": "k_mc", "peak_source": peak_src,
                      "algorithmic_bytes": statistics.mean(mc_alg)},

@@ -93,3 +93,12 @@ def test_batch_rejects_unsupported_parameters_on_the_host():
     with pytest.raises(VhError) as err:
         Batch([dict(width=64, height=48, voxel_size=0.0)])
     assert err.value.status == N.VH_ERR_INVALID_ARG
+
+
+def test_tuning_variant_counts():
+    """Launch-shape counts are host facts (no device call): 6 integration
+    shapes and 3 marching-cubes shapes, and both pointers may be NULL."""
+    from vhsdf import Volume
+    from vhsdf import _native as N
+    assert Volume.tuning_variants() == (6, 3)
+    N.lib().vh_tuning_variants(None, None)
