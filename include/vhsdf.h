@@ -166,6 +166,17 @@ vh_status vh_set_stream(vh_handle *h, void *stream);
 vh_status vh_sync(vh_handle *h);
 const char *vh_last_error(const vh_handle *h);
 
+/* Log sink (the reference prints errors with std::cout and glog,
+ * src/safecall.cpp:18-53).  fn(level, message, user) receives every error
+ * the library records on a handle (the text vh_last_error returns; sticky
+ * device errors when vh_sync or vh_get_stats reports them) or on a batch
+ * call, and the failures of vh_create before a handle exists.  level is VH_LOG_ERROR.  Process-wide; fn = NULL turns it off.
+ * fn runs on the thread that hit the error, possibly on several threads at
+ * once, and must not call back into the library.  Host only. */
+#define VH_LOG_ERROR 2
+typedef void (*vh_log_fn)(int32_t level, const char *message, void *user);
+void vh_set_log_callback(vh_log_fn fn, void *user);
+
 /* ---- per-frame path (GpuTsdfGenerator::processFrame) ---------------------- */
 
 /* Allocation + integration of one frame: replaces the HashAssign and

@@ -102,3 +102,32 @@ def test_tuning_variant_counts():
     from vhsdf import _native as N
     assert Volume.tuning_variants() == (6, 3)
     N.lib().vh_tuning_variants(None, None)
+
+
+def test_log_callback_receives_create_failures():
+    """vh_set_log_callback: a vh_create that fails before a handle exists
+    (device index 99: no device here, out of range on a GPU machine) reports
+    its reason to the callback; removing the callback stops the messages."""
+    import vhsdf
+    from vhsdf import _native as N
+    got = []
+    vhsdf.set_log_callback(lambda level, msg: got.append((level, msg)))
+    try:
+        L = N.lib()
+        p = N.VhParams()
+        L.vh_params_default(C.byref(p))
+        p.device = 99
+        h = C.c_void_p()
+        st = L.vh_create(C.byref(p), C.byref(h))
+        assert st in (N.VH_ERR_NO_DEVICE, N.VH_ERR_INVALID_ARG)
+        assert len(got) == 1 and got[0][0] == N.VH_LOG_ERROR
+        assert "vh_create" in got[0][1] and ("no CUDA device" in got[0][1] or "out of range" in got[0][1])
+        q = N.VhParams()
+        L.vh_params_default(C.byref(q))
+        q.voxel_size = 0.0
+        assert L.vh_create(C.byref(q), C.byref(h)) != N.VH_OK
+        assert len(got) == 2 and "invalid parameters" in got[1][1]
+    finally:
+        vhsdf.set_log_callback(None)
+    L.vh_create(C.byref(p), C.byref(h))
+    assert len(got) == 2

@@ -88,6 +88,26 @@ def test_bad_arguments(scene):
     assert e.value.status == N.VH_ERR_UNSUPPORTED
 
 
+def test_log_callback_sees_handle_and_device_errors(scene):
+    """The log callback receives a handle's argument errors with the text
+    vh_last_error returns, and a sticky device error (frame-list overflow)
+    when the handle reports it."""
+    import vhsdf
+    got = []
+    vhsdf.set_log_callback(lambda level, msg: got.append((level, msg)))
+    try:
+        vol = volume_for(scene)
+        L = N.lib()
+        assert L.vh_integrate(vol._h, None, 0, None, None, 0) == N.VH_ERR_INVALID_ARG
+        assert got == [(N.VH_LOG_ERROR, L.vh_last_error(vol._h).decode())]
+        small = volume_for(scene, max_frame_blocks=16)
+        with pytest.raises(VhError):
+            small.integrate(*scene.render(0))
+        assert len(got) == 2 and got[1][1] == L.vh_last_error(small._h).decode()
+    finally:
+        vhsdf.set_log_callback(None)
+
+
 @pytest.mark.parametrize("bad", [2.5, -1.0, np.nan, 2.0 ** 25])
 def test_import_rejects_weights_that_are_not_counts(scene, bad):
     """Weights are observation counts (whole numbers); anything else is

@@ -108,10 +108,36 @@ struct vh_handle {
   vh_stats stage{};
 };
 
+namespace vh {
+namespace {
+std::mutex g_log_mu;
+vh_log_fn g_log_fn = nullptr;
+void *g_log_user = nullptr;
+}  // namespace
+
+void log_error(const std::string &msg) {
+  vh_log_fn fn;
+  void *user;
+  {
+    std::lock_guard<std::mutex> lock(g_log_mu);
+    fn = g_log_fn;
+    user = g_log_user;
+  }
+  if (fn) fn(VH_LOG_ERROR, msg.c_str(), user);  // outside the lock
+}
+
+void set_log(vh_log_fn fn, void *user) {
+  std::lock_guard<std::mutex> lock(g_log_mu);
+  g_log_fn = fn;
+  g_log_user = user;
+}
+}  // namespace vh
+
 namespace {
 
 vh_status fail(vh_handle *h, vh_status s, const std::string &msg) {
   if (h) h->last_error = msg;
+  vh::log_error(msg);
   return s;
 }
 
@@ -686,13 +712,21 @@ vh_status vh_create(const vh_params *p, vh_handle **out) {
   if (!out) return VH_ERR_INVALID_ARG;
   *out = nullptr;
   vh_status vs = vh_params_validate(p);
-  if (vs != VH_OK) return vs;
+  if (vs != VH_OK) {
+    vh::log_error(std::string("vh_create: invalid parameters (") + vh_status_string(vs) + ")");
+    return vs;
+  }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
     cudaGetLastError();
+    vh::log_error("vh_create: no CUDA device");
     return VH_ERR_NO_DEVICE;
   }
-  if (p->device >= ndev) return VH_ERR_INVALID_ARG;
+  if (p->device >= ndev) {
+    vh::log_error("vh_create: device index " + std::to_string(p->device) + " out of range (" +
+              std::to_string(ndev) + " devices)");
+    return VH_ERR_INVALID_ARG;
+  }
   DeviceScope on_device(p->device);  // the caller's current device is restored
   if (!on_device.ok()) return VH_ERR_CUDA;
   vh_handle *h = new vh_handle();
@@ -734,7 +768,7 @@ vh_status vh_create(const vh_params *p, vh_handle **out) {
             cudaHostGetDevicePointer(&h->h_state_dev, h->h_state, 0) == cudaSuccess;
   if (!ok) {
     cudaGetLastError();
-    h->last_error = "device allocation failed";
+    vh::log_error("vh_create: device allocation failed");
     return bail(VH_ERR_CUDA);
   }
   for (int k = 0; k < 2; ++k)
@@ -1291,6 +1325,8 @@ vh_status vh_get_stats(vh_handle *h, vh_stats *out) {
   out->ms_frame = h->stage.ms_frame;
   return s;
 }
+
+void vh_set_log_callback(vh_log_fn fn, void *user) { vh::set_log(fn, user); }
 
 void vh_tuning_variants(int32_t *integrate, int32_t *mc) {
   if (integrate) *integrate = integrate_variants();

@@ -146,6 +146,7 @@ void enqueue_group_step(vh_batch *b, BatchGroup &g, int k, int fmt, bool with_me
 
 vh_status fail(vh_batch *b, vh_status s, const std::string &msg) {
   b->last_error = msg;
+  vh::log_error(msg);
   return s;
 }
 

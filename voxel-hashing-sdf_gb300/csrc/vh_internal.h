@@ -4,6 +4,7 @@
 #include "../../include/vhsdf.h"
 #include "vh_common.cuh"
 
+#include <string>
 #include <vector>
 
 #include <nvtx3/nvToolsExt.h>
@@ -24,6 +25,8 @@ cudaStream_t handle_stream(const vh_handle *h);
 int handle_device(const vh_handle *h);
 // Records `msg` as the handle's last error and returns `s`.
 vh_status handle_fail(vh_handle *h, vh_status s, const char *msg);
+// Passes an error message to the log callback (vh_set_log_callback), if any.
+void log_error(const std::string &msg);
 // Waits for the handle's stream and reports sticky device errors.
 vh_status handle_sync(vh_handle *h);
 CamParams handle_cam(const vh_handle *h);

@@ -120,6 +120,7 @@ SIGNATURES = {
     "vh_get_tuning": (I32, [P, C.POINTER(VhTuning)]),
     "vh_set_tuning": (I32, [P, C.POINTER(VhTuning)]),
     "vh_tuning_variants": (None, [C.POINTER(I32), C.POINTER(I32)]),
+    "vh_set_log_callback": (None, [C.c_void_p, C.c_void_p]),
     "vh_autotune": (I32, [P, P, I32, P, P, I32, C.POINTER(VhTuning)]),
     "vh_sdf_sample": (I32, [P, P, I64, P, P, P, I32]),
     "vh_pose_normal_equations": (I32, [P, P, I32, I32, P, I32, I32, P]),
@@ -197,3 +198,23 @@ def check(status, handle=None):
             if detail:
                 msg = f"{msg}: {detail.decode()}"
         raise VhError(status, msg)
+
+
+VH_LOG_ERROR = 2
+LOG_FN = C.CFUNCTYPE(None, C.c_int32, C.c_char_p, C.c_void_p)
+_log_cb = None  # the installed ctypes callback (kept alive while installed)
+
+
+def set_log_callback(fn):
+    """Installs fn(level, message) as the library's log sink
+    (vh_set_log_callback); None removes it.  fn runs on the thread that hit
+    the error and must not call back into the library."""
+    global _log_cb
+    L = lib()
+    if fn is None:
+        L.vh_set_log_callback(None, None)
+        _log_cb = None
+        return
+    cb = LOG_FN(lambda level, msg, user: fn(int(level), msg.decode(errors="replace")))
+    L.vh_set_log_callback(C.cast(cb, C.c_void_p), None)
+    _log_cb = cb
