@@ -42,7 +42,8 @@ typedef enum vh_status {
   VH_ERR_OUT_OF_RANGE = 8,    /* block coordinate outside the key range     */
   VH_ERR_CAPACITY = 9,        /* an output buffer is too small              */
   VH_ERR_IO = 10,             /* file could not be read or written          */
-  VH_ERR_NO_DEVICE = 11       /* no CUDA device                             */
+  VH_ERR_NO_DEVICE = 11,      /* no CUDA device                             */
+  VH_ERR_CHECK = 12           /* a bounds check of the checked build failed */
 } vh_status;
 
 typedef enum vh_depth_fmt {
@@ -323,6 +324,15 @@ vh_status vh_get_stats(vh_handle *h, vh_stats *out);
 
 vh_status vh_get_tuning(vh_handle *h, vh_tuning *out);
 vh_status vh_set_tuning(vh_handle *h, const vh_tuning *t);
+/* Build flags of the loaded library: VH_BUILD_CHECKED when its per-frame
+ * kernels were compiled with VH_CHECKED (lib/libvhsdf_checked.so): index
+ * checks at every pool, slot, frame-list, pixel and scene access of the
+ * allocation, resolve, integration and marching-cubes kernels, which record
+ * VH_ERR_CHECK in the device error word and skip the access instead of
+ * faulting.  Host only. */
+#define VH_BUILD_CHECKED 1u
+uint32_t vh_build_flags(void);
+
 /* Number of launch shapes: integrate_variant takes 0 .. *integrate - 1 and
  * mc_variant 0 .. *mc - 1 (either pointer may be NULL).  Host only. */
 void vh_tuning_variants(int32_t *integrate, int32_t *mc);

@@ -131,3 +131,18 @@ def test_log_callback_receives_create_failures():
         vhsdf.set_log_callback(None)
     L.vh_create(C.byref(p), C.byref(h))
     assert len(got) == 2
+
+
+def test_checked_build_loads_and_reports_its_flag():
+    """Both builds export every declared entry point; only the checked one
+    reports VH_BUILD_CHECKED."""
+    from vhsdf import _native as N
+    plain = C.CDLL(os.path.join(N.LIB_DIR, "libvhsdf.so"))
+    checked = C.CDLL(os.path.join(N.LIB_DIR, "libvhsdf_checked.so"))
+    for L in (plain, checked):
+        L.vh_build_flags.restype = C.c_uint32
+        for n in declared_functions():
+            assert hasattr(L, n), n
+    assert plain.vh_build_flags() == 0
+    assert checked.vh_build_flags() == N.VH_BUILD_CHECKED
+    assert plain.vh_status_string(N.VH_ERR_CHECK)

@@ -1,6 +1,9 @@
 """Builds the native libraries in-tree with nvcc / g++ (no cmake).
 
     lib/libvhsdf.so        the engine: CUDA kernels for sm_103a + C ABI
+    lib/libvhsdf_checked.so  the same with the per-frame kernels compiled with
+                           VH_CHECKED (index checks that record an error and
+                           skip the access; selected by VHSDF_CHECKED=1)
     lib/libvhsynth.so      synthetic RGB-D scene generator (OpenMP)
     ../oracle/lib/libvh_oracle.so   CPU oracle used by tests and the benchmark
 
@@ -41,6 +44,8 @@ ENGINE_SOURCES = [
 ENGINE_HEADERS = ["vh_common.cuh", "vh_device.cuh", "vh_mc_tables.h", "vh_mesh.h", "vh_internal.h"]
 
 ENGINE_LIB = os.path.join(LIB, "libvhsdf.so")
+CHECKED_LIB = os.path.join(LIB, "libvhsdf_checked.so")
+CHECKED_SOURCE = "vh_kernels.cu"  # where the VH_CHECK sites are
 SYNTH_LIB = os.path.join(LIB, "libvhsynth.so")
 ORACLE_LIB = os.path.join(ORACLE, "lib", "libvh_oracle.so")
 
@@ -71,18 +76,28 @@ def build_engine(force=False):
     headers = [os.path.join(CSRC, h) for h in ENGINE_HEADERS] + [
         os.path.join(REPO, "include", "vhsdf.h")]
     srcs = [os.path.join(CSRC, s) for s, _ in ENGINE_SOURCES]
-    if not force and not _newer(ENGINE_LIB, srcs + headers + [__file__]):
+    deps = srcs + headers + [__file__]
+    if not force and not _newer(ENGINE_LIB, deps) and not _newer(CHECKED_LIB, deps):
         return ENGINE_LIB
     jobs = []
     objs = []
+    checked_objs = []
     for name, extra in ENGINE_SOURCES:
         src = os.path.join(CSRC, name)
         obj = os.path.join(OBJ, name + ".o")
         objs.append(obj)
         jobs.append([nvcc()] + NVCC_COMMON + extra + ["-c", src, "-o", obj])
+        if name == CHECKED_SOURCE:
+            cobj = os.path.join(OBJ, name + ".checked.o")
+            checked_objs.append(cobj)
+            jobs.append([nvcc()] + NVCC_COMMON + extra + ["-DVH_CHECKED", "-c", src, "-o", cobj])
+        else:
+            checked_objs.append(obj)
     with cf.ThreadPoolExecutor(len(jobs)) as ex:
         list(ex.map(_run, jobs))
-    _run([nvcc()] + ARCH + ["-shared", "-o", ENGINE_LIB] + objs)
+    with cf.ThreadPoolExecutor(2) as ex:
+        list(ex.map(_run, [[nvcc()] + ARCH + ["-shared", "-o", ENGINE_LIB] + objs,
+                           [nvcc()] + ARCH + ["-shared", "-o", CHECKED_LIB] + checked_objs]))
     return ENGINE_LIB
 
 

@@ -194,6 +194,10 @@ vh_status status_of_bits(uint32_t bits, std::string &msg) {
     msg = "a bounded device wait gave up";
     return VH_ERR_RETRY_EXHAUSTED;
   }
+  if (bits & kErrCheck) {
+    msg = "an index check of the checked build failed (access skipped)";
+    return VH_ERR_CHECK;
+  }
   return VH_OK;
 }
 
@@ -656,6 +660,7 @@ const char *vh_status_string(vh_status s) {
     case VH_ERR_CAPACITY: return "capacity exceeded";
     case VH_ERR_IO: return "I/O error";
     case VH_ERR_NO_DEVICE: return "no CUDA device";
+    case VH_ERR_CHECK: return "bounds check failed";
   }
   return "unknown status";
 }

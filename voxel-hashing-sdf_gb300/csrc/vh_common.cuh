@@ -43,7 +43,18 @@ enum : uint32_t {
   kErrFrameCap = 8u,
   kErrTriCap = 16u,
   kErrRetry = 32u,
+  kErrCheck = 64u,  // a bounds check of the checked build failed
 };
+
+// Bounds checks of the checked build (compiled with -DVH_CHECKED): a failed
+// check sets kErrCheck in the volume's error word and evaluates to false, so
+// the caller skips the access instead of faulting.  In the normal build the
+// condition is not evaluated and the macro is `true`.
+#ifdef VH_CHECKED
+#define VH_CHECK(st, cond) ((cond) || (atomicOr(&(st)->error, kErrCheck), false))
+#else
+#define VH_CHECK(st, cond) true
+#endif
 
 struct __align__(16) Slot {
   unsigned long long key;

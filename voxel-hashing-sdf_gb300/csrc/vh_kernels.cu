@@ -102,7 +102,11 @@ __device__ uint32_t slot_insert(const VolumeView &V, unsigned long long key, boo
 // Block id for allocation ticket t of the open epoch (free list first).
 __device__ __forceinline__ uint32_t take_block(const VolumeView &V, uint32_t t, uint32_t free0,
                                                uint32_t top0) {
-  if (t < free0) return V.free_list[free0 - 1u - t];
+  if (t < free0) {
+    if (!VH_CHECK(V.st, free0 <= V.pool_cap)) return kNoBlock;
+    const uint32_t b = V.free_list[free0 - 1u - t];
+    return VH_CHECK(V.st, b < V.pool_cap) ? b : kNoBlock;
+  }
   const unsigned long long id = (unsigned long long)top0 + (t - free0);
   if (id >= V.pool_cap) {
     atomicOr(&V.st->error, kErrPoolFull);
@@ -534,7 +538,7 @@ template <int kV>
 __device__ __forceinline__ uint32_t update_run(const CamParams &C, const float P[12],
                                                const uint2 *__restrict__ pix, int ix, float wy,
                                                float wz, float (&sdf)[kV], float (&wt)[kV],
-                                               uint32_t (&rgb)[kV]) {
+                                               uint32_t (&rgb)[kV], DevState *st) {
   float z[kV];
   int idx[kV];
 #pragma unroll
@@ -542,7 +546,8 @@ __device__ __forceinline__ uint32_t update_run(const CamParams &C, const float P
   const uint2 none = make_uint2(0u, 0u);  // depth 0 = invalid
   uint2 px[kV];
 #pragma unroll
-  for (int k = 0; k < kV; ++k) px[k] = idx[k] >= 0 ? __ldg(pix + idx[k]) : none;
+  for (int k = 0; k < kV; ++k)
+    px[k] = idx[k] >= 0 && VH_CHECK(st, idx[k] < C.width * C.height) ? __ldg(pix + idx[k]) : none;
   uint32_t n = 0;
 #pragma unroll
   for (int k = 0; k < kV; ++k) n += update_voxel(C, px[k], z[k], sdf[k], wt[k], rgb[k]);
@@ -603,6 +608,10 @@ __device__ __forceinline__ void load_run(const VolumeView &V, uint32_t i, int t,
   q.key = r.x;
   q.block = (uint32_t)r.y;
   if (q.key >= kTombKey || q.block == kNoBlock) return;
+  if (!VH_CHECK(V.st, q.block < V.pool_cap)) {
+    q.block = kNoBlock;
+    return;
+  }
   const float *base = V.pool + (size_t)q.block * kBlockWords + kV * t;
   load_words<kV>(base, q.sdf);
   load_words<kV>(base + kB3, q.wt);
@@ -625,7 +634,8 @@ __device__ __forceinline__ uint32_t integrate_run(const VolumeView &V, const Cam
   unpack_key(cur.key, bx, by, bz);
   const float wy = (float)(by * kB + y) * C.voxel;
   const float wz = (float)(bz * kB + z) * C.voxel;
-  const uint32_t nu = update_run<kV>(C, P, pix, bx * kB + x0, wy, wz, cur.sdf, cur.wt, cur.rgb);
+  const uint32_t nu =
+      update_run<kV>(C, P, pix, bx * kB + x0, wy, wz, cur.sdf, cur.wt, cur.rgb, V.st);
   if (nu) {
     float *base = V.pool + (size_t)cur.block * kBlockWords + kV * t;
     store_words<kV>(base, cur.sdf);
@@ -897,6 +907,7 @@ __device__ __forceinline__ void mc_block(McShared &S, const VolumeView &V, int s
     own = key < kTombKey ? (uint32_t)r.y : kNoBlock;
   }
   if (own == kNoBlock) return;  // same entry for every thread: uniform
+  if (!VH_CHECK(V.st, own < V.pool_cap)) return;  // uniform as well
   int bx, by, bz;
   unpack_key(key, bx, by, bz);
   if (scope_all && t < 8) {
@@ -933,6 +944,8 @@ __device__ __forceinline__ void mc_block(McShared &S, const VolumeView &V, int s
     uint32_t blk1 = scope_all ? S.nb[nb1] : __ldg(V.frame_nb + 8 * (size_t)i + nb1);
     if (!has0) blk0 = kNoBlock;
     if (h1 >= kHalo) blk1 = kNoBlock;
+    if (!VH_CHECK(V.st, blk0 == kNoBlock || blk0 < V.pool_cap)) blk0 = kNoBlock;
+    if (!VH_CHECK(V.st, blk1 == kNoBlock || blk1 < V.pool_cap)) blk1 = kNoBlock;
     const int li0 = (int)(info0 >> 13), li1 = (int)(info1 >> 13);
     float w0 = 0.f, s0 = nanv, w1 = 0.f, s1 = nanv;
     uint32_t c0 = 0, c1 = 0;
@@ -1127,8 +1140,16 @@ __global__ void k_mc_begin(VolumeView V) {
 // {key, block} and frame_nb[8 i] = the block; k > 0 writes frame_nb[8 i + k]
 // = the block at +(k & 1, k >> 1 & 1, k >> 2) (read by marching cubes).
 __device__ __forceinline__ void resolve_entry(const VolumeView &V, uint32_t i, uint32_t k) {
-  const ulonglong2 sl = __ldg(reinterpret_cast<const ulonglong2 *>(V.slots) + V.frame_list[i]);
-  const uint32_t blk = (uint32_t)(sl.y & 0xFFFFFFFFull);
+  if (!VH_CHECK(V.st, i < V.frame_cap)) return;
+  const uint32_t slot = V.frame_list[i];
+  if (!VH_CHECK(V.st, slot <= V.slot_mask)) {
+    if (k == 0) V.frame_res[i] = make_ulonglong2(kTombKey, (unsigned long long)kNoBlock);
+    V.frame_nb[8 * (size_t)i + k] = kNoBlock;
+    return;
+  }
+  const ulonglong2 sl = __ldg(reinterpret_cast<const ulonglong2 *>(V.slots) + slot);
+  uint32_t blk = (uint32_t)(sl.y & 0xFFFFFFFFull);
+  if (!VH_CHECK(V.st, blk == kNoBlock || blk < V.pool_cap)) blk = kNoBlock;
   if (k == 0) V.frame_res[i] = make_ulonglong2(sl.x, (unsigned long long)blk);
   uint32_t nbid = kNoBlock;
   if (sl.x < kTombKey && blk != kNoBlock) {
@@ -1137,6 +1158,7 @@ __device__ __forceinline__ void resolve_entry(const VolumeView &V, uint32_t i, u
     const int nx = bx + (int)(k & 1u), ny = by + (int)((k >> 1) & 1u), nz = bz + (int)(k >> 2);
     nbid = k == 0 ? blk
                   : (key_in_range(nx, ny, nz) ? block_of(V, pack_key(nx, ny, nz)) : kNoBlock);
+    if (!VH_CHECK(V.st, nbid == kNoBlock || nbid < V.pool_cap)) nbid = kNoBlock;
   }
   V.frame_nb[8 * (size_t)i + k] = nbid;
 }
@@ -1681,3 +1703,13 @@ void launch_batch_clear_errors(const SceneDesc *d, int n, cudaStream_t s) {
 }
 
 }  // namespace vh
+
+// VH_BUILD_CHECKED (include/vhsdf.h) when this file was compiled with the
+// VH_CHECKED bounds checks.
+extern "C" uint32_t vh_build_flags(void) {
+#ifdef VH_CHECKED
+  return 1u;
+#else
+  return 0u;
+#endif
+}

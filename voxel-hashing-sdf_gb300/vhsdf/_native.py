@@ -8,7 +8,10 @@ import os
 
 PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_DIR = os.path.join(PKG, "lib")
-ENGINE_PATH = os.path.join(LIB_DIR, "libvhsdf.so")
+# VHSDF_CHECKED=1 selects the build whose per-frame kernels check every index
+# they derive (errors as VH_ERR_CHECK instead of faults), for debugging.
+ENGINE_PATH = os.path.join(LIB_DIR, "libvhsdf_checked.so" if os.environ.get("VHSDF_CHECKED") == "1"
+                           else "libvhsdf.so")
 SYNTH_PATH = os.path.join(LIB_DIR, "libvhsynth.so")
 
 VH_OK = 0
@@ -23,6 +26,8 @@ VH_ERR_OUT_OF_RANGE = 8
 VH_ERR_CAPACITY = 9
 VH_ERR_IO = 10
 VH_ERR_NO_DEVICE = 11
+VH_ERR_CHECK = 12
+VH_BUILD_CHECKED = 1
 
 VH_DEPTH_U16_MM = 0
 VH_DEPTH_F32_M = 1
@@ -121,6 +126,7 @@ SIGNATURES = {
     "vh_set_tuning": (I32, [P, C.POINTER(VhTuning)]),
     "vh_tuning_variants": (None, [C.POINTER(I32), C.POINTER(I32)]),
     "vh_set_log_callback": (None, [C.c_void_p, C.c_void_p]),
+    "vh_build_flags": (C.c_uint32, []),
     "vh_autotune": (I32, [P, P, I32, P, P, I32, C.POINTER(VhTuning)]),
     "vh_sdf_sample": (I32, [P, P, I64, P, P, P, I32]),
     "vh_pose_normal_equations": (I32, [P, P, I32, I32, P, I32, I32, P]),
