@@ -58,10 +58,14 @@ __device__ __forceinline__ uint32_t ld_volatile(const uint32_t *p) {
   return *(volatile const uint32_t *)p;
 }
 
-// Whole slot in one 16-byte access: {key, block | stamp << 32}.
+// Whole slot in one 16-byte access: {key, block | stamp << 32}, a relaxed
+// GPU-scope load (sees other threads' claims; not cached in L1) with the
+// table's L2 policy.
 __device__ __forceinline__ ulonglong2 ld_volatile_slot(const Slot *p) {
   ulonglong2 r;
-  asm volatile("ld.volatile.global.v2.u64 {%0, %1}, [%2];" : "=l"(r.x), "=l"(r.y) : "l"(p));
+  asm volatile("ld.relaxed.gpu.global.L2::cache_hint.v2.u64 {%0, %1}, [%2], %3;"
+               : "=l"(r.x), "=l"(r.y)
+               : "l"(p), "l"(l2_keep_policy()));
   return r;
 }
 
@@ -1147,7 +1151,7 @@ __device__ __forceinline__ void resolve_entry(const VolumeView &V, uint32_t i, u
     V.frame_nb[8 * (size_t)i + k] = kNoBlock;
     return;
   }
-  const ulonglong2 sl = __ldg(reinterpret_cast<const ulonglong2 *>(V.slots) + slot);
+  const ulonglong2 sl = ld_slot_ro(V.slots + slot);
   uint32_t blk = (uint32_t)(sl.y & 0xFFFFFFFFull);
   if (!VH_CHECK(V.st, blk == kNoBlock || blk < V.pool_cap)) blk = kNoBlock;
   if (k == 0) V.frame_res[i] = make_ulonglong2(sl.x, (unsigned long long)blk);
