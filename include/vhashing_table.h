@@ -10,10 +10,11 @@
  *   erase (bulk)                  include/vhashing.h:244-256
  *   clearheap                     include/vhashing.h:80-91
  *   key_heap / heap_counter       include/vhashing.h:43,55,417-425
- * The reference's device-side members - operator[] (a device reference into
- * a block value) and Filter / Apply (device functors over the table) - have
- * no host counterpart: block contents move through vh_export_blocks /
- * vh_import_blocks, and per-block work belongs in kernels of the engine.
+ * The reference's device-side members - operator[] and find (a device
+ * reference into a block value) and Filter / Apply (device functors over
+ * the table) - are in vhashing_device.cuh, for kernels the caller compiles
+ * with nvcc against the addresses device_table() returns; on the host,
+ * block contents move through vh_export_blocks / vh_import_blocks.
  */
 #ifndef VHASHING_TABLE_H
 #define VHASHING_TABLE_H
@@ -74,6 +75,14 @@ class BlockHashTable {
     int64_t n = 0;
     status_ = vh_block_list(h_, nullptr, 0, &n);
     return n;
+  }
+
+  /* Device addresses of the hash and the block pool for kernels compiled
+   * against vhashing_device.cuh (HashTable's device members). */
+  vh_device_table device_table() {
+    vh_device_table t{};
+    status_ = vh_get_device_table(h_, &t);
+    return t;
   }
 
   vh_status last_status() const { return status_; }

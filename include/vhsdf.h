@@ -291,6 +291,39 @@ vh_status vh_block_list(vh_handle *h, int32_t *xyz, int64_t capacity,
                         int64_t *n);
 /* The reference's BlockHasher (include/tsdf.cuh:144-156) value of a key. */
 uint64_t vh_block_hash_ref(int32_t x, int32_t y, int32_t z);
+
+/* Device addresses of a volume's hash and block pool, for kernels that the
+ * caller compiles against include/vhashing_device.cuh: the device members of
+ * vhashing::HashTable - operator[] and find (include/vhashing.h:122-135,
+ * probe :149-194), Filter (:790-805) and Apply (:818-825) - run as the
+ * caller's own device code on these arrays.  The arrays live as long as the
+ * handle; their contents are those left by the work enqueued on `stream`
+ * before the caller's kernel (order the kernel after it on that stream, or
+ * after a synchronising call).  Inserting or erasing keys stays with the
+ * library's calls; a caller's kernel may rewrite voxel values of live blocks
+ * but must leave slots, keys and ids alone. */
+#define VH_DEVICE_TABLE_LAYOUT 1
+typedef struct vh_device_table {
+  uint32_t layout;            /* VH_DEVICE_TABLE_LAYOUT                       */
+  uint32_t slot_mask;         /* slots - 1 (2^table_log2 slots)               */
+  int32_t max_probe;          /* bound of one linear probe sequence           */
+  int32_t key_bias;           /* packed key: (x + bias) | (y + bias) << 21 |  */
+                              /* (z + bias) << 42, coordinates in [-bias, bias) */
+  void *slots;                /* 16 B each: uint64 key (all ones empty, all   */
+                              /* ones - 1 erased), uint32 pool id, uint32 stamp */
+  float *pool;                /* pool_capacity blocks of 3 * 512 words:       */
+                              /* sdf[512] | weight[512] | rgba8[512], voxel   */
+                              /* index x + 8y + 64z                           */
+  const uint64_t *block_keys; /* packed key of every pool block (all ones:    */
+                              /* free)                                        */
+  const uint32_t *pool_top;   /* device word: ids [0, *pool_top) handed out   */
+  int64_t pool_capacity;
+  float voxel_size;
+  int32_t device;
+  void *stream;               /* cudaStream_t of the handle's work            */
+} vh_device_table;
+/* Fills *out for handle h.  Host only: enqueues nothing. */
+vh_status vh_get_device_table(vh_handle *h, vh_device_table *out);
 /* The marching-cubes tables the engine uses, i.e. the reference's
  * MarchingCubeParam idxMap / edgeTable / triTable (include/tsdf.cuh:234-534):
  * corner[8 * 3] voxel offsets of the cube corners, edge_mask[256] cut edges

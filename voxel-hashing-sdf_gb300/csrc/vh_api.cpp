@@ -1153,6 +1153,25 @@ vh_status vh_block_list(vh_handle *h, int32_t *xyz, int64_t capacity, int64_t *n
 
 uint64_t vh_block_hash_ref(int32_t x, int32_t y, int32_t z) { return ref_block_hash(x, y, z); }
 
+vh_status vh_get_device_table(vh_handle *h, vh_device_table *out) {
+  if (!h || !out) return VH_ERR_INVALID_ARG;
+  static_assert(sizeof(Slot) == 16 && kBlockWords == 3 * VH_BLOCK_VOXELS, "published layout");
+  std::memset(out, 0, sizeof(*out));
+  out->layout = VH_DEVICE_TABLE_LAYOUT;
+  out->slot_mask = h->V.slot_mask;
+  out->max_probe = h->V.max_probe;
+  out->key_bias = kKeyBias;
+  out->slots = h->V.slots;
+  out->pool = h->V.pool;
+  out->block_keys = reinterpret_cast<const uint64_t *>(h->V.block_keys);
+  out->pool_top = &h->V.st->pool_top;
+  out->pool_capacity = h->V.pool_cap;
+  out->voxel_size = h->p.voxel_size;
+  out->device = h->p.device;
+  out->stream = h->stream;
+  return VH_OK;
+}
+
 vh_status vh_mc_tables(int32_t *corner, int32_t *edge_mask, int32_t *tri) {
   for (int k = 0; corner && k < 8; ++k)
     for (int a = 0; a < 3; ++a) corner[3 * k + a] = kMcCorner[k][a];

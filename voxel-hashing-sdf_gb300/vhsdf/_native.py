@@ -86,6 +86,16 @@ class VhMeshView(C.Structure):
                 ("voxel_size", C.c_float)]
 
 
+class VhDeviceTable(C.Structure):
+    _fields_ = [("layout", C.c_uint32), ("slot_mask", C.c_uint32), ("max_probe", C.c_int32),
+                ("key_bias", C.c_int32), ("slots", C.c_void_p), ("pool", C.c_void_p),
+                ("block_keys", C.c_void_p), ("pool_top", C.c_void_p),
+                ("pool_capacity", C.c_int64), ("voxel_size", C.c_float), ("device", C.c_int32),
+                ("stream", C.c_void_p)]
+
+
+VH_DEVICE_TABLE_LAYOUT = 1
+
 P = C.c_void_p
 I32 = C.c_int32
 I64 = C.c_int64
@@ -116,6 +126,7 @@ SIGNATURES = {
     "vh_clear_block_list": (I32, [P]),
     "vh_block_list": (I32, [P, P, I64, PI64]),
     "vh_block_hash_ref": (C.c_uint64, [I32, I32, I32]),
+    "vh_get_device_table": (I32, [P, C.POINTER(VhDeviceTable)]),
     "vh_mc_tables": (I32, [P, P, P]),
     "vh_export_blocks": (I32, [P, P, P, P, P, I64, PI64]),
     "vh_import_blocks": (I32, [P, P, P, P, P, I64]),

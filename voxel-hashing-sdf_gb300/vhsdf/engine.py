@@ -324,6 +324,14 @@ class Volume:
         self._check(self._L.vh_block_list(self._h, out.ctypes.data, n.value, C.byref(n)))
         return out
 
+    def device_table(self):
+        """The vh_device_table of this volume (device addresses of the hash
+        and the block pool) for kernels compiled against
+        include/vhashing_device.cuh."""
+        t = N.VhDeviceTable()
+        self._check(self._L.vh_get_device_table(self._h, C.byref(t)))
+        return t
+
     # ---- gradients and pose refinement ----
     def sdf_sample(self, xyz):
         """Trilinear sdf (units of T), gradient (per metre) and validity at
