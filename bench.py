@@ -365,6 +365,29 @@ def batch_specs(num_scenes, small=False):
     return out
 
 
+def _timed_batch(params, frames, prepared, with_mesh):
+    """One batch over `params`: warm-up step (graph capture), volumes reset,
+    then the prepared steps through the C ABI, timed by the host clock
+    between device synchronisations.  Returns (seconds, status, stats)."""
+    from vhsdf import Batch
+    from vhsdf import _native as N
+    L = N.lib()
+    batch = Batch(params)
+    batch.process([fr[0] for fr in frames], with_mesh=with_mesh, depth_format="u16")
+    batch.sync()
+    for i in range(len(params)):
+        batch.scene(i).reset()
+    batch.sync()
+    t0 = time.perf_counter()
+    for dp, cp, poses in prepared:
+        N.check(L.vh_batch_process(batch._b, dp, N.VH_DEPTH_U16_MM, cp, poses.ctypes.data,
+                                   N.VH_MEM_DEVICE, 1 if with_mesh else 0))
+    status, bstats = batch.sync()
+    t = time.perf_counter() - t0
+    batch.close()
+    return t, status, bstats
+
+
 def batched_leg(num_scenes, steps, local, small=False):
     """Many uneven scenes in one persistent launch per stage (vh_batch) vs the
     same frames through one handle per scene (one per-frame graph each).
@@ -426,6 +449,10 @@ def batched_leg(num_scenes, steps, local, small=False):
     batch.sync()
     t_batch_py = time.perf_counter() - t0
     batch.close()
+    # the whole step as one persistent launch (VH_FLAG_BATCH_FUSED)
+    t_fused, fstatus, fstats = _timed_batch(
+        [dict(prm, device=local, flags=N.VH_FLAG_BATCH_FUSED) for _, _, prm in specs], frames,
+        prepared, False)
     vols = [Volume(**dict(prm, device=local)) for _, _, prm in specs]
     for v, fr in zip(vols, frames):
         v.integrate(*fr[0], depth_format="u16")
@@ -465,6 +492,9 @@ def batched_leg(num_scenes, steps, local, small=False):
     t_seq_py = time.perf_counter() - t0
     same = all(b["blocks_allocated"] == q["blocks_allocated"]
                and b["voxels_updated"] == q["voxels_updated"] for b, q in zip(bstats, sstats))
+    same_fused = all(b["blocks_allocated"] == q["blocks_allocated"]
+                     and b["voxels_updated"] == q["voxels_updated"]
+                     for b, q in zip(fstats, sstats))
     for v in vols:
         v.close()
     extraction = None
@@ -488,6 +518,13 @@ def batched_leg(num_scenes, steps, local, small=False):
                                         "per_scene_graphs_frames_per_s": total / t_seq_py,
                                         "speedup": t_seq_py / t_batch_py},
             "counts_equal_per_scene": same,
+            "one_persistent_launch": {
+                "what": "VH_FLAG_BATCH_FUSED: the step's allocation, resolve and integration of "
+                        "every scene in one persistent launch (after a one-CTA begin kernel)",
+                "frames_per_s": total / t_fused, "speedup_vs_per_scene_graphs": t_seq / t_fused,
+                "vs_staged_batch": t_batch / t_fused,
+                "status_ok": all(x == 0 for x in fstatus),
+                "counts_equal_per_scene": same_fused},
             "voxel_updates_per_s": sum(b["voxels_updated"] for b in bstats) / t_batch,
             "launches_per_step": {
                 "batched": 4 * min(16, num_scenes),  # frame_begin, allocate, resolve, integrate per group
@@ -557,6 +594,8 @@ def _batched_extraction(specs, frames, steps, local):
     status, bstats = batch.sync()
     t_batch = time.perf_counter() - t0
     batch.close()
+    t_fused, fstatus, fstats = _timed_batch(
+        [dict(prm, flags=N.VH_FLAG_BATCH_FUSED) for prm in params], frames, prepared, True)
     total = sum(len(fr) for fr in frames)
     return {"what": "allocate -> integrate -> per-frame marching cubes per frame, meshes left "
                     "on the device",
@@ -564,6 +603,11 @@ def _batched_extraction(specs, frames, steps, local):
             "speedup": t_seq / t_batch, "status_ok": all(x == 0 for x in status),
             "last_mesh_triangles_equal_per_scene":
                 [int(b["triangles"]) for b in bstats] == seq_tris,
+            "one_persistent_launch": {
+                "frames_per_s": total / t_fused, "speedup_vs_per_scene_graphs": t_seq / t_fused,
+                "status_ok": all(x == 0 for x in fstatus),
+                "last_mesh_triangles_equal_per_scene":
+                    [int(b["triangles"]) for b in fstats] == seq_tris},
             "triangles_last_step": sum(seq_tris)}
 
 

@@ -68,6 +68,9 @@ typedef enum vh_scope {
 #define VH_FLAG_DEPTH_FILTER 0x8u /* bilateral pre-filter of every depth    */
                                   /* frame (not the reference's rule; see    */
                                   /* vh_filter_depth)                        */
+#define VH_FLAG_BATCH_FUSED 0x10u /* batches only (scene 0's flags): a step */
+                                  /* is one persistent launch over every     */
+                                  /* stage of every scene (vh_batch_create)  */
 
 /*
  * Volume and camera parameters.  Replaces the arguments of
@@ -465,6 +468,14 @@ typedef struct vh_batch vh_batch;
  * from step to step independently (vh_batch_sync joins them).  The launch
  * shapes follow the first scene's tuning (vh_set_tuning / vh_autotune on
  * vh_batch_scene(b, 0)). */
+/* With VH_FLAG_BATCH_FUSED in params[0].flags the scenes form one group and
+ * a step is one persistent launch (after a one-CTA begin kernel): its CTAs
+ * take work items - 1024 pixels of allocation, 128 list entries of resolve,
+ * 8 blocks of integration, 2 blocks of marching cubes - from whichever
+ * scene has some in its current stage, and the CTA that finishes a scene's
+ * stage opens its next one, so one scene's allocation overlaps another's
+ * integration inside the launch.  Results are the same either way; the
+ * launch shapes then come from that kernel's occupancy, not the tuning. */
 vh_status vh_batch_create(const vh_params *params, int32_t n, vh_batch **out);
 vh_status vh_batch_destroy(vh_batch *b);
 int32_t vh_batch_size(const vh_batch *b);

@@ -7,6 +7,7 @@ import pytest
 
 from helpers import assert_same_blocks, oracle_for, sort_rows, tri_rows
 from vhsdf import Batch, VhError, Volume, synth
+from vhsdf import _native as N
 
 pytestmark = pytest.mark.gpu
 
@@ -30,12 +31,18 @@ def scene_params(kind, seed, w, h, voxel, tlog, frames):
     return sc, prm
 
 
-@pytest.fixture(scope="module")
-def runs(gpu):
+# Both step forms: a launch per stage and scene group, and one persistent
+# launch over every stage of every scene (VH_FLAG_BATCH_FUSED).
+MODES = {"staged": 0, "fused": N.VH_FLAG_BATCH_FUSED}
+
+
+@pytest.fixture(scope="module", params=sorted(MODES))
+def runs(gpu, request):
     scenes = [scene_params(*s) for s in SCENES]
     frames = [[sc.render(f) for f in range(s[-1])] for (sc, _), s in zip(scenes, SCENES)]
     steps = max(s[-1] for s in SCENES)
-    batch = Batch([prm for _, prm in scenes])
+    flags = [dict(prm, flags=N.VH_FLAG_SYNC | MODES[request.param]) for _, prm in scenes]
+    batch = Batch(flags)
     batch_meshes = [[] for _ in SCENES]
     for k in range(steps):
         step = [fr[k] if k < len(fr) else None for fr in frames]
@@ -97,9 +104,11 @@ def test_scene_handles_stay_usable(runs):
         assert vol.stats()["blocks_allocated"] == singles[i].stats()["blocks_allocated"]
 
 
-def test_pool_overflow_is_reported_per_scene(gpu):
+@pytest.mark.parametrize("mode", sorted(MODES))
+def test_pool_overflow_is_reported_per_scene(gpu, mode):
     sc_a, prm_a = scene_params(1, 0, 160, 120, 0.02, 16, 2)
     sc_b, prm_b = scene_params(3, 104, 160, 120, 0.02, 16, 2)
+    prm_a["flags"] = N.VH_FLAG_SYNC | MODES[mode]
     prm_b["pool_blocks"] = 64  # far too small
     batch = Batch([prm_a, prm_b])
     with pytest.raises(VhError) as err:  # synchronous handles: the step reports the first error
@@ -130,4 +139,30 @@ def test_retuning_scene_zero_rebuilds_the_batch_graph(gpu):
             v.process_frame(*fr[k])
     for i, v in enumerate(singles):
         assert_same_blocks(batch.scene(i).export_blocks(), v.export_blocks())
+    batch.close()
+
+
+def test_fused_steps_without_meshes_and_with_idle_scenes(gpu):
+    """The persistent step without extraction, with scenes that have no
+    frame in some steps and a scene whose frames miss the volume entirely
+    (no valid depth: an empty frame list), equals per-scene handles."""
+    specs = [scene_params(*s) for s in SCENES[:4]]
+    frames = [[sc.render(f) for f in range(3)] for sc, _ in specs]
+    d, c, p = frames[3][0]
+    empty = (np.zeros_like(d), c, p)
+    batch = Batch([dict(prm, flags=N.VH_FLAG_SYNC | N.VH_FLAG_BATCH_FUSED) for _, prm in specs])
+    singles = [Volume(**prm) for _, prm in specs]
+    plan = [[0, 1, 2, 3], [0, 2], [1, 3, 0]]
+    for k, which in enumerate(plan):
+        step = [None] * len(specs)
+        for i in which:
+            step[i] = empty if (i == 3 and k == 0) else frames[i][k]
+        batch.process(step, with_mesh=False)
+        status, stats = batch.sync()
+        assert status == [0] * len(specs)
+        for i in which:
+            singles[i].integrate(*step[i])
+    for i, v in enumerate(singles):
+        assert_same_blocks(batch.scene(i).export_blocks(), v.export_blocks())
+        assert batch.scene(i).stats()["blocks_allocated"] == v.stats()["blocks_allocated"]
     batch.close()

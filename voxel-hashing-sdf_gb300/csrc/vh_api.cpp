@@ -708,7 +708,8 @@ vh_status vh_params_validate(const vh_params *p) {
   if (p->max_triangles < 0 || p->max_triangles > 0x7FFFFFFF / 3) return VH_ERR_INVALID_ARG;
   if (p->device < 0) return VH_ERR_INVALID_ARG;
   if (p->flags &
-      ~(uint32_t)(VH_FLAG_SYNC | VH_FLAG_NO_GRAPH | VH_FLAG_PROFILE | VH_FLAG_DEPTH_FILTER))
+      ~(uint32_t)(VH_FLAG_SYNC | VH_FLAG_NO_GRAPH | VH_FLAG_PROFILE | VH_FLAG_DEPTH_FILTER |
+                  VH_FLAG_BATCH_FUSED))
     return VH_ERR_INVALID_ARG;
   return VH_OK;
 }

@@ -18,6 +18,11 @@
 // latency-bound allocation overlapping another's issue-bound integration.
 // The per-step descriptor blocks live in a ring on the device; a block is
 // rewritten only after every group has finished the step that read it.
+//
+// With VH_FLAG_BATCH_FUSED the scenes form one group whose step is one
+// persistent launch over all stages of all scenes (k_batch_step): one
+// scene's latency-bound allocation overlaps another's issue-bound
+// integration inside that launch instead of across group streams.
 
 #include <algorithm>
 #include <cmath>
@@ -72,6 +77,10 @@ struct vh_batch {
   DevState *d_states = nullptr;  // n
   DevState *h_states = nullptr;  // pinned, n
   int graph_shape[3] = {0, 0, -1};  // integrate grid, MC grid, MC variant the graphs hold
+  bool fused = false;                // VH_FLAG_BATCH_FUSED: one persistent launch per step
+  StepSched *d_sched = nullptr;      // fused: per-scene work hand-out (n)
+  StepGlobal *d_glob = nullptr;      // fused: scenes left in the step
+  int step_grid[2] = {0, 0};         // fused: persistent CTAs without / with meshes
   std::string last_error;
 
   unsigned char *block(int k) const { return d_block + block_bytes * (size_t)k; }
@@ -103,6 +112,8 @@ void free_batch(vh_batch *b) {
     if (h) vh_destroy(h);
   cudaFree(b->d_block);
   cudaFree(b->d_static);
+  cudaFree(b->d_sched);
+  cudaFree(b->d_glob);
   for (BatchGroup &g : b->groups) {
     cudaFree(g.d_px_start);
     cudaFree(g.d_prefix);
@@ -137,6 +148,11 @@ void enqueue_group_step(vh_batch *b, BatchGroup &g, int k, int fmt, bool with_me
   const SceneDesc *d = b->desc(k) + g.s0;
   const uint8_t *act = b->active(k) + g.s0;
   cudaStream_t s = g.stream;
+  if (b->fused) {
+    launch_batch_step(d, act, g.n, b->d_sched, b->d_glob, fmt, with_mesh,
+                      b->step_grid[with_mesh ? 1 : 0], s);
+    return;
+  }
   launch_batch_frame_begin(d, act, g.n, s);
   launch_batch_allocate(d, act, g.d_px_start, g.total_px, g.n, fmt, s);
   launch_batch_resolve(d, act, g.n, g.d_prefix, with_mesh, b->sm_count * 2, s);
@@ -197,7 +213,8 @@ vh_status vh_batch_create(const vh_params *params, int32_t n, vh_batch **out) {
     all_px += spx[i];
   }
   // contiguous groups of about equal pixel count, at least one scene each
-  const int ng = std::min(kMaxGroups, n);
+  b->fused = (params[0].flags & VH_FLAG_BATCH_FUSED) != 0;
+  const int ng = b->fused ? 1 : std::min(kMaxGroups, n);
   b->groups.resize(ng);
   for (int g = 0, i = 0; g < ng; ++g) {
     BatchGroup &G = b->groups[g];
@@ -220,6 +237,14 @@ vh_status vh_batch_create(const vh_params *params, int32_t n, vh_batch **out) {
             cudaMalloc(&b->d_states, sizeof(DevState) * n) == cudaSuccess &&
             cudaMallocHost(&b->h_states, sizeof(DevState) * n) == cudaSuccess &&
             cudaEventCreateWithFlags(&b->joined, cudaEventDisableTiming) == cudaSuccess;
+  if (ok && b->fused) {
+    ok = cudaMalloc(&b->d_sched, sizeof(StepSched) * n) == cudaSuccess &&
+         cudaMalloc(&b->d_glob, sizeof(StepGlobal)) == cudaSuccess &&
+         cudaMemset(b->d_sched, 0, sizeof(StepSched) * n) == cudaSuccess &&
+         cudaMemset(b->d_glob, 0, sizeof(StepGlobal)) == cudaSuccess;
+    b->step_grid[0] = b->sm_count * batch_step_ctas_per_sm(false);
+    b->step_grid[1] = b->sm_count * batch_step_ctas_per_sm(true);
+  }
   for (auto &e : b->ring_ev)
     ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
   for (BatchGroup &G : b->groups) {

@@ -158,6 +158,25 @@ struct SceneDesc {
 constexpr int kMaxBatchScenes = 1024;
 constexpr int kBatchPixelThreads = 256;  // threads of a batched allocation CTA
 
+// Work hand-out of a batched step run as one persistent launch
+// (k_batch_step): per scene, the stage it is in and the next ticket of that
+// stage in one 64-bit word, so that taking a ticket and learning which stage
+// it belongs to is one atomic.  Stages: 0 allocation, 1 frame-list resolve,
+// 2 integration, 3 marching cubes, 4 (kStepDone) finished or no frame.
+constexpr uint32_t kStepDone = 4;
+struct StepSched {
+  unsigned long long word;  // stage << 32 | next ticket of that stage
+  uint32_t total[4];        // items of each stage (written before it opens)
+  uint32_t done[4];         // finished items of each stage
+  uint32_t count;           // frame-list length after allocation
+  uint32_t pad[3];
+};
+struct StepGlobal {
+  uint32_t remaining;  // scenes of the step not finished yet
+  uint32_t gave_up;    // CTAs that stopped waiting for work (a bug: never expected)
+  uint32_t pad[2];
+};
+
 // The inputs of one frame as the kernels find them on the device: the
 // camera pose and where the depth and colour images live (the caller's own
 // device buffers, or the handle's staging copy of host images).  Written per
@@ -244,5 +263,14 @@ void launch_batch_gather_state(const SceneDesc *d, int n, DevState *out, cudaStr
 int batch_integrate_ctas_per_sm();
 int batch_mc_ctas_per_sm(int variant);
 void launch_batch_clear_errors(const SceneDesc *d, int n, cudaStream_t s);
+// A whole batched step as one persistent launch (after a one-CTA begin
+// kernel that opens every active scene's frame and resets the hand-out):
+// allocation, resolve, integration and, with with_mesh, marching cubes of
+// every active scene, CTAs taking work items of whichever scene has some.
+// sched: n entries; glob: one.  n <= kMaxBatchScenes.  grid: persistent
+// CTAs (SMs x batch_step_ctas_per_sm; progress does not depend on it).
+void launch_batch_step(const SceneDesc *d, const uint8_t *active, int n, StepSched *sched,
+                       StepGlobal *glob, int fmt, bool with_mesh, int grid, cudaStream_t s);
+int batch_step_ctas_per_sm(bool with_mesh);
 
 }  // namespace vh

@@ -1368,6 +1368,309 @@ __global__ void k_batch_clear_errors(const SceneDesc *__restrict__ d, int n) {
   if (s < n) d[s].V.st->error = 0;
 }
 
+// ---- batched step in one persistent launch ------------------------------------------
+// k_batch_step runs a whole batched step: the per-scene stage chain
+// allocate -> resolve -> integrate [-> marching cubes] of every active scene
+// in one launch of persistent 128-thread CTAs.  Each stage of a scene is cut
+// into items; a CTA takes a ticket of whichever scene has items left in its
+// current stage (StepSched::word), runs the item with the single-scene
+// bodies (allocate_pixel, resolve_entry, integrate_run, mc_block), and the
+// CTA that finishes a stage's last item opens the scene's next stage.  A
+// scene's stages therefore follow one another as in separate launches while
+// different scenes' stages overlap on the GPU.
+//
+// No CTA ever waits while holding an item: a ticket is taken only from an
+// open stage, whose earlier stages are complete, and an idle CTA polls
+// (bounded) until it finds an item or every scene is finished.  So the
+// lowest unfinished item always runs and the launch ends whatever the
+// residency.  Ordering between stages: every thread fences its writes, the
+// CTA arrives on the stage's counter after a barrier, and the opener fences
+// again before publishing the next stage; data written in one stage is read
+// in a later one only, never cached before it was written (allocation reads
+// slots through L2-coherent loads and the counters it reads do not change
+// during the stage; the epoch is closed with volatile accesses).
+constexpr int kStepThreads = 128;
+constexpr int kStepPixels = 8 * kStepThreads;  // pixels per allocation item
+constexpr int kStepEntries = kStepThreads;     // frame-list entries per resolve item
+constexpr int kStepBlocks = 8;                 // listed blocks per integration item
+constexpr int kStepMcBlocks = 2;               // listed blocks per marching-cubes item
+// An idle CTA gives up after this long without finding work while scenes
+// are unfinished (never expected; the scenes left get kErrRetry).
+constexpr unsigned long long kStepIdleLimitNs = 2000000000ull;
+constexpr uint32_t kStepMaxPolls = 1u << 24;  // and after this many idle polls
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+template <bool kMesh>
+struct StepShared;
+template <>
+struct StepShared<true> {
+  McShared mc;  // allocation items borrow its staging words for their key lists
+  __device__ unsigned long long *keys(int warp) {
+    return reinterpret_cast<unsigned long long *>(mc.sdf) + warp * (32 * kAllocChunk);
+  }
+};
+template <>
+struct StepShared<false> {
+  unsigned long long k[kStepThreads / 32][32 * kAllocChunk];
+  __device__ unsigned long long *keys(int warp) { return k[warp]; }
+};
+static_assert(offsetof(McShared, rgb) == sizeof(float) * kStaged &&
+                  (kStepThreads / 32) * 32 * kAllocChunk * sizeof(unsigned long long) <=
+                      2 * sizeof(float) * kStaged,
+              "allocation keys fit in the MC staging words");
+
+// Opens the frame of every active scene and resets the step's hand-out
+// (one CTA, a thread per scene, n <= blockDim.x <= 1024).
+__global__ void k_batch_step_begin(const SceneDesc *__restrict__ d,
+                                   const uint8_t *__restrict__ active, int n,
+                                   StepSched *__restrict__ sched, StepGlobal *__restrict__ glob) {
+  const int s = threadIdx.x;
+  const bool act = s < n && active[s];
+  if (s < n) {
+    StepSched &q = sched[s];
+    for (int k = 0; k < 4; ++k) {
+      q.total[k] = 0;
+      q.done[k] = 0;
+    }
+    q.count = 0;
+    if (act) {
+      frame_begin_state(d[s].V);
+      const uint32_t npx = (uint32_t)d[s].C.width * (uint32_t)d[s].C.height;
+      q.total[0] = (npx + kStepPixels - 1) / kStepPixels;
+      q.word = 0ull;  // stage 0 (allocation), ticket 0
+    } else {
+      q.word = (unsigned long long)kStepDone << 32;
+    }
+  }
+  const int nact = __syncthreads_count(act);
+  if (s == 0) {
+    glob->remaining = (uint32_t)nact;
+    glob->gave_up = 0;
+  }
+}
+
+__device__ __forceinline__ uint32_t ld_vol32(const uint32_t *p) {
+  return *(volatile const uint32_t *)p;
+}
+
+// A ticket of an open stage of some scene, looking at scenes from `hint`
+// on (thread 0 only).  Returns false when no scene has a free ticket now.
+__device__ __forceinline__ bool step_pick(StepSched *sched, int n, int hint, int *s_out, uint32_t *stage_out,
+                          uint32_t *item_out) {
+  for (int r = 0; r < n; ++r) {
+    int s = hint + r;
+    if (s >= n) s -= n;
+    StepSched &q = sched[s];
+    const unsigned long long w = ld_volatile(&q.word);
+    const uint32_t st = (uint32_t)(w >> 32);
+    if (st >= kStepDone || (uint32_t)w >= ld_vol32(&q.total[st])) continue;  // a hint only
+    const unsigned long long got = atomicAdd(&q.word, 1ull);
+    __threadfence();  // the stage's totals after the ticket
+    const uint32_t st2 = (uint32_t)(got >> 32), it = (uint32_t)got;
+    if (st2 < kStepDone && it < ld_vol32(&q.total[st2])) {
+      *s_out = s;
+      *stage_out = st2;
+      *item_out = it;
+      return true;
+    }
+  }
+  return false;
+}
+
+// The allocation epoch of a scene closed as reconcile_epoch does (and the
+// marching-cubes counters reset as mc_begin_state does), with volatile
+// accesses: this launch's allocation items may have left the state's line
+// in this SM's L1 before the tickets were counted.
+__device__ __forceinline__ void step_close_epoch(const VolumeView &V, bool mesh) {
+  volatile DevState *st = V.st;
+  const uint32_t t = st->ticket;
+  if (t) {
+    const uint32_t free_count = st->free_count, pool_top = st->pool_top;
+    const uint32_t from_free = min(t, free_count);
+    st->free_count = free_count - from_free;
+    const unsigned long long top = (unsigned long long)pool_top + (t - from_free);
+    const uint32_t new_top = (uint32_t)min(top, (unsigned long long)V.pool_cap);
+    st->new_blocks = st->new_blocks + from_free + (new_top - pool_top);
+    st->pool_top = new_top;
+    st->ticket = 0;
+  }
+  if (mesh) {
+    st->tri_count = 0;
+    st->mc_next = 0;
+  }
+}
+
+// Called by thread 0 after the CTA finished item of `stage` of scene `s`
+// (all its threads fenced, then a barrier): counts the item and, for the
+// stage's last one, opens the scene's next non-empty stage.
+__device__ __forceinline__ void step_finish(const VolumeView &V, StepSched &q, uint32_t stage, bool mesh,
+                            StepGlobal *glob) {
+  __threadfence();
+  const uint32_t total = ld_vol32(&q.total[stage]);
+  if (atomicAdd(&q.done[stage], 1u) + 1u != total) return;
+  __threadfence();  // every item of the stage, before what the opener reads
+  if (stage == 0) {
+    step_close_epoch(V, mesh);
+    const uint32_t c = min(ld_vol32(&V.st->frame_count), V.frame_cap);
+    q.count = c;
+    q.total[1] = (c + kStepEntries - 1) / kStepEntries;
+    q.total[2] = (c + kStepBlocks - 1) / kStepBlocks;
+    q.total[3] = mesh ? (c + kStepMcBlocks - 1) / kStepMcBlocks : 0u;
+  }
+  uint32_t next = stage + 1;
+  while (next < kStepDone && ld_vol32(&q.total[next]) == 0u) ++next;
+  __threadfence();  // totals and the closed epoch before the stage opens
+  atomicExch(&q.word, (unsigned long long)next << 32);
+  if (next == kStepDone) atomicSub(&glob->remaining, 1u);
+}
+
+// Stage bodies of k_batch_step.
+template <typename DepthT>
+__device__ __forceinline__ void step_allocate(const SceneDesc &sd, uint32_t item,
+                                           unsigned long long *wkeys) {
+  const int base = (int)(item * (uint32_t)kStepPixels) + (int)threadIdx.x;
+#pragma unroll 1
+  for (int r = 0; r < kStepPixels / kStepThreads; ++r)
+    allocate_pixel<DepthT>(sd.V, sd.C, static_cast<const DepthT *>(sd.depth), sd.rgb, sd.pose,
+                           sd.pix, base + r * kStepThreads, wkeys);
+}
+
+__device__ __forceinline__ void step_integrate(const SceneDesc &sd, const float *sp, uint32_t item,
+                                            uint32_t count) {
+  float P[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) P[k] = sp[k];
+  uint32_t updated = 0;
+  const uint32_t i0 = item * (uint32_t)kStepBlocks;
+  const uint32_t i1 = min(i0 + (uint32_t)kStepBlocks, count);
+#pragma unroll 1
+  for (uint32_t i = i0; i < i1; ++i) {
+    VoxelRun<4> q;
+    load_run<4>(sd.V, i, (int)threadIdx.x, q);
+    updated += integrate_run<4>(sd.V, sd.C, P, sd.pix, i, q);
+  }
+  flush_updated(sd, updated);
+}
+
+// Thread 0 picks the CTA's next item.  `spec` is the ticket it took while
+// the previous item ran (StepCta::spec_scene >= 0): a ticket of that item's
+// stage, which cannot close before that item is finished; a valid one is
+// run next.  Otherwise scenes are scanned from the current one on, polling
+// (bounded) while none has a free ticket and some are unfinished.  Returns
+// the scene, or -1 when the step is over.
+struct StepCta {
+  int scene, cur, spec_scene;
+  uint32_t stage, item, count, spec_stage, spec_total;
+};
+
+__device__ __forceinline__ int step_next(StepCta &c, unsigned long long spec,
+                                         const SceneDesc *__restrict__ d, int n,
+                                         StepSched *__restrict__ sched, StepGlobal *glob) {
+  int s = -1;
+  uint32_t stage = 0, item = 0;
+  if (c.spec_scene >= 0) {
+    const uint32_t st2 = (uint32_t)(spec >> 32), it = (uint32_t)spec;
+    if (st2 < kStepDone &&
+        it < (st2 == c.spec_stage ? c.spec_total : ld_vol32(&sched[c.spec_scene].total[st2]))) {
+      s = c.spec_scene;
+      stage = st2;
+      item = it;
+    }
+  }
+  c.spec_scene = -1;
+  const int hint = c.cur >= 0 ? c.cur : (int)(blockIdx.x % (unsigned)n);
+  unsigned long long idle_since = 0;
+  for (uint32_t polls = 0; s < 0; ++polls) {
+    if (step_pick(sched, n, hint, &s, &stage, &item)) break;
+    if (ld_vol32(&glob->remaining) == 0u) break;  // every scene finished
+    const unsigned long long now = global_ns();
+    if (polls == 0) idle_since = now;
+    if (polls >= kStepMaxPolls || now - idle_since > kStepIdleLimitNs) {
+      // never expected: report instead of waiting on
+      atomicAdd(&glob->gave_up, 1u);
+      for (int k = 0; k < n; ++k)
+        if ((uint32_t)(ld_volatile(&sched[k].word) >> 32) < kStepDone)
+          atomicOr(&d[k].V.st->error, kErrRetry);
+      break;
+    }
+    __nanosleep(200);
+  }
+  c.scene = s;
+  c.stage = stage;
+  c.item = item;
+  c.count = s >= 0 ? ld_vol32(&sched[s].count) : 0u;
+  return s;
+}
+
+// Register budget for 8 resident CTAs per SM (64 registers): with every
+// stage body in one loop, budgets for 10-12 CTAs spill 0.2-0.4 KB per thread
+// and measured 4-10 % slower on the batched-scenes workloads.
+template <typename DepthT, bool kMesh>
+__global__ void __launch_bounds__(kStepThreads, 8)
+    k_batch_step(const SceneDesc *__restrict__ d, int n, StepSched *__restrict__ sched,
+                 StepGlobal *__restrict__ glob) {
+  __shared__ __align__(16) StepShared<kMesh> sh;
+  __shared__ SceneDesc sd;
+  __shared__ float sp[12];
+  __shared__ StepCta c;  // the CTA's scheduling state (thread 0 writes it)
+  if constexpr (kMesh) mc_init_shared(sh.mc);
+  if (threadIdx.x == 0) {
+    c.cur = -1;
+    c.spec_scene = -1;
+  }
+  unsigned long long spec = 0;  // thread 0: the ticket taken while an item runs
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const int s = step_next(c, spec, d, n, sched, glob);
+      if (s >= 0) {  // take the following ticket now; it is looked at after this item
+        c.spec_stage = c.stage;
+        c.spec_total = ld_vol32(&sched[s].total[c.stage]);
+        spec = atomicAdd(&sched[s].word, 1ull);
+        c.spec_scene = s;
+      }
+    }
+    __syncthreads();
+    const int s = c.scene;
+    if (s < 0) break;  // uniform
+    if (s != c.cur) {  // uniform; the previous item's barrier freed sd
+      load_scene(sd, d, s);  // ends with a barrier: every thread has compared c.cur
+      if (threadIdx.x < 12) sp[threadIdx.x] = __ldg(sd.pose + threadIdx.x);
+      if (threadIdx.x == 0) c.cur = s;
+      __syncthreads();
+    }
+    const uint32_t stage = c.stage, item = c.item;
+    if (stage == 0) {  // allocation: kStepPixels pixels, every lane of each warp takes part
+      step_allocate<DepthT>(sd, item, sh.keys(threadIdx.x >> 5));
+    } else if (stage == 1) {  // resolve: kStepEntries entries, 8 threads each
+      const uint32_t e0 = item * (uint32_t)kStepEntries, count = c.count;
+#pragma unroll 1
+      for (int r = 0; r < 8; ++r) {
+        const uint32_t g8 = (uint32_t)(r * kStepThreads) + threadIdx.x;
+        const uint32_t e = e0 + (g8 >> 3);
+        if (e < count) resolve_entry(sd.V, e, g8 & 7u);
+      }
+    } else if (stage == 2) {  // integration: kStepBlocks listed blocks
+      step_integrate(sd, sp, item, c.count);
+    } else if constexpr (kMesh) {  // marching cubes: kStepMcBlocks listed blocks
+      const uint32_t i0 = item * (uint32_t)kStepMcBlocks;
+      const uint32_t i1 = min(i0 + (uint32_t)kStepMcBlocks, c.count);
+#pragma unroll 1
+      for (uint32_t i = i0; i < i1; ++i) {
+        if (i > i0) __syncthreads();  // the previous block is done with the shared state
+        mc_block<kStepThreads>(sh.mc, sd.V, 0, sd.C.mc_min_weight, sd.tris, sd.tri_cap, i);
+      }
+    }
+    __threadfence();  // this thread's writes of the item before the CTA arrives
+    __syncthreads();  // also frees the shared state for the next item
+    if (threadIdx.x == 0) step_finish(sd.V, sched[s], stage, kMesh, glob);
+  }
+}
+
 // ---- hash surface -----------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_alloc_keys(VolumeView V, const int32_t *__restrict__ xyz,
                                                     uint32_t n) {
@@ -1704,6 +2007,33 @@ void launch_batch_gather_state(const SceneDesc *d, int n, DevState *out, cudaStr
 }
 void launch_batch_clear_errors(const SceneDesc *d, int n, cudaStream_t s) {
   k_batch_clear_errors<<<grid_for((uint32_t)n, 128), 128, 0, s>>>(d, n);
+}
+
+int batch_step_ctas_per_sm(bool with_mesh) {
+  int n = 0;  // the same for both depth formats
+  if (with_mesh)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_step<uint16_t, true>, kStepThreads, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_step<uint16_t, false>, kStepThreads,
+                                                  0);
+  return n > 0 ? n : 1;
+}
+
+void launch_batch_step(const SceneDesc *d, const uint8_t *active, int n, StepSched *sched,
+                       StepGlobal *glob, int fmt, bool with_mesh, int grid, cudaStream_t s) {
+  if (n < 1 || n > kMaxBatchScenes || grid < 1) return;
+  k_batch_step_begin<<<1, (unsigned)((n + 31) / 32 * 32), 0, s>>>(d, active, n, sched, glob);
+  if (fmt == 0) {
+    if (with_mesh)
+      k_batch_step<uint16_t, true><<<grid, kStepThreads, 0, s>>>(d, n, sched, glob);
+    else
+      k_batch_step<uint16_t, false><<<grid, kStepThreads, 0, s>>>(d, n, sched, glob);
+  } else {
+    if (with_mesh)
+      k_batch_step<float, true><<<grid, kStepThreads, 0, s>>>(d, n, sched, glob);
+    else
+      k_batch_step<float, false><<<grid, kStepThreads, 0, s>>>(d, n, sched, glob);
+  }
 }
 
 }  // namespace vh

@@ -39,6 +39,7 @@ VH_FLAG_SYNC = 0x1
 VH_FLAG_NO_GRAPH = 0x2
 VH_FLAG_PROFILE = 0x4
 VH_FLAG_DEPTH_FILTER = 0x8
+VH_FLAG_BATCH_FUSED = 0x10
 VH_REFINE_BATCH_MAX = 256
 VH_REFINE_ADJOINT = 0
 VH_REFINE_FD = 1
