@@ -12,8 +12,9 @@ generator (no dataset is needed or present).
 Prints one JSON line (rank 0).  `value` is frames/s with the frames already
 in HBM (device time of each step, L2 flushed between steps); `e2e` is the
 same through the C ABI with host buffers (pinned): each frame's depth and
-colour uploaded and its whole triangle mesh copied back to host memory,
-frames submitted back to back (`e2e.sync_per_frame`: one frame at a time;
+colour uploaded and its whole mesh copied back to host memory as vertices
+and faces (`e2e.triangle_soup`: the same triangles as a soup), frames
+submitted back to back (`e2e.sync_per_frame`: one frame at a time;
 `e2e.mesh_left_on_device`: without the mesh copy).
 `--impl reference` times the CPU restatement of the reference's algorithm
 (oracle/) on all host cores on the same workload.
@@ -946,9 +947,37 @@ def run_engine(args):
         vol.sync()
         e2e_s = time.perf_counter() - t0
     vol.close()
+    e2e_soup_s = e2e_s
     e2e_tris = [int(c[0]) for c in mesh_counts[args.warmup:]]
     # the delivered counts are the device pass's, frame for frame
     mesh_counts_match = e2e_tris == [int(s["triangles"]) for s in stage]
+    del mesh_bufs
+    # The same frames with each frame's mesh delivered indexed
+    # (vh_process_frame_indexed: vertices shared within a block, faces as
+    # vertex numbers; the same triangles in about half the bytes).
+    idx_bufs = [(torch.empty((cap, 4), dtype=torch.float32, pin_memory=True).numpy(),
+                 torch.empty((cap, 3), dtype=torch.int32, pin_memory=True).numpy())
+                for _ in range(3)]
+    idx_counts = [np.zeros(2, np.int64) for _ in range(nframes)]
+    vol = Volume(**dict(params, max_triangles=cap))
+    vol.set_tuning(**tuning)
+    vol.set_stream(stream.cuda_stream)
+    with torch.cuda.stream(stream):
+        for i in range(args.warmup):
+            vol.process_frame_indexed(*pinned[i], *idx_bufs[i % 3], idx_counts[i],
+                                      depth_format="u16")
+        vol.sync()
+        t0 = time.perf_counter()
+        for i in range(args.warmup, nframes):
+            vol.process_frame_indexed(*pinned[i], *idx_bufs[i % 3], idx_counts[i],
+                                      depth_format="u16")
+        vol.sync()
+        e2e_idx_s = time.perf_counter() - t0
+    vol.close()
+    del idx_bufs
+    idx_verts = [int(c[0]) for c in idx_counts[args.warmup:]]
+    idx_faces = [int(c[1]) for c in idx_counts[args.warmup:]]
+    idx_counts_match = idx_faces == [int(s["triangles"]) for s in stage]
     # The same with the mesh left on the device (vh_process_frame; only the
     # 64-byte counters reach the host): what the copies cost.
     vol = Volume(**params)
@@ -967,8 +996,8 @@ def run_engine(args):
 
     eviction = (eviction_leg(params, tuning, stream, num=args.eviction_frames)
                 if rank == 0 and args.eviction_frames > 0 else None)
-    dev_ms, e2e_s, e2e_sync_s, e2e_dev_s = replicas.reduce_max(
-        [dev_ms, e2e_s, e2e_sync_s, e2e_dev_s], device="cuda")
+    dev_ms, e2e_idx_s, e2e_soup_s, e2e_sync_s, e2e_dev_s = replicas.reduce_max(
+        [dev_ms, e2e_idx_s, e2e_soup_s, e2e_sync_s, e2e_dev_s], device="cuda")
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
@@ -976,7 +1005,8 @@ def run_engine(args):
 
     frames_total = args.steps * world
     value = frames_total / (dev_ms / 1000.0)
-    e2e = frames_total / e2e_s
+    e2e = frames_total / e2e_idx_s
+    e2e_soup = frames_total / e2e_soup_s
     e2e_sync = frames_total / e2e_sync_s
     e2e_dev = frames_total / e2e_dev_s
     # Rooflines.  Algorithmic bytes per launch:
@@ -1023,15 +1053,26 @@ def run_engine(args):
         "voxel_updates_per_s": sum(updated) * world / (dev_ms / 1000.0),
         "e2e": {"value": e2e, "unit": UNIT,
                 "h2d_bytes_per_step": 2 * npx + 3 * npx + 80,
-                "d2h_bytes_per_step": 48 * statistics.mean(e2e_tris) + 64,
-                "mode": "vh_process_frame_mesh on pinned host frames submitted back to back "
+                "d2h_bytes_per_step": (16 * statistics.mean(idx_verts)
+                                       + 12 * statistics.mean(idx_faces) + 64),
+                "mode": "vh_process_frame_indexed on pinned host frames submitted back to back "
                         "(asynchronous mode, one sync at the end): per frame the depth + RGB "
-                        "upload and the copy of the frame's whole triangle mesh (48 B per "
-                        "triangle) into pinned host memory, plus the 64-byte counters; no L2 "
-                        "flush, the per-frame working set (listed blocks read, triangles "
-                        "written) exceeds L2",
-                "triangles_per_step": statistics.mean(e2e_tris),
-                "mesh_counts_match_device_pass": mesh_counts_match,
+                        "upload and the copy of the frame's whole mesh into pinned host "
+                        "memory as vertices (16 B: xyz f32 + rgb) and faces (3 int32 vertex "
+                        "numbers), the same triangles as the soup below, plus the 64-byte "
+                        "counters; no L2 flush, the per-frame working set (listed blocks "
+                        "read, mesh written) exceeds L2",
+                "vertices_per_step": statistics.mean(idx_verts),
+                "faces_per_step": statistics.mean(idx_faces),
+                "mesh_counts_match_device_pass": idx_counts_match,
+                "triangle_soup": {
+                    "value": e2e_soup,
+                    "mode": "vh_process_frame_mesh: the same frames with each frame's mesh "
+                            "copied as a triangle soup (48 B per triangle), the layout of the "
+                            "reference's per-frame triangle copy",
+                    "d2h_bytes_per_step": 48 * statistics.mean(e2e_tris) + 64,
+                    "triangles_per_step": statistics.mean(e2e_tris),
+                    "mesh_counts_match_device_pass": mesh_counts_match},
                 "sync_per_frame": e2e_sync,
                 "mesh_left_on_device": e2e_dev},
         "roofline": {"bound": "hbm", "achieved": mc_ach, "peak": peak, "unit": "GB/s",

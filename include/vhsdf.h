@@ -224,6 +224,24 @@ vh_status vh_process_frame(vh_handle *h, const void *depth, int32_t depth_fmt,
 vh_status vh_process_frame_mesh(vh_handle *h, const void *depth, int32_t depth_fmt,
                                 const uint8_t *rgb, const float *c2w, int32_t mem, float *tris,
                                 int64_t capacity, int64_t *num_triangles);
+/* vh_process_frame_mesh with the frame's mesh delivered indexed: vertices
+ * (4 floats each: x, y, z in global voxel units and the colour bytes
+ * r | g<<8 | b<<16 in the fourth float's bits, as vh_mesh_view) and faces
+ * (3 int32 vertex numbers each).  The faces are exactly the triangles
+ * vh_process_frame_mesh delivers (same vertices bit for bit, in another
+ * order); marching cubes interpolates each cut lattice edge of a block once
+ * and writes its vertex once per block, so a frame's mesh takes about half
+ * the bytes of the triangle soup - the copy to host memory is what bounds
+ * a stream of frames.  Counts, capacities, the asynchronous protocol
+ * (complete after the second call after the frame, or vh_sync) and
+ * VH_ERR_CAPACITY follow vh_process_frame_mesh; both buffers stay valid
+ * until then.  Two device buffers of max_triangles vertices and faces each
+ * are added on first use. */
+vh_status vh_process_frame_indexed(vh_handle *h, const void *depth, int32_t depth_fmt,
+                                   const uint8_t *rgb, const float *c2w, int32_t mem,
+                                   float *vertices, int64_t vertex_capacity, int32_t *faces,
+                                   int64_t face_capacity, int64_t *num_vertices,
+                                   int64_t *num_faces);
 /* Copies the last extraction to host: xyz (9 floats per triangle, voxel
  * units) and rgb (9 bytes per triangle).  Output copies and size queries
  * (all outputs NULL) follow one rule for every copy-out call here: the full

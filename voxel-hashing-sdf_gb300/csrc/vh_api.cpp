@@ -36,9 +36,11 @@ using namespace vh;
 namespace {
 constexpr int kNumEvents = 5;
 // Marching-cubes mode of a frame graph: none, into the handle's triangle
-// buffer (vh_process_frame, vh_extract), or into mesh slot 0 / 1 of
-// vh_process_frame_mesh.
-enum { kMcNone = 0, kMcMain = 1, kMcSlot0 = 2, kMcSlot1 = 3, kMcModes = 4 };
+// buffer (vh_process_frame, vh_extract), into mesh slot 0 / 1 of
+// vh_process_frame_mesh, or as an indexed mesh into slot 0 / 1 of
+// vh_process_frame_indexed.
+enum { kMcNone = 0, kMcMain = 1, kMcSlot0 = 2, kMcSlot1 = 3, kMcIdx0 = 4, kMcIdx1 = 5,
+       kMcModes = 6 };
 }  // namespace
 
 struct vh_handle {
@@ -81,6 +83,12 @@ struct vh_handle {
   // one frame's copy-out overlaps the next frame's kernels.
   float4 *d_mtris[2] = {nullptr, nullptr};
   int64_t mtri_cap = 0;
+  // Indexed per-frame meshes (vh_process_frame_indexed): vertices and faces
+  // of the two slots (the slots' mirrors, events and stream are shared).
+  float4 *d_mverts[2] = {nullptr, nullptr};
+  int32_t *d_mfaces[2] = {nullptr, nullptr};
+  int64_t midx_cap = 0;  // vertices and faces each slot holds
+  int mcidx_per_sm = 1;
   DevState *h_mstate = nullptr;      // 2 entries, pinned and mapped
   DevState *h_mstate_dev = nullptr;  // their device address
   cudaStream_t mesh_stream = nullptr;
@@ -89,10 +97,14 @@ struct vh_handle {
   int mesh_slot = 0;
   struct PendingMesh {
     bool valid = false;
+    bool indexed = false;  // faces in tris/capacity/count, vertices below
     int slot = 0;
     float *tris = nullptr;
     int64_t capacity = 0;
     int64_t *count = nullptr;
+    float *verts = nullptr;
+    int64_t vcapacity = 0;
+    int64_t *vcount = nullptr;
   } pending;
   bool mesh_overflow = false;  // a frame had more triangles than its host buffer
   cudaEvent_t ev[kNumEvents] = {};
@@ -286,8 +298,15 @@ void enqueue_frame(vh_handle *h, int fmt, int mc, bool events, bool capturing) {
       cap = h->mtri_cap;
       mirror = h->h_mstate_dev + k;
     }
-    launch_mc(h->V, 0, h->C.mc_min_weight, tris, (uint32_t)cap, mc_grid(h), h->tuning.mc_variant,
-              mirror, s);
+    if (mc == kMcIdx0 || mc == kMcIdx1) {
+      const int k = mc - kMcIdx0;
+      launch_mc_indexed(h->V, h->C.mc_min_weight, h->d_mverts[k], (uint32_t)h->midx_cap,
+                        h->d_mfaces[k], (uint32_t)h->midx_cap, h->sm_count * h->mcidx_per_sm,
+                        h->h_mstate_dev + k, s);
+    } else {
+      launch_mc(h->V, 0, h->C.mc_min_weight, tris, (uint32_t)cap, mc_grid(h),
+                h->tuning.mc_variant, mirror, s);
+    }
     ++kernels;
     if (events) stage_event(h->ev[3], s, capturing);
   } else if (mirror) {
@@ -416,6 +435,8 @@ void free_all(vh_handle *h) {
   if (h->mesh_stream) cudaStreamSynchronize(h->mesh_stream);
   for (int k = 0; k < 2; ++k) {
     cudaFree(h->d_mtris[k]);
+    cudaFree(h->d_mverts[k]);
+    cudaFree(h->d_mfaces[k]);
     if (h->mesh_done[k]) cudaEventDestroy(h->mesh_done[k]);
     if (h->mesh_copied[k]) cudaEventDestroy(h->mesh_copied[k]);
   }
@@ -513,34 +534,65 @@ vh_status grow_tris(vh_handle *h, int64_t need) {
   return VH_OK;
 }
 
-// First use of vh_process_frame_mesh: the two slot buffers, their mapped
-// counter mirrors, the copy-out stream and its events.
-vh_status mesh_setup(vh_handle *h) {
-  if (h->mesh_stream) return VH_OK;
+// First use of vh_process_frame_mesh / vh_process_frame_indexed: the two
+// slots' mapped counter mirrors, the copy-out stream and its events, then
+// the slots' buffers of the kind asked for (triangle soup, or vertices and
+// faces), each of max_triangles entries.
+vh_status mesh_setup(vh_handle *h, bool indexed) {
   const int64_t cap = h->tri_cap ? h->tri_cap : 1;
-  bool ok = cudaMalloc(&h->d_mtris[0], sizeof(float4) * 3 * (size_t)cap) == cudaSuccess &&
-            cudaMalloc(&h->d_mtris[1], sizeof(float4) * 3 * (size_t)cap) == cudaSuccess &&
-            cudaHostAlloc(&h->h_mstate, 2 * sizeof(DevState), cudaHostAllocMapped) == cudaSuccess &&
-            cudaHostGetDevicePointer(&h->h_mstate_dev, h->h_mstate, 0) == cudaSuccess;
-  for (int k = 0; ok && k < 2; ++k)
-    ok = cudaEventCreateWithFlags(&h->mesh_done[k], cudaEventDisableTiming) == cudaSuccess &&
-         cudaEventCreateWithFlags(&h->mesh_copied[k], cudaEventDisableTiming) == cudaSuccess;
-  if (ok) ok = cudaStreamCreateWithFlags(&h->mesh_stream, cudaStreamNonBlocking) == cudaSuccess;
-  if (!ok) {
-    cudaGetLastError();
-    for (int k = 0; k < 2; ++k) {
-      cudaFree(h->d_mtris[k]);
-      h->d_mtris[k] = nullptr;
-      if (h->mesh_done[k]) cudaEventDestroy(h->mesh_done[k]);
-      if (h->mesh_copied[k]) cudaEventDestroy(h->mesh_copied[k]);
-      h->mesh_done[k] = h->mesh_copied[k] = nullptr;
+  if (!h->mesh_stream) {
+    bool ok =
+        cudaHostAlloc(&h->h_mstate, 2 * sizeof(DevState), cudaHostAllocMapped) == cudaSuccess &&
+        cudaHostGetDevicePointer(&h->h_mstate_dev, h->h_mstate, 0) == cudaSuccess;
+    for (int k = 0; ok && k < 2; ++k)
+      ok = cudaEventCreateWithFlags(&h->mesh_done[k], cudaEventDisableTiming) == cudaSuccess &&
+           cudaEventCreateWithFlags(&h->mesh_copied[k], cudaEventDisableTiming) == cudaSuccess;
+    if (ok) ok = cudaStreamCreateWithFlags(&h->mesh_stream, cudaStreamNonBlocking) == cudaSuccess;
+    if (!ok) {
+      cudaGetLastError();
+      for (int k = 0; k < 2; ++k) {
+        if (h->mesh_done[k]) cudaEventDestroy(h->mesh_done[k]);
+        if (h->mesh_copied[k]) cudaEventDestroy(h->mesh_copied[k]);
+        h->mesh_done[k] = h->mesh_copied[k] = nullptr;
+      }
+      if (h->h_mstate) cudaFreeHost(h->h_mstate);
+      h->h_mstate = h->h_mstate_dev = nullptr;
+      return fail(h, VH_ERR_CUDA, "per-frame mesh buffers: allocation failed");
     }
-    if (h->h_mstate) cudaFreeHost(h->h_mstate);
-    h->h_mstate = h->h_mstate_dev = nullptr;
-    return fail(h, VH_ERR_CUDA, "per-frame mesh buffers: allocation failed");
+    std::memset(h->h_mstate, 0, 2 * sizeof(DevState));
   }
-  std::memset(h->h_mstate, 0, 2 * sizeof(DevState));
-  h->mtri_cap = cap;
+  if (!indexed && !h->d_mtris[0]) {
+    const bool ok =
+        cudaMalloc(&h->d_mtris[0], sizeof(float4) * 3 * (size_t)cap) == cudaSuccess &&
+        cudaMalloc(&h->d_mtris[1], sizeof(float4) * 3 * (size_t)cap) == cudaSuccess;
+    if (!ok) {
+      cudaGetLastError();
+      for (int k = 0; k < 2; ++k) {
+        cudaFree(h->d_mtris[k]);
+        h->d_mtris[k] = nullptr;
+      }
+      return fail(h, VH_ERR_CUDA, "per-frame mesh buffers: allocation failed");
+    }
+    h->mtri_cap = cap;
+  }
+  if (indexed && !h->d_mverts[0]) {
+    bool ok = true;
+    for (int k = 0; ok && k < 2; ++k)
+      ok = cudaMalloc(&h->d_mverts[k], sizeof(float4) * (size_t)cap) == cudaSuccess &&
+           cudaMalloc(&h->d_mfaces[k], 3 * sizeof(int32_t) * (size_t)cap) == cudaSuccess;
+    if (!ok) {
+      cudaGetLastError();
+      for (int k = 0; k < 2; ++k) {
+        cudaFree(h->d_mverts[k]);
+        cudaFree(h->d_mfaces[k]);
+        h->d_mverts[k] = nullptr;
+        h->d_mfaces[k] = nullptr;
+      }
+      return fail(h, VH_ERR_CUDA, "per-frame indexed mesh buffers: allocation failed");
+    }
+    h->midx_cap = cap;
+    h->mcidx_per_sm = mc_indexed_ctas_per_sm();
+  }
   return VH_OK;
 }
 
@@ -553,10 +605,24 @@ vh_status mesh_flush(vh_handle *h) {
   h->pending.valid = false;
   VH_CUDA(h, cudaEventSynchronize(h->mesh_done[p.slot]));
   const int64_t n = h->h_mstate[p.slot].tri_count;
-  const int64_t m = std::min(std::min(n, p.capacity), h->mtri_cap);
-  if (m > 0)
-    VH_CUDA(h, cudaMemcpyAsync(p.tris, h->d_mtris[p.slot], sizeof(float4) * 3 * (size_t)m,
-                               cudaMemcpyDeviceToHost, h->mesh_stream));
+  if (p.indexed) {  // faces, then the vertices they number
+    const int64_t nv = h->h_mstate[p.slot].vert_count;
+    const int64_t mf = std::min(std::min(n, p.capacity), h->midx_cap);
+    const int64_t mv = std::min(std::min(nv, p.vcapacity), h->midx_cap);
+    if (mv > 0)
+      VH_CUDA(h, cudaMemcpyAsync(p.verts, h->d_mverts[p.slot], sizeof(float4) * (size_t)mv,
+                                 cudaMemcpyDeviceToHost, h->mesh_stream));
+    if (mf > 0)
+      VH_CUDA(h, cudaMemcpyAsync(p.tris, h->d_mfaces[p.slot], 3 * sizeof(int32_t) * (size_t)mf,
+                                 cudaMemcpyDeviceToHost, h->mesh_stream));
+    if (p.vcount) *p.vcount = nv;
+    if (nv > p.vcapacity) h->mesh_overflow = true;
+  } else {
+    const int64_t m = std::min(std::min(n, p.capacity), h->mtri_cap);
+    if (m > 0)
+      VH_CUDA(h, cudaMemcpyAsync(p.tris, h->d_mtris[p.slot], sizeof(float4) * 3 * (size_t)m,
+                                 cudaMemcpyDeviceToHost, h->mesh_stream));
+  }
   VH_CUDA(h, cudaEventRecord(h->mesh_copied[p.slot], h->mesh_stream));
   h->mesh_copy_issued[p.slot] = true;
   if (p.count) *p.count = n;
@@ -946,7 +1012,7 @@ vh_status vh_process_frame_mesh(vh_handle *h, const void *depth, int32_t depth_f
     if (n > capacity) return fail(h, VH_ERR_CAPACITY, "the frame's mesh is larger than its buffer");
     return VH_OK;
   }
-  s = mesh_setup(h);
+  s = mesh_setup(h, false);
   if (s != VH_OK) return s;
   const int k = h->mesh_slot;
   // slot k's buffer was last read by the copy-out of the frame two back
@@ -958,11 +1024,73 @@ vh_status vh_process_frame_mesh(vh_handle *h, const void *depth, int32_t depth_f
   VH_CUDA(h, cudaEventRecord(h->mesh_done[k], h->stream));
   // this frame is queued behind the pending one: copy that one out now
   s = mesh_flush(h);
+  h->pending = vh_handle::PendingMesh{};
   h->pending.valid = true;
   h->pending.slot = k;
   h->pending.tris = tris;
   h->pending.capacity = capacity;
   h->pending.count = num_triangles;
+  h->mesh_slot = k ^ 1;
+  return s;
+}
+
+vh_status vh_process_frame_indexed(vh_handle *h, const void *depth, int32_t depth_fmt,
+                                   const uint8_t *rgb, const float *c2w, int32_t mem,
+                                   float *vertices, int64_t vertex_capacity, int32_t *faces,
+                                   int64_t face_capacity, int64_t *num_vertices,
+                                   int64_t *num_faces) {
+  VH_HANDLE_DEVICE(h);
+  VH_NVTX("vh_process_frame_indexed");
+  if (!h) return VH_ERR_INVALID_ARG;
+  if (vertex_capacity < 0 || face_capacity < 0 || (vertex_capacity > 0 && !vertices) ||
+      (face_capacity > 0 && !faces) || !num_vertices || !num_faces)
+    return fail(h, VH_ERR_INVALID_ARG, "indexed mesh output: null buffer or negative capacity");
+  vh_status s = stage_inputs(h, depth, depth_fmt, rgb, c2w, mem);
+  if (s != VH_OK) return s;
+  s = mesh_setup(h, true);
+  if (s != VH_OK) return s;
+  if (h->p.flags & VH_FLAG_SYNC) {  // the reference's blocking order, slot 0
+    if (h->mesh_copy_issued[0]) VH_CUDA(h, cudaStreamWaitEvent(h->stream, h->mesh_copied[0], 0));
+    s = run_frame(h, depth_fmt, kMcIdx0);
+    if (s != VH_OK) return s;
+    h->frames++;
+    h->nb_valid = true;
+    s = sync_and_check(h);
+    const int64_t nf = h->h_state->tri_count, nv = h->h_state->vert_count;
+    *num_faces = nf;
+    *num_vertices = nv;
+    const int64_t mf = std::min(std::min(nf, face_capacity), h->midx_cap);
+    const int64_t mv = std::min(std::min(nv, vertex_capacity), h->midx_cap);
+    if (mv > 0)
+      VH_CUDA(h, cudaMemcpy(vertices, h->d_mverts[0], sizeof(float4) * (size_t)mv,
+                            cudaMemcpyDeviceToHost));
+    if (mf > 0)
+      VH_CUDA(h, cudaMemcpy(faces, h->d_mfaces[0], 3 * sizeof(int32_t) * (size_t)mf,
+                            cudaMemcpyDeviceToHost));
+    if (s != VH_OK) return s;
+    if (nf > face_capacity || nv > vertex_capacity)
+      return fail(h, VH_ERR_CAPACITY, "the frame's mesh is larger than its buffers");
+    return VH_OK;
+  }
+  const int k = h->mesh_slot;
+  // slot k's buffers were last read by the copy-out of the frame two back
+  if (h->mesh_copy_issued[k]) VH_CUDA(h, cudaStreamWaitEvent(h->stream, h->mesh_copied[k], 0));
+  s = run_frame(h, depth_fmt, kMcIdx0 + k);
+  if (s != VH_OK) return s;
+  h->frames++;
+  h->nb_valid = true;
+  VH_CUDA(h, cudaEventRecord(h->mesh_done[k], h->stream));
+  s = mesh_flush(h);  // this frame is queued behind the pending one
+  h->pending = vh_handle::PendingMesh{};
+  h->pending.valid = true;
+  h->pending.indexed = true;
+  h->pending.slot = k;
+  h->pending.tris = reinterpret_cast<float *>(faces);
+  h->pending.capacity = face_capacity;
+  h->pending.count = num_faces;
+  h->pending.verts = vertices;
+  h->pending.vcapacity = vertex_capacity;
+  h->pending.vcount = num_vertices;
   h->mesh_slot = k ^ 1;
   return s;
 }

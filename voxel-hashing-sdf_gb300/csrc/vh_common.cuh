@@ -76,7 +76,8 @@ struct DevState {
   uint32_t erased;       // keys erased by the last erase call
   uint32_t mc_next;      // marching cubes: blocks handed out past the first grid
   uint32_t mc_done;      // marching cubes: CTAs finished (state copy-out)
-  uint32_t pad[2];
+  uint32_t vert_count;   // vertices of the last indexed per-frame mesh
+  uint32_t pad;
 };
 
 // Everything a kernel needs to reach the volume; passed by value.
@@ -214,6 +215,14 @@ void launch_integrate(const VolumeView &V, const CamParams &C, const uint2 *pix,
 // counters there, as launch_state_out would after the kernel.
 void launch_mc(const VolumeView &V, int scope_all, float min_weight, float4 *tris,
                uint32_t tri_cap, int grid, int variant, DevState *host_state, cudaStream_t s);
+// Marching cubes of the frame's blocks into an indexed mesh: vertices
+// (float4 {x, y, z, rgb bits}, global voxel units) and faces (3 vertex
+// numbers each), counts in the state's vert_count and tri_count; the last
+// CTA copies the counters to host_state (mapped host memory) if given.
+void launch_mc_indexed(const VolumeView &V, float min_weight, float4 *verts, uint32_t vcap,
+                       int32_t *faces, uint32_t fcap, int grid, DevState *host_state,
+                       cudaStream_t s);
+int mc_indexed_ctas_per_sm();
 // Resident CTAs per SM of the persistent kernels (for grid sizing), and the
 // number of launch shapes of each (variants 0 .. n - 1).
 int integrate_ctas_per_sm(int variant);

@@ -1077,6 +1077,490 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) k_mc(VolumeView V, int sco
   }
 }
 
+// ---- marching cubes into an indexed mesh (shared vertices per block) ----------
+// The frame's mesh as vertices + faces instead of a triangle soup: per block
+// every cut lattice edge is interpolated once (in both directions where the
+// reference's corner order runs it both ways, a separate vertex only where
+// the two results differ in a bit), the vertices are written once, and each
+// triangle is three vertex numbers.  The triangles are exactly those of k_mc
+// (same vertices bit for bit, same degenerate test); a vertex shared by
+// cubes of two blocks is written by each block.
+constexpr int kRows = kH * kH;         // corner rows (y, z), y and z in 0..8
+constexpr int kEdgeRows = 3 * kRows;   // lattice-edge rows: axis * 81 + y + 9 z
+// Capacities of one pass over a block.  A block whose cube cases need more
+// is processed again in 8 passes of one cube layer each (at most 320
+// triangles and 369 cut edges per layer), so no block is ever dropped.
+constexpr int kICandCap = 1536;  // candidate triangles per pass
+constexpr int kIEdgeCap = 512;   // cut lattice edges per pass
+constexpr int kISlots = kIEdgeCap / kMcThreads;  // edge slots per thread
+
+struct McIdxShared {
+  float sdf[kStaged];  // NaN = corner unusable (absent block or low weight)
+  uint32_t rgb[kStaged];
+  // corner row (y, z): bit x (0..8) = sdf < 0, bit 16 + x = unusable
+  uint32_t row[kRows];
+  // lattice-edge row: bit x = the edge from corner (x, y, z) one voxel along
+  // the row's axis is cut (both corners usable, signs differ)
+  uint16_t cut[kEdgeRows];
+  uint16_t first[kEdgeRows];  // slot of the row's first cut edge
+  uint16_t elist[kIEdgeCap];  // cut edge of a slot: x | y << 4 | z << 8 | axis << 12
+  // slot: the edge's vertex towards +axis and towards -axis (moved
+  // coordinate, global voxel units) and their colours
+  float4 vert[kIEdgeCap];
+  // slot: block-local number of its +axis vertex; bit 15 set when the
+  // -axis vertex differs and has the next number
+  uint16_t vid[kIEdgeCap];
+  uint16_t tri[256][5];  // triangle t of a case: edges e0 | e1 << 4 | e2 << 8
+  uint16_t edge[256];
+  uint8_t ntri[256];
+  uint8_t einfo[12];          // per cube edge, see lattice_edge_info()
+  uint8_t cases[kB3];         // cube case, 0 when the cube emits nothing
+  uint16_t cand[kICandCap];   // candidate triangles: cube | triangle << 9
+  uint32_t halo[kHalo];       // halo voxel: staged index | neighbour << 10 | voxel << 13
+  uint32_t warp_sum[kMcThreads / 32];
+  uint32_t vbase, fbase;
+  uint32_t next[2];  // the block after the current one (double-buffered)
+};
+
+// Cube edge e as a lattice edge: the offset bits x | y << 1 | z << 2 of its
+// lower corner (the smaller coordinate along the edge), the axis along which
+// it runs (bits 3-4) and whether the reference's corner order runs it
+// towards -axis (bit 5: from the upper to the lower corner).
+__device__ __forceinline__ uint32_t lattice_edge_info(int e) {
+  const uint32_t code =
+      (uint32_t)((e < 8 ? kMcEdgeCodeLo >> (8 * e) : kMcEdgeCodeHi >> (8 * (e - 8))) & 0x3Fu);
+  const int a = (int)(code & 7u), b = (int)(code >> 3);
+  const int ax = corner_dx(a), ay = corner_dy(a), az = corner_dz(a);
+  const int bx = corner_dx(b), by = corner_dy(b), bz = corner_dz(b);
+  const uint32_t axis = bx != ax ? 0u : (by != ay ? 1u : 2u);
+  const uint32_t neg = (bx - ax) + (by - ay) + (bz - az) < 0 ? 1u : 0u;
+  const uint32_t lower = (uint32_t)((ax & bx) | ((ay & by) << 1) | ((az & bz) << 2));
+  return lower | (axis << 3) | (neg << 5);
+}
+
+// VertexInterp(p1, p2, val1, val2) (src/tsdf.cu:1640-1660) for corners one
+// voxel apart along one axis: only that coordinate moves, from p (p1's) by
+// step = p2 - p1 = +-1; the colour is interpolated and truncated like the
+// reference's float-to-uchar store.  The same arithmetic as mc_vertex.
+__device__ __forceinline__ void interp_edge(float p, float step, float v1, float v2, uint32_t c1,
+                                            uint32_t c2, float &moved, uint32_t &col) {
+  float mu = 0.0f;
+  bool interp = false;
+  bool to_b = false;
+  if (fabsf(0.0f - v1) < kSnap) {
+    // p1
+  } else if (fabsf(0.0f - v2) < kSnap) {
+    to_b = true;  // p2
+  } else if (fabsf(v1 - v2) < kSnap) {
+    // p1
+  } else {
+    mu = (0.0f - v1) / (v2 - v1);
+    interp = true;
+  }
+  moved = p;
+  if (interp)
+    moved = moved + mu * step;
+  else if (to_b)
+    moved = moved + step;
+  if (!interp) {
+    col = to_b ? c2 : c1;
+    return;
+  }
+  uint32_t out = 0;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const int q1 = (int)((c1 >> (8 * c)) & 0xFFu), q2 = (int)((c2 >> (8 * c)) & 0xFFu);
+    const float v = (float)q1 + mu * (float)(q2 - q1);
+    out |= (__float2uint_rz(v) & 0xFFu) << (8 * c);
+  }
+  col = out;
+}
+
+__device__ __forceinline__ void mci_init_shared(McIdxShared &S) {
+  const int t = threadIdx.x;
+  for (int i = t; i < 256; i += kMcThreads) {
+    S.edge[i] = kMcEdgeMask[i];
+    int n = 0;
+    for (; n < 5 && kMcTri[i][3 * n] >= 0; ++n)
+      S.tri[i][n] = (uint16_t)(kMcTri[i][3 * n] | (kMcTri[i][3 * n + 1] << 4) |
+                               (kMcTri[i][3 * n + 2] << 8));
+    for (int m = n; m < 5; ++m) S.tri[i][m] = 0;
+    S.ntri[i] = (uint8_t)n;
+  }
+  if (t < 12) S.einfo[t] = (uint8_t)lattice_edge_info(t);
+  // halo: x == 8 (81), then y == 8 with x < 8 (72), then z == 8 with x, y < 8 (64)
+  for (int hh = t; hh < kHalo; hh += kMcThreads) {
+    int x, y, z;
+    if (hh < 81) {
+      x = 8;
+      y = hh % 9;
+      z = hh / 9;
+    } else if (hh < 153) {
+      x = (hh - 81) & 7;
+      y = 8;
+      z = (hh - 81) >> 3;
+    } else {
+      x = (hh - 153) & 7;
+      y = (hh - 153) >> 3;
+      z = 8;
+    }
+    const uint32_t nbi = (uint32_t)((x >> 3) | ((y >> 3) << 1) | ((z >> 3) << 2));
+    const uint32_t li = (uint32_t)((x & 7) + 8 * (y & 7) + 64 * (z & 7));
+    S.halo[hh] = (uint32_t)hidx(x, y, z) | (nbi << 10) | (li << 13);
+  }
+}
+
+// Cut-edge mask of lattice-edge row r (axis * 81 + y + 9 z) among the edges
+// that the cubes of layers [z0, z1) use.
+__device__ __forceinline__ uint32_t edge_row_mask(const McIdxShared &S, int r, int z0, int z1) {
+  const int axis = r / kRows, rr = r - axis * kRows;
+  const int y = rr % kH, z = rr / kH;
+  const uint32_t w = S.row[rr];
+  const uint32_t n = w & 0x1FFu, q = w >> 16;
+  if (axis == 0) {  // x edges of layer z are used by cubes z - 1 and z
+    if (z < z0 || z > z1) return 0u;
+    return (n ^ (n >> 1)) & ~(q | (q >> 1)) & 0xFFu;
+  }
+  if (axis == 1) {
+    if (y == 8 || z < z0 || z > z1) return 0u;
+    const uint32_t w2 = S.row[rr + 1];
+    return (n ^ w2) & ~(q | (w2 >> 16)) & 0x1FFu;
+  }
+  if (z == 8 || z < z0 || z >= z1) return 0u;  // z edges of layer z: cubes of layer z
+  const uint32_t w2 = S.row[rr + kH];
+  return (n ^ w2) & ~(q | (w2 >> 16)) & 0x1FFu;
+}
+
+// Cube cases of cubes (x0 .. x0 + 3, y, z) from the corner-row words: bit k
+// of a case is corner k's sign (corner order of src/tsdf.cu's idxMap), 0
+// for a cube with an unusable corner or no cut edge (src/tsdf.cu:930-986).
+__device__ __forceinline__ void classify4(const McIdxShared &S, int x0, int y, int z, int cs[4]) {
+  const uint32_t A = S.row[y + kH * z], B = S.row[y + 1 + kH * z];
+  const uint32_t C = S.row[y + kH * (z + 1)], D = S.row[y + 1 + kH * (z + 1)];
+  const uint32_t bad = (A | B | C | D) >> 16;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int x = x0 + j;
+    const uint32_t a = (A >> x) & 3u, b = (B >> x) & 3u, c = (C >> x) & 3u, d = (D >> x) & 3u;
+    // corners 0 (0,0,0) 3 (1,0,0) | 1 (0,1,0) 2 (1,1,0) | 4 (0,0,1) 7 (1,0,1) | 5 (0,1,1) 6 (1,1,1)
+    int ci = (int)((a & 1u) | ((a & 2u) << 2) | (b << 1) | ((c & 1u) << 4) | ((c & 2u) << 6) |
+                   (d << 5));
+    if (((bad >> x) & 3u) || S.edge[ci] == 0) ci = 0;
+    cs[j] = ci;
+  }
+}
+
+// Exclusive CTA-wide scan for McIdxShared (as cta_scan): one __syncthreads.
+__device__ __forceinline__ uint32_t cta_scan_idx(McIdxShared &S, uint32_t v, uint32_t *total) {
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t u = __shfl_up_sync(kFull, incl, o);
+    if (lane >= o) incl += u;
+  }
+  if (lane == 31) S.warp_sum[warp] = incl;
+  __syncthreads();
+  uint32_t before = 0, tot = 0;
+#pragma unroll
+  for (int q = 0; q < kMcThreads / 32; ++q) {
+    const uint32_t ws = S.warp_sum[q];
+    before += q < warp ? ws : 0u;
+    tot += ws;
+  }
+  *total = tot;
+  return before + incl - v;
+}
+
+// Frame-list entry i: stage the block and its halo, then per pass classify,
+// list cut edges, interpolate each once, number and write the vertices
+// (one atomic per pass), and write the surviving triangles as vertex
+// numbers (one atomic per round).  S must be free on entry.
+__device__ __forceinline__ void mci_block(McIdxShared &S, const VolumeView &V, float min_weight,
+                                          float4 *__restrict__ verts, uint32_t vcap,
+                                          int32_t *__restrict__ faces, uint32_t fcap, uint32_t i) {
+  const int t = threadIdx.x;
+  const float nanv = __int_as_float(0x7FC00000);
+  const ulonglong2 res = __ldg(V.frame_res + i);
+  const unsigned long long key = res.x;
+  const uint32_t own = key < kTombKey ? (uint32_t)res.y : kNoBlock;
+  if (own == kNoBlock) return;  // same entry for every thread: uniform
+  if (!VH_CHECK(V.st, own < V.pool_cap)) return;  // uniform as well
+  int bx, by, bz;
+  unpack_key(key, bx, by, bz);
+  {  // own block: 4 voxels per thread, 16-byte loads
+    const float *base = V.pool + (size_t)own * kBlockWords;
+    const float4 sd = reinterpret_cast<const float4 *>(base)[t];
+    const float4 wt = reinterpret_cast<const float4 *>(base + kB3)[t];
+    const uint4 cl = reinterpret_cast<const uint4 *>(base + 2 * kB3)[t];
+    const int li = 4 * t, x = li & 7, y = (li >> 3) & 7, z = li >> 6;
+    const int h = hidx(x, y, z);
+    S.sdf[h + 0] = wt.x >= min_weight ? sd.x : nanv;
+    S.sdf[h + 1] = wt.y >= min_weight ? sd.y : nanv;
+    S.sdf[h + 2] = wt.z >= min_weight ? sd.z : nanv;
+    S.sdf[h + 3] = wt.w >= min_weight ? sd.w : nanv;
+    S.rgb[h + 0] = cl.x;
+    S.rgb[h + 1] = cl.y;
+    S.rgb[h + 2] = cl.z;
+    S.rgb[h + 3] = cl.w;
+  }
+  {  // halo: every thread owns at most two entries; all loads issued together
+    const int h1 = t + kMcThreads;
+    const uint32_t info0 = S.halo[t];
+    const uint32_t info1 = h1 < kHalo ? S.halo[h1] : 0u;
+    const uint32_t nb0 = (info0 >> 10) & 7u, nb1 = (info1 >> 10) & 7u;
+    uint32_t blk0 = __ldg(V.frame_nb + 8 * (size_t)i + nb0);
+    uint32_t blk1 = h1 < kHalo ? __ldg(V.frame_nb + 8 * (size_t)i + nb1) : kNoBlock;
+    if (!VH_CHECK(V.st, blk0 == kNoBlock || blk0 < V.pool_cap)) blk0 = kNoBlock;
+    if (!VH_CHECK(V.st, blk1 == kNoBlock || blk1 < V.pool_cap)) blk1 = kNoBlock;
+    const int li0 = (int)(info0 >> 13), li1 = (int)(info1 >> 13);
+    float w0 = 0.f, s0 = nanv, w1 = 0.f, s1 = nanv;
+    uint32_t c0 = 0, c1 = 0;
+    if (blk0 != kNoBlock) {
+      const float *base = V.pool + (size_t)blk0 * kBlockWords;
+      w0 = __ldg(base + kB3 + li0);
+      s0 = __ldg(base + li0);
+      c0 = __ldg(reinterpret_cast<const uint32_t *>(base + 2 * kB3) + li0);
+    }
+    if (blk1 != kNoBlock) {
+      const float *base = V.pool + (size_t)blk1 * kBlockWords;
+      w1 = __ldg(base + kB3 + li1);
+      s1 = __ldg(base + li1);
+      c1 = __ldg(reinterpret_cast<const uint32_t *>(base + 2 * kB3) + li1);
+    }
+    S.sdf[info0 & 1023u] = blk0 != kNoBlock && w0 >= min_weight ? s0 : nanv;
+    S.rgb[info0 & 1023u] = c0;
+    if (h1 < kHalo) {
+      S.sdf[info1 & 1023u] = blk1 != kNoBlock && w1 >= min_weight ? s1 : nanv;
+      S.rgb[info1 & 1023u] = c1;
+    }
+  }
+  __syncthreads();
+  if (t < kRows) {  // corner-row words: sign and unusable bits of 9 corners
+    const float *r = S.sdf + hidx(0, t % kH, t / kH);
+    uint32_t w = 0;
+#pragma unroll
+    for (int x = 0; x < kH; ++x) {
+      const float v = r[x];
+      w |= (v < 0.0f ? 1u : 0u) << x;
+      w |= (v != v ? 1u : 0u) << (16 + x);
+    }
+    S.row[t] = w;
+  }
+  __syncthreads();
+
+  const int cy = (t >> 1) & 7, cz = t >> 4, cx0 = (t & 1) * 4;  // this thread's 4 cubes
+  const int gx0 = bx * kB, gy0 = by * kB, gz0 = bz * kB;
+  int z0 = 0, z1 = kB;
+  bool layered = false;
+  for (;;) {
+    // 1. classify this thread's cubes and the cut masks of its edge rows
+    int cs[4];
+    classify4(S, cx0, cy, cz, cs);
+    uint32_t ntri_mine = 0;
+    const bool in_pass = cz >= z0 && cz < z1;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (!in_pass) cs[j] = 0;
+      S.cases[cx0 + j + kB * cy + kB * kB * cz] = (uint8_t)cs[j];
+      ntri_mine += S.ntri[cs[j]];
+    }
+    const int r1 = t + kMcThreads;
+    const uint32_t m0 = edge_row_mask(S, t, z0, z1);
+    const uint32_t m1 = r1 < kEdgeRows ? edge_row_mask(S, r1, z0, z1) : 0u;
+    const uint32_t ncut_mine = (uint32_t)(__popc(m0) + __popc(m1));
+    uint32_t tot;
+    const uint32_t off = cta_scan_idx(S, ntri_mine | (ncut_mine << 16), &tot);
+    const uint32_t ncand = tot & 0xFFFFu, ncut = tot >> 16;
+    if (!layered && (ncand > (uint32_t)kICandCap || ncut > (uint32_t)kIEdgeCap)) {
+      layered = true;  // uniform: start again one layer at a time
+      z1 = 1;
+      __syncthreads();  // warp sums read before the next scan
+      continue;
+    }
+    if (ncand) {
+      // 2. expand candidate triangles and list the cut edges (slot order)
+      uint32_t ct = off & 0xFFFFu;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int c = cx0 + j + kB * cy + kB * kB * cz;
+        const int nt = S.ntri[cs[j]];
+        for (int tt = 0; tt < nt; ++tt) S.cand[ct++] = (uint16_t)(c | (tt << 9));
+      }
+      uint32_t se = off >> 16;
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const int r = k ? r1 : t;
+        if (r >= kEdgeRows) break;
+        uint32_t m = k ? m1 : m0;
+        S.cut[r] = (uint16_t)m;
+        S.first[r] = (uint16_t)se;
+        const int axis = r / kRows, rr = r - axis * kRows;
+        const uint32_t yz = (uint32_t)((rr % kH) << 4 | (rr / kH) << 8 | axis << 12);
+        while (m) {
+          const int x = __ffs(m) - 1;
+          m &= m - 1u;
+          S.elist[se++] = (uint16_t)(yz | (uint32_t)x);
+        }
+      }
+      __syncthreads();
+      // 3. this thread's slots [kISlots t, kISlots t + kISlots): the vertex
+      //    towards +axis VertexInterp(lower, upper) and towards -axis
+      //    VertexInterp(upper, lower) (z edges are only run upwards); a
+      //    separate -axis vertex only where the two differ
+      uint32_t two = 0, nv_mine = 0;
+#pragma unroll
+      for (int j = 0; j < kISlots; ++j) {
+        const uint32_t s = (uint32_t)(kISlots * t + j);
+        if (s >= ncut) break;
+        const uint32_t ent = S.elist[s];
+        const int x = (int)(ent & 15u), y = (int)((ent >> 4) & 15u), z = (int)((ent >> 8) & 15u);
+        const int axis = (int)(ent >> 12);
+        const int lo = hidx(x, y, z);
+        const int hi = lo + (axis == 0 ? 1 : (axis == 1 ? kH : kZPitch));
+        const float vl = S.sdf[lo], vh = S.sdf[hi];
+        const uint32_t cl = S.rgb[lo], ch = S.rgb[hi];
+        const int g = axis == 0 ? gx0 + x : (axis == 1 ? gy0 + y : gz0 + z);
+        float up, down = 0.0f;
+        uint32_t cup, cdown = 0u;
+        interp_edge((float)g, 1.0f, vl, vh, cl, ch, up, cup);
+        bool sep = false;
+        if (axis != 2) {
+          interp_edge((float)(g + 1), -1.0f, vh, vl, ch, cl, down, cdown);
+          sep = __float_as_uint(down) != __float_as_uint(up) || cdown != cup;
+        }
+        S.vert[s] = make_float4(up, down, __uint_as_float(cup), __uint_as_float(cdown));
+        two |= (sep ? 1u : 0u) << j;
+        nv_mine += sep ? 2u : 1u;
+      }
+      uint32_t nv;
+      uint32_t local = cta_scan_idx(S, nv_mine, &nv);
+#pragma unroll
+      for (int j = 0; j < kISlots; ++j) {
+        const uint32_t s = (uint32_t)(kISlots * t + j);
+        if (s >= ncut) break;
+        const uint32_t sep = (two >> j) & 1u;
+        S.vid[s] = (uint16_t)(local | (sep << 15));
+        local += 1u + sep;
+      }
+      if (t == 0) S.vbase = atomicAdd(&V.st->vert_count, nv);
+      __syncthreads();
+      // 4. the vertices, at vbase + their block-local numbers
+      const uint32_t vbase = S.vbase;
+#pragma unroll
+      for (int j = 0; j < kISlots; ++j) {
+        const uint32_t s = (uint32_t)(kISlots * t + j);
+        if (s >= ncut) break;
+        const uint32_t ent = S.elist[s];
+        const int x = (int)(ent & 15u), y = (int)((ent >> 4) & 15u), z = (int)((ent >> 8) & 15u);
+        const int axis = (int)(ent >> 12);
+        const float4 sv = S.vert[s];
+        const float px = (float)(gx0 + x), py = (float)(gy0 + y), pz = (float)(gz0 + z);
+        const uint32_t vv = S.vid[s];
+        const uint32_t o = vbase + (vv & 0x7FFFu);
+        const uint32_t nvs = (vv >> 15) ? 2u : 1u;
+        if (o + nvs <= vcap) {
+          verts[o] = make_float4(axis == 0 ? sv.x : px, axis == 1 ? sv.x : py,
+                                 axis == 2 ? sv.x : pz, sv.z);
+          if (nvs == 2u)
+            verts[o + 1] = make_float4(axis == 0 ? sv.y : px, axis == 1 ? sv.y : py, pz, sv.w);
+        } else {
+          atomicOr(&V.st->error, kErrTriCap);
+        }
+      }
+      // 5. candidates in rounds of one per thread: the three vertices from
+      //    the slots, the reference's degenerate test (p0 == p1 || p1 == p2,
+      //    src/tsdf.cu:1055-1057), a CTA scan over the survivors, one atomic
+      //    per round, each survivor's three vertex numbers
+      for (uint32_t q0 = 0; q0 < ncand; q0 += kMcThreads) {
+        const uint32_t k = q0 + (uint32_t)t;
+        float4 p[3];
+        uint32_t id[3] = {0u, 0u, 0u};
+        uint32_t ok = 0;
+        if (k < ncand) {
+          const uint32_t ent = S.cand[k];
+          const int c = (int)(ent & 511u), tt = (int)(ent >> 9);
+          const int x = c & 7, y = (c >> 3) & 7, z = c >> 6;
+          const uint32_t tri = S.tri[S.cases[c]][tt];
+#pragma unroll
+          for (int v = 0; v < 3; ++v) {
+            const uint32_t info = S.einfo[(tri >> (4 * v)) & 15u];
+            const int lx = x + (int)(info & 1u), ly = y + (int)((info >> 1) & 1u),
+                      lz = z + (int)((info >> 2) & 1u);
+            const int axis = (int)((info >> 3) & 3u);
+            const int r = axis * kRows + ly + kH * lz;
+            const uint32_t slot = S.first[r] + (uint32_t)__popc(S.cut[r] & ((1u << lx) - 1u));
+            const float4 sv = S.vert[slot];
+            const bool down = (info >> 5) & 1u;
+            const float moved = down ? sv.y : sv.x;
+            p[v] = make_float4(axis == 0 ? moved : (float)(gx0 + lx),
+                               axis == 1 ? moved : (float)(gy0 + ly),
+                               axis == 2 ? moved : (float)(gz0 + lz), 0.0f);
+            const uint32_t vv = S.vid[slot];
+            id[v] = vbase + (vv & 0x7FFFu) + ((down && (vv >> 15)) ? 1u : 0u);
+          }
+          ok = !(same_pos(p[0], p[1]) || same_pos(p[1], p[2]));
+        }
+        uint32_t nvalid;
+        const uint32_t pre = cta_scan_idx(S, ok, &nvalid);
+        if (t == 0) S.fbase = nvalid ? atomicAdd(&V.st->tri_count, nvalid) : 0u;
+        __syncthreads();
+        if (ok) {
+          const uint32_t out = S.fbase + pre;
+          if (out < fcap) {
+            int32_t *dst = faces + 3 * (size_t)out;
+            dst[0] = (int32_t)id[0];
+            dst[1] = (int32_t)id[1];
+            dst[2] = (int32_t)id[2];
+          } else {
+            atomicOr(&V.st->error, kErrTriCap);
+          }
+        }
+      }
+    }
+    if (!layered || z1 == kB) return;
+    __syncthreads();  // this layer's slots, lists and warp sums are free
+    ++z0;
+    ++z1;
+  }
+}
+
+// Persistent CTAs over the frame list, blocks handed out by a counter as in
+// k_mc; the last CTA to finish copies the counters to host_state.
+__global__ void __launch_bounds__(kMcThreads, 8)
+    k_mc_indexed(VolumeView V, float min_weight, float4 *__restrict__ verts, uint32_t vcap,
+                 int32_t *__restrict__ faces, uint32_t fcap, DevState *host_state) {
+  __shared__ McIdxShared S;
+  mci_init_shared(S);
+  const uint32_t n = min(V.st->frame_count, V.frame_cap);
+  __syncthreads();
+  uint32_t i = blockIdx.x;
+  for (int par = 0; i < n; par ^= 1) {
+    if (threadIdx.x == 0) S.next[par] = gridDim.x + atomicAdd(&V.st->mc_next, 1u);
+    mci_block(S, V, min_weight, verts, vcap, faces, fcap, i);
+    __syncthreads();  // S.next[par] visible; this block done with S
+    i = S.next[par];
+  }
+  if (host_state) {  // the last CTA to finish copies the counters out
+    __shared__ int last_cta;
+    if (threadIdx.x == 0) {
+      __threadfence();
+      last_cta = atomicAdd(&V.st->mc_done, 1u) == gridDim.x - 1u;
+    }
+    __syncthreads();
+    if (last_cta && threadIdx.x < 32) {
+      if (threadIdx.x == 0) {
+        __threadfence();
+        V.st->mc_done = 0u;
+      }
+      __syncwarp();
+      if (threadIdx.x < sizeof(DevState) / 4)
+        reinterpret_cast<volatile uint32_t *>(host_state)[threadIdx.x] =
+            reinterpret_cast<volatile const uint32_t *>(V.st)[threadIdx.x];
+    }
+  }
+}
+
 // ---- small state kernels --------------------------------------------------------
 __device__ __forceinline__ void reconcile(const VolumeView &V) { reconcile_epoch(V); }
 
@@ -1095,6 +1579,7 @@ __device__ void mc_begin_state(const VolumeView &V) {
   reconcile(V);
   V.st->tri_count = 0;
   V.st->mc_next = 0;
+  V.st->vert_count = 0;
 }
 
 // Opens a frame: stamp and counters (thread 0) and, with d_fin set, the
@@ -1502,6 +1987,7 @@ __device__ __forceinline__ void step_close_epoch(const VolumeView &V, bool mesh)
   if (mesh) {
     st->tri_count = 0;
     st->mc_next = 0;
+    st->vert_count = 0;
   }
 }
 
@@ -1935,6 +2421,18 @@ void launch_mc(const VolumeView &V, int scope_all, float min_weight, float4 *tri
   else
     k_mc<kMcThreads, 10><<<grid, kMcThreads, 0, s>>>(V, scope_all, min_weight, tris, tri_cap,
                                                       host_state);
+}
+
+int mc_indexed_ctas_per_sm() {
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mc_indexed, kMcThreads, 0);
+  return n > 0 ? n : 1;
+}
+
+void launch_mc_indexed(const VolumeView &V, float min_weight, float4 *verts, uint32_t vcap,
+                       int32_t *faces, uint32_t fcap, int grid, DevState *host_state,
+                       cudaStream_t s) {
+  k_mc_indexed<<<grid, kMcThreads, 0, s>>>(V, min_weight, verts, vcap, faces, fcap, host_state);
 }
 
 void launch_alloc_keys(const VolumeView &V, const int32_t *xyz, uint32_t n, cudaStream_t s) {

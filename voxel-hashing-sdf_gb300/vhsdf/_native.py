@@ -117,6 +117,7 @@ SIGNATURES = {
     "vh_extract": (I32, [P, I32, C.POINTER(VhMeshView)]),
     "vh_process_frame": (I32, [P, P, I32, P, P, I32, C.POINTER(VhMeshView)]),
     "vh_process_frame_mesh": (I32, [P, P, I32, P, P, I32, P, I64, PI64]),
+    "vh_process_frame_indexed": (I32, [P, P, I32, P, P, I32, P, I64, P, I64, PI64, PI64]),
     "vh_copy_mesh": (I32, [P, P, P, I64, PI64]),
     "vh_save_ply": (I32, [P, C.c_char_p, I32]),
     "vh_render": (I32, [P]),

@@ -166,6 +166,30 @@ class Volume:
             self._h, d.ptr, fmt, c.ptr, pose.ctypes.data, d.mem, out.ctypes.data, out.shape[0],
             count.ctypes.data_as(C.POINTER(C.c_int64))))
 
+    def process_frame_indexed(self, depth, rgb, c2w, verts, faces, counts, depth_format=None):
+        """process_frame, and the frame's mesh delivered indexed: vertices
+        into `verts` (host float32 array (capacity, 4): x, y, z in voxel
+        units and the colour bits), faces into `faces` (host int32 array
+        (capacity, 3)), counts[0] = vertices and counts[1] = faces (host
+        int64 array).  Without VH_FLAG_SYNC the copy completes by the next
+        sync(); the arrays are kept alive until then."""
+        d, fmt, c, pose = self._frame_args(depth, rgb, c2w, depth_format)
+        if not (isinstance(verts, np.ndarray) and verts.dtype == np.float32 and verts.ndim == 2
+                and verts.shape[1] == 4 and verts.flags.c_contiguous):
+            raise ValueError("verts must be a C-contiguous float32 array of shape (capacity, 4)")
+        if not (isinstance(faces, np.ndarray) and faces.dtype == np.int32 and faces.ndim == 2
+                and faces.shape[1] == 3 and faces.flags.c_contiguous):
+            raise ValueError("faces must be a C-contiguous int32 array of shape (capacity, 3)")
+        if not (isinstance(counts, np.ndarray) and counts.dtype == np.int64 and counts.size >= 2
+                and counts.flags.c_contiguous):
+            raise ValueError("counts must be an int64 array of two entries")
+        self._pending_meshes.append((verts, faces, counts))
+        p64 = C.POINTER(C.c_int64)
+        self._check(self._L.vh_process_frame_indexed(
+            self._h, d.ptr, fmt, c.ptr, pose.ctypes.data, d.mem, verts.ctypes.data, verts.shape[0],
+            faces.ctypes.data, faces.shape[0], counts.ctypes.data_as(p64),
+            C.cast(counts.ctypes.data + 8, p64)))
+
     # ---- launch tuning ----
     def tuning(self):
         t = N.VhTuning()
