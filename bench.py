@@ -973,6 +973,7 @@ def run_engine(args):
                                       depth_format="u16")
         vol.sync()
         e2e_idx_s = time.perf_counter() - t0
+    idx_last = vol.stats()  # per-stage events of the last frame (k_mc_indexed)
     vol.close()
     del idx_bufs
     idx_verts = [int(c[0]) for c in idx_counts[args.warmup:]]
@@ -1064,6 +1065,9 @@ def run_engine(args):
                         "read, mesh written) exceeds L2",
                 "vertices_per_step": statistics.mean(idx_verts),
                 "faces_per_step": statistics.mean(idx_faces),
+                "last_frame_stages_ms": {k: idx_last[k] for k in
+                                         ("ms_allocate", "ms_integrate", "ms_extract",
+                                          "ms_frame")},
                 "mesh_counts_match_device_pass": idx_counts_match,
                 "triangle_soup": {
                     "value": e2e_soup,
