@@ -42,6 +42,10 @@ def test_params_default_and_validate():
         assert L.vh_params_validate(C.byref(q)) != N.VH_OK, field
     q = N.VhParams()
     L.vh_params_default(C.byref(q))
+    q.flags = N.VH_FLAG_SYNC | N.VH_FLAG_BATCH_FUSED  # the batch form flag is a known flag
+    assert L.vh_params_validate(C.byref(q)) == N.VH_OK
+    q = N.VhParams()
+    L.vh_params_default(C.byref(q))
     q.trunc = float("nan")
     assert L.vh_params_validate(C.byref(q)) == N.VH_ERR_NOT_FINITE
     assert L.vh_params_validate(None) == N.VH_ERR_INVALID_ARG
