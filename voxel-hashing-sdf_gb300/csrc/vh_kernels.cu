@@ -1943,25 +1943,40 @@ __device__ __forceinline__ uint32_t ld_vol32(const uint32_t *p) {
   return *(volatile const uint32_t *)p;
 }
 
-// A ticket of an open stage of some scene, looking at scenes from `hint`
-// on (thread 0 only).  Returns false when no scene has a free ticket now.
-__device__ __forceinline__ bool step_pick(StepSched *sched, int n, int hint, int *s_out, uint32_t *stage_out,
-                          uint32_t *item_out) {
-  for (int r = 0; r < n; ++r) {
-    int s = hint + r;
-    if (s >= n) s -= n;
-    StepSched &q = sched[s];
-    const unsigned long long w = ld_volatile(&q.word);
-    const uint32_t st = (uint32_t)(w >> 32);
-    if (st >= kStepDone || (uint32_t)w >= ld_vol32(&q.total[st])) continue;  // a hint only
-    const unsigned long long got = atomicAdd(&q.word, 1ull);
-    __threadfence();  // the stage's totals after the ticket
-    const uint32_t st2 = (uint32_t)(got >> 32), it = (uint32_t)got;
-    if (st2 < kStepDone && it < ld_vol32(&q.total[st2])) {
-      *s_out = s;
-      *stage_out = st2;
-      *item_out = it;
-      return true;
+// A ticket of an open stage of some scene, called by all lanes of warp 0:
+// 32 scenes are looked at together from `hint` on, and the lanes whose scene
+// shows a free ticket try it in order until one gets a valid one (the
+// looks are only hints; the atomic decides).  Returns false, in every lane,
+// when no scene had a free ticket.
+__device__ __forceinline__ bool step_pick(StepSched *sched, int n, int hint, int *s_out,
+                                          uint32_t *stage_out, uint32_t *item_out) {
+  const int lane = threadIdx.x & 31;
+  for (int r0 = 0; r0 < n; r0 += 32) {
+    const int s = (hint + r0 + lane) % n;
+    bool cand = false;
+    if (r0 + lane < n) {
+      const unsigned long long w = ld_volatile(&sched[s].word);
+      const uint32_t st = (uint32_t)(w >> 32);
+      cand = st < kStepDone && (uint32_t)w < ld_vol32(&sched[s].total[st]);
+    }
+    unsigned m = __ballot_sync(kFull, cand);
+    while (m) {
+      const int l = __ffs(m) - 1;
+      m &= m - 1u;
+      uint32_t ok = 0, st2 = 0, it = 0;
+      if (lane == l) {
+        const unsigned long long got = atomicAdd(&sched[s].word, 1ull);
+        __threadfence();  // the stage's totals after the ticket
+        st2 = (uint32_t)(got >> 32);
+        it = (uint32_t)got;
+        ok = st2 < kStepDone && it < ld_vol32(&sched[s].total[st2]) ? 1u : 0u;
+      }
+      if (__shfl_sync(kFull, ok, l)) {
+        *s_out = __shfl_sync(kFull, s, l);
+        *stage_out = __shfl_sync(kFull, st2, l);
+        *item_out = __shfl_sync(kFull, it, l);
+        return true;
+      }
     }
   }
   return false;
@@ -2043,12 +2058,13 @@ __device__ __forceinline__ void step_integrate(const SceneDesc &sd, const float 
   flush_updated(sd, updated);
 }
 
-// Thread 0 picks the CTA's next item.  `spec` is the ticket it took while
-// the previous item ran (StepCta::spec_scene >= 0): a ticket of that item's
-// stage, which cannot close before that item is finished; a valid one is
-// run next.  Otherwise scenes are scanned from the current one on, polling
-// (bounded) while none has a free ticket and some are unfinished.  Returns
-// the scene, or -1 when the step is over.
+// Warp 0 picks the CTA's next item (lane 0 writes it to `c`).  `spec`
+// (lane 0's) is the ticket lane 0 took while the previous item ran
+// (StepCta::spec_scene >= 0): a ticket of that item's stage, which cannot
+// close before that item is finished; a valid one is run next.  Otherwise
+// scenes are scanned from the current one on, polling (bounded) while none
+// has a free ticket and some are unfinished.  Returns the scene in every
+// lane, or -1 when the step is over.
 struct StepCta {
   int scene, cur, spec_scene;
   uint32_t stage, item, count, spec_stage, spec_total;
@@ -2057,39 +2073,56 @@ struct StepCta {
 __device__ __forceinline__ int step_next(StepCta &c, unsigned long long spec,
                                          const SceneDesc *__restrict__ d, int n,
                                          StepSched *__restrict__ sched, StepGlobal *glob) {
+  const int lane = threadIdx.x & 31;
+  const int spec_scene = c.spec_scene, cur = c.cur;
+  const uint32_t spec_stage = c.spec_stage, spec_total = c.spec_total;
+  spec = __shfl_sync(kFull, spec, 0);
+  __syncwarp();  // every lane has read c before lane 0 rewrites it
   int s = -1;
   uint32_t stage = 0, item = 0;
-  if (c.spec_scene >= 0) {
+  if (spec_scene >= 0) {  // the same in every lane
     const uint32_t st2 = (uint32_t)(spec >> 32), it = (uint32_t)spec;
     if (st2 < kStepDone &&
-        it < (st2 == c.spec_stage ? c.spec_total : ld_vol32(&sched[c.spec_scene].total[st2]))) {
-      s = c.spec_scene;
+        it < (st2 == spec_stage ? spec_total : ld_vol32(&sched[spec_scene].total[st2]))) {
+      s = spec_scene;
       stage = st2;
       item = it;
     }
   }
-  c.spec_scene = -1;
-  const int hint = c.cur >= 0 ? c.cur : (int)(blockIdx.x % (unsigned)n);
+  const int hint = cur >= 0 ? cur : (int)(blockIdx.x % (unsigned)n);
   unsigned long long idle_since = 0;
   for (uint32_t polls = 0; s < 0; ++polls) {
     if (step_pick(sched, n, hint, &s, &stage, &item)) break;
-    if (ld_vol32(&glob->remaining) == 0u) break;  // every scene finished
-    const unsigned long long now = global_ns();
-    if (polls == 0) idle_since = now;
-    if (polls >= kStepMaxPolls || now - idle_since > kStepIdleLimitNs) {
-      // never expected: report instead of waiting on
-      atomicAdd(&glob->gave_up, 1u);
-      for (int k = 0; k < n; ++k)
-        if ((uint32_t)(ld_volatile(&sched[k].word) >> 32) < kStepDone)
-          atomicOr(&d[k].V.st->error, kErrRetry);
+    uint32_t stop = 0;  // lane 0 decides: 1 every scene finished, 2 give up
+    if (lane == 0) {
+      if (ld_vol32(&glob->remaining) == 0u) {
+        stop = 1u;
+      } else {
+        const unsigned long long now = global_ns();
+        if (polls == 0) idle_since = now;
+        if (polls >= kStepMaxPolls || now - idle_since > kStepIdleLimitNs) stop = 2u;
+      }
+    }
+    stop = __shfl_sync(kFull, stop, 0);
+    if (stop == 1u) break;
+    if (stop == 2u) {  // never expected: report instead of waiting on
+      if (lane == 0) {
+        atomicAdd(&glob->gave_up, 1u);
+        for (int k = 0; k < n; ++k)
+          if ((uint32_t)(ld_volatile(&sched[k].word) >> 32) < kStepDone)
+            atomicOr(&d[k].V.st->error, kErrRetry);
+      }
       break;
     }
     __nanosleep(200);
   }
-  c.scene = s;
-  c.stage = stage;
-  c.item = item;
-  c.count = s >= 0 ? ld_vol32(&sched[s].count) : 0u;
+  if (lane == 0) {
+    c.spec_scene = -1;
+    c.scene = s;
+    c.stage = stage;
+    c.item = item;
+    c.count = s >= 0 ? ld_vol32(&sched[s].count) : 0u;
+  }
   return s;
 }
 
@@ -2109,11 +2142,11 @@ __global__ void __launch_bounds__(kStepThreads, 8)
     c.cur = -1;
     c.spec_scene = -1;
   }
-  unsigned long long spec = 0;  // thread 0: the ticket taken while an item runs
+  unsigned long long spec = 0;  // lane 0 of warp 0: the ticket taken while an item runs
   for (;;) {
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < 32) {
       const int s = step_next(c, spec, d, n, sched, glob);
-      if (s >= 0) {  // take the following ticket now; it is looked at after this item
+      if (threadIdx.x == 0 && s >= 0) {  // take the following ticket now; it is looked at after this item
         c.spec_stage = c.stage;
         c.spec_total = ld_vol32(&sched[s].total[c.stage]);
         spec = atomicAdd(&sched[s].word, 1ull);
