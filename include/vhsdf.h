@@ -224,7 +224,9 @@ vh_status vh_process_frame(vh_handle *h, const void *depth, int32_t depth_fmt,
 vh_status vh_process_frame_mesh(vh_handle *h, const void *depth, int32_t depth_fmt,
                                 const uint8_t *rgb, const float *c2w, int32_t mem, float *tris,
                                 int64_t capacity, int64_t *num_triangles);
-/* vh_process_frame_mesh with the frame's mesh delivered indexed: vertices
+/* vh_process_frame_mesh with the frame's mesh delivered indexed - the
+ * per-frame triangle copy of processFrame (src/tsdf.cu:1554-1564) in
+ * another layout: vertices
  * (4 floats each: x, y, z in global voxel units and the colour bytes
  * r | g<<8 | b<<16 in the fourth float's bits, as vh_mesh_view) and faces
  * (3 int32 vertex numbers each).  The faces are exactly the triangles
