@@ -29,7 +29,10 @@ class _Scene(Volume):
 
 class Batch:
     def __init__(self, scenes):
-        """scenes: one dict of vh_params fields per scene."""
+        """scenes: one dict of vh_params fields per scene.  VH_FLAG_BATCH_FUSED
+        in the first scene's flags runs each step as one persistent launch
+        over every stage of every scene (the same results as the staged
+        launches)."""
         self._L = N.lib()
         n = len(scenes)
         arr = (N.VhParams * n)()
