@@ -34,6 +34,23 @@ def test_device_header_compiles(tmp_path):
                     str(tmp_path / "user.o")], check=True, capture_output=True)
 
 
+def test_device_header_hashes_like_the_engine():
+    """The header restates the table's slot hash for callers' kernels; its
+    finaliser constants and shifts must be the engine's (the GPU test below
+    then checks lookups end to end)."""
+    import re
+    hdr = open(os.path.join(REPO, "include", "vhashing_device.cuh")).read()
+    eng = open(os.path.join(PKG, "csrc", "vh_common.cuh")).read()
+
+    def mix_body(text, name):
+        body = re.search(name + r"\(unsigned long long z\) \{(.*?)\}", text, re.S).group(1)
+        return re.findall(r"0x[0-9A-Fa-f]+ull|>> \d+", body)
+
+    assert mix_body(hdr, "mix") == mix_body(eng, "mix64")
+    assert len(mix_body(eng, "mix64")) == 5
+    assert "<< 21" in hdr and "<< 42" in hdr and "0x1FFFFFull" in hdr
+
+
 def test_device_table_host_checks():
     L = N.lib()
     t = N.VhDeviceTable()
