@@ -1875,10 +1875,11 @@ __global__ void k_batch_clear_errors(const SceneDesc *__restrict__ d, int n) {
 // slots through L2-coherent loads and the counters it reads do not change
 // during the stage; the epoch is closed with volatile accesses).
 constexpr int kStepThreads = 128;
-constexpr int kStepPixels = 8 * kStepThreads;  // pixels per allocation item
-constexpr int kStepEntries = kStepThreads;     // frame-list entries per resolve item
-constexpr int kStepBlocks = 8;                 // listed blocks per integration item
-constexpr int kStepMcBlocks = 2;               // listed blocks per marching-cubes item
+constexpr int kStepPixels = 16 * kStepThreads;  // pixels per allocation item
+constexpr int kStepEntries = 2 * kStepThreads;  // frame-list entries per resolve item
+constexpr int kStepBlocks = 16;                 // listed blocks per integration item
+constexpr int kStepMcBlocks = 4;                // listed blocks per marching-cubes item
+static_assert(kStepEntries * 8 % kStepThreads == 0, "whole resolve rounds");
 // An idle CTA gives up after this long without finding work while scenes
 // are unfinished (never expected; the scenes left get kErrRetry).
 constexpr unsigned long long kStepIdleLimitNs = 2000000000ull;
@@ -2168,7 +2169,7 @@ __global__ void __launch_bounds__(kStepThreads, 8)
     } else if (stage == 1) {  // resolve: kStepEntries entries, 8 threads each
       const uint32_t e0 = item * (uint32_t)kStepEntries, count = c.count;
 #pragma unroll 1
-      for (int r = 0; r < 8; ++r) {
+      for (int r = 0; r < kStepEntries * 8 / kStepThreads; ++r) {
         const uint32_t g8 = (uint32_t)(r * kStepThreads) + threadIdx.x;
         const uint32_t e = e0 + (g8 >> 3);
         if (e < count) resolve_entry(sd.V, e, g8 & 7u);
