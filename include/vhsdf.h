@@ -490,8 +490,8 @@ typedef struct vh_batch vh_batch;
  * vh_batch_scene(b, 0)). */
 /* With VH_FLAG_BATCH_FUSED in params[0].flags the scenes form one group and
  * a step is one persistent launch (after a one-CTA begin kernel): its CTAs
- * take work items - 1024 pixels of allocation, 128 list entries of resolve,
- * 8 blocks of integration, 2 blocks of marching cubes - from whichever
+ * take work items - 2048 pixels of allocation, 256 list entries of resolve,
+ * 16 blocks of integration, 4 blocks of marching cubes - from whichever
  * scene has some in its current stage, and the CTA that finishes a scene's
  * stage opens its next one, so one scene's allocation overlaps another's
  * integration inside the launch.  Results are the same either way; the
