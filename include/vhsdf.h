@@ -343,7 +343,8 @@ typedef struct vh_device_table {
   int64_t pool_capacity;
   float voxel_size;
   int32_t device;
-  void *stream;               /* cudaStream_t of the handle's work            */
+  void *stream;               /* cudaStream_t of the handle's work when the   */
+                              /* table was taken (vh_set_stream changes it)  */
 } vh_device_table;
 /* Fills *out for handle h.  Host only: enqueues nothing. */
 vh_status vh_get_device_table(vh_handle *h, vh_device_table *out);
