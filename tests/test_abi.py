@@ -60,6 +60,12 @@ def test_status_strings_and_null_handles():
     assert L.vh_sync(None) == N.VH_ERR_INVALID_ARG
     assert L.vh_render(None) == N.VH_ERR_UNSUPPORTED
     assert L.vh_last_error(None) == b"null handle"
+    nv, nf = C.c_int64(-1), C.c_int64(-1)
+    assert L.vh_process_frame_indexed(None, None, N.VH_DEPTH_U16_MM, None, None, N.VH_MEM_HOST,
+                                      None, 0, None, 0, C.byref(nv),
+                                      C.byref(nf)) == N.VH_ERR_INVALID_ARG
+    t = N.VhDeviceTable()
+    assert L.vh_get_device_table(None, C.byref(t)) == N.VH_ERR_INVALID_ARG
     # argument checks come before any device work
     poses = (C.c_float * 16)()
     out = (C.c_float * 16)()
