@@ -401,6 +401,18 @@ void vh_tuning_variants(int32_t *integrate, int32_t *mc);
 vh_status vh_autotune(vh_handle *h, const void *depth, int32_t depth_fmt, const uint8_t *rgb,
                       const float *c2w, int32_t mem, vh_tuning *chosen);
 
+/* Decodes a grayscale PNG depth image (8- or 16-bit samples, not
+ * interlaced; 16-bit is the millimetre format the reference reads with
+ * cv::imread(path, -1) before scaling to metres, src/SaveFrame.cpp:174-180)
+ * into out[height * width] uint16, row-major, ready for vh_integrate as
+ * VH_DEPTH_U16_MM.  out == NULL: *width and *height only.  Chunk CRCs and
+ * the zlib Adler-32 are checked; a malformed stream gives
+ * VH_ERR_INVALID_ARG, another colour type, bit depth or interlacing
+ * VH_ERR_UNSUPPORTED, capacity < width * height VH_ERR_CAPACITY (the size
+ * is reported anyway).  Images up to 2^26 pixels.  Host only. */
+vh_status vh_decode_depth_png(const uint8_t *png, int64_t bytes, uint16_t *out,
+                              int64_t capacity, int32_t *width, int32_t *height);
+
 /* The depth pre-filter of VH_FLAG_DEPTH_FILTER applied to one image: an
  * edge-preserving bilateral filter over 5x5 pixels (spatial sigma 2 px,
  * range sigma 5 mm + 1.5e-3 d^2 x 3, neighbours beyond 3 range sigmas or

@@ -1,0 +1,155 @@
+"""vh_decode_depth_png: grayscale PNG depth frames (the reference reads its
+depth frames with cv::imread(path, -1), src/SaveFrame.cpp:174-180) decoded
+by the library into uint16.  The PNGs are written here by a small encoder
+over Python's zlib: every filter type, stored / fixed-Huffman / dynamic
+blocks, several IDAT chunks, 8- and 16-bit samples; the decoded image must
+equal the encoder's input exactly.  Corrupt and unsupported files give a
+status, never a crash.  Host only (no GPU)."""
+import struct
+import zlib
+
+import numpy as np
+import pytest
+
+from vhsdf import VhError, decode_depth_png, synth
+from vhsdf import _native as N
+
+
+def _chunk(kind, data):
+    body = kind + data
+    return struct.pack(">I", len(data)) + body + struct.pack(">I", zlib.crc32(body) & 0xFFFFFFFF)
+
+
+def _paeth(a, b, c):
+    p = a + b - c
+    pa, pb, pc = abs(p - a), abs(p - b), abs(p - c)
+    return np.where((pa <= pb) & (pa <= pc), a, np.where(pb <= pc, b, c))
+
+
+def _filter_row(ft, cur, prev, bpp):
+    """PNG filter `ft` of one row of bytes (cur, prev: int arrays)."""
+    left = np.concatenate([np.zeros(bpp, np.int64), cur[:-bpp]])
+    upleft = np.concatenate([np.zeros(bpp, np.int64), prev[:-bpp]])
+    if ft == 0:
+        pred = np.zeros_like(cur)
+    elif ft == 1:
+        pred = left
+    elif ft == 2:
+        pred = prev
+    elif ft == 3:
+        pred = (left + prev) >> 1
+    else:
+        pred = _paeth(left, prev, upleft)
+    return ((cur - pred) & 0xFF).astype(np.uint8)
+
+
+def encode_png(img, depth=16, filters=None, level=6, strategy=zlib.Z_DEFAULT_STRATEGY,
+               idat_parts=1, interlace=0, colour=0):
+    """A grayscale PNG of `img` (uint16 or uint8, (h, w)); filters: one
+    filter type per row, cycled."""
+    h, w = img.shape
+    if depth == 16:
+        raw = img.astype(">u2").view(np.uint8).reshape(h, 2 * w)
+    else:
+        raw = img.astype(np.uint8).reshape(h, w)
+    bpp = depth // 8
+    filters = filters or [0]
+    rows = []
+    prev = np.zeros(raw.shape[1], np.int64)
+    for y in range(h):
+        cur = raw[y].astype(np.int64)
+        ft = filters[y % len(filters)]
+        rows.append(bytes([ft]) + _filter_row(ft, cur, prev, bpp).tobytes())
+        prev = cur
+    co = zlib.compressobj(level, zlib.DEFLATED, 15, 8, strategy)
+    z = co.compress(b"".join(rows)) + co.flush()
+    parts = [z[i * len(z) // idat_parts:(i + 1) * len(z) // idat_parts] for i in range(idat_parts)]
+    ihdr = struct.pack(">IIBBBBB", w, h, depth, colour, 0, 0, interlace)
+    return (b"\x89PNG\r\n\x1a\n" + _chunk(b"IHDR", ihdr) + _chunk(b"tEXt", b"k\x00v") +
+            b"".join(_chunk(b"IDAT", p) for p in parts) + _chunk(b"IEND", b""))
+
+
+def depth_frame(w=160, h=120):
+    d, _, _ = synth.Scene(kind=1, seed=0, num_frames=2, width=w, height=h).render(0)
+    return d
+
+
+@pytest.mark.parametrize("filters", [[0], [1], [2], [3], [4], [0, 1, 2, 3, 4], [4, 3, 2, 1, 0]])
+def test_every_filter_type(filters):
+    img = depth_frame()
+    assert img.dtype == np.uint16 and img.max() > 1000
+    out = decode_depth_png(encode_png(img, filters=filters))
+    assert out.dtype == np.uint16 and np.array_equal(out, img)
+
+
+@pytest.mark.parametrize("level,strategy", [(0, zlib.Z_DEFAULT_STRATEGY),
+                                            (1, zlib.Z_DEFAULT_STRATEGY),
+                                            (9, zlib.Z_DEFAULT_STRATEGY),
+                                            (6, zlib.Z_FIXED),
+                                            (6, zlib.Z_HUFFMAN_ONLY),
+                                            (6, zlib.Z_RLE)])
+def test_block_kinds(level, strategy):
+    """Stored blocks (level 0), fixed-Huffman blocks (Z_FIXED), literal-only
+    and run-length streams, and dynamic blocks."""
+    rng = np.random.default_rng(level * 10 + strategy)
+    img = depth_frame()
+    img[rng.random(img.shape) < 0.05] = 0  # dropouts, as real depth has
+    out = decode_depth_png(encode_png(img, filters=[0, 1, 2, 3, 4], level=level,
+                                      strategy=strategy, idat_parts=3))
+    assert np.array_equal(out, img)
+
+
+def test_full_size_frame_and_noise():
+    img = depth_frame(640, 480)
+    assert np.array_equal(decode_depth_png(encode_png(img, filters=[4, 1])), img)
+    noise = np.random.default_rng(7).integers(0, 65536, (37, 53), dtype=np.uint16)
+    assert np.array_equal(decode_depth_png(encode_png(noise, filters=[0, 1, 2, 3, 4])), noise)
+
+
+def test_eight_bit_and_tiny_images():
+    g = np.random.default_rng(1).integers(0, 256, (9, 13)).astype(np.uint8)
+    out = decode_depth_png(encode_png(g, depth=8, filters=[0, 1, 2, 3, 4]))
+    assert out.dtype == np.uint16 and np.array_equal(out, g.astype(np.uint16))
+    for shape in [(1, 1), (1, 17), (17, 1)]:
+        img = np.arange(np.prod(shape), dtype=np.uint16).reshape(shape) * 977
+        assert np.array_equal(decode_depth_png(encode_png(img, filters=[4])), img)
+
+
+def test_size_query_and_capacity():
+    import ctypes as C
+    img = depth_frame(64, 48)
+    png = np.frombuffer(encode_png(img), np.uint8)
+    L = N.lib()
+    w, h = C.c_int32(), C.c_int32()
+    assert L.vh_decode_depth_png(png.ctypes.data, png.size, None, 0, C.byref(w),
+                                 C.byref(h)) == N.VH_OK
+    assert (w.value, h.value) == (64, 48)
+    small = np.zeros(100, np.uint16)
+    assert L.vh_decode_depth_png(png.ctypes.data, png.size, small.ctypes.data, small.size,
+                                 C.byref(w), C.byref(h)) == N.VH_ERR_CAPACITY
+
+
+def test_corrupt_and_unsupported_files():
+    img = depth_frame(64, 48)
+    good = encode_png(img, filters=[0, 1, 2, 3, 4])
+    bad_crc = bytearray(good)
+    bad_crc[40] ^= 0x01  # inside IHDR/tEXt/IDAT: its chunk CRC no longer matches
+    cases = [b"not a png at all", good[:7], good[:60], good[:-12], bytes(bad_crc)]
+    for data in cases:
+        with pytest.raises(VhError) as e:
+            decode_depth_png(data)
+        assert e.value.status == N.VH_ERR_INVALID_ARG
+    for kw in (dict(interlace=1), dict(colour=2)):
+        with pytest.raises(VhError) as e:
+            decode_depth_png(encode_png(img, **kw))
+        assert e.value.status == N.VH_ERR_UNSUPPORTED
+    # damaged compressed data with valid chunk CRCs: the Adler-32 or the
+    # inflater rejects it
+    z = zlib.compress(b"\x00" + b"\x01" * 10)
+    broken = z[:2] + bytes([z[2] ^ 0xFF]) + z[3:]
+    ihdr = struct.pack(">IIBBBBB", 5, 1, 16, 0, 0, 0, 0)
+    png = (b"\x89PNG\r\n\x1a\n" + _chunk(b"IHDR", ihdr) + _chunk(b"IDAT", broken) +
+           _chunk(b"IEND", b""))
+    with pytest.raises(VhError) as e:
+        decode_depth_png(png)
+    assert e.value.status == N.VH_ERR_INVALID_ARG

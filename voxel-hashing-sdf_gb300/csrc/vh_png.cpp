@@ -1,0 +1,389 @@
+// vh_png.cpp - grayscale PNG depth images to uint16 (vh_decode_depth_png).
+//
+// The reference loads each depth frame with cv::imread(path, -1), a 16-bit
+// grayscale PNG of millimetres, and converts it to float metres
+// (src/SaveFrame.cpp:174-180).  Here the PNG is decoded into the uint16
+// millimetre image that vh_integrate takes as VH_DEPTH_U16_MM, so the scale
+// to metres happens inside the allocation kernel and the host never holds a
+// float copy.  The decoder follows the PNG specification (chunk layout,
+// CRC-32, filter types 0-4 with the Paeth predictor) and RFC 1950/1951
+// (zlib wrapper with Adler-32, DEFLATE stored / fixed / dynamic Huffman
+// blocks); every read is bounds-checked and the output size is fixed by the
+// header before anything is inflated.
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "../../include/vhsdf.h"
+
+namespace {
+
+// ---- CRC-32 (PNG chunks) and Adler-32 (zlib stream) ----------------------
+struct CrcTable {
+  uint32_t v[256];
+  CrcTable() {  // the reflected polynomial 0xEDB88320
+    for (uint32_t i = 0; i < 256; ++i) {
+      uint32_t c = i;
+      for (int k = 0; k < 8; ++k) c = (c & 1u) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
+      v[i] = c;
+    }
+  }
+};
+
+uint32_t crc32_of(const uint8_t *p, size_t n) {
+  static const CrcTable table;  // built once, thread-safe
+  uint32_t c = 0xFFFFFFFFu;
+  for (size_t i = 0; i < n; ++i) c = table.v[(c ^ p[i]) & 0xFFu] ^ (c >> 8);
+  return c ^ 0xFFFFFFFFu;
+}
+
+uint32_t adler32_of(const uint8_t *p, size_t n) {
+  uint32_t a = 1, b = 0;
+  while (n) {  // 5552 bytes keep b below 2^32 before the reduction
+    const size_t k = n < 5552 ? n : 5552;
+    for (size_t i = 0; i < k; ++i) {
+      a += p[i];
+      b += a;
+    }
+    a %= 65521u;
+    b %= 65521u;
+    p += k;
+    n -= k;
+  }
+  return (b << 16) | a;
+}
+
+uint32_t be32(const uint8_t *p) {
+  return ((uint32_t)p[0] << 24) | ((uint32_t)p[1] << 16) | ((uint32_t)p[2] << 8) | (uint32_t)p[3];
+}
+
+// ---- DEFLATE (RFC 1951) ---------------------------------------------------
+// Bits least significant first, through a 64-bit buffer; reading past the
+// end pads with zeros and marks the reader bad.
+struct BitReader {
+  const uint8_t *p;
+  size_t n;
+  size_t pos = 0;         // next byte to load
+  uint64_t buf = 0;       // loaded, unconsumed bits
+  int cnt = 0;            // bits in buf
+  uint64_t consumed = 0;  // bits consumed from the start
+  bool bad = false;
+  void refill() {
+    while (cnt <= 56) {
+      if (pos < n) buf |= (uint64_t)p[pos] << cnt;
+      ++pos;  // past the end: zeros, caught by the consumed count
+      cnt += 8;
+    }
+  }
+  uint32_t peek(int count) {  // count <= 32
+    refill();
+    return (uint32_t)(buf & ((1ull << count) - 1ull));
+  }
+  void drop(int count) {
+    buf >>= count;
+    cnt -= count;
+    consumed += (uint64_t)count;
+    if (consumed > 8ull * n) bad = true;
+  }
+  int get(int count) {  // count <= 32
+    if (count == 0) return 0;
+    const uint32_t v = peek(count);
+    drop(count);
+    return (int)v;
+  }
+  void align() {
+    const int r = (int)(consumed & 7u);
+    if (r) drop(8 - r);
+  }
+  // `len` whole bytes at a byte boundary, copied straight from the input
+  bool copy_bytes(size_t len, std::vector<uint8_t> &out) {
+    const size_t at = (size_t)(consumed >> 3);
+    if ((consumed & 7u) || at > n || len > n - at) return false;
+    out.insert(out.end(), p + at, p + at + len);
+    consumed += 8ull * len;
+    pos = at + len;  // reload from here: the buffered bits are past it
+    buf = 0;
+    cnt = 0;
+    return true;
+  }
+};
+
+// Canonical Huffman code from code lengths: a table indexed by the next
+// kFastBits input bits for the codes that short, and the count of codes per
+// length with the symbols ordered by (length, symbol) for the longer ones.
+constexpr int kFastBits = 9;
+struct Huffman {
+  uint16_t count[16] = {};
+  std::vector<uint16_t> symbol;
+  uint16_t fast[1 << kFastBits] = {};  // symbol << 4 | length, 0 = longer code
+  // false for an over-subscribed set of lengths
+  bool build(const uint8_t *len, int n) {
+    std::memset(count, 0, sizeof(count));
+    std::memset(fast, 0, sizeof(fast));
+    for (int s = 0; s < n; ++s) count[len[s]]++;
+    count[0] = 0;
+    int left = 1;
+    for (int l = 1; l < 16; ++l) {
+      left <<= 1;
+      left -= count[l];
+      if (left < 0) return false;
+    }
+    uint16_t offs[16] = {};
+    for (int l = 1; l < 15; ++l) offs[l + 1] = (uint16_t)(offs[l] + count[l]);
+    symbol.assign((size_t)n, 0);
+    for (int s = 0; s < n; ++s)
+      if (len[s]) symbol[offs[len[s]]++] = (uint16_t)s;
+    // canonical codes (RFC 1951 3.2.2), stored most significant bit first in
+    // the stream: the table index is the code's bits reversed
+    uint32_t next[16] = {};
+    uint32_t code = 0;
+    for (int l = 1; l < 16; ++l) {
+      code = (code + count[l - 1]) << 1;
+      next[l] = code;
+    }
+    for (int s = 0; s < n; ++s) {
+      const int l = len[s];
+      if (!l) continue;
+      const uint32_t c = next[l]++;
+      if (l > kFastBits) continue;
+      uint32_t rev = 0;
+      for (int i = 0; i < l; ++i) rev |= ((c >> i) & 1u) << (l - 1 - i);
+      for (uint32_t k = rev; k < (1u << kFastBits); k += 1u << l)
+        fast[k] = (uint16_t)((s << 4) | l);
+    }
+    return true;
+  }
+  // one symbol, or -1 when the input ends or matches no code
+  int decode(BitReader &br) const {
+    const uint16_t e = fast[br.peek(kFastBits)];
+    if (e) {
+      br.drop(e & 15);
+      return br.bad ? -1 : (int)(e >> 4);
+    }
+    int code = 0, first = 0, index = 0;
+    for (int l = 1; l < 16; ++l) {
+      code |= br.get(1);
+      if (br.bad) return -1;
+      const int c = count[l];
+      if (code - first < c) return symbol[(size_t)(index + code - first)];
+      index += c;
+      first = (first + c) << 1;
+      code <<= 1;
+    }
+    return -1;
+  }
+};
+
+const uint16_t kLenBase[29] = {3,  4,  5,  6,  7,  8,  9,  10, 11,  13,  15,  17,  19,  23, 27,
+                               31, 35, 43, 51, 59, 67, 83, 99, 115, 131, 163, 195, 227, 258};
+const uint8_t kLenExtra[29] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2,
+                               2, 3, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 0};
+const uint16_t kDistBase[30] = {1,    2,    3,    4,    5,    7,     9,     13,    17,  25,
+                                33,   49,   65,   97,   129,  193,   257,   385,   513, 769,
+                                1025, 1537, 2049, 3073, 4097, 6145,  8193,  12289, 16385, 24577};
+const uint8_t kDistExtra[30] = {0, 0, 0, 0, 1, 1, 2, 2,  3,  3,  4,  4,  5,  5,  6,
+                                6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
+
+// Inflates a raw DEFLATE stream into out, which must end up exactly `want`
+// bytes long (more output is an error: the size comes from the PNG header).
+bool inflate(BitReader &br, std::vector<uint8_t> &out, size_t want) {
+  out.clear();
+  out.reserve(want < ((size_t)1 << 26) ? want : ((size_t)1 << 26));
+  Huffman fixed_lit, fixed_dist;
+  {
+    uint8_t l[288];
+    for (int s = 0; s < 288; ++s) l[s] = s < 144 ? 8 : (s < 256 ? 9 : (s < 280 ? 7 : 8));
+    fixed_lit.build(l, 288);
+    uint8_t d[30];
+    for (int s = 0; s < 30; ++s) d[s] = 5;
+    fixed_dist.build(d, 30);
+  }
+  for (;;) {
+    const int last = br.get(1);
+    const int type = br.get(2);
+    if (br.bad) return false;
+    if (type == 0) {  // stored: byte-aligned LEN, ~LEN, then LEN raw bytes
+      br.align();
+      const uint32_t len = (uint32_t)br.get(16), nlen = (uint32_t)br.get(16);
+      if (br.bad || (len ^ 0xFFFFu) != nlen || out.size() + len > want) return false;
+      if (!br.copy_bytes(len, out)) return false;
+    } else if (type == 1 || type == 2) {
+      Huffman dyn_lit, dyn_dist;
+      const Huffman *lit = &fixed_lit, *dist = &fixed_dist;
+      if (type == 2) {
+        const int hlit = br.get(5) + 257, hdist = br.get(5) + 1, hclen = br.get(4) + 4;
+        static const uint8_t order[19] = {16, 17, 18, 0, 8,  7, 9,  6, 10, 5,
+                                          11, 4,  12, 3, 13, 2, 14, 1, 15};
+        uint8_t cl[19] = {};
+        for (int i = 0; i < hclen; ++i) cl[order[i]] = (uint8_t)br.get(3);
+        if (br.bad || hlit > 286 || hdist > 30) return false;
+        Huffman clh;
+        if (!clh.build(cl, 19)) return false;
+        uint8_t lens[286 + 30] = {};
+        int k = 0;
+        while (k < hlit + hdist) {
+          const int sym = clh.decode(br);
+          if (sym < 0) return false;
+          if (sym < 16) {
+            lens[k++] = (uint8_t)sym;
+            continue;
+          }
+          int rep = 0;
+          uint8_t val = 0;
+          if (sym == 16) {
+            if (k == 0) return false;
+            val = lens[k - 1];
+            rep = 3 + br.get(2);
+          } else if (sym == 17) {
+            rep = 3 + br.get(3);
+          } else {
+            rep = 11 + br.get(7);
+          }
+          if (br.bad || k + rep > hlit + hdist) return false;
+          while (rep--) lens[k++] = val;
+        }
+        if (lens[256] == 0) return false;  // no end-of-block code
+        if (!dyn_lit.build(lens, hlit) || !dyn_dist.build(lens + hlit, hdist)) return false;
+        lit = &dyn_lit;
+        dist = &dyn_dist;
+      }
+      for (;;) {
+        const int sym = lit->decode(br);
+        if (sym < 0) return false;
+        if (sym < 256) {
+          if (out.size() >= want) return false;
+          out.push_back((uint8_t)sym);
+        } else if (sym == 256) {
+          break;
+        } else {
+          const int li = sym - 257;
+          if (li >= 29) return false;
+          const size_t len = kLenBase[li] + (size_t)br.get(kLenExtra[li]);
+          const int di = dist->decode(br);
+          if (di < 0 || di >= 30) return false;
+          const size_t d = kDistBase[di] + (size_t)br.get(kDistExtra[di]);
+          if (br.bad || d > out.size() || out.size() + len > want) return false;
+          const size_t from = out.size() - d;
+          for (size_t i = 0; i < len; ++i) out.push_back(out[from + i]);  // may overlap
+        }
+      }
+    } else {
+      return false;
+    }
+    if (last) return out.size() == want;
+  }
+}
+
+// The Paeth predictor: of a (left), b (above) and c (above-left), the one
+// nearest to a + b - c, ties in the order a, b, c.  With p = a + b - c the
+// distances are |p - a| = |b - c|, |p - b| = |a - c|, |p - c| = |a + b - 2c|.
+inline int paeth(int a, int b, int c) {
+  const int pa = std::abs(b - c), pb = std::abs(a - c), pc = std::abs(a + b - 2 * c);
+  const int ab = pb < pa ? b : a, dab = pb < pa ? pb : pa;
+  return pc < dab ? c : ab;
+}
+
+}  // namespace
+
+extern "C" vh_status vh_decode_depth_png(const uint8_t *png, int64_t bytes, uint16_t *out,
+                                         int64_t capacity, int32_t *width, int32_t *height) {
+  static const uint8_t kSig[8] = {0x89, 'P', 'N', 'G', '\r', '\n', 0x1A, '\n'};
+  if (!png || bytes < 8 || capacity < 0 || !width || !height) return VH_ERR_INVALID_ARG;
+  if (std::memcmp(png, kSig, 8) != 0) return VH_ERR_INVALID_ARG;
+  const size_t n = (size_t)bytes;
+  size_t pos = 8;
+  uint32_t w = 0, h = 0;
+  int depth = 0;
+  bool have_header = false, have_end = false;
+  std::vector<uint8_t> idat;
+  while (pos + 12 <= n) {
+    const uint32_t len = be32(png + pos);
+    if (len > n - pos - 12) return VH_ERR_INVALID_ARG;
+    const uint8_t *type = png + pos + 4, *data = png + pos + 8;
+    if (crc32_of(type, (size_t)len + 4) != be32(data + len)) return VH_ERR_INVALID_ARG;
+    if (std::memcmp(type, "IHDR", 4) == 0) {
+      if (len != 13 || have_header) return VH_ERR_INVALID_ARG;
+      w = be32(data);
+      h = be32(data + 4);
+      depth = data[8];
+      const int colour = data[9], compression = data[10], filter = data[11], interlace = data[12];
+      if (w == 0 || h == 0 || w > 32768 || h > 32768 || (uint64_t)w * h > ((uint64_t)1 << 26))
+        return VH_ERR_INVALID_ARG;
+      if (colour != 0 || (depth != 8 && depth != 16) || compression != 0 || filter != 0 ||
+          interlace != 0)
+        return VH_ERR_UNSUPPORTED;  // only non-interlaced 8/16-bit grayscale
+      have_header = true;
+      if (!out) {  // size query: the header is enough
+        *width = (int32_t)w;
+        *height = (int32_t)h;
+        return VH_OK;
+      }
+    } else if (std::memcmp(type, "IDAT", 4) == 0) {
+      if (!have_header) return VH_ERR_INVALID_ARG;
+      idat.insert(idat.end(), data, data + len);
+    } else if (std::memcmp(type, "IEND", 4) == 0) {
+      have_end = true;
+      break;
+    } else if (!(type[0] & 0x20)) {  // an unknown critical chunk
+      return VH_ERR_UNSUPPORTED;
+    }
+    pos += (size_t)len + 12;
+  }
+  if (!have_header || !have_end || idat.size() < 6) return VH_ERR_INVALID_ARG;
+  *width = (int32_t)w;
+  *height = (int32_t)h;
+  const int64_t npx = (int64_t)w * (int64_t)h;
+  if (!out) return VH_OK;  // size query
+  if (capacity < npx) return VH_ERR_CAPACITY;
+  // zlib wrapper: CM 8 with a window of at most 32 KiB, no preset dictionary
+  const uint8_t cmf = idat[0], flg = idat[1];
+  if ((cmf & 0x0F) != 8 || (cmf >> 4) > 7 || ((cmf << 8) | flg) % 31 != 0 || (flg & 0x20))
+    return VH_ERR_INVALID_ARG;
+  const int bpp = depth / 8;
+  const size_t stride = (size_t)w * (size_t)bpp;
+  const size_t raw_size = (size_t)h * (stride + 1);
+  std::vector<uint8_t> raw;
+  BitReader br{idat.data() + 2, idat.size() - 6};  // between the zlib header and Adler-32
+  if (!inflate(br, raw, raw_size)) return VH_ERR_INVALID_ARG;
+  if (adler32_of(raw.data(), raw.size()) != be32(idat.data() + idat.size() - 4))
+    return VH_ERR_INVALID_ARG;
+  // unfilter row by row in place (a is the byte bpp to the left, b the one
+  // above, c above-left), then the big-endian samples to native uint16
+  std::vector<uint8_t> prev(stride, 0);
+  for (uint32_t y = 0; y < h; ++y) {
+    uint8_t *row = raw.data() + (size_t)y * (stride + 1);
+    const int ft = row[0];
+    uint8_t *cur = row + 1;
+    const uint8_t *up = prev.data();
+    const size_t k = (size_t)bpp;
+    switch (ft) {  // a: the byte bpp to the left, b: above, c: above-left
+      case 0:
+        break;
+      case 1:
+        for (size_t i = k; i < stride; ++i) cur[i] = (uint8_t)(cur[i] + cur[i - k]);
+        break;
+      case 2:
+        for (size_t i = 0; i < stride; ++i) cur[i] = (uint8_t)(cur[i] + up[i]);
+        break;
+      case 3:
+        for (size_t i = 0; i < stride; ++i)
+          cur[i] = (uint8_t)(cur[i] + (((i >= k ? cur[i - k] : 0) + up[i]) >> 1));
+        break;
+      case 4:
+        for (size_t i = 0; i < stride; ++i)
+          cur[i] = (uint8_t)(cur[i] + paeth(i >= k ? cur[i - k] : 0, up[i], i >= k ? up[i - k] : 0));
+        break;
+      default:
+        return VH_ERR_INVALID_ARG;
+    }
+    uint16_t *dst = out + (size_t)y * w;
+    if (bpp == 2)
+      for (uint32_t x = 0; x < w; ++x)
+        dst[x] = (uint16_t)(((uint32_t)cur[2 * x] << 8) | cur[2 * x + 1]);
+    else
+      for (uint32_t x = 0; x < w; ++x) dst[x] = cur[x];
+    std::memcpy(prev.data(), cur, stride);
+  }
+  return VH_OK;
+}

@@ -489,3 +489,18 @@ class Volume:
 def block_hash_ref(x, y, z):
     """The reference's BlockHasher value (include/tsdf.cuh:144-156)."""
     return int(N.lib().vh_block_hash_ref(int(x), int(y), int(z)))
+
+
+def decode_depth_png(data):
+    """A grayscale PNG depth image (bytes) as a (height, width) uint16 array,
+    decoded by the library (vh_decode_depth_png): the millimetre frames the
+    reference reads with cv::imread (src/SaveFrame.cpp:174-180), ready for
+    Volume.integrate as VH_DEPTH_U16_MM."""
+    buf = np.frombuffer(bytes(data), np.uint8)
+    L = N.lib()
+    w, h = C.c_int32(), C.c_int32()
+    N.check(L.vh_decode_depth_png(buf.ctypes.data, buf.size, None, 0, C.byref(w), C.byref(h)))
+    out = np.empty((h.value, w.value), np.uint16)
+    N.check(L.vh_decode_depth_png(buf.ctypes.data, buf.size, out.ctypes.data, out.size,
+                                  C.byref(w), C.byref(h)))
+    return out
