@@ -413,6 +413,29 @@ vh_status vh_autotune(vh_handle *h, const void *depth, int32_t depth_fmt, const 
 vh_status vh_decode_depth_png(const uint8_t *png, int64_t bytes, uint16_t *out,
                               int64_t capacity, int32_t *width, int32_t *height);
 
+/* Decodes a PNG colour frame (RGB, RGBA, grayscale or grayscale + alpha;
+ * 8- or 16-bit samples; not interlaced) into rgb[height * width * 3]
+ * interleaved R, G, B bytes, row-major: the colour image vh_integrate takes.
+ * It stands in for the reference's cv::imread(path, IMREAD_COLOR) followed
+ * by its BGR-to-RGB swap (src/SaveFrame.cpp:164, src/main.cpp:273): 16-bit
+ * samples keep their high byte, grayscale fills all three channels, alpha is
+ * dropped.  rgb == NULL: *width and *height only.  Errors as for
+ * vh_decode_depth_png (palette images and bit depths below 8:
+ * VH_ERR_UNSUPPORTED; capacity, in bytes, < 3 * width * height:
+ * VH_ERR_CAPACITY).  Host only. */
+vh_status vh_decode_colour_png(const uint8_t *png, int64_t bytes, uint8_t *rgb,
+                               int64_t capacity, int32_t *width, int32_t *height);
+
+/* Resizes an interleaved RGB u8 image (src_height x src_width x 3) to
+ * dst_height x dst_width x 3 by bilinear interpolation, the way the
+ * reference brings every colour frame to the depth frame's 640 x 480 grid
+ * with cv::resize (src/SaveFrame.cpp:164-171): pixel centres at
+ * half-integer positions, sources clamped at the borders, weights in double
+ * rounded to the nearest level (OpenCV's fixed-point weights may differ by
+ * one level on some pixels).  Sizes 1 .. 32768 per side.  Host only. */
+vh_status vh_resize_colour(const uint8_t *src, int32_t src_width, int32_t src_height,
+                           uint8_t *dst, int32_t dst_width, int32_t dst_height);
+
 /* The depth pre-filter of VH_FLAG_DEPTH_FILTER applied to one image: an
  * edge-preserving bilateral filter over 5x5 pixels (spatial sigma 2 px,
  * range sigma 5 mm + 1.5e-3 d^2 x 3, neighbours beyond 3 range sigmas or

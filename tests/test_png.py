@@ -2,71 +2,19 @@
 depth frames with cv::imread(path, -1), src/SaveFrame.cpp:174-180) decoded
 by the library into uint16.  The PNGs are written here by a small encoder
 over Python's zlib: every filter type, stored / fixed-Huffman / dynamic
-blocks, several IDAT chunks, 8- and 16-bit samples; the decoded image must
-equal the encoder's input exactly.  Corrupt and unsupported files give a
-status, never a crash.  Host only (no GPU)."""
+blocks, several IDAT chunks, 8- and 16-bit samples (tests/png_writer.py);
+the decoded image must equal the encoder's input exactly.  Corrupt and
+unsupported files give a status, never a crash.  Host only (no GPU)."""
 import struct
 import zlib
 
 import numpy as np
 import pytest
 
+from png_writer import chunk as _chunk
+from png_writer import encode_png
 from vhsdf import VhError, decode_depth_png, synth
 from vhsdf import _native as N
-
-
-def _chunk(kind, data):
-    body = kind + data
-    return struct.pack(">I", len(data)) + body + struct.pack(">I", zlib.crc32(body) & 0xFFFFFFFF)
-
-
-def _paeth(a, b, c):
-    p = a + b - c
-    pa, pb, pc = abs(p - a), abs(p - b), abs(p - c)
-    return np.where((pa <= pb) & (pa <= pc), a, np.where(pb <= pc, b, c))
-
-
-def _filter_row(ft, cur, prev, bpp):
-    """PNG filter `ft` of one row of bytes (cur, prev: int arrays)."""
-    left = np.concatenate([np.zeros(bpp, np.int64), cur[:-bpp]])
-    upleft = np.concatenate([np.zeros(bpp, np.int64), prev[:-bpp]])
-    if ft == 0:
-        pred = np.zeros_like(cur)
-    elif ft == 1:
-        pred = left
-    elif ft == 2:
-        pred = prev
-    elif ft == 3:
-        pred = (left + prev) >> 1
-    else:
-        pred = _paeth(left, prev, upleft)
-    return ((cur - pred) & 0xFF).astype(np.uint8)
-
-
-def encode_png(img, depth=16, filters=None, level=6, strategy=zlib.Z_DEFAULT_STRATEGY,
-               idat_parts=1, interlace=0, colour=0):
-    """A grayscale PNG of `img` (uint16 or uint8, (h, w)); filters: one
-    filter type per row, cycled."""
-    h, w = img.shape
-    if depth == 16:
-        raw = img.astype(">u2").view(np.uint8).reshape(h, 2 * w)
-    else:
-        raw = img.astype(np.uint8).reshape(h, w)
-    bpp = depth // 8
-    filters = filters or [0]
-    rows = []
-    prev = np.zeros(raw.shape[1], np.int64)
-    for y in range(h):
-        cur = raw[y].astype(np.int64)
-        ft = filters[y % len(filters)]
-        rows.append(bytes([ft]) + _filter_row(ft, cur, prev, bpp).tobytes())
-        prev = cur
-    co = zlib.compressobj(level, zlib.DEFLATED, 15, 8, strategy)
-    z = co.compress(b"".join(rows)) + co.flush()
-    parts = [z[i * len(z) // idat_parts:(i + 1) * len(z) // idat_parts] for i in range(idat_parts)]
-    ihdr = struct.pack(">IIBBBBB", w, h, depth, colour, 0, 0, interlace)
-    return (b"\x89PNG\r\n\x1a\n" + _chunk(b"IHDR", ihdr) + _chunk(b"tEXt", b"k\x00v") +
-            b"".join(_chunk(b"IDAT", p) for p in parts) + _chunk(b"IEND", b""))
 
 
 def depth_frame(w=160, h=120):

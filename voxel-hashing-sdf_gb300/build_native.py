@@ -41,6 +41,7 @@ ENGINE_SOURCES = [
     ("vh_raycast.cu", []),
     ("vh_stream.cu", []),
     ("vh_png.cpp", []),
+    ("vh_frames.cpp", []),
 ]
 ENGINE_HEADERS = ["vh_common.cuh", "vh_device.cuh", "vh_mc_tables.h", "vh_mesh.h", "vh_internal.h"]
 

@@ -1,11 +1,15 @@
-// vh_png.cpp - grayscale PNG depth images to uint16 (vh_decode_depth_png).
+// vh_png.cpp - PNG frames for the integration inputs: grayscale depth images
+// to uint16 (vh_decode_depth_png) and colour images to interleaved RGB u8
+// (vh_decode_colour_png).
 //
 // The reference loads each depth frame with cv::imread(path, -1), a 16-bit
 // grayscale PNG of millimetres, and converts it to float metres
 // (src/SaveFrame.cpp:174-180).  Here the PNG is decoded into the uint16
 // millimetre image that vh_integrate takes as VH_DEPTH_U16_MM, so the scale
 // to metres happens inside the allocation kernel and the host never holds a
-// float copy.  The decoder follows the PNG specification (chunk layout,
+// float copy.  Its colour frames go through cv::imread(path, IMREAD_COLOR)
+// and a BGR-to-RGB swap (src/SaveFrame.cpp:164, src/main.cpp:273); the
+// colour decoder gives the RGB bytes directly.  The decoder follows the PNG specification (chunk layout,
 // CRC-32, filter types 0-4 with the Paeth predictor) and RFC 1950/1951
 // (zlib wrapper with Adler-32, DEFLATE stored / fixed / dynamic Huffman
 // blocks); every read is bounds-checked and the output size is fixed by the
@@ -284,17 +288,65 @@ inline int paeth(int a, int b, int c) {
   return pc < dab ? c : ab;
 }
 
-}  // namespace
+// Undoes one row's PNG filter in place: cur holds the filtered bytes, up the
+// previous row's unfiltered bytes (zeros above the first row), k the bytes
+// per pixel (a: the byte k to the left, b: above, c: above-left).
+bool unfilter_row(uint8_t *cur, const uint8_t *up, size_t stride, size_t k, int ft) {
+  switch (ft) {
+    case 0:
+      return true;
+    case 1:
+      for (size_t i = k; i < stride; ++i) cur[i] = (uint8_t)(cur[i] + cur[i - k]);
+      return true;
+    case 2:
+      for (size_t i = 0; i < stride; ++i) cur[i] = (uint8_t)(cur[i] + up[i]);
+      return true;
+    case 3:
+      for (size_t i = 0; i < stride; ++i)
+        cur[i] = (uint8_t)(cur[i] + (((i >= k ? cur[i - k] : 0) + up[i]) >> 1));
+      return true;
+    case 4:
+      for (size_t i = 0; i < stride; ++i)
+        cur[i] = (uint8_t)(cur[i] + paeth(i >= k ? cur[i - k] : 0, up[i], i >= k ? up[i - k] : 0));
+      return true;
+    default:
+      return false;
+  }
+}
 
-extern "C" vh_status vh_decode_depth_png(const uint8_t *png, int64_t bytes, uint16_t *out,
-                                         int64_t capacity, int32_t *width, int32_t *height) {
+// One decoded PNG: rows of `stride` unfiltered bytes, each after its filter
+// byte at raw[y * (stride + 1) + 1]; samples big-endian as in the file.
+struct PngImage {
+  uint32_t w = 0, h = 0;
+  int depth = 0, channels = 0;
+  size_t stride = 0;
+  std::vector<uint8_t> raw;
+  const uint8_t *row(uint32_t y) const { return raw.data() + (size_t)y * (stride + 1) + 1; }
+};
+
+// Channels of a PNG colour type that the decoder reads (grayscale, RGB,
+// grayscale + alpha, RGBA), 0 for the palette type and unknown ones.
+int png_channels(int colour) {
+  switch (colour) {
+    case 0: return 1;
+    case 2: return 3;
+    case 4: return 2;
+    case 6: return 4;
+    default: return 0;
+  }
+}
+
+// Parses the chunks, checks every CRC, and (pixels == true) inflates and
+// unfilters the image data.  `gray_only` admits colour type 0 alone.  Only
+// 8- and 16-bit samples, without interlacing, are read.  With pixels ==
+// false it returns after IHDR, having filled w, h, depth and channels.
+vh_status png_decode(const uint8_t *png, int64_t bytes, bool gray_only, bool pixels,
+                     PngImage &img) {
   static const uint8_t kSig[8] = {0x89, 'P', 'N', 'G', '\r', '\n', 0x1A, '\n'};
-  if (!png || bytes < 8 || capacity < 0 || !width || !height) return VH_ERR_INVALID_ARG;
+  if (!png || bytes < 8) return VH_ERR_INVALID_ARG;
   if (std::memcmp(png, kSig, 8) != 0) return VH_ERR_INVALID_ARG;
   const size_t n = (size_t)bytes;
   size_t pos = 8;
-  uint32_t w = 0, h = 0;
-  int depth = 0;
   bool have_header = false, have_end = false;
   std::vector<uint8_t> idat;
   while (pos + 12 <= n) {
@@ -304,21 +356,20 @@ extern "C" vh_status vh_decode_depth_png(const uint8_t *png, int64_t bytes, uint
     if (crc32_of(type, (size_t)len + 4) != be32(data + len)) return VH_ERR_INVALID_ARG;
     if (std::memcmp(type, "IHDR", 4) == 0) {
       if (len != 13 || have_header) return VH_ERR_INVALID_ARG;
-      w = be32(data);
-      h = be32(data + 4);
-      depth = data[8];
+      img.w = be32(data);
+      img.h = be32(data + 4);
+      img.depth = data[8];
       const int colour = data[9], compression = data[10], filter = data[11], interlace = data[12];
-      if (w == 0 || h == 0 || w > 32768 || h > 32768 || (uint64_t)w * h > ((uint64_t)1 << 26))
+      if (img.w == 0 || img.h == 0 || img.w > 32768 || img.h > 32768 ||
+          (uint64_t)img.w * img.h > ((uint64_t)1 << 26))
         return VH_ERR_INVALID_ARG;
-      if (colour != 0 || (depth != 8 && depth != 16) || compression != 0 || filter != 0 ||
-          interlace != 0)
-        return VH_ERR_UNSUPPORTED;  // only non-interlaced 8/16-bit grayscale
+      img.channels = png_channels(colour);
+      if (img.channels == 0 || (gray_only && colour != 0) || (img.depth != 8 && img.depth != 16) ||
+          compression != 0 || filter != 0 || interlace != 0)
+        return VH_ERR_UNSUPPORTED;
+      img.stride = (size_t)img.w * (size_t)(img.channels * img.depth / 8);
       have_header = true;
-      if (!out) {  // size query: the header is enough
-        *width = (int32_t)w;
-        *height = (int32_t)h;
-        return VH_OK;
-      }
+      if (!pixels) return VH_OK;  // size query: the header is enough
     } else if (std::memcmp(type, "IDAT", 4) == 0) {
       if (!have_header) return VH_ERR_INVALID_ARG;
       idat.insert(idat.end(), data, data + len);
@@ -331,59 +382,80 @@ extern "C" vh_status vh_decode_depth_png(const uint8_t *png, int64_t bytes, uint
     pos += (size_t)len + 12;
   }
   if (!have_header || !have_end || idat.size() < 6) return VH_ERR_INVALID_ARG;
-  *width = (int32_t)w;
-  *height = (int32_t)h;
-  const int64_t npx = (int64_t)w * (int64_t)h;
-  if (!out) return VH_OK;  // size query
-  if (capacity < npx) return VH_ERR_CAPACITY;
   // zlib wrapper: CM 8 with a window of at most 32 KiB, no preset dictionary
   const uint8_t cmf = idat[0], flg = idat[1];
   if ((cmf & 0x0F) != 8 || (cmf >> 4) > 7 || ((cmf << 8) | flg) % 31 != 0 || (flg & 0x20))
     return VH_ERR_INVALID_ARG;
-  const int bpp = depth / 8;
-  const size_t stride = (size_t)w * (size_t)bpp;
-  const size_t raw_size = (size_t)h * (stride + 1);
-  std::vector<uint8_t> raw;
   BitReader br{idat.data() + 2, idat.size() - 6};  // between the zlib header and Adler-32
-  if (!inflate(br, raw, raw_size)) return VH_ERR_INVALID_ARG;
-  if (adler32_of(raw.data(), raw.size()) != be32(idat.data() + idat.size() - 4))
+  if (!inflate(br, img.raw, (size_t)img.h * (img.stride + 1))) return VH_ERR_INVALID_ARG;
+  if (adler32_of(img.raw.data(), img.raw.size()) != be32(idat.data() + idat.size() - 4))
     return VH_ERR_INVALID_ARG;
-  // unfilter row by row in place (a is the byte bpp to the left, b the one
-  // above, c above-left), then the big-endian samples to native uint16
-  std::vector<uint8_t> prev(stride, 0);
-  for (uint32_t y = 0; y < h; ++y) {
-    uint8_t *row = raw.data() + (size_t)y * (stride + 1);
-    const int ft = row[0];
-    uint8_t *cur = row + 1;
-    const uint8_t *up = prev.data();
-    const size_t k = (size_t)bpp;
-    switch (ft) {  // a: the byte bpp to the left, b: above, c: above-left
-      case 0:
-        break;
-      case 1:
-        for (size_t i = k; i < stride; ++i) cur[i] = (uint8_t)(cur[i] + cur[i - k]);
-        break;
-      case 2:
-        for (size_t i = 0; i < stride; ++i) cur[i] = (uint8_t)(cur[i] + up[i]);
-        break;
-      case 3:
-        for (size_t i = 0; i < stride; ++i)
-          cur[i] = (uint8_t)(cur[i] + (((i >= k ? cur[i - k] : 0) + up[i]) >> 1));
-        break;
-      case 4:
-        for (size_t i = 0; i < stride; ++i)
-          cur[i] = (uint8_t)(cur[i] + paeth(i >= k ? cur[i - k] : 0, up[i], i >= k ? up[i - k] : 0));
-        break;
-      default:
-        return VH_ERR_INVALID_ARG;
-    }
-    uint16_t *dst = out + (size_t)y * w;
-    if (bpp == 2)
-      for (uint32_t x = 0; x < w; ++x)
-        dst[x] = (uint16_t)(((uint32_t)cur[2 * x] << 8) | cur[2 * x + 1]);
+  const std::vector<uint8_t> zeros(img.stride, 0);
+  const size_t k = (size_t)(img.channels * img.depth / 8);
+  for (uint32_t y = 0; y < img.h; ++y) {
+    uint8_t *filt = img.raw.data() + (size_t)y * (img.stride + 1);
+    const uint8_t *up = y ? filt - img.stride : zeros.data();
+    if (!unfilter_row(filt + 1, up, img.stride, k, filt[0])) return VH_ERR_INVALID_ARG;
+  }
+  return VH_OK;
+}
+
+}  // namespace
+
+extern "C" vh_status vh_decode_depth_png(const uint8_t *png, int64_t bytes, uint16_t *out,
+                                         int64_t capacity, int32_t *width, int32_t *height) {
+  if (capacity < 0 || !width || !height) return VH_ERR_INVALID_ARG;
+  PngImage img;
+  vh_status s = png_decode(png, bytes, true, false, img);
+  if (s != VH_OK) return s;
+  if (out && capacity < (int64_t)img.w * (int64_t)img.h) {
+    *width = (int32_t)img.w;  // the size is reported with the capacity error
+    *height = (int32_t)img.h;
+    return VH_ERR_CAPACITY;
+  }
+  if (out && (s = png_decode(png, bytes, true, true, img)) != VH_OK) return s;
+  *width = (int32_t)img.w;
+  *height = (int32_t)img.h;
+  if (!out) return VH_OK;
+  for (uint32_t y = 0; y < img.h; ++y) {  // big-endian samples to native uint16
+    const uint8_t *src = img.row(y);
+    uint16_t *dst = out + (size_t)y * img.w;
+    if (img.depth == 16)
+      for (uint32_t x = 0; x < img.w; ++x)
+        dst[x] = (uint16_t)(((uint32_t)src[2 * x] << 8) | src[2 * x + 1]);
     else
-      for (uint32_t x = 0; x < w; ++x) dst[x] = cur[x];
-    std::memcpy(prev.data(), cur, stride);
+      for (uint32_t x = 0; x < img.w; ++x) dst[x] = src[x];
+  }
+  return VH_OK;
+}
+
+extern "C" vh_status vh_decode_colour_png(const uint8_t *png, int64_t bytes, uint8_t *rgb,
+                                          int64_t capacity, int32_t *width, int32_t *height) {
+  if (capacity < 0 || !width || !height) return VH_ERR_INVALID_ARG;
+  PngImage img;
+  vh_status s = png_decode(png, bytes, false, false, img);
+  if (s != VH_OK) return s;
+  if (rgb && capacity < 3 * (int64_t)img.w * (int64_t)img.h) {
+    *width = (int32_t)img.w;
+    *height = (int32_t)img.h;
+    return VH_ERR_CAPACITY;
+  }
+  if (rgb && (s = png_decode(png, bytes, false, true, img)) != VH_OK) return s;
+  *width = (int32_t)img.w;
+  *height = (int32_t)img.h;
+  if (!rgb) return VH_OK;
+  // 16-bit samples keep their high byte; grayscale is repeated into R, G and
+  // B; alpha is dropped
+  const int step = img.depth / 8, px = img.channels * step;
+  const int c1 = img.channels >= 3 ? step : 0, c2 = img.channels >= 3 ? 2 * step : 0;
+  for (uint32_t y = 0; y < img.h; ++y) {
+    const uint8_t *src = img.row(y);
+    uint8_t *dst = rgb + (size_t)y * img.w * 3;
+    for (uint32_t x = 0; x < img.w; ++x, src += px, dst += 3) {
+      dst[0] = src[0];
+      dst[1] = src[c1];
+      dst[2] = src[c2];
+    }
   }
   return VH_OK;
 }

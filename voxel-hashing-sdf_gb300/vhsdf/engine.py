@@ -504,3 +504,31 @@ def decode_depth_png(data):
     N.check(L.vh_decode_depth_png(buf.ctypes.data, buf.size, out.ctypes.data, out.size,
                                   C.byref(w), C.byref(h)))
     return out
+
+
+def decode_colour_png(data):
+    """A PNG colour image (bytes) as a (height, width, 3) uint8 RGB array,
+    decoded by the library (vh_decode_colour_png): what the reference gets
+    from cv::imread(path, IMREAD_COLOR) and its BGR-to-RGB swap
+    (src/SaveFrame.cpp:164, src/main.cpp:273)."""
+    buf = np.frombuffer(bytes(data), np.uint8)
+    L = N.lib()
+    w, h = C.c_int32(), C.c_int32()
+    N.check(L.vh_decode_colour_png(buf.ctypes.data, buf.size, None, 0, C.byref(w), C.byref(h)))
+    out = np.empty((h.value, w.value, 3), np.uint8)
+    N.check(L.vh_decode_colour_png(buf.ctypes.data, buf.size, out.ctypes.data, out.size,
+                                   C.byref(w), C.byref(h)))
+    return out
+
+
+def resize_colour(rgb, width, height):
+    """An RGB uint8 image (h, w, 3) resized bilinearly to (height, width, 3)
+    by the library (vh_resize_colour), as the reference scales its colour
+    frames to the depth grid with cv::resize (src/SaveFrame.cpp:164-171)."""
+    src = np.ascontiguousarray(rgb, np.uint8)
+    if src.ndim != 3 or src.shape[2] != 3:
+        raise ValueError(f"rgb must have shape (h, w, 3), got {src.shape}")
+    out = np.empty((int(height), int(width), 3), np.uint8)
+    N.check(N.lib().vh_resize_colour(src.ctypes.data, src.shape[1], src.shape[0],
+                                     out.ctypes.data, out.shape[1], out.shape[0]))
+    return out
