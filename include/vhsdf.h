@@ -426,6 +426,21 @@ vh_status vh_decode_depth_png(const uint8_t *png, int64_t bytes, uint16_t *out,
 vh_status vh_decode_colour_png(const uint8_t *png, int64_t bytes, uint8_t *rgb,
                                int64_t capacity, int32_t *width, int32_t *height);
 
+/* Decodes a JPEG colour frame, the <i>.jpg files the reference loads with
+ * cv::imread(path, IMREAD_COLOR) and swaps to RGB (src/SaveFrame.cpp:164,
+ * src/main.cpp:273), into rgb[height * width * 3] interleaved R, G, B
+ * bytes.  Sequential Huffman-coded files (baseline and extended, 8-bit
+ * samples, grayscale or YCbCr/RGB, any whole chroma subsampling ratio,
+ * restart intervals); the exact inverse DCT, a triangle filter for 2x
+ * chroma and the JFIF colour transform, so libjpeg's integer arithmetic
+ * may differ by one level on some pixels.  rgb == NULL: *width and *height
+ * only.  A malformed stream gives VH_ERR_INVALID_ARG; progressive,
+ * lossless, arithmetic-coded, 12-bit and CMYK files VH_ERR_UNSUPPORTED;
+ * capacity, in bytes, < 3 * width * height VH_ERR_CAPACITY.  Images up to
+ * 2^26 pixels.  Host only. */
+vh_status vh_decode_colour_jpeg(const uint8_t *jpg, int64_t bytes, uint8_t *rgb,
+                                int64_t capacity, int32_t *width, int32_t *height);
+
 /* Resizes an interleaved RGB u8 image (src_height x src_width x 3) to
  * dst_height x dst_width x 3 by bilinear interpolation, the way the
  * reference brings every colour frame to the depth frame's 640 x 480 grid

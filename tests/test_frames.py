@@ -212,9 +212,15 @@ def test_frame_folder_file_rules(tmp_path):
     folder = FrameFolder(root)
     assert folder.paths(0)[0].endswith("0.jpg") and folder.paths(1)[0].endswith("1.png")
     assert np.array_equal(folder.load(0).rgb, rgb)  # decoded by content, not by name
-    # a colour file that is not a PNG (a JPEG's start of image)
+    # a JPEG start of image with nothing valid after it, and a file that
+    # is neither JPEG nor PNG
     with open(os.path.join(root, "RGB", "0.jpg"), "wb") as f:
         f.write(b"\xff\xd8\xff\xe0" + bytes(60))
+    with pytest.raises(VhError) as e:
+        folder.load(0)
+    assert e.value.status == N.VH_ERR_INVALID_ARG
+    with open(os.path.join(root, "RGB", "0.jpg"), "wb") as f:
+        f.write(b"GIF89a" + bytes(60))
     with pytest.raises(VhError) as e:
         folder.load(0)
     assert e.value.status == N.VH_ERR_UNSUPPORTED

@@ -30,6 +30,10 @@ NVCC_COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
 # CPU oracle reproduces them bit for bit.
 KERNEL_FLAGS = ["-fmad=false", "--prec-div=true", "--prec-sqrt=true"]
 
+# host code whose floating-point results must not depend on the machine:
+# no contraction of a * b + c into a fused multiply-add (gcc contracts by
+# default on aarch64, not on x86-64)
+HOST_EXACT = ["-Xcompiler", "-ffp-contract=off"]
 ENGINE_SOURCES = [
     ("vh_kernels.cu", KERNEL_FLAGS),
     ("vh_api.cpp", []),
@@ -41,7 +45,8 @@ ENGINE_SOURCES = [
     ("vh_raycast.cu", []),
     ("vh_stream.cu", []),
     ("vh_png.cpp", []),
-    ("vh_frames.cpp", []),
+    ("vh_frames.cpp", HOST_EXACT),
+    ("vh_jpeg.cpp", HOST_EXACT),
 ]
 ENGINE_HEADERS = ["vh_common.cuh", "vh_device.cuh", "vh_mc_tables.h", "vh_mesh.h", "vh_internal.h"]
 

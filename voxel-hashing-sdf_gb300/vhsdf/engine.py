@@ -521,6 +521,20 @@ def decode_colour_png(data):
     return out
 
 
+def decode_colour_jpeg(data):
+    """A JPEG colour image (bytes) as a (height, width, 3) uint8 RGB array,
+    decoded by the library (vh_decode_colour_jpeg): the <i>.jpg colour
+    frames the reference reads with cv::imread (src/SaveFrame.cpp:164)."""
+    buf = np.frombuffer(bytes(data), np.uint8)
+    L = N.lib()
+    w, h = C.c_int32(), C.c_int32()
+    N.check(L.vh_decode_colour_jpeg(buf.ctypes.data, buf.size, None, 0, C.byref(w), C.byref(h)))
+    out = np.empty((h.value, w.value, 3), np.uint8)
+    N.check(L.vh_decode_colour_jpeg(buf.ctypes.data, buf.size, out.ctypes.data, out.size,
+                                    C.byref(w), C.byref(h)))
+    return out
+
+
 def resize_colour(rgb, width, height):
     """An RGB uint8 image (h, w, 3) resized bilinearly to (height, width, 3)
     by the library (vh_resize_colour), as the reference scales its colour

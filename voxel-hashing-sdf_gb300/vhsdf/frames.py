@@ -11,8 +11,9 @@ The reference's frame store (src/SaveFrame.cpp:44-52, 154-218) keeps frame
 and its application loop (src/main.cpp:242-258) fuses frames 0, 20, 40, ...
 below 2025, stopping once five of them were missing.  FrameFolder.load
 returns one frame, FrameFolder.frames walks that schedule.  The decoding
-and resizing are the library's (vh_decode_depth_png, vh_decode_colour_png,
-vh_resize_colour); this module only finds files and reads the pose text.
+and resizing are the library's (vh_decode_depth_png, vh_decode_colour_jpeg,
+vh_decode_colour_png, vh_resize_colour); this module only finds files and
+reads the pose text.
 
 Differences from the reference's loader, by design:
 - depth stays uint16 millimetres (VH_DEPTH_U16_MM); the reference converts
@@ -25,8 +26,9 @@ Differences from the reference's loader, by design:
   118-125); the reference inverts the matrix on loading and inverts it back
   before fusing (src/SaveFrame.cpp:206, src/PointCloudGenerator.cpp:140),
   which returns the same matrix up to float rounding;
-- colour in JPEG form is not decoded (VhError with VH_ERR_UNSUPPORTED);
-  PNG colour, as the reference's own writer stores it, is.
+- colour files are decoded by their content, JPEG or PNG, whatever their
+  name (the reference's writer stores PNG under <i>.png, its loader reads
+  <i>.jpg).
 """
 import os
 from typing import NamedTuple
@@ -34,9 +36,10 @@ from typing import NamedTuple
 import numpy as np
 
 from . import _native as N
-from .engine import decode_colour_png, decode_depth_png, resize_colour
+from .engine import decode_colour_jpeg, decode_colour_png, decode_depth_png, resize_colour
 
 _PNG_SIGNATURE = b"\x89PNG\r\n\x1a\n"
+_JPEG_SIGNATURE = b"\xff\xd8"
 
 
 class Frame(NamedTuple):
@@ -61,10 +64,12 @@ def read_pose(path):
 
 
 def decode_colour(data):
-    """A colour file's bytes as (H, W, 3) uint8 RGB; PNG only."""
+    """A colour file's bytes (JPEG or PNG) as (H, W, 3) uint8 RGB."""
     if bytes(data[:8]) == _PNG_SIGNATURE:
         return decode_colour_png(data)
-    raise N.VhError(N.VH_ERR_UNSUPPORTED, "colour image is not a PNG (JPEG is not decoded)")
+    if bytes(data[:2]) == _JPEG_SIGNATURE:
+        return decode_colour_jpeg(data)
+    raise N.VhError(N.VH_ERR_UNSUPPORTED, "colour image is neither JPEG nor PNG")
 
 
 class FrameFolder:
