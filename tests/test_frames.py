@@ -201,6 +201,18 @@ def test_frame_schedule_stops_after_missing_frames(tmp_path):
     assert [f.frame_id for f in folder.frames(start=20, step=40, stop=200)] == [20, 60, 100, 180]
     with pytest.raises(ValueError):
         next(folder.frames(step=0))
+    # decoding ahead on threads: the same frames in the same order
+    for workers in (1, 3, 8):
+        for kw in (dict(), dict(max_missing=2), dict(start=20, step=40, stop=200)):
+            seq = list(folder.frames(**kw))
+            par = list(folder.frames(workers=workers, **kw))
+            assert [f.frame_id for f in par] == [f.frame_id for f in seq]
+            for a, b in zip(seq, par):
+                assert np.array_equal(a.depth, b.depth) and np.array_equal(a.rgb, b.rgb)
+                assert np.array_equal(a.c2w, b.c2w)
+    walk = folder.frames(workers=2)  # left early: the walk closes cleanly
+    assert next(walk).frame_id == 0
+    walk.close()
 
 
 def test_frame_folder_file_rules(tmp_path):
@@ -224,6 +236,8 @@ def test_frame_folder_file_rules(tmp_path):
     with pytest.raises(VhError) as e:
         folder.load(0)
     assert e.value.status == N.VH_ERR_UNSUPPORTED
+    with pytest.raises(VhError):  # the error reaches the caller from a worker too
+        list(folder.frames(start=0, step=1, stop=2, workers=2))
     # missing depth or pose: the frame is missing
     os.remove(os.path.join(root, "tcw", "1.txt"))
     assert folder.load(1) is None

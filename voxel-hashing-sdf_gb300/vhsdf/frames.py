@@ -31,6 +31,8 @@ Differences from the reference's loader, by design:
   <i>.jpg).
 """
 import os
+from collections import deque
+from concurrent.futures import ThreadPoolExecutor
 from typing import NamedTuple
 
 import numpy as np
@@ -109,19 +111,51 @@ class FrameFolder:
             rgb = resize_colour(rgb, depth.shape[1], depth.shape[0])
         return Frame(int(frame_id), depth, rgb, read_pose(pose_path))
 
-    def frames(self, start=0, step=20, stop=2025, max_missing=5):
+    def frames(self, start=0, step=20, stop=2025, max_missing=5, workers=0):
         """Frames start, start + step, ... below stop, as the reference's
         application loop visits them.  The walk ends once `max_missing`
         frames were missing; as in the reference, a frame that loads does
-        not reset that count."""
+        not reset that count.
+
+        workers > 0 decodes up to 2 * workers frames ahead on that many
+        threads (the library's decoders run without the interpreter lock),
+        so that decoding overlaps the caller's use of each frame; the frames
+        and their order are the same as with workers = 0."""
         if step <= 0:
             raise ValueError("step must be positive")
-        missing = 0
-        for i in range(int(start), int(stop), int(step)):
-            if missing == max_missing:
-                return
-            frame = self.load(i)
-            if frame is None:
-                missing += 1
-                continue
-            yield frame
+        ids = range(int(start), int(stop), int(step))
+        if workers <= 0:
+            missing = 0
+            for i in ids:
+                if missing == max_missing:
+                    return
+                frame = self.load(i)
+                if frame is None:
+                    missing += 1
+                    continue
+                yield frame
+            return
+        with ThreadPoolExecutor(int(workers)) as pool:
+            ahead = deque()
+            todo = iter(ids)
+
+            def top_up():
+                while len(ahead) < 2 * workers:
+                    i = next(todo, None)
+                    if i is None:
+                        return
+                    ahead.append(pool.submit(self.load, i))
+
+            try:
+                top_up()
+                missing = 0
+                while ahead and missing < max_missing:
+                    frame = ahead.popleft().result()
+                    top_up()
+                    if frame is None:
+                        missing += 1
+                        continue
+                    yield frame
+            finally:
+                for f in ahead:  # loads past the end of the walk
+                    f.cancel()
