@@ -4,7 +4,9 @@
   with 8- or 16-bit samples (tests/png_writer.py) decode to the RGB bytes
   the reference's cv::imread(IMREAD_COLOR) and BGR-to-RGB swap give
   (src/SaveFrame.cpp:164, src/main.cpp:273): 16-bit samples keep the high
-  byte, grayscale fills all three channels, alpha is dropped.
+  byte, grayscale fills all three channels, alpha is dropped.  PNGs that
+  other encoders wrote (this machine's package images, where present)
+  decode to exactly the pixels they were filtered from.
 - vh_resize_colour: equal, byte for byte, to a numpy restatement of the
   bilinear map cv::resize applies to the reference's colour frames
   (src/SaveFrame.cpp:171).
@@ -259,3 +261,63 @@ def test_read_pose(tmp_path):
     p.write_text(" ".join(["nan"] * 16))
     with pytest.raises(ValueError):
         read_pose(p)
+
+
+def _system_pngs():
+    """PNG files that other encoders wrote (icons and documentation images
+    of this machine's packages), or none."""
+    import glob
+    found = []
+    for pattern in ("/usr/share/**/*.png", "/usr/local/cuda*/**/*.png", "/opt/nvidia/**/*.png",
+                    "/usr/local/lib/python3*/dist-packages/*/**/*.png"):
+        found += glob.glob(pattern, recursive=True)
+    return sorted(found)[:400]
+
+
+def test_pngs_from_other_encoders_decode_exactly():
+    """Files written by other PNG encoders (libpng with adaptive filters,
+    zlib at their levels): the decoded pixels, filtered again row by row
+    with the file's own filter types (tests/png_writer.py's filters), give
+    back exactly the filtered bytes of the file, so they are the pixels
+    the encoder started from.  Lossless cases: 8-bit RGB through
+    vh_decode_colour_png, 8- and 16-bit grayscale through
+    vh_decode_depth_png."""
+    import struct
+    import zlib
+    from png_writer import _filter_row
+    from vhsdf import decode_depth_png
+    checked = 0
+    for path in _system_pngs():
+        with open(path, "rb") as f:
+            data = f.read()
+        if data[:8] != b"\x89PNG\r\n\x1a\n":
+            continue
+        w, h, depth, colour, _, _, interlace = struct.unpack(">IIBBBBB", data[16:29])
+        if interlace or (colour, depth) not in ((2, 8), (0, 8), (0, 16)):
+            continue
+        pos, idat = 8, b""
+        while pos + 8 <= len(data):
+            n = struct.unpack(">I", data[pos:pos + 4])[0]
+            if data[pos + 4:pos + 8] == b"IDAT":
+                idat += data[pos + 8:pos + 8 + n]
+            pos += n + 12
+        if colour == 2:
+            img = decode_colour_png(data)
+            raw = img.reshape(h, w * 3)
+            bpp = 3
+        else:
+            img = decode_depth_png(data)
+            raw = img.astype(">u2").view(np.uint8).reshape(h, 2 * w) if depth == 16 else \
+                img.astype(np.uint8)
+            bpp = depth // 8
+        stride = raw.shape[1]
+        filtered = np.frombuffer(zlib.decompress(idat), np.uint8).reshape(h, stride + 1)
+        prev = np.zeros(stride, np.int64)
+        for y in range(h):
+            cur = raw[y].astype(np.int64)
+            again = _filter_row(int(filtered[y, 0]), cur, prev, bpp)
+            assert np.array_equal(again, filtered[y, 1:]), (path, y, int(filtered[y, 0]))
+            prev = cur
+        checked += 1
+    if checked == 0:
+        pytest.skip("no RGB or grayscale PNG from another encoder on this machine")
