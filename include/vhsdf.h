@@ -451,6 +451,27 @@ vh_status vh_decode_colour_jpeg(const uint8_t *jpg, int64_t bytes, uint8_t *rgb,
 vh_status vh_resize_colour(const uint8_t *src, int32_t src_width, int32_t src_height,
                            uint8_t *dst, int32_t dst_width, int32_t dst_height);
 
+/* Reads frame `frame_id` of a sequence stored in the reference's folder
+ * layout (SaveFrame::frameLoad, src/SaveFrame.cpp:44-52,154-218):
+ * <root>/depth/<id>.png (16-bit millimetres) into depth[height * width]
+ * uint16, <root>/RGB/<id>.jpg or, failing that, <id>.png (decoded by
+ * content, JPEG or PNG) into rgb[height * width * 3], resized onto the
+ * depth grid when its size differs (vh_resize_colour; the reference
+ * resizes to 640 x 480, src/SaveFrame.cpp:171), and <root>/tcw/<id>.txt
+ * (16 numbers, each read as the nearest float like the reference's
+ * operator>>) into c2w[16], row-major camera-to-world with the last row
+ * set to 0 0 0 1 (the reference inverts the matrix twice on the way,
+ * src/SaveFrame.cpp:206, src/PointCloudGenerator.cpp:140, which returns
+ * it up to float rounding).  The result is ready for vh_integrate with
+ * VH_DEPTH_U16_MM.  depth == NULL: *width and *height only.  A missing
+ * colour, depth or pose file gives VH_ERR_IO (the frame is missing); too
+ * small buffers VH_ERR_CAPACITY; a pose with fewer than 16 numbers
+ * VH_ERR_INVALID_ARG, a non-finite one VH_ERR_NOT_FINITE; decoder errors
+ * as from the decoders.  Host only. */
+vh_status vh_load_frame(const char *root, int32_t frame_id, uint16_t *depth,
+                        int64_t depth_capacity, uint8_t *rgb, int64_t rgb_capacity, float *c2w,
+                        int32_t *width, int32_t *height);
+
 /* The depth pre-filter of VH_FLAG_DEPTH_FILTER applied to one image: an
  * edge-preserving bilateral filter over 5x5 pixels (spatial sigma 2 px,
  * range sigma 5 mm + 1.5e-3 d^2 x 3, neighbours beyond 3 range sigmas or

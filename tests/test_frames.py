@@ -22,7 +22,6 @@ import pytest
 from png_writer import encode_png
 from vhsdf import Frame, FrameFolder, VhError, decode_colour_png, resize_colour, synth
 from vhsdf import _native as N
-from vhsdf.frames import read_pose
 
 
 def colour_frame(w=96, h=72, seed=0):
@@ -248,19 +247,32 @@ def test_frame_folder_file_rules(tmp_path):
     assert folder.load(2) is None
 
 
-def test_read_pose(tmp_path):
-    p = tmp_path / "p.txt"
-    p.write_text("1 0 0 0.5\n0 1 0 -1e-3\n0 0 1 2\n7 7 7 7\n")
-    m = read_pose(p)
+def test_pose_text(tmp_path):
+    """tcw/<i>.txt: 16 numbers separated by any white space, each the
+    nearest float to its decimal (the reference reads them with
+    operator>>), the last row set to 0 0 0 1; fewer numbers or a
+    non-finite one are errors."""
+    scene = synth.Scene(kind=1, seed=0, num_frames=2, width=16, height=12)
+    depth, rgb, c2w = scene.render(0)
+    root = str(tmp_path / "seq")
+    write_frame(root, 0, depth, rgb, c2w)
+    folder = FrameFolder(root)
+    pose = os.path.join(root, "tcw", "0.txt")
+    with open(pose, "w") as f:
+        f.write("1 0 0 0.5\n0 1\t0 -1e-3\n0 0 1 2.0000001\n7 7 7 7\n")
+    m = folder.load(0).c2w
     assert m.dtype == np.float32 and m.shape == (4, 4)
     assert np.array_equal(m[3], [0, 0, 0, 1]) and m[0, 3] == np.float32(0.5)
-    assert m[1, 3] == np.float32(-1e-3)
-    p.write_text("1 2 3")
-    with pytest.raises(ValueError):
-        read_pose(p)
-    p.write_text(" ".join(["nan"] * 16))
-    with pytest.raises(ValueError):
-        read_pose(p)
+    assert m[1, 3] == np.float32(-1e-3) and m[2, 3] == np.float32("2.0000001")
+    for text, status in (("1 2 3", N.VH_ERR_INVALID_ARG),
+                         ("1 0 0 x 0 1 0 0 0 0 1 0 0 0 0 1", N.VH_ERR_INVALID_ARG),
+                         (" ".join(["nan"] * 16), N.VH_ERR_NOT_FINITE),
+                         ("1e39 " * 16, N.VH_ERR_NOT_FINITE)):
+        with open(pose, "w") as f:
+            f.write(text)
+        with pytest.raises(VhError) as e:
+            folder.load(0)
+        assert e.value.status == status, text
 
 
 def _system_pngs():
@@ -321,3 +333,37 @@ def test_pngs_from_other_encoders_decode_exactly():
         checked += 1
     if checked == 0:
         pytest.skip("no RGB or grayscale PNG from another encoder on this machine")
+
+
+def test_load_frame_c_abi(tmp_path):
+    """vh_load_frame called directly: the size query, the buffers, the
+    status of a missing frame and of bad arguments."""
+    import ctypes as C
+    scene = synth.Scene(kind=1, seed=0, num_frames=2, width=32, height=24)
+    depth, rgb, c2w = scene.render(0)
+    root = str(tmp_path / "seq")
+    write_frame(root, 3, depth, resize_colour(rgb, 64, 48), c2w)
+    L = N.lib()
+    w, h = C.c_int32(), C.c_int32()
+    r = root.encode()
+    assert L.vh_load_frame(r, 3, None, 0, None, 0, None, C.byref(w), C.byref(h)) == N.VH_OK
+    assert (w.value, h.value) == (32, 24)
+    d = np.zeros((24, 32), np.uint16)
+    c = np.zeros((24, 32, 3), np.uint8)
+    m = np.zeros(16, np.float32)
+    args = (d.ctypes.data, d.size, c.ctypes.data, c.size, m.ctypes.data, C.byref(w), C.byref(h))
+    assert L.vh_load_frame(r, 3, *args) == N.VH_OK
+    assert np.array_equal(d, depth) and np.array_equal(m.reshape(4, 4), c2w)
+    assert np.array_equal(c, resize_colour(resize_colour(rgb, 64, 48), 32, 24))
+    assert L.vh_load_frame(r, 4, *args) == N.VH_ERR_IO                       # missing
+    assert L.vh_load_frame(b"/nonexistent-dir", 3, *args) == N.VH_ERR_IO
+    assert L.vh_load_frame(r, -1, *args) == N.VH_ERR_INVALID_ARG
+    assert L.vh_load_frame(None, 3, *args) == N.VH_ERR_INVALID_ARG
+    assert L.vh_load_frame(r, 3, d.ctypes.data, d.size - 1, c.ctypes.data, c.size,
+                           m.ctypes.data, C.byref(w), C.byref(h)) == N.VH_ERR_CAPACITY
+    assert L.vh_load_frame(r, 3, d.ctypes.data, d.size, c.ctypes.data, c.size - 1,
+                           m.ctypes.data, C.byref(w), C.byref(h)) == N.VH_ERR_CAPACITY
+    assert L.vh_load_frame(r, 3, d.ctypes.data, d.size, None, 0, m.ctypes.data,
+                           C.byref(w), C.byref(h)) == N.VH_ERR_INVALID_ARG
+    assert L.vh_load_frame(r, 3, d.ctypes.data, d.size, c.ctypes.data, c.size, None,
+                           C.byref(w), C.byref(h)) == N.VH_ERR_INVALID_ARG

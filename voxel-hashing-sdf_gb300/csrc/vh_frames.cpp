@@ -1,4 +1,6 @@
-// vh_frames.cpp - host-side preparation of colour frames (vh_resize_colour).
+// vh_frames.cpp - host-side frame preparation: colour resizing
+// (vh_resize_colour) and whole frames read from the reference's frame
+// folders (vh_load_frame).
 //
 // The reference scales every colour frame to 640 x 480 with cv::resize's
 // default bilinear interpolation before fusing it with the depth frame
@@ -12,6 +14,10 @@
 // one level away on some pixels.
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
 #include <vector>
 
 #include "../../include/vhsdf.h"
@@ -70,4 +76,100 @@ extern "C" vh_status vh_resize_colour(const uint8_t *src, int32_t src_width, int
     }
   }
   return VH_OK;
+}
+
+// ---- frames in the reference's folder layout -----------------------------
+//
+// SaveFrame::frameLoad (src/SaveFrame.cpp:154-218) reads frame i as
+// <root>/RGB/<i>.jpg (colour), <root>/depth/<i>.png (16-bit millimetres)
+// and <root>/tcw/<i>.txt (16 numbers read with operator>> into floats, a
+// row-major 4 x 4 camera-to-world pose, which it inverts and
+// PointCloudGenerator::PushFrame inverts back, src/SaveFrame.cpp:206,
+// src/PointCloudGenerator.cpp:140; Reproject then sets the last row to
+// 0 0 0 1, src/PointCloudGenerator.cpp:118-125).
+
+namespace {
+
+bool read_file(const std::string &path, std::vector<uint8_t> &out) {
+  FILE *f = std::fopen(path.c_str(), "rb");
+  if (!f) return false;
+  out.clear();
+  uint8_t chunk[1 << 16];
+  size_t got;
+  while ((got = std::fread(chunk, 1, sizeof(chunk), f)) > 0) out.insert(out.end(), chunk, chunk + got);
+  const bool ok = !std::ferror(f);
+  std::fclose(f);
+  return ok;
+}
+
+bool exists(const std::string &path) {
+  FILE *f = std::fopen(path.c_str(), "rb");
+  if (!f) return false;
+  std::fclose(f);
+  return true;
+}
+
+// 16 numbers separated by white space, each read as a float the way
+// operator>> reads one (strtof: the nearest float to the decimal)
+vh_status parse_pose(const std::vector<uint8_t> &text, float *c2w) {
+  std::string s(text.begin(), text.end());
+  const char *p = s.c_str();
+  for (int i = 0; i < 16; ++i) {
+    char *end = nullptr;
+    const float v = std::strtof(p, &end);
+    if (end == p) return VH_ERR_INVALID_ARG;
+    if (!std::isfinite(v)) return VH_ERR_NOT_FINITE;
+    c2w[i] = v;
+    p = end;
+  }
+  c2w[12] = c2w[13] = c2w[14] = 0.0f;
+  c2w[15] = 1.0f;
+  return VH_OK;
+}
+
+}  // namespace
+
+extern "C" vh_status vh_load_frame(const char *root, int32_t frame_id, uint16_t *depth,
+                                   int64_t depth_capacity, uint8_t *rgb, int64_t rgb_capacity,
+                                   float *c2w, int32_t *width, int32_t *height) {
+  if (!root || !width || !height || depth_capacity < 0 || rgb_capacity < 0 || frame_id < 0)
+    return VH_ERR_INVALID_ARG;
+  const std::string id = std::to_string(frame_id), base(root);
+  const std::string depth_path = base + "/depth/" + id + ".png";
+  const std::string pose_path = base + "/tcw/" + id + ".txt";
+  std::string colour_path = base + "/RGB/" + id + ".jpg";
+  if (!exists(colour_path)) colour_path = base + "/RGB/" + id + ".png";
+  std::vector<uint8_t> file;
+  if (!exists(colour_path) || !exists(pose_path) || !read_file(depth_path, file))
+    return VH_ERR_IO;  // the frame is missing
+  int32_t w = 0, h = 0;
+  vh_status s = vh_decode_depth_png(file.data(), (int64_t)file.size(), nullptr, 0, &w, &h);
+  if (s != VH_OK) return s;
+  *width = w;
+  *height = h;
+  if (!depth) return VH_OK;  // size query
+  const int64_t npx = (int64_t)w * (int64_t)h;
+  if (depth_capacity < npx || !rgb || rgb_capacity < 3 * npx || !c2w) {
+    return (!rgb || !c2w) ? VH_ERR_INVALID_ARG : VH_ERR_CAPACITY;
+  }
+  if ((s = vh_decode_depth_png(file.data(), (int64_t)file.size(), depth, depth_capacity, &w,
+                               &h)) != VH_OK)
+    return s;
+  if (!read_file(colour_path, file)) return VH_ERR_IO;
+  const bool png = file.size() >= 8 && file[0] == 0x89 && file[1] == 'P';
+  const bool jpeg = file.size() >= 2 && file[0] == 0xFF && file[1] == 0xD8;
+  if (!png && !jpeg) return VH_ERR_UNSUPPORTED;
+  int32_t cw = 0, ch = 0;
+  s = png ? vh_decode_colour_png(file.data(), (int64_t)file.size(), nullptr, 0, &cw, &ch)
+          : vh_decode_colour_jpeg(file.data(), (int64_t)file.size(), nullptr, 0, &cw, &ch);
+  if (s != VH_OK) return s;
+  std::vector<uint8_t> colour((size_t)cw * (size_t)ch * 3);
+  uint8_t *dst = (cw == w && ch == h) ? rgb : colour.data();
+  const int64_t cap = 3 * (int64_t)cw * (int64_t)ch;
+  s = png ? vh_decode_colour_png(file.data(), (int64_t)file.size(), dst, cap, &cw, &ch)
+          : vh_decode_colour_jpeg(file.data(), (int64_t)file.size(), dst, cap, &cw, &ch);
+  if (s != VH_OK) return s;
+  if (dst != rgb && (s = vh_resize_colour(colour.data(), cw, ch, rgb, w, h)) != VH_OK) return s;
+  if (!read_file(pose_path, file)) return VH_ERR_IO;
+  return parse_pose(file, c2w);
 }

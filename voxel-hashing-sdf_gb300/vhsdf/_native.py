@@ -152,6 +152,7 @@ SIGNATURES = {
     "vh_decode_colour_png": (I32, [P, I64, P, I64, C.POINTER(I32), C.POINTER(I32)]),
     "vh_resize_colour": (I32, [P, I32, I32, P, I32, I32]),
     "vh_decode_colour_jpeg": (I32, [P, I64, P, I64, C.POINTER(I32), C.POINTER(I32)]),
+    "vh_load_frame": (I32, [C.c_char_p, I32, P, I64, P, I64, P, C.POINTER(I32), C.POINTER(I32)]),
     "vh_stream_out": (I32, [P, P, C.c_float, PI64]),
     "vh_stream_in": (I32, [P, P, C.c_float, PI64]),
     "vh_evict_async": (I32, [P, P, C.c_float]),

@@ -10,10 +10,10 @@ The reference's frame store (src/SaveFrame.cpp:44-52, 154-218) keeps frame
 
 and its application loop (src/main.cpp:242-258) fuses frames 0, 20, 40, ...
 below 2025, stopping once five of them were missing.  FrameFolder.load
-returns one frame, FrameFolder.frames walks that schedule.  The decoding
-and resizing are the library's (vh_decode_depth_png, vh_decode_colour_jpeg,
-vh_decode_colour_png, vh_resize_colour); this module only finds files and
-reads the pose text.
+returns one frame through the library's vh_load_frame (which decodes with
+vh_decode_depth_png, vh_decode_colour_jpeg / vh_decode_colour_png and
+vh_resize_colour, and reads the pose as the reference does, each number
+as the nearest float); FrameFolder.frames walks the schedule.
 
 Differences from the reference's loader, by design:
 - depth stays uint16 millimetres (VH_DEPTH_U16_MM); the reference converts
@@ -30,6 +30,7 @@ Differences from the reference's loader, by design:
   name (the reference's writer stores PNG under <i>.png, its loader reads
   <i>.jpg).
 """
+import ctypes as C
 import os
 from collections import deque
 from concurrent.futures import ThreadPoolExecutor
@@ -38,10 +39,6 @@ from typing import NamedTuple
 import numpy as np
 
 from . import _native as N
-from .engine import decode_colour_jpeg, decode_colour_png, decode_depth_png, resize_colour
-
-_PNG_SIGNATURE = b"\x89PNG\r\n\x1a\n"
-_JPEG_SIGNATURE = b"\xff\xd8"
 
 
 class Frame(NamedTuple):
@@ -49,29 +46,6 @@ class Frame(NamedTuple):
     depth: np.ndarray  # (H, W) uint16, millimetres
     rgb: np.ndarray    # (H, W, 3) uint8, R, G, B, on the depth image's grid
     c2w: np.ndarray    # (4, 4) float32, camera-to-world, row-major
-
-
-def read_pose(path):
-    """The 4 x 4 camera-to-world pose of a tcw/<i>.txt file (16 numbers,
-    row-major, separated by white space), last row set to (0, 0, 0, 1)."""
-    with open(path) as f:
-        values = f.read().split()
-    if len(values) < 16:
-        raise ValueError(f"{path}: a pose needs 16 numbers, found {len(values)}")
-    m = np.array([float(v) for v in values[:16]], np.float32).reshape(4, 4)
-    if not np.isfinite(m).all():
-        raise ValueError(f"{path}: the pose is not finite")
-    m[3] = (0.0, 0.0, 0.0, 1.0)
-    return m
-
-
-def decode_colour(data):
-    """A colour file's bytes (JPEG or PNG) as (H, W, 3) uint8 RGB."""
-    if bytes(data[:8]) == _PNG_SIGNATURE:
-        return decode_colour_png(data)
-    if bytes(data[:2]) == _JPEG_SIGNATURE:
-        return decode_colour_jpeg(data)
-    raise N.VhError(N.VH_ERR_UNSUPPORTED, "colour image is neither JPEG nor PNG")
 
 
 class FrameFolder:
@@ -97,19 +71,26 @@ class FrameFolder:
                 os.path.join(self.pose_dir, i + ".txt"))
 
     def load(self, frame_id):
-        """Frame `frame_id`, or None when its colour, depth or pose file is
-        missing (the reference marks a frame without colour as missing,
-        src/SaveFrame.cpp:166-169)."""
-        colour, depth_path, pose_path = self.paths(frame_id)
-        if colour is None or not os.path.exists(depth_path) or not os.path.exists(pose_path):
+        """Frame `frame_id` (vh_load_frame), or None when its colour, depth
+        or pose file is missing (the reference marks a frame without
+        colour as missing, src/SaveFrame.cpp:166-169)."""
+        L = N.lib()
+        root = self.root.encode()
+        i = int(frame_id)
+        w, h = C.c_int32(), C.c_int32()
+        s = L.vh_load_frame(root, i, None, 0, None, 0, None, C.byref(w), C.byref(h))
+        if s == N.VH_ERR_IO:
             return None
-        with open(depth_path, "rb") as f:
-            depth = decode_depth_png(f.read())
-        with open(colour, "rb") as f:
-            rgb = decode_colour(f.read())
-        if rgb.shape[:2] != depth.shape:
-            rgb = resize_colour(rgb, depth.shape[1], depth.shape[0])
-        return Frame(int(frame_id), depth, rgb, read_pose(pose_path))
+        N.check(s)
+        depth = np.empty((h.value, w.value), np.uint16)
+        rgb = np.empty((h.value, w.value, 3), np.uint8)
+        c2w = np.empty((4, 4), np.float32)
+        s = L.vh_load_frame(root, i, depth.ctypes.data, depth.size, rgb.ctypes.data, rgb.size,
+                            c2w.ctypes.data, C.byref(w), C.byref(h))
+        if s == N.VH_ERR_IO:  # removed between the two calls
+            return None
+        N.check(s)
+        return Frame(i, depth, rgb, c2w)
 
     def frames(self, start=0, step=20, stop=2025, max_missing=5, workers=0):
         """Frames start, start + step, ... below stop, as the reference's
