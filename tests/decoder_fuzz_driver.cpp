@@ -2,7 +2,8 @@
 // (PNG or JPEG; the first argument is the number of mutations per seed) is
 // damaged by seeded bit flips, byte overwrites, insertions, truncations and
 // planted markers, then decoded: a size query, then the pixels when the
-// size is modest.  Built with -fsanitize=address,undefined by
+// size is modest; a decoded image is then resized to a random size
+// (vh_resize_colour).  Built with -fsanitize=address,undefined by
 // tests/test_decoder_fuzz.py; an out-of-bounds access or undefined
 // behaviour ends the run with a report and a non-zero exit.
 #include <cstdint>
@@ -68,6 +69,11 @@ int main(int argc, char **argv) {
         if (png) {
           std::vector<uint16_t> depth((size_t)w * (size_t)h);
           vh_decode_depth_png(d, n, depth.data(), (int64_t)depth.size(), &w, &h);
+        }
+        if (s == VH_OK) {
+          const int32_t dw = 1 + (int32_t)(rng() % 70), dh = 1 + (int32_t)(rng() % 70);
+          std::unique_ptr<uint8_t[]> out(new uint8_t[(size_t)dw * (size_t)dh * 3]);
+          if (vh_resize_colour(rgb.data(), w, h, out.get(), dw, dh) != VH_OK) return 3;
         }
       }
       (s == VH_OK ? decoded : rejected)++;

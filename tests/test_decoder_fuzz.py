@@ -80,8 +80,8 @@ def test_mutated_files(kind):
 
 
 def test_mutations_under_address_sanitizer(tmp_path):
-    """The decoders' sources built with AddressSanitizer and
-    UndefinedBehaviorSanitizer (tests/decoder_fuzz_driver.cpp), 20000
+    """The decoders' and the resize's sources built with AddressSanitizer
+    and UndefinedBehaviorSanitizer (tests/decoder_fuzz_driver.cpp), 20000
     mutations of each seed: no report, exit 0."""
     import os
     import shutil
@@ -96,7 +96,8 @@ def test_mutations_under_address_sanitizer(tmp_path):
         [gxx, "-O1", "-g", "-std=c++17", "-fsanitize=address,undefined",
          "-fno-sanitize-recover=undefined", "-I", os.path.join(repo, "include"),
          os.path.join(repo, "tests", "decoder_fuzz_driver.cpp"),
-         os.path.join(csrc, "vh_png.cpp"), os.path.join(csrc, "vh_jpeg.cpp"), "-o", exe],
+         os.path.join(csrc, "vh_png.cpp"), os.path.join(csrc, "vh_jpeg.cpp"),
+         os.path.join(csrc, "vh_frames.cpp"), "-o", exe],
         capture_output=True, text=True)
     if build.returncode != 0:
         if "asan" in build.stderr.lower() or "ubsan" in build.stderr.lower():
