@@ -56,14 +56,17 @@ struct Zigzag {
 };
 const Zigzag kZig;
 
-// c[x][u] = C(u) / 2 * cos((2x + 1) u pi / 16), C(0) = 1 / sqrt(2), else 1
+// c[x][u] = C(u) / 2 * cos((2x + 1) u pi / 16), C(0) = 1 / sqrt(2), else 1;
+// t[u][x] = c[x][u]
 struct IdctBasis {
-  double c[8][8];
+  double c[8][8], t[8][8];
   IdctBasis() {
     const double pi = 3.14159265358979323846;
     for (int x = 0; x < 8; ++x)
-      for (int u = 0; u < 8; ++u)
+      for (int u = 0; u < 8; ++u) {
         c[x][u] = (u == 0 ? std::sqrt(0.5) : 1.0) * 0.5 * std::cos((2 * x + 1) * u * pi / 16.0);
+        t[u][x] = c[x][u];
+      }
   }
 };
 const IdctBasis kBasis;
@@ -208,25 +211,32 @@ struct Decoder {
       for (int y = 0; y < 8; ++y) std::memset(dst + (size_t)y * stride, s, 8);
       return;
     }
-    double tmp[8][8];  // tmp[v][x] = sum_u F(v, u) c[x][u]; rows of zeros skipped
+    // tmp[v][x] = sum_u F(v, u) c[x][u], rows of zeros skipped; then
+    // s(y, x) = sum_v c[y][v] tmp[v][x].  Each sum runs in ascending u or
+    // v; the eight columns x are the inner loop, so they vectorise.
+    double tmp[8][8];
     bool nz[8];
     for (int v = 0; v <= rmax; ++v) {
       const int32_t *row = coef + v * 8;
       nz[v] = (row[0] | row[1] | row[2] | row[3] | row[4] | row[5] | row[6] | row[7]) != 0;
       if (!nz[v]) continue;
-      for (int x = 0; x < 8; ++x) {
-        double s = 0.0;
-        for (int u = 0; u <= cmax; ++u) s += kBasis.c[x][u] * (double)row[u];
-        tmp[v][x] = s;
+      double acc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+      for (int u = 0; u <= cmax; ++u) {
+        const double f = (double)row[u];
+        for (int x = 0; x < 8; ++x) acc[x] += kBasis.t[u][x] * f;
       }
+      for (int x = 0; x < 8; ++x) tmp[v][x] = acc[x];
     }
     for (int y = 0; y < 8; ++y) {
+      double acc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+      for (int v = 0; v <= rmax; ++v) {
+        if (!nz[v]) continue;
+        const double c = kBasis.c[y][v];
+        for (int x = 0; x < 8; ++x) acc[x] += c * tmp[v][x];
+      }
       uint8_t *out = dst + (size_t)y * stride;
       for (int x = 0; x < 8; ++x) {
-        double s = 0.0;
-        for (int v = 0; v <= rmax; ++v)
-          if (nz[v]) s += kBasis.c[y][v] * tmp[v][x];
-        const double val = std::floor(s + 128.0 + 0.5);
+        const double val = std::floor(acc[x] + 128.0 + 0.5);
         out[x] = (uint8_t)(val < 0 ? 0 : (val > 255 ? 255 : val));
       }
     }
@@ -412,6 +422,10 @@ struct Decoder {
     const int rx = hmax / k.h, ry = vmax / k.v;
     const uint8_t *pl = k.plane.data();
     const int cw = k.w, ch = k.ht;
+    if (rx == 1 && ry == 1) {  // full resolution: the row itself
+      std::memcpy(out, pl + (size_t)y * k.pw, width);
+      return;
+    }
     if ((rx != 1 && rx != 2) || (ry != 1 && ry != 2)) {  // replication
       const uint8_t *row = pl + (size_t)(y / ry < (uint32_t)ch ? y / ry : ch - 1) * k.pw;
       for (uint32_t x = 0; x < width; ++x) {
