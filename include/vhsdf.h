@@ -433,8 +433,11 @@ vh_status vh_decode_colour_png(const uint8_t *png, int64_t bytes, uint8_t *rgb,
  * samples, grayscale or YCbCr/RGB, any whole chroma subsampling ratio,
  * restart intervals); the exact inverse DCT, a triangle filter for 2x
  * chroma and the JFIF colour transform, so libjpeg's integer arithmetic
- * may differ by one level on some pixels.  rgb == NULL: *width and *height
- * only.  A malformed stream gives VH_ERR_INVALID_ARG; progressive,
+ * may differ by one level on some pixels.  An Exif Orientation tag (in an
+ * APP1 segment before the frame header) turns or mirrors the image into
+ * its displayed orientation, as cv::imread does for IMREAD_COLOR; width
+ * and height are then those of the displayed image.  rgb == NULL: *width
+ * and *height only.  A malformed stream gives VH_ERR_INVALID_ARG; progressive,
  * lossless, arithmetic-coded, 12-bit and CMYK files VH_ERR_UNSUPPORTED;
  * capacity, in bytes, < 3 * width * height VH_ERR_CAPACITY.  Images up to
  * 2^26 pixels.  Host only. */

@@ -142,12 +142,27 @@ class Encoded:
         self.rgb_components = rgb_components
 
 
+def exif_segment(orientation, big_endian=False):
+    """An Exif APP1 segment whose first image file directory holds the
+    Orientation tag (0x0112, one SHORT) and one more tag before it."""
+    e = ">" if big_endian else "<"
+    tiff = (b"MM" if big_endian else b"II") + struct.pack(e + "HI", 42, 8)
+    ifd = struct.pack(e + "H", 2)
+    ifd += struct.pack(e + "HHI", 0x010F, 2, 4) + b"cam\x00"          # Make, ASCII, inline
+    ifd += struct.pack(e + "HHIH", 0x0112, 3, 1, orientation) + b"\x00\x00"
+    ifd += struct.pack(e + "I", 0)                                      # no next directory
+    return _segment(0xE1, b"Exif\x00\x00" + tiff + ifd)
+
+
 def encode_jpeg(img, sampling=((1, 1), (1, 1), (1, 1)), quality_table=None, restart=0,
-                interleaved=True, q16=False, extended=False, rgb_mode=None):
+                interleaved=True, q16=False, extended=False, rgb_mode=None, app1=b"",
+                app1_after_frame=b""):
     """A JPEG of `img` ((h, w) grayscale or (h, w, 3) RGB uint8).
     sampling: (h, v) per component; quality_table: a scalar or an 8 x 8 table
     (natural order) of quantiser steps (default 1: near lossless);
-    rgb_mode: None (YCbCr), "adobe" or "ids" (samples stored as R, G, B)."""
+    rgb_mode: None (YCbCr), "adobe" or "ids" (samples stored as R, G, B);
+    app1 / app1_after_frame: segments written before the quantisation
+    tables / right after the frame header."""
     img = np.asarray(img)
     gray = img.ndim == 2
     height, width = img.shape[:2]
@@ -261,6 +276,7 @@ def encode_jpeg(img, sampling=((1, 1), (1, 1), (1, 1)), quality_table=None, rest
 
     out = bytearray(b"\xFF\xD8")
     out += _segment(0xE0, b"JFIF\x00\x01\x01\x00\x00\x01\x00\x01\x00\x00")
+    out += app1
     if rgb_mode == "adobe":
         out += _segment(0xEE, b"Adobe" + bytes([0, 100, 0, 0, 0, 0, 0]))
     for t in range(ntab):
@@ -273,6 +289,7 @@ def encode_jpeg(img, sampling=((1, 1), (1, 1), (1, 1)), quality_table=None, rest
     for ci, c in enumerate(comps):
         sof += bytes([ids[ci], (c["h"] << 4) | c["v"], c["tq"]])
     out += _segment(0xC1 if extended else 0xC0, sof)
+    out += app1_after_frame
     for t in range(ntab):
         out += _segment(0xC4, dct_tabs[t].dht(0, t))
         out += _segment(0xC4, act_tabs[t].dht(1, t))

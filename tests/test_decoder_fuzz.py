@@ -9,7 +9,7 @@ import zlib
 import numpy as np
 import pytest
 
-from jpeg_writer import encode_jpeg
+from jpeg_writer import encode_jpeg, exif_segment
 from png_writer import encode_png
 from vhsdf import VhError, decode_colour_jpeg, decode_colour_png, decode_depth_png
 from vhsdf import _native as N
@@ -56,8 +56,8 @@ def _decodes_or_fails_cleanly(fn, data):
 def test_mutated_files(kind):
     img = _image()
     if kind == "jpeg_420_restart":
-        seed, fns = encode_jpeg(img, sampling=((2, 2), (1, 1), (1, 1)), restart=3).data, \
-            [decode_colour_jpeg]
+        seed, fns = encode_jpeg(img, sampling=((2, 2), (1, 1), (1, 1)), restart=3,
+                                app1=exif_segment(6)).data, [decode_colour_jpeg]
     elif kind == "jpeg_gray":
         seed, fns = encode_jpeg(img[:, :, 0]).data, [decode_colour_jpeg]
     elif kind == "jpeg_separate_q16":
@@ -105,7 +105,9 @@ def test_mutations_under_address_sanitizer(tmp_path):
         raise AssertionError(build.stderr)
     img = _image()
     seeds = {
-        "a.jpg": encode_jpeg(img, sampling=((2, 2), (1, 1), (1, 1)), restart=3).data,
+        "a.jpg": encode_jpeg(img, sampling=((2, 2), (1, 1), (1, 1)), restart=3,
+                             app1=exif_segment(6)).data,
+        "f.jpg": encode_jpeg(img, app1=exif_segment(7, big_endian=True)).data,
         "b.jpg": encode_jpeg(img[:, :, 0]).data,
         "c.jpg": encode_jpeg(img, interleaved=False, q16=True, sampling=((1, 2), (1, 1),
                                                                          (1, 1))).data,

@@ -23,7 +23,7 @@ import os
 import numpy as np
 import pytest
 
-from jpeg_writer import ZIGZAG, encode_jpeg, expected_decode
+from jpeg_writer import ZIGZAG, encode_jpeg, exif_segment, expected_decode
 from vhsdf import VhError, decode_colour_jpeg, synth
 from vhsdf import _native as N
 
@@ -210,3 +210,47 @@ def test_frame_folder_reads_jpeg_colour(tmp_path):
     from vhsdf import resize_colour
     assert np.array_equal(fr.rgb, resize_colour(decode_colour_jpeg(enc.data), 64, 48))
     assert np.array_equal(fr.depth, depth)
+
+
+# Exif orientation -> the displayed image, by the tag's definitions:
+# mirrored, rotated 180, flipped, transposed, rotated 90 clockwise to show,
+# transversed (mirrored, then rotated 90 clockwise), rotated 90 anticlockwise
+ORIENTED = {
+    1: lambda a: a,
+    2: np.fliplr,
+    3: lambda a: np.rot90(a, 2),
+    4: np.flipud,
+    5: lambda a: np.rot90(np.fliplr(a), 1),
+    6: lambda a: np.rot90(a, -1),
+    7: lambda a: np.rot90(np.fliplr(a), -1),
+    8: lambda a: np.rot90(a, 1),
+}
+
+
+@pytest.mark.parametrize("orientation", range(1, 9))
+@pytest.mark.parametrize("big_endian", [False, True])
+def test_exif_orientation(orientation, big_endian):
+    """cv::imread(IMREAD_COLOR) shows a JPEG the way its Exif Orientation
+    tag says; the decoder does the same, size query included."""
+    img = noisy(37, 22, 5)
+    plain = decode_colour_jpeg(encode_jpeg(img, sampling=((2, 2), (1, 1), (1, 1))).data)
+    data = encode_jpeg(img, sampling=((2, 2), (1, 1), (1, 1)),
+                       app1=exif_segment(orientation, big_endian)).data
+    got = decode_colour_jpeg(data)
+    want = np.ascontiguousarray(ORIENTED[orientation](plain))
+    assert got.shape == want.shape and np.array_equal(got, want)
+    buf = np.frombuffer(data, np.uint8)
+    w, h = C.c_int32(), C.c_int32()
+    assert N.lib().vh_decode_colour_jpeg(buf.ctypes.data, buf.size, None, 0, C.byref(w),
+                                         C.byref(h)) == N.VH_OK
+    assert (h.value, w.value) == want.shape[:2]
+
+
+def test_exif_ignored_when_malformed_or_late():
+    img = noisy(21, 13, 6)
+    plain = decode_colour_jpeg(encode_jpeg(img).data)
+    seg = exif_segment(6)
+    cut = seg[:2] + bytes([0, len(seg) - 2 - 12]) + seg[4:-12]   # directory cut short
+    for kw in (dict(app1=cut), dict(app1_after_frame=seg),
+               dict(app1=seg[:10] + b"XX" + seg[12:])):               # no byte-order mark
+        assert np.array_equal(decode_colour_jpeg(encode_jpeg(img, **kw).data), plain)

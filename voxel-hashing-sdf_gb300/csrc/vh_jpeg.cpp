@@ -24,7 +24,10 @@
 //   colour - the JFIF YCbCr to RGB transform (R = Y + 1.402 Cr',
 //     G = Y - 0.34414 Cb' - 0.71414 Cr', B = Y + 1.772 Cb', with
 //     Cb' = Cb - 128 and Cr' = Cr - 128), or none for an Adobe file
-//     marked RGB or components named 'R', 'G', 'B'.
+//     marked RGB or components named 'R', 'G', 'B';
+//   orientation - an Exif Orientation tag (APP1, before the frame header)
+//     turns and mirrors the image into its displayed orientation, as
+//     cv::imread does for IMREAD_COLOR.
 // libjpeg's integer IDCT and fixed-point colour tables can land one level
 // away from these exact forms on some pixels.  Every read is
 // bounds-checked; a stream whose codes run past the end of its data is
@@ -198,7 +201,12 @@ struct Decoder {
   bool qt_defined[4] = {false, false, false, false};
   Huffman dc[4], ac[4];
   uint32_t restart = 0;
+  int orientation = 1;  // Exif orientation, 1..8
   bool have_frame = false, adobe_rgb = false, ids_rgb = false;
+
+  // the size the image is delivered in: orientations 5..8 swap the axes
+  uint32_t out_width() const { return orientation >= 5 ? height : width; }
+  uint32_t out_height() const { return orientation >= 5 ? width : height; }
 
   // one 8 x 8 block: coefficients -> samples at (bx, by) of the plane.
   // Coefficients beyond row rmax or column cmax are zero and left out of
@@ -507,6 +515,33 @@ struct Decoder {
 
 inline uint32_t be16(const uint8_t *p) { return ((uint32_t)p[0] << 8) | p[1]; }
 
+// The Orientation tag (0x0112) of an Exif APP1 segment's first image file
+// directory (TIFF layout, either byte order), 1 when absent or malformed.
+int exif_orientation(const uint8_t *t, size_t n) {
+  if (n < 8) return 1;
+  const bool le = t[0] == 'I' && t[1] == 'I';
+  if (!le && !(t[0] == 'M' && t[1] == 'M')) return 1;
+  auto u16 = [&](size_t o) -> uint32_t {
+    return le ? (uint32_t)t[o] | ((uint32_t)t[o + 1] << 8) : ((uint32_t)t[o] << 8) | t[o + 1];
+  };
+  auto u32 = [&](size_t o) -> uint32_t {
+    return le ? u16(o) | (u16(o + 2) << 16) : (u16(o) << 16) | u16(o + 2);
+  };
+  if (u16(2) != 42) return 1;
+  const size_t ifd = u32(4);
+  if (ifd > n - 2) return 1;
+  const size_t entries = u16(ifd);
+  for (size_t k = 0; k < entries; ++k) {
+    const size_t e = ifd + 2 + 12 * k;
+    if (e + 12 > n) return 1;
+    if (u16(e) == 0x0112 && u16(e + 2) == 3 && u32(e + 4) == 1) {  // one SHORT
+      const uint32_t v = u16(e + 8);
+      return v >= 1 && v <= 8 ? (int)v : 1;
+    }
+  }
+  return 1;
+}
+
 }  // namespace
 
 extern "C" vh_status vh_decode_colour_jpeg(const uint8_t *jpg, int64_t bytes, uint8_t *rgb,
@@ -537,13 +572,13 @@ extern "C" vh_status vh_decode_colour_jpeg(const uint8_t *jpg, int64_t bytes, ui
     if (m == 0xC0 || m == 0xC1) {
       s = dec.frame(d, len, m == 0xC1);
       if (s == VH_OK && !rgb) {  // size query: the frame header is enough
-        *width = (int32_t)dec.width;
-        *height = (int32_t)dec.height;
+        *width = (int32_t)dec.out_width();
+        *height = (int32_t)dec.out_height();
         return VH_OK;
       }
       if (s == VH_OK && capacity < 3 * (int64_t)dec.width * (int64_t)dec.height) {
-        *width = (int32_t)dec.width;
-        *height = (int32_t)dec.height;
+        *width = (int32_t)dec.out_width();
+        *height = (int32_t)dec.out_height();
         return VH_ERR_CAPACITY;
       }
     } else if ((m >= 0xC2 && m <= 0xCF && m != 0xC4 && m != 0xC8) || m == 0xDC) {
@@ -555,6 +590,8 @@ extern "C" vh_status vh_decode_colour_jpeg(const uint8_t *jpg, int64_t bytes, ui
     } else if (m == 0xDD) {
       if (len != 2) return VH_ERR_INVALID_ARG;
       dec.restart = be16(d);
+    } else if (m == 0xE1 && !dec.have_frame && len >= 6 && std::memcmp(d, "Exif\0\0", 6) == 0) {
+      dec.orientation = exif_orientation(d + 6, len - 6);  // only before the frame header
     } else if (m == 0xEE && len >= 12 && std::memcmp(d, "Adobe", 5) == 0) {
       dec.adobe_rgb = d[11] == 0;  // colour transform 0: the components are R, G, B
     } else if (m == 0xDA) {
@@ -572,8 +609,31 @@ extern "C" vh_status vh_decode_colour_jpeg(const uint8_t *jpg, int64_t bytes, ui
   if (!have_end) return VH_ERR_INVALID_ARG;
   for (int c = 0; c < dec.ncomp; ++c)
     if (!dec.comp[c].scanned) return VH_ERR_INVALID_ARG;
-  *width = (int32_t)dec.width;
-  *height = (int32_t)dec.height;
-  dec.write_rgb(rgb);
+  *width = (int32_t)dec.out_width();
+  *height = (int32_t)dec.out_height();
+  if (dec.orientation == 1) {
+    dec.write_rgb(rgb);
+    return VH_OK;
+  }
+  // stored image -> displayed image: output pixel (ox, oy) takes stored
+  // pixel (sx, sy) of the W x H image, per Exif orientation
+  std::vector<uint8_t> stored((size_t)dec.width * dec.height * 3);
+  dec.write_rgb(stored.data());
+  const int64_t W = dec.width, H = dec.height, ow = dec.out_width(), oh = dec.out_height();
+  for (int64_t oy = 0; oy < oh; ++oy)
+    for (int64_t ox = 0; ox < ow; ++ox) {
+      int64_t sx = ox, sy = oy;
+      switch (dec.orientation) {
+        case 2: sx = W - 1 - ox; break;                      // mirrored left-right
+        case 3: sx = W - 1 - ox; sy = H - 1 - oy; break;     // rotated 180
+        case 4: sy = H - 1 - oy; break;                      // mirrored top-bottom
+        case 5: sx = oy; sy = ox; break;                     // transposed
+        case 6: sx = oy; sy = H - 1 - ox; break;             // rotate 90 clockwise to show
+        case 7: sx = W - 1 - oy; sy = H - 1 - ox; break;     // transversed
+        case 8: sx = W - 1 - oy; sy = ox; break;             // rotate 90 anticlockwise to show
+        default: break;
+      }
+      std::memcpy(rgb + (size_t)(oy * ow + ox) * 3, stored.data() + (size_t)(sy * W + sx) * 3, 3);
+    }
   return VH_OK;
 }
