@@ -425,8 +425,9 @@ struct Decoder {
     return VH_OK;
   }
 
-  // one output row of component c, at full resolution
-  void upsample_row(const Component &k, uint32_t y, uint8_t *out) const {
+  // one output row of component c, at full resolution (cs: scratch of the
+  // component's width)
+  void upsample_row(const Component &k, uint32_t y, uint8_t *out, int32_t *cs) const {
     const int rx = hmax / k.h, ry = vmax / k.v;
     const uint8_t *pl = k.plane.data();
     const int cw = k.w, ch = k.ht;
@@ -456,28 +457,28 @@ struct Decoder {
       w1 = 1;
     }
     if (r0 >= ch) r0 = ch - 1;
+    // the rows blended first (cs, weights summing to 4), then the columns
+    // (weights 3 and 1, or 4): the same integer sums as weighting each
+    // of the four samples by its product of weights
     const uint8_t *a = pl + (size_t)r0 * k.pw, *b = pl + (size_t)r1 * k.pw;
-    for (uint32_t x = 0; x < width; ++x) {
-      int c0, c1, u0, u1;
-      if (rx == 1) {
-        c0 = c1 = (int)x;
-        u0 = 4;
-        u1 = 0;
-      } else {
-        c0 = (int)(x >> 1);
-        c1 = (x & 1) ? (c0 + 1 < cw ? c0 + 1 : cw - 1) : (c0 > 0 ? c0 - 1 : 0);
-        u0 = 3;
-        u1 = 1;
-      }
-      if (c0 >= cw) c0 = cw - 1;
-      const int acc = w0 * (u0 * a[c0] + u1 * a[c1]) + w1 * (u0 * b[c0] + u1 * b[c1]);
-      out[x] = (uint8_t)((acc + 8) >> 4);
+    for (int i = 0; i < cw; ++i) cs[i] = w0 * a[i] + w1 * b[i];
+    if (rx == 1) {
+      for (uint32_t x = 0; x < width; ++x) out[x] = (uint8_t)((4 * cs[x] + 8) >> 4);
+      return;
+    }
+    for (int i = 0; i < cw; ++i) {  // output columns 2i and 2i + 1
+      const int mid = 3 * cs[i];
+      const int left = cs[i > 0 ? i - 1 : 0], right = cs[i + 1 < cw ? i + 1 : cw - 1];
+      const uint32_t x = 2u * (uint32_t)i;
+      out[x] = (uint8_t)((mid + left + 8) >> 4);
+      if (x + 1 < width) out[x + 1] = (uint8_t)((mid + right + 8) >> 4);
     }
   }
 
   void write_rgb(uint8_t *rgb) const {
     std::vector<uint8_t> rows((size_t)width * 3);
     uint8_t *r[3] = {rows.data(), rows.data() + width, rows.data() + 2 * (size_t)width};
+    std::vector<int32_t> cs((size_t)width + 1);
     double cr_r[256], cb_g[256], cr_g[256], cb_b[256];
     for (int i = 0; i < 256; ++i) {
       cr_r[i] = 1.402 * (i - 128);
@@ -490,7 +491,7 @@ struct Decoder {
       return (uint8_t)(f < 0 ? 0 : (f > 255 ? 255 : f));
     };
     for (uint32_t y = 0; y < height; ++y) {
-      for (int c = 0; c < ncomp; ++c) upsample_row(comp[c], y, r[c]);
+      for (int c = 0; c < ncomp; ++c) upsample_row(comp[c], y, r[c], cs.data());
       uint8_t *out = rgb + (size_t)y * width * 3;
       if (ncomp == 1) {
         for (uint32_t x = 0; x < width; ++x) out[3 * x] = out[3 * x + 1] = out[3 * x + 2] = r[0][x];
